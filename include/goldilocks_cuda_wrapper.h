@@ -1,0 +1,168 @@
+/*
+ * goldilocks_cuda_wrapper.h -- C ABI of the GB300-native Goldilocks prover library.
+ *
+ * Part 1 is a drop-in for the extern "C" surface that goldilocks-cuda-rs binds
+ * (goldilocks-cuda-rs/src/ffi.rs, implemented by goldilocks-cuda-rs/cuda/wrapper.cu):
+ * same names, argument meaning and return codes (0 ok, -1 CUDA error; -2 invalid
+ * argument where the reference would have launched out of bounds).  Every data
+ * pointer is a caller-owned device pointer unless its name starts with h_.
+ * Field elements are raw u64 (any representative mod p is accepted); Ext2
+ * values are interleaved (c0, c1); folding tables are (point, weight) pairs;
+ * digests are 4 u64.
+ *
+ * Part 2 (gb_*) adds entry points with no reference counterpart: stream
+ * selection, whole-proof drivers that keep every round on the device, and the
+ * batched prover.  Outputs of the gb_* drivers are canonical.
+ *
+ * All launches go to the calling thread's stream: the per-thread default stream
+ * (as the reference, built with --default-stream per-thread) unless gb_set_stream
+ * selected another.  Functions documented as synchronising wait for that stream.
+ */
+#ifndef GOLDILOCKS_CUDA_WRAPPER_H
+#define GOLDILOCKS_CUDA_WRAPPER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===================== Part 1: reference ABI ===================== */
+
+/* goldilocks-cuda-rs/src/ffi.rs:11-12 (wrapper.cu:27-50).  Constants are compiled in,
+ * so both only select/validate device 0 as the reference does. */
+int goldilocks_cuda_init(void);
+int poseidon2_cuda_init(void);
+
+/* Memory / device (ffi.rs:18-26, :306-309) */
+int cuda_malloc(void **ptr, size_t size);
+int cuda_free(void *ptr);
+int cuda_memcpy_htod(void *dst, const void *src, size_t size);
+int cuda_memcpy_dtoh(void *dst, const void *src, size_t size);
+int cuda_memcpy_dtod(void *dst, const void *src, size_t size);
+int cuda_device_synchronize(void);
+int cuda_get_last_error(void);
+int cuda_peek_at_last_error(void);
+int cuda_mem_get_info(size_t *free_bytes, size_t *total_bytes);
+int cuda_set_device(int device);
+int cuda_get_device(int *device);
+int cuda_get_device_count(int *count);
+int cuda_get_device_name(int device, char *name, int max_len);
+
+/* Batch field ops (ffi.rs:32-60, :185-260) */
+int gl_batch_add(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int gl_batch_sub(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int gl_batch_mul(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int gl_batch_inverse(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext2_batch_add_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int ext2_batch_sub_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int ext2_batch_mul_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+
+/* Poseidon2 width 8 (ffi.rs:287-300; wrapper.cu:864-962).
+ * hash_batch: full permutation of n 8-element states; compress/merkle_layer: 2-to-1. */
+int poseidon2_hash_batch_ffi(const uint64_t *d_input, uint64_t *d_output, int n);
+int poseidon2_compress_batch_ffi(const uint64_t *d_left, const uint64_t *d_right, uint64_t *d_output, int n);
+int poseidon2_merkle_layer_ffi(const uint64_t *d_input, uint64_t *d_output, int n);
+
+/* eq(r, x) tables (ffi.rs:396-410; wrapper.cu:1117-1160).  Result lands in d_buf_a or
+ * d_buf_b; *d_result tells which.  Variable i <-> bit i of x. */
+int eq_dp_all_ffi(const uint64_t *d_r, uint64_t *d_buf_a, uint64_t *d_buf_b, int log_n, uint64_t **d_result);
+int ext2_eq_dp_all_ffi(const uint64_t *d_r, uint64_t *d_buf_a, uint64_t *d_buf_b, int log_n, uint64_t **d_result);
+
+/* Basefold (ffi.rs:416-545; wrapper.cu:1223-1600) */
+int basefold_bit_reverse_gl_ffi(uint64_t *d_data, int log_n);
+int basefold_bit_reverse_ext2_ffi(uint64_t *d_data, int log_n);
+/* evals -> Type2 monomial coefficients + bit-reversed copy of evals; synchronising */
+int basefold_bhc_interpolate_ffi(const uint64_t *d_evals, uint64_t *d_coeffs, uint64_t *d_bh_evals, int num_vars);
+/* repetition x 2^log_rate, num_vars +-1 butterfly layers, bit reversal; synchronising */
+int basefold_encode_ffi(const uint64_t *d_coeffs, uint64_t *d_codeword, int num_vars, int log_rate);
+int basefold_fold_gl_ffi(const uint64_t *d_codeword, const uint64_t *d_table, uint64_t challenge,
+                         uint64_t *d_output, int pair_count);
+int basefold_fold_mixed_ffi(const uint64_t *d_codeword, const uint64_t *d_table, uint64_t challenge_c0,
+                            uint64_t challenge_c1, uint64_t *d_output, int pair_count);
+int basefold_fold_ext2_ffi(const uint64_t *d_codeword, const uint64_t *d_table, uint64_t challenge_c0,
+                           uint64_t challenge_c1, uint64_t *d_output, int pair_count);
+int basefold_sumcheck_interp_gl_ffi(uint64_t *d_data, int pair_count);
+int basefold_sumcheck_interp_ext2_ffi(uint64_t *d_data, int pair_count);
+/* product kernels: per-block partials of (c0, c1, c2), num_blocks of each; the caller sums them */
+int basefold_sumcheck_product_gl_ffi(const uint64_t *d_eq, const uint64_t *d_bh, uint64_t *d_partial_c0,
+                                     uint64_t *d_partial_c1, uint64_t *d_partial_c2, int pair_count, int num_blocks);
+int basefold_sumcheck_product_mixed_ffi(const uint64_t *d_eq, const uint64_t *d_bh, uint64_t *d_partial_c0,
+                                        uint64_t *d_partial_c1, uint64_t *d_partial_c2, int pair_count,
+                                        int num_blocks);
+int basefold_sumcheck_product_ext2_ffi(const uint64_t *d_eq, const uint64_t *d_bh, uint64_t *d_partial_c0,
+                                       uint64_t *d_partial_c1, uint64_t *d_partial_c2, int pair_count,
+                                       int num_blocks);
+int basefold_sumcheck_eval_gl_ffi(const uint64_t *d_data, uint64_t challenge, uint64_t *d_output, int pair_count);
+int basefold_sumcheck_eval_mixed_ffi(const uint64_t *d_data, uint64_t challenge_c0, uint64_t challenge_c1,
+                                     uint64_t *d_output, int pair_count);
+int basefold_sumcheck_eval_ext2_ffi(const uint64_t *d_data, uint64_t challenge_c0, uint64_t challenge_c1,
+                                    uint64_t *d_output, int pair_count);
+int fused_sumcheck_round_ext2_ffi(const uint64_t *d_eq_in, const uint64_t *d_bh_in, uint64_t challenge_c0,
+                                  uint64_t challenge_c1, uint64_t *d_eq_out, uint64_t *d_bh_out,
+                                  uint64_t *d_partial_c0, uint64_t *d_partial_c1, uint64_t *d_partial_c2,
+                                  int pair_count, int num_blocks);
+int basefold_dot_product_gl_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_partial, int n, int num_blocks);
+int basefold_dot_product_mixed_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_partial, int n,
+                                   int num_blocks);
+
+/* Merkle trees (ffi.rs:549-560; wrapper.cu:1604-1714).  d_tree holds (2 num_leaves - 1) digests,
+ * layers packed leaves first, root last.  Synchronising. */
+int poseidon2_merkle_tree_gl_ffi(const uint64_t *d_codeword, uint64_t *d_tree, int num_leaves);
+int poseidon2_merkle_tree_ext2_ffi(const uint64_t *d_codeword, uint64_t *d_tree, int num_leaves);
+
+/* Product sumcheck (ffi.rs:588-630; wrapper.cu:1716-1790).  d polynomials packed with
+ * stride original_size (Ext2: 2*original_size u64).  round_message writes num_blocks*(d+1)
+ * partial sums (Ext2: x2) whose sum is the round message; synchronising. */
+int sumcheck_round_message_ffi(const uint64_t *d_polys, uint64_t *d_partial, int d, size_t original_size,
+                               size_t half, int num_blocks);
+int sumcheck_fold_ffi(const uint64_t *d_input, uint64_t *d_output, uint64_t challenge, int d,
+                      size_t original_size, size_t half);
+int sumcheck_round_message_ext2_ffi(const uint64_t *d_polys, uint64_t *d_partial, int d, size_t original_size,
+                                    size_t half, int num_blocks);
+int sumcheck_fold_ext2_ffi(const uint64_t *d_input, uint64_t *d_output, uint64_t challenge_c0,
+                           uint64_t challenge_c1, int d, size_t original_size, size_t half);
+
+/* ===================== Part 2: GB300 additions (no reference counterpart) ===================== */
+
+/* Fiat-Shamir transcript state: the fields of zk-torch-3's Transcript
+ * (zk-torch-3/src/transcript.rs:178-185) in a C layout. */
+typedef struct gb_transcript {
+    uint64_t st[8];
+    uint64_t inb[4];
+    uint64_t outb[4];
+    uint32_t nin;
+    uint32_t nout;
+} gb_transcript;
+
+/* Launch stream of the calling thread (NULL = per-thread default stream). */
+int gb_set_stream(void *stream);
+void *gb_get_stream(void);
+/* Last error message of the calling thread ("" if none). */
+const char *gb_last_error(void);
+int gb_device_sm_count(void);
+
+/* Transcript helpers (host): new(label), append_u64(label), challenge_ext2(label). */
+void gb_transcript_new(gb_transcript *t, const char *label);
+void gb_transcript_append_u64(gb_transcript *t, const char *label, uint64_t v);
+void gb_transcript_append_ext2(gb_transcript *t, const char *label, const uint64_t v[2]);
+void gb_transcript_challenge_ext2(gb_transcript *t, const char *label, uint64_t out[2]);
+
+/* Whole product-sumcheck proof, GpuLinearSumcheckProver::{new, prove} semantics
+ * (zk-torch-3/src/sumcheck/gpu_prover.rs:21-89): appends num_var/num_poly, then per round
+ * d+1 Ext2 messages and one Ext2 challenge.  polys: d x 2^n base-field values, on the
+ * device (d_polys, left unchanged) or on the host (h_polys; the other must be NULL).
+ * Outputs (host, canonical): h_msgs[n][d+1][2], h_challenges[n][2], h_finals[d][2],
+ * h_final_eval[2].  Synchronising. */
+int gb_sumcheck_prove_ext2(gb_transcript *t, int n, int d, const uint64_t *d_polys, const uint64_t *h_polys,
+                           uint64_t *h_msgs, uint64_t *h_challenges, uint64_t *h_finals, uint64_t *h_final_eval);
+/* LinearSumcheckProver::{new, prove} semantics (zk-torch-3/src/sumcheck/linear_prover.rs:23-63):
+ * base-field messages and challenges.  h_msgs[n][d+1], h_challenges[n], h_finals[d], h_final_eval[1]. */
+int gb_sumcheck_prove_base(gb_transcript *t, int n, int d, const uint64_t *d_polys, const uint64_t *h_polys,
+                           uint64_t *h_msgs, uint64_t *h_challenges, uint64_t *h_finals, uint64_t *h_final_eval);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

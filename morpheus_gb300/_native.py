@@ -1,0 +1,92 @@
+"""ctypes binding of libmorpheus_gb300.so (the C ABI in include/*.h).
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is visible,
+calls raise.  Loading the library itself needs no GPU (the symbol check in the
+CPU test-suite relies on that).
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmorpheus_gb300.so")
+_lib = None
+
+u64 = ctypes.c_uint64
+i32 = ctypes.c_int
+sz = ctypes.c_size_t
+vp = ctypes.c_void_p
+u64p = ctypes.POINTER(ctypes.c_uint64)
+u32p = ctypes.POINTER(ctypes.c_uint32)
+
+
+class GbTranscript(ctypes.Structure):
+    """gb_transcript: the fields of zk-torch-3's Transcript in C layout."""
+    _fields_ = [("st", ctypes.c_uint64 * 8), ("inb", ctypes.c_uint64 * 4), ("outb", ctypes.c_uint64 * 4),
+                ("nin", ctypes.c_uint32), ("nout", ctypes.c_uint32)]
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "goldilocks_cuda_init": (i32, []),
+    "poseidon2_cuda_init": (i32, []),
+    "cuda_malloc": (i32, [ctypes.POINTER(vp), sz]),
+    "cuda_free": (i32, [vp]),
+    "cuda_memcpy_htod": (i32, [vp, vp, sz]),
+    "cuda_memcpy_dtoh": (i32, [vp, vp, sz]),
+    "cuda_memcpy_dtod": (i32, [vp, vp, sz]),
+    "cuda_device_synchronize": (i32, []),
+    "cuda_get_last_error": (i32, []),
+    "cuda_peek_at_last_error": (i32, []),
+    "cuda_mem_get_info": (i32, [ctypes.POINTER(sz), ctypes.POINTER(sz)]),
+    "cuda_set_device": (i32, [i32]),
+    "cuda_get_device": (i32, [ctypes.POINTER(i32)]),
+    "cuda_get_device_count": (i32, [ctypes.POINTER(i32)]),
+    "cuda_get_device_name": (i32, [i32, ctypes.c_char_p, i32]),
+    "gl_batch_add": (i32, [vp, vp, vp, i32]),
+    "gl_batch_sub": (i32, [vp, vp, vp, i32]),
+    "gl_batch_mul": (i32, [vp, vp, vp, i32]),
+    "gl_batch_inverse": (i32, [vp, vp, i32]),
+    "ext2_batch_add_ffi": (i32, [vp, vp, vp, i32]),
+    "ext2_batch_sub_ffi": (i32, [vp, vp, vp, i32]),
+    "ext2_batch_mul_ffi": (i32, [vp, vp, vp, i32]),
+    "sumcheck_round_message_ffi": (i32, [vp, vp, i32, sz, sz, i32]),
+    "sumcheck_fold_ffi": (i32, [vp, vp, u64, i32, sz, sz]),
+    "sumcheck_round_message_ext2_ffi": (i32, [vp, vp, i32, sz, sz, i32]),
+    "sumcheck_fold_ext2_ffi": (i32, [vp, vp, u64, u64, i32, sz, sz]),
+    "gb_set_stream": (i32, [vp]),
+    "gb_get_stream": (vp, []),
+    "gb_last_error": (ctypes.c_char_p, []),
+    "gb_device_sm_count": (i32, []),
+    "gb_transcript_new": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p]),
+    "gb_transcript_append_u64": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64]),
+    "gb_transcript_append_ext2": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64p]),
+    "gb_transcript_challenge_ext2": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64p]),
+    "gb_sumcheck_prove_ext2": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
+    "gb_sumcheck_prove_base": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
+}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NativeError(
+                f"{LIB_PATH} is missing: build it with morpheus_gb300.build.build() "
+                "(there is no CPU fallback for the prover kernels)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc, what):
+    if rc != 0:
+        msg = lib().gb_last_error() or b""
+        raise NativeError(f"{what} failed with code {rc}: {msg.decode(errors='replace')}")

@@ -1,0 +1,156 @@
+// Host-side Goldilocks arithmetic, Poseidon2 and the Fiat-Shamir transcript
+// used by the C++ proof drivers.  Canonical values throughout.
+//
+// The transcript is the zk-torch-3 overwrite-mode duplex sponge (width 8,
+// rate 4; zk-torch-3/src/transcript.rs:174-330): absorbed values overwrite the
+// rate, squeezes pop the rate in reverse order, labels are a length prefix plus
+// one element per byte (empty labels absorb nothing).  gb_transcript carries
+// exactly the Rust Transcript's fields so a caller can hand its state across the
+// C ABI and take it back.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+
+#include "../../include/goldilocks_cuda_wrapper.h"
+#include "poseidon2.cuh"
+
+namespace gb {
+namespace host {
+
+typedef unsigned __int128 u128;
+
+inline u64 canon(u64 a) { return a >= GL_P ? a - GL_P : a; }
+inline u64 add(u64 a, u64 b) {
+    a = canon(a);
+    b = canon(b);
+    u64 s = a + b;
+    if (s < a || s >= GL_P) s -= GL_P;
+    return s;
+}
+inline u64 sub(u64 a, u64 b) {
+    a = canon(a);
+    b = canon(b);
+    return a >= b ? a - b : a + (GL_P - b);
+}
+inline u64 neg(u64 a) {
+    a = canon(a);
+    return a ? GL_P - a : 0;
+}
+inline u64 reduce(u128 x) {
+    u64 lo = (u64)x, hi = (u64)(x >> 64);
+    u64 h1 = hi >> 32, h0 = hi & GL_EPS;
+    u64 t0 = lo - h1;
+    if (lo < h1) t0 -= GL_EPS;
+    u64 t1 = (h0 << 32) - h0;
+    u64 r = t0 + t1;
+    if (r < t1) r += GL_EPS;
+    return canon(r);
+}
+inline u64 mul(u64 a, u64 b) { return reduce((u128)a * b); }
+inline u64 pow(u64 a, u64 e) {
+    u64 r = 1;
+    while (e) {
+        if (e & 1) r = mul(r, a);
+        a = mul(a, a);
+        e >>= 1;
+    }
+    return r;
+}
+inline u64 inv(u64 a) { return canon(a) ? pow(a, GL_P - 2) : 0; }
+
+struct E2 {
+    u64 c0, c1;
+};
+inline E2 e2(u64 a, u64 b) { return E2{canon(a), canon(b)}; }
+inline E2 e2add(E2 a, E2 b) { return E2{add(a.c0, b.c0), add(a.c1, b.c1)}; }
+inline E2 e2sub(E2 a, E2 b) { return E2{sub(a.c0, b.c0), sub(a.c1, b.c1)}; }
+inline E2 e2mul(E2 a, E2 b) {
+    u64 m0 = mul(a.c0, b.c0), m1 = mul(a.c1, b.c1);
+    return E2{add(m0, mul(7, m1)), add(mul(a.c0, b.c1), mul(a.c1, b.c0))};
+}
+
+inline void p2_permute(u64 s[8]) {
+    auto sbox = [](u64 x) {
+        u64 x2 = mul(x, x), x4 = mul(x2, x2), x3 = mul(x2, x);
+        return mul(x4, x3);
+    };
+    auto ext = [](u64* v) {
+        for (int h = 0; h < 8; h += 4) {
+            u64 a = v[h], b = v[h + 1], c = v[h + 2], d = v[h + 3];
+            u64 ab = add(a, b), cd = add(c, d), all = add(ab, cd);
+            u64 all_b = add(all, b), all_d = add(all, d);
+            v[h] = add(all_b, ab);
+            v[h + 1] = add(all_b, add(c, c));
+            v[h + 2] = add(all_d, cd);
+            v[h + 3] = add(all_d, add(a, a));
+        }
+        for (int i = 0; i < 4; i++) {
+            u64 col = add(v[i], v[i + 4]);
+            v[i] = add(v[i], col);
+            v[i + 4] = add(v[i + 4], col);
+        }
+    };
+    for (int i = 0; i < 8; i++) s[i] = canon(s[i]);
+    for (int r = 0; r < 4; r++) {
+        for (int i = 0; i < 8; i++) s[i] = sbox(add(s[i], P2Const::ext[r][i]));
+        ext(s);
+    }
+    for (int r = 0; r < 22; r++) {
+        s[0] = sbox(add(s[0], P2Const::inner[r]));
+        u64 sum = 0;
+        for (int i = 0; i < 8; i++) sum = add(sum, s[i]);
+        for (int i = 0; i < 8; i++) s[i] = add(mul(s[i], P2Const::diag[i]), sum);
+    }
+    for (int r = 4; r < 8; r++) {
+        for (int i = 0; i < 8; i++) s[i] = sbox(add(s[i], P2Const::ext[r][i]));
+        ext(s);
+    }
+}
+
+// ---- transcript ----
+inline void tr_duplex(gb_transcript* t) {
+    for (uint32_t i = 0; i < t->nin; i++) t->st[i] = t->inb[i];
+    for (uint32_t i = t->nin; i < 4; i++) t->st[i] = 0;
+    t->nin = 0;
+    p2_permute(t->st);
+    for (int i = 0; i < 4; i++) t->outb[3 - i] = t->st[i];
+    t->nout = 4;
+}
+inline void tr_absorb(gb_transcript* t, u64 v) {
+    t->nout = 0;
+    t->inb[t->nin++] = v;
+    if (t->nin == 4) tr_duplex(t);
+}
+inline u64 tr_squeeze(gb_transcript* t) {
+    if (t->nout == 0) tr_duplex(t);
+    return t->outb[--t->nout];
+}
+inline void tr_label(gb_transcript* t, const char* label) {
+    size_t len = std::strlen(label);
+    if (len == 0) return;
+    tr_absorb(t, (u64)len);
+    for (size_t i = 0; i < len; i++) tr_absorb(t, (u64)(unsigned char)label[i]);
+}
+inline void tr_append_u64(gb_transcript* t, const char* label, u64 v) {
+    tr_label(t, label);
+    tr_absorb(t, v);
+}
+inline void tr_append_ext2(gb_transcript* t, const char* label, E2 v) {
+    tr_label(t, label);
+    tr_absorb(t, v.c0);
+    tr_absorb(t, v.c1);
+}
+inline u64 tr_challenge(gb_transcript* t, const char* label) {
+    tr_label(t, label);
+    return tr_squeeze(t);
+}
+inline E2 tr_challenge_ext2(gb_transcript* t, const char* label) {
+    tr_label(t, label);
+    u64 a = tr_squeeze(t);
+    u64 b = tr_squeeze(t);
+    return E2{a, b};
+}
+
+}  // namespace host
+}  // namespace gb

@@ -1,0 +1,151 @@
+// Runtime plumbing of the C ABI: stream selection, error strings, the memory and
+// device entry points (goldilocks-cuda-rs/src/ffi.rs:11-26, :306-309), batch
+// field ops and host transcript helpers.
+#include <cstring>
+#include <string>
+
+#include "../../include/goldilocks_cuda_wrapper.h"
+#include "common.cuh"
+#include "host_field.hpp"
+
+namespace gb {
+
+static thread_local cudaStream_t t_stream = cudaStreamPerThread;
+static thread_local std::string t_err;
+
+cudaStream_t stream() { return t_stream; }
+
+void set_error(const char* where, cudaError_t e) {
+    t_err = std::string(where) + ": " + cudaGetErrorString(e);
+}
+void set_error_msg(const std::string& msg) { t_err = msg; }
+
+int num_sms() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 148;
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// batch field kernels
+// ---------------------------------------------------------------------------
+template <int OP>
+__global__ void gl_batch_kernel(const u64* __restrict__ a, const u64* __restrict__ b, u64* __restrict__ r, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u64 x = a[i];
+    u64 y = (OP == 3) ? 0 : b[i];
+    u64 z;
+    if (OP == 0) z = gl_add(x, y);
+    else if (OP == 1) z = gl_sub(x, y);
+    else if (OP == 2) z = gl_mul(x, y);
+    else z = gl_inv(x);
+    r[i] = z;
+}
+
+template <int OP>
+__global__ void e2_batch_kernel(const u64* __restrict__ a, const u64* __restrict__ b, u64* __restrict__ r, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    e2 x = e2_ld(a + 2 * (size_t)i), y = e2_ld(b + 2 * (size_t)i), z;
+    if (OP == 0) z = e2_add(x, y);
+    else if (OP == 1) z = e2_sub(x, y);
+    else z = e2_mul(x, y);
+    e2_st(r + 2 * (size_t)i, z);
+}
+
+template <int OP>
+static int gl_batch(const u64* a, const u64* b, u64* r, int n, const char* name) {
+    if (n < 0) return GB_EINVAL;
+    if (n == 0) return GB_OK;
+    gl_batch_kernel<OP><<<grid_for(n, 256), 256, 0, stream()>>>(a, b, r, n);
+    return check_launch(name);
+}
+template <int OP>
+static int e2_batch(const u64* a, const u64* b, u64* r, int n, const char* name) {
+    if (n < 0) return GB_EINVAL;
+    if (n == 0) return GB_OK;
+    e2_batch_kernel<OP><<<grid_for(n, 256), 256, 0, stream()>>>(a, b, r, n);
+    return check_launch(name);
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int gb_set_stream(void* s) {
+    t_stream = s ? (cudaStream_t)s : cudaStreamPerThread;
+    return 0;
+}
+void* gb_get_stream(void) { return (void*)t_stream; }
+const char* gb_last_error(void) { return t_err.c_str(); }
+int gb_device_sm_count(void) { return num_sms(); }
+
+int goldilocks_cuda_init(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return -1;
+    return cudaSetDevice(0) == cudaSuccess ? 0 : -1;
+}
+int poseidon2_cuda_init(void) { return 0; }
+
+int cuda_malloc(void** ptr, size_t size) { return cudaMalloc(ptr, size) == cudaSuccess ? 0 : -1; }
+int cuda_free(void* ptr) { return cudaFree(ptr) == cudaSuccess ? 0 : -1; }
+int cuda_memcpy_htod(void* dst, const void* src, size_t size) {
+    return cudaMemcpyAsync(dst, src, size, cudaMemcpyHostToDevice, stream()) == cudaSuccess &&
+                   cudaStreamSynchronize(stream()) == cudaSuccess
+               ? 0
+               : -1;
+}
+int cuda_memcpy_dtoh(void* dst, const void* src, size_t size) {
+    return cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToHost, stream()) == cudaSuccess &&
+                   cudaStreamSynchronize(stream()) == cudaSuccess
+               ? 0
+               : -1;
+}
+int cuda_memcpy_dtod(void* dst, const void* src, size_t size) {
+    return cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToDevice, stream()) == cudaSuccess &&
+                   cudaStreamSynchronize(stream()) == cudaSuccess
+               ? 0
+               : -1;
+}
+int cuda_device_synchronize(void) { return cudaDeviceSynchronize() == cudaSuccess ? 0 : -1; }
+int cuda_get_last_error(void) { return (int)cudaGetLastError(); }
+int cuda_peek_at_last_error(void) { return (int)cudaPeekAtLastError(); }
+int cuda_mem_get_info(size_t* f, size_t* t) { return cudaMemGetInfo(f, t) == cudaSuccess ? 0 : -1; }
+int cuda_set_device(int d) { return cudaSetDevice(d) == cudaSuccess ? 0 : -1; }
+int cuda_get_device(int* d) { return cudaGetDevice(d) == cudaSuccess ? 0 : -1; }
+int cuda_get_device_count(int* c) { return cudaGetDeviceCount(c) == cudaSuccess ? 0 : -1; }
+int cuda_get_device_name(int device, char* name, int max_len) {
+    cudaDeviceProp prop;
+    if (max_len <= 0 || cudaGetDeviceProperties(&prop, device) != cudaSuccess) return -1;
+    std::strncpy(name, prop.name, (size_t)max_len - 1);
+    name[max_len - 1] = '\0';
+    return 0;
+}
+
+int gl_batch_add(const uint64_t* a, const uint64_t* b, uint64_t* r, int n) { return gl_batch<0>(a, b, r, n, "gl_batch_add"); }
+int gl_batch_sub(const uint64_t* a, const uint64_t* b, uint64_t* r, int n) { return gl_batch<1>(a, b, r, n, "gl_batch_sub"); }
+int gl_batch_mul(const uint64_t* a, const uint64_t* b, uint64_t* r, int n) { return gl_batch<2>(a, b, r, n, "gl_batch_mul"); }
+int gl_batch_inverse(const uint64_t* a, uint64_t* r, int n) { return gl_batch<3>(a, nullptr, r, n, "gl_batch_inverse"); }
+int ext2_batch_add_ffi(const uint64_t* a, const uint64_t* b, uint64_t* r, int n) { return e2_batch<0>(a, b, r, n, "ext2_batch_add"); }
+int ext2_batch_sub_ffi(const uint64_t* a, const uint64_t* b, uint64_t* r, int n) { return e2_batch<1>(a, b, r, n, "ext2_batch_sub"); }
+int ext2_batch_mul_ffi(const uint64_t* a, const uint64_t* b, uint64_t* r, int n) { return e2_batch<2>(a, b, r, n, "ext2_batch_mul"); }
+
+void gb_transcript_new(gb_transcript* t, const char* label) {
+    std::memset(t, 0, sizeof(*t));
+    for (const char* p = label; *p; p++) host::tr_absorb(t, (u64)(unsigned char)*p);
+}
+void gb_transcript_append_u64(gb_transcript* t, const char* label, uint64_t v) { host::tr_append_u64(t, label, v); }
+void gb_transcript_append_ext2(gb_transcript* t, const char* label, const uint64_t v[2]) {
+    host::tr_append_ext2(t, label, host::E2{v[0], v[1]});
+}
+void gb_transcript_challenge_ext2(gb_transcript* t, const char* label, uint64_t out[2]) {
+    host::E2 c = host::tr_challenge_ext2(t, label);
+    out[0] = c.c0;
+    out[1] = c.c1;
+}
+
+}  // extern "C"

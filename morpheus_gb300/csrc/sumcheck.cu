@@ -1,0 +1,566 @@
+// Multilinear product sumcheck: the reference-ABI round/fold kernels and the
+// fused whole-proof driver.
+//
+// Round k of the protocol (zk-torch-3/src/sumcheck/linear_prover.rs:66-118,
+// cuda/sumcheck_prover.cuh:37-151): for c = 0..d,
+//     s_k(c) = sum_y prod_i (p_i[2y] + c (p_i[2y+1] - p_i[2y])),
+// then every p_i is folded with the round challenge r:
+//     p_i[y] <- p_i[2y] + r (p_i[2y+1] - p_i[2y]).
+//
+// Fused driver layout: round 0 reads the caller's base-field polynomials
+// directly (one 128-bit load per (poly, pair)) -- the reference lifts them to
+// Ext2 on the host first, which doubles round-0 traffic.  Each later round is a
+// single launch that folds the previous level with r_{k-1} (writing the folded
+// level, 128-bit stores) and accumulates round k's message from the folded
+// values still in registers, so the folded level is written once and never
+// re-read within the round.  The message is reduced inside the launch (last
+// block finishes), leaving d+1 canonical values for a 16*(d+1)-byte copy.
+#include <vector>
+
+#include "../../include/goldilocks_cuda_wrapper.h"
+#include "common.cuh"
+#include "host_field.hpp"
+#include "reduce.cuh"
+
+namespace gb {
+
+constexpr int SC_MAX_D = 8;
+
+__device__ __forceinline__ bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+// Pair (p[0], p[1]) of base elements; vector load when the address allows it.
+__device__ __forceinline__ void ld_pair(const u64* p, bool vec, u64& a, u64& b) {
+    if (vec) {
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(p));
+        a = v.x;
+        b = v.y;
+    } else {
+        a = __ldg(p);
+        b = __ldg(p + 1);
+    }
+}
+__device__ __forceinline__ e2 ld_e2(const u64* p, bool vec) {
+    if (vec) {
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(p));
+        return e2_make(v.x, v.y);
+    }
+    return e2_make(__ldg(p), __ldg(p + 1));
+}
+__device__ __forceinline__ void st_e2(u64* p, e2 a, bool vec) {
+    if (vec) e2_st(p, a);
+    else {
+        p[0] = a.c0;
+        p[1] = a.c1;
+    }
+}
+
+// Accumulate prod_i (e_i + c delta_i) for c = 0..D into acc (base field).
+template <int D>
+__device__ __forceinline__ void accum_base(const u64 (&e)[D], const u64 (&dl)[D], u64 (&acc)[D + 1]) {
+    u64 v[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) v[i] = e[i];
+#pragma unroll
+    for (int c = 0; c <= D; c++) {
+        u64 prod = v[0];
+#pragma unroll
+        for (int i = 1; i < D; i++) prod = gl_mul(prod, v[i]);
+        acc[c] = gl_add(acc[c], prod);
+        if (c < D) {
+#pragma unroll
+            for (int i = 0; i < D; i++) v[i] = gl_add(v[i], dl[i]);
+        }
+    }
+}
+
+// Same over Ext2; acc is laid out [c][c0, c1].
+template <int D>
+__device__ __forceinline__ void accum_e2(const e2 (&e)[D], const e2 (&dl)[D], u64 (&acc)[2 * (D + 1)]) {
+    e2 v[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) v[i] = e[i];
+#pragma unroll
+    for (int c = 0; c <= D; c++) {
+        e2 prod = v[0];
+#pragma unroll
+        for (int i = 1; i < D; i++) prod = e2_mul(prod, v[i]);
+        acc[2 * c] = gl_add(acc[2 * c], prod.c0);
+        acc[2 * c + 1] = gl_add(acc[2 * c + 1], prod.c1);
+        if (c < D) {
+#pragma unroll
+            for (int i = 0; i < D; i++) v[i] = e2_add(v[i], dl[i]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reference-ABI kernels (per-block partials, stride = original size)
+// ---------------------------------------------------------------------------
+template <int D, bool EXT>
+__global__ void __launch_bounds__(RED_THREADS) ref_round_msg_kernel(const u64* __restrict__ polys, u64* __restrict__ partial,
+                                                                    size_t stride, size_t half) {
+    constexpr int W = EXT ? 2 * (D + 1) : (D + 1);
+    u64 acc[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    const bool vec = aligned16(polys) && ((stride & 1) == 0);
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < half; y += (size_t)gridDim.x * blockDim.x) {
+        if constexpr (EXT) {
+            e2 e[D], dl[D];
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+                const u64* p = polys + (size_t)i * 2 * stride + 4 * y;
+                e[i] = ld_e2(p, vec);
+                dl[i] = e2_sub(ld_e2(p + 2, vec), e[i]);
+            }
+            accum_e2<D>(e, dl, acc);
+        } else {
+            u64 e[D], dl[D];
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+                u64 a, b;
+                ld_pair(polys + (size_t)i * stride + 2 * y, vec, a, b);
+                e[i] = a;
+                dl[i] = gl_sub(b, a);
+            }
+            accum_base<D>(e, dl, acc);
+        }
+    }
+    block_partials<W>(acc, partial);
+}
+
+template <bool EXT>
+__global__ void ref_fold_kernel(const u64* __restrict__ in, u64* __restrict__ out, u64 r0, u64 r1, int d, size_t stride,
+                                size_t half) {
+    size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (y >= half) return;
+    for (int i = 0; i < d; i++) {
+        if constexpr (EXT) {
+            const u64* p = in + (size_t)i * 2 * stride + 4 * y;
+            e2 a = e2_make(p[0], p[1]), b = e2_make(p[2], p[3]);
+            e2 f = e2_add(a, e2_mul(e2_make(r0, r1), e2_sub(b, a)));
+            u64* q = out + (size_t)i * 2 * stride + 2 * y;
+            q[0] = f.c0;
+            q[1] = f.c1;
+        } else {
+            const u64* p = in + (size_t)i * stride + 2 * y;
+            out[(size_t)i * stride + y] = gl_add(p[0], gl_mul(r0, gl_sub(p[1], p[0])));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused driver kernels
+// ---------------------------------------------------------------------------
+
+// Round 0 on base-field inputs: message only (EXT decides the output width).
+template <int D, bool EXT>
+__global__ void __launch_bounds__(RED_THREADS) sc_round0_kernel(const u64* __restrict__ polys, size_t stride, size_t half,
+                                                                u64* __restrict__ partials, u64* __restrict__ msg,
+                                                                unsigned* __restrict__ counter) {
+    constexpr int W = EXT ? 2 * (D + 1) : (D + 1);
+    u64 acc[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < half; y += (size_t)gridDim.x * blockDim.x) {
+        u64 e[D], dl[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            u64 a, b;
+            ld_pair(polys + (size_t)i * stride + 2 * y, true, a, b);
+            e[i] = a;
+            dl[i] = gl_sub(b, a);
+        }
+        if constexpr (EXT) {
+            u64 bacc[D + 1];
+#pragma unroll
+            for (int c = 0; c <= D; c++) bacc[c] = 0;
+            accum_base<D>(e, dl, bacc);
+#pragma unroll
+            for (int c = 0; c <= D; c++) acc[2 * c] = gl_add(acc[2 * c], bacc[c]);
+        } else {
+            accum_base<D>(e, dl, acc);
+        }
+    }
+    grid_reduce_finish<W>(acc, partials, msg, counter);
+}
+
+// Round k >= 1, Ext2 challenge: fold level k-1 (base if BASE_IN) with r, store the folded
+// level, accumulate round k's message.  quarter = number of output pairs.
+template <int D, bool BASE_IN>
+__global__ void __launch_bounds__(RED_THREADS) sc_fold_round_e2_kernel(const u64* __restrict__ in, size_t in_stride,
+                                                                       u64* __restrict__ out, size_t out_stride,
+                                                                       size_t quarter, u64 r0, u64 r1,
+                                                                       u64* __restrict__ partials, u64* __restrict__ msg,
+                                                                       unsigned* __restrict__ counter) {
+    constexpr int W = 2 * (D + 1);
+    u64 acc[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    const e2 r = e2_make(r0, r1);
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < quarter; y += (size_t)gridDim.x * blockDim.x) {
+        e2 e[D], dl[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            e2 a, b;
+            if constexpr (BASE_IN) {
+                const u64* p = in + (size_t)i * in_stride + 4 * y;
+                u64 x0, x1, x2, x3;
+                ld_pair(p, true, x0, x1);
+                ld_pair(p + 2, true, x2, x3);
+                u64 d0 = gl_sub(x1, x0), d1 = gl_sub(x3, x2);
+                a = e2_make(gl_add(x0, gl_mul(r0, d0)), gl_mul(r1, d0));
+                b = e2_make(gl_add(x2, gl_mul(r0, d1)), gl_mul(r1, d1));
+            } else {
+                const u64* p = in + (size_t)i * 2 * in_stride + 8 * y;
+                e2 x0 = ld_e2(p, true), x1 = ld_e2(p + 2, true), x2 = ld_e2(p + 4, true), x3 = ld_e2(p + 6, true);
+                a = e2_add(x0, e2_mul(r, e2_sub(x1, x0)));
+                b = e2_add(x2, e2_mul(r, e2_sub(x3, x2)));
+            }
+            u64* q = out + (size_t)i * 2 * out_stride + 4 * y;
+            e2_st(q, a);
+            e2_st(q + 2, b);
+            e[i] = a;
+            dl[i] = e2_sub(b, a);
+        }
+        accum_e2<D>(e, dl, acc);
+    }
+    grid_reduce_finish<W>(acc, partials, msg, counter);
+}
+
+// Round k >= 1, base-field challenge (LinearSumcheckProver).
+template <int D>
+__global__ void __launch_bounds__(RED_THREADS) sc_fold_round_base_kernel(const u64* __restrict__ in, size_t in_stride,
+                                                                         u64* __restrict__ out, size_t out_stride,
+                                                                         size_t quarter, u64 r,
+                                                                         u64* __restrict__ partials, u64* __restrict__ msg,
+                                                                         unsigned* __restrict__ counter) {
+    constexpr int W = D + 1;
+    u64 acc[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < quarter; y += (size_t)gridDim.x * blockDim.x) {
+        u64 e[D], dl[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            const u64* p = in + (size_t)i * in_stride + 4 * y;
+            u64 x0, x1, x2, x3;
+            ld_pair(p, true, x0, x1);
+            ld_pair(p + 2, true, x2, x3);
+            u64 a = gl_add(x0, gl_mul(r, gl_sub(x1, x0)));
+            u64 b = gl_add(x2, gl_mul(r, gl_sub(x3, x2)));
+            ulonglong2 v;
+            v.x = a;
+            v.y = b;
+            *reinterpret_cast<ulonglong2*>(out + (size_t)i * out_stride + 2 * y) = v;
+            e[i] = a;
+            dl[i] = gl_sub(b, a);
+        }
+        accum_base<D>(e, dl, acc);
+    }
+    grid_reduce_finish<W>(acc, partials, msg, counter);
+}
+
+// Final fold of the last pair of every polynomial; canonical outputs.
+// EXT_CH: Ext2 challenge; BASE_IN: the pair is base-field (n == 1).
+template <bool EXT_CH, bool BASE_IN>
+__global__ void sc_final_kernel(const u64* __restrict__ in, size_t in_stride, int d, u64 r0, u64 r1,
+                                u64* __restrict__ finals) {
+    int i = threadIdx.x;
+    if (i >= d) return;
+    if constexpr (!EXT_CH) {
+        const u64* p = in + (size_t)i * in_stride;
+        finals[i] = gl_canon(gl_add(p[0], gl_mul(r0, gl_sub(p[1], p[0]))));
+    } else if constexpr (BASE_IN) {
+        const u64* p = in + (size_t)i * in_stride;
+        u64 dd = gl_sub(p[1], p[0]);
+        finals[2 * i] = gl_canon(gl_add(p[0], gl_mul(r0, dd)));
+        finals[2 * i + 1] = gl_canon(gl_mul(r1, dd));
+    } else {
+        const u64* p = in + (size_t)i * 2 * in_stride;
+        e2 a = e2_make(p[0], p[1]), b = e2_make(p[2], p[3]);
+        e2 f = e2_canon(e2_add(a, e2_mul(e2_make(r0, r1), e2_sub(b, a))));
+        finals[2 * i] = f.c0;
+        finals[2 * i + 1] = f.c1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// dispatch helpers
+// ---------------------------------------------------------------------------
+template <template <int> class F, typename... A>
+static int dispatch_d(int d, A... args) {
+    switch (d) {
+        case 1: return F<1>::run(args...);
+        case 2: return F<2>::run(args...);
+        case 3: return F<3>::run(args...);
+        case 4: return F<4>::run(args...);
+        case 5: return F<5>::run(args...);
+        case 6: return F<6>::run(args...);
+        case 7: return F<7>::run(args...);
+        case 8: return F<8>::run(args...);
+        default: return GB_EINVAL;
+    }
+}
+
+template <bool EXT>
+struct RefRound {
+    template <int D>
+    struct K {
+        static int run(const u64* polys, u64* partial, size_t stride, size_t half, int blocks) {
+            ref_round_msg_kernel<D, EXT><<<blocks, RED_THREADS, 0, stream()>>>(polys, partial, stride, half);
+            return check_launch("sumcheck_round_message");
+        }
+    };
+};
+
+template <int D>
+struct Round0E2 {
+    static int run(const u64* polys, size_t stride, size_t half, unsigned grid, u64* part, u64* msg, unsigned* ctr) {
+        sc_round0_kernel<D, true><<<grid, RED_THREADS, 0, stream()>>>(polys, stride, half, part, msg, ctr);
+        return check_launch("sc_round0");
+    }
+};
+template <int D>
+struct Round0Base {
+    static int run(const u64* polys, size_t stride, size_t half, unsigned grid, u64* part, u64* msg, unsigned* ctr) {
+        sc_round0_kernel<D, false><<<grid, RED_THREADS, 0, stream()>>>(polys, stride, half, part, msg, ctr);
+        return check_launch("sc_round0");
+    }
+};
+template <int D>
+struct FoldRoundE2 {
+    static int run(bool base_in, const u64* in, size_t in_stride, u64* out, size_t out_stride, size_t quarter,
+                   unsigned grid, u64 r0, u64 r1, u64* part, u64* msg, unsigned* ctr) {
+        if (base_in)
+            sc_fold_round_e2_kernel<D, true><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
+                                                                                 r0, r1, part, msg, ctr);
+        else
+            sc_fold_round_e2_kernel<D, false><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
+                                                                                  r0, r1, part, msg, ctr);
+        return check_launch("sc_fold_round_e2");
+    }
+};
+template <int D>
+struct FoldRoundBase {
+    static int run(const u64* in, size_t in_stride, u64* out, size_t out_stride, size_t quarter, unsigned grid, u64 r,
+                   u64* part, u64* msg, unsigned* ctr) {
+        sc_fold_round_base_kernel<D><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter, r, part,
+                                                                         msg, ctr);
+        return check_launch("sc_fold_round_base");
+    }
+};
+
+// Grid size for a round over `work` items: enough blocks to fill the GPU, at most one
+// item per thread when work is small.
+static unsigned round_grid(size_t work) {
+    size_t cap = (size_t)num_sms() * 4;
+    size_t need = (work + RED_THREADS - 1) / RED_THREADS;
+    if (need < 1) need = 1;
+    return (unsigned)(need < cap ? need : cap);
+}
+
+// Pinned host staging reused by the calling thread.
+static u64* pinned_staging(size_t words) {
+    static thread_local u64* buf = nullptr;
+    static thread_local size_t cap = 0;
+    if (words > cap) {
+        if (buf) cudaFreeHost(buf);
+        size_t c = words < 4096 ? 4096 : words;
+        if (cudaMallocHost(&buf, c * 8) != cudaSuccess) {
+            buf = nullptr;
+            cap = 0;
+            return nullptr;
+        }
+        cap = c;
+    }
+    return buf;
+}
+
+// Device workspace of one proof.
+struct ScWork {
+    u64* base = nullptr;  // caller-independent aligned copy of the inputs (when needed)
+    u64* a = nullptr;     // ping
+    u64* b = nullptr;     // pong
+    u64* partials = nullptr;
+    u64* out = nullptr;   // message / finals staging (device)
+    unsigned* counter = nullptr;
+    ~ScWork() {
+        cudaStream_t s = stream();
+        if (base) cudaFreeAsync(base, s);
+        if (a) cudaFreeAsync(a, s);
+        if (b) cudaFreeAsync(b, s);
+        if (partials) cudaFreeAsync(partials, s);
+        if (out) cudaFreeAsync(out, s);
+        if (counter) cudaFreeAsync(counter, s);
+    }
+};
+
+static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* h_polys, bool ext, u64* h_msgs,
+                 u64* h_ch, u64* h_finals, u64* h_final_eval) {
+    using namespace host;
+    if (!t || n < 0 || n > 40 || d < 1 || d > SC_MAX_D || (!d_polys == !h_polys) || !h_msgs || !h_ch || !h_finals ||
+        !h_final_eval) {
+        set_error_msg("gb_sumcheck_prove: invalid argument");
+        return GB_EINVAL;
+    }
+    cudaStream_t s = stream();
+    const size_t N = (size_t)1 << n;
+    const int W = ext ? 2 : 1;  // words per value in messages / challenges
+    tr_append_u64(t, "num_var", (u64)n);
+    tr_append_u64(t, "num_poly", (u64)d);
+
+    ScWork w;
+    const u64* polys = d_polys;
+    if (h_polys || (((uintptr_t)d_polys) & 15)) {
+        GB_CUDA_TRY(cudaMallocAsync(&w.base, N * d * 8, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(w.base, h_polys ? (const void*)h_polys : (const void*)d_polys, N * d * 8,
+                                    h_polys ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+        polys = w.base;
+    }
+    u64* stage = pinned_staging(2 * (SC_MAX_D + 1) + 2 * SC_MAX_D);
+    if (!stage) {
+        set_error_msg("gb_sumcheck_prove: pinned staging allocation failed");
+        return GB_ECUDA;
+    }
+    const unsigned max_grid = round_grid(N / 2 > 0 ? N / 2 : 1);
+    GB_CUDA_TRY(cudaMallocAsync(&w.partials, (size_t)max_grid * 2 * (SC_MAX_D + 1) * 8, s));
+    GB_CUDA_TRY(cudaMallocAsync(&w.out, 2 * (SC_MAX_D + 1) * 8, s));
+    GB_CUDA_TRY(cudaMallocAsync(&w.counter, sizeof(unsigned), s));
+    GB_CUDA_TRY(cudaMemsetAsync(w.counter, 0, sizeof(unsigned), s));
+    const size_t lvl_stride = N / 2 > 0 ? N / 2 : 1;  // elements per poly in the ping/pong buffers
+    if (n >= 2) {
+        size_t words = lvl_stride * d * (ext ? 2 : 1);
+        GB_CUDA_TRY(cudaMallocAsync(&w.a, words * 8, s));
+        GB_CUDA_TRY(cudaMallocAsync(&w.b, words * 8, s));
+    }
+
+    std::vector<u64> finals(2 * d, 0);
+    if (n == 0) {
+        // no rounds: the single evaluation of every polynomial is its final value
+        for (int i = 0; i < d; i++) GB_CUDA_TRY(cudaMemcpyAsync(stage + i, polys + i, 8, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int i = 0; i < d; i++) finals[W * i] = canon(stage[i]);
+    } else {
+        u64 r0 = 0, r1 = 0;
+        const u64* cur = polys;
+        size_t cur_stride = N;
+        bool base_in = true;
+        u64* bufs[2] = {w.a, w.b};
+        int pp = 0;
+        for (int k = 0; k < n; k++) {
+            const size_t level = N >> k;  // elements of the level this round's message is taken over
+            int rc;
+            if (k == 0) {
+                unsigned g = round_grid(level / 2);
+                rc = ext ? dispatch_d<Round0E2>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter)
+                         : dispatch_d<Round0Base>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter);
+            } else {
+                u64* dst = bufs[pp];
+                size_t quarter = level / 2;  // output pairs
+                unsigned g = round_grid(quarter);
+                rc = ext ? dispatch_d<FoldRoundE2>(d, base_in, cur, cur_stride, dst, lvl_stride, quarter, g, r0, r1,
+                                                   w.partials, w.out, w.counter)
+                         : dispatch_d<FoldRoundBase>(d, cur, cur_stride, dst, lvl_stride, quarter, g, r0, w.partials, w.out,
+                                                     w.counter);
+                cur = dst;
+                cur_stride = lvl_stride;
+                base_in = false;
+                pp ^= 1;
+            }
+            if (rc) return rc;
+            const int words = W * (d + 1);
+            GB_CUDA_TRY(cudaMemcpyAsync(stage, w.out, words * 8, cudaMemcpyDeviceToHost, s));
+            GB_CUDA_TRY(cudaStreamSynchronize(s));
+            u64* m = h_msgs + (size_t)k * words;
+            for (int i = 0; i < words; i++) m[i] = stage[i];
+            if (ext) {
+                for (int c = 0; c <= d; c++) tr_append_ext2(t, "round_message", E2{m[2 * c], m[2 * c + 1]});
+                E2 ch = tr_challenge_ext2(t, "challenge");
+                r0 = ch.c0;
+                r1 = ch.c1;
+                h_ch[2 * k] = r0;
+                h_ch[2 * k + 1] = r1;
+            } else {
+                for (int c = 0; c <= d; c++) tr_append_u64(t, "round_message", m[c]);
+                r0 = tr_challenge(t, "challenge");
+                h_ch[k] = r0;
+            }
+        }
+        if (ext) {
+            if (base_in)
+                sc_final_kernel<true, true><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, w.out);
+            else
+                sc_final_kernel<true, false><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, w.out);
+        } else {
+            sc_final_kernel<false, true><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, w.out);
+        }
+        GB_LAUNCH_CHECK("sc_final");
+        GB_CUDA_TRY(cudaMemcpyAsync(stage, w.out, (size_t)W * d * 8, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int i = 0; i < W * d; i++) finals[i] = stage[i];
+    }
+    for (int i = 0; i < W * d; i++) h_finals[i] = finals[i];
+    if (ext) {
+        E2 fe{1, 0};
+        for (int i = 0; i < d; i++) fe = e2mul(fe, E2{finals[2 * i], finals[2 * i + 1]});
+        h_final_eval[0] = fe.c0;
+        h_final_eval[1] = fe.c1;
+    } else {
+        u64 fe = 1;
+        for (int i = 0; i < d; i++) fe = mul(fe, finals[i]);
+        h_final_eval[0] = fe;
+    }
+    return GB_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int sumcheck_round_message_ffi(const uint64_t* d_polys, uint64_t* d_partial, int d, size_t original_size, size_t half,
+                               int num_blocks) {
+    if (num_blocks <= 0 || d < 1 || d > SC_MAX_D) return GB_EINVAL;
+    int rc = dispatch_d<RefRound<false>::K>(d, d_polys, d_partial, original_size, half, num_blocks);
+    return rc ? rc : sync_stream("sumcheck_round_message_ffi");
+}
+
+int sumcheck_round_message_ext2_ffi(const uint64_t* d_polys, uint64_t* d_partial, int d, size_t original_size,
+                                    size_t half, int num_blocks) {
+    if (num_blocks <= 0 || d < 1 || d > SC_MAX_D) return GB_EINVAL;
+    int rc = dispatch_d<RefRound<true>::K>(d, d_polys, d_partial, original_size, half, num_blocks);
+    return rc ? rc : sync_stream("sumcheck_round_message_ext2_ffi");
+}
+
+int sumcheck_fold_ffi(const uint64_t* d_input, uint64_t* d_output, uint64_t challenge, int d, size_t original_size,
+                      size_t half) {
+    if (d < 1) return GB_EINVAL;
+    if (half == 0) return GB_OK;
+    ref_fold_kernel<false><<<grid_for(half, 256), 256, 0, stream()>>>(d_input, d_output, challenge, 0, d, original_size,
+                                                                       half);
+    GB_LAUNCH_CHECK("sumcheck_fold_ffi");
+    return sync_stream("sumcheck_fold_ffi");
+}
+
+int sumcheck_fold_ext2_ffi(const uint64_t* d_input, uint64_t* d_output, uint64_t c0, uint64_t c1, int d,
+                           size_t original_size, size_t half) {
+    if (d < 1) return GB_EINVAL;
+    if (half == 0) return GB_OK;
+    ref_fold_kernel<true><<<grid_for(half, 256), 256, 0, stream()>>>(d_input, d_output, c0, c1, d, original_size, half);
+    GB_LAUNCH_CHECK("sumcheck_fold_ext2_ffi");
+    return sync_stream("sumcheck_fold_ext2_ffi");
+}
+
+int gb_sumcheck_prove_ext2(gb_transcript* t, int n, int d, const uint64_t* d_polys, const uint64_t* h_polys,
+                           uint64_t* h_msgs, uint64_t* h_challenges, uint64_t* h_finals, uint64_t* h_final_eval) {
+    return prove(t, n, d, d_polys, h_polys, true, h_msgs, h_challenges, h_finals, h_final_eval);
+}
+
+int gb_sumcheck_prove_base(gb_transcript* t, int n, int d, const uint64_t* d_polys, const uint64_t* h_polys,
+                           uint64_t* h_msgs, uint64_t* h_challenges, uint64_t* h_finals, uint64_t* h_final_eval) {
+    return prove(t, n, d, d_polys, h_polys, false, h_msgs, h_challenges, h_finals, h_final_eval);
+}
+
+}  // extern "C"

@@ -1,0 +1,289 @@
+"""CPU oracle for the prover field hot path -- TEST INFRASTRUCTURE ONLY.
+
+This package is the checker: a plain-C restatement (oracle.c) of the reference's
+CPU code, plus an optional host build of the reference's own Ajtai CPU reference
+(_ref/).  Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+bench.py may import it.  The product package ``morpheus_gb300`` never does.
+
+Parity pinning: the restatement is checked against the reference's golden
+vectors (tests/golden/) and against the reference's own Ajtai code built from
+its sources (oracle/_ref).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+P = 0xFFFFFFFF00000001
+Q_AGL = 0xFFFFFFFEFFFFFFE1
+
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_c = ctypes
+
+
+def build(ref=None):
+    """Compile liboracle.so (and _ref/ when the reference tree is present)."""
+    subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    if ref is None:
+        ref = os.path.isdir("/root/reference/cuda_almost_goldilocks")
+    if ref:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build(ref=False)
+        L = ctypes.CDLL(path)
+        u64, i32, sz = _c.c_uint64, _c.c_int, _c.c_size_t
+        vp = _c.c_void_p
+        for name, res, args in [
+            ("or_gl_add", u64, [u64, u64]),
+            ("or_gl_sub", u64, [u64, u64]),
+            ("or_gl_mul", u64, [u64, u64]),
+            ("or_gl_inv", u64, [u64]),
+            ("or_ext2_mul", None, [_u64p, _u64p, _u64p]),
+            ("or_ext2_inv", None, [_u64p, _u64p]),
+            ("or_poseidon2_permute", None, [_u64p]),
+            ("or_poseidon2_compress", None, [_u64p, _u64p, _u64p]),
+            ("or_transcript_size", sz, []),
+            ("or_tr_new", None, [vp, _c.c_char_p, sz]),
+            ("or_tr_append_u64", None, [vp, _c.c_char_p, sz, u64]),
+            ("or_tr_append_scalar", None, [vp, _c.c_char_p, sz, u64]),
+            ("or_tr_append_ext2", None, [vp, _c.c_char_p, sz, _u64p]),
+            ("or_tr_challenge_scalar", u64, [vp, _c.c_char_p, sz]),
+            ("or_tr_challenge_ext2", None, [vp, _c.c_char_p, sz, _u64p]),
+            ("or_sumcheck_prove_ext2", i32, [vp, i32, i32, _u64p, _u64p, _u64p, _u64p, _u64p]),
+            ("or_sumcheck_prove_base", i32, [vp, i32, i32, _u64p, _u64p, _u64p, _u64p, _u64p]),
+            ("or_sumcheck_verify_ext2", i32, [vp, i32, i32, _u64p, _u64p, _u64p]),
+            ("or_eq_table_base", None, [_u64p, i32, _u64p]),
+            ("or_eq_table_ext2", None, [_u64p, i32, _u64p]),
+            ("or_basefold_table_entries", sz, [i32, i32, i32]),
+            ("or_basefold_table_generate", None, [i32, i32, i32, u64, _u64p, _u64p]),
+            ("or_bhc_interpolate", None, [_u64p, i32, _u64p, _u64p]),
+            ("or_basefold_encode", None, [_u64p, i32, i32, _u64p]),
+            ("or_merkle_tree_gl", None, [_u64p, sz, _u64p]),
+            ("or_merkle_tree_ext2", None, [_u64p, sz, _u64p]),
+            ("or_basefold_commit", None, [_u64p, i32, i32, _u64p, _u64p, _u64p, _u64p]),
+            ("or_basefold_proof_len", sz, [i32, i32, i32]),
+            ("or_basefold_open_ext2", i32, [_u64p, _u64p, _u64p, _u64p, i32, i32, _u64p, _u64p, _u64p,
+                                            vp, i32, _u64p]),
+            ("or_basefold_verify_ext2", i32, [_u64p, i32, i32, _u64p, _u64p, i32, _u64p, _u64p, vp]),
+            ("or_agl_add", u64, [u64, u64]),
+            ("or_agl_sub", u64, [u64, u64]),
+            ("or_agl_mul", u64, [u64, u64]),
+            ("or_aext2_mul", None, [_u64p, _u64p, _u64p]),
+            ("or_chacha8_block", None, [_u32p, _c.c_uint32, _u32p, _u32p]),
+            ("or_ajtai_ring_elem", None, [_u32p, _c.c_uint32, u64, _u64p]),
+            ("or_ajtai_commit_wide", None, [_u32p, _u64p, u64, u64, i32, i32, _u64p]),
+            ("or_ajtai_commit_u8_batch", None, [_u32p, _u8p, u64, i32, i32, i32, _u64p]),
+        ]:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def ref_lib():
+    """The reference's own Ajtai CPU code (host build), or None when not built."""
+    global _REF
+    if _REF is None:
+        path = os.path.join(_HERE, "_ref", "libajtai_ref.so")
+        if not os.path.exists(path):
+            return None
+        R = ctypes.CDLL(path)
+        R.ref_chacha8_block.argtypes = [_u32p, _c.c_uint32, _u32p, _u32p]
+        R.ref_ring_elem.argtypes = [_u32p, _c.c_int, _c.c_uint64, _u64p]
+        R.ref_commit_wide.argtypes = [_u32p, _u64p, _c.c_uint64, _c.c_uint64, _c.c_int, _c.c_int, _u64p]
+        R.ref_commit_binary.argtypes = [_u32p, _u64p, _c.c_uint64, _u64p]
+        _REF = R
+    return _REF
+
+
+def _a(x, dt=np.uint64):
+    return np.ascontiguousarray(np.asarray(x, dtype=dt))
+
+
+class Transcript:
+    """zk-torch-3 Transcript (transcript.rs:174-350)."""
+
+    def __init__(self, label=b""):
+        self.buf = ctypes.create_string_buffer(lib().or_transcript_size())
+        lib().or_tr_new(self.buf, label, len(label))
+
+    @property
+    def ptr(self):
+        return ctypes.cast(self.buf, ctypes.c_void_p)
+
+    def append_u64(self, label, v):
+        lib().or_tr_append_u64(self.ptr, label, len(label), int(v))
+
+    def append_scalar(self, label, v):
+        lib().or_tr_append_scalar(self.ptr, label, len(label), int(v))
+
+    def append_ext2(self, label, v):
+        lib().or_tr_append_ext2(self.ptr, label, len(label), _a(v))
+
+    def challenge_scalar(self, label):
+        return int(lib().or_tr_challenge_scalar(self.ptr, label, len(label)))
+
+    def challenge_ext2(self, label):
+        out = np.zeros(2, np.uint64)
+        lib().or_tr_challenge_ext2(self.ptr, label, len(label), out)
+        return out
+
+    def state_bytes(self):
+        return bytes(self.buf.raw)
+
+
+def poseidon2_permute(state):
+    s = _a(state).copy()
+    lib().or_poseidon2_permute(s)
+    return s
+
+
+def sumcheck_prove_ext2(transcript, polys):
+    polys = _a(polys)
+    d, N = polys.shape
+    n = N.bit_length() - 1
+    msgs = np.zeros((n, d + 1, 2), np.uint64)
+    ch = np.zeros((n, 2), np.uint64)
+    finals = np.zeros((d, 2), np.uint64)
+    fe = np.zeros(2, np.uint64)
+    rc = lib().or_sumcheck_prove_ext2(transcript.ptr, n, d, polys.reshape(-1), msgs.reshape(-1),
+                                      ch.reshape(-1), finals.reshape(-1), fe)
+    assert rc == 0
+    return {"round_messages": msgs, "challenges": ch, "final_evals": finals, "final_eval": fe}
+
+
+def sumcheck_prove_base(transcript, polys):
+    polys = _a(polys)
+    d, N = polys.shape
+    n = N.bit_length() - 1
+    msgs = np.zeros((n, d + 1), np.uint64)
+    ch = np.zeros(n, np.uint64)
+    finals = np.zeros(d, np.uint64)
+    fe = np.zeros(1, np.uint64)
+    rc = lib().or_sumcheck_prove_base(transcript.ptr, n, d, polys.reshape(-1), msgs.reshape(-1), ch,
+                                      finals, fe)
+    assert rc == 0
+    return {"round_messages": msgs, "challenges": ch, "final_evals": finals, "final_eval": fe}
+
+
+def sumcheck_verify_ext2(transcript, n, d, claimed, msgs, final_eval):
+    return bool(lib().or_sumcheck_verify_ext2(transcript.ptr, n, d, _a(claimed), _a(msgs).reshape(-1),
+                                              _a(final_eval)))
+
+
+def eq_table_ext2(point):
+    point = _a(point).reshape(-1, 2)
+    n = point.shape[0]
+    out = np.zeros((1 << n, 2), np.uint64)
+    lib().or_eq_table_ext2(point.reshape(-1), n, out.reshape(-1))
+    return out
+
+
+def basefold_table(num_vars, log_rate, num_rounds, seed):
+    tot = lib().or_basefold_table_entries(num_vars, log_rate, num_rounds)
+    ent = np.zeros((tot, 2), np.uint64)
+    off = np.zeros(num_rounds, np.uint64)
+    lib().or_basefold_table_generate(num_vars, log_rate, num_rounds, seed, ent.reshape(-1), off)
+    return ent, off
+
+
+def bhc_interpolate(evals):
+    evals = _a(evals)
+    n = evals.size.bit_length() - 1
+    co = np.zeros_like(evals)
+    bh = np.zeros_like(evals)
+    lib().or_bhc_interpolate(evals, n, co, bh)
+    return co, bh
+
+
+def basefold_encode(coeffs, log_rate):
+    coeffs = _a(coeffs)
+    n = coeffs.size.bit_length() - 1
+    cw = np.zeros(coeffs.size << log_rate, np.uint64)
+    lib().or_basefold_encode(coeffs, n, log_rate, cw)
+    return cw
+
+
+def merkle_tree_gl(cw):
+    cw = _a(cw)
+    leaves = cw.size // 2
+    tree = np.zeros((2 * leaves - 1) * 4, np.uint64)
+    lib().or_merkle_tree_gl(cw, leaves, tree)
+    return tree
+
+
+def merkle_tree_ext2(cw):
+    cw = _a(cw).reshape(-1)
+    leaves = cw.size // 4
+    tree = np.zeros((2 * leaves - 1) * 4, np.uint64)
+    lib().or_merkle_tree_ext2(cw, leaves, tree)
+    return tree
+
+
+def basefold_commit(evals, log_rate):
+    evals = _a(evals)
+    n = evals.size.bit_length() - 1
+    cw = np.zeros(evals.size << log_rate, np.uint64)
+    bh = np.zeros_like(evals)
+    tree = np.zeros((2 * (cw.size // 2) - 1) * 4, np.uint64)
+    root = np.zeros(4, np.uint64)
+    lib().or_basefold_commit(evals, n, log_rate, cw, bh, tree, root)
+    return {"root": root, "codeword": cw, "bh_evals": bh, "tree": tree, "num_vars": n, "log_rate": log_rate}
+
+
+def basefold_proof_len(n, log_rate, q):
+    return lib().or_basefold_proof_len(n, log_rate, q)
+
+
+def basefold_open_ext2(comm, point, table, transcript, num_queries):
+    n, lr = comm["num_vars"], comm["log_rate"]
+    ent, off = table
+    proof = np.zeros(basefold_proof_len(n, lr, num_queries), np.uint64)
+    rc = lib().or_basefold_open_ext2(comm["codeword"], comm["bh_evals"], comm["tree"], comm["root"], n, lr,
+                                     _a(point).reshape(-1), ent.reshape(-1), off, transcript.ptr,
+                                     num_queries, proof)
+    assert rc == 0
+    return proof
+
+
+def basefold_verify_ext2(root, n, log_rate, point, proof, num_queries, table, transcript):
+    ent, off = table
+    return bool(lib().or_basefold_verify_ext2(_a(root), n, log_rate, _a(point).reshape(-1), _a(proof),
+                                              num_queries, ent.reshape(-1), off, transcript.ptr))
+
+
+def ajtai_ring_elem(key, row, j):
+    out = np.zeros(64, np.uint64)
+    lib().or_ajtai_ring_elem(_a(key, np.uint32), row, j, out)
+    return out
+
+
+def ajtai_commit_wide(key, z, col_offset=0, row_lo=0, nrows=42):
+    z = _a(z).reshape(-1)
+    N = z.size // 64
+    out = np.zeros((nrows, 64), np.uint64)
+    lib().or_ajtai_commit_wide(_a(key, np.uint32), z, N, col_offset, row_lo, nrows, out.reshape(-1))
+    return out
+
+
+def ajtai_commit_u8_batch(key, z8, row_lo=0, nrows=16):
+    z8 = _a(z8, np.uint8)
+    B = z8.shape[0]
+    N = z8.shape[1] // 64
+    out = np.zeros((B, nrows, 64), np.uint64)
+    lib().or_ajtai_commit_u8_batch(_a(key, np.uint32), z8.reshape(-1), N, B, row_lo, nrows, out.reshape(-1))
+    return out

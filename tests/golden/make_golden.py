@@ -1,0 +1,200 @@
+"""Generate tests/golden/reference_vectors.json from the reference tree.
+
+Run here (where the reference sources exist), never on the GPU machine:
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+Two kinds of vectors are written:
+
+* golden values stated in the reference's own tests, read from the test files
+  as text (each entry records file:line and the literal it was read from);
+* outputs of the reference's own code, built for the host from its sources by
+  oracle/Makefile into oracle/_ref/ (Poseidon2 / Goldilocks / Ext2 device code
+  and the Ajtai ChaCha8 PRG + CPU reference).
+
+The GPU tests and the CPU oracle tests both check against this file, so it
+travels with the repository while the reference tree does not.
+"""
+import argparse
+import ctypes
+import json
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+P = 0xFFFFFFFF00000001
+Q = 0xFFFFFFFEFFFFFFE1
+C_AGL = 0x10000001F
+HALF_AGL = 0x7FFFFFFF7FFFFFF1
+
+
+def find_line(path, literal):
+    with open(path) as f:
+        for i, line in enumerate(f, 1):
+            if literal in line:
+                return i
+    raise SystemExit(f"literal {literal!r} not found in {path}")
+
+
+def text_vectors(ref):
+    out = {}
+    # Poseidon2 width-8 KAT printed by the reference's standalone test.
+    f = os.path.join(ref, "cuda/poseidon2_kernels.cu")
+    src = open(f).read()
+    m = re.search(r"uint64_t expected\[8\] = \{([^}]*)\}", src)
+    vals = [int(x.strip().rstrip("ULL")) for x in m.group(1).replace("\n", " ").split(",") if x.strip()]
+    out["poseidon2_plonky3_kat"] = {
+        "source": f"cuda/poseidon2_kernels.cu:{find_line(f, 'uint64_t expected[8]')}",
+        "input": list(range(8)),
+        "expected": vals,
+        "note": "The reference's permutation (same constants in cuda/poseidon2.cuh, "
+                "goldilocks-cuda-rs/src/cpu_poseidon2.rs, zk-torch-3/src/transcript.rs) does not "
+                "produce this vector; the reference's own code output is in poseidon2_ref.",
+    }
+    # almost-Goldilocks golden add/mul cases (hand-computed in the test).
+    f = os.path.join(ref, "cuda_almost_goldilocks/almost_field_test.cu")
+    sym = {"AGL_PRIME": Q, "ALMOST_REDUCE_C": C_AGL, "ALMOST_HALF_P_PLUS_ONE": HALF_AGL}
+
+    def ev(expr):
+        e = expr.strip().replace("ULL", "")
+        for k, v in sym.items():
+            e = e.replace(k, str(v))
+        e = e.replace("0xFFFFFFFFFFFFFFFF", str(2**64 - 1))
+        return int(eval(e, {"__builtins__": {}}))  # arithmetic on literals only
+
+    src = open(f).read()
+    adds = re.search(r"AddCase add_cases\[\] = \{(.*?)\};", src, re.S).group(1)
+    muls = re.search(r"MulCase mul_cases\[\] = \{(.*?)\};", src, re.S).group(1)
+
+    def cases(block):
+        res = []
+        for line in block.splitlines():
+            line = line.split("//")[0]
+            mm = re.search(r"\{([^{}]*)\}", line)
+            if mm:
+                res.append([ev(x) for x in mm.group(1).split(",")])
+        return res
+
+    out["agl_add_golden"] = {"source": f"cuda_almost_goldilocks/almost_field_test.cu:{find_line(f, 'AddCase add_cases')}",
+                             "cases": cases(adds)}
+    out["agl_mul_golden"] = {"source": f"cuda_almost_goldilocks/almost_field_test.cu:{find_line(f, 'MulCase mul_cases')}",
+                             "cases": cases(muls)}
+    f = os.path.join(ref, "cuda_almost_goldilocks/almost_extension_test.cu")
+    ln = find_line(f, "(1 + 2X)(3 + 4X)")
+    assert "27 + 10X" in open(f).read()
+    out["aext2_mul_golden"] = {"source": f"cuda_almost_goldilocks/almost_extension_test.cu:{ln}",
+                               "cases": [[[1, 2], [3, 4], [27, 10]], [[2, 3], [2, 3], [31, 12]]]}
+    f = os.path.join(ref, "zk-torch-3/src/sumcheck/linear_prover.rs")
+    ln = find_line(f, "1*5 + 2*6 + 3*7 + 4*8 = 5 + 12 + 21 + 32 = 70")
+    out["sumcheck_h70"] = {"source": f"zk-torch-3/src/sumcheck/linear_prover.rs:{ln}",
+                           "p1": [1, 2, 3, 4], "p2": [5, 6, 7, 8], "sum": 70,
+                           "labels": {"base": "test", "ext2": "test_cpu_ext2"}}
+    f = os.path.join(ref, "zk-torch-3/src/commit/basefold.rs")
+    ln = find_line(f, "num_queries: 34")
+    out["basefold_key_default"] = {"source": f"zk-torch-3/src/commit/basefold.rs:{ln}",
+                                   "log_rate": 3, "num_queries": 34, "seed": 42}
+    return out
+
+
+def ref_vectors():
+    u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+    u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+    G = ctypes.CDLL(os.path.join(REPO, "oracle/_ref/libgl_ref.so"))
+    A = ctypes.CDLL(os.path.join(REPO, "oracle/_ref/libajtai_ref.so"))
+    G.ref_poseidon2_init()
+    G.ref_poseidon2_permute.argtypes = [u64p]
+    for nm in ("ref_gl_mul", "ref_gl_add", "ref_gl_sub"):
+        getattr(G, nm).restype = ctypes.c_uint64
+        getattr(G, nm).argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+    G.ref_ext2_mul.argtypes = [u64p, u64p, u64p]
+    A.ref_chacha8_block.argtypes = [u32p, ctypes.c_uint32, u32p, u32p]
+    A.ref_ring_elem.argtypes = [u32p, ctypes.c_int, ctypes.c_uint64, u64p]
+    A.ref_commit_wide.argtypes = [u32p, u64p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, u64p]
+    A.ref_commit_binary.argtypes = [u32p, u64p, ctypes.c_uint64, u64p]
+
+    rng = np.random.default_rng(20261203)
+    out = {}
+    ins = [np.arange(8, dtype=np.uint64), np.zeros(8, np.uint64),
+           np.full(8, P - 1, np.uint64), np.full(8, 2**64 - 1, np.uint64)]
+    ins += [rng.integers(0, 2**64, size=8, dtype=np.uint64, endpoint=False) for _ in range(12)]
+    p2 = []
+    for s in ins:
+        o = s.copy()
+        G.ref_poseidon2_permute(o)
+        p2.append([[int(x) for x in s], [int(x) for x in o]])
+    out["poseidon2_ref"] = {"source": "cuda/poseidon2.cuh:322-362 built for the host (oracle/_ref/libgl_ref.so)",
+                            "cases": p2}
+    edge = [0, 1, 2, P - 1, P, P + 1, 2**64 - 1, 2**32, 2**32 - 1, 2**63]
+    pairs = [(a, b) for a in edge for b in edge]
+    pairs += [tuple(int(x) for x in rng.integers(0, 2**64, size=2, dtype=np.uint64)) for _ in range(64)]
+    out["gl_ops_ref"] = {"source": "cuda/goldilocks.cuh:182-311 built for the host; outputs canonicalised",
+                         "cases": [[a, b, int(G.ref_gl_add(a, b)), int(G.ref_gl_sub(a, b)), int(G.ref_gl_mul(a, b))]
+                                   for a, b in pairs]}
+    e2 = []
+    for _ in range(32):
+        a = rng.integers(0, P, size=2, dtype=np.uint64)
+        b = rng.integers(0, P, size=2, dtype=np.uint64)
+        o = np.zeros(2, np.uint64)
+        G.ref_ext2_mul(a, b, o)
+        e2.append([[int(x) for x in a], [int(x) for x in b], [int(x) for x in o]])
+    out["ext2_mul_ref"] = {"source": "cuda/extension.cuh:113-125 built for the host", "cases": e2}
+
+    cc = []
+    for key, ctr, nonce in [([1, 2, 3, 4, 5, 6, 7, 8], 0, [42, 1000, 1]), ([1, 2, 3, 4, 5, 6, 7, 8], 1, [42, 1000, 1]),
+                            ([0] * 8, 0, [0, 0, 0]), ([0xFFFFFFFF] * 8, 7, [3, 5, 7])]:
+        o = np.zeros(16, np.uint32)
+        A.ref_chacha8_block(np.array(key, np.uint32), ctr, np.array(nonce, np.uint32), o)
+        cc.append([key, ctr, nonce, [int(x) for x in o]])
+    out["chacha8_ref"] = {"source": "cuda_almost_goldilocks/ajtai_chacha8.cuh:60-98", "cases": cc}
+    key = np.array([9, 8, 7, 6, 5, 4, 3, 2], np.uint32)
+    ring = []
+    for row, j in [(0, 0), (3, 77), (41, 1023), (15, 2**33 + 5)]:
+        o = np.zeros(64, np.uint64)
+        A.ref_ring_elem(key, row, j, o)
+        ring.append([row, j, [int(x) for x in o]])
+    out["ajtai_ring_elem_ref"] = {"source": "cuda_almost_goldilocks/ajtai_cpu_reference.cuh:124-148",
+                                  "key": [int(x) for x in key], "cases": ring}
+    N = 4
+    z = rng.integers(0, Q, size=N * 64, dtype=np.uint64)
+    o = np.zeros(42 * 64, np.uint64)
+    A.ref_commit_wide(key, z, N, 3, 0, 42, o)
+    out["ajtai_commit_wide_ref"] = {"source": "cpu_prg_ring_elem<64> + cpu_ring_mul<64> (ajtai_cpu_reference.cuh:78-148)",
+                                    "key": [int(x) for x in key], "N": N, "col_offset": 3, "rows": 42,
+                                    "z": [int(x) for x in z], "out": [int(x) for x in o]}
+    z8 = rng.integers(0, 256, size=N * 64, dtype=np.uint64)
+    o = np.zeros(16 * 64, np.uint64)
+    A.ref_commit_wide(key, z8, N, 0, 0, 16, o)
+    out["ajtai_commit_u8_ref"] = {"source": "as ajtai_commit_wide_ref, witness entries in [0, 256), rows 0..15",
+                                  "key": [int(x) for x in key], "N": N, "rows": 16,
+                                  "z": [int(x) for x in z8], "out": [int(x) for x in o]}
+    bits = rng.integers(0, 2**64, size=3, dtype=np.uint64)
+    o = np.zeros(42 * 64, np.uint64)
+    A.ref_commit_binary(key, bits, 3, o)
+    out["ajtai_commit_binary_ref"] = {"source": "cpu_ajtai_commit<64, 42> (ajtai_cpu_reference.cuh:157-181)",
+                                      "key": [int(x) for x in key], "z_bits": [int(x) for x in bits],
+                                      "out": [int(x) for x in o]}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    if not os.path.isdir(args.ref):
+        sys.exit("reference tree not found; fixtures are generated only where it exists")
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all", "ref", f"REF={args.ref}"], check=True)
+    data = {"generated_by": "tests/golden/make_golden.py"}
+    data.update(text_vectors(args.ref))
+    data.update(ref_vectors())
+    with open(os.path.join(HERE, "reference_vectors.json"), "w") as f:
+        json.dump(data, f, indent=0)
+    print("wrote", os.path.join(HERE, "reference_vectors.json"))
+
+
+if __name__ == "__main__":
+    main()
