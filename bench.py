@@ -1,0 +1,239 @@
+"""Benchmark: Basefold commit + open_ext2 proofs on one GB300 (proofs/sec).
+
+Workload (the reference's Basefold configuration): one multilinear polynomial of
+2^22 Goldilocks evaluations uniform in [0, p) from a fixed seed, rate 1/2
+(codeword 2^23), Poseidon2-w8 Merkle trees, 22 fold rounds with the interleaved
+sumcheck, 34 queries (the reference key's default), folding table
+BasefoldTable::generate(22, 1, 22, seed 42) resident on the device.  One step =
+commit + open of one proof with a fresh per-proof transcript.
+
+value: steps with evaluations already in HBM (device-timed with CUDA events on the
+       library's launch stream, L2 flushed between steps).
+e2e:   the same step through the C ABI from pinned host evaluations (host->device
+       copy inside the timed region) with the proof returned to host memory.
+
+--impl reference runs the CPU restatement of the reference's prover (the
+reference is Rust; its toolchain is absent) on a bounded sample and prints the
+same JSON line with impl=reference.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+P = 0xFFFFFFFF00000001
+N_VARS, LOG_RATE, QUERIES, TABLE_SEED = 22, 1, 34, 42
+METRIC = "proofs/sec"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-i", "0"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.splitlines()[0].split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._th.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_reference(args):
+    """CPU restatement of the reference prover on a bounded sample (the reference's Rust
+    crates cannot be built: no cargo/rustc here or on the GPU machine)."""
+    rank, world = env_rank()
+    if rank != 0:
+        return
+    import oracle as O
+    O.build(ref=False)
+    n_s = 14  # bounded sample: 2^14-evaluation proofs, scaled to the 2^22 workload by work ratio
+    rng = np.random.default_rng(7)
+    ev = rng.integers(0, P, size=1 << n_s, dtype=np.uint64)
+    pt = rng.integers(0, P, size=(n_s, 2), dtype=np.uint64)
+    table = O.basefold_table(n_s, LOG_RATE, n_s, TABLE_SEED)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        c = O.basefold_commit(ev, LOG_RATE)
+        O.basefold_open_ext2(c, pt, table, O.Transcript(b"bf-open"), QUERIES)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    # work scales ~linearly with 2^n (permutations, passes); the sample proof is 2^(22-14) smaller
+    scale = float(1 << (N_VARS - n_s))
+    sec_per_proof = statistics.mean(times) * scale
+    value = 1.0 / sec_per_proof
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_proof * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic",
+        "config": {"workload": "basefold commit+open_ext2, 2^22 evals, rate 1/2, 34 queries", "num_vars": N_VARS,
+                   "log_rate": LOG_RATE, "num_queries": QUERIES},
+        "cpu_baseline": {"value": value, "unit": "proofs/s", "cores": 1, "kind": "port",
+                         "sample": f"2^{n_s}-evaluation proofs x{args.steps}, time scaled x{int(scale)} to 2^22"},
+        "e2e": {"value": value, "unit": "proofs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--num-vars", type=int, default=N_VARS)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from morpheus_gb300 import build as B
+    B.build()
+    from morpheus_gb300 import _native as Nn
+    from morpheus_gb300.basefold import BasefoldCommitment, BasefoldTable
+    from morpheus_gb300.memory import DeviceBuffer
+    from morpheus_gb300.sumcheck import Transcript
+
+    rank, world = env_rank()
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group("nccl")
+    dev = torch.cuda.current_device()
+    L = Nn.lib()
+    stream = torch.cuda.Stream()
+    L.gb_set_stream(ctypes.c_void_p(stream.cuda_stream))
+
+    n = args.num_vars
+    rng = np.random.default_rng(1234 + rank)
+    ev_host = rng.integers(0, P, size=1 << n, dtype=np.uint64)
+    pt = rng.integers(0, P, size=(n, 2), dtype=np.uint64)
+    ev_dev = DeviceBuffer.from_numpy(ev_host)
+    table = BasefoldTable.generate(n, LOG_RATE, n, TABLE_SEED)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
+
+    def step_device():
+        c = BasefoldCommitment.commit(ev_dev, n, LOG_RATE)
+        proof = c.open_ext2(pt, table, Transcript(b"bf-open"), QUERIES)
+        return c, proof
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    if dist:
+        tdist.barrier()
+
+    times = []
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step_device()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        if dist:
+            tdist.barrier()
+        # e2e: pinned host evaluations through the C ABI, proof back to host
+        ev_pinned = torch.from_numpy(ev_host.view(np.int64)).pin_memory()
+        hptr = ev_pinned.data_ptr()
+        proof_len = L.gb_basefold_proof_len(n, LOG_RATE, QUERIES)
+        e2e_times = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h = ctypes.c_void_p()
+            root = np.zeros(4, np.uint64)
+            Nn.check(L.gb_basefold_commit(None, ctypes.c_void_p(hptr), n, LOG_RATE, ctypes.byref(h),
+                                          root.ctypes.data), "commit")
+            c = BasefoldCommitment(h, n, LOG_RATE, root)
+            c.open_ext2(pt, table, Transcript(b"bf-open"), QUERIES)
+            e2e_times.append(time.perf_counter() - t0)
+            del c
+    ms = statistics.mean(times)
+    tmax = torch.tensor([ms], device=dev)
+    if dist:
+        tdist.all_reduce(tmax, op=tdist.ReduceOp.MAX)
+    ms_max = float(tmax.item())
+    value = world * 1000.0 / ms_max
+    e2e_ms = statistics.mean(e2e_times) * 1e3
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic",
+            "config": {"workload": f"basefold commit+open_ext2, 2^{n} evals, rate 1/2, {QUERIES} queries",
+                       "num_vars": n, "log_rate": LOG_RATE, "num_queries": QUERIES, "table_seed": TABLE_SEED,
+                       "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "proofs/s", "h2d_bytes_per_step": 8 << n,
+                    "d2h_bytes_per_step": 8 * int(proof_len)},
+            "clocks": clk.summary(),
+            "step_ms_all": [round(t, 3) for t in times],
+        }
+        print(json.dumps(line))
+    if dist:
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -162,6 +162,32 @@ int gb_sumcheck_prove_ext2(gb_transcript *t, int n, int d, const uint64_t *d_pol
 int gb_sumcheck_prove_base(gb_transcript *t, int n, int d, const uint64_t *d_polys, const uint64_t *h_polys,
                            uint64_t *h_msgs, uint64_t *h_challenges, uint64_t *h_finals, uint64_t *h_final_eval);
 
+/* Basefold folding table: BasefoldTable::generate + upload (goldilocks-cuda-rs/src/basefold.rs:281-333).
+ * The xorshift draws run on the host, the 2^(n+lr) inversions on the device.  Synchronising. */
+int gb_basefold_table_create(int num_vars, int log_rate, int num_rounds, uint64_t seed, void **handle);
+int gb_basefold_table_destroy(void *handle);
+/* device pointer to the (point, weight) entries and the per-level entry offsets (num_rounds of them) */
+int gb_basefold_table_info(void *handle, uint64_t **d_entries, uint64_t *h_level_offsets);
+
+/* BasefoldCommitment::commit / commit_device (basefold.rs:382-427): evaluations (natural order,
+ * variable i <-> bit i) on the device or the host; the codeword, its Merkle tree and the
+ * evaluations stay device-resident in the returned handle.  root: canonical.  Synchronising. */
+int gb_basefold_commit(const uint64_t *d_evals, const uint64_t *h_evals, int num_vars, int log_rate, void **handle,
+                       uint64_t root[4]);
+int gb_basefold_commitment_destroy(void *handle);
+int gb_basefold_commitment_info(void *handle, uint64_t **d_codeword, uint64_t **d_tree, uint64_t **d_evals,
+                                uint64_t root[4]);
+
+/* Number of u64 in a flat open_ext2 proof: eval[2], oracles[n][3][2], folded_roots[n-1][4],
+ * final_codeword[2^lr][2], then per query: index, values[n][2][2], auth paths of depths
+ * n+lr-1, n+lr-2, ..., lr (4 u64 per digest) -- BasefoldProofExt2 (basefold.rs:124-132) flattened. */
+size_t gb_basefold_proof_len(int num_vars, int log_rate, int num_queries);
+/* BasefoldCommitment::open_ext2 (basefold.rs:578-870) with the zk-torch-3 transcript
+ * (BasefoldTranscript for Transcript, zk-torch-3/src/transcript.rs:331-350).  h_point: n Ext2
+ * values.  h_proof: gb_basefold_proof_len words, canonical.  Synchronising. */
+int gb_basefold_open_ext2(void *commitment, void *table, const uint64_t *h_point, gb_transcript *t,
+                          int num_queries, uint64_t *h_proof);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,39 @@ SIGNATURES = {
     "gb_transcript_challenge_ext2": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64p]),
     "gb_sumcheck_prove_ext2": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
     "gb_sumcheck_prove_base": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
+    "poseidon2_hash_batch_ffi": (i32, [vp, vp, i32]),
+    "poseidon2_compress_batch_ffi": (i32, [vp, vp, vp, i32]),
+    "poseidon2_merkle_layer_ffi": (i32, [vp, vp, i32]),
+    "poseidon2_merkle_tree_gl_ffi": (i32, [vp, vp, i32]),
+    "poseidon2_merkle_tree_ext2_ffi": (i32, [vp, vp, i32]),
+    "eq_dp_all_ffi": (i32, [vp, vp, vp, i32, ctypes.POINTER(vp)]),
+    "ext2_eq_dp_all_ffi": (i32, [vp, vp, vp, i32, ctypes.POINTER(vp)]),
+    "basefold_bit_reverse_gl_ffi": (i32, [vp, i32]),
+    "basefold_bit_reverse_ext2_ffi": (i32, [vp, i32]),
+    "basefold_bhc_interpolate_ffi": (i32, [vp, vp, vp, i32]),
+    "basefold_encode_ffi": (i32, [vp, vp, i32, i32]),
+    "basefold_fold_gl_ffi": (i32, [vp, vp, u64, vp, i32]),
+    "basefold_fold_mixed_ffi": (i32, [vp, vp, u64, u64, vp, i32]),
+    "basefold_fold_ext2_ffi": (i32, [vp, vp, u64, u64, vp, i32]),
+    "basefold_sumcheck_interp_gl_ffi": (i32, [vp, i32]),
+    "basefold_sumcheck_interp_ext2_ffi": (i32, [vp, i32]),
+    "basefold_sumcheck_product_gl_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32]),
+    "basefold_sumcheck_product_mixed_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32]),
+    "basefold_sumcheck_product_ext2_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32]),
+    "basefold_sumcheck_eval_gl_ffi": (i32, [vp, u64, vp, i32]),
+    "basefold_sumcheck_eval_mixed_ffi": (i32, [vp, u64, u64, vp, i32]),
+    "basefold_sumcheck_eval_ext2_ffi": (i32, [vp, u64, u64, vp, i32]),
+    "fused_sumcheck_round_ext2_ffi": (i32, [vp, vp, u64, u64, vp, vp, vp, vp, vp, i32, i32]),
+    "basefold_dot_product_gl_ffi": (i32, [vp, vp, vp, i32, i32]),
+    "basefold_dot_product_mixed_ffi": (i32, [vp, vp, vp, i32, i32]),
+    "gb_basefold_table_create": (i32, [i32, i32, i32, u64, ctypes.POINTER(vp)]),
+    "gb_basefold_table_destroy": (i32, [vp]),
+    "gb_basefold_table_info": (i32, [vp, ctypes.POINTER(vp), vp]),
+    "gb_basefold_commit": (i32, [vp, vp, i32, i32, ctypes.POINTER(vp), vp]),
+    "gb_basefold_commitment_destroy": (i32, [vp]),
+    "gb_basefold_commitment_info": (i32, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), vp]),
+    "gb_basefold_proof_len": (sz, [i32, i32, i32]),
+    "gb_basefold_open_ext2": (i32, [vp, vp, vp, ctypes.POINTER(GbTranscript), i32, vp]),
 }
 
 

@@ -1,0 +1,1023 @@
+// Basefold commit / open on the device: reference-ABI kernels
+// (goldilocks-cuda-rs/src/ffi.rs:416-545, wrapper.cu:1223-1600) and the
+// whole-proof drivers gb_basefold_*.
+//
+// Commit.  The reference interpolates evaluations to monomial coefficients
+// (per variable (e0, e1) -> (e0, e1 - e0)), repeats every coefficient 2^lr times,
+// applies n +-1 butterfly layers on bits lr..n+lr-1 and bit-reverses
+// (cuda/basefold.cuh:103-205).  Per variable the two steps compose to
+//     T = [[1,1],[1,-1]] [[1,0],[-1,1]] = [[0,1],[2,-1]]:  (e0, e1) -> (e1, 2 e0 - e1),
+// and because the repetition bits end up as the top bits after the reversal,
+//     codeword[j] = u[bitrev_n(j mod 2^n)],  u = T^(x)n (evals).
+// The codeword is 2^lr copies of one block, so its Merkle tree consists of 2^lr
+// identical subtrees: one is hashed, the others are copied (merkle.cu).
+//
+// Open (BasefoldCommitment::open_ext2, basefold.rs:578-870).  Round r's sumcheck
+// oracle (c0, c1, c2) over the pairs of the folded eq / bh tables comes from one
+// launch that also folds both tables with the previous challenge; the codeword
+// fold of round r writes the folded codeword and hashes its leaves in the same
+// launch.  Per round the host receives 10 canonical words (oracle + root), runs the
+// transcript and launches the next round.  Queries are gathered by one kernel.
+#include <cstring>
+#include <vector>
+
+#include "../../include/goldilocks_cuda_wrapper.h"
+#include "basefold.cuh"
+#include "host_field.hpp"
+#include "merkle.cuh"
+#include "reduce.cuh"
+
+namespace gb {
+
+// ===========================================================================
+// 2x2 per-variable transforms applied to K consecutive bits [b, b+K) in registers
+// MAT 0: T = (e1, 2 e0 - e1)   1: Moebius (e0, e1 - e0)   2: WHT (e0 + e1, e0 - e1)
+// ===========================================================================
+template <int MAT>
+__device__ __forceinline__ void bf_butterfly(u64& x0, u64& x1) {
+    if (MAT == 0) {
+        u64 t = gl_sub(gl_double(x0), x1);
+        x0 = x1;
+        x1 = t;
+    } else if (MAT == 1) {
+        x1 = gl_sub(x1, x0);
+    } else {
+        u64 a = gl_add(x0, x1), b = gl_sub(x0, x1);
+        x0 = a;
+        x1 = b;
+    }
+}
+
+template <int MAT, int K>
+__global__ void bf_transform_pass_kernel(const u64* __restrict__ in, u64* __restrict__ out, int b, size_t groups) {
+    size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (g >= groups) return;
+    size_t low = g & (((size_t)1 << b) - 1), high = g >> b;
+    size_t base = (high << (b + K)) | low;
+    u64 v[1 << K];
+#pragma unroll
+    for (int j = 0; j < (1 << K); j++) v[j] = in[base + ((size_t)j << b)];
+#pragma unroll
+    for (int l = 0; l < K; l++) {
+#pragma unroll
+        for (int j = 0; j < (1 << K); j++) {
+            if (!(j & (1 << l))) bf_butterfly<MAT>(v[j], v[j | (1 << l)]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < (1 << K); j++) out[base + ((size_t)j << b)] = v[j];
+}
+
+// apply the transform on all n bits; in may equal out
+template <int MAT>
+static int bf_transform(const u64* in, u64* out, int n) {
+    cudaStream_t s = stream();
+    size_t N = (size_t)1 << n;
+    if (n == 0) {
+        if (in != out) GB_CUDA_TRY(cudaMemcpyAsync(out, in, 8, cudaMemcpyDeviceToDevice, s));
+        return GB_OK;
+    }
+    const u64* src = in;
+    for (int b = 0; b < n;) {
+        int k = n - b >= 4 ? 4 : n - b;
+        size_t groups = N >> k;
+        switch (k) {
+            case 4: bf_transform_pass_kernel<MAT, 4><<<grid_for(groups, 128), 128, 0, s>>>(src, out, b, groups); break;
+            case 3: bf_transform_pass_kernel<MAT, 3><<<grid_for(groups, 128), 128, 0, s>>>(src, out, b, groups); break;
+            case 2: bf_transform_pass_kernel<MAT, 2><<<grid_for(groups, 128), 128, 0, s>>>(src, out, b, groups); break;
+            default: bf_transform_pass_kernel<MAT, 1><<<grid_for(groups, 128), 128, 0, s>>>(src, out, b, groups); break;
+        }
+        GB_LAUNCH_CHECK("bf_transform_pass_kernel");
+        src = out;
+        b += k;
+    }
+    return GB_OK;
+}
+
+__device__ __forceinline__ size_t bitrev_dev(size_t x, int bits) { return bits ? (__brevll(x) >> (64 - bits)) : 0; }
+
+// out[j] = in[bitrev_n(j mod 2^n)] for j < 2^(n+reps_log)
+__global__ void bitrev_replicate_kernel(const u64* __restrict__ in, u64* __restrict__ out, int n, size_t total) {
+    size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j >= total) return;
+    size_t m = j & (((size_t)1 << n) - 1);
+    out[j] = __ldg(in + bitrev_dev(m, n));
+}
+
+template <int W>
+__global__ void bit_reverse_inplace_kernel(u64* __restrict__ data, int log_n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >> log_n) return;
+    size_t j = bitrev_dev(i, log_n);
+    if (i < j) {
+#pragma unroll
+        for (int k = 0; k < W; k++) {
+            u64 t = data[W * i + k];
+            data[W * i + k] = data[W * j + k];
+            data[W * j + k] = t;
+        }
+    }
+}
+
+// ===========================================================================
+// reference-ABI elementwise kernels (sumcheck interp / eval / fold)
+// ===========================================================================
+template <bool EXT>
+__global__ void sc_interp_kernel(u64* __restrict__ d, size_t pairs) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= pairs) return;
+    if (EXT) {
+        u64* p = d + 4 * i;
+        p[2] = gl_sub(p[2], p[0]);
+        p[3] = gl_sub(p[3], p[1]);
+    } else {
+        d[2 * i + 1] = gl_sub(d[2 * i + 1], d[2 * i]);
+    }
+}
+
+// out[i] = data[2i] + ch * data[2i+1]; MODE 0 base/base, 1 base data + Ext2 ch, 2 Ext2
+template <int MODE>
+__global__ void sc_eval_kernel(const u64* __restrict__ d, u64 c0, u64 c1, u64* __restrict__ out, size_t pairs) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= pairs) return;
+    if (MODE == 0) {
+        out[i] = gl_add(d[2 * i], gl_mul(c0, d[2 * i + 1]));
+    } else if (MODE == 1) {
+        u64 a = d[2 * i], b = d[2 * i + 1];
+        out[2 * i] = gl_add(a, gl_mul(c0, b));
+        out[2 * i + 1] = gl_mul(c1, b);
+    } else {
+        const u64* p = d + 4 * i;
+        e2 r = e2_add(e2_make(p[0], p[1]), e2_mul(e2_make(c0, c1), e2_make(p[2], p[3])));
+        out[2 * i] = r.c0;
+        out[2 * i + 1] = r.c1;
+    }
+}
+
+// val0 + (ch - x0) (val1 - val0) w     (basefold.cuh:397-419, :522-548, :739-761)
+// MODE 0: base cw + base ch; 1: base cw + Ext2 ch (mixed); 2: Ext2 cw + Ext2 ch
+template <int MODE>
+__device__ __forceinline__ void fold_pair(const u64* cw, size_t i, u64 x0, u64 w, u64 c0, u64 c1, u64* o) {
+    if (MODE == 0) {
+        u64 v0 = cw[2 * i], v1 = cw[2 * i + 1];
+        o[0] = gl_add(v0, gl_mul(gl_mul(gl_sub(c0, x0), gl_sub(v1, v0)), w));
+    } else if (MODE == 1) {
+        u64 v0 = cw[2 * i], v1 = cw[2 * i + 1];
+        u64 dw = gl_mul(gl_sub(v1, v0), w);
+        o[0] = gl_add(v0, gl_mul(gl_sub(c0, x0), dw));
+        o[1] = gl_mul(c1, dw);
+    } else {
+        e2 v0 = e2_make(cw[4 * i], cw[4 * i + 1]), v1 = e2_make(cw[4 * i + 2], cw[4 * i + 3]);
+        e2 dw = e2_mul_base(e2_sub(v1, v0), w);
+        e2 r = e2_add(v0, e2_mul(e2_make(gl_sub(c0, x0), c1), dw));
+        o[0] = r.c0;
+        o[1] = r.c1;
+    }
+}
+
+template <int MODE>
+__global__ void bf_fold_kernel(const u64* __restrict__ cw, const u64* __restrict__ tab, u64 c0, u64 c1,
+                               u64* __restrict__ out, size_t pairs) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= pairs) return;
+    fold_pair<MODE>(cw, i, tab[2 * i], tab[2 * i + 1], c0, c1, out + (MODE == 0 ? i : 2 * i));
+}
+
+// Reference product kernels: per-block partials of c0 = sum eq_e bh_e,
+// c1 = sum (eq_e bh_o + eq_o bh_e), c2 = sum eq_o bh_o on interp'd (value, diff) pairs.
+// EQ_EXT/BH_EXT select Ext2 operands.
+template <bool EQ_EXT, bool BH_EXT>
+__device__ __forceinline__ void product_terms(const u64* eq, const u64* bh, size_t i, u64 (&acc)[6]) {
+    e2 ee, eo, be, bo;
+    if (EQ_EXT) {
+        ee = e2_make(eq[4 * i], eq[4 * i + 1]);
+        eo = e2_make(eq[4 * i + 2], eq[4 * i + 3]);
+    } else {
+        ee = e2_make(eq[2 * i], 0);
+        eo = e2_make(eq[2 * i + 1], 0);
+    }
+    if (BH_EXT) {
+        be = e2_make(bh[4 * i], bh[4 * i + 1]);
+        bo = e2_make(bh[4 * i + 2], bh[4 * i + 3]);
+    } else {
+        be = e2_make(bh[2 * i], 0);
+        bo = e2_make(bh[2 * i + 1], 0);
+    }
+    e2 t0, t1, t2;
+    if (!EQ_EXT && !BH_EXT) {
+        t0 = e2_make(gl_mul(ee.c0, be.c0), 0);
+        t1 = e2_make(gl_add(gl_mul(ee.c0, bo.c0), gl_mul(eo.c0, be.c0)), 0);
+        t2 = e2_make(gl_mul(eo.c0, bo.c0), 0);
+    } else if (!BH_EXT) {
+        t0 = e2_mul_base(ee, be.c0);
+        t1 = e2_add(e2_mul_base(ee, bo.c0), e2_mul_base(eo, be.c0));
+        t2 = e2_mul_base(eo, bo.c0);
+    } else {
+        t0 = e2_mul(ee, be);
+        t1 = e2_add(e2_mul(ee, bo), e2_mul(eo, be));
+        t2 = e2_mul(eo, bo);
+    }
+    acc[0] = gl_add(acc[0], t0.c0);
+    acc[1] = gl_add(acc[1], t0.c1);
+    acc[2] = gl_add(acc[2], t1.c0);
+    acc[3] = gl_add(acc[3], t1.c1);
+    acc[4] = gl_add(acc[4], t2.c0);
+    acc[5] = gl_add(acc[5], t2.c1);
+}
+
+__device__ __forceinline__ void write_c_partials(const u64 (&acc)[6], bool ext, u64* p0, u64* p1, u64* p2) {
+    if (threadIdx.x) return;
+    if (ext) {
+        p0[2 * blockIdx.x] = acc[0];
+        p0[2 * blockIdx.x + 1] = acc[1];
+        p1[2 * blockIdx.x] = acc[2];
+        p1[2 * blockIdx.x + 1] = acc[3];
+        p2[2 * blockIdx.x] = acc[4];
+        p2[2 * blockIdx.x + 1] = acc[5];
+    } else {
+        p0[blockIdx.x] = acc[0];
+        p1[blockIdx.x] = acc[2];
+        p2[blockIdx.x] = acc[4];
+    }
+}
+
+template <bool EQ_EXT, bool BH_EXT>
+__global__ void __launch_bounds__(RED_THREADS) sc_product_kernel(const u64* __restrict__ eq, const u64* __restrict__ bh,
+                                                                 u64* p0, u64* p1, u64* p2, size_t pairs) {
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x)
+        product_terms<EQ_EXT, BH_EXT>(eq, bh, i, acc);
+    block_reduce<6>(acc);
+    write_c_partials(acc, EQ_EXT || BH_EXT, p0, p1, p2);
+}
+
+// fused_sumcheck_round_ext2_kernel semantics (basefold.cuh:654-735): eval at ch, interp, product
+__global__ void __launch_bounds__(RED_THREADS) sc_fused_round_ref_kernel(const u64* __restrict__ eq_in,
+                                                                         const u64* __restrict__ bh_in, u64 c0, u64 c1,
+                                                                         u64* __restrict__ eq_out, u64* __restrict__ bh_out,
+                                                                         u64* p0, u64* p1, u64* p2, size_t pairs) {
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    const e2 ch = e2_make(c0, c1);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x) {
+        const u64* q = eq_in + 8 * i;
+        const u64* h = bh_in + 8 * i;
+        e2 ea = e2_add(e2_make(q[0], q[1]), e2_mul(ch, e2_make(q[2], q[3])));
+        e2 eb = e2_add(e2_make(q[4], q[5]), e2_mul(ch, e2_make(q[6], q[7])));
+        e2 ba = e2_add(e2_make(h[0], h[1]), e2_mul(ch, e2_make(h[2], h[3])));
+        e2 bb = e2_add(e2_make(h[4], h[5]), e2_mul(ch, e2_make(h[6], h[7])));
+        e2 eo = e2_sub(eb, ea), bo = e2_sub(bb, ba);
+        e2_st(eq_out + 4 * i, ea);
+        e2_st(eq_out + 4 * i + 2, eo);
+        e2_st(bh_out + 4 * i, ba);
+        e2_st(bh_out + 4 * i + 2, bo);
+        e2 t0 = e2_mul(ea, ba), t1 = e2_add(e2_mul(ea, bo), e2_mul(eo, ba)), t2 = e2_mul(eo, bo);
+        acc[0] = gl_add(acc[0], t0.c0);
+        acc[1] = gl_add(acc[1], t0.c1);
+        acc[2] = gl_add(acc[2], t1.c0);
+        acc[3] = gl_add(acc[3], t1.c1);
+        acc[4] = gl_add(acc[4], t2.c0);
+        acc[5] = gl_add(acc[5], t2.c1);
+    }
+    block_reduce<6>(acc);
+    write_c_partials(acc, true, p0, p1, p2);
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(RED_THREADS) dot_product_kernel(const u64* __restrict__ a, const u64* __restrict__ b,
+                                                                  u64* __restrict__ out, size_t n) {
+    u64 acc[2] = {0, 0};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (MIXED) {
+            e2 v = e2_mul_base(e2_make(b[2 * i], b[2 * i + 1]), a[i]);
+            acc[0] = gl_add(acc[0], v.c0);
+            acc[1] = gl_add(acc[1], v.c1);
+        } else {
+            acc[0] = gl_add(acc[0], gl_mul(a[i], b[i]));
+        }
+    }
+    block_reduce<2>(acc);
+    if (threadIdx.x == 0) {
+        if (MIXED) {
+            out[2 * blockIdx.x] = acc[0];
+            out[2 * blockIdx.x + 1] = acc[1];
+        } else {
+            out[blockIdx.x] = acc[0];
+        }
+    }
+}
+
+// ===========================================================================
+// open_ext2 driver kernels
+// ===========================================================================
+
+// Round 0 oracle on (bh base, eq Ext2) at full size: acc = (c0, s1, c2) with
+// s1 = sum eq_o bh_o = c0 + c1 + c2.  Also the pairs' eval = c0 + s1.
+__global__ void __launch_bounds__(RED_THREADS) open_round0_kernel(const u64* __restrict__ bh, const u64* __restrict__ eq,
+                                                                  size_t pairs, u64* __restrict__ partials,
+                                                                  u64* __restrict__ out, unsigned* __restrict__ counter) {
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x) {
+        ulonglong2 b2 = __ldg(reinterpret_cast<const ulonglong2*>(bh) + i);
+        e2 ee = e2_ld(eq + 4 * i), eo = e2_ld(eq + 4 * i + 2);
+        u64 bd = gl_sub(b2.y, b2.x);
+        e2 ed = e2_sub(eo, ee);
+        e2 t0 = e2_mul_base(ee, b2.x), t1 = e2_mul_base(eo, b2.y), t2 = e2_mul_base(ed, bd);
+        acc[0] = gl_add(acc[0], t0.c0);
+        acc[1] = gl_add(acc[1], t0.c1);
+        acc[2] = gl_add(acc[2], t1.c0);
+        acc[3] = gl_add(acc[3], t1.c1);
+        acc[4] = gl_add(acc[4], t2.c0);
+        acc[5] = gl_add(acc[5], t2.c1);
+    }
+    grid_reduce_finish<6>(acc, partials, out, counter);
+}
+
+// Round r >= 1: fold eq (Ext2) and bh (base when BH_BASE) with ch = (c0, c1) from the
+// previous level, store the folded level, accumulate (c0, s1, c2) over its pairs.
+template <bool BH_BASE>
+__global__ void __launch_bounds__(RED_THREADS) open_round_kernel(const u64* __restrict__ eq_in, const u64* __restrict__ bh_in,
+                                                                 u64* __restrict__ eq_out, u64* __restrict__ bh_out,
+                                                                 size_t quarter, u64 c0, u64 c1,
+                                                                 u64* __restrict__ partials, u64* __restrict__ out,
+                                                                 unsigned* __restrict__ counter) {
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    const e2 ch = e2_make(c0, c1);
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < quarter; y += (size_t)gridDim.x * blockDim.x) {
+        const u64* q = eq_in + 8 * y;
+        e2 x0 = e2_ld(q), x1 = e2_ld(q + 2), x2 = e2_ld(q + 4), x3 = e2_ld(q + 6);
+        e2 ea = e2_add(x0, e2_mul(ch, e2_sub(x1, x0)));
+        e2 eb = e2_add(x2, e2_mul(ch, e2_sub(x3, x2)));
+        e2 ba, bb;
+        if (BH_BASE) {
+            ulonglong2 p = __ldg(reinterpret_cast<const ulonglong2*>(bh_in + 4 * y));
+            ulonglong2 r = __ldg(reinterpret_cast<const ulonglong2*>(bh_in + 4 * y + 2));
+            u64 d0 = gl_sub(p.y, p.x), d1 = gl_sub(r.y, r.x);
+            ba = e2_make(gl_add(p.x, gl_mul(c0, d0)), gl_mul(c1, d0));
+            bb = e2_make(gl_add(r.x, gl_mul(c0, d1)), gl_mul(c1, d1));
+        } else {
+            const u64* h = bh_in + 8 * y;
+            e2 h0 = e2_ld(h), h1 = e2_ld(h + 2), h2 = e2_ld(h + 4), h3 = e2_ld(h + 6);
+            ba = e2_add(h0, e2_mul(ch, e2_sub(h1, h0)));
+            bb = e2_add(h2, e2_mul(ch, e2_sub(h3, h2)));
+        }
+        e2_st(eq_out + 4 * y, ea);
+        e2_st(eq_out + 4 * y + 2, eb);
+        e2_st(bh_out + 4 * y, ba);
+        e2_st(bh_out + 4 * y + 2, bb);
+        e2 t0 = e2_mul(ea, ba), t1 = e2_mul(eb, bb), t2 = e2_mul(e2_sub(eb, ea), e2_sub(bb, ba));
+        acc[0] = gl_add(acc[0], t0.c0);
+        acc[1] = gl_add(acc[1], t0.c1);
+        acc[2] = gl_add(acc[2], t1.c0);
+        acc[3] = gl_add(acc[3], t1.c1);
+        acc[4] = gl_add(acc[4], t2.c0);
+        acc[5] = gl_add(acc[5], t2.c1);
+    }
+    grid_reduce_finish<6>(acc, partials, out, counter);
+}
+
+// Codeword fold of one round fused with hashing the folded codeword's leaves:
+// leaf i = P2(f[2i], f[2i+1]) with f[k] = fold(cw[2k], cw[2k+1], table[k]).
+// BASE_IN: the input codeword is the base-field committed one (mixed fold).
+template <bool BASE_IN>
+__global__ void __launch_bounds__(128) fold_hash_leaves_kernel(const u64* __restrict__ cw, const u64* __restrict__ tab,
+                                                               u64 c0, u64 c1, u64* __restrict__ folded,
+                                                               u64* __restrict__ tree, size_t leaves) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= leaves) return;
+    ulonglong2 t0 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i);
+    ulonglong2 t1 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i + 1);
+    e2 f0, f1;
+    if (BASE_IN) {
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i);
+        ulonglong2 u = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i + 1);
+        u64 dw0 = gl_mul(gl_sub(v.y, v.x), t0.y), dw1 = gl_mul(gl_sub(u.y, u.x), t1.y);
+        f0 = e2_make(gl_add(v.x, gl_mul(gl_sub(c0, t0.x), dw0)), gl_mul(c1, dw0));
+        f1 = e2_make(gl_add(u.x, gl_mul(gl_sub(c0, t1.x), dw1)), gl_mul(c1, dw1));
+    } else {
+        const u64* p = cw + 8 * i;
+        e2 a0 = e2_ld(p), a1 = e2_ld(p + 2), b0 = e2_ld(p + 4), b1 = e2_ld(p + 6);
+        e2 dw0 = e2_mul_base(e2_sub(a1, a0), t0.y), dw1 = e2_mul_base(e2_sub(b1, b0), t1.y);
+        f0 = e2_add(a0, e2_mul(e2_make(gl_sub(c0, t0.x), c1), dw0));
+        f1 = e2_add(b0, e2_mul(e2_make(gl_sub(c0, t1.x), c1), dw1));
+    }
+    e2_st(folded + 4 * i, f0);
+    e2_st(folded + 4 * i + 2, f1);
+    u64 s[8] = {f0.c0, f0.c1, f1.c0, f1.c1, 0, 0, 0, 0};
+    p2_permute(s);
+    st_digest(tree + 4 * i, s);
+}
+
+// Final fold (no tree): Ext2 codeword of 2*pairs elements -> pairs elements, canonical.
+__global__ void fold_final_kernel(const u64* __restrict__ cw, const u64* __restrict__ tab, u64 c0, u64 c1,
+                                  u64* __restrict__ out, size_t pairs, bool base_in) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= pairs) return;
+    u64 o[2];
+    if (base_in) fold_pair<1>(cw, i, tab[2 * i], tab[2 * i + 1], c0, c1, o);
+    else fold_pair<2>(cw, i, tab[2 * i], tab[2 * i + 1], c0, c1, o);
+    out[2 * i] = gl_canon(o[0]);
+    out[2 * i + 1] = gl_canon(o[1]);
+}
+
+// Query gather.  For query q with leaf index L (computed on the host from the transcript):
+// index, values of every round (initial pair lifted to Ext2, then the folded pairs) and all
+// authentication paths, written canonical into the flat proof layout.
+struct QueryJob {
+    const u64* cw0;           // base codeword
+    const u64* tree0;         // its tree
+    const u64* const* fcw;    // folded codewords r = 0..n-2 (device array of pointers)
+    const u64* const* ftree;  // their trees
+    int n, lr;
+};
+
+__global__ void query_gather_kernel(QueryJob job, const u64* __restrict__ leaf_idx, int num_queries, size_t per_query,
+                                    u64* __restrict__ out) {
+    int q = blockIdx.x;
+    if (q >= num_queries) return;
+    const int n = job.n, lr = job.lr;
+    const size_t leaf = leaf_idx[q];
+    u64* o = out + (size_t)q * per_query;
+    u64* vals = o + 1;
+    u64* paths = vals + (size_t)n * 4;
+    if (threadIdx.x == 0) {
+        o[0] = leaf;
+        vals[0] = gl_canon(job.cw0[2 * leaf]);
+        vals[1] = 0;
+        vals[2] = gl_canon(job.cw0[2 * leaf + 1]);
+        vals[3] = 0;
+    }
+    for (int r = threadIdx.x; r + 1 < n; r += blockDim.x) {
+        size_t pi = leaf >> (r + 1);
+        const u64* f = job.fcw[r] + 4 * pi;
+        u64* v = vals + 4 * (r + 1);
+        for (int k = 0; k < 4; k++) v[k] = gl_canon(f[k]);
+    }
+    // path words: tree 0 has depth n+lr-1, tree r+1 (folded r) depth n+lr-2-r
+    size_t total_depth = 0;
+    for (int r = 0; r < n; r++) total_depth += (size_t)(n + lr - 1 - r);
+    for (size_t node = threadIdx.x; node < total_depth; node += blockDim.x) {
+        // locate (tree t, level l) of this path node
+        size_t rem = node;
+        int t = 0;
+        size_t depth = (size_t)(n + lr - 1);
+        while (rem >= depth) {
+            rem -= depth;
+            t++;
+            depth--;
+        }
+        int level = (int)rem;
+        size_t leaves = (size_t)1 << (n + lr - 1 - t);
+        const u64* tree = t == 0 ? job.tree0 : job.ftree[t - 1];
+        size_t li = (t == 0 ? leaf : (leaf >> t)) >> level;
+        size_t off = 0, sz = leaves;
+        for (int l = 0; l < level; l++) {
+            off += sz;
+            sz >>= 1;
+        }
+        const u64* dg = tree + 4 * (off + (li ^ 1));
+        u64* dst = paths + 4 * node;
+        for (int k = 0; k < 4; k++) dst[k] = gl_canon(dg[k]);
+    }
+}
+
+// ===========================================================================
+// host side
+// ===========================================================================
+static inline size_t path_words_total(int n, int lr) {
+    size_t s = 0;
+    for (int r = 0; r < n; r++) s += (size_t)(n + lr - 1 - r);
+    return s * 4;
+}
+static inline size_t proof_len(int n, int lr, int q) {
+    size_t per_q = 1 + (size_t)n * 4 + path_words_total(n, lr);
+    return 2 + (size_t)n * 6 + (size_t)(n - 1) * 4 + ((size_t)2 << lr) + (size_t)q * per_q;
+}
+
+static unsigned red_grid(size_t work) {
+    size_t cap = (size_t)num_sms() * 4;
+    size_t need = (work + RED_THREADS - 1) / RED_THREADS;
+    if (need < 1) need = 1;
+    return (unsigned)(need < cap ? need : cap);
+}
+
+struct DevMem {
+    std::vector<void*> ptrs;
+    template <typename T>
+    int alloc(T** p, size_t bytes) {
+        void* q = nullptr;
+        cudaError_t e = cudaMallocAsync(&q, bytes < 16 ? 16 : bytes, stream());
+        if (e != cudaSuccess) {
+            set_error("cudaMallocAsync", e);
+            return GB_ECUDA;
+        }
+        ptrs.push_back(q);
+        *p = (T*)q;
+        return GB_OK;
+    }
+    ~DevMem() {
+        for (void* p : ptrs) cudaFreeAsync(p, stream());
+    }
+};
+
+static u64* pinned(size_t words) {
+    static thread_local u64* buf = nullptr;
+    static thread_local size_t cap = 0;
+    if (words > cap) {
+        if (buf) cudaFreeHost(buf);
+        size_t c = words < 8192 ? 8192 : words;
+        if (cudaMallocHost(&buf, c * 8) != cudaSuccess) {
+            buf = nullptr;
+            cap = 0;
+            return nullptr;
+        }
+        cap = c;
+    }
+    return buf;
+}
+
+#define RC_TRY(x)                 \
+    do {                          \
+        int _r = (x);             \
+        if (_r) return _r;        \
+    } while (0)
+
+// commit from device evaluations (natural order) into a new commitment object
+static int commit_device(const u64* d_evals, int n, int lr, BfCommitment* c) {
+    cudaStream_t s = stream();
+    size_t N = (size_t)1 << n, L = N << lr, leaves = L / 2;
+    c->num_vars = n;
+    c->log_rate = lr;
+    GB_CUDA_TRY(cudaMallocAsync(&c->d_evals, N * 8, s));
+    GB_CUDA_TRY(cudaMallocAsync(&c->d_codeword, L * 8, s));
+    GB_CUDA_TRY(cudaMallocAsync(&c->d_tree, (2 * leaves - 1) * 32, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(c->d_evals, d_evals, N * 8, cudaMemcpyDeviceToDevice, s));
+    u64* u = nullptr;
+    GB_CUDA_TRY(cudaMallocAsync(&u, N * 8, s));
+    int rc = bf_transform<0>(d_evals, u, n);
+    if (!rc) {
+        bitrev_replicate_kernel<<<grid_for(L, 256), 256, 0, s>>>(u, c->d_codeword, n, L);
+        rc = check_launch("bitrev_replicate_kernel");
+    }
+    cudaFreeAsync(u, s);
+    RC_TRY(rc);
+    RC_TRY(merkle_tree_gl_replicated(c->d_codeword, c->d_tree, leaves, n >= 1 ? lr : 0));
+    u64* st = pinned(4);
+    if (!st) return GB_ECUDA;
+    GB_CUDA_TRY(cudaMemcpyAsync(st, c->d_tree + (2 * leaves - 2) * 4, 32, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int k = 0; k < 4; k++) c->root[k] = gl_canon(st[k]);
+    return GB_OK;
+}
+
+static void commitment_free(BfCommitment* c) {
+    cudaStream_t s = stream();
+    if (c->d_evals) cudaFreeAsync(c->d_evals, s);
+    if (c->d_codeword) cudaFreeAsync(c->d_codeword, s);
+    if (c->d_tree) cudaFreeAsync(c->d_tree, s);
+    c->d_evals = c->d_codeword = c->d_tree = nullptr;
+}
+
+__global__ void table_weights_kernel(const u64* __restrict__ x1, u64* __restrict__ ent, size_t total) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    u64 x0 = ent[2 * i];
+    ent[2 * i + 1] = gl_canon(gl_inv(gl_canon(gl_sub(x1[i], x0))));
+}
+
+static int table_create(int num_vars, int log_rate, int num_rounds, u64 seed, BfTable* t) {
+    if (num_vars < 1 || log_rate < 0 || num_rounds < 1 || num_rounds > num_vars + log_rate || num_vars + log_rate > 40)
+        return GB_EINVAL;
+    t->num_vars = num_vars;
+    t->log_rate = log_rate;
+    t->num_rounds = num_rounds;
+    t->seed = seed;
+    size_t total = 0;
+    t->level_offsets.clear();
+    for (int i = 0; i < num_rounds; i++) {
+        t->level_offsets.push_back(total);
+        total += (size_t)1 << (num_vars + log_rate - i - 1);
+    }
+    t->total = total;
+    // xorshift64 (13, 7, 17), every draw reduced mod p; x1 redrawn while equal to x0
+    // (goldilocks-cuda-rs/src/basefold.rs:281-321).  The draws are sequential; the
+    // inversions run on the device.
+    std::vector<u64> host(2 * total);
+    std::vector<u64> x1s(total);
+    u64 st = seed;
+    auto next = [&st]() {
+        st ^= st << 13;
+        st ^= st >> 7;
+        st ^= st << 17;
+        return st % GL_P;
+    };
+    for (size_t k = 0; k < total; k++) {
+        u64 x0 = next(), x1 = next();
+        while (x1 == x0) x1 = next();
+        host[2 * k] = x0;
+        x1s[k] = x1;
+    }
+    cudaStream_t s = stream();
+    u64* d_x1 = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&t->d_entries, total * 16));
+    GB_CUDA_TRY(cudaMallocAsync(&d_x1, total * 8, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(t->d_entries, host.data(), total * 16, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_x1, x1s.data(), total * 8, cudaMemcpyHostToDevice, s));
+    table_weights_kernel<<<grid_for(total, 256), 256, 0, s>>>(d_x1, t->d_entries, total);
+    GB_LAUNCH_CHECK("table_weights_kernel");
+    cudaFreeAsync(d_x1, s);
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return GB_OK;
+}
+
+// BasefoldCommitment::open_ext2 (basefold.rs:578-870) into the flat proof layout.
+static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_point, gb_transcript* t, int num_queries,
+                     u64* h_proof) {
+    using namespace host;
+    const int n = c->num_vars, lr = c->log_rate;
+    if (n < 2 || num_queries < 0 || !tab->d_entries || tab->num_rounds < n || tab->log_rate != lr ||
+        tab->num_vars < n) {
+        set_error_msg("gb_basefold_open_ext2: table does not cover this commitment (or num_vars < 2)");
+        return GB_EINVAL;
+    }
+    cudaStream_t s = stream();
+    const size_t N = (size_t)1 << n, L = N << lr;
+    DevMem m;
+    u64 *d_point, *eq, *eqA, *eqB, *bhA, *bhB, *partials, *rec;
+    unsigned* counter;
+    RC_TRY(m.alloc(&d_point, (size_t)n * 16));
+    RC_TRY(m.alloc(&eq, N * 16));
+    RC_TRY(m.alloc(&eqA, N * 8));  // N/2 Ext2
+    RC_TRY(m.alloc(&eqB, N * 8));
+    RC_TRY(m.alloc(&bhA, N * 8));
+    RC_TRY(m.alloc(&bhB, N * 8));
+    const unsigned gmax = red_grid(N / 2);
+    RC_TRY(m.alloc(&partials, (size_t)gmax * 6 * 8));
+    RC_TRY(m.alloc(&rec, 16 * 8));
+    RC_TRY(m.alloc(&counter, 16));
+    GB_CUDA_TRY(cudaMemsetAsync(counter, 0, 16, s));
+    // folded codewords r = 0..n-1 (L >> (r+1) Ext2 each) and trees r = 0..n-2
+    std::vector<u64*> fcw(n), ftree(n - 1);
+    for (int r = 0; r < n; r++) RC_TRY(m.alloc(&fcw[r], (L >> (r + 1)) * 16));
+    for (int r = 0; r + 1 < n; r++) {
+        size_t leaves = (L >> (r + 1)) / 2;
+        RC_TRY(m.alloc(&ftree[r], (2 * leaves - 1) * 32));
+    }
+    u64* stage = pinned(64);
+    if (!stage) return GB_ECUDA;
+
+    u64* pp = h_proof;
+    u64* p_eval = pp;
+    u64* p_oracles = pp + 2;
+    u64* p_roots = p_oracles + (size_t)n * 6;
+    u64* p_final = p_roots + (size_t)(n - 1) * 4;
+    u64* p_queries = p_final + ((size_t)2 << lr);
+
+    // transcript preamble
+    for (int k = 0; k < 4; k++) tr_append_u64(t, "", c->root[k]);
+    std::vector<u64> pt(2 * n);
+    for (int i = 0; i < n; i++) {
+        pt[2 * i] = canon(h_point[2 * i]);
+        pt[2 * i + 1] = canon(h_point[2 * i + 1]);
+        tr_append_ext2(t, "", E2{pt[2 * i], pt[2 * i + 1]});
+    }
+    GB_CUDA_TRY(cudaMemcpyAsync(d_point, pt.data(), (size_t)n * 16, cudaMemcpyHostToDevice, s));
+    RC_TRY(eq_table(d_point, n, true, eq));
+
+    auto read_rec = [&](int words) -> int {
+        GB_CUDA_TRY(cudaMemcpyAsync(stage, rec, (size_t)words * 8, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        return GB_OK;
+    };
+    auto put_oracle = [&](int r) {
+        // stage: c0 (2), s1 (2), c2 (2) -> c1 = s1 - c0 - c2
+        E2 c0{stage[0], stage[1]}, s1{stage[2], stage[3]}, c2{stage[4], stage[5]};
+        E2 c1 = e2sub(e2sub(s1, c0), c2);
+        u64* o = p_oracles + (size_t)r * 6;
+        o[0] = c0.c0;
+        o[1] = c0.c1;
+        o[2] = c1.c0;
+        o[3] = c1.c1;
+        o[4] = c2.c0;
+        o[5] = c2.c1;
+        tr_append_ext2(t, "", c0);
+        tr_append_ext2(t, "", c1);
+        tr_append_ext2(t, "", c2);
+        return s1;
+    };
+
+    // round 0 oracle (bh = evals base, eq Ext2); eval = c0 + s1
+    open_round0_kernel<<<red_grid(N / 2), RED_THREADS, 0, s>>>(c->d_evals, eq, N / 2, partials, rec, counter);
+    GB_LAUNCH_CHECK("open_round0_kernel");
+    RC_TRY(read_rec(6));
+    {
+        E2 c0{stage[0], stage[1]};
+        E2 s1 = put_oracle(0);
+        E2 ev = e2add(c0, s1);
+        p_eval[0] = ev.c0;
+        p_eval[1] = ev.c1;
+    }
+
+    const u64* eq_cur = eq;
+    const u64* bh_cur = c->d_evals;
+    u64* eq_bufs[2] = {eqA, eqB};
+    u64* bh_bufs[2] = {bhA, bhB};
+    int pp_i = 0;
+    size_t sc = N;  // current sumcheck table size
+    for (int rd = 0; rd < n; rd++) {
+        E2 ch = tr_challenge_ext2(t, "");
+        if (rd < n - 1) {
+            size_t quarter = sc / 4;  // output pairs of the folded level
+            u64* eo = eq_bufs[pp_i];
+            u64* bo = bh_bufs[pp_i];
+            unsigned g = red_grid(quarter);
+            if (rd == 0)
+                open_round_kernel<true><<<g, RED_THREADS, 0, s>>>(eq_cur, bh_cur, eo, bo, quarter, ch.c0, ch.c1, partials,
+                                                                  rec, counter);
+            else
+                open_round_kernel<false><<<g, RED_THREADS, 0, s>>>(eq_cur, bh_cur, eo, bo, quarter, ch.c0, ch.c1,
+                                                                   partials, rec, counter);
+            GB_LAUNCH_CHECK("open_round_kernel");
+            eq_cur = eo;
+            bh_cur = bo;
+            pp_i ^= 1;
+            sc /= 2;
+        }
+        const u64* lvl = tab->d_entries + 2 * tab->level_offsets[rd];
+        const u64* cw_in = rd == 0 ? c->d_codeword : fcw[rd - 1];
+        size_t pairs = L >> (rd + 1);
+        if (rd < n - 1) {
+            size_t leaves = pairs / 2;
+            if (rd == 0)
+                fold_hash_leaves_kernel<true><<<grid_for(leaves, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                                     ftree[rd], leaves);
+            else
+                fold_hash_leaves_kernel<false><<<grid_for(leaves, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                                      ftree[rd], leaves);
+            GB_LAUNCH_CHECK("fold_hash_leaves_kernel");
+            RC_TRY(merkle_build_from_leaves(ftree[rd], leaves));
+            GB_CUDA_TRY(cudaMemcpyAsync(rec + 8, ftree[rd] + (2 * leaves - 2) * 4, 32, cudaMemcpyDeviceToDevice, s));
+            RC_TRY(read_rec(12));
+            put_oracle(rd + 1);
+            u64* root = p_roots + (size_t)rd * 4;
+            for (int k = 0; k < 4; k++) {
+                root[k] = canon(stage[8 + k]);
+                tr_append_u64(t, "", root[k]);
+            }
+        } else {
+            fold_final_kernel<<<grid_for(pairs, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], pairs, rd == 0);
+            GB_LAUNCH_CHECK("fold_final_kernel");
+        }
+    }
+    // final codeword (2^lr Ext2)
+    GB_CUDA_TRY(cudaMemcpyAsync(p_final, fcw[n - 1], ((size_t)2 << lr) * 8, cudaMemcpyDeviceToHost, s));
+
+    // query phase: indices from the transcript, one gather launch
+    const size_t per_q = 1 + (size_t)n * 4 + path_words_total(n, lr);
+    if (num_queries > 0) {
+        std::vector<u64> idx(num_queries);
+        for (int q = 0; q < num_queries; q++) idx[q] = tr_challenge(t, "") % (u64)(L / 2);
+        u64 *d_idx, *d_out;
+        const u64** d_ptrs;
+        RC_TRY(m.alloc(&d_idx, (size_t)num_queries * 8));
+        RC_TRY(m.alloc(&d_out, (size_t)num_queries * per_q * 8));
+        RC_TRY(m.alloc(&d_ptrs, (size_t)2 * n * sizeof(u64*)));
+        std::vector<const u64*> ptrs(2 * n, nullptr);
+        for (int r = 0; r + 1 < n; r++) {
+            ptrs[r] = fcw[r];
+            ptrs[n + r] = ftree[r];
+        }
+        GB_CUDA_TRY(cudaMemcpyAsync(d_idx, idx.data(), (size_t)num_queries * 8, cudaMemcpyHostToDevice, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), ptrs.size() * sizeof(u64*), cudaMemcpyHostToDevice, s));
+        QueryJob job{c->d_codeword, c->d_tree, d_ptrs, d_ptrs + n, n, lr};
+        query_gather_kernel<<<num_queries, 128, 0, s>>>(job, d_idx, num_queries, per_q, d_out);
+        GB_LAUNCH_CHECK("query_gather_kernel");
+        GB_CUDA_TRY(cudaMemcpyAsync(p_queries, d_out, (size_t)num_queries * per_q * 8, cudaMemcpyDeviceToHost, s));
+    }
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return GB_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+// ---------------------------------------------------------------- reference ABI
+int basefold_bit_reverse_gl_ffi(uint64_t* d, int log_n) {
+    if (log_n < 0 || log_n > 40) return GB_EINVAL;
+    bit_reverse_inplace_kernel<1><<<grid_for((size_t)1 << log_n, 256), 256, 0, stream()>>>(d, log_n);
+    return check_launch("basefold_bit_reverse_gl_ffi");
+}
+int basefold_bit_reverse_ext2_ffi(uint64_t* d, int log_n) {
+    if (log_n < 0 || log_n > 40) return GB_EINVAL;
+    bit_reverse_inplace_kernel<2><<<grid_for((size_t)1 << log_n, 256), 256, 0, stream()>>>(d, log_n);
+    return check_launch("basefold_bit_reverse_ext2_ffi");
+}
+
+int basefold_bhc_interpolate_ffi(const uint64_t* d_evals, uint64_t* d_coeffs, uint64_t* d_bh_evals, int num_vars) {
+    if (num_vars < 0 || num_vars > 40) return GB_EINVAL;
+    size_t N = (size_t)1 << num_vars;
+    RC_TRY(bf_transform<1>(d_evals, d_coeffs, num_vars));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_bh_evals, d_evals, N * 8, cudaMemcpyDeviceToDevice, stream()));
+    bit_reverse_inplace_kernel<1><<<grid_for(N, 256), 256, 0, stream()>>>(d_bh_evals, num_vars);
+    GB_LAUNCH_CHECK("basefold_bhc_interpolate_ffi");
+    return sync_stream("basefold_bhc_interpolate_ffi");
+}
+
+int basefold_encode_ffi(const uint64_t* d_coeffs, uint64_t* d_codeword, int num_vars, int log_rate) {
+    if (num_vars < 0 || log_rate < 0 || num_vars + log_rate > 40) return GB_EINVAL;
+    cudaStream_t s = stream();
+    size_t N = (size_t)1 << num_vars, L = N << log_rate;
+    u64* u = nullptr;
+    GB_CUDA_TRY(cudaMallocAsync(&u, N * 8, s));
+    int rc = bf_transform<2>(d_coeffs, u, num_vars);
+    if (!rc) {
+        bitrev_replicate_kernel<<<grid_for(L, 256), 256, 0, s>>>(u, d_codeword, num_vars, L);
+        rc = check_launch("basefold_encode_ffi");
+    }
+    cudaFreeAsync(u, s);
+    RC_TRY(rc);
+    return sync_stream("basefold_encode_ffi");
+}
+
+int basefold_fold_gl_ffi(const uint64_t* cw, const uint64_t* tab, uint64_t ch, uint64_t* out, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    bf_fold_kernel<0><<<grid_for(pairs, 256), 256, 0, stream()>>>(cw, tab, ch, 0, out, pairs);
+    return check_launch("basefold_fold_gl_ffi");
+}
+int basefold_fold_mixed_ffi(const uint64_t* cw, const uint64_t* tab, uint64_t c0, uint64_t c1, uint64_t* out, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    bf_fold_kernel<1><<<grid_for(pairs, 256), 256, 0, stream()>>>(cw, tab, c0, c1, out, pairs);
+    return check_launch("basefold_fold_mixed_ffi");
+}
+int basefold_fold_ext2_ffi(const uint64_t* cw, const uint64_t* tab, uint64_t c0, uint64_t c1, uint64_t* out, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    bf_fold_kernel<2><<<grid_for(pairs, 256), 256, 0, stream()>>>(cw, tab, c0, c1, out, pairs);
+    return check_launch("basefold_fold_ext2_ffi");
+}
+
+int basefold_sumcheck_interp_gl_ffi(uint64_t* d, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    sc_interp_kernel<false><<<grid_for(pairs, 256), 256, 0, stream()>>>(d, pairs);
+    return check_launch("basefold_sumcheck_interp_gl_ffi");
+}
+int basefold_sumcheck_interp_ext2_ffi(uint64_t* d, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    sc_interp_kernel<true><<<grid_for(pairs, 256), 256, 0, stream()>>>(d, pairs);
+    return check_launch("basefold_sumcheck_interp_ext2_ffi");
+}
+
+int basefold_sumcheck_product_gl_ffi(const uint64_t* eq, const uint64_t* bh, uint64_t* p0, uint64_t* p1, uint64_t* p2,
+                                     int pairs, int blocks) {
+    if (pairs < 0 || blocks <= 0) return GB_EINVAL;
+    sc_product_kernel<false, false><<<blocks, RED_THREADS, 0, stream()>>>(eq, bh, p0, p1, p2, (size_t)pairs);
+    return check_launch("basefold_sumcheck_product_gl_ffi");
+}
+int basefold_sumcheck_product_mixed_ffi(const uint64_t* eq, const uint64_t* bh, uint64_t* p0, uint64_t* p1,
+                                        uint64_t* p2, int pairs, int blocks) {
+    if (pairs < 0 || blocks <= 0) return GB_EINVAL;
+    sc_product_kernel<true, false><<<blocks, RED_THREADS, 0, stream()>>>(eq, bh, p0, p1, p2, (size_t)pairs);
+    return check_launch("basefold_sumcheck_product_mixed_ffi");
+}
+int basefold_sumcheck_product_ext2_ffi(const uint64_t* eq, const uint64_t* bh, uint64_t* p0, uint64_t* p1,
+                                       uint64_t* p2, int pairs, int blocks) {
+    if (pairs < 0 || blocks <= 0) return GB_EINVAL;
+    sc_product_kernel<true, true><<<blocks, RED_THREADS, 0, stream()>>>(eq, bh, p0, p1, p2, (size_t)pairs);
+    return check_launch("basefold_sumcheck_product_ext2_ffi");
+}
+
+int basefold_sumcheck_eval_gl_ffi(const uint64_t* d, uint64_t ch, uint64_t* out, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    sc_eval_kernel<0><<<grid_for(pairs, 256), 256, 0, stream()>>>(d, ch, 0, out, pairs);
+    return check_launch("basefold_sumcheck_eval_gl_ffi");
+}
+int basefold_sumcheck_eval_mixed_ffi(const uint64_t* d, uint64_t c0, uint64_t c1, uint64_t* out, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    sc_eval_kernel<1><<<grid_for(pairs, 256), 256, 0, stream()>>>(d, c0, c1, out, pairs);
+    return check_launch("basefold_sumcheck_eval_mixed_ffi");
+}
+int basefold_sumcheck_eval_ext2_ffi(const uint64_t* d, uint64_t c0, uint64_t c1, uint64_t* out, int pairs) {
+    if (pairs < 0) return GB_EINVAL;
+    if (!pairs) return GB_OK;
+    sc_eval_kernel<2><<<grid_for(pairs, 256), 256, 0, stream()>>>(d, c0, c1, out, pairs);
+    return check_launch("basefold_sumcheck_eval_ext2_ffi");
+}
+
+int fused_sumcheck_round_ext2_ffi(const uint64_t* eq_in, const uint64_t* bh_in, uint64_t c0, uint64_t c1,
+                                  uint64_t* eq_out, uint64_t* bh_out, uint64_t* p0, uint64_t* p1, uint64_t* p2, int pairs,
+                                  int blocks) {
+    if (pairs < 0 || blocks <= 0) return GB_EINVAL;
+    sc_fused_round_ref_kernel<<<blocks, RED_THREADS, 0, stream()>>>(eq_in, bh_in, c0, c1, eq_out, bh_out, p0, p1, p2,
+                                                                    (size_t)pairs);
+    return check_launch("fused_sumcheck_round_ext2_ffi");
+}
+
+int basefold_dot_product_gl_ffi(const uint64_t* a, const uint64_t* b, uint64_t* partial, int n, int blocks) {
+    if (n < 0 || blocks <= 0) return GB_EINVAL;
+    dot_product_kernel<false><<<blocks, RED_THREADS, 0, stream()>>>(a, b, partial, (size_t)n);
+    return check_launch("basefold_dot_product_gl_ffi");
+}
+int basefold_dot_product_mixed_ffi(const uint64_t* a, const uint64_t* b, uint64_t* partial, int n, int blocks) {
+    if (n < 0 || blocks <= 0) return GB_EINVAL;
+    dot_product_kernel<true><<<blocks, RED_THREADS, 0, stream()>>>(a, b, partial, (size_t)n);
+    return check_launch("basefold_dot_product_mixed_ffi");
+}
+
+// ---------------------------------------------------------------- gb_* drivers
+int gb_basefold_table_create(int num_vars, int log_rate, int num_rounds, uint64_t seed, void** handle) {
+    if (!handle) return GB_EINVAL;
+    BfTable* t = new BfTable();
+    int rc = table_create(num_vars, log_rate, num_rounds, seed, t);
+    if (rc) {
+        if (t->d_entries) cudaFree(t->d_entries);
+        delete t;
+        return rc;
+    }
+    *handle = t;
+    return GB_OK;
+}
+
+int gb_basefold_table_destroy(void* handle) {
+    BfTable* t = (BfTable*)handle;
+    if (!t) return GB_OK;
+    if (t->d_entries) cudaFree(t->d_entries);
+    delete t;
+    return GB_OK;
+}
+
+int gb_basefold_table_info(void* handle, uint64_t** d_entries, uint64_t* h_level_offsets) {
+    BfTable* t = (BfTable*)handle;
+    if (!t) return GB_EINVAL;
+    if (d_entries) *d_entries = t->d_entries;
+    if (h_level_offsets)
+        for (int i = 0; i < t->num_rounds; i++) h_level_offsets[i] = t->level_offsets[i];
+    return GB_OK;
+}
+
+int gb_basefold_commit(const uint64_t* d_evals, const uint64_t* h_evals, int num_vars, int log_rate, void** handle,
+                       uint64_t root[4]) {
+    if (!handle || (!d_evals == !h_evals) || num_vars < 0 || log_rate < 0 || num_vars + log_rate < 1 ||
+        num_vars + log_rate > 40)
+        return GB_EINVAL;
+    cudaStream_t s = stream();
+    size_t N = (size_t)1 << num_vars;
+    u64* tmp = nullptr;
+    const u64* src = d_evals;
+    if (h_evals) {
+        GB_CUDA_TRY(cudaMallocAsync(&tmp, N * 8, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(tmp, h_evals, N * 8, cudaMemcpyHostToDevice, s));
+        src = tmp;
+    }
+    BfCommitment* c = new BfCommitment();
+    int rc = commit_device(src, num_vars, log_rate, c);
+    if (tmp) cudaFreeAsync(tmp, s);
+    if (rc) {
+        commitment_free(c);
+        delete c;
+        return rc;
+    }
+    if (root)
+        for (int k = 0; k < 4; k++) root[k] = c->root[k];
+    *handle = c;
+    return GB_OK;
+}
+
+int gb_basefold_commitment_destroy(void* handle) {
+    BfCommitment* c = (BfCommitment*)handle;
+    if (!c) return GB_OK;
+    commitment_free(c);
+    delete c;
+    return GB_OK;
+}
+
+int gb_basefold_commitment_info(void* handle, uint64_t** d_codeword, uint64_t** d_tree, uint64_t** d_evals,
+                                uint64_t root[4]) {
+    BfCommitment* c = (BfCommitment*)handle;
+    if (!c) return GB_EINVAL;
+    if (d_codeword) *d_codeword = c->d_codeword;
+    if (d_tree) *d_tree = c->d_tree;
+    if (d_evals) *d_evals = c->d_evals;
+    if (root)
+        for (int k = 0; k < 4; k++) root[k] = c->root[k];
+    return GB_OK;
+}
+
+size_t gb_basefold_proof_len(int num_vars, int log_rate, int num_queries) {
+    return proof_len(num_vars, log_rate, num_queries);
+}
+
+int gb_basefold_open_ext2(void* commitment, void* table, const uint64_t* h_point, gb_transcript* t, int num_queries,
+                          uint64_t* h_proof) {
+    if (!commitment || !table || !h_point || !t || !h_proof) return GB_EINVAL;
+    return open_ext2((BfCommitment*)commitment, (BfTable*)table, h_point, t, num_queries, h_proof);
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// Poseidon2 Merkle trees on the device.
+//
+// Layout (goldilocks-cuda-rs/src/merkle.rs:1-10): one buffer of (2L - 1) digests of
+// 4 u64, layers packed leaves first, root last.  Leaves hash pairs of codeword
+// elements: P2(a, b, 0^6)[0..4] for base-field codewords, P2(a.c0, a.c1, b.c0,
+// b.c1, 0^4)[0..4] for Ext2 codewords (goldilocks-cuda-rs/cuda/wrapper.cu:1604-1650);
+// parents are P2(left || right)[0..4].
+#pragma once
+#include "common.cuh"
+#include "poseidon2.cuh"
+
+namespace gb {
+
+// Number of u64 words before layer `level` of a tree with `leaves` leaves.
+__host__ __device__ inline size_t tree_layer_offset(size_t leaves, int level) {
+    size_t off = 0, sz = leaves;
+    for (int l = 0; l < level; l++) {
+        off += sz;
+        sz >>= 1;
+    }
+    return off * 4;
+}
+
+__host__ __device__ inline int tree_depth(size_t leaves) {
+    int d = 0;
+    while (((size_t)1 << d) < leaves) d++;
+    return d;
+}
+
+__device__ __forceinline__ void st_digest(u64* p, const u64* s) {
+    ulonglong2 a, b;
+    a.x = s[0];
+    a.y = s[1];
+    b.x = s[2];
+    b.y = s[3];
+    reinterpret_cast<ulonglong2*>(p)[0] = a;
+    reinterpret_cast<ulonglong2*>(p)[1] = b;
+}
+__device__ __forceinline__ void ld_digest(const u64* p, u64* s) {
+    ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2*>(p));
+    ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2*>(p) + 1);
+    s[0] = a.x;
+    s[1] = a.y;
+    s[2] = b.x;
+    s[3] = b.y;
+}
+
+// Host-side tree builders (merkle.cu).  `leaves_done`: leaf digests are already in
+// layer 0.  All launches on gb::stream(); no synchronisation.
+int merkle_build_from_leaves(u64* tree, size_t leaves);
+int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves);
+int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves);
+// Tree over a base-field codeword made of 2^copies identical blocks: hashes one
+// block's subtree, replicates it, and finishes the top `copies` levels.
+int merkle_tree_gl_replicated(const u64* cw, u64* tree, size_t leaves, int copies_log);
+
+}  // namespace gb

@@ -12,38 +12,60 @@
 
 namespace gb {
 
+// The tables are written once, as macros, and expanded into a host table (P2Const)
+// and into device function-local tables that fold to immediates when unrolled.
+#define GB_P2_RC_EXT \
+    { \
+    {0xdd5743e7f2a5a5d9ull, 0xcb3a864e58ada44bull, 0xd5a3726889dedc0dull, 0x79365a7f967583c1ull, \
+    0xb7820c177b0a3c30ull, 0x68a60479943b7240ull, 0x0a22eeab67b97c41ull, 0xbee9d90e037fa7d4ull}, \
+    {0xf1dda5b9259dfcb4ull, 0x27515210be112d59ull, 0x654a4db8f15f6c3aull, 0x5a9bfff8c29db0c4ull, \
+    0xb72f2628c95a885bull, 0xffcb54fc166beaddull, 0xe32f91d59c463772ull, 0x9e0ff2a9bbea79dbull}, \
+    {0xce57d6245ddca6b2ull, 0xb1fc8d402bba1eb1ull, 0x64df974fb666d528ull, 0x59e4e5b237e52e78ull, \
+    0x5e255e2742caa8fcull, 0xc4a17304e330ef9aull, 0x60e3a513cdd9f0b1ull, 0xbf29a6a5a0c9c8baull}, \
+    {0xcea721cce82fb11bull, 0xe5b55eb8098ece81ull, 0x4ec66bfb89f7c380ull, 0xc33be12b6ef7e4faull, \
+    0xa41b5f5b84c57d7dull, 0xb526206b2138a936ull, 0x9f7a5ac62f16eb4eull, 0x7de77f405f683aa5ull}, \
+    {0x014ef1197d341346ull, 0x9725e20825d07394ull, 0xc8ff2a22516f3604ull, 0xde1b51f7cf493493ull, \
+    0xa7e3af1a53eadb78ull, 0x9b7b7ee0ddf9f229ull, 0xf0a460f2dc649e7dull, 0xdc4448d02c2cb823ull}, \
+    {0xaa62c88e0b294011ull, 0x058eb9d810ce9f74ull, 0x4e3d7a5403566d24ull, 0xe8ae66da2f8b7a63ull, \
+    0x3fdad3b08dae2e0bull, 0xec81e61303dd409bull, 0x3cbaa1cd35d31fc4ull, 0x847f7806eec88ffaull}, \
+    {0x98ae09a325893803ull, 0xf8a6475077968838ull, 0xdf55b7419443de5bull, 0xdbe15699e696ca70ull, \
+    0x8e54a27d8db00424ull, 0x7679a45cd9d1e12aull, 0x2844f52be73e0e2full, 0xd41f8eb31ada34f8ull}, \
+    {0xe9dd318bae1f3961ull, 0xf7462137299efe1aull, 0x6dbbe06779e1d573ull, 0xfe35b05cbe707632ull, \
+    0x5d8896b12654fd8cull, 0x6f96ef47c32d4ae2ull, 0xb0caa221dbbfc0daull, 0x0bc2a5bf1f238d3full}, \
+    }
+#define GB_P2_RC_INT \
+    { \
+    0x488897d85ff51f56ull, 0x1140737ccb162218ull, 0xa7eeb9215866ed35ull, 0x9bd2976fee49fcc9ull, \
+    0xc0c8f0de580a3fccull, 0x4fb2dae6ee8fc793ull, 0x343a89f35f37395bull, 0x223b525a77ca72c8ull, \
+    0x56ccb62574aaa918ull, 0xc4d507d8027af9edull, 0xa080673cf0b7e95cull, 0xf0184884eb70dcf8ull, \
+    0x044f10b0cb3d5c69ull, 0xe9e3f7993938f186ull, 0x1b761c80e772f459ull, 0x606cec607a1b5facull, \
+    0x14a0c2e1d45f03cdull, 0x4eace8855398574full, 0xf905ca7103eff3e6ull, 0xf8c8f8d20862c059ull, \
+    0xb524fe8bdd678e5aull, 0xfbb7865901a1ec41ull, \
+    }
+#define GB_P2_DIAG \
+    { \
+    0xa98811a1fed4e3a5ull, 0x1cc48b54f377e2a0ull, 0xe40cd4f6c5609a26ull, 0x11de79ebca97a4a3ull, \
+    0x9177c73d8b7e929cull, 0x2a6fe8085797e791ull, 0x3de6e93329f8d5adull, 0x3f7af9125da962feull, \
+    }
+
 struct P2Const {
-    static constexpr u64 ext[8][8] = {
-        {0xdd5743e7f2a5a5d9ull, 0xcb3a864e58ada44bull, 0xd5a3726889dedc0dull, 0x79365a7f967583c1ull,
-         0xb7820c177b0a3c30ull, 0x68a60479943b7240ull, 0x0a22eeab67b97c41ull, 0xbee9d90e037fa7d4ull},
-        {0xf1dda5b9259dfcb4ull, 0x27515210be112d59ull, 0x654a4db8f15f6c3aull, 0x5a9bfff8c29db0c4ull,
-         0xb72f2628c95a885bull, 0xffcb54fc166beaddull, 0xe32f91d59c463772ull, 0x9e0ff2a9bbea79dbull},
-        {0xce57d6245ddca6b2ull, 0xb1fc8d402bba1eb1ull, 0x64df974fb666d528ull, 0x59e4e5b237e52e78ull,
-         0x5e255e2742caa8fcull, 0xc4a17304e330ef9aull, 0x60e3a513cdd9f0b1ull, 0xbf29a6a5a0c9c8baull},
-        {0xcea721cce82fb11bull, 0xe5b55eb8098ece81ull, 0x4ec66bfb89f7c380ull, 0xc33be12b6ef7e4faull,
-         0xa41b5f5b84c57d7dull, 0xb526206b2138a936ull, 0x9f7a5ac62f16eb4eull, 0x7de77f405f683aa5ull},
-        {0x014ef1197d341346ull, 0x9725e20825d07394ull, 0xc8ff2a22516f3604ull, 0xde1b51f7cf493493ull,
-         0xa7e3af1a53eadb78ull, 0x9b7b7ee0ddf9f229ull, 0xf0a460f2dc649e7dull, 0xdc4448d02c2cb823ull},
-        {0xaa62c88e0b294011ull, 0x058eb9d810ce9f74ull, 0x4e3d7a5403566d24ull, 0xe8ae66da2f8b7a63ull,
-         0x3fdad3b08dae2e0bull, 0xec81e61303dd409bull, 0x3cbaa1cd35d31fc4ull, 0x847f7806eec88ffaull},
-        {0x98ae09a325893803ull, 0xf8a6475077968838ull, 0xdf55b7419443de5bull, 0xdbe15699e696ca70ull,
-         0x8e54a27d8db00424ull, 0x7679a45cd9d1e12aull, 0x2844f52be73e0e2full, 0xd41f8eb31ada34f8ull},
-        {0xe9dd318bae1f3961ull, 0xf7462137299efe1aull, 0x6dbbe06779e1d573ull, 0xfe35b05cbe707632ull,
-         0x5d8896b12654fd8cull, 0x6f96ef47c32d4ae2ull, 0xb0caa221dbbfc0daull, 0x0bc2a5bf1f238d3full},
-    };
-    static constexpr u64 inner[22] = {
-        0x488897d85ff51f56ull, 0x1140737ccb162218ull, 0xa7eeb9215866ed35ull, 0x9bd2976fee49fcc9ull,
-        0xc0c8f0de580a3fccull, 0x4fb2dae6ee8fc793ull, 0x343a89f35f37395bull, 0x223b525a77ca72c8ull,
-        0x56ccb62574aaa918ull, 0xc4d507d8027af9edull, 0xa080673cf0b7e95cull, 0xf0184884eb70dcf8ull,
-        0x044f10b0cb3d5c69ull, 0xe9e3f7993938f186ull, 0x1b761c80e772f459ull, 0x606cec607a1b5facull,
-        0x14a0c2e1d45f03cdull, 0x4eace8855398574full, 0xf905ca7103eff3e6ull, 0xf8c8f8d20862c059ull,
-        0xb524fe8bdd678e5aull, 0xfbb7865901a1ec41ull,
-    };
-    static constexpr u64 diag[8] = {
-        0xa98811a1fed4e3a5ull, 0x1cc48b54f377e2a0ull, 0xe40cd4f6c5609a26ull, 0x11de79ebca97a4a3ull,
-        0x9177c73d8b7e929cull, 0x2a6fe8085797e791ull, 0x3de6e93329f8d5adull, 0x3f7af9125da962feull,
-    };
+    static constexpr u64 ext[8][8] = GB_P2_RC_EXT;
+    static constexpr u64 inner[22] = GB_P2_RC_INT;
+    static constexpr u64 diag[8] = GB_P2_DIAG;
 };
+
+__device__ __forceinline__ u64 p2_rc_ext(int r, int i) {
+    constexpr u64 t[8][8] = GB_P2_RC_EXT;
+    return t[r][i];
+}
+__device__ __forceinline__ u64 p2_rc_int(int r) {
+    constexpr u64 t[22] = GB_P2_RC_INT;
+    return t[r];
+}
+__device__ __forceinline__ u64 p2_diag(int i) {
+    constexpr u64 t[8] = GB_P2_DIAG;
+    return t[i];
+}
 
 __device__ __forceinline__ u64 p2_sbox(u64 x) {
     u64 x2 = gl_sqr(x);
@@ -76,20 +98,20 @@ __device__ __forceinline__ void p2_permute(u64* s) {
 #pragma unroll
     for (int r = 0; r < 4; r++) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) s[i] = p2_sbox(gl_add(s[i], P2Const::ext[r][i]));
+        for (int i = 0; i < 8; i++) s[i] = p2_sbox(gl_add(s[i], p2_rc_ext(r, i)));
         p2_external_linear(s);
     }
 #pragma unroll
     for (int r = 0; r < 22; r++) {
-        s[0] = p2_sbox(gl_add(s[0], P2Const::inner[r]));
+        s[0] = p2_sbox(gl_add(s[0], p2_rc_int(r)));
         u64 sum = gl_add(gl_add(gl_add(s[0], s[1]), gl_add(s[2], s[3])), gl_add(gl_add(s[4], s[5]), gl_add(s[6], s[7])));
 #pragma unroll
-        for (int i = 0; i < 8; i++) s[i] = gl_add(gl_mul(s[i], P2Const::diag[i]), sum);
+        for (int i = 0; i < 8; i++) s[i] = gl_add(gl_mul(s[i], p2_diag(i)), sum);
     }
 #pragma unroll
     for (int r = 4; r < 8; r++) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) s[i] = p2_sbox(gl_add(s[i], P2Const::ext[r][i]));
+        for (int i = 0; i < 8; i++) s[i] = p2_sbox(gl_add(s[i], p2_rc_ext(r, i)));
         p2_external_linear(s);
     }
 }

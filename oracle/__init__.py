@@ -67,6 +67,7 @@ def lib():
             ("or_sumcheck_verify_ext2", i32, [vp, i32, i32, _u64p, _u64p, _u64p]),
             ("or_eq_table_base", None, [_u64p, i32, _u64p]),
             ("or_eq_table_ext2", None, [_u64p, i32, _u64p]),
+            ("or_ml_eval_ext2", None, [_u64p, i32, _u64p, _u64p]),
             ("or_basefold_table_entries", sz, [i32, i32, i32]),
             ("or_basefold_table_generate", None, [i32, i32, i32, u64, _u64p, _u64p]),
             ("or_bhc_interpolate", None, [_u64p, i32, _u64p, _u64p]),
@@ -190,6 +191,14 @@ def eq_table_ext2(point):
     n = point.shape[0]
     out = np.zeros((1 << n, 2), np.uint64)
     lib().or_eq_table_ext2(point.reshape(-1), n, out.reshape(-1))
+    return out
+
+
+def ml_eval_ext2(evals, point):
+    evals = _a(evals)
+    n = evals.size.bit_length() - 1
+    out = np.zeros(2, np.uint64)
+    lib().or_ml_eval_ext2(evals, n, _a(point).reshape(-1), out)
     return out
 
 

@@ -464,6 +464,21 @@ void or_eq_table_ext2(const u64 *r, int n, u64 *out) {
     free(rr);
 }
 
+/* multilinear extension of base-field evals at an Ext2 point: sum_x evals[x] eq(r, x) */
+void or_ml_eval_ext2(const u64 *evals, int n, const u64 *point, u64 out[2]) {
+    size_t N = (size_t)1 << n;
+    e2 *eq = (e2 *)malloc(sizeof(e2) * N);
+    e2 *rr = (e2 *)calloc(n > 0 ? n : 1, sizeof(e2));
+    for (int i = 0; i < n; i++) rr[i] = e2_mk(point[2 * i], point[2 * i + 1]);
+    eq_table_ext2(rr, n, eq);
+    e2 acc = e2_base(0);
+    for (size_t k = 0; k < N; k++) acc = e2_add(acc, e2_scale(eq[k], evals[k]));
+    out[0] = acc.c0;
+    out[1] = acc.c1;
+    free(eq);
+    free(rr);
+}
+
 /* ======================================================================
  * Basefold
  * ====================================================================== */

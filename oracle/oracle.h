@@ -80,6 +80,7 @@ int or_sumcheck_verify_ext2(or_transcript *t, int n, int d, const uint64_t claim
 /* ---- eq / Lagrange basis (zk-torch-3/src/poly/mod.rs:106-161) ---- */
 void or_eq_table_base(const uint64_t *r, int n, uint64_t *out);
 void or_eq_table_ext2(const uint64_t *r, int n, uint64_t *out);
+void or_ml_eval_ext2(const uint64_t *evals, int n, const uint64_t *point, uint64_t out[2]);
 
 /* ---- Basefold ---- */
 /* BasefoldTable::generate (goldilocks-cuda-rs/src/basefold.rs:281-321).
