@@ -91,42 +91,67 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+SAMPLE_VARS = 14  # bounded CPU sample: 2^14-evaluation proofs, time scaled by 2^(22-14)
+
+
+def _cpu_proof(seed):
+    """One commit + open_ext2 of a 2^SAMPLE_VARS polynomial by the CPU restatement
+    of the reference prover (runs in a spawned worker)."""
+    import oracle as O
+    rng = np.random.default_rng(seed)
+    ev = rng.integers(0, P, size=1 << SAMPLE_VARS, dtype=np.uint64)
+    pt = rng.integers(0, P, size=(SAMPLE_VARS, 2), dtype=np.uint64)
+    table = O.basefold_table(SAMPLE_VARS, LOG_RATE, SAMPLE_VARS, TABLE_SEED)
+    t0 = time.perf_counter()
+    c = O.basefold_commit(ev, LOG_RATE)
+    O.basefold_open_ext2(c, pt, table, O.Transcript(b"bf-open"), QUERIES)
+    return time.perf_counter() - t0
+
+
+def cpu_throughput(steps, warmup=0):
+    """Proofs/s of the CPU restatement with one proof per host core in parallel (the
+    reference runs its CPU openings one per thread, many in parallel), scaled from the
+    2^14 sample to the 2^22 workload by the work ratio."""
+    import multiprocessing as mp
+    import oracle as O
+    O.build(ref=False)
+    cores = os.cpu_count() or 1
+    scale = float(1 << (N_VARS - SAMPLE_VARS))
+    rates = []
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            pool.map(_cpu_proof, range(i * cores, (i + 1) * cores))
+            wall = time.perf_counter() - t0
+            if i >= warmup:
+                rates.append(cores / (wall * scale))
+    value = statistics.mean(rates)
+    return value, cores, (f"{steps} x {cores} parallel proofs of 2^{SAMPLE_VARS} evaluations "
+                          f"(C restatement, one per core), time scaled x{int(scale)} to 2^22")
+
+
 def run_reference(args):
-    """CPU restatement of the reference prover on a bounded sample (the reference's Rust
-    crates cannot be built: no cargo/rustc here or on the GPU machine)."""
+    """The reference's CPU prover path, restated in C (the reference is Rust and no Rust
+    toolchain exists here or on the GPU machine), on all host cores.  Rank 0 only."""
     rank, world = env_rank()
     if rank != 0:
         return
-    import oracle as O
-    O.build(ref=False)
-    n_s = 14  # bounded sample: 2^14-evaluation proofs, scaled to the 2^22 workload by work ratio
-    rng = np.random.default_rng(7)
-    ev = rng.integers(0, P, size=1 << n_s, dtype=np.uint64)
-    pt = rng.integers(0, P, size=(n_s, 2), dtype=np.uint64)
-    table = O.basefold_table(n_s, LOG_RATE, n_s, TABLE_SEED)
-    times = []
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        c = O.basefold_commit(ev, LOG_RATE)
-        O.basefold_open_ext2(c, pt, table, O.Transcript(b"bf-open"), QUERIES)
-        dt = time.perf_counter() - t0
-        if i >= args.warmup:
-            times.append(dt)
-    # work scales ~linearly with 2^n (permutations, passes); the sample proof is 2^(22-14) smaller
-    scale = float(1 << (N_VARS - n_s))
-    sec_per_proof = statistics.mean(times) * scale
-    value = 1.0 / sec_per_proof
+    value, cores, sample = cpu_throughput(args.steps, min(args.warmup, 1))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_proof * 1e3, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic",
-        "config": {"workload": "basefold commit+open_ext2, 2^22 evals, rate 1/2, 34 queries", "num_vars": N_VARS,
-                   "log_rate": LOG_RATE, "num_queries": QUERIES},
-        "cpu_baseline": {"value": value, "unit": "proofs/s", "cores": 1, "kind": "port",
-                         "sample": f"2^{n_s}-evaluation proofs x{args.steps}, time scaled x{int(scale)} to 2^22"},
+        "config": {"workload": f"basefold commit+open_ext2, 2^{N_VARS} evals, rate 1/2, {QUERIES} queries",
+                   "num_vars": N_VARS, "log_rate": LOG_RATE, "num_queries": QUERIES, "table_seed": TABLE_SEED},
+        "cpu_baseline": {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "proofs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def cpu_baseline_sample():
+    value, cores, sample = cpu_throughput(1, 0)
+    return {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port", "sample": sample}
 
 
 def main():
@@ -136,6 +161,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--num-vars", type=int, default=N_VARS)
+    ap.add_argument("--no-extras", action="store_true", help="skip the roofline probes and the CPU baseline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -146,7 +172,7 @@ def main():
     from morpheus_gb300 import _native as Nn
     from morpheus_gb300.basefold import BasefoldCommitment, BasefoldTable
     from morpheus_gb300.memory import DeviceBuffer
-    from morpheus_gb300.sumcheck import Transcript
+    from morpheus_gb300.sumcheck import GpuLinearSumcheckProver, Transcript
 
     rank, world = env_rank()
     dist = world > 1
@@ -158,6 +184,14 @@ def main():
     L = Nn.lib()
     stream = torch.cuda.Stream()
     L.gb_set_stream(ctypes.c_void_p(stream.cuda_stream))
+
+    def ev_time(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
 
     n = args.num_vars
     rng = np.random.default_rng(1234 + rank)
@@ -180,19 +214,16 @@ def main():
 
     times = []
     with ClockSampler() as clk:
+        l0 = L.gb_launch_count()
         for _ in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step_device()
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
+            times.append(ev_time(step_device))
+        launches = (L.gb_launch_count() - l0) // max(1, args.steps)
         torch.cuda.synchronize()
         if dist:
             tdist.barrier()
-        # e2e: pinned host evaluations through the C ABI, proof back to host
+        # e2e: pinned host evaluations through the C ABI, proof back to host memory
         ev_pinned = torch.from_numpy(ev_host.view(np.int64)).pin_memory()
         hptr = ev_pinned.data_ptr()
         proof_len = L.gb_basefold_proof_len(n, LOG_RATE, QUERIES)
@@ -217,6 +248,61 @@ def main():
     ms_max = float(tmax.item())
     value = world * 1000.0 / ms_max
     e2e_ms = statistics.mean(e2e_times) * 1e3
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # --- integer-pipe roofline of the dominant kernel (Poseidon2 Merkle layer over 2^21 parents)
+        half = 1 << 21
+        layer_in = DeviceBuffer(8 * half)
+        layer_out = DeviceBuffer(4 * half)
+        Nn.check(L.poseidon2_merkle_layer_ffi(layer_in.ptr, layer_out.ptr, half), "layer")
+        lay_ms = min(ev_time(lambda: L.poseidon2_merkle_layer_ffi(layer_in.ptr, layer_out.ptr, half)) for _ in range(5))
+        mulmods_per_perm = 520  # 8 external x 8 lanes x 4 + 22 internal x (4 + 8)
+        achieved = half * mulmods_per_perm / (lay_ms * 1e-3) / 1e9
+        blocks, iters = Nn.lib().gb_device_sm_count() * 8, 2048
+        probe = DeviceBuffer(blocks * 256)
+        Nn.check(L.gb_mulmod_probe(probe.ptr, blocks, iters), "probe")
+        pr_ms = min(ev_time(lambda: L.gb_mulmod_probe(probe.ptr, blocks, iters)) for _ in range(5))
+        peak = blocks * 256 * 8 * iters / (pr_ms * 1e-3) / 1e9
+        extras["roofline"] = {
+            "kernel": "merkle_level_kernel (Poseidon2 width 8, one permutation per thread)",
+            "bound": "int", "achieved": achieved, "peak": peak, "unit": "Gmulmod/s", "frac": achieved / peak,
+            "peak_source": "in-run probe: independent Goldilocks multiplication chains (gb_mulmod_probe); "
+                           "neither hbm nor tensor bounds this kernel",
+            "perms_per_s": half / (lay_ms * 1e-3), "launch_ms": lay_ms, "traffic": None,
+        }
+        # --- HBM roofline of the fused sumcheck fold round (2 polys x 2^24 Ext2 -> 2 x 2^23 Ext2)
+        hbm_peak, src = measured_peaks()
+        nf = 24
+        src_buf = DeviceBuffer(2 * 2 * (1 << nf))
+        dst_buf = DeviceBuffer(2 * 2 * (1 << (nf - 1)))
+        msg = DeviceBuffer(16)
+        work = DeviceBuffer(L.gb_sumcheck_round_workspace_words())
+        work_np = np.zeros(work.len, np.uint64)
+        Nn.check(L.cuda_memcpy_htod(work.ptr, work_np.ctypes.data, work.nbytes), "zero")
+        pairs_out = 1 << (nf - 2)
+        fr = lambda: L.gb_sumcheck_fold_round_ext2(src_buf.ptr, 0, 1 << nf, dst_buf.ptr, 1 << (nf - 1), 2,
+                                                   pairs_out, 5, 7, msg.ptr, work.ptr)
+        Nn.check(fr(), "fold round")
+        fr_ms = min(ev_time(fr) for _ in range(5))
+        fbytes = 2 * (1 << nf) * 16 + 2 * (1 << (nf - 1)) * 16
+        extras["roofline_hbm"] = {
+            "kernel": "sc_fold_round_e2_kernel (fold 2 x 2^24 Ext2 + next round message)",
+            "bound": "hbm", "achieved": fbytes / (fr_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+            "frac": fbytes / (fr_ms * 1e-3) / 1e9 / hbm_peak, "peak_source": src, "bytes_per_launch": fbytes,
+            "launch_ms": fr_ms,
+        }
+        # --- sumcheck Melem/s at the 2 x 2^20 shape (whole proof, host transcript)
+        polys = DeviceBuffer.from_numpy(rng.integers(0, P, size=2 << 20, dtype=np.uint64))
+
+        def sc():
+            t = Transcript(b"bench")
+            GpuLinearSumcheckProver(20, 2, t).prove((polys, 2), t)
+        sc()
+        sc_ms = statistics.median(ev_time(sc) for _ in range(5))
+        extras["sumcheck_2x2^20"] = {"ms_per_proof": sc_ms, "melem_per_s": 2 * (1 << 20) / (sc_ms * 1e-3) / 1e6}
+        extras["cpu_baseline"] = cpu_baseline_sample()
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": world, "steps": args.steps,
@@ -227,9 +313,11 @@ def main():
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
             "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "proofs/s", "h2d_bytes_per_step": 8 << n,
                     "d2h_bytes_per_step": 8 * int(proof_len)},
+            "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "step_ms_all": [round(t, 3) for t in times],
         }
+        line.update(extras)
         print(json.dumps(line))
     if dist:
         tdist.destroy_process_group()

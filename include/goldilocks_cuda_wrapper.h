@@ -142,6 +142,12 @@ void *gb_get_stream(void);
 /* Last error message of the calling thread ("" if none). */
 const char *gb_last_error(void);
 int gb_device_sm_count(void);
+/* Number of kernels this library has launched in the process (all threads). */
+unsigned long long gb_launch_count(void);
+/* Measurement probe: blocks x 256 threads, each running 8 independent chains of `iters`
+ * Goldilocks multiplications; d_out receives blocks*256 words.  Times the arithmetic
+ * ceiling that the Poseidon2 kernels are compared against.  Launch only. */
+int gb_mulmod_probe(uint64_t *d_out, int blocks, int iters);
 
 /* Transcript helpers (host): new(label), append_u64(label), challenge_ext2(label). */
 void gb_transcript_new(gb_transcript *t, const char *label);
@@ -157,6 +163,15 @@ void gb_transcript_challenge_ext2(gb_transcript *t, const char *label, uint64_t 
  * h_final_eval[2].  Synchronising. */
 int gb_sumcheck_prove_ext2(gb_transcript *t, int n, int d, const uint64_t *d_polys, const uint64_t *h_polys,
                            uint64_t *h_msgs, uint64_t *h_challenges, uint64_t *h_finals, uint64_t *h_final_eval);
+/* One fused round as a device building block: fold d polynomials (base-field input when
+ * in_base, element stride in_stride) with the Ext2 challenge (r0, r1) into d_out (Ext2,
+ * stride out_stride), producing pairs_out output pairs per polynomial, and write the next
+ * round's d+1 Ext2 message values (canonical) to d_msg.  d_work: zeroed workspace of
+ * gb_sumcheck_round_workspace_words() words (left zeroed again).  Launch only. */
+size_t gb_sumcheck_round_workspace_words(void);
+int gb_sumcheck_fold_round_ext2(const uint64_t *d_in, int in_base, size_t in_stride, uint64_t *d_out,
+                                size_t out_stride, int d, size_t pairs_out, uint64_t r0, uint64_t r1,
+                                uint64_t *d_msg, uint64_t *d_work);
 /* LinearSumcheckProver::{new, prove} semantics (zk-torch-3/src/sumcheck/linear_prover.rs:23-63):
  * base-field messages and challenges.  h_msgs[n][d+1], h_challenges[n], h_finals[d], h_final_eval[1]. */
 int gb_sumcheck_prove_base(gb_transcript *t, int n, int d, const uint64_t *d_polys, const uint64_t *h_polys,

@@ -61,12 +61,16 @@ SIGNATURES = {
     "gb_get_stream": (vp, []),
     "gb_last_error": (ctypes.c_char_p, []),
     "gb_device_sm_count": (i32, []),
+    "gb_launch_count": (ctypes.c_ulonglong, []),
+    "gb_mulmod_probe": (i32, [vp, i32, i32]),
     "gb_transcript_new": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p]),
     "gb_transcript_append_u64": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64]),
     "gb_transcript_append_ext2": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64p]),
     "gb_transcript_challenge_ext2": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64p]),
     "gb_sumcheck_prove_ext2": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
     "gb_sumcheck_prove_base": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
+    "gb_sumcheck_round_workspace_words": (sz, []),
+    "gb_sumcheck_fold_round_ext2": (i32, [vp, i32, sz, vp, sz, i32, sz, u64, u64, vp, vp]),
     "poseidon2_hash_batch_ffi": (i32, [vp, vp, i32]),
     "poseidon2_compress_batch_ffi": (i32, [vp, vp, vp, i32]),
     "poseidon2_merkle_layer_ffi": (i32, [vp, vp, i32]),

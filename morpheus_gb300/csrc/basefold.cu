@@ -407,6 +407,40 @@ __global__ void __launch_bounds__(128) fold_hash_leaves_kernel(const u64* __rest
     st_digest(tree + 4 * i, s);
 }
 
+// Same with 8 lanes per leaf (latency-bound rounds, see MK_COOP_BELOW): every lane of a
+// group folds both elements, lane l takes state element l, lanes 0..3 store.
+template <bool BASE_IN>
+__global__ void __launch_bounds__(256) fold_hash_leaves_coop_kernel(const u64* __restrict__ cw,
+                                                                    const u64* __restrict__ tab, u64 c0, u64 c1,
+                                                                    u64* __restrict__ folded, u64* __restrict__ tree,
+                                                                    size_t leaves) {
+    size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 3;
+    const int l = threadIdx.x & 7;
+    const bool live = g < leaves;
+    const size_t i = live ? g : 0;
+    ulonglong2 t0 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i);
+    ulonglong2 t1 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i + 1);
+    e2 f0, f1;
+    if (BASE_IN) {
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i);
+        ulonglong2 u = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i + 1);
+        u64 dw0 = gl_mul(gl_sub(v.y, v.x), t0.y), dw1 = gl_mul(gl_sub(u.y, u.x), t1.y);
+        f0 = e2_make(gl_add(v.x, gl_mul(gl_sub(c0, t0.x), dw0)), gl_mul(c1, dw0));
+        f1 = e2_make(gl_add(u.x, gl_mul(gl_sub(c0, t1.x), dw1)), gl_mul(c1, dw1));
+    } else {
+        const u64* p = cw + 8 * i;
+        e2 a0 = e2_ld(p), a1 = e2_ld(p + 2), b0 = e2_ld(p + 4), b1 = e2_ld(p + 6);
+        e2 dw0 = e2_mul_base(e2_sub(a1, a0), t0.y), dw1 = e2_mul_base(e2_sub(b1, b0), t1.y);
+        f0 = e2_add(a0, e2_mul(e2_make(gl_sub(c0, t0.x), c1), dw0));
+        f1 = e2_add(b0, e2_mul(e2_make(gl_sub(c0, t1.x), c1), dw1));
+    }
+    u64 x = l == 0 ? f0.c0 : l == 1 ? f0.c1 : l == 2 ? f1.c0 : l == 3 ? f1.c1 : 0;
+    if (live && l < 4) folded[4 * g + l] = x;
+    P2Lane c = p2_lane_consts(l);
+    x = p2_permute_coop(x, l, c);
+    if (live && l < 4) tree[4 * g + l] = x;
+}
+
 // Final fold (no tree): Ext2 codeword of 2*pairs elements -> pairs elements, canonical.
 __global__ void fold_final_kernel(const u64* __restrict__ cw, const u64* __restrict__ tab, u64 c0, u64 c1,
                                   u64* __restrict__ out, size_t pairs, bool base_in) {
@@ -747,12 +781,22 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
         size_t pairs = L >> (rd + 1);
         if (rd < n - 1) {
             size_t leaves = pairs / 2;
-            if (rd == 0)
+            if (leaves < MK_COOP_BELOW) {
+                int th = coop_threads(leaves);
+                unsigned g = grid_for(leaves * 8, th);
+                if (rd == 0)
+                    fold_hash_leaves_coop_kernel<true><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
+                                                                         leaves);
+                else
+                    fold_hash_leaves_coop_kernel<false><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
+                                                                          leaves);
+            } else if (rd == 0) {
                 fold_hash_leaves_kernel<true><<<grid_for(leaves, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
                                                                                      ftree[rd], leaves);
-            else
+            } else {
                 fold_hash_leaves_kernel<false><<<grid_for(leaves, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
                                                                                       ftree[rd], leaves);
+            }
             GB_LAUNCH_CHECK("fold_hash_leaves_kernel");
             RC_TRY(merkle_build_from_leaves(ftree[rd], leaves));
             GB_CUDA_TRY(cudaMemcpyAsync(rec + 8, ftree[rd] + (2 * leaves - 2) * 4, 32, cudaMemcpyDeviceToDevice, s));

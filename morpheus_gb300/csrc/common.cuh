@@ -27,7 +27,10 @@ constexpr int GB_ECUDA = -1;
 constexpr int GB_EINVAL = -2;
 constexpr int GB_EUNSUPPORTED = -3;
 
+void count_launch();
+
 inline int check_launch(const char* where) {
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error(where, e);

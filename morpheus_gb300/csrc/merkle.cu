@@ -13,7 +13,7 @@
 namespace gb {
 
 constexpr int MK_THREADS = 128;
-constexpr size_t MK_TOP_NODES = 2048;  // layers at or below this size finish in one CTA
+constexpr int MK_COOP_THREADS = 256;
 
 __global__ void __launch_bounds__(MK_THREADS) merkle_level_kernel(const u64* __restrict__ in, u64* __restrict__ out,
                                                                   size_t nodes) {
@@ -38,23 +38,47 @@ __global__ void __launch_bounds__(MK_THREADS) merkle_level_scalar_kernel(const u
     for (int k = 0; k < 4; k++) out[4 * j + k] = s[k];
 }
 
-// Finish all layers from a layer of `nodes` digests at `layer` up to the root.
-__global__ void __launch_bounds__(512) merkle_top_kernel(u64* __restrict__ layer, size_t nodes) {
+// One parent per 8-lane group.  Groups past the end compute node 0 and store nothing:
+// their warp still has to take part in the shuffles.
+__global__ void __launch_bounds__(MK_COOP_THREADS) merkle_level_coop_kernel(const u64* __restrict__ in,
+                                                                          u64* __restrict__ out, size_t nodes) {
+    size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 3;
+    int l = threadIdx.x & 7;
+    bool live = g < nodes;
+    size_t gg = live ? g : 0;
+    P2Lane c = p2_lane_consts(l);
+    u64 x = p2_permute_coop(in[8 * gg + l], l, c);
+    if (live && l < 4) out[4 * g + l] = x;
+}
+
+// Finish all layers from a layer of at most MK_TOP_NODES digests up to the root:
+// one CTA of 8 * MK_TOP_NODES / 2 threads, one 8-lane group per parent.
+__global__ void __launch_bounds__(8 * (MK_TOP_NODES / 2)) merkle_top_coop_kernel(u64* __restrict__ layer, size_t nodes) {
+    const int grp = threadIdx.x >> 3, l = threadIdx.x & 7;
+    P2Lane c = p2_lane_consts(l);
     while (nodes > 1) {
-        u64* out = layer + 4 * nodes;
         size_t half = nodes >> 1;
-        for (size_t j = threadIdx.x; j < half; j += blockDim.x) {
-            u64 s[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++) s[k] = layer[8 * j + k];
-            p2_permute(s);
-#pragma unroll
-            for (int k = 0; k < 4; k++) out[4 * j + k] = s[k];
-        }
+        u64* out = layer + 4 * nodes;
+        bool live = (size_t)grp < half;
+        u64 x = p2_permute_coop(layer[8 * (live ? grp : 0) + l], l, c);
+        if (live && l < 4) out[4 * grp + l] = x;
         __syncthreads();
         layer = out;
         nodes = half;
     }
+}
+
+__global__ void __launch_bounds__(MK_COOP_THREADS) hash_leaves_coop_kernel(const u64* __restrict__ cw,
+                                                                         u64* __restrict__ tree, size_t leaves,
+                                                                         int width) {
+    size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 3;
+    int l = threadIdx.x & 7;
+    bool live = g < leaves;
+    size_t gg = live ? g : 0;
+    P2Lane c = p2_lane_consts(l);
+    u64 x = l < width ? cw[(size_t)width * gg + l] : 0;
+    x = p2_permute_coop(x, l, c);
+    if (live && l < 4) tree[4 * g + l] = x;
 }
 
 __global__ void __launch_bounds__(MK_THREADS) hash_leaves_gl_kernel(const u64* __restrict__ cw, u64* __restrict__ tree,
@@ -86,30 +110,51 @@ __global__ void replicate_kernel(u64* __restrict__ layer, size_t count, int copi
     layer[words + k] = layer[k % words];
 }
 
-int merkle_build_from_leaves(u64* tree, size_t leaves) {
+// one layer: `half` parents from the 2*half digests at `in`
+static int merkle_level(const u64* in, u64* out, size_t half) {
     cudaStream_t s = stream();
+    if (half >= MK_COOP_BELOW) {
+        merkle_level_kernel<<<grid_for(half, MK_THREADS), MK_THREADS, 0, s>>>(in, out, half);
+        return check_launch("merkle_level_kernel");
+    }
+    int threads = coop_threads(half);
+    merkle_level_coop_kernel<<<grid_for(half * 8, threads), threads, 0, s>>>(in, out, half);
+    return check_launch("merkle_level_coop_kernel");
+}
+
+int merkle_build_from_leaves(u64* tree, size_t leaves) {
     u64* layer = tree;
     size_t nodes = leaves;
     while (nodes > MK_TOP_NODES) {
         size_t half = nodes >> 1;
-        merkle_level_kernel<<<grid_for(half, MK_THREADS), MK_THREADS, 0, s>>>(layer, layer + 4 * nodes, half);
-        GB_LAUNCH_CHECK("merkle_level_kernel");
+        int rc = merkle_level(layer, layer + 4 * nodes, half);
+        if (rc) return rc;
         layer += 4 * nodes;
         nodes = half;
     }
     if (nodes > 1) {
-        merkle_top_kernel<<<1, 512, 0, s>>>(layer, nodes);
-        GB_LAUNCH_CHECK("merkle_top_kernel");
+        merkle_top_coop_kernel<<<1, 8 * (MK_TOP_NODES / 2), 0, stream()>>>(layer, nodes);
+        GB_LAUNCH_CHECK("merkle_top_coop_kernel");
     }
     return GB_OK;
 }
 
 int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves) {
+    if (leaves < MK_COOP_BELOW) {
+        int t = coop_threads(leaves);
+        hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 2);
+        return check_launch("hash_leaves_coop_kernel");
+    }
     hash_leaves_gl_kernel<<<grid_for(leaves, MK_THREADS), MK_THREADS, 0, stream()>>>(cw, tree, leaves);
     return check_launch("hash_leaves_gl_kernel");
 }
 
 int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves) {
+    if (leaves < MK_COOP_BELOW) {
+        int t = coop_threads(leaves);
+        hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 4);
+        return check_launch("hash_leaves_coop_kernel");
+    }
     hash_leaves_ext2_kernel<<<grid_for(leaves, MK_THREADS), MK_THREADS, 0, stream()>>>(cw, tree, leaves);
     return check_launch("hash_leaves_ext2_kernel");
 }
@@ -135,8 +180,8 @@ int merkle_tree_gl_replicated(const u64* cw, u64* tree, size_t leaves, int copie
         }
         if (n == 1) break;
         size_t half = n >> 1;
-        merkle_level_kernel<<<grid_for(half, MK_THREADS), MK_THREADS, 0, s>>>(layer, layer + 4 * layer_nodes, half);
-        GB_LAUNCH_CHECK("merkle_level_kernel");
+        rc = merkle_level(layer, layer + 4 * layer_nodes, half);
+        if (rc) return rc;
         off += 4 * layer_nodes;
         layer_nodes >>= 1;
         n = half;

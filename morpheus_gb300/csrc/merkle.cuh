@@ -45,8 +45,18 @@ __device__ __forceinline__ void ld_digest(const u64* p, u64* s) {
     s[3] = b.y;
 }
 
-// Host-side tree builders (merkle.cu).  `leaves_done`: leaf digests are already in
-// layer 0.  All launches on gb::stream(); no synchronisation.
+// Work below this many permutations per launch is latency-bound: one thread's
+// permutation is a long serial chain, so those launches use 8 lanes per state.
+constexpr size_t MK_COOP_BELOW = 32768;
+// Once a layer has at most this many nodes, the layers above it are finished by one CTA.
+constexpr size_t MK_TOP_NODES = 16;
+
+// CTA size for a cooperative launch over `groups` 8-lane groups: small launches use
+// 64-thread CTAs so that the work spreads over as many SMs as there are CTAs.
+inline int coop_threads(size_t groups) { return groups * 8 >= (size_t)num_sms() * 256 ? 256 : 64; }
+
+// Host-side tree builders (merkle.cu).  merkle_build_from_leaves expects the leaf
+// digests in layer 0.  All launches on gb::stream(); no synchronisation.
 int merkle_build_from_leaves(u64* tree, size_t leaves);
 int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves);
 int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves);

@@ -116,6 +116,66 @@ __device__ __forceinline__ void p2_permute(u64* s) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Cooperative form: 8 lanes of a warp hold one state, lane l holding s[l].
+// One thread's permutation is a serial chain of ~112 dependent multiplications;
+// spreading the lanes over 8 threads leaves only the S-box chain and the linear
+// layers' shuffles on the critical path, which is what latency-bound work (the
+// small top layers of a Merkle tree) needs.  All 32 lanes of a warp must call it.
+// ---------------------------------------------------------------------------
+static __constant__ u64 c_p2_ext[8][8] = GB_P2_RC_EXT;
+static __constant__ u64 c_p2_int[22] = GB_P2_RC_INT;
+static __constant__ u64 c_p2_diag[8] = GB_P2_DIAG;
+
+__device__ __forceinline__ u64 shfl_xor64(u64 v, int m) {
+    u32 lo = __shfl_xor_sync(0xffffffffu, (u32)v, m), hi = __shfl_xor_sync(0xffffffffu, (u32)(v >> 32), m);
+    return ((u64)hi << 32) | lo;
+}
+__device__ __forceinline__ u64 shfl_idx64(u64 v, int src) {
+    u32 lo = __shfl_sync(0xffffffffu, (u32)v, src), hi = __shfl_sync(0xffffffffu, (u32)(v >> 32), src);
+    return ((u64)hi << 32) | lo;
+}
+
+// per-lane round constants of lane l (8 external-round constants and the diagonal entry)
+struct P2Lane {
+    u64 ext[8];
+    u64 diag;
+};
+__device__ __forceinline__ P2Lane p2_lane_consts(int l) {
+    P2Lane c;
+#pragma unroll
+    for (int r = 0; r < 8; r++) c.ext[r] = c_p2_ext[r][l];
+    c.diag = c_p2_diag[l];
+    return c;
+}
+
+// external layer on 8 lanes: within a half, out_j = (x0+x1+x2+x3) + x_j + 2 x_{j+1};
+// then every lane adds the column sum of both halves
+__device__ __forceinline__ u64 p2_coop_external_linear(u64 x) {
+    int lane = threadIdx.x & 31;
+    u64 t = gl_add(x, shfl_xor64(x, 1));
+    u64 all = gl_add(t, shfl_xor64(t, 2));
+    u64 nxt = shfl_idx64(x, (lane & ~3) | ((lane + 1) & 3));
+    u64 out = gl_add(gl_add(all, x), gl_double(nxt));
+    return gl_add(out, gl_add(out, shfl_xor64(out, 4)));
+}
+
+__device__ __forceinline__ u64 p2_permute_coop(u64 x, int l, const P2Lane& c) {
+#pragma unroll
+    for (int r = 0; r < 4; r++) x = p2_coop_external_linear(p2_sbox(gl_add(x, c.ext[r])));
+#pragma unroll
+    for (int r = 0; r < 22; r++) {
+        if (l == 0) x = p2_sbox(gl_add(x, c_p2_int[r]));
+        u64 t = gl_add(x, shfl_xor64(x, 1));
+        t = gl_add(t, shfl_xor64(t, 2));
+        t = gl_add(t, shfl_xor64(t, 4));
+        x = gl_add(gl_mul(x, c.diag), t);
+    }
+#pragma unroll
+    for (int r = 4; r < 8; r++) x = p2_coop_external_linear(p2_sbox(gl_add(x, c.ext[r])));
+    return x;
+}
+
 // 2-to-1 compression P2(l || r)[0..4]
 __device__ __forceinline__ void p2_compress(const u64* l, const u64* r, u64* out) {
     u64 s[8] = {l[0], l[1], l[2], l[3], r[0], r[1], r[2], r[3]};

@@ -1,6 +1,7 @@
 // Runtime plumbing of the C ABI: stream selection, error strings, the memory and
 // device entry points (goldilocks-cuda-rs/src/ffi.rs:11-26, :306-309), batch
 // field ops and host transcript helpers.
+#include <atomic>
 #include <cstring>
 #include <string>
 
@@ -12,6 +13,9 @@ namespace gb {
 
 static thread_local cudaStream_t t_stream = cudaStreamPerThread;
 static thread_local std::string t_err;
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 cudaStream_t stream() { return t_stream; }
 
@@ -70,6 +74,23 @@ static int e2_batch(const u64* a, const u64* b, u64* r, int n, const char* name)
     return check_launch(name);
 }
 
+// Throughput ceiling of this file's Goldilocks multiplication: every thread runs
+// 8 independent chains of `iters` multiplications (no memory traffic).
+__global__ void __launch_bounds__(256) mulmod_probe_kernel(u64* out, int iters) {
+    u64 a[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] = 0x9E3779B97F4A7C15ull * (threadIdx.x + 1 + j) + blockIdx.x;
+    const u64 m = 0x0123456789ABCDEFull;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) a[j] = gl_mul(a[j], m);
+    }
+    u64 r = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) r ^= a[j];
+    out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = r;
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -83,6 +104,13 @@ int gb_set_stream(void* s) {
 void* gb_get_stream(void) { return (void*)t_stream; }
 const char* gb_last_error(void) { return t_err.c_str(); }
 int gb_device_sm_count(void) { return num_sms(); }
+unsigned long long gb_launch_count(void) { return g_launches.load(); }
+
+int gb_mulmod_probe(uint64_t* d_out, int blocks, int iters) {
+    if (blocks <= 0 || iters <= 0) return GB_EINVAL;
+    mulmod_probe_kernel<<<blocks, 256, 0, stream()>>>(d_out, iters);
+    return check_launch("gb_mulmod_probe");
+}
 
 int goldilocks_cuda_init(void) {
     int n = 0;

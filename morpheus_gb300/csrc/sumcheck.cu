@@ -558,6 +558,21 @@ int gb_sumcheck_prove_ext2(gb_transcript* t, int n, int d, const uint64_t* d_pol
     return prove(t, n, d, d_polys, h_polys, true, h_msgs, h_challenges, h_finals, h_final_eval);
 }
 
+size_t gb_sumcheck_round_workspace_words(void) {
+    return (size_t)num_sms() * 4 * 2 * (SC_MAX_D + 1) + 2;
+}
+
+int gb_sumcheck_fold_round_ext2(const uint64_t* d_in, int in_base, size_t in_stride, uint64_t* d_out,
+                                size_t out_stride, int d, size_t pairs_out, uint64_t r0, uint64_t r1, uint64_t* d_msg,
+                                uint64_t* d_work) {
+    if (d < 1 || d > SC_MAX_D || pairs_out == 0 || !d_work || !d_msg) return GB_EINVAL;
+    unsigned g = round_grid(pairs_out);
+    u64* partials = d_work;
+    unsigned* counter = reinterpret_cast<unsigned*>(d_work + (size_t)num_sms() * 4 * 2 * (SC_MAX_D + 1));
+    return dispatch_d<FoldRoundE2>(d, in_base != 0, d_in, in_stride, d_out, out_stride, pairs_out, g, r0, r1, partials,
+                                   d_msg, counter);
+}
+
 int gb_sumcheck_prove_base(gb_transcript* t, int n, int d, const uint64_t* d_polys, const uint64_t* h_polys,
                            uint64_t* h_msgs, uint64_t* h_challenges, uint64_t* h_finals, uint64_t* h_final_eval) {
     return prove(t, n, d, d_polys, h_polys, false, h_msgs, h_challenges, h_finals, h_final_eval);

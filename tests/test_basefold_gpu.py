@@ -14,9 +14,22 @@ def rnd(seed, *shape):
     return np.random.default_rng(seed).integers(0, P, size=shape, dtype=np.uint64)
 
 
+_KEEP = []
+
+
+@pytest.fixture(autouse=True)
+def _release_buffers():
+    """Buffers made by dev() live until the test ends: a temporary passed as
+    dev(x).ptr would otherwise be freed before the kernel that reads it runs."""
+    yield
+    _KEEP.clear()
+
+
 def dev(arr):
     from morpheus_gb300.memory import DeviceBuffer
-    return DeviceBuffer.from_numpy(np.ascontiguousarray(arr, dtype=np.uint64).reshape(-1))
+    buf = DeviceBuffer.from_numpy(np.ascontiguousarray(arr, dtype=np.uint64).reshape(-1))
+    _KEEP.append(buf)
+    return buf
 
 
 def canon(x):
