@@ -104,6 +104,11 @@ SIGNATURES = {
     "gb_basefold_commitment_info": (i32, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), vp]),
     "gb_basefold_proof_len": (sz, [i32, i32, i32]),
     "gb_basefold_open_ext2": (i32, [vp, vp, vp, ctypes.POINTER(GbTranscript), i32, vp]),
+    "almost_goldilocks_cuda_init": (i32, []),
+    "ajtai_commit_wide_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
+    "gb_ajtai_key_create": (i32, [vp, i32, i32, u64, ctypes.POINTER(vp)]),
+    "gb_ajtai_key_destroy": (i32, [vp]),
+    "gb_ajtai_commit_u8_batched": (i32, [vp, vp, i32, vp]),
 }
 
 

@@ -63,7 +63,7 @@ def build(verbose=False, extra=()):
         raise RuntimeError("nvcc failed:\n" + "\n\n".join(errors))
     newest = max(os.path.getmtime(o) for o in objs)
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcuda"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{p.stdout}\n{p.stderr}")

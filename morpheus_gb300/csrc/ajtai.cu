@@ -1,0 +1,625 @@
+// Ajtai commitment over R_q = F_q[X]/(X^64 + 1), q = 2^64 - 2^32 - 31.
+//
+//   c_i = sum_j M[i][j] * z_j,   c_i[r] = sum_j sum_l s(r,l) M[i][j][(r-l) mod 64] z_j[l],
+//   s = -1 when l > r (negacyclic wrap)     (cuda_almost_goldilocks/ajtai.cuh:164-275)
+// with M[i][j] drawn by the ChaCha8 PRG keyed by the seed (ajtai_chacha8.cuh:115-178).
+//
+// Batched small-witness path (witness coefficients in [0, 256)): one exact GEMM on the
+// tcgen05 tensor cores.  sm_103a has no integer MMA (ptxas rejects tcgen05 kind::i8), so
+// the contraction runs in bf16 with fp32 accumulation, kept exact by construction:
+//   * every matrix coefficient m is centred (v = m or m - q, |v| < q/2) and split into
+//     8 balanced base-256 digits d_p with |d_p| <= 128 (v = sum_p d_p 256^p);
+//   * witness coefficients are centred, z' = z - 128 in [-128, 127];
+//   * so every product has |d z'| <= 2^14 and a sum of 1024 of them stays <= 2^24, which
+//     fp32 represents exactly.  The K dimension is cut into 1024-long chunks; after each
+//     chunk the fp32 accumulator (TMEM) is drained into int32 registers (|sum| <= 2^30 over
+//     K = 2^16) while the tensor core fills the other accumulator buffer.
+//   The GEMM is S_p = T_p . Z'^T with T_p the negacyclic Toeplitz expansion of digit p
+//   (rows (p, i, r), columns (j, l)), and c = sum_p 256^p S_p + 128 * rowsum(T) mod q.
+// The digit-expanded matrix is built once per (key, rows, columns) and kept in HBM.
+//
+// The full-width entry point ajtai_commit_wide_ffi (arbitrary field coefficients) runs
+// on the CUDA cores with modular multiplications.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/almost_goldilocks_cuda_wrapper.h"
+#include "agl.cuh"
+#include "common.cuh"
+
+namespace gb {
+
+constexpr int AJ_D = 64;
+constexpr int AJ_KAPPA = 42;
+constexpr u64 AJ_HALF_Q = AGL_Q / 2;  // centred representatives: m > q/2 maps to m - q
+
+// ---------------------------------------------------------------------------
+// matrix PRG: M[i][j][0..63] for rows [row_lo, row_lo + rows), columns [col0, col0 + N)
+// ---------------------------------------------------------------------------
+__global__ void ajtai_prg_kernel(const u32* __restrict__ key, int row_lo, int rows, u64 col0, u64 N,
+                                 u64* __restrict__ M) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t total = (size_t)rows * N * 8;
+    if (t >= total) return;
+    u32 k[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) k[q] = __ldg(key + q);
+    u32 blk = (u32)(t & 7);
+    size_t ij = t >> 3;
+    u64 j = ij % N;
+    int i = (int)(ij / N);
+    u64 out[8];
+    ajtai_prg_block(k, (u32)(row_lo + i), j + col0, blk, out);
+    u64* dst = M + ij * AJ_D + 8 * blk;
+#pragma unroll
+    for (int q = 0; q < 8; q++) dst[q] = out[q];
+}
+
+// balanced base-256 digits of the centred value of m in [0, q)
+__device__ __forceinline__ void centred_digits(u64 m, int* d) {
+    bool neg = m > AJ_HALF_Q;
+    u64 mag = neg ? (AGL_Q - m) : m;  // |v| < 2^63
+    long long v = neg ? -(long long)mag : (long long)mag;
+#pragma unroll
+    for (int p = 0; p < 7; p++) {
+        int lo = (int)(v & 255);
+        if (lo >= 128) lo -= 256;
+        d[p] = lo;
+        v = (v - lo) >> 8;
+    }
+    d[7] = (int)v;  // |d7| <= 128
+}
+
+// T[(p, i, r)][(j, l)] = s(r,l) d_p(M[i][j][(r-l) mod 64]) as bf16, K padded with zeros to Kp.
+// One block per (i, j), 64 threads (thread r writes 8 rows x 64 columns).
+__global__ void __launch_bounds__(64) ajtai_expand_kernel(const u64* __restrict__ M, int rows, u64 N, size_t Kp,
+                                                          __nv_bfloat16* __restrict__ T) {
+    __shared__ short dig[AJ_D][8];  // the top digit can be +128: not a signed char
+    const u64 j = blockIdx.x;
+    const int i = blockIdx.y;
+    const int r = threadIdx.x;
+    {
+        int d[8];
+        centred_digits(M[((size_t)i * N + j) * AJ_D + r], d);
+#pragma unroll
+        for (int p = 0; p < 8; p++) dig[r][p] = (short)d[p];
+    }
+    __syncthreads();
+    const size_t row_stride = (size_t)rows * AJ_D;  // rows per digit
+#pragma unroll 1
+    for (int p = 0; p < 8; p++) {
+        __nv_bfloat16* dst = T + ((size_t)p * row_stride + (size_t)i * AJ_D + r) * Kp + j * AJ_D;
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+            __align__(16) __nv_bfloat16 w[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+                int l = v * 8 + e;
+                int k = (r - l) & 63;
+                int val = dig[k][p];
+                w[e] = __int2bfloat16_rn(l <= r ? val : -val);
+            }
+            *reinterpret_cast<uint4*>(dst + v * 8) = *reinterpret_cast<uint4*>(w);
+        }
+    }
+}
+
+// zero the padded K columns [K, Kp) of every row
+__global__ void ajtai_pad_cols_kernel(__nv_bfloat16* __restrict__ T, size_t nrows, size_t K, size_t Kp) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t w = Kp - K;
+    if (t >= nrows * w) return;
+    T[(t / w) * Kp + K + t % w] = __int2bfloat16_rn(0);
+}
+
+// rowsum(T)[i][r] mod q = sum_j (2 prefix_r(M_ij) - total(M_ij)), one thread per (i, r)
+__global__ void ajtai_rowsum_kernel(const u64* __restrict__ M, int rows, u64 N, u64* __restrict__ RS) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rows * AJ_D) return;
+    int i = t / AJ_D, r = t % AJ_D;
+    u64 acc = 0;
+    for (u64 j = 0; j < N; j++) {
+        const u64* m = M + ((size_t)i * N + j) * AJ_D;
+        for (int k = 0; k < AJ_D; k++) acc = k <= r ? agl_add(acc, m[k]) : agl_sub(acc, m[k]);
+    }
+    RS[t] = agl_canon(acc);
+}
+
+// z'[b][k] = z[b][k] - 128 (bf16); padded witnesses / columns are 0
+__global__ void ajtai_zprep_kernel(const uint8_t* __restrict__ z, int B, size_t K, int Bp, size_t Kp,
+                                   __nv_bfloat16* __restrict__ zc) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)Bp * Kp) return;
+    size_t b = t / Kp, k = t % Kp;
+    int v = (b < (size_t)B && k < K) ? (int)z[b * K + k] - 128 : 0;
+    zc[t] = __int2bfloat16_rn(v);
+}
+
+// c[b][i][r] = sum_p 256^p S[(p, i, r)][b] + 128 rowsum[i][r]  mod q, canonical
+__global__ void ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows, int B, const u64* __restrict__ RS,
+                                     u64* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= B * rows * AJ_D) return;
+    int b = t / (rows * AJ_D), ir = t % (rows * AJ_D);
+    __int128 acc = 0;
+#pragma unroll
+    for (int p = 7; p >= 0; p--) acc = acc * 256 + (__int128)S[((size_t)p * rows * AJ_D + ir) * Bp + b];
+    const __int128 Q = (__int128)AGL_Q;
+    __int128 m = acc % Q;
+    if (m < 0) m += Q;
+    u64 rs128 = agl_mul(__ldg(RS + ir), 128);
+    out[t] = agl_canon(agl_add((u64)m, agl_canon(rs128)));
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 GEMM:  S[m][n] = sum_k A[m][k] B[n][k]   (bf16, K-major both, fp32 in TMEM,
+// exact per 1024-K chunk, int32 totals), M tile 128, N tile 128, K tile 64 (128-byte
+// swizzled rows), 4-stage TMA pipeline.
+//   warp 0: TMA producer   warp 1: MMA issuer (one thread)   warps 2..9: epilogue, warp w owning
+//   TMEM lanes 32 (w % 4) .. +31 and columns 64 ((w - 2) / 4) .. +63 of each accumulator
+// ---------------------------------------------------------------------------
+constexpr int GM_BM = 128, GM_BN = 128, GM_BK = 64, GM_STAGES = 4, GM_CHUNK_TILES = 16;
+constexpr int GM_TILE_BYTES = GM_BM * GM_BK * 2;  // 16 KB (A and B tiles are the same size)
+constexpr int GM_STAGE_BYTES = 2 * GM_TILE_BYTES;
+constexpr int GM_EPI_WARPS = 8;  // two warps per TMEM lane quarter, one per 64-column half
+constexpr int GM_THREADS = 64 + 32 * GM_EPI_WARPS;
+constexpr int GM_SMEM = GM_STAGES * GM_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr unsigned long long GM_SPIN_LIMIT = 1ull << 26;  // bounded waits (seconds at worst)
+
+__device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(u32 bar, u32 count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(u32 bar, u32 bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(u32 bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(u32 bar, u32 parity) {
+    u32 ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false (and the error flag set) when the limit is reached
+__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity, int* err, int code) {
+    for (unsigned long long it = 0; it < GM_SPIN_LIMIT; it++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 1023) == 1023 && *(volatile int*)err) return false;  // another role already gave up
+    }
+    atomicCAS(err, 0, code);
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(u32 dst, const CUtensorMap* map, int x, int y, u32 bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
+__device__ __forceinline__ u64 umma_desc_sw128(u32 saddr) {
+    u64 d = 0;
+    d |= (u64)((saddr & 0x3FFFF) >> 4);  // start address
+    d |= (u64)1 << 16;                   // leading-dimension offset (unused for swizzled K-major)
+    d |= (u64)(1024 >> 4) << 32;         // stride-dimension offset
+    d |= (u64)1 << 46;                   // descriptor version for tcgen05
+    d |= (u64)2 << 61;                   // 128-byte swizzle
+    return d;
+}
+
+// instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 128
+constexpr u32 GM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(GM_BN >> 3) << 17) | ((u32)(GM_BM >> 4) << 24);
+
+__global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                                   const __grid_constant__ CUtensorMap tmB, int k_tiles,
+                                                                   int* __restrict__ S, int ldS, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + GM_STAGES * GM_STAGE_BYTES);
+    // bars: full[S], empty[S], acc_full[2], acc_empty[2], mma_done; tmem base address after them
+    u32* tmem_slot = (u32*)(bars + 2 * GM_STAGES + 5);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * GM_BM, n0 = blockIdx.y * GM_BN;
+    const int chunks = k_tiles / GM_CHUNK_TILES;
+
+    auto full = [&](int s) { return smem_u32(bars + s); };
+    auto empty = [&](int s) { return smem_u32(bars + GM_STAGES + s); };
+    auto acc_full = [&](int a) { return smem_u32(bars + 2 * GM_STAGES + a); };
+    auto acc_empty = [&](int a) { return smem_u32(bars + 2 * GM_STAGES + 2 + a); };
+    const u32 mma_done = smem_u32(bars + 2 * GM_STAGES + 4);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < GM_STAGES; s++) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(acc_full(a), 1);
+            mbar_init(acc_empty(a), 32 * GM_EPI_WARPS);
+        }
+        mbar_init(mma_done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {  // TMEM: two 128-column fp32 accumulators
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const u32 tmem = *(volatile u32*)tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int kt = 0; kt < k_tiles; kt++) {
+                int s = kt % GM_STAGES;
+                u32 ph = (kt / GM_STAGES) & 1;
+                if (!mbar_wait(empty(s), ph ^ 1, err, 1)) break;
+                mbar_expect_tx(full(s), GM_STAGE_BYTES);
+                uint8_t* sa = smem + s * GM_STAGE_BYTES;
+                tma_load_2d(smem_u32(sa), &tmA, kt * GM_BK, m0, full(s));
+                tma_load_2d(smem_u32(sa + GM_TILE_BYTES), &tmB, kt * GM_BK, n0, full(s));
+                issued = kt + 1;
+            }
+            // loads still in flight land in shared memory: wait (bounded) for every issued stage
+            for (int kt = issued - GM_STAGES < 0 ? 0 : issued - GM_STAGES; kt < issued; kt++)
+                mbar_wait(full(kt % GM_STAGES), (kt / GM_STAGES) & 1, err, 5);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            bool ok = true;
+            for (int c = 0; c < chunks && ok; c++) {
+                int a = c & 1;
+                u32 use = (u32)(c >> 1);
+                if (!mbar_wait(acc_empty(a), (use & 1) ^ 1, err, 2)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const u32 d_tmem = tmem + (u32)(a * GM_BN);
+                for (int t = 0; t < GM_CHUNK_TILES; t++) {
+                    int kt = c * GM_CHUNK_TILES + t;
+                    int s = kt % GM_STAGES;
+                    if (!mbar_wait(full(s), (kt / GM_STAGES) & 1, err, 3)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    u32 sa = smem_u32(smem + s * GM_STAGE_BYTES);
+                    u64 adesc = umma_desc_sw128(sa), bdesc = umma_desc_sw128(sa + GM_TILE_BYTES);
+#pragma unroll
+                    for (int k = 0; k < GM_BK / 16; k++) {
+                        u32 acc = (t > 0 || k > 0) ? 1u : 0u;
+                        // advance 16 bf16 = 32 bytes along K inside the swizzled rows
+                        u64 ad = adesc + (u64)((k * 32) >> 4), bd = bdesc + (u64)((k * 32) >> 4);
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                            "l"(ad), "l"(bd), "r"(GM_IDESC), "r"(acc));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        empty(s)));
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    acc_full(a)));
+            }
+            // every MMA this thread issued has completed before TMEM can be released
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done));
+            mbar_wait(mma_done, 0, err, 6);
+        }
+    } else {
+        // epilogue: int32 totals of one TMEM row (lane) x 64 columns in registers
+        const int quarter = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const int row = quarter * 32 + lane;
+        constexpr int COLS = GM_BN / 2;
+        int acc[COLS];
+#pragma unroll
+        for (int q = 0; q < COLS; q++) acc[q] = 0;
+        bool ok = true;
+        for (int c = 0; c < chunks && ok; c++) {
+            int a = c & 1;
+            u32 use = (u32)(c >> 1);
+            if (!mbar_wait(acc_full(a), use & 1, err, 4)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+            for (int cb = 0; cb < COLS; cb += 32) {
+                u32 v[32];
+                u32 taddr = tmem + ((u32)(quarter * 32) << 16) + (u32)(a * GM_BN + half * COLS + cb);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+                    "[%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int e = 0; e < 32; e++) acc[cb + e] += __float2int_rn(__uint_as_float(v[e]));
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(acc_empty(a));
+        }
+        int* dst = S + (size_t)(m0 + row) * ldS + n0 + half * COLS;
+#pragma unroll
+        for (int q = 0; q < COLS; q += 4) *reinterpret_cast<int4*>(dst + q) = make_int4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+// The driver's tensor-map encoder, resolved at run time so that loading the library
+// needs no driver (CPU-only hosts load it to check its exports).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// 2D bf16 tensor map, inner dimension contiguous, 64 x 128 boxes with 128-byte swizzle
+static int make_map(CUtensorMap* map, void* base, u64 inner, u64 outer) {
+    static EncodeTiledFn encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            !fn) {
+            set_error_msg("cuTensorMapEncodeTiled is not available from the driver");
+            return GB_ECUDA;
+        }
+        encode = (EncodeTiledFn)fn;
+    }
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {inner * 2};
+    cuuint32_t box[2] = {GM_BK, GM_BM};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error_msg("cuTensorMapEncodeTiled failed");
+        return GB_ECUDA;
+    }
+    return GB_OK;
+}
+
+// Key-dependent operand: digit-expanded Toeplitz matrix and row sums.
+struct AjtaiKey {
+    u32 seed[8];
+    int row_lo = 0, rows = 0;
+    u64 N = 0;        // ring columns
+    size_t K = 0, Kp = 0;
+    u64* d_M = nullptr;              // [rows][N][64]
+    __nv_bfloat16* d_T = nullptr;    // [8 * rows * 64][Kp]
+    u64* d_RS = nullptr;             // [rows][64]
+    CUtensorMap mapA;
+};
+
+static size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* k) {
+    if (rows < 1 || N < 1 || N > (1ull << 24)) return GB_EINVAL;
+    cudaStream_t s = stream();
+    for (int q = 0; q < 8; q++) k->seed[q] = h_seed[q];
+    k->row_lo = row_lo;
+    k->rows = rows;
+    k->N = N;
+    k->K = (size_t)N * AJ_D;
+    k->Kp = round_up(k->K, (size_t)GM_BK * GM_CHUNK_TILES);
+    const size_t Mrows = (size_t)8 * rows * AJ_D;
+    u32* d_key = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&k->d_M, (size_t)rows * N * AJ_D * 8));
+    GB_CUDA_TRY(cudaMalloc(&k->d_T, Mrows * k->Kp * 2));
+    GB_CUDA_TRY(cudaMalloc(&k->d_RS, (size_t)rows * AJ_D * 8));
+    GB_CUDA_TRY(cudaMallocAsync(&d_key, 32, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_key, h_seed, 32, cudaMemcpyHostToDevice, s));
+    size_t tasks = (size_t)rows * N * 8;
+    ajtai_prg_kernel<<<grid_for(tasks, 256), 256, 0, s>>>(d_key, row_lo, rows, 0, N, k->d_M);
+    GB_LAUNCH_CHECK("ajtai_prg_kernel");
+    dim3 g((unsigned)N, (unsigned)rows);
+    ajtai_expand_kernel<<<g, 64, 0, s>>>(k->d_M, rows, N, k->Kp, k->d_T);
+    GB_LAUNCH_CHECK("ajtai_expand_kernel");
+    if (k->Kp > k->K) {
+        size_t work = Mrows * (k->Kp - k->K);
+        ajtai_pad_cols_kernel<<<grid_for(work, 256), 256, 0, s>>>(k->d_T, Mrows, k->K, k->Kp);
+        GB_LAUNCH_CHECK("ajtai_pad_cols_kernel");
+    }
+    ajtai_rowsum_kernel<<<grid_for((size_t)rows * AJ_D, 64), 64, 0, s>>>(k->d_M, rows, N, k->d_RS);
+    GB_LAUNCH_CHECK("ajtai_rowsum_kernel");
+    cudaFreeAsync(d_key, s);
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return make_map(&k->mapA, k->d_T, k->Kp, Mrows);
+}
+
+static void key_free(AjtaiKey* k) {
+    if (k->d_M) cudaFree(k->d_M);
+    if (k->d_T) cudaFree(k->d_T);
+    if (k->d_RS) cudaFree(k->d_RS);
+    k->d_M = nullptr;
+    k->d_T = nullptr;
+    k->d_RS = nullptr;
+}
+
+static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
+    if (B < 1) return GB_EINVAL;
+    cudaStream_t s = stream();
+    const int Bp = (int)round_up((size_t)B, GM_BN);
+    const size_t Mrows = (size_t)8 * k->rows * AJ_D;
+    __nv_bfloat16* zc = nullptr;
+    int* S = nullptr;
+    int* err = nullptr;
+    GB_CUDA_TRY(cudaMallocAsync(&zc, (size_t)Bp * k->Kp * 2, s));
+    GB_CUDA_TRY(cudaMallocAsync(&S, Mrows * Bp * 4, s));
+    GB_CUDA_TRY(cudaMallocAsync(&err, 4, s));
+    GB_CUDA_TRY(cudaMemsetAsync(err, 0, 4, s));
+    ajtai_zprep_kernel<<<grid_for((size_t)Bp * k->Kp, 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+    int rc = check_launch("ajtai_zprep_kernel");
+    CUtensorMap mapB;
+    if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp);
+    if (!rc) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(ajtai_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GM_SMEM);
+            attr = true;
+        }
+        dim3 grid((unsigned)(Mrows / GM_BM), (unsigned)(Bp / GM_BN));
+        int k_tiles = (int)(k->Kp / GM_BK);
+        ajtai_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, s>>>(k->mapA, mapB, k_tiles, S, Bp, err);
+        rc = check_launch("ajtai_gemm_kernel");
+    }
+    if (!rc) {
+        int total = B * k->rows * AJ_D;
+        ajtai_combine_kernel<<<grid_for(total, 256), 256, 0, s>>>(S, Bp, k->rows, B, k->d_RS, d_out);
+        rc = check_launch("ajtai_combine_kernel");
+    }
+    int h_err = 0;
+    if (!rc) {
+        cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) rc = GB_ECUDA;
+    }
+    cudaFreeAsync(zc, s);
+    cudaFreeAsync(S, s);
+    cudaFreeAsync(err, s);
+    if (!rc && h_err) {
+        set_error_msg("ajtai_gemm_kernel: pipeline wait timed out (code " + std::to_string(h_err) + ")");
+        rc = GB_ECUDA;
+    }
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// full-width commitment on the CUDA cores (reference ABI):
+// thread (i, r) of column chunk accumulates sum_j sum_l s(r,l) M[i][j][(r-l) mod 64] z_j[l].
+// One block per (chunk, row tile of 8 rows); the block generates the matrix columns it
+// needs into shared memory, as the reference kernel does, then every thread runs the
+// negacyclic dot product with modular multiplications.
+// ---------------------------------------------------------------------------
+constexpr int WIDE_ROWS = 8;
+constexpr int WIDE_CHUNK = 16;  // columns per block
+
+__global__ void __launch_bounds__(WIDE_ROWS * AJ_D) ajtai_wide_kernel(const u32* __restrict__ key,
+                                                                    const u64* __restrict__ z, u64 N, u64 col_offset,
+                                                                    u64* __restrict__ partial, int nchunks) {
+    __shared__ u64 Msh[WIDE_ROWS * AJ_D];
+    __shared__ u64 zsh[AJ_D];
+    __shared__ u32 ksh[8];
+    const int t = threadIdx.x, il = t / AJ_D, r = t % AJ_D;
+    const int chunk = blockIdx.x, tile = blockIdx.y;
+    const int row = tile * WIDE_ROWS + il;
+    if (t < 8) ksh[t] = key[t];
+    __syncthreads();
+    u64 acc = 0;
+    u64 j0 = (u64)chunk * WIDE_CHUNK, j1 = j0 + WIDE_CHUNK < N ? j0 + WIDE_CHUNK : N;
+    for (u64 j = j0; j < j1; j++) {
+        if (t < AJ_D) zsh[t] = z[j * AJ_D + t];
+        if (t < WIDE_ROWS * 8) {
+            int rl = t / 8, blk = t % 8;
+            int rr = tile * WIDE_ROWS + rl;
+            u64 out[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (rr < AJ_KAPPA) ajtai_prg_block(ksh, (u32)rr, j + col_offset, (u32)blk, out);
+#pragma unroll
+            for (int q = 0; q < 8; q++) Msh[rl * AJ_D + blk * 8 + q] = out[q];
+        }
+        __syncthreads();
+        if (row < AJ_KAPPA) {
+            const u64* m = Msh + il * AJ_D;
+            for (int l = 0; l <= r; l++) acc = agl_add(acc, agl_mul(m[r - l], zsh[l]));
+            for (int l = r + 1; l < AJ_D; l++) acc = agl_sub(acc, agl_mul(m[r - l + AJ_D], zsh[l]));
+        }
+        __syncthreads();
+    }
+    if (row < AJ_KAPPA) partial[((size_t)chunk * AJ_KAPPA + row) * AJ_D + r] = acc;
+}
+
+__global__ void ajtai_wide_reduce_kernel(const u64* __restrict__ partial, int nchunks, u64* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= AJ_KAPPA * AJ_D) return;
+    u64 acc = 0;
+    for (int c = 0; c < nchunks; c++) acc = agl_add(acc, partial[(size_t)c * AJ_KAPPA * AJ_D + t]);
+    out[t] = agl_canon(acc);
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int almost_goldilocks_cuda_init(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return -1;
+    return cudaSetDevice(0) == cudaSuccess ? 0 : -1;
+}
+
+int ajtai_commit_wide_ffi(const uint32_t* d_key, const uint64_t* d_z_wide, uint64_t N, uint64_t col_offset, int chunk,
+                          uint64_t* d_out) {
+    // The reference accepts chunk sizes 64/128/256/1024/4096 (a tuning knob); any of them
+    // gives the same commitment, so the value is validated and otherwise ignored.
+    if (chunk != 64 && chunk != 128 && chunk != 256 && chunk != 1024 && chunk != 4096) return GB_EUNSUPPORTED;
+    if (N == 0) return GB_EINVAL;
+    cudaStream_t s = stream();
+    int nchunks = (int)((N + WIDE_CHUNK - 1) / WIDE_CHUNK);
+    u64* partial = nullptr;
+    GB_CUDA_TRY(cudaMallocAsync(&partial, (size_t)nchunks * AJ_KAPPA * AJ_D * 8, s));
+    dim3 g((unsigned)nchunks, (unsigned)((AJ_KAPPA + WIDE_ROWS - 1) / WIDE_ROWS));
+    ajtai_wide_kernel<<<g, WIDE_ROWS * AJ_D, 0, s>>>(d_key, d_z_wide, N, col_offset, partial, nchunks);
+    int rc = check_launch("ajtai_wide_kernel");
+    if (!rc) {
+        ajtai_wide_reduce_kernel<<<grid_for(AJ_KAPPA * AJ_D, 256), 256, 0, s>>>(partial, nchunks, d_out);
+        rc = check_launch("ajtai_wide_reduce_kernel");
+    }
+    cudaFreeAsync(partial, s);
+    if (rc) return rc;
+    return sync_stream("ajtai_commit_wide_ffi");
+}
+
+int gb_ajtai_key_create(const uint32_t* h_seed, int row_lo, int rows, uint64_t n_ring, void** handle) {
+    if (!h_seed || !handle) return GB_EINVAL;
+    AjtaiKey* k = new AjtaiKey();
+    int rc = key_create(h_seed, row_lo, rows, n_ring, k);
+    if (rc) {
+        key_free(k);
+        delete k;
+        return rc;
+    }
+    *handle = k;
+    return GB_OK;
+}
+
+int gb_ajtai_key_destroy(void* handle) {
+    AjtaiKey* k = (AjtaiKey*)handle;
+    if (!k) return GB_OK;
+    key_free(k);
+    delete k;
+    return GB_OK;
+}
+
+int gb_ajtai_commit_u8_batched(void* handle, const uint8_t* d_z, int num_witnesses, uint64_t* d_out) {
+    AjtaiKey* k = (AjtaiKey*)handle;
+    if (!k || !d_z || !d_out) return GB_EINVAL;
+    return commit_batch(k, d_z, num_witnesses, d_out);
+}
+
+}  // extern "C"
