@@ -154,6 +154,65 @@ def cpu_baseline_sample():
     return {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port", "sample": sample}
 
 
+def run_side_workload(args):
+    """Configs other than the headline, each on one GPU with inputs resident in HBM."""
+    import torch
+    from morpheus_gb300 import build as B
+    B.build()
+    from morpheus_gb300 import _native as Nn
+    from morpheus_gb300.memory import DeviceBuffer
+    L = Nn.lib()
+    stream = torch.cuda.Stream()
+    L.gb_set_stream(ctypes.c_void_p(stream.cuda_stream))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    rng = np.random.default_rng(99)
+
+    def ev_time(fn):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    if args.workload == "sumcheck":
+        from morpheus_gb300.sumcheck import GpuLinearSumcheckProver, Transcript
+        n, d = 20, 2
+        polys = DeviceBuffer.from_numpy(rng.integers(0, P, size=d << n, dtype=np.uint64))
+
+        def step():
+            t = Transcript(b"bench")
+            GpuLinearSumcheckProver(n, d, t).prove((polys, d), t)
+        unit, metric, work = "Melem/s", "sumcheck Melem/s", d * (1 << n) / 1e6
+        cfg = {"workload": "product sumcheck, 2 polys x 2^20 Goldilocks, Ext2 challenges, 20 rounds"}
+    else:
+        n_ring, Bw, rows = 1024, 256, 16
+        key = np.array([0x5EED, 1, 2, 3, 4, 5, 6, 7], np.uint32)
+        h = ctypes.c_void_p()
+        Nn.check(L.gb_ajtai_key_create(key.ctypes.data, 0, rows, n_ring, ctypes.byref(h)), "key")
+        z = DeviceBuffer.from_numpy(rng.integers(0, 256, size=Bw * n_ring * 64, dtype=np.uint8))
+        out = DeviceBuffer(Bw * rows * 64)
+
+        def step():
+            Nn.check(L.gb_ajtai_commit_u8_batched(h, z.ptr, Bw, out.ptr), "ajtai")
+        unit, metric, work = "commitments/s", "ajtai witness commitments/s", float(Bw)
+        cfg = {"workload": "ajtai commit, 256 witnesses x 2^16 coefficients in [0,256), rows 0..15, q = 2^64-2^32-31"}
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    times = [ev_time(step) for _ in range(args.steps)]
+    ms = statistics.mean(times)
+    line = {"metric": metric, "value": work / (ms * 1e-3), "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64" if args.workload == "sumcheck" else "bf16 limbs (exact), u64 out",
+            "data": "synthetic", "config": cfg, "step_ms_all": [round(t, 4) for t in times]}
+    if args.workload == "ajtai":
+        line["tensor_tflops_equiv"] = 2.0 * 8 * rows * 64 * Bw * n_ring * 64 / (ms * 1e-3) / 1e12
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -162,9 +221,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--num-vars", type=int, default=N_VARS)
     ap.add_argument("--no-extras", action="store_true", help="skip the roofline probes and the CPU baseline")
+    ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "ajtai"],
+                    help="basefold (headline): commit+open proofs; sumcheck: 2 x 2^20 product sumcheck; "
+                         "ajtai: 256 witnesses x 16 rows x 2^16 coefficients")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "basefold":
+        return run_side_workload(args)
 
     import torch
     from morpheus_gb300 import build as B
