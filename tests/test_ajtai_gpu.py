@@ -31,6 +31,18 @@ def test_commit_wide_random_vs_oracle(gpu_lib):
     assert np.array_equal(ajtai.commit_wide(key, z, col_offset=11), O.ajtai_commit_wide(key, z, 11, 0, 42))
 
 
+def test_commit_wide_rejects_unsupported_chunk(gpu_lib):
+    """almost wrapper.cu:1203: a chunk outside {64, 128, 256, 1024, 4096} returns -3."""
+    from morpheus_gb300 import ajtai
+    from morpheus_gb300 import _native as N
+    key = np.arange(8, dtype=np.uint32)
+    z = np.ones(64, np.uint64)
+    for chunk in (0, 100, 512, 8192):
+        with pytest.raises(RuntimeError, match="-3"):
+            ajtai.commit_wide(key, z, chunk=chunk)
+    assert N.lib().ajtai_commit_wide_ffi(None, None, 1, 0, 100, None) == -3
+
+
 def test_batched_matches_reference(gpu_lib, golden):
     from morpheus_gb300.ajtai import AjtaiKey
     g = golden["ajtai_commit_u8_ref"]
