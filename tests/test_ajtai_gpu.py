@@ -37,10 +37,11 @@ def test_commit_wide_rejects_unsupported_chunk(gpu_lib):
     from morpheus_gb300 import _native as N
     key = np.arange(8, dtype=np.uint32)
     z = np.ones(64, np.uint64)
-    for chunk in (0, 100, 512, 8192):
+    for chunk in (100, 512, 8192):
         with pytest.raises(RuntimeError, match="-3"):
             ajtai.commit_wide(key, z, chunk=chunk)
-    assert N.lib().ajtai_commit_wide_ffi(None, None, 1, 0, 100, None) == -3
+    for chunk in (0, -64, 100):
+        assert N.lib().ajtai_commit_wide_ffi(None, None, 1, 0, chunk, None) == -3
 
 
 def test_batched_matches_reference(gpu_lib, golden):
