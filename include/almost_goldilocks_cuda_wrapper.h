@@ -48,6 +48,22 @@ int gb_ajtai_key_destroy(void *handle);
  * the key; the result equals ajtai_commit_wide_ffi restricted to those rows.  Synchronising. */
 int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses, uint64_t *d_out);
 
+/* ajtai_commit_wide_ffi without any device allocation (no counterpart in the reference).
+ * Same arguments, result and return codes as ajtai_commit_wide_ffi, whose every call
+ * allocates and frees its per-column-chunk partial sums.  This variant keeps them in a
+ * static device array of the library sized for N <= 4096 ring elements (5.25 MiB); a larger
+ * N returns -2 with a message in gb_last_error().  It is for callers that must not allocate
+ * on their request path: a service that has reserved its whole HBM budget up front, where an
+ * allocation inside the call could fail or wait on the memory pool.
+ *   - The first call on each device (with that device current) looks the scratch address up
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Calls share the one scratch: calls that overlap in time (other threads, other streams)
+ *     race on it and must be serialised by the caller.
+ *   - Nothing in the scratch needs clearing: every word read is written by the same call.
+ * Synchronising. */
+int ajtai_commit_wide_noalloc_ffi(const uint32_t *d_key, const uint64_t *d_z_wide, uint64_t N, uint64_t col_offset,
+                                  int chunk, uint64_t *d_out);
+
 #ifdef __cplusplus
 }
 #endif

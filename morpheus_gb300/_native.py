@@ -106,6 +106,7 @@ SIGNATURES = {
     "gb_basefold_open_ext2": (i32, [vp, vp, vp, ctypes.POINTER(GbTranscript), i32, vp]),
     "almost_goldilocks_cuda_init": (i32, []),
     "ajtai_commit_wide_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
+    "ajtai_commit_wide_noalloc_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
     "gb_ajtai_key_create": (i32, [vp, i32, i32, u64, ctypes.POINTER(vp)]),
     "gb_ajtai_key_destroy": (i32, [vp]),
     "gb_ajtai_commit_u8_batched": (i32, [vp, vp, i32, vp]),

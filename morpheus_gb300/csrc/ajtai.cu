@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -593,6 +594,63 @@ int ajtai_commit_wide_ffi(const uint32_t* d_key, const uint64_t* d_z_wide, uint6
     cudaFreeAsync(partial, s);
     if (rc) return rc;
     return sync_stream("ajtai_commit_wide_ffi");
+}
+
+}  // extern "C"
+
+namespace gb {
+// Scratch of ajtai_commit_wide_noalloc_ffi: the per-chunk partial commitments of at most
+// AJ_NOALLOC_MAX_RING ring columns (256 chunks x 42 rows x 64 coefficients x 8 B = 5.25 MiB),
+// in the module's static device memory so that the call allocates nothing.  Nothing in it has
+// to start at zero: ajtai_wide_kernel writes every word that ajtai_wide_reduce_kernel reads.
+constexpr u64 AJ_NOALLOC_MAX_RING = 4096;
+constexpr int AJ_NOALLOC_MAX_CHUNKS = (int)(AJ_NOALLOC_MAX_RING / WIDE_CHUNK);
+static __device__ __align__(256) u64 g_wide_noalloc_scratch[(size_t)AJ_NOALLOC_MAX_CHUNKS * AJ_KAPPA * AJ_D];
+
+// Device address of the scratch, looked up once per device (with that device current).
+static int wide_noalloc_scratch(u64** out) {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mu;
+    static u64* addr[MAX_DEVICES] = {};
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= MAX_DEVICES) {
+        set_error_msg("ajtai_commit_wide_noalloc_ffi: device ordinal out of range");
+        return GB_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_wide_noalloc_scratch));
+        addr[dev] = static_cast<u64*>(p);
+    }
+    *out = addr[dev];
+    return GB_OK;
+}
+}  // namespace gb
+
+extern "C" {
+
+int ajtai_commit_wide_noalloc_ffi(const uint32_t* d_key, const uint64_t* d_z_wide, uint64_t N, uint64_t col_offset,
+                                  int chunk, uint64_t* d_out) {
+    if (chunk != 64 && chunk != 128 && chunk != 256 && chunk != 1024 && chunk != 4096) return GB_EUNSUPPORTED;
+    if (N == 0) return GB_EINVAL;
+    if (N > AJ_NOALLOC_MAX_RING) {
+        set_error_msg("ajtai_commit_wide_noalloc_ffi: N = " + std::to_string(N) + " ring elements exceeds the " +
+                      std::to_string(AJ_NOALLOC_MAX_RING) + " that its static scratch holds");
+        return GB_EINVAL;
+    }
+    u64* partial = nullptr;
+    int rc = wide_noalloc_scratch(&partial);
+    if (rc) return rc;
+    cudaStream_t s = stream();
+    int nchunks = (int)((N + WIDE_CHUNK - 1) / WIDE_CHUNK);
+    dim3 g((unsigned)nchunks, (unsigned)((AJ_KAPPA + WIDE_ROWS - 1) / WIDE_ROWS));
+    ajtai_wide_kernel<<<g, WIDE_ROWS * AJ_D, 0, s>>>(d_key, d_z_wide, N, col_offset, partial, nchunks);
+    GB_LAUNCH_CHECK("ajtai_wide_kernel");
+    ajtai_wide_reduce_kernel<<<grid_for(AJ_KAPPA * AJ_D, 256), 256, 0, s>>>(partial, nchunks, d_out);
+    GB_LAUNCH_CHECK("ajtai_wide_reduce_kernel");
+    return sync_stream("ajtai_commit_wide_noalloc_ffi");
 }
 
 int gb_ajtai_key_create(const uint32_t* h_seed, int row_lo, int rows, uint64_t n_ring, void** handle) {
