@@ -45,6 +45,10 @@ int cuda_device_synchronize(void);
 int cuda_get_last_error(void);
 int cuda_peek_at_last_error(void);
 int cuda_mem_get_info(size_t *free_bytes, size_t *total_bytes);
+/* almost-goldilocks-cuda-rs/src/ffi.rs:85 (almost wrapper.cu:283-296): trim the current device's
+ * stream-ordered pool to min_bytes_to_keep.  The library sets that pool's release threshold to
+ * the maximum on first use, as the reference does, so pooled memory is kept until trimmed. */
+int cuda_pool_trim(size_t min_bytes_to_keep);
 int cuda_set_device(int device);
 int cuda_get_device(int *device);
 int cuda_get_device_count(int *count);
@@ -202,6 +206,55 @@ size_t gb_basefold_proof_len(int num_vars, int log_rate, int num_queries);
  * values.  h_proof: gb_basefold_proof_len words, canonical.  Synchronising. */
 int gb_basefold_open_ext2(void *commitment, void *table, const uint64_t *h_point, gb_transcript *t,
                           int num_queries, uint64_t *h_proof);
+
+/* ---- Batched and served proving (no reference counterpart) ----
+ * An instance is `degree` multilinear polynomials of 2^num_vars base-field values, proven by
+ * (1) Basefold commit of each (log_rate 1), (2) the product sumcheck with Ext2 challenges on
+ * Transcript::new("sumcheck") + append_ext2("", master_seed) + append_u64("", index) + the
+ * roots' words (append_u64("", w) each), (3) open_ext2 of each polynomial j at the sumcheck
+ * point on Transcript::new("bf-open") + append_ext2("", master_seed) + append_u64("", 8 index + j)
+ * (the per-opening transcript of zk-torch-3/src/dag/mod.rs:1128-1133).
+ * Proof (gb_instance_proof_len words, canonical): roots[d][4], msgs[n][d+1][2],
+ * challenges[n][2], finals[d][2], final_eval[2], then d open proofs of
+ * gb_basefold_proof_len(n, 1, num_queries) words.  2 <= num_vars <= 30, 1 <= degree <= 8. */
+typedef struct gb_instance {
+    int num_vars;
+    int degree;
+    uint64_t index;
+    const uint64_t *h_polys; /* degree x 2^num_vars values on the host, or NULL */
+    const uint64_t *d_polys; /* ... on the device (16-byte aligned), or NULL */
+    uint64_t *h_proof;       /* output (host) */
+} gb_instance;
+
+typedef struct gb_job_stats {
+    double queued_ms;  /* submit -> start */
+    double run_ms;     /* start -> finish */
+    double latency_ms; /* submit -> finish */
+} gb_job_stats;
+
+size_t gb_instance_proof_len(int num_vars, int degree, int num_queries);
+/* Estimated peak device bytes of one instance (the admission charge). */
+size_t gb_instance_hbm_bytes(int num_vars, int degree);
+/* One instance on the calling thread's stream (the per-call path).  table: a
+ * gb_basefold_table_create handle with log_rate 1 covering num_vars.  Synchronising. */
+int gb_prove_instance(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *inst);
+
+/* Prover service: `workers` host threads, each launching on a stream of its own, admit
+ * submitted instances in arrival order as their estimated footprint fits in hbm_budget
+ * bytes beside the running ones (a job larger than the budget runs alone).  The instance's
+ * host buffers must stay valid until gb_prover_wait returns for its ticket. */
+int gb_prover_create(void *table, const uint64_t master_seed[2], int num_queries, int workers, size_t hbm_budget,
+                     void **handle);
+int gb_prover_submit(void *prover, const gb_instance *inst, uint64_t *ticket); /* non-blocking */
+/* Blocks until the ticket's job is done; returns the job's return code (its message in
+ * gb_last_error()); stats may be NULL.  Each ticket is waited for once. */
+int gb_prover_wait(void *prover, uint64_t ticket, gb_job_stats *stats);
+int gb_prover_drain(void *prover); /* blocks until no job is queued or running */
+int gb_prover_destroy(void *prover);
+/* All instances through a prover service of `workers` threads, largest first; returns the
+ * first non-zero job return code.  Synchronising. */
+int gb_batch_prove(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *insts, int count,
+                   int workers, size_t hbm_budget);
 
 #ifdef __cplusplus
 }

@@ -42,6 +42,7 @@ SIGNATURES = {
     "cuda_get_last_error": (i32, []),
     "cuda_peek_at_last_error": (i32, []),
     "cuda_mem_get_info": (i32, [ctypes.POINTER(sz), ctypes.POINTER(sz)]),
+    "cuda_pool_trim": (i32, [sz]),
     "cuda_set_device": (i32, [i32]),
     "cuda_get_device": (i32, [ctypes.POINTER(i32)]),
     "cuda_get_device_count": (i32, [ctypes.POINTER(i32)]),
@@ -104,6 +105,15 @@ SIGNATURES = {
     "gb_basefold_commitment_info": (i32, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), vp]),
     "gb_basefold_proof_len": (sz, [i32, i32, i32]),
     "gb_basefold_open_ext2": (i32, [vp, vp, vp, ctypes.POINTER(GbTranscript), i32, vp]),
+    "gb_instance_proof_len": (sz, [i32, i32, i32]),
+    "gb_instance_hbm_bytes": (sz, [i32, i32]),
+    "gb_prove_instance": (i32, [vp, vp, i32, vp]),
+    "gb_prover_create": (i32, [vp, vp, i32, i32, sz, ctypes.POINTER(vp)]),
+    "gb_prover_submit": (i32, [vp, vp, ctypes.POINTER(ctypes.c_uint64)]),
+    "gb_prover_wait": (i32, [vp, ctypes.c_uint64, vp]),
+    "gb_prover_drain": (i32, [vp]),
+    "gb_prover_destroy": (i32, [vp]),
+    "gb_batch_prove": (i32, [vp, vp, i32, vp, i32, i32, sz]),
     "almost_goldilocks_cuda_init": (i32, []),
     "ajtai_commit_wide_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
     "ajtai_commit_wide_noalloc_ffi": (i32, [vp, vp, u64, u64, i32, vp]),

@@ -1,0 +1,179 @@
+"""Batched and served proving of many independent instances (native prover service).
+
+An instance is ``degree`` multilinear polynomials of 2^num_vars Goldilocks values, proven by
+Basefold commits, the product sumcheck, and one open_ext2 per polynomial at the sumcheck
+point, on per-instance transcripts (the layout is documented beside ``gb_instance`` in
+include/goldilocks_cuda_wrapper.h).  ``prove_instance`` is the per-call path;
+``batch_prove`` and ``ProverService`` run many instances concurrently on worker threads with
+a stream each, admitted against an HBM budget.  The worker count is tuned by ``autotune``.
+"""
+import ctypes
+import time
+
+import numpy as np
+
+from . import _native as N
+from .basefold import split_proof
+
+P = 0xFFFFFFFF00000001
+LOG_RATE = 1
+
+
+class GbInstance(ctypes.Structure):
+    _fields_ = [("num_vars", ctypes.c_int), ("degree", ctypes.c_int), ("index", ctypes.c_uint64),
+                ("h_polys", ctypes.c_void_p), ("d_polys", ctypes.c_void_p), ("h_proof", ctypes.c_void_p)]
+
+
+class GbJobStats(ctypes.Structure):
+    _fields_ = [("queued_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+def instance_proof_len(num_vars, degree, num_queries):
+    return N.lib().gb_instance_proof_len(num_vars, degree, num_queries)
+
+
+class Instance:
+    """Host-side instance: polys [degree][2^num_vars] (u64, < p) and its proof buffer."""
+
+    def __init__(self, polys, index, num_queries):
+        self.polys = np.ascontiguousarray(np.asarray(polys, dtype=np.uint64))
+        self.degree, size = self.polys.shape
+        self.num_vars = size.bit_length() - 1
+        assert size == 1 << self.num_vars
+        self.index = int(index)
+        self.num_queries = num_queries
+        self.proof = np.zeros(instance_proof_len(self.num_vars, self.degree, num_queries), np.uint64)
+        self.device = None
+
+    def to_device(self):
+        """Keep the polynomials resident in HBM; later proofs read them from there."""
+        from .memory import DeviceBuffer
+        if self.device is None:
+            self.device = DeviceBuffer.from_numpy(self.polys.reshape(-1))
+        return self
+
+    def struct(self):
+        if self.device is not None:
+            return GbInstance(self.num_vars, self.degree, self.index, None, self.device.ptr, self.proof.ctypes.data)
+        return GbInstance(self.num_vars, self.degree, self.index, self.polys.ctypes.data, None,
+                          self.proof.ctypes.data)
+
+    def split(self):
+        return split_instance_proof(self.proof, self.num_vars, self.degree, self.num_queries)
+
+
+def split_instance_proof(proof, n, d, q):
+    o = 0
+
+    def take(k, shape):
+        nonlocal o
+        v = proof[o:o + k].reshape(shape)
+        o += k
+        return v
+
+    roots = take(4 * d, (d, 4))
+    msgs = take(n * (d + 1) * 2, (n, d + 1, 2))
+    ch = take(2 * n, (n, 2))
+    finals = take(2 * d, (d, 2))
+    fe = take(2, (2,))
+    plen = N.lib().gb_basefold_proof_len(n, LOG_RATE, q)
+    opens = [split_proof(take(plen, (plen,)), n, LOG_RATE, q) for _ in range(d)]
+    assert o == proof.size
+    return {"roots": roots, "round_messages": msgs, "challenges": ch, "final_evals": finals, "final_eval": fe,
+            "opens": opens}
+
+
+def _seed(master_seed):
+    return (ctypes.c_uint64 * 2)(int(master_seed[0]), int(master_seed[1]))
+
+
+def prove_instance(table, master_seed, inst):
+    """The per-call path: one instance on the calling thread's stream."""
+    s = inst.struct()
+    N.check(N.lib().gb_prove_instance(table.handle, _seed(master_seed), inst.num_queries, ctypes.byref(s)),
+            "gb_prove_instance")
+    return inst.proof
+
+
+def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30):
+    """All instances through the prover service, largest first."""
+    if not instances:
+        return
+    q = instances[0].num_queries
+    assert all(i.num_queries == q for i in instances)
+    arr = (GbInstance * len(instances))(*[i.struct() for i in instances])
+    N.check(N.lib().gb_batch_prove(table.handle, _seed(master_seed), q, arr, len(instances), workers, hbm_budget),
+            "gb_batch_prove")
+
+
+class ProverService:
+    """Continuous-batching prover: submit instances as they arrive; each runs as soon as a
+    worker is free and its estimated device footprint fits the HBM budget."""
+
+    def __init__(self, table, master_seed, num_queries, workers=8, hbm_budget=64 << 30):
+        self.handle = ctypes.c_void_p()
+        self.num_queries = num_queries
+        N.check(N.lib().gb_prover_create(table.handle, _seed(master_seed), num_queries, workers, hbm_budget,
+                                         ctypes.byref(self.handle)), "gb_prover_create")
+        self._live = {}
+
+    def submit(self, inst):
+        assert inst.num_queries == self.num_queries
+        s = inst.struct()
+        t = ctypes.c_uint64()
+        N.check(N.lib().gb_prover_submit(self.handle, ctypes.byref(s), ctypes.byref(t)), "gb_prover_submit")
+        self._live[t.value] = inst  # keeps the host buffers alive until waited for
+        return t.value
+
+    def wait(self, ticket):
+        st = GbJobStats()
+        rc = N.lib().gb_prover_wait(self.handle, ticket, ctypes.byref(st))
+        inst = self._live.pop(ticket, None)
+        N.check(rc, "gb_prover_wait")
+        return inst, {"queued_ms": st.queued_ms, "run_ms": st.run_ms, "latency_ms": st.latency_ms}
+
+    def close(self):
+        if self.handle:
+            N.lib().gb_prover_drain(self.handle)
+            N.lib().gb_prover_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mixed_workload(count, seed, min_vars=10, max_vars=20, degrees=(2, 3, 4), num_queries=34):
+    """``count`` instances with log2 size uniform over the integers [min_vars, max_vars] and
+    degree uniform over ``degrees``; values uniform in [0, p) from a seeded generator."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(min_vars, max_vars + 1, size=count)
+    degs = rng.choice(np.asarray(degrees), size=count)
+    out = []
+    for k in range(count):
+        polys = rng.integers(0, P, size=(int(degs[k]), 1 << int(sizes[k])), dtype=np.uint64)
+        out.append(Instance(polys, k, num_queries))
+    return out
+
+
+def autotune(table, master_seed, instances, candidates=(1, 2, 4, 8, 12, 16), hbm_budget=64 << 30, repeats=1):
+    """Worker count with the shortest wall time for this batch (measured, after one warm-up
+    run at the largest candidate).  Returns (best_workers, {workers: seconds})."""
+    batch_prove(table, master_seed, instances, max(candidates), hbm_budget)
+    times = {}
+    for w in candidates:
+        best = float("inf")
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            batch_prove(table, master_seed, instances, w, hbm_budget)
+            best = min(best, time.perf_counter() - t0)
+        times[w] = best
+    return min(times, key=times.get), times

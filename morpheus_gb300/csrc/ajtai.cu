@@ -380,17 +380,17 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
 
 // 2D bf16 tensor map, inner dimension contiguous, 64 x 128 boxes with 128-byte swizzle
 static int make_map(CUtensorMap* map, void* base, u64 inner, u64 outer) {
-    static EncodeTiledFn encode = nullptr;
-    if (!encode) {
+    static const EncodeTiledFn encode = [] {  // resolved once (thread-safe static init)
         void* fn = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            !fn) {
-            set_error_msg("cuTensorMapEncodeTiled is not available from the driver");
-            return GB_ECUDA;
-        }
-        encode = (EncodeTiledFn)fn;
+            cudaSuccess)
+            fn = nullptr;
+        return (EncodeTiledFn)fn;
+    }();
+    if (!encode) {
+        set_error_msg("cuTensorMapEncodeTiled is not available from the driver");
+        return GB_ECUDA;
     }
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {inner * 2};

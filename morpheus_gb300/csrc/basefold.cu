@@ -553,21 +553,7 @@ struct DevMem {
     }
 };
 
-static u64* pinned(size_t words) {
-    static thread_local u64* buf = nullptr;
-    static thread_local size_t cap = 0;
-    if (words > cap) {
-        if (buf) cudaFreeHost(buf);
-        size_t c = words < 8192 ? 8192 : words;
-        if (cudaMallocHost(&buf, c * 8) != cudaSuccess) {
-            buf = nullptr;
-            cap = 0;
-            return nullptr;
-        }
-        cap = c;
-    }
-    return buf;
-}
+static u64* pinned(size_t words) { return thread_pinned(1, words); }
 
 #define RC_TRY(x)                 \
     do {                          \

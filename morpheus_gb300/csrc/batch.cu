@@ -1,0 +1,363 @@
+// Batched and served proving of many independent instances.
+//
+// An instance is d multilinear polynomials p_0..p_{d-1} over n variables, proven as
+//   1. Basefold commit of every p_j (roots),
+//   2. the product sumcheck of prod_j p_j over {0,1}^n with Ext2 challenges
+//      (GpuLinearSumcheckProver, zk-torch-3/src/sumcheck/gpu_prover.rs:21-89), on the transcript
+//      Transcript::new("sumcheck") . append_ext2("", master_seed) . append_u64("", index)
+//      . append_u64("", root words of p_0..p_{d-1}),
+//   3. Basefold open_ext2 of every p_j at the sumcheck point, each on its own transcript
+//      Transcript::new("bf-open") . append_ext2("", master_seed) . append_u64("", 8 index + j),
+//      the per-opening transcript of the reference's DAG prover (zk-torch-3/src/dag/mod.rs:1128-1133).
+// Every transcript belongs to one instance, so an instance's proof does not depend on which
+// other instances run beside it.
+//
+// The prover service runs instances on a pool of host worker threads, each launching on a
+// stream of its own, so that the kernels of concurrent instances overlap on the device and
+// one instance's host round trips (transcript challenges between rounds) hide behind the
+// others' kernels.  The reference's DAG prover uses the same shape for its GPU openings
+// (a rayon pool of GPU_OPEN_THREADS_PER_DEVICE = 12 threads per device, largest task first,
+// zk-torch-3/src/dag/mod.rs:1102-1117).  Jobs are admitted against an HBM budget: a job
+// starts when its estimated device footprint fits beside the running ones (the first queued
+// job that fits, in arrival order; a job larger than the whole budget runs alone).
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/goldilocks_cuda_wrapper.h"
+#include "basefold.cuh"
+#include "common.cuh"
+#include "host_field.hpp"
+
+namespace gb {
+
+constexpr int INST_MAX_D = 8;
+constexpr int INST_LOG_RATE = 1;
+
+static size_t inst_proof_len(int n, int d, int q) {
+    size_t sc = (size_t)n * (d + 1) * 2 + (size_t)n * 2 + (size_t)d * 2 + 2;
+    return (size_t)d * 4 + sc + (size_t)d * gb_basefold_proof_len(n, INST_LOG_RATE, q);
+}
+
+// Device bytes one instance holds at its peak: inputs and d commitments (evaluation copy,
+// codeword, tree), the sumcheck's two Ext2 levels, and one opening's workspace.
+static size_t inst_hbm_bytes(int n, int d) {
+    size_t N = (size_t)1 << n;
+    return N * ((size_t)d * (8 + 8 + 16 + 64 + 16) + 144) + ((size_t)1 << 20);
+}
+
+using Clock = std::chrono::steady_clock;
+static double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+// Prove one instance on the calling thread's stream.
+static int prove_instance(void* table, const u64 seed[2], int q, const gb_instance* in) {
+    using namespace host;
+    const int n = in->num_vars, d = in->degree;
+    if (!table || !in || n < 2 || n > 30 || d < 1 || d > INST_MAX_D || (!in->h_polys == !in->d_polys) ||
+        !in->h_proof || q < 0) {
+        set_error_msg("gb_prove_instance: invalid argument");
+        return GB_EINVAL;
+    }
+    cudaStream_t s = stream();
+    const size_t N = (size_t)1 << n;
+    const u64* polys = in->d_polys;
+    u64* owned = nullptr;
+    if (in->h_polys) {
+        GB_CUDA_TRY(cudaMallocAsync(&owned, N * d * 8, s));
+        cudaError_t e = cudaMemcpyAsync(owned, in->h_polys, N * d * 8, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) {
+            cudaFreeAsync(owned, s);
+            set_error("cudaMemcpyAsync", e);
+            return GB_ECUDA;
+        }
+        polys = owned;
+    }
+    u64* out = in->h_proof;
+    u64* roots = out;
+    u64* msgs = roots + (size_t)d * 4;
+    u64* chal = msgs + (size_t)n * (d + 1) * 2;
+    u64* finals = chal + (size_t)n * 2;
+    u64* final_eval = finals + (size_t)d * 2;
+    u64* opens = final_eval + 2;
+    const size_t plen = gb_basefold_proof_len(n, INST_LOG_RATE, q);
+
+    std::vector<void*> com(d, nullptr);
+    int rc = GB_OK;
+    for (int j = 0; j < d && !rc; j++)
+        rc = gb_basefold_commit(polys + (size_t)j * N, nullptr, n, INST_LOG_RATE, &com[j], roots + 4 * j);
+    if (!rc) {
+        gb_transcript t;
+        gb_transcript_new(&t, "sumcheck");
+        tr_append_ext2(&t, "", E2{canon(seed[0]), canon(seed[1])});
+        tr_append_u64(&t, "", in->index);
+        for (int k = 0; k < 4 * d; k++) tr_append_u64(&t, "", roots[k]);
+        rc = gb_sumcheck_prove_ext2(&t, n, d, polys, nullptr, msgs, chal, finals, final_eval);
+    }
+    for (int j = 0; j < d && !rc; j++) {
+        gb_transcript t;
+        gb_transcript_new(&t, "bf-open");
+        tr_append_ext2(&t, "", E2{canon(seed[0]), canon(seed[1])});
+        tr_append_u64(&t, "", 8 * in->index + (u64)j);
+        rc = gb_basefold_open_ext2(com[j], table, chal, &t, q, opens + (size_t)j * plen);
+    }
+    for (int j = 0; j < d; j++)
+        if (com[j]) gb_basefold_commitment_destroy(com[j]);
+    if (owned) cudaFreeAsync(owned, s);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("cudaStreamSynchronize", e);
+            rc = GB_ECUDA;
+        }
+    }
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// prover service
+// ---------------------------------------------------------------------------
+struct Job {
+    gb_instance inst;
+    uint64_t ticket = 0;
+    size_t bytes = 0;
+    int rc = 0;
+    bool done = false;
+    Clock::time_point submitted, started, finished;
+    std::string err;
+};
+
+class Prover {
+  public:
+    Prover(void* table, const u64 seed[2], int q, int workers, size_t budget, int device)
+        : table_(table), q_(q), budget_(budget), device_(device) {
+        seed_[0] = seed[0];
+        seed_[1] = seed[1];
+        for (int w = 0; w < workers; w++) threads_.emplace_back([this] { run(); });
+    }
+    ~Prover() {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+        }
+        cv_work_.notify_all();
+        for (auto& t : threads_) t.join();
+    }
+    int start_error() {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_done_.wait(l, [this] { return ready_ == (int)threads_.size(); });
+        return start_rc_;
+    }
+    uint64_t submit(const gb_instance& in) {
+        auto j = std::make_unique<Job>();
+        j->inst = in;
+        j->bytes = inst_hbm_bytes(in.num_vars, in.degree);
+        j->submitted = Clock::now();
+        std::lock_guard<std::mutex> l(mu_);
+        j->ticket = ++next_ticket_;
+        uint64_t t = j->ticket;
+        queue_.push_back(j.get());
+        jobs_.emplace(t, std::move(j));
+        cv_work_.notify_one();
+        return t;
+    }
+    int wait(uint64_t ticket, gb_job_stats* st) {
+        std::unique_lock<std::mutex> l(mu_);
+        auto it = jobs_.find(ticket);
+        if (it == jobs_.end()) {
+            set_error_msg("gb_prover_wait: unknown ticket");
+            return GB_EINVAL;
+        }
+        Job* j = it->second.get();
+        cv_done_.wait(l, [j] { return j->done; });
+        if (st) {
+            st->queued_ms = ms_between(j->submitted, j->started);
+            st->run_ms = ms_between(j->started, j->finished);
+            st->latency_ms = ms_between(j->submitted, j->finished);
+        }
+        int rc = j->rc;
+        if (rc) set_error_msg(j->err);
+        jobs_.erase(it);
+        return rc;
+    }
+    int drain() {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_done_.wait(l, [this] { return queue_.empty() && running_ == 0; });
+        return GB_OK;
+    }
+
+  private:
+    // the first queued job that fits the budget beside the running ones; a job larger than
+    // the whole budget is taken only when nothing runs
+    Job* take_locked() {
+        for (auto it = queue_.begin(); it != queue_.end(); ++it) {
+            Job* j = *it;
+            if (in_use_ + j->bytes <= budget_ || running_ == 0) {
+                queue_.erase(it);
+                return j;
+            }
+        }
+        return nullptr;
+    }
+    void run() {
+        cudaStream_t st = nullptr;
+        int rc = cudaSetDevice(device_) == cudaSuccess &&
+                         cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess
+                     ? GB_OK
+                     : GB_ECUDA;
+        if (!rc) gb_set_stream(st);
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            if (rc) start_rc_ = rc;
+            ready_++;
+        }
+        cv_done_.notify_all();
+        for (;;) {
+            Job* j = nullptr;
+            {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_work_.wait(l, [&] { return stop_ || (j = take_locked()) != nullptr; });
+                if (!j) break;
+                in_use_ += j->bytes;
+                running_++;
+                j->started = Clock::now();
+            }
+            int jrc = rc ? rc : prove_instance(table_, seed_, q_, &j->inst);
+            std::string err = jrc ? std::string(gb_last_error()) : std::string();
+            {
+                std::lock_guard<std::mutex> l(mu_);
+                j->finished = Clock::now();
+                j->rc = jrc;
+                j->err = err;
+                j->done = true;
+                in_use_ -= j->bytes;
+                running_--;
+            }
+            cv_done_.notify_all();
+            cv_work_.notify_all();  // freed budget may admit a waiting job
+        }
+        if (st) {
+            cudaStreamSynchronize(st);
+            gb_set_stream(nullptr);
+            cudaStreamDestroy(st);
+        }
+    }
+
+    void* table_;
+    u64 seed_[2];
+    int q_;
+    size_t budget_;
+    int device_;
+    std::mutex mu_;
+    std::condition_variable cv_work_, cv_done_;
+    std::deque<Job*> queue_;
+    std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs_;
+    std::vector<std::thread> threads_;
+    uint64_t next_ticket_ = 0;
+    size_t in_use_ = 0;
+    int running_ = 0, ready_ = 0, start_rc_ = 0;
+    bool stop_ = false;
+};
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+size_t gb_instance_proof_len(int num_vars, int degree, int num_queries) {
+    return inst_proof_len(num_vars, degree, num_queries);
+}
+
+size_t gb_instance_hbm_bytes(int num_vars, int degree) { return inst_hbm_bytes(num_vars, degree); }
+
+int gb_prove_instance(void* table, const uint64_t master_seed[2], int num_queries, const gb_instance* inst) {
+    if (!master_seed) return GB_EINVAL;
+    return prove_instance(table, master_seed, num_queries, inst);
+}
+
+int gb_prover_create(void* table, const uint64_t master_seed[2], int num_queries, int workers, size_t hbm_budget,
+                     void** handle) {
+    if (!table || !master_seed || !handle || workers < 1 || workers > 256 || num_queries < 0) {
+        set_error_msg("gb_prover_create: invalid argument");
+        return GB_EINVAL;
+    }
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    Prover* p = new Prover(table, master_seed, num_queries, workers, hbm_budget, dev);
+    int rc = p->start_error();
+    if (rc) {
+        delete p;
+        set_error_msg("gb_prover_create: a worker could not create its stream");
+        return rc;
+    }
+    *handle = p;
+    return GB_OK;
+}
+
+int gb_prover_submit(void* prover, const gb_instance* inst, uint64_t* ticket) {
+    if (!prover || !inst || !ticket) return GB_EINVAL;
+    const int n = inst->num_vars, d = inst->degree;
+    if (n < 2 || n > 30 || d < 1 || d > INST_MAX_D || (!inst->h_polys == !inst->d_polys) || !inst->h_proof) {
+        set_error_msg("gb_prover_submit: invalid instance");
+        return GB_EINVAL;
+    }
+    *ticket = static_cast<Prover*>(prover)->submit(*inst);
+    return GB_OK;
+}
+
+int gb_prover_wait(void* prover, uint64_t ticket, gb_job_stats* stats) {
+    if (!prover) return GB_EINVAL;
+    return static_cast<Prover*>(prover)->wait(ticket, stats);
+}
+
+int gb_prover_drain(void* prover) {
+    if (!prover) return GB_EINVAL;
+    return static_cast<Prover*>(prover)->drain();
+}
+
+int gb_prover_destroy(void* prover) {
+    if (!prover) return GB_EINVAL;
+    delete static_cast<Prover*>(prover);
+    return GB_OK;
+}
+
+int gb_batch_prove(void* table, const uint64_t master_seed[2], int num_queries, const gb_instance* insts, int count,
+                   int workers, size_t hbm_budget) {
+    if (count < 0 || (count > 0 && !insts)) return GB_EINVAL;
+    if (count == 0) return GB_OK;
+    void* h = nullptr;
+    int rc = gb_prover_create(table, master_seed, num_queries, workers, hbm_budget, &h);
+    if (rc) return rc;
+    // largest instance first: the long ones start early and the small ones fill in behind
+    std::vector<int> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return inst_hbm_bytes(insts[a].num_vars, insts[a].degree) > inst_hbm_bytes(insts[b].num_vars, insts[b].degree);
+    });
+    std::vector<uint64_t> tickets(count, 0);
+    for (int k = 0; k < count && !rc; k++) rc = gb_prover_submit(h, &insts[order[k]], &tickets[k]);
+    int first = rc;
+    std::string msg = rc ? std::string(gb_last_error()) : std::string();
+    for (int k = 0; k < count; k++) {
+        if (!tickets[k]) continue;
+        int r = gb_prover_wait(h, tickets[k], nullptr);
+        if (r && !first) {
+            first = r;
+            msg = gb_last_error();
+        }
+    }
+    gb_prover_destroy(h);
+    if (first) set_error_msg(msg);
+    return first;
+}
+
+}  // extern "C"

@@ -18,6 +18,9 @@ cudaStream_t stream();
 void set_error(const char* where, cudaError_t e);
 void set_error_msg(const std::string& msg);
 int num_sms();
+// Pinned host staging of the calling thread: slot 0 sumcheck, slot 1 Basefold.
+constexpr int PINNED_SLOTS = 2;
+uint64_t* thread_pinned(int slot, size_t words);
 
 // Return-code conventions of the reference C ABI (goldilocks-cuda-rs/cuda/wrapper.cu):
 // 0 ok, -1 CUDA error; -2 invalid argument and -3 unsupported option are this

@@ -2,7 +2,9 @@
 // device entry points (goldilocks-cuda-rs/src/ffi.rs:11-26, :306-309), batch
 // field ops and host transcript helpers.
 #include <atomic>
+#include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/goldilocks_cuda_wrapper.h"
@@ -17,7 +19,66 @@ static thread_local std::string t_err;
 static std::atomic<unsigned long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
-cudaStream_t stream() { return t_stream; }
+// The stream-ordered pool behind cudaMallocAsync defaults to a release threshold of 0: it
+// hands its memory back to the driver at every synchronisation, and the next allocation maps
+// it again.  Like the reference (almost-goldilocks-cuda-rs/cuda/wrapper.cu:151-166), let the
+// pool keep what it holds; cuda_pool_trim releases it explicitly.  Done once per device, on
+// the first launch-stream lookup with that device current.
+static void keep_pool_memory() {
+    constexpr int MAX_DEVICES = 64;
+    static thread_local uint64_t t_done = 0;  // devices this thread has seen configured
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return;
+    if (t_done & (1ull << dev)) return;
+    static std::mutex mu;
+    static bool done[MAX_DEVICES] = {};
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!done[dev]) {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+                uint64_t thr = UINT64_MAX;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+            }
+            done[dev] = true;
+        }
+    }
+    t_done |= 1ull << dev;
+}
+
+cudaStream_t stream() {
+    keep_pool_memory();
+    return t_stream;
+}
+
+// Pinned host staging owned by the calling thread, one buffer per slot, released when the
+// thread exits (worker threads of the prover service come and go).
+namespace {
+struct PinnedSlots {
+    uint64_t* buf[PINNED_SLOTS] = {};
+    size_t cap[PINNED_SLOTS] = {};
+    ~PinnedSlots() {
+        for (int i = 0; i < PINNED_SLOTS; i++)
+            if (buf[i]) cudaFreeHost(buf[i]);
+    }
+};
+}  // namespace
+
+uint64_t* thread_pinned(int slot, size_t words) {
+    static thread_local PinnedSlots t;
+    if (slot < 0 || slot >= PINNED_SLOTS) return nullptr;
+    if (words > t.cap[slot]) {
+        if (t.buf[slot]) cudaFreeHost(t.buf[slot]);
+        size_t c = words < 8192 ? 8192 : words;
+        if (cudaMallocHost(&t.buf[slot], c * 8) != cudaSuccess) {
+            t.buf[slot] = nullptr;
+            t.cap[slot] = 0;
+            return nullptr;
+        }
+        t.cap[slot] = c;
+    }
+    return t.buf[slot];
+}
 
 void set_error(const char* where, cudaError_t e) {
     t_err = std::string(where) + ": " + cudaGetErrorString(e);
@@ -143,6 +204,12 @@ int cuda_device_synchronize(void) { return cudaDeviceSynchronize() == cudaSucces
 int cuda_get_last_error(void) { return (int)cudaGetLastError(); }
 int cuda_peek_at_last_error(void) { return (int)cudaPeekAtLastError(); }
 int cuda_mem_get_info(size_t* f, size_t* t) { return cudaMemGetInfo(f, t) == cudaSuccess ? 0 : -1; }
+int cuda_pool_trim(size_t min_bytes_to_keep) {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return -1;
+    return cudaMemPoolTrimTo(pool, min_bytes_to_keep) == cudaSuccess ? 0 : -1;
+}
 int cuda_set_device(int d) { return cudaSetDevice(d) == cudaSuccess ? 0 : -1; }
 int cuda_get_device(int* d) { return cudaGetDevice(d) == cudaSuccess ? 0 : -1; }
 int cuda_get_device_count(int* c) { return cudaGetDeviceCount(c) == cudaSuccess ? 0 : -1; }

@@ -361,21 +361,7 @@ static unsigned round_grid(size_t work) {
 }
 
 // Pinned host staging reused by the calling thread.
-static u64* pinned_staging(size_t words) {
-    static thread_local u64* buf = nullptr;
-    static thread_local size_t cap = 0;
-    if (words > cap) {
-        if (buf) cudaFreeHost(buf);
-        size_t c = words < 4096 ? 4096 : words;
-        if (cudaMallocHost(&buf, c * 8) != cudaSuccess) {
-            buf = nullptr;
-            cap = 0;
-            return nullptr;
-        }
-        cap = c;
-    }
-    return buf;
-}
+static u64* pinned_staging(size_t words) { return thread_pinned(0, words); }
 
 // Device workspace of one proof.
 struct ScWork {
