@@ -45,31 +45,101 @@ __device__ __forceinline__ u64 gl_neg(u64 a) {
     return a ? GL_P - a : 0;
 }
 
-// 128-bit x = lo + 2^64 (h1 2^32 + h0) == lo - h1 + h0 (2^32 - 1)   (2^96 == -1 mod p)
-__device__ __forceinline__ u64 gl_reduce(u64 lo, u64 hi) {
-    u64 h1 = hi >> 32;
-    u64 h0 = hi & GL_EPS;
-    u64 t0 = lo - h1;
-    if (lo < h1) t0 -= GL_EPS;
-    u64 t1 = (h0 << 32) - h0;
-    u64 r = t0 + t1;
-    if (r < t1) r += GL_EPS;
-    return r;
+// Full 64 x 64 -> 128-bit product from 32-bit multiply-adds with carry chains (full-rate
+// IMAD work; the 64-bit multiply-high would go through the slower wide-multiply path).
+__device__ __forceinline__ void gl_mul128(u64 a, u64 b, u64& lo, u64& hi) {
+    u32 a0 = (u32)a, a1 = (u32)(a >> 32), b0 = (u32)b, b1 = (u32)(b >> 32);
+    u32 r0, r1, r2, r3;
+    asm("{\n\t"
+        "mul.lo.u32 %0, %4, %6;\n\t"
+        "mul.hi.u32 %1, %4, %6;\n\t"
+        "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+        "madc.hi.u32 %2, %4, %7, 0;\n\t"
+        "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+        "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+        "madc.hi.u32 %3, %5, %7, 0;\n\t"
+        "mad.lo.cc.u32 %2, %5, %7, %2;\n\t"
+        "addc.u32 %3, %3, 0;\n\t"
+        "}"
+        : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+        : "r"(a0), "r"(a1), "r"(b0), "r"(b1));
+    lo = ((u64)r1 << 32) | r0;
+    hi = ((u64)r3 << 32) | r2;
 }
 
-__device__ __forceinline__ u64 gl_mul(u64 a, u64 b) { return gl_reduce(a * b, __umul64hi(a, b)); }
+// 128-bit x = lo + 2^64 (h1 2^32 + h0) == lo - h1 + h0 (2^32 - 1)   (2^96 == -1 mod p),
+// with 32-bit carry chains: a borrow of lo - h1 is worth -EPS, a carry of the final sum +EPS
+// (neither correction can wrap again).  Any (lo, hi) in, a u64 congruent to x out.
+__device__ __forceinline__ u64 gl_reduce(u64 lo, u64 hi) {
+    u32 l0 = (u32)lo, l1 = (u32)(lo >> 32), h0 = (u32)hi, h1 = (u32)(hi >> 32);
+    u32 s0, s1;
+    asm("{\n\t.reg .u32 b, t0, t1, c, m;\n\t"
+        "sub.cc.u32 %0, %2, %5;\n\t"
+        "subc.cc.u32 %1, %3, 0;\n\t"
+        "subc.u32 b, 0, 0;\n\t"
+        "sub.cc.u32 %0, %0, b;\n\t"
+        "subc.u32 %1, %1, 0;\n\t"
+        "sub.cc.u32 t0, 0, %4;\n\t"
+        "subc.u32 t1, %4, 0;\n\t"
+        "add.cc.u32 %0, %0, t0;\n\t"
+        "addc.cc.u32 %1, %1, t1;\n\t"
+        "addc.u32 c, 0, 0;\n\t"
+        "sub.u32 m, 0, c;\n\t"
+        "add.cc.u32 %0, %0, m;\n\t"
+        "addc.u32 %1, %1, 0;\n\t}"
+        : "=r"(s0), "=r"(s1)
+        : "r"(l0), "r"(l1), "r"(h0), "r"(h1));
+    return ((u64)s1 << 32) | s0;
+}
 
-// x^2 from 32-bit limbs: x0^2 + 2 x0 x1 2^32 + x1^2 2^64 (three wide multiplies).
-__device__ __forceinline__ u64 gl_sqr(u64 x) {
-    u32 x0 = (u32)x, x1 = (u32)(x >> 32);
-    u64 p00 = (u64)x0 * x0;
-    u64 p01 = (u64)x0 * x1;
-    u64 p11 = (u64)x1 * x1;
-    // cross = 2 * p01 is up to 65 bits
-    u64 c_lo = p01 << 33;
-    u64 c_hi = p01 >> 31;
-    u64 lo = p00 + c_lo;
-    u64 hi = p11 + c_hi + (lo < p00 ? 1ull : 0ull);
+__device__ __forceinline__ u64 gl_mul(u64 a, u64 b) {
+    u64 lo, hi;
+    gl_mul128(a, b, lo, hi);
+    return gl_reduce(lo, hi);
+}
+
+__device__ __forceinline__ u64 gl_sqr(u64 x) { return gl_mul(x, x); }
+
+// ---------------------------------------------------------------------------
+// Lazy sums: lo + 2^64 hi with a small hi, reduced once (linear layers, dot products).
+// ---------------------------------------------------------------------------
+struct glw {
+    u64 lo;
+    u32 hi;
+};
+__device__ __forceinline__ glw glw_of(u64 x) {
+    glw r;
+    r.lo = x;
+    r.hi = 0u;
+    return r;
+}
+__device__ __forceinline__ glw glw_add(glw a, glw b) {
+    glw r;
+    asm("add.cc.u64 %0, %2, %4;\n\taddc.u32 %1, %3, %5;"
+        : "=l"(r.lo), "=r"(r.hi)
+        : "l"(a.lo), "r"(a.hi), "l"(b.lo), "r"(b.hi));
+    return r;
+}
+__device__ __forceinline__ glw glw_add(glw a, u64 b) {
+    glw r;
+    asm("add.cc.u64 %0, %2, %4;\n\taddc.u32 %1, %3, 0;" : "=l"(r.lo), "=r"(r.hi) : "l"(a.lo), "r"(a.hi), "l"(b));
+    return r;
+}
+// lo + hi EPS for hi < 2^32: one carry at most, worth EPS, after which no carry is possible
+// (the wrapped sum is below hi EPS <= 2^64 - 2^32)
+__device__ __forceinline__ u64 glw_reduce(glw a) {
+    u64 t = ((u64)a.hi << 32) - a.hi;
+    u64 r;
+    u32 c;
+    asm("add.cc.u64 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=l"(r), "=r"(c) : "l"(a.lo), "l"(t));
+    return r + (u64)(0u - c);
+}
+// a b + c reduced, for b < p: the product's high word is then below 2^64 - 2^32, so adding
+// c (hi < 2^32) cannot carry out of 128 bits
+__device__ __forceinline__ u64 gl_mul_add(u64 a, u64 b, glw c) {
+    u64 lo, hi;
+    gl_mul128(a, b, lo, hi);
+    asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(c.lo), "l"((u64)c.hi));
     return gl_reduce(lo, hi);
 }
 

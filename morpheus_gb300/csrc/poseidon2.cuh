@@ -53,6 +53,11 @@ struct P2Const {
     static constexpr u64 inner[22] = GB_P2_RC_INT;
     static constexpr u64 diag[8] = GB_P2_DIAG;
 };
+// p2_permute's multiply-add needs every diagonal entry below p
+static_assert(P2Const::diag[0] < GL_P && P2Const::diag[1] < GL_P && P2Const::diag[2] < GL_P &&
+                  P2Const::diag[3] < GL_P && P2Const::diag[4] < GL_P && P2Const::diag[5] < GL_P &&
+                  P2Const::diag[6] < GL_P && P2Const::diag[7] < GL_P,
+              "internal diagonal must be canonical");
 
 __device__ __forceinline__ u64 p2_rc_ext(int r, int i) {
     constexpr u64 t[8][8] = GB_P2_RC_EXT;
@@ -74,45 +79,86 @@ __device__ __forceinline__ u64 p2_sbox(u64 x) {
     return gl_mul(x4, x3);
 }
 
-__device__ __forceinline__ void p2_external_linear(u64* s) {
+// External linear layer on the S-box outputs x, with lazy sums: per half the circulant
+// [2 3 1 1] (each output a sum of the half's inputs with coefficients 1..3), then each
+// output plus the column sum of both halves; add[i] (the next round's constant) is folded
+// into the same sum, and each output is reduced once (its high part is at most 21 + 1).
+__device__ __forceinline__ void p2_external_linear_add(u64* x, const u64* add, bool has_add) {
+    glw o[8];
 #pragma unroll
     for (int h = 0; h < 8; h += 4) {
-        u64 a = s[h], b = s[h + 1], c = s[h + 2], d = s[h + 3];
-        u64 ab = gl_add(a, b), cd = gl_add(c, d);
-        u64 all = gl_add(ab, cd);
-        u64 all_b = gl_add(all, b), all_d = gl_add(all, d);
-        s[h] = gl_add(all_b, ab);
-        s[h + 1] = gl_add(all_b, gl_double(c));
-        s[h + 2] = gl_add(all_d, cd);
-        s[h + 3] = gl_add(all_d, gl_double(a));
+        glw a = glw_of(x[h]), b = glw_of(x[h + 1]), c = glw_of(x[h + 2]), d = glw_of(x[h + 3]);
+        glw t01 = glw_add(a, b), t23 = glw_add(c, d);
+        glw t0123 = glw_add(t01, t23);
+        glw t01123 = glw_add(t0123, b), t01233 = glw_add(t0123, d);
+        o[h] = glw_add(t01123, t01);                 // 2a + 3b + c + d
+        o[h + 1] = glw_add(t01123, glw_add(c, c));   // a + 2b + 3c + d
+        o[h + 2] = glw_add(t01233, t23);             // a + b + 2c + 3d
+        o[h + 3] = glw_add(t01233, glw_add(a, a));   // 3a + b + c + 2d
     }
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        u64 col = gl_add(s[i], s[i + 4]);
-        s[i] = gl_add(s[i], col);
-        s[i + 4] = gl_add(s[i + 4], col);
+        glw col = glw_add(o[i], o[i + 4]);
+        glw u = glw_add(o[i], col), v = glw_add(o[i + 4], col);
+        if (has_add) {
+            u = glw_add(u, add[i]);
+            v = glw_add(v, add[i + 4]);
+        }
+        x[i] = glw_reduce(u);
+        x[i + 4] = glw_reduce(v);
     }
 }
 
+// The permutation with every round constant folded into the preceding linear layer:
+//   external round r: s <- E(sbox(s + rc_ext[r]));  internal round r: s0 <- sbox(s0 + rc_int[r]),
+//   s_i <- diag_i s_i + sum(s) -- computed as one multiply-add per lane with the sum (and the
+//   next round's constant) unreduced.
 __device__ __forceinline__ void p2_permute(u64* s) {
+    u64 rc[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) s[i] = p2_sbox(glw_reduce(glw_add(glw_of(s[i]), p2_rc_ext(0, i))));
 #pragma unroll
     for (int r = 0; r < 4; r++) {
+        if (r < 3) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) s[i] = p2_sbox(gl_add(s[i], p2_rc_ext(r, i)));
-        p2_external_linear(s);
+            for (int i = 0; i < 8; i++) rc[i] = p2_rc_ext(r + 1, i);
+            p2_external_linear_add(s, rc, true);
+#pragma unroll
+            for (int i = 0; i < 8; i++) s[i] = p2_sbox(s[i]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; i++) rc[i] = i == 0 ? p2_rc_int(0) : 0;
+            p2_external_linear_add(s, rc, true);
+        }
     }
+    // internal rounds; s[0] already holds s0 + rc_int[r]
 #pragma unroll
     for (int r = 0; r < 22; r++) {
-        s[0] = p2_sbox(gl_add(s[0], p2_rc_int(r)));
-        u64 sum = gl_add(gl_add(gl_add(s[0], s[1]), gl_add(s[2], s[3])), gl_add(gl_add(s[4], s[5]), gl_add(s[6], s[7])));
+        s[0] = p2_sbox(s[0]);
+        glw sum = glw_add(glw_add(glw_add(glw_of(s[0]), glw_of(s[1])), glw_add(glw_of(s[2]), glw_of(s[3]))),
+                          glw_add(glw_add(glw_of(s[4]), glw_of(s[5])), glw_add(glw_of(s[6]), glw_of(s[7]))));
+        if (r < 21) {
+            s[0] = gl_mul_add(s[0], p2_diag(0), glw_add(sum, p2_rc_int(r + 1)));
 #pragma unroll
-        for (int i = 0; i < 8; i++) s[i] = gl_add(gl_mul(s[i], p2_diag(i)), sum);
+            for (int i = 1; i < 8; i++) s[i] = gl_mul_add(s[i], p2_diag(i), sum);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; i++) s[i] = gl_mul_add(s[i], p2_diag(i), glw_add(sum, p2_rc_ext(4, i)));
+        }
     }
 #pragma unroll
-    for (int r = 4; r < 8; r++) {
+    for (int i = 0; i < 8; i++) s[i] = p2_sbox(s[i]);
 #pragma unroll
-        for (int i = 0; i < 8; i++) s[i] = p2_sbox(gl_add(s[i], p2_rc_ext(r, i)));
-        p2_external_linear(s);
+    for (int r = 4; r < 8; r++) {
+        if (r < 7) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) rc[i] = p2_rc_ext(r + 1, i);
+            p2_external_linear_add(s, rc, true);
+#pragma unroll
+            for (int i = 0; i < 8; i++) s[i] = p2_sbox(s[i]);
+        } else {
+            p2_external_linear_add(s, rc, false);
+        }
     }
 }
 
