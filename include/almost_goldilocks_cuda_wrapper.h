@@ -43,6 +43,8 @@ int ajtai_commit_wide_ffi(const uint32_t *d_key, const uint64_t *d_z_wide, uint6
  * Synchronising. */
 int gb_ajtai_key_create(const uint32_t *h_seed, int row_lo, int rows, uint64_t n_ring, void **handle);
 int gb_ajtai_key_destroy(void *handle);
+/* The key's first row, row count and ring columns (any output pointer may be NULL). */
+int gb_ajtai_key_info(void *handle, int *row_lo, int *rows, uint64_t *n_ring);
 /* Commit num_witnesses witnesses with coefficients in [0, 256): d_z is [num_witnesses][n_ring * 64]
  * bytes (device); d_out is [num_witnesses][rows][64] canonical u64 (device).  Rows are those of
  * the key; the result equals ajtai_commit_wide_ffi restricted to those rows.  Synchronising. */

@@ -167,6 +167,10 @@ void gb_transcript_challenge_ext2(gb_transcript *t, const char *label, uint64_t 
  * h_final_eval[2].  Synchronising. */
 int gb_sumcheck_prove_ext2(gb_transcript *t, int n, int d, const uint64_t *d_polys, const uint64_t *h_polys,
                            uint64_t *h_msgs, uint64_t *h_challenges, uint64_t *h_finals, uint64_t *h_final_eval);
+/* CpuLinearSumcheckProverExt2::{new, prove} semantics (zk-torch-3/src/sumcheck/cpu_ext2_prover.rs:21-110):
+ * as gb_sumcheck_prove_ext2 but the polynomials are Ext2, [d][2^n][c0, c1]. */
+int gb_sumcheck_prove_ext2_polys(gb_transcript *t, int n, int d, const uint64_t *d_polys, const uint64_t *h_polys,
+                                 uint64_t *h_msgs, uint64_t *h_challenges, uint64_t *h_finals, uint64_t *h_final_eval);
 /* One fused round as a device building block: fold d polynomials (base-field input when
  * in_base, element stride in_stride) with the Ext2 challenge (r0, r1) into d_out (Ext2,
  * stride out_stride), producing pairs_out output pairs per polynomial, and write the next
@@ -255,6 +259,35 @@ int gb_prover_destroy(void *prover);
  * first non-zero job return code.  Synchronising. */
 int gb_batch_prove(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *insts, int count,
                    int workers, size_t hbm_budget);
+
+/* A quantized matmul layer C = A B as a served job (no reference counterpart; the field work
+ * of zk-torch-3/src/basicblock/einsum.rs:807-1000): A is m x k, B is k x n (row-major int8),
+ * m, n, k powers of two with m k >= 2^16.  The proof (gb_matmul_proof_len words, canonical):
+ * roots of A and B [2][4], claim C~(r_i, r_j) [2], sumcheck over the log k variables of the
+ * inner index: msgs[log k][3][2], challenges r_k[log k][2], finals [2][2], final_eval [2]; then
+ * open_ext2 proofs of A at (r_k, r_i) and of B at (r_j, r_k) (log_rate 1); then the Ajtai
+ * commitment [16][64] of the first 2^16 entries of A as bytes v + 128 under the attached key.
+ * r_i, r_j are Ext2 challenges of Transcript::new("matmul") + append_ext2("", master_seed) +
+ * append_u64("", index), ("", m), ("", n), ("", k), the 8 root words ("" each); the sumcheck
+ * continues on that transcript; the openings use "bf-open" transcripts with 8 index + 0 / 1. */
+typedef struct gb_matmul_job {
+    int m, n, k;
+    uint64_t index;
+    const int8_t *h_a; /* m x k (host) */
+    const int8_t *h_b; /* k x n (host) */
+    uint64_t *h_proof; /* output (host) */
+} gb_matmul_job;
+
+size_t gb_matmul_proof_len(int m, int n, int k, int num_queries);
+size_t gb_matmul_hbm_bytes(int m, int n, int k);
+/* One matmul job on the calling thread's stream.  table: log_rate 1, covering log(m k) and
+ * log(k n) variables; ajtai_key: a gb_ajtai_key_create handle of 16 rows over 1024 ring columns.
+ * Synchronising. */
+int gb_prove_matmul(void *table, void *ajtai_key, const uint64_t master_seed[2], int num_queries,
+                    const gb_matmul_job *job);
+/* Attach the Ajtai key used by the service's matmul jobs (before submitting any). */
+int gb_prover_set_ajtai_key(void *prover, void *ajtai_key);
+int gb_prover_submit_matmul(void *prover, const gb_matmul_job *job, uint64_t *ticket); /* non-blocking */
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,7 @@ SIGNATURES = {
     "gb_transcript_append_ext2": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64p]),
     "gb_transcript_challenge_ext2": (None, [ctypes.POINTER(GbTranscript), ctypes.c_char_p, u64p]),
     "gb_sumcheck_prove_ext2": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
+    "gb_sumcheck_prove_ext2_polys": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
     "gb_sumcheck_prove_base": (i32, [ctypes.POINTER(GbTranscript), i32, i32, vp, vp, vp, vp, vp, vp]),
     "gb_sumcheck_round_workspace_words": (sz, []),
     "gb_sumcheck_fold_round_ext2": (i32, [vp, i32, sz, vp, sz, i32, sz, u64, u64, vp, vp]),
@@ -114,11 +115,17 @@ SIGNATURES = {
     "gb_prover_drain": (i32, [vp]),
     "gb_prover_destroy": (i32, [vp]),
     "gb_batch_prove": (i32, [vp, vp, i32, vp, i32, i32, sz]),
+    "gb_matmul_proof_len": (sz, [i32, i32, i32, i32]),
+    "gb_matmul_hbm_bytes": (sz, [i32, i32, i32]),
+    "gb_prove_matmul": (i32, [vp, vp, vp, i32, vp]),
+    "gb_prover_set_ajtai_key": (i32, [vp, vp]),
+    "gb_prover_submit_matmul": (i32, [vp, vp, ctypes.POINTER(ctypes.c_uint64)]),
     "almost_goldilocks_cuda_init": (i32, []),
     "ajtai_commit_wide_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
     "ajtai_commit_wide_noalloc_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
     "gb_ajtai_key_create": (i32, [vp, i32, i32, u64, ctypes.POINTER(vp)]),
     "gb_ajtai_key_destroy": (i32, [vp]),
+    "gb_ajtai_key_info": (i32, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(u64)]),
     "gb_ajtai_commit_u8_batched": (i32, [vp, vp, i32, vp]),
 }
 

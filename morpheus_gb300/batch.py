@@ -24,6 +24,11 @@ class GbInstance(ctypes.Structure):
                 ("h_polys", ctypes.c_void_p), ("d_polys", ctypes.c_void_p), ("h_proof", ctypes.c_void_p)]
 
 
+class GbMatmulJob(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_int), ("n", ctypes.c_int), ("k", ctypes.c_int), ("index", ctypes.c_uint64),
+                ("h_a", ctypes.c_void_p), ("h_b", ctypes.c_void_p), ("h_proof", ctypes.c_void_p)]
+
+
 class GbJobStats(ctypes.Structure):
     _fields_ = [("queued_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
 
@@ -60,6 +65,70 @@ class Instance:
 
     def split(self):
         return split_instance_proof(self.proof, self.num_vars, self.degree, self.num_queries)
+
+
+class MatmulJob:
+    """A quantized matmul layer C = A B as a proof job: A [m][k] and B [k][n] int8 (host)."""
+
+    def __init__(self, a, b, index, num_queries):
+        self.a = np.ascontiguousarray(np.asarray(a, dtype=np.int8))
+        self.b = np.ascontiguousarray(np.asarray(b, dtype=np.int8))
+        self.m, self.k = self.a.shape
+        k2, self.n = self.b.shape
+        assert k2 == self.k
+        self.index = int(index)
+        self.num_queries = num_queries
+        length = N.lib().gb_matmul_proof_len(self.m, self.n, self.k, num_queries)
+        if length == 0:
+            raise ValueError("m, n, k must be powers of two (k >= 2)")
+        self.proof = np.zeros(length, np.uint64)
+
+    def struct(self):
+        return GbMatmulJob(self.m, self.n, self.k, self.index, self.a.ctypes.data, self.b.ctypes.data,
+                           self.proof.ctypes.data)
+
+    def split(self):
+        lm, ln, lk = (self.m.bit_length() - 1, self.n.bit_length() - 1, self.k.bit_length() - 1)
+        p, o = self.proof, 0
+
+        def take(k, shape):
+            nonlocal o
+            v = p[o:o + k].reshape(shape)
+            o += k
+            return v
+
+        q = self.num_queries
+        out = {"roots": take(8, (2, 4)), "claim": take(2, (2,)), "round_messages": take(lk * 6, (lk, 3, 2)),
+               "challenges": take(lk * 2, (lk, 2)), "final_evals": take(4, (2, 2)), "final_eval": take(2, (2,))}
+        la = N.lib().gb_basefold_proof_len(lm + lk, LOG_RATE, q)
+        lb = N.lib().gb_basefold_proof_len(lk + ln, LOG_RATE, q)
+        out["open_a"] = take(la, (la,))
+        out["open_b"] = take(lb, (lb,))
+        out["ajtai"] = take(16 * 64, (16, 64))
+        assert o == p.size
+        return out
+
+
+def prove_matmul(table, ajtai_key, master_seed, job):
+    """The per-call path for one matmul job."""
+    s = job.struct()
+    N.check(N.lib().gb_prove_matmul(table.handle, ajtai_key.handle, _seed(master_seed), job.num_queries,
+                                    ctypes.byref(s)), "gb_prove_matmul")
+    return job.proof
+
+
+def matmul_stream(count, seed, rate_per_s=200.0, dims=(256, 512, 1024, 4096), num_queries=34):
+    """``count`` matmul jobs with M, N, K uniform over ``dims``, int8 values uniform in
+    [-128, 127], and Poisson arrival times (seconds from 0) of mean rate ``rate_per_s``."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=count))
+    jobs = []
+    for k in range(count):
+        m, n, kk = (int(x) for x in rng.choice(np.asarray(dims), size=3))
+        a = rng.integers(-128, 128, size=(m, kk), dtype=np.int8)
+        b = rng.integers(-128, 128, size=(kk, n), dtype=np.int8)
+        jobs.append(MatmulJob(a, b, k, num_queries))
+    return jobs, arrivals
 
 
 def split_instance_proof(proof, n, d, q):
@@ -117,12 +186,22 @@ class ProverService:
                                          ctypes.byref(self.handle)), "gb_prover_create")
         self._live = {}
 
-    def submit(self, inst):
-        assert inst.num_queries == self.num_queries
-        s = inst.struct()
+    def set_ajtai_key(self, key):
+        """Key for matmul jobs (an AjtaiKey of 16 rows over 1024 ring columns)."""
+        self._key = key
+        N.check(N.lib().gb_prover_set_ajtai_key(self.handle, key.handle), "gb_prover_set_ajtai_key")
+
+    def submit(self, job):
+        """Submit an Instance or a MatmulJob; returns its ticket."""
+        assert job.num_queries == self.num_queries
+        s = job.struct()
         t = ctypes.c_uint64()
-        N.check(N.lib().gb_prover_submit(self.handle, ctypes.byref(s), ctypes.byref(t)), "gb_prover_submit")
-        self._live[t.value] = inst  # keeps the host buffers alive until waited for
+        if isinstance(job, MatmulJob):
+            N.check(N.lib().gb_prover_submit_matmul(self.handle, ctypes.byref(s), ctypes.byref(t)),
+                    "gb_prover_submit_matmul")
+        else:
+            N.check(N.lib().gb_prover_submit(self.handle, ctypes.byref(s), ctypes.byref(t)), "gb_prover_submit")
+        self._live[t.value] = job  # keeps the host buffers alive until waited for
         return t.value
 
     def wait(self, ticket):

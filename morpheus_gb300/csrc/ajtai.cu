@@ -674,6 +674,15 @@ int gb_ajtai_key_destroy(void* handle) {
     return GB_OK;
 }
 
+int gb_ajtai_key_info(void* handle, int* row_lo, int* rows, uint64_t* n_ring) {
+    AjtaiKey* k = (AjtaiKey*)handle;
+    if (!k) return GB_EINVAL;
+    if (row_lo) *row_lo = k->row_lo;
+    if (rows) *rows = k->rows;
+    if (n_ring) *n_ring = k->N;
+    return GB_OK;
+}
+
 int gb_ajtai_commit_u8_batched(void* handle, const uint8_t* d_z, int num_witnesses, uint64_t* d_out) {
     AjtaiKey* k = (AjtaiKey*)handle;
     if (!k || !d_z || !d_out) return GB_EINVAL;

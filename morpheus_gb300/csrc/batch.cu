@@ -126,7 +126,9 @@ static int prove_instance(void* table, const u64 seed[2], int q, const gb_instan
 // prover service
 // ---------------------------------------------------------------------------
 struct Job {
+    int kind = 0;  // 0: instance, 1: matmul layer
     gb_instance inst;
+    gb_matmul_job mm;
     uint64_t ticket = 0;
     size_t bytes = 0;
     int rc = 0;
@@ -156,10 +158,24 @@ class Prover {
         cv_done_.wait(l, [this] { return ready_ == (int)threads_.size(); });
         return start_rc_;
     }
+    void set_ajtai_key(void* key) {
+        std::lock_guard<std::mutex> l(mu_);
+        ajtai_key_ = key;
+    }
     uint64_t submit(const gb_instance& in) {
         auto j = std::make_unique<Job>();
         j->inst = in;
         j->bytes = inst_hbm_bytes(in.num_vars, in.degree);
+        return enqueue(std::move(j));
+    }
+    uint64_t submit(const gb_matmul_job& mm) {
+        auto j = std::make_unique<Job>();
+        j->kind = 1;
+        j->mm = mm;
+        j->bytes = gb_matmul_hbm_bytes(mm.m, mm.n, mm.k);
+        return enqueue(std::move(j));
+    }
+    uint64_t enqueue(std::unique_ptr<Job> j) {
         j->submitted = Clock::now();
         std::lock_guard<std::mutex> l(mu_);
         j->ticket = ++next_ticket_;
@@ -230,7 +246,9 @@ class Prover {
                 running_++;
                 j->started = Clock::now();
             }
-            int jrc = rc ? rc : prove_instance(table_, seed_, q_, &j->inst);
+            int jrc = rc ? rc
+                      : j->kind == 0 ? prove_instance(table_, seed_, q_, &j->inst)
+                                     : gb_prove_matmul(table_, ajtai_key_, seed_, q_, &j->mm);
             std::string err = jrc ? std::string(gb_last_error()) : std::string();
             {
                 std::lock_guard<std::mutex> l(mu_);
@@ -252,6 +270,7 @@ class Prover {
     }
 
     void* table_;
+    void* ajtai_key_ = nullptr;
     u64 seed_[2];
     int q_;
     size_t budget_;
@@ -311,6 +330,22 @@ int gb_prover_submit(void* prover, const gb_instance* inst, uint64_t* ticket) {
         return GB_EINVAL;
     }
     *ticket = static_cast<Prover*>(prover)->submit(*inst);
+    return GB_OK;
+}
+
+int gb_prover_set_ajtai_key(void* prover, void* ajtai_key) {
+    if (!prover || !ajtai_key) return GB_EINVAL;
+    static_cast<Prover*>(prover)->set_ajtai_key(ajtai_key);
+    return GB_OK;
+}
+
+int gb_prover_submit_matmul(void* prover, const gb_matmul_job* job, uint64_t* ticket) {
+    if (!prover || !job || !ticket) return GB_EINVAL;
+    if (gb_matmul_proof_len(job->m, job->n, job->k, 0) == 0 || !job->h_a || !job->h_b || !job->h_proof) {
+        set_error_msg("gb_prover_submit_matmul: invalid job");
+        return GB_EINVAL;
+    }
+    *ticket = static_cast<Prover*>(prover)->submit(*job);
     return GB_OK;
 }
 

@@ -185,6 +185,28 @@ __global__ void __launch_bounds__(RED_THREADS) sc_round0_kernel(const u64* __res
     grid_reduce_finish<W>(acc, partials, msg, counter);
 }
 
+// Round 0 on Ext2 inputs (CpuLinearSumcheckProverExt2): message only.
+template <int D>
+__global__ void __launch_bounds__(RED_THREADS) sc_round0_e2in_kernel(const u64* __restrict__ polys, size_t stride,
+                                                                     size_t half, u64* __restrict__ partials,
+                                                                     u64* __restrict__ msg, unsigned* __restrict__ counter) {
+    constexpr int W = 2 * (D + 1);
+    u64 acc[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < half; y += (size_t)gridDim.x * blockDim.x) {
+        e2 e[D], dl[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            const u64* p = polys + (size_t)i * 2 * stride + 4 * y;
+            e[i] = ld_e2(p, true);
+            dl[i] = e2_sub(ld_e2(p + 2, true), e[i]);
+        }
+        accum_e2<D>(e, dl, acc);
+    }
+    grid_reduce_finish<W>(acc, partials, msg, counter);
+}
+
 // Round k >= 1, Ext2 challenge: fold level k-1 (base if BASE_IN) with r, store the folded
 // level, accumulate round k's message.  quarter = number of output pairs.
 template <int D, bool BASE_IN>
@@ -322,6 +344,13 @@ struct Round0E2 {
     }
 };
 template <int D>
+struct Round0E2In {
+    static int run(const u64* polys, size_t stride, size_t half, unsigned grid, u64* part, u64* msg, unsigned* ctr) {
+        sc_round0_e2in_kernel<D><<<grid, RED_THREADS, 0, stream()>>>(polys, stride, half, part, msg, ctr);
+        return check_launch("sc_round0_e2in");
+    }
+};
+template <int D>
 struct Round0Base {
     static int run(const u64* polys, size_t stride, size_t half, unsigned grid, u64* part, u64* msg, unsigned* ctr) {
         sc_round0_kernel<D, false><<<grid, RED_THREADS, 0, stream()>>>(polys, stride, half, part, msg, ctr);
@@ -382,8 +411,10 @@ struct ScWork {
     }
 };
 
-static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* h_polys, bool ext, u64* h_msgs,
-                 u64* h_ch, u64* h_finals, u64* h_final_eval) {
+// ext: Ext2 challenges and messages; in_ext (with ext): the polynomials themselves are Ext2,
+// [d][2^n][c0, c1].
+static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* h_polys, bool ext, bool in_ext,
+                 u64* h_msgs, u64* h_ch, u64* h_finals, u64* h_final_eval) {
     using namespace host;
     if (!t || n < 0 || n > 40 || d < 1 || d > SC_MAX_D || (!d_polys == !h_polys) || !h_msgs || !h_ch || !h_finals ||
         !h_final_eval) {
@@ -398,9 +429,10 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
 
     ScWork w;
     const u64* polys = d_polys;
+    const int IW = in_ext ? 2 : 1;  // words per input value
     if (h_polys || (((uintptr_t)d_polys) & 15)) {
-        GB_CUDA_TRY(cudaMallocAsync(&w.base, N * d * 8, s));
-        GB_CUDA_TRY(cudaMemcpyAsync(w.base, h_polys ? (const void*)h_polys : (const void*)d_polys, N * d * 8,
+        GB_CUDA_TRY(cudaMallocAsync(&w.base, N * d * IW * 8, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(w.base, h_polys ? (const void*)h_polys : (const void*)d_polys, N * d * IW * 8,
                                     h_polys ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
         polys = w.base;
     }
@@ -424,14 +456,15 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
     std::vector<u64> finals(2 * d, 0);
     if (n == 0) {
         // no rounds: the single evaluation of every polynomial is its final value
-        for (int i = 0; i < d; i++) GB_CUDA_TRY(cudaMemcpyAsync(stage + i, polys + i, 8, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(stage, polys, (size_t)d * IW * 8, cudaMemcpyDeviceToHost, s));
         GB_CUDA_TRY(cudaStreamSynchronize(s));
-        for (int i = 0; i < d; i++) finals[W * i] = canon(stage[i]);
+        for (int i = 0; i < d; i++)
+            for (int c = 0; c < IW; c++) finals[W * i + c] = canon(stage[IW * i + c]);
     } else {
         u64 r0 = 0, r1 = 0;
         const u64* cur = polys;
         size_t cur_stride = N;
-        bool base_in = true;
+        bool base_in = !in_ext;
         u64* bufs[2] = {w.a, w.b};
         int pp = 0;
         for (int k = 0; k < n; k++) {
@@ -439,8 +472,9 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
             int rc;
             if (k == 0) {
                 unsigned g = round_grid(level / 2);
-                rc = ext ? dispatch_d<Round0E2>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter)
-                         : dispatch_d<Round0Base>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter);
+                rc = in_ext ? dispatch_d<Round0E2In>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter)
+                     : ext  ? dispatch_d<Round0E2>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter)
+                            : dispatch_d<Round0Base>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter);
             } else {
                 u64* dst = bufs[pp];
                 size_t quarter = level / 2;  // output pairs
@@ -541,7 +575,12 @@ int sumcheck_fold_ext2_ffi(const uint64_t* d_input, uint64_t* d_output, uint64_t
 
 int gb_sumcheck_prove_ext2(gb_transcript* t, int n, int d, const uint64_t* d_polys, const uint64_t* h_polys,
                            uint64_t* h_msgs, uint64_t* h_challenges, uint64_t* h_finals, uint64_t* h_final_eval) {
-    return prove(t, n, d, d_polys, h_polys, true, h_msgs, h_challenges, h_finals, h_final_eval);
+    return prove(t, n, d, d_polys, h_polys, true, false, h_msgs, h_challenges, h_finals, h_final_eval);
+}
+
+int gb_sumcheck_prove_ext2_polys(gb_transcript* t, int n, int d, const uint64_t* d_polys, const uint64_t* h_polys,
+                                 uint64_t* h_msgs, uint64_t* h_challenges, uint64_t* h_finals, uint64_t* h_final_eval) {
+    return prove(t, n, d, d_polys, h_polys, true, true, h_msgs, h_challenges, h_finals, h_final_eval);
 }
 
 size_t gb_sumcheck_round_workspace_words(void) {
@@ -561,7 +600,7 @@ int gb_sumcheck_fold_round_ext2(const uint64_t* d_in, int in_base, size_t in_str
 
 int gb_sumcheck_prove_base(gb_transcript* t, int n, int d, const uint64_t* d_polys, const uint64_t* h_polys,
                            uint64_t* h_msgs, uint64_t* h_challenges, uint64_t* h_finals, uint64_t* h_final_eval) {
-    return prove(t, n, d, d_polys, h_polys, false, h_msgs, h_challenges, h_finals, h_final_eval);
+    return prove(t, n, d, d_polys, h_polys, false, false, h_msgs, h_challenges, h_finals, h_final_eval);
 }
 
 }  // extern "C"

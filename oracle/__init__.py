@@ -63,6 +63,7 @@ def lib():
             ("or_tr_challenge_scalar", u64, [vp, _c.c_char_p, sz]),
             ("or_tr_challenge_ext2", None, [vp, _c.c_char_p, sz, _u64p]),
             ("or_sumcheck_prove_ext2", i32, [vp, i32, i32, _u64p, _u64p, _u64p, _u64p, _u64p]),
+            ("or_sumcheck_prove_ext2_polys", i32, [vp, i32, i32, _u64p, _u64p, _u64p, _u64p, _u64p]),
             ("or_sumcheck_prove_base", i32, [vp, i32, i32, _u64p, _u64p, _u64p, _u64p, _u64p]),
             ("or_sumcheck_verify_ext2", i32, [vp, i32, i32, _u64p, _u64p, _u64p]),
             ("or_eq_table_base", None, [_u64p, i32, _u64p]),
@@ -163,6 +164,21 @@ def sumcheck_prove_ext2(transcript, polys):
     fe = np.zeros(2, np.uint64)
     rc = lib().or_sumcheck_prove_ext2(transcript.ptr, n, d, polys.reshape(-1), msgs.reshape(-1),
                                       ch.reshape(-1), finals.reshape(-1), fe)
+    assert rc == 0
+    return {"round_messages": msgs, "challenges": ch, "final_evals": finals, "final_eval": fe}
+
+
+def sumcheck_prove_ext2_polys(transcript, polys):
+    """polys: [d][2^n][2] Ext2 values."""
+    polys = _a(polys)
+    d, N = polys.shape[0], polys.shape[1]
+    n = N.bit_length() - 1
+    msgs = np.zeros((n, d + 1, 2), np.uint64)
+    ch = np.zeros((n, 2), np.uint64)
+    finals = np.zeros((d, 2), np.uint64)
+    fe = np.zeros(2, np.uint64)
+    rc = lib().or_sumcheck_prove_ext2_polys(transcript.ptr, n, d, polys.reshape(-1), msgs.reshape(-1),
+                                            ch.reshape(-1), finals.reshape(-1), fe)
     assert rc == 0
     return {"round_messages": msgs, "challenges": ch, "final_evals": finals, "final_eval": fe}
 

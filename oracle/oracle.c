@@ -290,16 +290,38 @@ static e2 bt_sample_ext2(or_transcript *t) {
 /* CpuLinearSumcheckProverExt2::{new,prove} on base inputs lifted to Ext2
  * (zk-torch-3/src/sumcheck/cpu_ext2_prover.rs:23-110; identical transcript calls
  * to GpuLinearSumcheckProver::prove, gpu_prover.rs:21-89). */
+static int sumcheck_ext2_rounds(or_transcript *t, int n, int d, e2 *w, u64 *msgs, u64 *challenges, u64 *finals,
+                                u64 *final_eval);
+
 int or_sumcheck_prove_ext2(or_transcript *t, int n, int d, const u64 *polys, u64 *msgs,
                            u64 *challenges, u64 *finals, u64 *final_eval) {
     if (n < 0 || d < 1) return -1;
     size_t N = (size_t)1 << n;
-    or_tr_append_u64(t, LBL("num_var"), (u64)n);
-    or_tr_append_u64(t, LBL("num_poly"), (u64)d);
     e2 *w = (e2 *)malloc(sizeof(e2) * N * d);
     if (!w) return -2;
     for (int i = 0; i < d; i++)
         for (size_t k = 0; k < N; k++) w[i * N + k] = e2_base(polys[i * N + k]);
+    return sumcheck_ext2_rounds(t, n, d, w, msgs, challenges, finals, final_eval);
+}
+
+/* The same prover on Ext2 polynomials, polys[d][2^n][2] (CpuLinearSumcheckProverExt2::prove takes
+ * Ext2 vectors, cpu_ext2_prover.rs:35-110). */
+int or_sumcheck_prove_ext2_polys(or_transcript *t, int n, int d, const u64 *polys, u64 *msgs,
+                                 u64 *challenges, u64 *finals, u64 *final_eval) {
+    if (n < 0 || d < 1) return -1;
+    size_t N = (size_t)1 << n;
+    e2 *w = (e2 *)malloc(sizeof(e2) * N * d);
+    if (!w) return -2;
+    for (size_t k = 0; k < N * d; k++) w[k] = e2_mk(polys[2 * k], polys[2 * k + 1]);
+    return sumcheck_ext2_rounds(t, n, d, w, msgs, challenges, finals, final_eval);
+}
+
+/* rounds of the Ext2 prover over w (freed here) */
+static int sumcheck_ext2_rounds(or_transcript *t, int n, int d, e2 *w, u64 *msgs, u64 *challenges, u64 *finals,
+                                u64 *final_eval) {
+    size_t N = (size_t)1 << n;
+    or_tr_append_u64(t, LBL("num_var"), (u64)n);
+    or_tr_append_u64(t, LBL("num_poly"), (u64)d);
     size_t cur = N;
     for (int rd = 0; rd < n; rd++) {
         size_t half = cur / 2;

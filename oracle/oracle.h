@@ -70,6 +70,8 @@ void or_tr_challenge_ext2(or_transcript *t, const uint8_t *label, size_t len, ui
 int or_sumcheck_prove_ext2(or_transcript *t, int n, int d, const uint64_t *polys,
                            uint64_t *msgs, uint64_t *challenges, uint64_t *finals,
                            uint64_t *final_eval);
+int or_sumcheck_prove_ext2_polys(or_transcript *t, int n, int d, const uint64_t *polys, uint64_t *msgs,
+                                 uint64_t *challenges, uint64_t *finals, uint64_t *final_eval);
 int or_sumcheck_prove_base(or_transcript *t, int n, int d, const uint64_t *polys,
                            uint64_t *msgs, uint64_t *challenges, uint64_t *finals,
                            uint64_t *final_eval);
