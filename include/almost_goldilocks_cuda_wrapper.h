@@ -35,6 +35,77 @@ int almost_goldilocks_cuda_init(void);
 int ajtai_commit_wide_ffi(const uint32_t *d_key, const uint64_t *d_z_wide, uint64_t N, uint64_t col_offset, int chunk,
                           uint64_t *d_out);
 
+/* Binary witnesses, batched (commit_dense_batched_kernel, cuda_almost_goldilocks/ajtai.cuh:82-162;
+ * almost wrapper.cu:1139-1170): d_z is [B][N] u64 bitmasks (bit l of word (b, j) = coefficient l
+ * of ring element j of witness b); d_out is [B][KAPPA][64] canonical.  1 <= B <= 16 (-2
+ * otherwise); chunk as for ajtai_commit_wide_ffi.  The _at form uses matrix columns from
+ * col_offset.  Synchronising. */
+int ajtai_commit_dense_batched_ffi(const uint32_t *d_key, const uint64_t *d_z, uint64_t N, int B, int chunk,
+                                   uint64_t *d_out);
+int ajtai_commit_dense_batched_at_ffi(const uint32_t *d_key, const uint64_t *d_z, uint64_t N, int B, int chunk,
+                                      uint64_t col_offset, uint64_t *d_out);
+/* Ternary witness (almost wrapper.cu:1642-1660): coefficient l of ring element j is
+ * bit l of d_pos[j] minus bit l of d_neg[j]; d_out [KAPPA][64].  Synchronising. */
+int ajtai_commit_ternary_ffi(const uint32_t *d_key, const uint64_t *d_pos, const uint64_t *d_neg, uint64_t N_ring,
+                             int chunk, uint64_t *d_out);
+/* Sparse binary witness (commit_sparse_partial_kernel, ajtai.cuh:382-440; almost wrapper.cu:1741-1756):
+ * d_positions holds K coefficient indices 64 j + l with value 1 (a repeated index counts once
+ * per occurrence); d_out [KAPPA][64].  Synchronising. */
+int ajtai_commit_sparse_ffi(const uint32_t *d_key, const uint64_t *d_positions, uint64_t K, int chunk,
+                            uint64_t *d_out);
+
+/* ---- memory and streams (almost-goldilocks-cuda-rs/src/ffi.rs:77-100, almost wrapper.cu:255-411);
+ * cuda_malloc, cuda_free, cuda_memcpy_{htod,dtoh,dtod}, cuda_pool_trim, cuda_device_synchronize,
+ * cuda_get/peek_last_error, cuda_mem_get_info and the device calls are the shared ones of
+ * goldilocks_cuda_wrapper.h. */
+const char *agl_cuda_error_string(int code);
+int cuda_memset(void *dst, int value, size_t size);
+/* Waits for this thread's launch stream ("my kernels are done"). */
+int cuda_sync_mine(void);
+int cuda_stream_create(void **stream);
+int cuda_stream_destroy(void *stream);
+int cuda_stream_synchronize(void *stream);
+int cuda_memcpy_dtod_async(void *dst, const void *src, size_t size, void *stream);
+int cuda_memcpy_htod_async(void *dst, const void *src, size_t size, void *stream);
+/* Device memory the stream-ordered pool of the current device holds (reserved, in use or not). */
+size_t agl_cached_bytes(void);
+/* Synchronous copies through pinned staging (any host memory). */
+int agl_d2h_staged(void *h_dst, const void *d_src, size_t bytes);
+int agl_h2d_staged(void *d_dst, const void *h_src, size_t bytes);
+
+/* ---- almost-Goldilocks sumcheck (cuda_almost_goldilocks/almost_sumcheck_prover.cuh:24-225):
+ * d polynomials at stride original_size (Ext2: [poly][original_size][2]); round k uses pairs
+ * (2y, 2y + 1), y < half.  The message entry points write per-block partial sums
+ * d_partial[block][c] (Ext2: [block][c][2]), c = 0..d, for num_blocks blocks of 256 threads
+ * over a grid-stride loop (the caller adds them up mod q); the folds write
+ * p_i[y] = p_i[2y] + r (p_i[2y+1] - p_i[2y]) at the same stride.  Launch only; 1 <= d <= 8. */
+int agl_sumcheck_round_message_ffi(const uint64_t *d_polys, uint64_t *d_partial, int d, size_t original_size,
+                                   size_t half, int num_blocks);
+int agl_sumcheck_fold_ffi(const uint64_t *d_input, uint64_t *d_output, uint64_t challenge, int d,
+                          size_t original_size, size_t half);
+int aext2_sumcheck_round_message_ffi(const uint64_t *d_polys, uint64_t *d_partial, int d, size_t original_size,
+                                     size_t half, int num_blocks);
+int aext2_sumcheck_fold_ffi(const uint64_t *d_input, uint64_t *d_output, uint64_t challenge_c0,
+                            uint64_t challenge_c1, int d, size_t original_size, size_t half);
+/* Batched same-point degree-2 sumcheck (almost_sumcheck_prover.cuh:220-368): per leaf the pair
+ * (eq, f) of original_size Ext2 values each, leaf l at d_polys + 4 l original_size; partials
+ * [block_x][leaf][c][2], c = 0, 1, 2, grid (num_blocks_x, num_leaves).  Launch only. */
+int aext2_sumcheck_batched_round_message_ffi(const uint64_t *d_polys, uint64_t *d_partial, size_t original_size,
+                                             size_t half, int num_leaves, int num_blocks_x);
+int aext2_sumcheck_batched_fold_ffi(const uint64_t *d_input, uint64_t *d_output, uint64_t challenge_c0,
+                                    uint64_t challenge_c1, size_t original_size, size_t half, int num_leaves);
+
+/* ---- eq tables (almost_eq_lagrange.cuh:23-219): eq(r, x), variable i <-> bit i of x.  As with
+ * the reference's ping-pong DP the table ends in d_buf_a when log_n is even and in d_buf_b when
+ * it is odd; *d_result is set to that buffer, the other one is scratch.  The batched form takes
+ * num_leaves points [leaf][log_n] and buffers of num_leaves x leaf_stride entries. */
+int agl_eq_dp_all_ffi(const uint64_t *d_r, uint64_t *d_buf_a, uint64_t *d_buf_b, int log_n, uint64_t **d_result);
+int aext2_eq_dp_all_ffi(const uint64_t *d_r, uint64_t *d_buf_a, uint64_t *d_buf_b, int log_n, uint64_t **d_result);
+int aext2_eq_dp_all_stream_ffi(const uint64_t *d_r, uint64_t *d_buf_a, uint64_t *d_buf_b, int log_n,
+                               uint64_t **d_result, void *stream);
+int aext2_eq_dp_all_batched_ffi(const uint64_t *d_r_all, uint64_t *d_buf_a_all, uint64_t *d_buf_b_all, int log_n,
+                                int num_leaves, size_t leaf_stride, uint64_t **d_result, void *stream);
+
 /* ===================== Part 2: GB300 additions (no reference counterpart) ===================== */
 
 /* Matrix rows [row_lo, row_lo + rows) over n_ring ring columns of the ChaCha8 key h_seed,

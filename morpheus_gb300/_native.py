@@ -121,8 +121,33 @@ SIGNATURES = {
     "gb_prover_set_ajtai_key": (i32, [vp, vp]),
     "gb_prover_submit_matmul": (i32, [vp, vp, ctypes.POINTER(ctypes.c_uint64)]),
     "almost_goldilocks_cuda_init": (i32, []),
+    "agl_cuda_error_string": (ctypes.c_char_p, [i32]),
+    "cuda_memset": (i32, [vp, i32, sz]),
+    "cuda_sync_mine": (i32, []),
+    "cuda_stream_create": (i32, [ctypes.POINTER(vp)]),
+    "cuda_stream_destroy": (i32, [vp]),
+    "cuda_stream_synchronize": (i32, [vp]),
+    "cuda_memcpy_dtod_async": (i32, [vp, vp, sz, vp]),
+    "cuda_memcpy_htod_async": (i32, [vp, vp, sz, vp]),
+    "agl_cached_bytes": (sz, []),
+    "agl_d2h_staged": (i32, [vp, vp, sz]),
+    "agl_h2d_staged": (i32, [vp, vp, sz]),
+    "agl_sumcheck_round_message_ffi": (i32, [vp, vp, i32, sz, sz, i32]),
+    "agl_sumcheck_fold_ffi": (i32, [vp, vp, u64, i32, sz, sz]),
+    "aext2_sumcheck_round_message_ffi": (i32, [vp, vp, i32, sz, sz, i32]),
+    "aext2_sumcheck_fold_ffi": (i32, [vp, vp, u64, u64, i32, sz, sz]),
+    "aext2_sumcheck_batched_round_message_ffi": (i32, [vp, vp, sz, sz, i32, i32]),
+    "aext2_sumcheck_batched_fold_ffi": (i32, [vp, vp, u64, u64, sz, sz, i32]),
+    "agl_eq_dp_all_ffi": (i32, [vp, vp, vp, i32, ctypes.POINTER(vp)]),
+    "aext2_eq_dp_all_ffi": (i32, [vp, vp, vp, i32, ctypes.POINTER(vp)]),
+    "aext2_eq_dp_all_stream_ffi": (i32, [vp, vp, vp, i32, ctypes.POINTER(vp), vp]),
+    "aext2_eq_dp_all_batched_ffi": (i32, [vp, vp, vp, i32, i32, sz, ctypes.POINTER(vp), vp]),
     "ajtai_commit_wide_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
     "ajtai_commit_wide_noalloc_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
+    "ajtai_commit_dense_batched_ffi": (i32, [vp, vp, u64, i32, i32, vp]),
+    "ajtai_commit_dense_batched_at_ffi": (i32, [vp, vp, u64, i32, i32, u64, vp]),
+    "ajtai_commit_ternary_ffi": (i32, [vp, vp, vp, u64, i32, vp]),
+    "ajtai_commit_sparse_ffi": (i32, [vp, vp, u64, i32, vp]),
     "gb_ajtai_key_create": (i32, [vp, i32, i32, u64, ctypes.POINTER(vp)]),
     "gb_ajtai_key_destroy": (i32, [vp]),
     "gb_ajtai_key_info": (i32, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(u64)]),

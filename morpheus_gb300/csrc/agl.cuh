@@ -39,7 +39,32 @@ __device__ __forceinline__ u64 agl_reduce(u64 lo, u64 hi) {
     q_hi += (r2 < r);
     return agl_add(r2, q_hi * AGL_C);
 }
-__device__ __forceinline__ u64 agl_mul(u64 a, u64 b) { return agl_reduce(a * b, __umul64hi(a, b)); }
+__device__ __forceinline__ u64 agl_mul(u64 a, u64 b) {
+    u64 lo, hi;
+    gl_mul128(a, b, lo, hi);
+    return agl_reduce(lo, hi);
+}
+
+// Ext2 of the almost-Goldilocks field: c0 + c1 X, X^2 = 3 (cuda_almost_goldilocks/almost_extension.cuh:31-32)
+struct ae2 {
+    u64 c0, c1;
+};
+__device__ __forceinline__ ae2 ae2_make(u64 a, u64 b) {
+    ae2 r;
+    r.c0 = a;
+    r.c1 = b;
+    return r;
+}
+__device__ __forceinline__ ae2 ae2_add(ae2 a, ae2 b) { return ae2_make(agl_add(a.c0, b.c0), agl_add(a.c1, b.c1)); }
+__device__ __forceinline__ ae2 ae2_sub(ae2 a, ae2 b) { return ae2_make(agl_sub(a.c0, b.c0), agl_sub(a.c1, b.c1)); }
+// Karatsuba: three base multiplies
+__device__ __forceinline__ ae2 ae2_mul(ae2 a, ae2 b) {
+    u64 m0 = agl_mul(a.c0, b.c0), m1 = agl_mul(a.c1, b.c1);
+    u64 m2 = agl_mul(agl_add(a.c0, a.c1), agl_add(b.c0, b.c1));
+    u64 m1x3 = agl_add(agl_add(m1, m1), m1);
+    return ae2_make(agl_add(m0, m1x3), agl_sub(agl_sub(m2, m0), m1));
+}
+__device__ __forceinline__ ae2 ae2_canon(ae2 a) { return ae2_make(agl_canon(a.c0), agl_canon(a.c1)); }
 
 // ---------------------------------------------------------------------------
 // ChaCha8 block: 8 rounds (4 double rounds) of the ChaCha quarter-round network over

@@ -562,6 +562,137 @@ __global__ void ajtai_wide_reduce_kernel(const u64* __restrict__ partial, int nc
     out[t] = agl_canon(acc);
 }
 
+// ---------------------------------------------------------------------------
+// Set-bit commitments of small-coefficient witnesses (reference ABI): binary batches
+// (commit_dense_batched_kernel, ajtai.cuh:82-162), ternary pos/neg bitmasks and sparse
+// position lists (commit_sparse_partial_kernel, ajtai.cuh:382-440).  Same tiling as the
+// wide kernel (8 matrix rows x 64 coefficients per block, the rows' column generated into
+// shared memory); each set coefficient l of column j adds s(r, l) M[i][j][(r - l) mod 64].
+// ---------------------------------------------------------------------------
+constexpr int BITS_MAX_B = 16;
+
+__device__ __forceinline__ void wide_fill_rows(const u32* ksh, int tile, u64 j, u64* Msh, int t) {
+    if (t < WIDE_ROWS * 8) {
+        int rl = t / 8, blk = t % 8;
+        int rr = tile * WIDE_ROWS + rl;
+        u64 out[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (rr < AJ_KAPPA) ajtai_prg_block(ksh, (u32)rr, j, (u32)blk, out);
+#pragma unroll
+        for (int q = 0; q < 8; q++) Msh[rl * AJ_D + blk * 8 + q] = out[q];
+    }
+}
+
+// pos/neg: [B][N] bitmasks (neg may be null); partial [chunk][B][KAPPA][D]
+__global__ void __launch_bounds__(WIDE_ROWS * AJ_D) ajtai_bits_kernel(const u32* __restrict__ key,
+                                                                    const u64* __restrict__ pos,
+                                                                    const u64* __restrict__ neg, u64 N, int B,
+                                                                    u64 col_offset, u64* __restrict__ partial) {
+    __shared__ u64 Msh[WIDE_ROWS * AJ_D];
+    __shared__ u64 psh[BITS_MAX_B], nsh[BITS_MAX_B];
+    __shared__ u32 ksh[8];
+    const int t = threadIdx.x, il = t / AJ_D, r = t % AJ_D;
+    const int chunk = blockIdx.x, tile = blockIdx.y, row = tile * WIDE_ROWS + il;
+    if (t < 8) ksh[t] = key[t];
+    u64 acc[BITS_MAX_B];
+#pragma unroll
+    for (int b = 0; b < BITS_MAX_B; b++) acc[b] = 0;
+    __syncthreads();
+    const u64 j0 = (u64)chunk * WIDE_CHUNK, j1 = j0 + WIDE_CHUNK < N ? j0 + WIDE_CHUNK : N;
+    for (u64 j = j0; j < j1; j++) {
+        if (t < B) {
+            psh[t] = pos[(u64)t * N + j];
+            nsh[t] = neg ? neg[(u64)t * N + j] : 0;
+        }
+        wide_fill_rows(ksh, tile, j + col_offset, Msh, t);
+        __syncthreads();
+        const u64* m = Msh + il * AJ_D;
+#pragma unroll
+        for (int b = 0; b < BITS_MAX_B; b++) {
+            if (b >= B) break;
+            u64 mask = psh[b];
+            while (mask) {
+                int l = __ffsll((long long)mask) - 1;
+                mask &= mask - 1;
+                acc[b] = l <= r ? agl_add(acc[b], m[r - l]) : agl_sub(acc[b], m[r - l + AJ_D]);
+            }
+            mask = nsh[b];
+            while (mask) {
+                int l = __ffsll((long long)mask) - 1;
+                mask &= mask - 1;
+                acc[b] = l <= r ? agl_sub(acc[b], m[r - l]) : agl_add(acc[b], m[r - l + AJ_D]);
+            }
+        }
+        __syncthreads();
+    }
+    if (row < AJ_KAPPA)
+#pragma unroll
+        for (int b = 0; b < BITS_MAX_B; b++) {
+            if (b >= B) break;
+            partial[(((size_t)chunk * B + b) * AJ_KAPPA + row) * AJ_D + r] = acc[b];
+        }
+}
+
+// positions: K global coefficient indices p = 64 j + l of a binary witness (a repeated index
+// counts twice); partial [chunk][KAPPA][D] over WIDE_CHUNK * 16 positions per chunk
+constexpr int SPARSE_CHUNK = WIDE_CHUNK * 16;
+__global__ void __launch_bounds__(WIDE_ROWS * AJ_D) ajtai_sparse_kernel(const u32* __restrict__ key,
+                                                                      const u64* __restrict__ positions, u64 K,
+                                                                      u64* __restrict__ partial) {
+    __shared__ u64 Msh[WIDE_ROWS * AJ_D];
+    __shared__ u32 ksh[8];
+    const int t = threadIdx.x, il = t / AJ_D, r = t % AJ_D;
+    const int chunk = blockIdx.x, tile = blockIdx.y, row = tile * WIDE_ROWS + il;
+    if (t < 8) ksh[t] = key[t];
+    __syncthreads();
+    u64 acc = 0;
+    u64 prev = ~(u64)0;
+    const u64 k0 = (u64)chunk * SPARSE_CHUNK, k1 = k0 + SPARSE_CHUNK < K ? k0 + SPARSE_CHUNK : K;
+    for (u64 k = k0; k < k1; k++) {
+        const u64 p = positions[k], j = p >> 6;
+        const int l = (int)(p & 63);
+        if (j != prev) {  // the same for the whole block
+            __syncthreads();
+            wide_fill_rows(ksh, tile, j, Msh, t);
+            __syncthreads();
+            prev = j;
+        }
+        const u64* m = Msh + il * AJ_D;
+        acc = l <= r ? agl_add(acc, m[r - l]) : agl_sub(acc, m[r - l + AJ_D]);
+    }
+    if (row < AJ_KAPPA) partial[((size_t)chunk * AJ_KAPPA + row) * AJ_D + r] = acc;
+}
+
+// out[b][i][r] = sum over chunks of partial[chunk][b][i][r], canonical
+__global__ void ajtai_reduce_b_kernel(const u64* __restrict__ partial, int nchunks, int B, u64* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= B * AJ_KAPPA * AJ_D) return;
+    u64 acc = 0;
+    for (int c = 0; c < nchunks; c++) acc = agl_add(acc, partial[(size_t)c * B * AJ_KAPPA * AJ_D + t]);
+    out[t] = agl_canon(acc);
+}
+
+static bool chunk_ok(int chunk) {
+    return chunk == 64 || chunk == 128 || chunk == 256 || chunk == 1024 || chunk == 4096;
+}
+
+static int commit_bits(const u32* d_key, const u64* d_pos, const u64* d_neg, u64 N, int B, u64 col_offset,
+                       u64* d_out, const char* name) {
+    if (N == 0 || B < 1 || B > BITS_MAX_B || !d_key || !d_pos || !d_out) return GB_EINVAL;
+    cudaStream_t s = stream();
+    const int nchunks = (int)((N + WIDE_CHUNK - 1) / WIDE_CHUNK);
+    u64* partial = nullptr;
+    GB_CUDA_TRY(cudaMallocAsync(&partial, (size_t)nchunks * B * AJ_KAPPA * AJ_D * 8, s));
+    dim3 g((unsigned)nchunks, (unsigned)((AJ_KAPPA + WIDE_ROWS - 1) / WIDE_ROWS));
+    ajtai_bits_kernel<<<g, WIDE_ROWS * AJ_D, 0, s>>>(d_key, d_pos, d_neg, N, B, col_offset, partial);
+    int rc = check_launch(name);
+    if (!rc) {
+        ajtai_reduce_b_kernel<<<grid_for((size_t)B * AJ_KAPPA * AJ_D, 256), 256, 0, s>>>(partial, nchunks, B, d_out);
+        rc = check_launch("ajtai_reduce_b_kernel");
+    }
+    cudaFreeAsync(partial, s);
+    return rc ? rc : sync_stream(name);
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -651,6 +782,47 @@ int ajtai_commit_wide_noalloc_ffi(const uint32_t* d_key, const uint64_t* d_z_wid
     ajtai_wide_reduce_kernel<<<grid_for(AJ_KAPPA * AJ_D, 256), 256, 0, s>>>(partial, nchunks, d_out);
     GB_LAUNCH_CHECK("ajtai_wide_reduce_kernel");
     return sync_stream("ajtai_commit_wide_noalloc_ffi");
+}
+
+int ajtai_commit_dense_batched_at_ffi(const uint32_t* d_key, const uint64_t* d_z, uint64_t N, int B, int chunk,
+                                      uint64_t col_offset, uint64_t* d_out) {
+    if (!chunk_ok(chunk)) return GB_EUNSUPPORTED;
+    return commit_bits(d_key, d_z, nullptr, N, B, col_offset, d_out, "ajtai_commit_dense_batched_ffi");
+}
+
+int ajtai_commit_dense_batched_ffi(const uint32_t* d_key, const uint64_t* d_z, uint64_t N, int B, int chunk,
+                                   uint64_t* d_out) {
+    return ajtai_commit_dense_batched_at_ffi(d_key, d_z, N, B, chunk, 0, d_out);
+}
+
+int ajtai_commit_ternary_ffi(const uint32_t* d_key, const uint64_t* d_pos, const uint64_t* d_neg, uint64_t N_ring,
+                             int chunk, uint64_t* d_out) {
+    if (!chunk_ok(chunk)) return GB_EUNSUPPORTED;
+    if (!d_neg) return GB_EINVAL;
+    return commit_bits(d_key, d_pos, d_neg, N_ring, 1, 0, d_out, "ajtai_commit_ternary_ffi");
+}
+
+int ajtai_commit_sparse_ffi(const uint32_t* d_key, const uint64_t* d_positions, uint64_t K, int chunk,
+                            uint64_t* d_out) {
+    if (!chunk_ok(chunk)) return GB_EUNSUPPORTED;
+    if (!d_key || !d_out || (K && !d_positions)) return GB_EINVAL;
+    cudaStream_t s = stream();
+    if (K == 0) {
+        GB_CUDA_TRY(cudaMemsetAsync(d_out, 0, AJ_KAPPA * AJ_D * 8, s));
+        return sync_stream("ajtai_commit_sparse_ffi");
+    }
+    const int nchunks = (int)((K + SPARSE_CHUNK - 1) / SPARSE_CHUNK);
+    u64* partial = nullptr;
+    GB_CUDA_TRY(cudaMallocAsync(&partial, (size_t)nchunks * AJ_KAPPA * AJ_D * 8, s));
+    dim3 g((unsigned)nchunks, (unsigned)((AJ_KAPPA + WIDE_ROWS - 1) / WIDE_ROWS));
+    ajtai_sparse_kernel<<<g, WIDE_ROWS * AJ_D, 0, s>>>(d_key, d_positions, K, partial);
+    int rc = check_launch("ajtai_sparse_kernel");
+    if (!rc) {
+        ajtai_reduce_b_kernel<<<grid_for(AJ_KAPPA * AJ_D, 256), 256, 0, s>>>(partial, nchunks, 1, d_out);
+        rc = check_launch("ajtai_reduce_b_kernel");
+    }
+    cudaFreeAsync(partial, s);
+    return rc ? rc : sync_stream("ajtai_commit_sparse_ffi");
 }
 
 int gb_ajtai_key_create(const uint32_t* h_seed, int row_lo, int rows, uint64_t n_ring, void** handle) {

@@ -18,8 +18,8 @@ cudaStream_t stream();
 void set_error(const char* where, cudaError_t e);
 void set_error_msg(const std::string& msg);
 int num_sms();
-// Pinned host staging of the calling thread: slot 0 sumcheck, slot 1 Basefold.
-constexpr int PINNED_SLOTS = 2;
+// Pinned host staging of the calling thread: slot 0 sumcheck, slot 1 Basefold, slot 2 staged copies.
+constexpr int PINNED_SLOTS = 3;
 uint64_t* thread_pinned(int slot, size_t words);
 
 // Return-code conventions of the reference C ABI (goldilocks-cuda-rs/cuda/wrapper.cu):

@@ -7,6 +7,7 @@
 #include <mutex>
 #include <string>
 
+#include "../../include/almost_goldilocks_cuda_wrapper.h"
 #include "../../include/goldilocks_cuda_wrapper.h"
 #include "common.cuh"
 #include "host_field.hpp"
@@ -204,6 +205,61 @@ int cuda_device_synchronize(void) { return cudaDeviceSynchronize() == cudaSucces
 int cuda_get_last_error(void) { return (int)cudaGetLastError(); }
 int cuda_peek_at_last_error(void) { return (int)cudaPeekAtLastError(); }
 int cuda_mem_get_info(size_t* f, size_t* t) { return cudaMemGetInfo(f, t) == cudaSuccess ? 0 : -1; }
+const char* agl_cuda_error_string(int code) { return cudaGetErrorString((cudaError_t)code); }
+int cuda_memset(void* dst, int value, size_t size) {
+    return cudaMemsetAsync(dst, value, size, stream()) == cudaSuccess && cudaStreamSynchronize(stream()) == cudaSuccess
+               ? 0
+               : -1;
+}
+int cuda_sync_mine(void) { return cudaStreamSynchronize(stream()) == cudaSuccess ? 0 : -1; }
+int cuda_stream_create(void** s) {
+    cudaStream_t st;
+    if (!s || cudaStreamCreate(&st) != cudaSuccess) return -1;
+    *s = (void*)st;
+    return 0;
+}
+int cuda_stream_destroy(void* s) { return cudaStreamDestroy((cudaStream_t)s) == cudaSuccess ? 0 : -1; }
+int cuda_stream_synchronize(void* s) { return cudaStreamSynchronize((cudaStream_t)s) == cudaSuccess ? 0 : -1; }
+int cuda_memcpy_dtod_async(void* dst, const void* src, size_t size, void* s) {
+    return cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToDevice, (cudaStream_t)s) == cudaSuccess ? 0 : -1;
+}
+int cuda_memcpy_htod_async(void* dst, const void* src, size_t size, void* s) {
+    return cudaMemcpyAsync(dst, src, size, cudaMemcpyHostToDevice, (cudaStream_t)s) == cudaSuccess ? 0 : -1;
+}
+size_t agl_cached_bytes(void) {
+    int dev = 0;
+    cudaMemPool_t pool;
+    uint64_t reserved = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess ||
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess)
+        return 0;
+    return (size_t)reserved;
+}
+// chunked copies through the thread's pinned staging buffer
+static int staged_copy(void* dst, const void* src, size_t bytes, bool to_host) {
+    constexpr size_t CH = (size_t)16 << 20;
+    if (bytes == 0) return 0;
+    uint64_t* buf = gb::thread_pinned(2, CH / 8);
+    if (!buf) return -1;
+    cudaStream_t s = stream();
+    for (size_t o = 0; o < bytes; o += CH) {
+        size_t n = bytes - o < CH ? bytes - o : CH;
+        if (to_host) {
+            if (cudaMemcpyAsync(buf, (const char*)src + o, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess)
+                return -1;
+            std::memcpy((char*)dst + o, buf, n);
+        } else {
+            std::memcpy(buf, (const char*)src + o, n);
+            if (cudaMemcpyAsync((char*)dst + o, buf, n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess)
+                return -1;
+        }
+    }
+    return 0;
+}
+int agl_d2h_staged(void* h_dst, const void* d_src, size_t bytes) { return staged_copy(h_dst, d_src, bytes, true); }
+int agl_h2d_staged(void* d_dst, const void* h_src, size_t bytes) { return staged_copy(d_dst, h_src, bytes, false); }
 int cuda_pool_trim(size_t min_bytes_to_keep) {
     int dev = 0;
     cudaMemPool_t pool;

@@ -148,6 +148,13 @@ class Transcript:
         return bytes(self.buf.raw)
 
 
+def aext2_mul(a, b):
+    """almost-Goldilocks Ext2 product (X^2 = 3), pinned to the reference's golden vectors."""
+    out = np.zeros(2, np.uint64)
+    lib().or_aext2_mul(_a(a), _a(b), out)
+    return out
+
+
 def poseidon2_permute(state):
     s = _a(state).copy()
     lib().or_poseidon2_permute(s)

@@ -103,3 +103,67 @@ def test_full_size_config(gpu_lib):
     assert out.shape == (B, 16, 64) and (out < Q).all()
     pick = [0, 255]
     assert np.array_equal(out[pick], O.ajtai_commit_u8_batch(key, z8[pick], row_lo=0, nrows=16))
+
+
+def _dev(a):
+    from morpheus_gb300.memory import DeviceBuffer
+    return DeviceBuffer.from_numpy(np.ascontiguousarray(a))
+
+
+def _bits_to_coeffs(words, neg_words=None):
+    """u64 bitmasks -> full-width coefficients (1, q - 1 for -1, 0)"""
+    out = np.zeros((len(words), 64), np.uint64)
+    for j, w in enumerate(words):
+        for l in range(64):
+            v = (int(w) >> l) & 1
+            if neg_words is not None:
+                v -= (int(neg_words[j]) >> l) & 1
+            out[j, l] = v % Q
+    return out.reshape(-1)
+
+
+def test_dense_batched_matches_reference_and_oracle(gpu_lib, golden):
+    from morpheus_gb300 import _native as N
+    L = N.lib()
+    g = golden["ajtai_commit_binary_ref"]
+    key = np.array(g["key"], np.uint32)
+    z = np.array(g["z_bits"], np.uint64)
+    d_key, d_z, d_out = _dev(key), _dev(z), _dev(np.zeros(42 * 64, np.uint64))
+    assert L.ajtai_commit_dense_batched_ffi(d_key.ptr, d_z.ptr, len(z), 1, 64, d_out.ptr) == 0
+    assert [int(x) for x in d_out.to_numpy()] == g["out"]
+    # a batch of 5 witnesses against a column window
+    rng = np.random.default_rng(4)
+    n, B, off = 37, 5, 9
+    zb = rng.integers(0, 1 << 63, size=(B, n), dtype=np.uint64) | (rng.integers(0, 2, size=(B, n), dtype=np.uint64) << np.uint64(63))
+    d_zb, d_ob = _dev(zb), _dev(np.zeros(B * 42 * 64, np.uint64))
+    assert L.ajtai_commit_dense_batched_at_ffi(d_key.ptr, d_zb.ptr, n, B, 256, off, d_ob.ptr) == 0
+    got = d_ob.to_numpy().reshape(B, 42, 64)
+    for b in range(B):
+        assert np.array_equal(got[b], O.ajtai_commit_wide(key, _bits_to_coeffs(zb[b]), off, 0, 42))
+    assert L.ajtai_commit_dense_batched_ffi(d_key.ptr, d_zb.ptr, n, 17, 64, d_ob.ptr) == -2
+    assert L.ajtai_commit_dense_batched_ffi(d_key.ptr, d_zb.ptr, n, 2, 100, d_ob.ptr) == -3
+
+
+def test_ternary_and_sparse_vs_oracle(gpu_lib):
+    from morpheus_gb300 import _native as N
+    L = N.lib()
+    rng = np.random.default_rng(8)
+    key = np.array([9, 9, 8, 8, 7, 7, 6, 6], np.uint32)
+    n = 21
+    pos = rng.integers(0, 1 << 63, size=n, dtype=np.uint64)
+    neg = rng.integers(0, 1 << 63, size=n, dtype=np.uint64) & ~pos
+    d_key, d_out = _dev(key), _dev(np.zeros(42 * 64, np.uint64))
+    d_pos, d_neg = _dev(pos), _dev(neg)
+    assert L.ajtai_commit_ternary_ffi(d_key.ptr, d_pos.ptr, d_neg.ptr, n, 1024, d_out.ptr) == 0
+    assert np.array_equal(d_out.to_numpy().reshape(42, 64), O.ajtai_commit_wide(key, _bits_to_coeffs(pos, neg), 0, 0, 42))
+    # sparse positions (ascending with gaps, one repeated index counted twice) across > 1 chunk
+    cols = 700
+    p = np.sort(rng.choice(cols * 64, size=300, replace=False)).astype(np.uint64)
+    p = np.concatenate([p[:150], p[149:150], p[150:]])
+    coeff = np.zeros(cols * 64, np.uint64)
+    for x in p:
+        coeff[int(x)] += 1
+    d_p = _dev(p)
+    assert L.ajtai_commit_sparse_ffi(d_key.ptr, d_p.ptr, len(p), 64, d_out.ptr) == 0
+    assert np.array_equal(d_out.to_numpy().reshape(42, 64), O.ajtai_commit_wide(key, coeff, 0, 0, 42))
+    assert L.ajtai_commit_sparse_ffi(d_key.ptr, d_p.ptr, 0, 64, d_out.ptr) == 0 and not d_out.to_numpy().any()

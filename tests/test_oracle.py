@@ -184,3 +184,16 @@ def test_basefold_open_verify_and_tamper(n, lr, q):
         bad = proof.copy()
         bad[pos] = (int(bad[pos]) + 1) % P
         assert not ver(bad), pos
+
+
+def test_agl_ext2_test_restatement_matches_pinned_oracle():
+    """The big-integer Ext2 product the almost-Goldilocks GPU tests use equals the pinned oracle's."""
+    import importlib.util, os
+    spec = importlib.util.spec_from_file_location("tag", os.path.join(os.path.dirname(__file__), "test_agl_gpu.py"))
+    tag = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(tag)
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        a = [int(x) for x in rng.integers(0, O.Q_AGL, 2, dtype=np.uint64)]
+        b = [int(x) for x in rng.integers(0, O.Q_AGL, 2, dtype=np.uint64)]
+        assert list(tag.e2mul(a, b)) == [int(x) for x in O.aext2_mul(a, b)]
