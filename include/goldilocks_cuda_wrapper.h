@@ -128,6 +128,26 @@ int sumcheck_round_message_ext2_ffi(const uint64_t *d_polys, uint64_t *d_partial
 int sumcheck_fold_ext2_ffi(const uint64_t *d_input, uint64_t *d_output, uint64_t challenge_c0,
                            uint64_t challenge_c1, int d, size_t original_size, size_t half);
 
+/* ---- Fiat-Shamir challengers on the device (goldilocks-cuda-rs/src/ffi.rs:314-372; semantics of
+ * cuda/challenger.cuh:37-222): n independent duplex sponges over Poseidon2-w8, rate 4.  A state
+ * is challenger_state_size() = 136 bytes (sponge[8], input[4], output[4] u64, input_count,
+ * output_count int).  Batched entry points act on states 0..n-1; state i observes values
+ * [i*count, (i+1)*count) (observe: count = 1, observe_ext2: 2) and writes its samples to
+ * [i*count, ...) (sample: 1, ext2: 2, ext5: 5).  Sampled values are canonical.  Launch only. */
+int challenger_state_size(void);
+int challenger_alloc_states(void **d_states, int n);
+int challenger_init_states(void *d_states, int n);
+int challenger_observe_ffi(void *d_states, const uint64_t *d_values, int n);
+int challenger_observe_slice_ffi(void *d_states, const uint64_t *d_values, int count, int n);
+int challenger_sample_ffi(void *d_states, uint64_t *d_outputs, int n);
+int challenger_sample_array_ffi(void *d_states, uint64_t *d_outputs, int count, int n);
+int challenger_sample_ext2_ffi(void *d_states, uint64_t *d_outputs, int n);
+int challenger_sample_ext5_ffi(void *d_states, uint64_t *d_outputs, int n);
+int challenger_observe_ext2_ffi(void *d_states, const uint64_t *d_values, int n);
+/* one state (challenger_state_size() bytes); synchronising */
+int challenger_copy_state_to_host(void *h_state, const void *d_state);
+int challenger_copy_state_to_device(void *d_state, const void *h_state);
+
 /* ===================== Part 2: GB300 additions (no reference counterpart) ===================== */
 
 /* Fiat-Shamir transcript state: the fields of zk-torch-3's Transcript
@@ -152,6 +172,13 @@ unsigned long long gb_launch_count(void);
  * Goldilocks multiplications; d_out receives blocks*256 words.  Times the arithmetic
  * ceiling that the Poseidon2 kernels are compared against.  Launch only. */
 int gb_mulmod_probe(uint64_t *d_out, int blocks, int iters);
+
+/* Merkle scheduling knob of the calling thread: tree layers (and leaf hashes) of fewer than
+ * `parents` permutations use 8 lanes per permutation (lower latency), larger ones one thread
+ * per permutation (higher throughput).  Default 32768; results do not depend on it.  Returns
+ * the previous value. */
+size_t gb_set_coop_threshold(size_t parents);
+size_t gb_get_coop_threshold(void);
 
 /* Transcript helpers (host): new(label), append_u64(label), challenge_ext2(label). */
 void gb_transcript_new(gb_transcript *t, const char *label);
@@ -254,6 +281,9 @@ int gb_prover_submit(void *prover, const gb_instance *inst, uint64_t *ticket); /
  * gb_last_error()); stats may be NULL.  Each ticket is waited for once. */
 int gb_prover_wait(void *prover, uint64_t ticket, gb_job_stats *stats);
 int gb_prover_drain(void *prover); /* blocks until no job is queued or running */
+/* Merkle cooperative threshold the service's workers use (see gb_set_coop_threshold); the
+ * service starts with its creating thread's value. */
+int gb_prover_set_coop_threshold(void *prover, size_t parents);
 int gb_prover_destroy(void *prover);
 /* All instances through a prover service of `workers` threads, largest first; returns the
  * first non-zero job return code.  Synchronising. */

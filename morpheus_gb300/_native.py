@@ -58,6 +58,21 @@ SIGNATURES = {
     "sumcheck_fold_ffi": (i32, [vp, vp, u64, i32, sz, sz]),
     "sumcheck_round_message_ext2_ffi": (i32, [vp, vp, i32, sz, sz, i32]),
     "sumcheck_fold_ext2_ffi": (i32, [vp, vp, u64, u64, i32, sz, sz]),
+    "challenger_state_size": (i32, []),
+    "challenger_alloc_states": (i32, [ctypes.POINTER(vp), i32]),
+    "challenger_init_states": (i32, [vp, i32]),
+    "challenger_observe_ffi": (i32, [vp, vp, i32]),
+    "challenger_observe_slice_ffi": (i32, [vp, vp, i32, i32]),
+    "challenger_sample_ffi": (i32, [vp, vp, i32]),
+    "challenger_sample_array_ffi": (i32, [vp, vp, i32, i32]),
+    "challenger_sample_ext2_ffi": (i32, [vp, vp, i32]),
+    "challenger_sample_ext5_ffi": (i32, [vp, vp, i32]),
+    "challenger_observe_ext2_ffi": (i32, [vp, vp, i32]),
+    "challenger_copy_state_to_host": (i32, [vp, vp]),
+    "challenger_copy_state_to_device": (i32, [vp, vp]),
+    "gb_set_coop_threshold": (sz, [sz]),
+    "gb_get_coop_threshold": (sz, []),
+    "gb_prover_set_coop_threshold": (i32, [vp, sz]),
     "gb_set_stream": (i32, [vp]),
     "gb_get_stream": (vp, []),
     "gb_last_error": (ctypes.c_char_p, []),

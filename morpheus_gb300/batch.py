@@ -164,10 +164,17 @@ def prove_instance(table, master_seed, inst):
     return inst.proof
 
 
-def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30):
-    """All instances through the prover service, largest first."""
+def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30, coop_threshold=None):
+    """All instances through the prover service, largest first.  coop_threshold: the Merkle
+    scheduling knob (gb_set_coop_threshold) for this batch; None keeps the current one."""
     if not instances:
         return
+    if coop_threshold is not None:
+        old = N.lib().gb_set_coop_threshold(coop_threshold)
+        try:
+            return batch_prove(table, master_seed, instances, workers, hbm_budget)
+        finally:
+            N.lib().gb_set_coop_threshold(old)
     q = instances[0].num_queries
     assert all(i.num_queries == q for i in instances)
     arr = (GbInstance * len(instances))(*[i.struct() for i in instances])
@@ -179,11 +186,13 @@ class ProverService:
     """Continuous-batching prover: submit instances as they arrive; each runs as soon as a
     worker is free and its estimated device footprint fits the HBM budget."""
 
-    def __init__(self, table, master_seed, num_queries, workers=8, hbm_budget=64 << 30):
+    def __init__(self, table, master_seed, num_queries, workers=8, hbm_budget=64 << 30, coop_threshold=None):
         self.handle = ctypes.c_void_p()
         self.num_queries = num_queries
         N.check(N.lib().gb_prover_create(table.handle, _seed(master_seed), num_queries, workers, hbm_budget,
                                          ctypes.byref(self.handle)), "gb_prover_create")
+        if coop_threshold is not None:
+            N.check(N.lib().gb_prover_set_coop_threshold(self.handle, coop_threshold), "gb_prover_set_coop_threshold")
         self._live = {}
 
     def set_ajtai_key(self, key):
@@ -243,16 +252,20 @@ def mixed_workload(count, seed, min_vars=10, max_vars=20, degrees=(2, 3, 4), num
     return out
 
 
-def autotune(table, master_seed, instances, candidates=(1, 2, 4, 8, 12, 16), hbm_budget=64 << 30, repeats=1):
-    """Worker count with the shortest wall time for this batch (measured, after one warm-up
-    run at the largest candidate).  Returns (best_workers, {workers: seconds})."""
+def autotune(table, master_seed, instances, candidates=(4, 8, 12, 16, 24), coop_thresholds=(32768, 4096, 512),
+             hbm_budget=64 << 30, repeats=1):
+    """The (workers, Merkle cooperative threshold) schedule with the shortest wall time for this
+    batch, measured after one warm-up run.  Few concurrent proofs favour latency (8-lane
+    permutations on small layers); many favour throughput (one thread per permutation).
+    Returns ((workers, coop_threshold), {(workers, coop_threshold): seconds})."""
     batch_prove(table, master_seed, instances, max(candidates), hbm_budget)
     times = {}
-    for w in candidates:
-        best = float("inf")
-        for _ in range(repeats):
-            t0 = time.perf_counter()
-            batch_prove(table, master_seed, instances, w, hbm_budget)
-            best = min(best, time.perf_counter() - t0)
-        times[w] = best
+    for c in coop_thresholds:
+        for w in candidates:
+            best = float("inf")
+            for _ in range(repeats):
+                t0 = time.perf_counter()
+                batch_prove(table, master_seed, instances, w, hbm_budget, coop_threshold=c)
+                best = min(best, time.perf_counter() - t0)
+            times[(w, c)] = best
     return min(times, key=times.get), times

@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(128) fold_hash_leaves_kernel(const u64* __rest
     st_digest(tree + 4 * i, s);
 }
 
-// Same with 8 lanes per leaf (latency-bound rounds, see MK_COOP_BELOW): every lane of a
+// Same with 8 lanes per leaf (latency-bound rounds, see mk_coop_below): every lane of a
 // group folds both elements, lane l takes state element l, lanes 0..3 store.
 template <bool BASE_IN>
 __global__ void __launch_bounds__(256) fold_hash_leaves_coop_kernel(const u64* __restrict__ cw,
@@ -767,7 +767,7 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
         size_t pairs = L >> (rd + 1);
         if (rd < n - 1) {
             size_t leaves = pairs / 2;
-            if (leaves < MK_COOP_BELOW) {
+            if (leaves < mk_coop_below()) {
                 int th = coop_threads(leaves);
                 unsigned g = grid_for(leaves * 8, th);
                 if (rd == 0)

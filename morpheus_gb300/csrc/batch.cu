@@ -21,6 +21,7 @@
 // starts when its estimated device footprint fits beside the running ones (the first queued
 // job that fits, in arrival order; a job larger than the whole budget runs alone).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -158,6 +159,7 @@ class Prover {
         cv_done_.wait(l, [this] { return ready_ == (int)threads_.size(); });
         return start_rc_;
     }
+    void set_coop(size_t v) { coop_.store(v); }
     void set_ajtai_key(void* key) {
         std::lock_guard<std::mutex> l(mu_);
         ajtai_key_ = key;
@@ -246,6 +248,7 @@ class Prover {
                 running_++;
                 j->started = Clock::now();
             }
+            gb_set_coop_threshold(coop_.load());
             int jrc = rc ? rc
                       : j->kind == 0 ? prove_instance(table_, seed_, q_, &j->inst)
                                      : gb_prove_matmul(table_, ajtai_key_, seed_, q_, &j->mm);
@@ -271,6 +274,7 @@ class Prover {
 
     void* table_;
     void* ajtai_key_ = nullptr;
+    std::atomic<size_t> coop_{gb_get_coop_threshold()};
     u64 seed_[2];
     int q_;
     size_t budget_;
@@ -330,6 +334,12 @@ int gb_prover_submit(void* prover, const gb_instance* inst, uint64_t* ticket) {
         return GB_EINVAL;
     }
     *ticket = static_cast<Prover*>(prover)->submit(*inst);
+    return GB_OK;
+}
+
+int gb_prover_set_coop_threshold(void* prover, size_t parents) {
+    if (!prover) return GB_EINVAL;
+    static_cast<Prover*>(prover)->set_coop(parents);
     return GB_OK;
 }
 

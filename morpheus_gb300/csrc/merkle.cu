@@ -110,10 +110,13 @@ __global__ void replicate_kernel(u64* __restrict__ layer, size_t count, int copi
     layer[words + k] = layer[k % words];
 }
 
+static thread_local size_t t_coop_below = MK_COOP_BELOW_DEFAULT;
+size_t mk_coop_below() { return t_coop_below; }
+
 // one layer: `half` parents from the 2*half digests at `in`
 static int merkle_level(const u64* in, u64* out, size_t half) {
     cudaStream_t s = stream();
-    if (half >= MK_COOP_BELOW) {
+    if (half >= mk_coop_below()) {
         merkle_level_kernel<<<grid_for(half, MK_THREADS), MK_THREADS, 0, s>>>(in, out, half);
         return check_launch("merkle_level_kernel");
     }
@@ -140,7 +143,7 @@ int merkle_build_from_leaves(u64* tree, size_t leaves) {
 }
 
 int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves) {
-    if (leaves < MK_COOP_BELOW) {
+    if (leaves < mk_coop_below()) {
         int t = coop_threads(leaves);
         hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 2);
         return check_launch("hash_leaves_coop_kernel");
@@ -150,7 +153,7 @@ int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves) {
 }
 
 int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves) {
-    if (leaves < MK_COOP_BELOW) {
+    if (leaves < mk_coop_below()) {
         int t = coop_threads(leaves);
         hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 4);
         return check_launch("hash_leaves_coop_kernel");
@@ -220,6 +223,13 @@ __global__ void compress_batch_kernel(const u64* __restrict__ l, const u64* __re
 using namespace gb;
 
 extern "C" {
+
+size_t gb_set_coop_threshold(size_t parents) {
+    size_t old = t_coop_below;
+    t_coop_below = parents;
+    return old;
+}
+size_t gb_get_coop_threshold(void) { return t_coop_below; }
 
 int poseidon2_hash_batch_ffi(const uint64_t* d_input, uint64_t* d_output, int n) {
     if (n < 0) return GB_EINVAL;

@@ -46,8 +46,11 @@ __device__ __forceinline__ void ld_digest(const u64* p, u64* s) {
 }
 
 // Work below this many permutations per launch is latency-bound: one thread's
-// permutation is a long serial chain, so those launches use 8 lanes per state.
-constexpr size_t MK_COOP_BELOW = 32768;
+// permutation is a long serial chain, so those launches use 8 lanes per state (at about
+// half the throughput of one state per thread).  The threshold belongs to the calling
+// thread (gb_set_coop_threshold); many concurrent proofs favour a lower one.
+constexpr size_t MK_COOP_BELOW_DEFAULT = 32768;
+size_t mk_coop_below();
 // Once a layer has at most this many nodes, the layers above it are finished by one CTA.
 constexpr size_t MK_TOP_NODES = 16;
 
