@@ -251,8 +251,9 @@ def run_batched(args):
     alone = [i.proof.copy() for i in insts]
 
     # batched: tune the worker count on this batch (these runs are the warm-up), then time
-    (best, coop), tune = batch.autotune(table, seed, insts)
+    (best, coop, top), tune = batch.autotune(table, seed, insts)
     L.gb_set_coop_threshold(coop)
+    L.gb_set_merkle_top_nodes(top)
     for _ in range(max(0, args.warmup - 1)):
         batch.batch_prove(table, seed, insts, best)
     l0 = L.gb_launch_count()
@@ -281,14 +282,14 @@ def run_batched(args):
             "config": {"workload": f"{count} instances: product sumcheck + Basefold commit/open_ext2 of every "
                                    "polynomial at the sumcheck point; 2^10..2^20 evaluations (log-uniform), "
                                    "degree in {2,3,4}, rate 1/2, 34 queries, table (22, 1, 22, seed 42)",
-                       "instances": count, "evaluations": elems, "workers": best, "coop_threshold": coop,
+                       "instances": count, "evaluations": elems, "workers": best, "coop_threshold": coop, "merkle_top_nodes": top,
                        "l2": "inputs larger than L2 (batch inputs resident in HBM)",
                        "timing": "host wall clock between device synchronisations (the batch spans one "
                                  "stream per worker)", "parallelism": "replicas x1"},
             "per_call": {"value": count / per_call_s, "unit": "proofs/s", "ms_per_step": per_call_s * 1e3,
                          "how": "every instance through gb_prove_instance, one after another, one stream"},
             "batched_over_per_call": per_call_s / step_s,
-            "autotune_s": {f"{k[0]}w/{k[1]}": round(v, 4) for k, v in tune.items()},
+            "autotune_s": {f"{k[0]}w/{k[1]}/{k[2]}": round(v, 4) for k, v in tune.items()},
             "identical_to_per_call": {"device_inputs": f"{same}/{count}", "host_inputs": f"{same_e2e}/{count}"},
             "e2e": {"value": count / statistics.mean(e2e_times), "unit": "proofs/s",
                     "h2d_bytes_per_step": int(total),

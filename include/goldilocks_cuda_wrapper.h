@@ -179,6 +179,11 @@ int gb_mulmod_probe(uint64_t *d_out, int blocks, int iters);
  * the previous value. */
 size_t gb_set_coop_threshold(size_t parents);
 size_t gb_get_coop_threshold(void);
+/* Second Merkle knob of the calling thread: once a layer has at most `nodes` digests (2..2048,
+ * default 16), one CTA finishes the tree in a single launch.  Larger values mean fewer launches
+ * and a longer chain inside that CTA.  Returns the previous value. */
+size_t gb_set_merkle_top_nodes(size_t nodes);
+size_t gb_get_merkle_top_nodes(void);
 
 /* Transcript helpers (host): new(label), append_u64(label), challenge_ext2(label). */
 void gb_transcript_new(gb_transcript *t, const char *label);
@@ -284,6 +289,7 @@ int gb_prover_drain(void *prover); /* blocks until no job is queued or running *
 /* Merkle cooperative threshold the service's workers use (see gb_set_coop_threshold); the
  * service starts with its creating thread's value. */
 int gb_prover_set_coop_threshold(void *prover, size_t parents);
+int gb_prover_set_merkle_top_nodes(void *prover, size_t nodes); /* see gb_set_merkle_top_nodes */
 int gb_prover_destroy(void *prover);
 /* All instances through a prover service of `workers` threads, largest first; returns the
  * first non-zero job return code.  Synchronising. */

@@ -72,7 +72,10 @@ SIGNATURES = {
     "challenger_copy_state_to_device": (i32, [vp, vp]),
     "gb_set_coop_threshold": (sz, [sz]),
     "gb_get_coop_threshold": (sz, []),
+    "gb_set_merkle_top_nodes": (sz, [sz]),
+    "gb_get_merkle_top_nodes": (sz, []),
     "gb_prover_set_coop_threshold": (i32, [vp, sz]),
+    "gb_prover_set_merkle_top_nodes": (i32, [vp, sz]),
     "gb_set_stream": (i32, [vp]),
     "gb_get_stream": (vp, []),
     "gb_last_error": (ctypes.c_char_p, []),

@@ -164,35 +164,56 @@ def prove_instance(table, master_seed, inst):
     return inst.proof
 
 
-def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30, coop_threshold=None):
-    """All instances through the prover service, largest first.  coop_threshold: the Merkle
-    scheduling knob (gb_set_coop_threshold) for this batch; None keeps the current one."""
+class Schedule:
+    """Per-thread Merkle scheduling knobs (results never depend on them): the cooperative
+    threshold (gb_set_coop_threshold) and the single-CTA top size (gb_set_merkle_top_nodes).
+    A context manager that sets them on the calling thread and restores the previous ones."""
+
+    def __init__(self, coop_threshold=None, top_nodes=None):
+        self.coop, self.top = coop_threshold, top_nodes
+
+    def __enter__(self):
+        L = N.lib()
+        self._old = (L.gb_get_coop_threshold(), L.gb_get_merkle_top_nodes())
+        if self.coop is not None:
+            L.gb_set_coop_threshold(self.coop)
+        if self.top is not None:
+            L.gb_set_merkle_top_nodes(self.top)
+        return self
+
+    def __exit__(self, *a):
+        L = N.lib()
+        L.gb_set_coop_threshold(self._old[0])
+        L.gb_set_merkle_top_nodes(self._old[1])
+
+
+def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30, coop_threshold=None, top_nodes=None):
+    """All instances through the prover service, largest first, with the given Merkle
+    schedule (None keeps the calling thread's)."""
     if not instances:
         return
-    if coop_threshold is not None:
-        old = N.lib().gb_set_coop_threshold(coop_threshold)
-        try:
-            return batch_prove(table, master_seed, instances, workers, hbm_budget)
-        finally:
-            N.lib().gb_set_coop_threshold(old)
     q = instances[0].num_queries
     assert all(i.num_queries == q for i in instances)
     arr = (GbInstance * len(instances))(*[i.struct() for i in instances])
-    N.check(N.lib().gb_batch_prove(table.handle, _seed(master_seed), q, arr, len(instances), workers, hbm_budget),
-            "gb_batch_prove")
+    with Schedule(coop_threshold, top_nodes):
+        N.check(N.lib().gb_batch_prove(table.handle, _seed(master_seed), q, arr, len(instances), workers,
+                                       hbm_budget), "gb_batch_prove")
 
 
 class ProverService:
     """Continuous-batching prover: submit instances as they arrive; each runs as soon as a
     worker is free and its estimated device footprint fits the HBM budget."""
 
-    def __init__(self, table, master_seed, num_queries, workers=8, hbm_budget=64 << 30, coop_threshold=None):
+    def __init__(self, table, master_seed, num_queries, workers=8, hbm_budget=64 << 30, coop_threshold=None,
+                 top_nodes=None):
         self.handle = ctypes.c_void_p()
         self.num_queries = num_queries
         N.check(N.lib().gb_prover_create(table.handle, _seed(master_seed), num_queries, workers, hbm_budget,
                                          ctypes.byref(self.handle)), "gb_prover_create")
         if coop_threshold is not None:
             N.check(N.lib().gb_prover_set_coop_threshold(self.handle, coop_threshold), "gb_prover_set_coop_threshold")
+        if top_nodes is not None:
+            N.check(N.lib().gb_prover_set_merkle_top_nodes(self.handle, top_nodes), "gb_prover_set_merkle_top_nodes")
         self._live = {}
 
     def set_ajtai_key(self, key):
@@ -252,20 +273,27 @@ def mixed_workload(count, seed, min_vars=10, max_vars=20, degrees=(2, 3, 4), num
     return out
 
 
-def autotune(table, master_seed, instances, candidates=(4, 8, 12, 16, 24), coop_thresholds=(32768, 4096, 512),
-             hbm_budget=64 << 30, repeats=1):
-    """The (workers, Merkle cooperative threshold) schedule with the shortest wall time for this
-    batch, measured after one warm-up run.  Few concurrent proofs favour latency (8-lane
-    permutations on small layers); many favour throughput (one thread per permutation).
-    Returns ((workers, coop_threshold), {(workers, coop_threshold): seconds})."""
-    batch_prove(table, master_seed, instances, max(candidates), hbm_budget)
+def autotune(table, master_seed, instances, workers=(8, 12, 16, 24), coop_thresholds=(32768, 4096),
+             top_nodes=(16, 256, 2048), hbm_budget=64 << 30):
+    """Schedule (workers, cooperative threshold, top size) for this batch by coordinate search:
+    after a warm-up run, the worker count at the default Merkle schedule, then the
+    cooperative threshold, then the top size, each measured by wall time.  Few concurrent
+    proofs favour latency (8-lane permutations, small single-CTA tops); many favour throughput
+    and fewer launches.  Returns ((workers, coop, top), {schedule: seconds})."""
+    def run(w, c, t):
+        t0 = time.perf_counter()
+        batch_prove(table, master_seed, instances, w, hbm_budget, coop_threshold=c, top_nodes=t)
+        return time.perf_counter() - t0
+
+    best = (workers[0], coop_thresholds[0], top_nodes[0])
+    run(*best)
     times = {}
-    for c in coop_thresholds:
-        for w in candidates:
-            best = float("inf")
-            for _ in range(repeats):
-                t0 = time.perf_counter()
-                batch_prove(table, master_seed, instances, w, hbm_budget, coop_threshold=c)
-                best = min(best, time.perf_counter() - t0)
-            times[(w, c)] = best
-    return min(times, key=times.get), times
+    for axis, values in ((0, workers), (1, coop_thresholds), (2, top_nodes)):
+        for v in values:
+            cand = list(best)
+            cand[axis] = v
+            cand = tuple(cand)
+            if cand not in times:
+                times[cand] = run(*cand)
+        best = min(times, key=times.get)
+    return best, times

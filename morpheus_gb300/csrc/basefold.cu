@@ -784,8 +784,7 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
                                                                                       ftree[rd], leaves);
             }
             GB_LAUNCH_CHECK("fold_hash_leaves_kernel");
-            RC_TRY(merkle_build_from_leaves(ftree[rd], leaves));
-            GB_CUDA_TRY(cudaMemcpyAsync(rec + 8, ftree[rd] + (2 * leaves - 2) * 4, 32, cudaMemcpyDeviceToDevice, s));
+            RC_TRY(merkle_build_from_leaves(ftree[rd], leaves, rec + 8));
             RC_TRY(read_rec(12));
             put_oracle(rd + 1);
             u64* root = p_roots + (size_t)rd * 4;

@@ -160,6 +160,7 @@ class Prover {
         return start_rc_;
     }
     void set_coop(size_t v) { coop_.store(v); }
+    void set_top(size_t v) { top_.store(v); }
     void set_ajtai_key(void* key) {
         std::lock_guard<std::mutex> l(mu_);
         ajtai_key_ = key;
@@ -249,6 +250,7 @@ class Prover {
                 j->started = Clock::now();
             }
             gb_set_coop_threshold(coop_.load());
+            gb_set_merkle_top_nodes(top_.load());
             int jrc = rc ? rc
                       : j->kind == 0 ? prove_instance(table_, seed_, q_, &j->inst)
                                      : gb_prove_matmul(table_, ajtai_key_, seed_, q_, &j->mm);
@@ -275,6 +277,7 @@ class Prover {
     void* table_;
     void* ajtai_key_ = nullptr;
     std::atomic<size_t> coop_{gb_get_coop_threshold()};
+    std::atomic<size_t> top_{gb_get_merkle_top_nodes()};
     u64 seed_[2];
     int q_;
     size_t budget_;
@@ -340,6 +343,12 @@ int gb_prover_submit(void* prover, const gb_instance* inst, uint64_t* ticket) {
 int gb_prover_set_coop_threshold(void* prover, size_t parents) {
     if (!prover) return GB_EINVAL;
     static_cast<Prover*>(prover)->set_coop(parents);
+    return GB_OK;
+}
+
+int gb_prover_set_merkle_top_nodes(void* prover, size_t nodes) {
+    if (!prover) return GB_EINVAL;
+    static_cast<Prover*>(prover)->set_top(nodes);
     return GB_OK;
 }
 

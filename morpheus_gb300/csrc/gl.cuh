@@ -134,6 +134,33 @@ __device__ __forceinline__ u64 glw_reduce(glw a) {
     asm("add.cc.u64 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=l"(r), "=r"(c) : "l"(a.lo), "l"(t));
     return r + (u64)(0u - c);
 }
+// Three-word lazy sums of full 128-bit products: lo + 2^64 hi + 2^128 top.
+// 2^128 == -2^32 (mod p) (2^64 == 2^32 - 1, squared), so the value reduces to
+// gl_reduce(lo, hi) - top 2^32.
+struct gl3 {
+    u64 lo, hi;
+    u32 top;
+};
+__device__ __forceinline__ gl3 gl3_zero() {
+    gl3 r;
+    r.lo = r.hi = 0;
+    r.top = 0;
+    return r;
+}
+__device__ __forceinline__ void gl3_add_prod(gl3& a, u64 x, u64 y) {
+    u64 lo, hi;
+    gl_mul128(x, y, lo, hi);
+    asm("add.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, %4;\n\taddc.u32 %2, %2, 0;"
+        : "+l"(a.lo), "+l"(a.hi), "+r"(a.top)
+        : "l"(lo), "l"(hi));
+}
+__device__ __forceinline__ void gl3_add(gl3& a, u64 x) {
+    asm("add.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, 0;\n\taddc.u32 %2, %2, 0;"
+        : "+l"(a.lo), "+l"(a.hi), "+r"(a.top)
+        : "l"(x));
+}
+__device__ __forceinline__ u64 gl3_reduce(gl3 a) { return gl_sub(gl_reduce(a.lo, a.hi), (u64)a.top << 32); }
+
 // a b + c reduced, for b < p: the product's high word is then below 2^64 - 2^32, so adding
 // c (hi < 2^32) cannot carry out of 128 bits
 __device__ __forceinline__ u64 gl_mul_add(u64 a, u64 b, glw c) {

@@ -51,20 +51,49 @@ __global__ void __launch_bounds__(MK_COOP_THREADS) merkle_level_coop_kernel(cons
     if (live && l < 4) out[4 * g + l] = x;
 }
 
-// Finish all layers from a layer of at most MK_TOP_NODES digests up to the root:
-// one CTA of 8 * MK_TOP_NODES / 2 threads, one 8-lane group per parent.
-__global__ void __launch_bounds__(8 * (MK_TOP_NODES / 2)) merkle_top_coop_kernel(u64* __restrict__ layer, size_t nodes) {
-    const int grp = threadIdx.x >> 3, l = threadIdx.x & 7;
+// Finish all layers from a small layer up to the root in one CTA: 8-lane groups take the
+// parents of a layer in turns (every warp runs the same number of turns, since the
+// permutation's shuffles need all 32 lanes), then the CTA moves up a layer.  The root is also
+// written to root_out when given.
+__global__ void __launch_bounds__(1024) merkle_top_coop_kernel(u64* __restrict__ layer, size_t nodes,
+                                                               u64* __restrict__ root_out) {
+    const int groups = blockDim.x >> 3, grp = threadIdx.x >> 3, l = threadIdx.x & 7;
     P2Lane c = p2_lane_consts(l);
     while (nodes > 1) {
         size_t half = nodes >> 1;
         u64* out = layer + 4 * nodes;
-        bool live = (size_t)grp < half;
-        u64 x = p2_permute_coop(layer[8 * (live ? grp : 0) + l], l, c);
-        if (live && l < 4) out[4 * grp + l] = x;
+        for (size_t base = 0; base < half; base += groups) {
+            size_t p = base + grp;
+            bool live = p < half;
+            u64 x = p2_permute_coop(layer[8 * (live ? p : 0) + l], l, c);
+            if (live && l < 4) out[4 * p + l] = x;
+        }
         __syncthreads();
         layer = out;
         nodes = half;
+    }
+    if (root_out && threadIdx.x < 4) root_out[threadIdx.x] = layer[threadIdx.x];
+}
+
+// Copies of the first copy's subtree: on layer k (2^(levels-k) * copies nodes, offsets as in
+// the full tree) the first sub >> k digests are repeated copies - 1 times.  One thread per
+// copied word, all layers in one launch.
+__global__ void replicate_layers_kernel(u64* __restrict__ tree, size_t leaves, size_t sub, int copies, size_t total) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    size_t off = 0, nodes = leaves, n = sub;
+    for (;;) {
+        size_t words = 4 * n * (size_t)(copies - 1);
+        if (t < words) {
+            u64* layer = tree + off;
+            layer[4 * n + t] = layer[t % (4 * n)];
+            return;
+        }
+        t -= words;
+        off += 4 * nodes;
+        nodes >>= 1;
+        n >>= 1;
+        if (n == 0) return;
     }
 }
 
@@ -125,10 +154,13 @@ static int merkle_level(const u64* in, u64* out, size_t half) {
     return check_launch("merkle_level_coop_kernel");
 }
 
-int merkle_build_from_leaves(u64* tree, size_t leaves) {
+static thread_local size_t t_top_nodes = MK_TOP_NODES;
+
+int merkle_build_from_leaves(u64* tree, size_t leaves, u64* root_out) {
     u64* layer = tree;
     size_t nodes = leaves;
-    while (nodes > MK_TOP_NODES) {
+    const size_t top = t_top_nodes;
+    while (nodes > top) {
         size_t half = nodes >> 1;
         int rc = merkle_level(layer, layer + 4 * nodes, half);
         if (rc) return rc;
@@ -136,8 +168,13 @@ int merkle_build_from_leaves(u64* tree, size_t leaves) {
         nodes = half;
     }
     if (nodes > 1) {
-        merkle_top_coop_kernel<<<1, 8 * (MK_TOP_NODES / 2), 0, stream()>>>(layer, nodes);
+        size_t half = nodes >> 1;
+        int threads = (int)(8 * (half < 128 ? half : 128));
+        threads = threads < 64 ? 64 : (threads + 31) / 32 * 32;
+        merkle_top_coop_kernel<<<1, threads, 0, stream()>>>(layer, nodes, root_out);
         GB_LAUNCH_CHECK("merkle_top_coop_kernel");
+    } else if (root_out) {
+        GB_CUDA_TRY(cudaMemcpyAsync(root_out, layer, 32, cudaMemcpyDeviceToDevice, stream()));
     }
     return GB_OK;
 }
@@ -170,25 +207,23 @@ int merkle_tree_gl_replicated(const u64* cw, u64* tree, size_t leaves, int copie
         return rc ? rc : merkle_build_from_leaves(tree, leaves);
     }
     cudaStream_t s = stream();
-    // one copy's subtree: its nodes are the leading entries of every layer
+    // one copy's subtree: its nodes are the leading entries of every layer; the copies are
+    // filled afterwards, all layers in one launch
     int rc = merkle_hash_leaves_gl(cw, tree, sub);
     if (rc) return rc;
-    size_t off = 0, layer_nodes = leaves, n = sub;
+    size_t off = 0, layer_nodes = leaves, n = sub, total = 0;
     for (;;) {
-        u64* layer = tree + off;
-        if (copies > 1) {
-            size_t work = n * 4 * (copies - 1);
-            replicate_kernel<<<grid_for(work, 256), 256, 0, s>>>(layer, n, (int)copies);
-            GB_LAUNCH_CHECK("replicate_kernel");
-        }
+        total += 4 * n * (copies - 1);
         if (n == 1) break;
         size_t half = n >> 1;
-        rc = merkle_level(layer, layer + 4 * layer_nodes, half);
+        rc = merkle_level(tree + off, tree + off + 4 * layer_nodes, half);
         if (rc) return rc;
         off += 4 * layer_nodes;
         layer_nodes >>= 1;
         n = half;
     }
+    replicate_layers_kernel<<<grid_for(total, 256), 256, 0, s>>>(tree, leaves, sub, (int)copies, total);
+    GB_LAUNCH_CHECK("replicate_layers_kernel");
     // the layer holding the copy roots is complete; finish the top copies_log levels
     return merkle_build_from_leaves(tree + off, layer_nodes);
 }
@@ -230,6 +265,13 @@ size_t gb_set_coop_threshold(size_t parents) {
     return old;
 }
 size_t gb_get_coop_threshold(void) { return t_coop_below; }
+
+size_t gb_set_merkle_top_nodes(size_t nodes) {
+    size_t old = t_top_nodes;
+    t_top_nodes = nodes < 2 ? 2 : nodes > 2048 ? 2048 : nodes;
+    return old;
+}
+size_t gb_get_merkle_top_nodes(void) { return t_top_nodes; }
 
 int poseidon2_hash_batch_ffi(const uint64_t* d_input, uint64_t* d_output, int n) {
     if (n < 0) return GB_EINVAL;

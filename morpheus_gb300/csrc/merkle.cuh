@@ -51,7 +51,9 @@ __device__ __forceinline__ void ld_digest(const u64* p, u64* s) {
 // thread (gb_set_coop_threshold); many concurrent proofs favour a lower one.
 constexpr size_t MK_COOP_BELOW_DEFAULT = 32768;
 size_t mk_coop_below();
-// Once a layer has at most this many nodes, the layers above it are finished by one CTA.
+// Once a layer has at most this many nodes, the layers above it are finished by one CTA
+// (default; the calling thread can raise it with gb_set_merkle_top_nodes: fewer launches,
+// a longer chain inside the one CTA).
 constexpr size_t MK_TOP_NODES = 16;
 
 // CTA size for a cooperative launch over `groups` 8-lane groups: small launches use
@@ -60,7 +62,8 @@ inline int coop_threads(size_t groups) { return groups * 8 >= (size_t)num_sms() 
 
 // Host-side tree builders (merkle.cu).  merkle_build_from_leaves expects the leaf
 // digests in layer 0.  All launches on gb::stream(); no synchronisation.
-int merkle_build_from_leaves(u64* tree, size_t leaves);
+// root_out (device, 4 words) also receives the root when given.
+int merkle_build_from_leaves(u64* tree, size_t leaves, u64* root_out = nullptr);
 int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves);
 int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves);
 // Tree over a base-field codeword made of 2^copies identical blocks: hashes one

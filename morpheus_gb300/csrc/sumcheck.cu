@@ -250,6 +250,84 @@ __global__ void __launch_bounds__(RED_THREADS) sc_fold_round_e2_kernel(const u64
     grid_reduce_finish<W>(acc, partials, msg, counter);
 }
 
+// Round k >= 2 (Ext2 input) for D <= 4 with lazy arithmetic:
+//   fold  a = x0 + r (x1 - x0) per coordinate as ONE three-word multiply-accumulate,
+//         c0 = x0.c0 + r0 d0 + (7 r1) d1,  c1 = x0.c1 + r0 d1 + r1 d0  (d = x1 - x0; r0, r1,
+//         7 r1 canonical, so each product is below 2^128 - 2^96), reduced once;
+//   message: s(c) = sum_y prod_i v_i(c): the product of the first D-1 factors is reduced, the
+//         last multiplication is accumulated as raw 128-bit products (schoolbook:
+//         A += p0 q0 + p1 (7 q1), C += p0 q1 + p1 q0), reduced once per thread.
+// Same outputs (mod p) as sc_fold_round_e2_kernel<D, false>.
+template <int D>
+__global__ void __launch_bounds__(RED_THREADS) sc_fold_round_e2_lazy_kernel(const u64* __restrict__ in, size_t in_stride,
+                                                                            u64* __restrict__ out, size_t out_stride,
+                                                                            size_t quarter, u64 r0_, u64 r1_,
+                                                                            u64* __restrict__ partials,
+                                                                            u64* __restrict__ msg,
+                                                                            unsigned* __restrict__ counter) {
+    constexpr int W = 2 * (D + 1);
+    const u64 r0 = gl_canon(r0_), r1 = gl_canon(r1_), r1x7 = gl_canon(gl_mul7(r1));
+    gl3 A[D + 1], C[D + 1];
+#pragma unroll
+    for (int c = 0; c <= D; c++) A[c] = C[c] = gl3_zero();
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < quarter; y += (size_t)gridDim.x * blockDim.x) {
+        e2 e[D], dl[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            const u64* p = in + (size_t)i * 2 * in_stride + 8 * y;
+            e2 x[4] = {ld_e2(p, true), ld_e2(p + 2, true), ld_e2(p + 4, true), ld_e2(p + 6, true)};
+            e2 f[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                u64 d0 = gl_sub(x[2 * h + 1].c0, x[2 * h].c0), d1 = gl_sub(x[2 * h + 1].c1, x[2 * h].c1);
+                gl3 c0 = gl3_zero(), c1 = gl3_zero();
+                c0.lo = x[2 * h].c0;
+                c1.lo = x[2 * h].c1;
+                gl3_add_prod(c0, r0, d0);
+                gl3_add_prod(c0, r1x7, d1);
+                gl3_add_prod(c1, r0, d1);
+                gl3_add_prod(c1, r1, d0);
+                f[h] = e2_make(gl3_reduce(c0), gl3_reduce(c1));
+            }
+            u64* q = out + (size_t)i * 2 * out_stride + 4 * y;
+            e2_st(q, f[0]);
+            e2_st(q + 2, f[1]);
+            e[i] = f[0];
+            dl[i] = e2_sub(f[1], f[0]);
+        }
+        e2 v[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) v[i] = e[i];
+#pragma unroll
+        for (int c = 0; c <= D; c++) {
+            e2 pre = v[0];
+#pragma unroll
+            for (int i = 1; i + 1 < D; i++) pre = e2_mul(pre, v[i]);
+            if constexpr (D == 1) {
+                gl3_add(A[c], pre.c0);
+                gl3_add(C[c], pre.c1);
+            } else {
+                const e2 last = v[D - 1];
+                gl3_add_prod(A[c], pre.c0, last.c0);
+                gl3_add_prod(A[c], pre.c1, gl_mul7(last.c1));
+                gl3_add_prod(C[c], pre.c0, last.c1);
+                gl3_add_prod(C[c], pre.c1, last.c0);
+            }
+            if (c < D) {
+#pragma unroll
+                for (int i = 0; i < D; i++) v[i] = e2_add(v[i], dl[i]);
+            }
+        }
+    }
+    u64 acc[W];
+#pragma unroll
+    for (int c = 0; c <= D; c++) {
+        acc[2 * c] = gl3_reduce(A[c]);
+        acc[2 * c + 1] = gl3_reduce(C[c]);
+    }
+    grid_reduce_finish<W>(acc, partials, msg, counter);
+}
+
 // Round k >= 1, base-field challenge (LinearSumcheckProver).
 template <int D>
 __global__ void __launch_bounds__(RED_THREADS) sc_fold_round_base_kernel(const u64* __restrict__ in, size_t in_stride,
@@ -364,6 +442,9 @@ struct FoldRoundE2 {
         if (base_in)
             sc_fold_round_e2_kernel<D, true><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
                                                                                  r0, r1, part, msg, ctr);
+        else if constexpr (D <= 4)
+            sc_fold_round_e2_lazy_kernel<D><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
+                                                                                r0, r1, part, msg, ctr);
         else
             sc_fold_round_e2_kernel<D, false><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
                                                                                   r0, r1, part, msg, ctr);

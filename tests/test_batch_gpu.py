@@ -124,3 +124,15 @@ def test_mixed_workload_shapes(gpu_lib):
     assert {i.degree for i in w} <= {2, 3, 4}
     assert min(i.num_vars for i in w) >= 4 and max(i.num_vars for i in w) <= 9
     assert all(int(i.polys.max()) < P for i in w)
+
+
+@pytest.mark.parametrize("coop,top", [(32768, 16), (0, 2), (1 << 40, 2048), (64, 256)])
+def test_merkle_schedule_does_not_change_proofs(tables, coop, top):
+    """The cooperative threshold and the single-CTA top size only change how the trees are
+    scheduled (commit trees with replicated copies and every open round's tree)."""
+    from morpheus_gb300 import batch
+    gt, ot = tables
+    inst = make(11, 2, 77, 4242)
+    with batch.Schedule(coop, top):
+        batch.prove_instance(gt, SEED, inst)
+    assert np.array_equal(inst.proof, oracle_instance_proof(inst.polys, inst.index, Q, ot))
