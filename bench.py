@@ -524,7 +524,7 @@ def main():
         fr_ms = min(ev_time(fr) for _ in range(5))
         fbytes = 2 * (1 << nf) * 16 + 2 * (1 << (nf - 1)) * 16
         extras["roofline_hbm"] = {
-            "kernel": "sc_fold_round_e2_kernel (fold 2 x 2^24 Ext2 + next round message)",
+            "kernel": "sc_fold_round_e2_lazy_kernel (fold 2 x 2^24 Ext2 + next round message)",
             "bound": "hbm", "achieved": fbytes / (fr_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
             "frac": fbytes / (fr_ms * 1e-3) / 1e9 / hbm_peak, "peak_source": src, "bytes_per_launch": fbytes,
             "launch_ms": fr_ms,
