@@ -257,11 +257,23 @@ def run_batched(args):
     for _ in range(max(0, args.warmup - 1)):
         batch.batch_prove(table, seed, insts, best)
     l0 = L.gb_launch_count()
-    with ClockSampler() as clk:
-        times = [wall(lambda: batch.batch_prove(table, seed, insts, best)) for _ in range(args.steps)]
-    launches = (L.gb_launch_count() - l0) // max(1, args.steps)
+    with ClockSampler() as clk_svc:
+        times_svc = [wall(lambda: batch.batch_prove(table, seed, insts, best)) for _ in range(args.steps)]
+    launches_svc = (L.gb_launch_count() - l0) // max(1, args.steps)
     same = sum(np.array_equal(i.proof, a) for i, a in zip(insts, alone))
-
+    # the round-synchronous engine on the same batch (same worker count for commits + sumchecks)
+    for i in insts:
+        i.proof[:] = 0
+    budget = 160 << 30
+    batch.batch_prove(table, seed, insts, best, budget, engine="lockstep")
+    l1 = L.gb_launch_count()
+    with ClockSampler() as clk_ls:
+        times_ls = [wall(lambda: batch.batch_prove(table, seed, insts, best, budget, engine="lockstep"))
+                    for _ in range(args.steps)]
+    launches_ls = (L.gb_launch_count() - l1) // max(1, args.steps)
+    same_ls = sum(np.array_equal(i.proof, a) for i, a in zip(insts, alone))
+    engine = "lockstep" if statistics.mean(times_ls) < statistics.mean(times_svc) else "service"
+    times, launches, clk = (times_ls, launches_ls, clk_ls) if engine == "lockstep" else (times_svc, launches_svc, clk_svc)
     # end to end: the same batch from pinned host memory (host->device copies inside)
     total = sum(i.polys.nbytes for i in insts)
     pinned = torch.empty(total, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint64)
@@ -271,8 +283,9 @@ def run_batched(args):
         pinned[o:o + k] = i.polys.reshape(-1)
         host_insts.append(batch.Instance(pinned[o:o + k].reshape(i.polys.shape), i.index, QUERIES))
         o += k
-    batch.batch_prove(table, seed, host_insts, best)
-    e2e_times = [wall(lambda: batch.batch_prove(table, seed, host_insts, best)) for _ in range(args.steps)]
+    batch.batch_prove(table, seed, host_insts, best, budget, engine=engine)
+    e2e_times = [wall(lambda: batch.batch_prove(table, seed, host_insts, best, budget, engine=engine))
+                 for _ in range(args.steps)]
     same_e2e = sum(np.array_equal(h.proof, a) for h, a in zip(host_insts, alone))
 
     step_s = statistics.mean(times)
@@ -282,7 +295,7 @@ def run_batched(args):
             "config": {"workload": f"{count} instances: product sumcheck + Basefold commit/open_ext2 of every "
                                    "polynomial at the sumcheck point; 2^10..2^20 evaluations (log-uniform), "
                                    "degree in {2,3,4}, rate 1/2, 34 queries, table (22, 1, 22, seed 42)",
-                       "instances": count, "evaluations": elems, "workers": best, "coop_threshold": coop, "merkle_top_nodes": top,
+                       "instances": count, "evaluations": elems, "engine": engine, "workers": best, "coop_threshold": coop, "merkle_top_nodes": top,
                        "l2": "inputs larger than L2 (batch inputs resident in HBM)",
                        "timing": "host wall clock between device synchronisations (the batch spans one "
                                  "stream per worker)", "parallelism": "replicas x1"},
@@ -290,7 +303,11 @@ def run_batched(args):
                          "how": "every instance through gb_prove_instance, one after another, one stream"},
             "batched_over_per_call": per_call_s / step_s,
             "autotune_s": {f"{k[0]}w/{k[1]}/{k[2]}": round(v, 4) for k, v in tune.items()},
-            "identical_to_per_call": {"device_inputs": f"{same}/{count}", "host_inputs": f"{same_e2e}/{count}"},
+            "identical_to_per_call": {"service": f"{same}/{count}", "lockstep": f"{same_ls}/{count}",
+                                      "host_inputs": f"{same_e2e}/{count}"},
+            "engines": {"service": {"ms_per_step": statistics.mean(times_svc) * 1e3, "gpu_launches": int(launches_svc)},
+                        "lockstep": {"ms_per_step": statistics.mean(times_ls) * 1e3, "gpu_launches": int(launches_ls)},
+                        "chosen": engine},
             "e2e": {"value": count / statistics.mean(e2e_times), "unit": "proofs/s",
                     "h2d_bytes_per_step": int(total),
                     "d2h_bytes_per_step": int(sum(i.proof.nbytes for i in insts))},

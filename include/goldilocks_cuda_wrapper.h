@@ -296,6 +296,14 @@ int gb_prover_destroy(void *prover);
 int gb_batch_prove(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *insts, int count,
                    int workers, size_t hbm_budget);
 
+/* The same batch as gb_batch_prove with the openings run round-synchronously: commits and
+ * sumchecks on `workers` threads, then every round of every polynomial's opening as one launch
+ * per step for all polynomials (and one per Merkle layer), with one host round trip per round.
+ * Instances that do not fit hbm_budget together run in waves, largest first.  Proofs are
+ * identical to gb_prove_instance's.  table: log_rate 1.  Synchronising. */
+int gb_batch_prove_lockstep(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *insts,
+                            int count, int workers, size_t hbm_budget);
+
 /* A quantized matmul layer C = A B as a served job (no reference counterpart; the field work
  * of zk-torch-3/src/basicblock/einsum.rs:807-1000): A is m x k, B is k x n (row-major int8),
  * m, n, k powers of two with m k >= 2^16.  The proof (gb_matmul_proof_len words, canonical):

@@ -187,17 +187,21 @@ class Schedule:
         L.gb_set_merkle_top_nodes(self._old[1])
 
 
-def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30, coop_threshold=None, top_nodes=None):
-    """All instances through the prover service, largest first, with the given Merkle
-    schedule (None keeps the calling thread's)."""
+def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30, coop_threshold=None, top_nodes=None,
+                engine="service"):
+    """All instances at once.  engine "service": the prover service, whole instances on worker
+    streams, largest first; "lockstep": commits and sumchecks on workers, then every
+    opening round-synchronously (one launch per step for all polynomials).  The Merkle schedule
+    (None keeps the calling thread's) applies to both; proofs are the same either way."""
     if not instances:
         return
     q = instances[0].num_queries
     assert all(i.num_queries == q for i in instances)
     arr = (GbInstance * len(instances))(*[i.struct() for i in instances])
+    fn = {"service": N.lib().gb_batch_prove, "lockstep": N.lib().gb_batch_prove_lockstep}[engine]
     with Schedule(coop_threshold, top_nodes):
-        N.check(N.lib().gb_batch_prove(table.handle, _seed(master_seed), q, arr, len(instances), workers,
-                                       hbm_budget), "gb_batch_prove")
+        N.check(fn(table.handle, _seed(master_seed), q, arr, len(instances), workers, hbm_budget),
+                "gb_batch_prove" if engine == "service" else "gb_batch_prove_lockstep")
 
 
 class ProverService:

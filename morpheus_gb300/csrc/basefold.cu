@@ -25,6 +25,7 @@
 #include "basefold.cuh"
 #include "host_field.hpp"
 #include "merkle.cuh"
+#include "bf_device.cuh"
 #include "reduce.cuh"
 
 namespace gb {
@@ -151,27 +152,6 @@ __global__ void sc_eval_kernel(const u64* __restrict__ d, u64 c0, u64 c1, u64* _
         e2 r = e2_add(e2_make(p[0], p[1]), e2_mul(e2_make(c0, c1), e2_make(p[2], p[3])));
         out[2 * i] = r.c0;
         out[2 * i + 1] = r.c1;
-    }
-}
-
-// val0 + (ch - x0) (val1 - val0) w     (basefold.cuh:397-419, :522-548, :739-761)
-// MODE 0: base cw + base ch; 1: base cw + Ext2 ch (mixed); 2: Ext2 cw + Ext2 ch
-template <int MODE>
-__device__ __forceinline__ void fold_pair(const u64* cw, size_t i, u64 x0, u64 w, u64 c0, u64 c1, u64* o) {
-    if (MODE == 0) {
-        u64 v0 = cw[2 * i], v1 = cw[2 * i + 1];
-        o[0] = gl_add(v0, gl_mul(gl_mul(gl_sub(c0, x0), gl_sub(v1, v0)), w));
-    } else if (MODE == 1) {
-        u64 v0 = cw[2 * i], v1 = cw[2 * i + 1];
-        u64 dw = gl_mul(gl_sub(v1, v0), w);
-        o[0] = gl_add(v0, gl_mul(gl_sub(c0, x0), dw));
-        o[1] = gl_mul(c1, dw);
-    } else {
-        e2 v0 = e2_make(cw[4 * i], cw[4 * i + 1]), v1 = e2_make(cw[4 * i + 2], cw[4 * i + 3]);
-        e2 dw = e2_mul_base(e2_sub(v1, v0), w);
-        e2 r = e2_add(v0, e2_mul(e2_make(gl_sub(c0, x0), c1), dw));
-        o[0] = r.c0;
-        o[1] = r.c1;
     }
 }
 
@@ -316,19 +296,8 @@ __global__ void __launch_bounds__(RED_THREADS) open_round0_kernel(const u64* __r
                                                                   size_t pairs, u64* __restrict__ partials,
                                                                   u64* __restrict__ out, unsigned* __restrict__ counter) {
     u64 acc[6] = {0, 0, 0, 0, 0, 0};
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x) {
-        ulonglong2 b2 = __ldg(reinterpret_cast<const ulonglong2*>(bh) + i);
-        e2 ee = e2_ld(eq + 4 * i), eo = e2_ld(eq + 4 * i + 2);
-        u64 bd = gl_sub(b2.y, b2.x);
-        e2 ed = e2_sub(eo, ee);
-        e2 t0 = e2_mul_base(ee, b2.x), t1 = e2_mul_base(eo, b2.y), t2 = e2_mul_base(ed, bd);
-        acc[0] = gl_add(acc[0], t0.c0);
-        acc[1] = gl_add(acc[1], t0.c1);
-        acc[2] = gl_add(acc[2], t1.c0);
-        acc[3] = gl_add(acc[3], t1.c1);
-        acc[4] = gl_add(acc[4], t2.c0);
-        acc[5] = gl_add(acc[5], t2.c1);
-    }
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x)
+        open_round0_item(bh, eq, i, acc);
     grid_reduce_finish<6>(acc, partials, out, counter);
 }
 
@@ -342,36 +311,8 @@ __global__ void __launch_bounds__(RED_THREADS) open_round_kernel(const u64* __re
                                                                  unsigned* __restrict__ counter) {
     u64 acc[6] = {0, 0, 0, 0, 0, 0};
     const e2 ch = e2_make(c0, c1);
-    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < quarter; y += (size_t)gridDim.x * blockDim.x) {
-        const u64* q = eq_in + 8 * y;
-        e2 x0 = e2_ld(q), x1 = e2_ld(q + 2), x2 = e2_ld(q + 4), x3 = e2_ld(q + 6);
-        e2 ea = e2_add(x0, e2_mul(ch, e2_sub(x1, x0)));
-        e2 eb = e2_add(x2, e2_mul(ch, e2_sub(x3, x2)));
-        e2 ba, bb;
-        if (BH_BASE) {
-            ulonglong2 p = __ldg(reinterpret_cast<const ulonglong2*>(bh_in + 4 * y));
-            ulonglong2 r = __ldg(reinterpret_cast<const ulonglong2*>(bh_in + 4 * y + 2));
-            u64 d0 = gl_sub(p.y, p.x), d1 = gl_sub(r.y, r.x);
-            ba = e2_make(gl_add(p.x, gl_mul(c0, d0)), gl_mul(c1, d0));
-            bb = e2_make(gl_add(r.x, gl_mul(c0, d1)), gl_mul(c1, d1));
-        } else {
-            const u64* h = bh_in + 8 * y;
-            e2 h0 = e2_ld(h), h1 = e2_ld(h + 2), h2 = e2_ld(h + 4), h3 = e2_ld(h + 6);
-            ba = e2_add(h0, e2_mul(ch, e2_sub(h1, h0)));
-            bb = e2_add(h2, e2_mul(ch, e2_sub(h3, h2)));
-        }
-        e2_st(eq_out + 4 * y, ea);
-        e2_st(eq_out + 4 * y + 2, eb);
-        e2_st(bh_out + 4 * y, ba);
-        e2_st(bh_out + 4 * y + 2, bb);
-        e2 t0 = e2_mul(ea, ba), t1 = e2_mul(eb, bb), t2 = e2_mul(e2_sub(eb, ea), e2_sub(bb, ba));
-        acc[0] = gl_add(acc[0], t0.c0);
-        acc[1] = gl_add(acc[1], t0.c1);
-        acc[2] = gl_add(acc[2], t1.c0);
-        acc[3] = gl_add(acc[3], t1.c1);
-        acc[4] = gl_add(acc[4], t2.c0);
-        acc[5] = gl_add(acc[5], t2.c1);
-    }
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < quarter; y += (size_t)gridDim.x * blockDim.x)
+        open_round_item<BH_BASE>(eq_in, bh_in, eq_out, bh_out, y, ch, acc);
     grid_reduce_finish<6>(acc, partials, out, counter);
 }
 
@@ -384,22 +325,8 @@ __global__ void __launch_bounds__(128) fold_hash_leaves_kernel(const u64* __rest
                                                                u64* __restrict__ tree, size_t leaves) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= leaves) return;
-    ulonglong2 t0 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i);
-    ulonglong2 t1 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i + 1);
     e2 f0, f1;
-    if (BASE_IN) {
-        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i);
-        ulonglong2 u = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i + 1);
-        u64 dw0 = gl_mul(gl_sub(v.y, v.x), t0.y), dw1 = gl_mul(gl_sub(u.y, u.x), t1.y);
-        f0 = e2_make(gl_add(v.x, gl_mul(gl_sub(c0, t0.x), dw0)), gl_mul(c1, dw0));
-        f1 = e2_make(gl_add(u.x, gl_mul(gl_sub(c0, t1.x), dw1)), gl_mul(c1, dw1));
-    } else {
-        const u64* p = cw + 8 * i;
-        e2 a0 = e2_ld(p), a1 = e2_ld(p + 2), b0 = e2_ld(p + 4), b1 = e2_ld(p + 6);
-        e2 dw0 = e2_mul_base(e2_sub(a1, a0), t0.y), dw1 = e2_mul_base(e2_sub(b1, b0), t1.y);
-        f0 = e2_add(a0, e2_mul(e2_make(gl_sub(c0, t0.x), c1), dw0));
-        f1 = e2_add(b0, e2_mul(e2_make(gl_sub(c0, t1.x), c1), dw1));
-    }
+    fold_leaf_item<BASE_IN>(cw, tab, i, c0, c1, f0, f1);
     e2_st(folded + 4 * i, f0);
     e2_st(folded + 4 * i + 2, f1);
     u64 s[8] = {f0.c0, f0.c1, f1.c0, f1.c1, 0, 0, 0, 0};
@@ -418,22 +345,8 @@ __global__ void __launch_bounds__(256) fold_hash_leaves_coop_kernel(const u64* _
     const int l = threadIdx.x & 7;
     const bool live = g < leaves;
     const size_t i = live ? g : 0;
-    ulonglong2 t0 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i);
-    ulonglong2 t1 = __ldg(reinterpret_cast<const ulonglong2*>(tab) + 2 * i + 1);
     e2 f0, f1;
-    if (BASE_IN) {
-        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i);
-        ulonglong2 u = __ldg(reinterpret_cast<const ulonglong2*>(cw) + 2 * i + 1);
-        u64 dw0 = gl_mul(gl_sub(v.y, v.x), t0.y), dw1 = gl_mul(gl_sub(u.y, u.x), t1.y);
-        f0 = e2_make(gl_add(v.x, gl_mul(gl_sub(c0, t0.x), dw0)), gl_mul(c1, dw0));
-        f1 = e2_make(gl_add(u.x, gl_mul(gl_sub(c0, t1.x), dw1)), gl_mul(c1, dw1));
-    } else {
-        const u64* p = cw + 8 * i;
-        e2 a0 = e2_ld(p), a1 = e2_ld(p + 2), b0 = e2_ld(p + 4), b1 = e2_ld(p + 6);
-        e2 dw0 = e2_mul_base(e2_sub(a1, a0), t0.y), dw1 = e2_mul_base(e2_sub(b1, b0), t1.y);
-        f0 = e2_add(a0, e2_mul(e2_make(gl_sub(c0, t0.x), c1), dw0));
-        f1 = e2_add(b0, e2_mul(e2_make(gl_sub(c0, t1.x), c1), dw1));
-    }
+    fold_leaf_item<BASE_IN>(cw, tab, i, c0, c1, f0, f1);
     u64 x = l == 0 ? f0.c0 : l == 1 ? f0.c1 : l == 2 ? f1.c0 : l == 3 ? f1.c1 : 0;
     if (live && l < 4) folded[4 * g + l] = x;
     P2Lane c = p2_lane_consts(l);
@@ -453,65 +366,11 @@ __global__ void fold_final_kernel(const u64* __restrict__ cw, const u64* __restr
     out[2 * i + 1] = gl_canon(o[1]);
 }
 
-// Query gather.  For query q with leaf index L (computed on the host from the transcript):
-// index, values of every round (initial pair lifted to Ext2, then the folded pairs) and all
-// authentication paths, written canonical into the flat proof layout.
-struct QueryJob {
-    const u64* cw0;           // base codeword
-    const u64* tree0;         // its tree
-    const u64* const* fcw;    // folded codewords r = 0..n-2 (device array of pointers)
-    const u64* const* ftree;  // their trees
-    int n, lr;
-};
-
 __global__ void query_gather_kernel(QueryJob job, const u64* __restrict__ leaf_idx, int num_queries, size_t per_query,
                                     u64* __restrict__ out) {
     int q = blockIdx.x;
     if (q >= num_queries) return;
-    const int n = job.n, lr = job.lr;
-    const size_t leaf = leaf_idx[q];
-    u64* o = out + (size_t)q * per_query;
-    u64* vals = o + 1;
-    u64* paths = vals + (size_t)n * 4;
-    if (threadIdx.x == 0) {
-        o[0] = leaf;
-        vals[0] = gl_canon(job.cw0[2 * leaf]);
-        vals[1] = 0;
-        vals[2] = gl_canon(job.cw0[2 * leaf + 1]);
-        vals[3] = 0;
-    }
-    for (int r = threadIdx.x; r + 1 < n; r += blockDim.x) {
-        size_t pi = leaf >> (r + 1);
-        const u64* f = job.fcw[r] + 4 * pi;
-        u64* v = vals + 4 * (r + 1);
-        for (int k = 0; k < 4; k++) v[k] = gl_canon(f[k]);
-    }
-    // path words: tree 0 has depth n+lr-1, tree r+1 (folded r) depth n+lr-2-r
-    size_t total_depth = 0;
-    for (int r = 0; r < n; r++) total_depth += (size_t)(n + lr - 1 - r);
-    for (size_t node = threadIdx.x; node < total_depth; node += blockDim.x) {
-        // locate (tree t, level l) of this path node
-        size_t rem = node;
-        int t = 0;
-        size_t depth = (size_t)(n + lr - 1);
-        while (rem >= depth) {
-            rem -= depth;
-            t++;
-            depth--;
-        }
-        int level = (int)rem;
-        size_t leaves = (size_t)1 << (n + lr - 1 - t);
-        const u64* tree = t == 0 ? job.tree0 : job.ftree[t - 1];
-        size_t li = (t == 0 ? leaf : (leaf >> t)) >> level;
-        size_t off = 0, sz = leaves;
-        for (int l = 0; l < level; l++) {
-            off += sz;
-            sz >>= 1;
-        }
-        const u64* dg = tree + 4 * (off + (li ^ 1));
-        u64* dst = paths + 4 * node;
-        for (int k = 0; k < 4; k++) dst[k] = gl_canon(dg[k]);
-    }
+    query_gather_block(job, leaf_idx[q], out + (size_t)q * per_query);
 }
 
 // ===========================================================================

@@ -1,0 +1,723 @@
+// Round-synchronous batch prover: many instances (gb_instance, the protocol of batch.cu) with
+// their Basefold openings run in lockstep, so that every step of a round is ONE launch over
+// all polynomials (ragged segment tables) instead of one launch per polynomial:
+//   1. commits and product sumchecks: a pool of worker threads, a stream each (as in the
+//      prover service), keeping every commitment resident;
+//   2. openings: for round r = 0, 1, ... on the calling thread's stream, one launch each for
+//      the eq/bh fold + oracle partials, their per-polynomial reduction, the codeword fold +
+//      leaf hash, every Merkle layer, the roots and the final folds of all polynomials still
+//      in round r; then one copy of all round records to the host, where each polynomial's
+//      own transcript advances exactly as in open_ext2 (basefold.rs:578-870);
+//   3. queries: one gather launch for all polynomials.
+// Work that does not fit the HBM budget runs in several waves (largest instances first).
+// Every proof is bit-identical to gb_prove_instance's.
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/goldilocks_cuda_wrapper.h"
+#include "basefold.cuh"
+#include "bf_device.cuh"
+#include "host_field.hpp"
+#include "merkle.cuh"
+#include "reduce.cuh"
+
+namespace gb {
+
+constexpr int LS_RED_THREADS = RED_THREADS;  // 256
+constexpr int LS_ITEMS = 4;                  // items per thread in the reduction kernels
+constexpr int LS_THREADS = 128;              // per-item kernels
+constexpr int LS_REC = 16;                   // record words per polynomial: oracle 0..5, root 8..11, final 12..15
+
+#define LS_RC(x)           \
+    do {                   \
+        int _r = (x);      \
+        if (_r) return _r; \
+    } while (0)
+
+// One polynomial's part of one launch.
+struct LsSeg {
+    const u64* a;
+    const u64* b;
+    u64* c;
+    u64* d;
+    u64 c0, c1;
+    u64 items;
+    u64 block0;
+};
+
+__device__ __forceinline__ int ls_find(const LsSeg* __restrict__ segs, int nseg, u64 block) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].block0 <= block) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+#define LS_SEG_PROLOGUE                                       \
+    __shared__ int s_seg;                                     \
+    if (threadIdx.x == 0) s_seg = ls_find(segs, nseg, blockIdx.x); \
+    __syncthreads();                                          \
+    const LsSeg sg = segs[s_seg];
+
+// round 0 oracle partials: a = bh (base), b = eq (Ext2), items = pairs
+__global__ void __launch_bounds__(LS_RED_THREADS) ls_round0_kernel(const LsSeg* __restrict__ segs, int nseg,
+                                                                   u64* __restrict__ partials) {
+    LS_SEG_PROLOGUE
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    const u64 base = (blockIdx.x - sg.block0) * (u64)blockDim.x * LS_ITEMS;
+#pragma unroll
+    for (int k = 0; k < LS_ITEMS; k++) {
+        u64 i = base + (u64)k * blockDim.x + threadIdx.x;
+        if (i < sg.items) open_round0_item(sg.a, sg.b, i, acc);
+    }
+    block_reduce<6>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int w = 0; w < 6; w++) partials[(size_t)blockIdx.x * 6 + w] = acc[w];
+}
+
+// round r >= 1 oracle partials with the eq/bh folds: a = eq_in, b = bh_in, c = eq_out, d = bh_out
+template <bool BH_BASE>
+__global__ void __launch_bounds__(LS_RED_THREADS) ls_open_round_kernel(const LsSeg* __restrict__ segs, int nseg,
+                                                                       u64* __restrict__ partials) {
+    LS_SEG_PROLOGUE
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    const e2 ch = e2_make(sg.c0, sg.c1);
+    const u64 base = (blockIdx.x - sg.block0) * (u64)blockDim.x * LS_ITEMS;
+#pragma unroll
+    for (int k = 0; k < LS_ITEMS; k++) {
+        u64 y = base + (u64)k * blockDim.x + threadIdx.x;
+        if (y < sg.items) open_round_item<BH_BASE>(sg.a, sg.b, sg.c, sg.d, y, ch, acc);
+    }
+    block_reduce<6>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int w = 0; w < 6; w++) partials[(size_t)blockIdx.x * 6 + w] = acc[w];
+}
+
+// per polynomial: sum its blocks' partials into recs[seg][0..5] (canonical); one warp each
+__global__ void ls_reduce_kernel(const LsSeg* __restrict__ segs, int nseg, const u64* __restrict__ partials,
+                                 u64* __restrict__ recs) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nseg) return;
+    const u64 per_block = (u64)LS_RED_THREADS * LS_ITEMS;
+    const u64 nb = (segs[w].items + per_block - 1) / per_block;
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    for (u64 b = lane; b < nb; b += 32)
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc[k] = gl_add(acc[k], partials[(segs[w].block0 + b) * 6 + k]);
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        u64 v = gl_warp_sum(acc[k]);
+        if (lane == 0) recs[(size_t)w * LS_REC + k] = gl_canon(v);
+    }
+}
+
+// codeword fold + leaf hash: a = codeword in, b = table level, c = folded out, d = tree leaves
+template <bool BASE_IN>
+__global__ void __launch_bounds__(LS_THREADS) ls_fold_hash_kernel(const LsSeg* __restrict__ segs, int nseg) {
+    LS_SEG_PROLOGUE
+    const u64 i = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
+    if (i >= sg.items) return;
+    e2 f0, f1;
+    fold_leaf_item<BASE_IN>(sg.a, sg.b, i, sg.c0, sg.c1, f0, f1);
+    e2_st(sg.c + 4 * i, f0);
+    e2_st(sg.c + 4 * i + 2, f1);
+    u64 s[8] = {f0.c0, f0.c1, f1.c0, f1.c1, 0, 0, 0, 0};
+    p2_permute(s);
+    st_digest(sg.d + 4 * i, s);
+}
+
+// one Merkle layer: a = children, c = parents
+__global__ void __launch_bounds__(LS_THREADS) ls_merkle_level_kernel(const LsSeg* __restrict__ segs, int nseg) {
+    LS_SEG_PROLOGUE
+    const u64 j = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
+    if (j >= sg.items) return;
+    u64 s[8];
+    ld_digest(sg.a + 8 * j, s);
+    ld_digest(sg.a + 8 * j + 4, s + 4);
+    p2_permute(s);
+    st_digest(sg.c + 4 * j, s);
+}
+
+// recs[seg][8..11] = root digest at a (canonical); one thread per polynomial
+__global__ void ls_root_kernel(const LsSeg* __restrict__ segs, int nseg, u64* __restrict__ recs) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+#pragma unroll
+    for (int k = 0; k < 4; k++) recs[(size_t)s * LS_REC + 8 + k] = gl_canon(segs[s].a[k]);
+}
+
+// last round's fold (Ext2 codeword, no tree): a = codeword in, b = table level, c = out,
+// items = pairs (<= 2 for rate 1/2); also copied into recs[seg][12..]
+__global__ void ls_fold_final_kernel(const LsSeg* __restrict__ segs, int nseg, u64* __restrict__ recs) {
+    int s = blockIdx.x;
+    if (s >= nseg) return;
+    const LsSeg sg = segs[s];
+    for (u64 i = threadIdx.x; i < sg.items; i += blockDim.x) {
+        u64 o[2];
+        fold_pair<2>(sg.a, i, sg.b[2 * i], sg.b[2 * i + 1], sg.c0, sg.c1, o);
+        sg.c[2 * i] = gl_canon(o[0]);
+        sg.c[2 * i + 1] = gl_canon(o[1]);
+        if (2 * i + 1 < 4) {
+            recs[(size_t)s * LS_REC + 12 + 2 * i] = gl_canon(o[0]);
+            recs[(size_t)s * LS_REC + 13 + 2 * i] = gl_canon(o[1]);
+        }
+    }
+}
+
+// all polynomials' queries: block (query k, polynomial p)
+__global__ void ls_query_kernel(const QueryJob* __restrict__ jobs, const u64* __restrict__ idx, int q,
+                                u64* const* __restrict__ outs, const u64* __restrict__ per_query) {
+    const int k = blockIdx.x, p = blockIdx.y;
+    query_gather_block(jobs[p], idx[(size_t)p * q + k], outs[p] + (size_t)k * per_query[p]);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static size_t align2(size_t w) { return (w + 1) & ~(size_t)1; }  // 16-byte multiples of words
+
+struct LsPoly {
+    int n = 0;
+    size_t N = 0, L = 0;
+    const BfCommitment* com = nullptr;
+    const u64* point = nullptr;  // host, 2n canonical words (the instance's sumcheck challenges)
+    gb_transcript t;
+    u64* proof = nullptr;  // host, gb_basefold_proof_len(n, 1, q) words
+    u64 *d_point = nullptr, *eq = nullptr, *bufs_eq[2] = {nullptr, nullptr}, *bufs_bh[2] = {nullptr, nullptr};
+    std::vector<u64*> fcw, ftree;
+    const u64* eq_cur = nullptr;
+    const u64* bh_cur = nullptr;
+    int pp = 0;
+    size_t sc = 0;
+};
+
+// device words one polynomial's opening needs
+static size_t ls_poly_words(int n, int lr) {
+    size_t N = (size_t)1 << n, L = N << lr, w = 0;
+    w += align2(2 * (size_t)n) + 2 * N + 4 * N;  // point, eq, eqA, eqB, bhA, bhB (N/2 Ext2 each)
+    for (int r = 0; r < n; r++) w += align2(2 * (L >> (r + 1)));
+    for (int r = 0; r + 1 < n; r++) w += 4 * (2 * ((L >> (r + 1)) / 2) - 1) + 2;
+    return w;
+}
+
+class LsRunner {
+  public:
+    LsRunner(const BfTable* tab, int q) : tab_(tab), q_(q) {}
+
+    // openings of `polys` (transcripts already hold their "bf-open" preamble prefix)
+    int open(std::vector<LsPoly>& P) {
+        using namespace host;
+        cudaStream_t s = stream();
+        const int np = (int)P.size();
+        const int lr = 1;
+        size_t words = 0;
+        for (auto& p : P) words += ls_poly_words(p.n, lr);
+        int maxn = 0;
+        for (auto& p : P) maxn = std::max(maxn, p.n);
+        // workspace carving
+        GB_CUDA_TRY(cudaMallocAsync(&ws_, std::max<size_t>(words, 2) * 8, s));
+        {
+            u64* cur = ws_;
+            for (auto& p : P) {
+                p.d_point = cur;
+                cur += align2(2 * (size_t)p.n);
+                p.eq = cur;
+                cur += 2 * p.N;
+                p.bufs_eq[0] = cur;
+                cur += p.N;
+                p.bufs_eq[1] = cur;
+                cur += p.N;
+                p.bufs_bh[0] = cur;
+                cur += p.N;
+                p.bufs_bh[1] = cur;
+                cur += p.N;
+                p.fcw.assign(p.n, nullptr);
+                p.ftree.assign(p.n > 1 ? p.n - 1 : 0, nullptr);
+                for (int r = 0; r < p.n; r++) {
+                    p.fcw[r] = cur;
+                    cur += align2(2 * (p.L >> (r + 1)));
+                }
+                for (int r = 0; r + 1 < p.n; r++) {
+                    p.ftree[r] = cur;
+                    cur += 4 * (2 * ((p.L >> (r + 1)) / 2) - 1) + 2;
+                }
+            }
+        }
+        // per-launch tables and records
+        np_max_ = (size_t)np;
+        seg_cap_ = (size_t)np * (maxn + 8);  // one round's launches (layers + 4) never need more slots
+        GB_CUDA_TRY(cudaMallocAsync(&d_segs_, seg_cap_ * sizeof(LsSeg), s));
+        GB_CUDA_TRY(cudaMallocAsync(&d_recs_, (size_t)np * LS_REC * 8, s));
+        GB_CUDA_TRY(cudaMallocHost(&h_segs_, seg_cap_ * sizeof(LsSeg)));
+        GB_CUDA_TRY(cudaMallocHost(&h_recs_, (size_t)np * LS_REC * 8));
+        size_t max_blocks = 0;
+        for (auto& p : P) max_blocks += (p.N / 2 + LS_RED_THREADS * LS_ITEMS - 1) / (LS_RED_THREADS * LS_ITEMS) + 1;
+        GB_CUDA_TRY(cudaMallocAsync(&d_partials_, max_blocks * 6 * 8, s));
+
+        // preamble: root and point into each transcript; eq tables
+        {
+            std::vector<u64> pts;
+            for (auto& p : P) {
+                for (int k = 0; k < 4; k++) tr_append_u64(&p.t, "", p.com->root[k]);
+                for (int i = 0; i < p.n; i++) tr_append_ext2(&p.t, "", E2{canon(p.point[2 * i]), canon(p.point[2 * i + 1])});
+            }
+            for (auto& p : P) {
+                std::vector<u64> v(2 * p.n);
+                for (int i = 0; i < 2 * p.n; i++) v[i] = canon(p.point[i]);
+                GB_CUDA_TRY(cudaMemcpyAsync(p.d_point, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s));
+                int rc = eq_table(p.d_point, p.n, true, p.eq);
+                if (rc) return rc;
+            }
+            GB_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors above go out of scope
+        }
+        // round 0 oracle
+        std::vector<int> all(np);
+        std::iota(all.begin(), all.end(), 0);
+        {
+            u64 nb = 0;
+            LsSeg* hs = next_slot(); if (!hs) return GB_EINVAL;
+            for (int k = 0; k < np; k++) {
+                LsPoly& p = P[k];
+                hs[k] = LsSeg{p.com->d_evals, p.eq, nullptr, nullptr, 0, 0, p.N / 2, nb};
+                nb += blocks_red(p.N / 2);
+            }
+            const LsSeg* ds = upload(hs, np);
+            if (!ds) return GB_ECUDA;
+            ls_round0_kernel<<<(unsigned)nb, LS_RED_THREADS, 0, s>>>(ds, np, d_partials_);
+            GB_LAUNCH_CHECK("ls_round0_kernel");
+            ls_reduce_kernel<<<(unsigned)((np * 32 + 255) / 256), 256, 0, s>>>(ds, np, d_partials_, d_recs_);
+            GB_LAUNCH_CHECK("ls_reduce_kernel");
+            LS_RC(read_recs(np));
+            for (int k = 0; k < np; k++) {
+                LsPoly& p = P[k];
+                const u64* rec = h_recs_ + (size_t)k * LS_REC;
+                E2 c0{rec[0], rec[1]};
+                E2 s1 = put_oracle(p, 0, rec);
+                E2 ev = e2add(c0, s1);
+                p.proof[0] = ev.c0;
+                p.proof[1] = ev.c1;
+                p.eq_cur = p.eq;
+                p.bh_cur = p.com->d_evals;
+                p.pp = 0;
+                p.sc = p.N;
+            }
+        }
+        // rounds
+        std::vector<E2> ch(np);
+        for (int rd = 0; rd < maxn; rd++) {
+            std::vector<int> mid, last;  // still folding with a tree / final fold
+            for (int k = 0; k < np; k++) {
+                if (rd >= P[k].n) continue;
+                ch[k] = tr_challenge_ext2(&P[k].t, "");
+                (rd < P[k].n - 1 ? mid : last).push_back(k);
+            }
+            if (!mid.empty()) {
+                // eq/bh folds + next oracle
+                u64 nb = 0;
+                LsSeg* hs = next_slot(); if (!hs) return GB_EINVAL;
+                for (size_t m = 0; m < mid.size(); m++) {
+                    LsPoly& p = P[mid[m]];
+                    size_t quarter = p.sc / 4;
+                    hs[m] = LsSeg{p.eq_cur, p.bh_cur, p.bufs_eq[p.pp], p.bufs_bh[p.pp], ch[mid[m]].c0, ch[mid[m]].c1,
+                                  quarter, nb};
+                    nb += blocks_red(quarter);
+                }
+                const LsSeg* ds = upload(hs, (int)mid.size());
+                if (!ds) return GB_ECUDA;
+                if (rd == 0)
+                    ls_open_round_kernel<true><<<(unsigned)nb, LS_RED_THREADS, 0, s>>>(ds, (int)mid.size(), d_partials_);
+                else
+                    ls_open_round_kernel<false><<<(unsigned)nb, LS_RED_THREADS, 0, s>>>(ds, (int)mid.size(), d_partials_);
+                GB_LAUNCH_CHECK("ls_open_round_kernel");
+                // records of `mid` are written in mid order; the host reads them back by m
+                ls_reduce_kernel<<<(unsigned)((mid.size() * 32 + 255) / 256), 256, 0, s>>>(ds, (int)mid.size(),
+                                                                                           d_partials_, d_recs_);
+                GB_LAUNCH_CHECK("ls_reduce_kernel");
+                for (int k : mid) {
+                    LsPoly& p = P[k];
+                    p.eq_cur = p.bufs_eq[p.pp];
+                    p.bh_cur = p.bufs_bh[p.pp];
+                    p.pp ^= 1;
+                    p.sc /= 2;
+                }
+                // codeword fold + leaf hash
+                nb = 0;
+                hs = next_slot(); if (!hs) return GB_EINVAL;
+                for (size_t m = 0; m < mid.size(); m++) {
+                    LsPoly& p = P[mid[m]];
+                    size_t leaves = (p.L >> (rd + 1)) / 2;
+                    const u64* cw_in = rd == 0 ? p.com->d_codeword : p.fcw[rd - 1];
+                    hs[m] = LsSeg{cw_in, tab_->d_entries + 2 * tab_->level_offsets[rd], p.fcw[rd], p.ftree[rd],
+                                  ch[mid[m]].c0, ch[mid[m]].c1, leaves, nb};
+                    nb += blocks(leaves);
+                }
+                ds = upload(hs, (int)mid.size());
+                if (!ds) return GB_ECUDA;
+                if (rd == 0) ls_fold_hash_kernel<true><<<(unsigned)nb, LS_THREADS, 0, s>>>(ds, (int)mid.size());
+                else ls_fold_hash_kernel<false><<<(unsigned)nb, LS_THREADS, 0, s>>>(ds, (int)mid.size());
+                GB_LAUNCH_CHECK("ls_fold_hash_kernel");
+                // Merkle layers, all trees at once
+                for (int lvl = 0;; lvl++) {
+                    int cnt = 0;
+                    nb = 0;
+                    hs = next_slot(); if (!hs) return GB_EINVAL;
+                    for (size_t m = 0; m < mid.size(); m++) {
+                        LsPoly& p = P[mid[m]];
+                        size_t leaves = (p.L >> (rd + 1)) / 2;
+                        size_t nodes = leaves >> lvl;
+                        if (nodes < 2) continue;
+                        size_t off = 0;
+                        for (int l = 0; l < lvl; l++) off += leaves >> l;
+                        u64* layer = p.ftree[rd] + 4 * off;
+                        hs[cnt++] = LsSeg{layer, nullptr, layer + 4 * nodes, nullptr, 0, 0, nodes / 2, nb};
+                        nb += blocks(nodes / 2);
+                    }
+                    if (!cnt) {
+                        unslot();
+                        break;
+                    }
+                    ds = upload(hs, cnt);
+                    if (!ds) return GB_ECUDA;
+                    ls_merkle_level_kernel<<<(unsigned)nb, LS_THREADS, 0, s>>>(ds, cnt);
+                    GB_LAUNCH_CHECK("ls_merkle_level_kernel");
+                }
+                hs = next_slot(); if (!hs) return GB_EINVAL;
+                for (size_t m = 0; m < mid.size(); m++) {
+                    LsPoly& p = P[mid[m]];
+                    size_t leaves = (p.L >> (rd + 1)) / 2;
+                    hs[m] = LsSeg{p.ftree[rd] + 4 * (2 * leaves - 2), nullptr, nullptr, nullptr, 0, 0, 0, 0};
+                }
+                ds = upload(hs, (int)mid.size());
+                if (!ds) return GB_ECUDA;
+                ls_root_kernel<<<(unsigned)((mid.size() + 127) / 128), 128, 0, s>>>(ds, (int)mid.size(), d_recs_);
+                GB_LAUNCH_CHECK("ls_root_kernel");
+                LS_RC(read_recs((int)mid.size()));
+                for (size_t m = 0; m < mid.size(); m++) {
+                    LsPoly& p = P[mid[m]];
+                    const u64* rec = h_recs_ + m * LS_REC;
+                    put_oracle(p, rd + 1, rec);
+                    u64* root = p.proof + 2 + (size_t)p.n * 6 + (size_t)rd * 4;
+                    for (int k = 0; k < 4; k++) {
+                        root[k] = rec[8 + k];
+                        tr_append_u64(&p.t, "", root[k]);
+                    }
+                }
+            }
+            if (!last.empty()) {
+                LsSeg* hs = next_slot(); if (!hs) return GB_EINVAL;
+                for (size_t m = 0; m < last.size(); m++) {
+                    LsPoly& p = P[last[m]];
+                    size_t pairs = p.L >> (rd + 1);
+                    const u64* cw_in = rd == 0 ? p.com->d_codeword : p.fcw[rd - 1];
+                    hs[m] = LsSeg{cw_in, tab_->d_entries + 2 * tab_->level_offsets[rd], p.fcw[rd], nullptr,
+                                  ch[last[m]].c0, ch[last[m]].c1, pairs, 0};
+                }
+                const LsSeg* ds = upload(hs, (int)last.size());
+                if (!ds) return GB_ECUDA;
+                ls_fold_final_kernel<<<(unsigned)last.size(), 32, 0, s>>>(ds, (int)last.size(), d_recs_);
+                GB_LAUNCH_CHECK("ls_fold_final_kernel");
+                LS_RC(read_recs((int)last.size()));
+                for (size_t m = 0; m < last.size(); m++) {
+                    LsPoly& p = P[last[m]];
+                    u64* fin = p.proof + 2 + (size_t)p.n * 6 + (size_t)(p.n - 1) * 4;
+                    for (int k = 0; k < (2 << lr); k++) fin[k] = h_recs_[m * LS_REC + 12 + k];
+                }
+            }
+        }
+        // queries: indices from each transcript, one gather launch
+        if (q_ > 0) {
+            std::vector<QueryJob> jobs(np);
+            std::vector<u64> idx((size_t)np * q_), per_q(np);
+            std::vector<const u64*> ptrs;
+            std::vector<size_t> out_off(np);
+            size_t out_words = 0;
+            for (int k = 0; k < np; k++) {
+                LsPoly& p = P[k];
+                for (int j = 0; j < q_; j++) idx[(size_t)k * q_ + j] = tr_challenge(&p.t, "") % (u64)(p.L / 2);
+                size_t pw = 0;
+                for (int r = 0; r < p.n; r++) pw += (size_t)(p.n + lr - 1 - r);
+                per_q[k] = 1 + (size_t)p.n * 4 + pw * 4;
+                out_off[k] = out_words;
+                out_words += per_q[k] * q_;
+            }
+            // pointer tables: per polynomial fcw[0..n-2] then ftree[0..n-2]
+            std::vector<size_t> ptr_off(np);
+            for (int k = 0; k < np; k++) {
+                ptr_off[k] = ptrs.size();
+                for (int r = 0; r + 1 < P[k].n; r++) ptrs.push_back(P[k].fcw[r]);
+                for (int r = 0; r + 1 < P[k].n; r++) ptrs.push_back(P[k].ftree[r]);
+            }
+            u64 *d_idx = nullptr, *d_perq = nullptr, *d_out = nullptr;
+            const u64** d_ptrs = nullptr;
+            QueryJob* d_jobs = nullptr;
+            u64** d_outs = nullptr;
+            GB_CUDA_TRY(cudaMallocAsync(&d_idx, idx.size() * 8, s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_perq, per_q.size() * 8, s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_out, std::max<size_t>(out_words, 1) * 8, s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_ptrs, std::max<size_t>(ptrs.size(), 1) * sizeof(u64*), s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_jobs, (size_t)np * sizeof(QueryJob), s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_outs, (size_t)np * sizeof(u64*), s));
+            std::vector<u64*> outs(np);
+            for (int k = 0; k < np; k++) {
+                LsPoly& p = P[k];
+                const u64* const* base = d_ptrs + ptr_off[k];
+                jobs[k] = QueryJob{p.com->d_codeword, p.com->d_tree, base, base + (p.n - 1), p.n, lr};
+                outs[k] = d_out + out_off[k];
+            }
+            GB_CUDA_TRY(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * 8, cudaMemcpyHostToDevice, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(d_perq, per_q.data(), per_q.size() * 8, cudaMemcpyHostToDevice, s));
+            if (!ptrs.empty())
+                GB_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), ptrs.size() * sizeof(u64*), cudaMemcpyHostToDevice, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(QueryJob), cudaMemcpyHostToDevice, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(d_outs, outs.data(), outs.size() * sizeof(u64*), cudaMemcpyHostToDevice, s));
+            ls_query_kernel<<<dim3((unsigned)q_, (unsigned)np), 128, 0, s>>>(d_jobs, d_idx, q_, d_outs, d_perq);
+            GB_LAUNCH_CHECK("ls_query_kernel");
+            std::vector<u64> host_out(out_words);
+            GB_CUDA_TRY(cudaMemcpyAsync(host_out.data(), d_out, out_words * 8, cudaMemcpyDeviceToHost, s));
+            GB_CUDA_TRY(cudaStreamSynchronize(s));
+            for (int k = 0; k < np; k++) {
+                LsPoly& p = P[k];
+                u64* dst = p.proof + 2 + (size_t)p.n * 6 + (size_t)(p.n - 1) * 4 + ((size_t)2 << lr);
+                std::memcpy(dst, host_out.data() + out_off[k], per_q[k] * q_ * 8);
+            }
+            for (void* x : {(void*)d_idx, (void*)d_perq, (void*)d_out, (void*)d_ptrs, (void*)d_jobs, (void*)d_outs})
+                cudaFreeAsync(x, s);
+        }
+        return GB_OK;
+    }
+
+    ~LsRunner() {
+        cudaStream_t s = stream();
+        if (ws_) cudaFreeAsync(ws_, s);
+        if (d_segs_) cudaFreeAsync(d_segs_, s);
+        if (d_recs_) cudaFreeAsync(d_recs_, s);
+        if (d_partials_) cudaFreeAsync(d_partials_, s);
+        cudaStreamSynchronize(s);
+        if (h_segs_) cudaFreeHost(h_segs_);
+        if (h_recs_) cudaFreeHost(h_recs_);
+    }
+
+  private:
+    static u64 blocks_red(u64 items) {
+        u64 per = (u64)LS_RED_THREADS * LS_ITEMS;
+        return items ? (items + per - 1) / per : 1;
+    }
+    static u64 blocks(u64 items) { return items ? (items + LS_THREADS - 1) / LS_THREADS : 1; }
+    // Descriptor slots: each launch takes a fresh slot of np entries; the slots are reused only
+    // after read_recs, which waits for every launch before it.
+    LsSeg* next_slot() {
+        if (slot_ + 1 > seg_cap_ / np_max_) return nullptr;
+        return h_segs_ + (slot_++) * np_max_;
+    }
+    void unslot() { slot_--; }
+    const LsSeg* upload(const LsSeg* hs, int count) {
+        if (!hs) return nullptr;
+        size_t off = (size_t)(hs - h_segs_);
+        if (cudaMemcpyAsync(d_segs_ + off, hs, (size_t)count * sizeof(LsSeg), cudaMemcpyHostToDevice, stream()) !=
+            cudaSuccess)
+            return nullptr;
+        return d_segs_ + off;
+    }
+    int read_recs(int count) {
+        GB_CUDA_TRY(cudaMemcpyAsync(h_recs_, d_recs_, (size_t)count * LS_REC * 8, cudaMemcpyDeviceToHost, stream()));
+        GB_CUDA_TRY(cudaStreamSynchronize(stream()));
+        slot_ = 0;
+        return GB_OK;
+    }
+    // oracle r from a record (c0, s1, c2): c1 = s1 - c0 - c2; written to the proof and the transcript
+    static host::E2 put_oracle(LsPoly& p, int r, const u64* rec) {
+        using namespace host;
+        E2 c0{rec[0], rec[1]}, s1{rec[2], rec[3]}, c2{rec[4], rec[5]};
+        E2 c1 = e2sub(e2sub(s1, c0), c2);
+        u64* o = p.proof + 2 + (size_t)r * 6;
+        o[0] = c0.c0;
+        o[1] = c0.c1;
+        o[2] = c1.c0;
+        o[3] = c1.c1;
+        o[4] = c2.c0;
+        o[5] = c2.c1;
+        tr_append_ext2(&p.t, "", c0);
+        tr_append_ext2(&p.t, "", c1);
+        tr_append_ext2(&p.t, "", c2);
+        return s1;
+    }
+
+    const BfTable* tab_;
+    int q_;
+    u64* ws_ = nullptr;
+    LsSeg* d_segs_ = nullptr;
+    LsSeg* h_segs_ = nullptr;
+    u64* d_recs_ = nullptr;
+    u64* h_recs_ = nullptr;
+    u64* d_partials_ = nullptr;
+    size_t seg_cap_ = 0, np_max_ = 1, slot_ = 0;
+};
+// ---------------------------------------------------------------------------
+// driver: waves of instances; commits + sumchecks on worker threads, openings in lockstep
+// ---------------------------------------------------------------------------
+// words of an instance proof before its openings (batch.cu's layout)
+static size_t inst_proof_words_before_opens(int n, int d) {
+    return (size_t)d * 4 + (size_t)n * (d + 1) * 2 + (size_t)n * 2 + (size_t)d * 2 + 2;
+}
+
+static size_t ls_inst_bytes(const gb_instance& in) {
+    size_t N = (size_t)1 << in.num_vars;
+    // uploaded inputs, commitments (evaluations, codeword, tree), the sumcheck's levels and the
+    // opening workspace, per polynomial
+    return (size_t)in.degree * (N * (8 + 8 + 16 + 64 + 16) + ls_poly_words(in.num_vars, 1) * 8) + ((size_t)1 << 20);
+}
+
+static int ls_commit_and_sumcheck(const u64 seed[2], const gb_instance& in, std::vector<void*>& com, u64*& owned) {
+    using namespace host;
+    const int n = in.num_vars, d = in.degree;
+    const size_t N = (size_t)1 << n;
+    cudaStream_t s = stream();
+    const u64* polys = in.d_polys;
+    if (in.h_polys) {
+        GB_CUDA_TRY(cudaMallocAsync(&owned, N * d * 8, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(owned, in.h_polys, N * d * 8, cudaMemcpyHostToDevice, s));
+        polys = owned;
+    }
+    u64* roots = in.h_proof;
+    u64* msgs = roots + (size_t)d * 4;
+    u64* chal = msgs + (size_t)n * (d + 1) * 2;
+    u64* finals = chal + (size_t)n * 2;
+    u64* fe = finals + (size_t)d * 2;
+    com.assign(d, nullptr);
+    for (int j = 0; j < d; j++) {
+        int rc = gb_basefold_commit(polys + (size_t)j * N, nullptr, n, 1, &com[j], roots + 4 * j);
+        if (rc) return rc;
+    }
+    gb_transcript t;
+    gb_transcript_new(&t, "sumcheck");
+    tr_append_ext2(&t, "", E2{canon(seed[0]), canon(seed[1])});
+    tr_append_u64(&t, "", in.index);
+    for (int k = 0; k < 4 * d; k++) tr_append_u64(&t, "", roots[k]);
+    return gb_sumcheck_prove_ext2(&t, n, d, polys, nullptr, msgs, chal, finals, fe);
+}
+
+static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instance* insts, int count, int workers,
+                          size_t budget) {
+    using namespace host;
+    const BfTable* tab = (const BfTable*)table;
+    if (!tab || !seed || count < 0 || (count && !insts) || workers < 1 || q < 0 || tab->log_rate != 1) {
+        set_error_msg("gb_batch_prove_lockstep: invalid argument (the table must have log_rate 1)");
+        return GB_EINVAL;
+    }
+    for (int i = 0; i < count; i++) {
+        const gb_instance& in = insts[i];
+        if (in.num_vars < 2 || in.num_vars > 30 || in.degree < 1 || in.degree > 8 || (!in.h_polys == !in.d_polys) ||
+            !in.h_proof || tab->num_vars < in.num_vars || tab->num_rounds < in.num_vars) {
+            set_error_msg("gb_batch_prove_lockstep: invalid instance " + std::to_string(i));
+            return GB_EINVAL;
+        }
+    }
+    std::vector<int> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return ls_inst_bytes(insts[a]) > ls_inst_bytes(insts[b]); });
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    const size_t coop = gb_get_coop_threshold(), top = gb_get_merkle_top_nodes();
+    size_t next = 0;
+    while (next < order.size()) {
+        // the wave: largest remaining first, as many as fit the budget (at least one)
+        std::vector<int> wave;
+        size_t used = 0;
+        while (next < order.size() && (wave.empty() || used + ls_inst_bytes(insts[order[next]]) <= budget)) {
+            used += ls_inst_bytes(insts[order[next]]);
+            wave.push_back(order[next++]);
+        }
+        std::vector<std::vector<void*>> com(wave.size());
+        std::vector<u64*> owned(wave.size(), nullptr);
+        std::vector<int> rcs(wave.size(), GB_OK);
+        std::vector<std::string> errs(wave.size());
+        std::atomic<size_t> cursor{0};
+        const int nt = (int)std::min<size_t>((size_t)workers, wave.size());
+        std::vector<std::thread> th;
+        for (int w = 0; w < nt; w++)
+            th.emplace_back([&] {
+                cudaStream_t st = nullptr;
+                if (cudaSetDevice(dev) != cudaSuccess || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+                    st = nullptr;
+                if (st) gb_set_stream(st);
+                gb_set_coop_threshold(coop);
+                gb_set_merkle_top_nodes(top);
+                for (size_t k; (k = cursor.fetch_add(1)) < wave.size();) {
+                    int rc = st ? ls_commit_and_sumcheck(seed, insts[wave[k]], com[k], owned[k]) : GB_ECUDA;
+                    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = GB_ECUDA;
+                    rcs[k] = rc;
+                    if (rc) errs[k] = st ? gb_last_error() : "stream creation failed";
+                }
+                if (st) {
+                    cudaStreamSynchronize(st);
+                    gb_set_stream(nullptr);
+                    cudaStreamDestroy(st);
+                }
+            });
+        for (auto& t : th) t.join();
+        int rc = GB_OK;
+        for (size_t k = 0; k < wave.size() && !rc; k++)
+            if (rcs[k]) {
+                rc = rcs[k];
+                set_error_msg(errs[k]);
+            }
+        if (!rc) {
+            // openings of every polynomial of the wave, in lockstep
+            std::vector<LsPoly> P;
+            for (size_t k = 0; k < wave.size(); k++) {
+                const gb_instance& in = insts[wave[k]];
+                const int n = in.num_vars, d = in.degree;
+                const size_t plen = gb_basefold_proof_len(n, 1, q);
+                const u64* chal = in.h_proof + (size_t)d * 4 + (size_t)n * (d + 1) * 2;
+                u64* opens = in.h_proof + inst_proof_words_before_opens(n, d);
+                for (int j = 0; j < d; j++) {
+                    LsPoly p;
+                    p.n = n;
+                    p.N = (size_t)1 << n;
+                    p.L = p.N << 1;
+                    p.com = (const BfCommitment*)com[k][j];
+                    p.point = chal;
+                    gb_transcript_new(&p.t, "bf-open");
+                    tr_append_ext2(&p.t, "", E2{canon(seed[0]), canon(seed[1])});
+                    tr_append_u64(&p.t, "", 8 * in.index + (u64)j);
+                    p.proof = opens + (size_t)j * plen;
+                    P.push_back(std::move(p));
+                }
+            }
+            LsRunner runner(tab, q);
+            rc = runner.open(P);
+        }
+        cudaStream_t s = stream();
+        for (size_t k = 0; k < wave.size(); k++) {
+            for (void* c : com[k])
+                if (c) gb_basefold_commitment_destroy(c);
+            if (owned[k]) cudaFreeAsync(owned[k], s);
+        }
+        if (rc) return rc;
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    return GB_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int gb_batch_prove_lockstep(void* table, const uint64_t master_seed[2], int num_queries, const gb_instance* insts,
+                            int count, int workers, size_t hbm_budget) {
+    return lockstep_prove(table, master_seed, num_queries, insts, count, workers, hbm_budget);
+}
+
+}  // extern "C"

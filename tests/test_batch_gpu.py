@@ -136,3 +136,24 @@ def test_merkle_schedule_does_not_change_proofs(tables, coop, top):
     with batch.Schedule(coop, top):
         batch.prove_instance(gt, SEED, inst)
     assert np.array_equal(inst.proof, oracle_instance_proof(inst.polys, inst.index, Q, ot))
+
+
+@pytest.mark.parametrize("budget,device", [(64 << 30, True), (1, False)])
+def test_lockstep_engine_equals_alone(tables, budget, device):
+    """The round-synchronous engine gives every instance its alone-run proof, in one wave or
+    (1-byte budget) one instance per wave, from device or host inputs."""
+    from morpheus_gb300 import batch
+    gt, ot = tables
+    rng = np.random.default_rng(21)
+    specs = [(int(rng.integers(2, TABLE_NV + 1)), int(rng.integers(1, 5))) for _ in range(20)] + [(2, 1), (TABLE_NV, 4)]
+    alone = [make(n, d, k, 300 + k) for k, (n, d) in enumerate(specs)]
+    for inst in alone:
+        batch.prove_instance(gt, SEED, inst)
+    together = [make(n, d, k, 300 + k) for k, (n, d) in enumerate(specs)]
+    if device:
+        for inst in together:
+            inst.to_device()
+    batch.batch_prove(gt, SEED, together, workers=4, hbm_budget=budget, engine="lockstep")
+    for a, b in zip(alone, together):
+        assert np.array_equal(a.proof, b.proof)
+    assert np.array_equal(alone[0].proof, oracle_instance_proof(alone[0].polys, alone[0].index, Q, ot))
