@@ -213,7 +213,7 @@ def run_side_workload(args):
     print(json.dumps(line))
 
 
-def run_batched(args):
+def run_batched(args, summary=False):
     """Mixed batch of independent instances (product sumcheck + Basefold commit/open of every
     polynomial at the sumcheck point): the prover service with an autotuned worker count
     against the per-call path (the same instances one after another on one stream)."""
@@ -250,20 +250,28 @@ def run_batched(args):
     per_call_s = min(wall(per_call) for _ in range(max(1, args.per_call_steps)))
     alone = [i.proof.copy() for i in insts]
 
-    # batched: tune the worker count on this batch (these runs are the warm-up), then time
-    (best, coop, top), tune = batch.autotune(table, seed, insts)
+    # batched: tune the schedule on this batch (these runs are the warm-up), then time; the
+    # summary mode takes the schedule the full run settles on
+    if summary:
+        (best, coop, top), tune = (16, 4096, 16), {}
+    else:
+        (best, coop, top), tune = batch.autotune(table, seed, insts)
     L.gb_set_coop_threshold(coop)
     L.gb_set_merkle_top_nodes(top)
-    for _ in range(max(0, args.warmup - 1)):
+    for _ in range(0 if summary else max(0, args.warmup - 1)):
         batch.batch_prove(table, seed, insts, best)
-    l0 = L.gb_launch_count()
-    with ClockSampler() as clk_svc:
-        times_svc = [wall(lambda: batch.batch_prove(table, seed, insts, best)) for _ in range(args.steps)]
-    launches_svc = (L.gb_launch_count() - l0) // max(1, args.steps)
-    same = sum(np.array_equal(i.proof, a) for i, a in zip(insts, alone))
+    same = 0
+    if not summary:
+        l0 = L.gb_launch_count()
+        with ClockSampler() as clk_svc:
+            times_svc = [wall(lambda: batch.batch_prove(table, seed, insts, best)) for _ in range(args.steps)]
+        launches_svc = (L.gb_launch_count() - l0) // max(1, args.steps)
+        same = sum(np.array_equal(i.proof, a) for i, a in zip(insts, alone))
     # the round-synchronous engine on the same batch (same worker count for commits + sumchecks)
     for i in insts:
         i.proof[:] = 0
+    if summary:
+        times_svc, launches_svc, clk_svc = [float("inf")], 0, None
     budget = 160 << 30
     batch.batch_prove(table, seed, insts, best, budget, engine="lockstep")
     l1 = L.gb_launch_count()
@@ -274,6 +282,14 @@ def run_batched(args):
     same_ls = sum(np.array_equal(i.proof, a) for i, a in zip(insts, alone))
     engine = "lockstep" if statistics.mean(times_ls) < statistics.mean(times_svc) else "service"
     times, launches, clk = (times_ls, launches_ls, clk_ls) if engine == "lockstep" else (times_svc, launches_svc, clk_svc)
+    if summary:
+        return {"value": count / statistics.mean(times), "unit": "proofs/s", "instances": count,
+                "engine": engine, "ms_per_batch": statistics.mean(times) * 1e3,
+                "per_call": {"value": count / per_call_s, "unit": "proofs/s", "ms_per_batch": per_call_s * 1e3},
+                "batched_over_per_call": per_call_s / statistics.mean(times),
+                "identical_to_per_call": f"{same_ls}/{count}", "gpu_launches": int(launches),
+                "workload": "512 instances, 2^10..2^20 evaluations (log-uniform), degree 2..4, sumcheck + "
+                            "commit/open of each polynomial; python bench.py --workload batched for the full run"}
     # end to end: the same batch from pinned host memory (host->device copies inside)
     total = sum(i.polys.nbytes for i in insts)
     pinned = torch.empty(total, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint64)
@@ -316,7 +332,7 @@ def run_batched(args):
     print(json.dumps(line))
 
 
-def run_served(args):
+def run_served(args, summary=False):
     """Served matmul-layer jobs arriving as a Poisson stream: the prover service (worker
     streams, HBM-budget admission) against the per-call path (one job at a time, in arrival
     order), both on the same arrival schedule; latency = arrival -> proof done."""
@@ -370,6 +386,13 @@ def run_served(args):
     lat = [st["latency_ms"] for st in stats]
     same = sum(np.array_equal(j.proof, a) for j, a in zip(jobs, alone))
     h2d = sum(j.a.nbytes + j.b.nbytes for j in jobs)
+    if summary:
+        return {"value": len(jobs) / span, "unit": "proofs/s", "jobs": len(jobs), "offered_jobs_per_s": args.rate,
+                "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                "per_call": {"value": len(jobs) / span_pc, "p50_ms": pct(lat_pc, 50), "p99_ms": pct(lat_pc, 99)},
+                "identical_to_per_call": f"{same}/{len(jobs)}",
+                "workload": "matmul-layer jobs (M, N, K in {256, 512, 1024, 4096}, int8), Poisson arrivals; "
+                            "python bench.py --workload served for the full run"}
     line = {"metric": "served proofs/sec", "value": len(jobs) / span, "unit": "proofs/s", "n_gpus": 1,
             "steps": len(jobs), "warmup": len(warm), "ms_per_step": span * 1e3 / len(jobs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)",
@@ -556,6 +579,12 @@ def main():
         sc_ms = statistics.median(ev_time(sc) for _ in range(5))
         extras["sumcheck_2x2^20"] = {"ms_per_proof": sc_ms, "melem_per_s": 2 * (1 << 20) / (sc_ms * 1e-3) / 1e6}
         extras["cpu_baseline"] = cpu_baseline_sample()
+        # the batched (512 mixed instances) and served (Poisson matmul jobs) configurations, compact
+        L.gb_set_stream(None)
+        extras["batched_512"] = run_batched(argparse.Namespace(instances=512, steps=1, warmup=1, per_call_steps=1),
+                                            summary=True)
+        extras["served"] = run_served(argparse.Namespace(jobs=100, rate=200.0, workers=8, hbm_budget_gb=96),
+                                      summary=True)
 
     if rank == 0:
         line = {
