@@ -303,6 +303,9 @@ int gb_batch_prove(void *table, const uint64_t master_seed[2], int num_queries, 
  * identical to gb_prove_instance's.  table: log_rate 1.  Synchronising. */
 int gb_batch_prove_lockstep(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *insts,
                             int count, int workers, size_t hbm_budget);
+/* Host wall time of the calling thread's last gb_batch_prove_lockstep: the commit + sumcheck
+ * phase and the opening phase, summed over its waves (either pointer may be NULL). */
+void gb_lockstep_last_timing(double *commit_sumcheck_ms, double *open_ms);
 
 /* A quantized matmul layer C = A B as a served job (no reference counterpart; the field work
  * of zk-torch-3/src/basicblock/einsum.rs:807-1000): A is m x k, B is k x n (row-major int8),

@@ -134,6 +134,7 @@ SIGNATURES = {
     "gb_prover_destroy": (i32, [vp]),
     "gb_batch_prove": (i32, [vp, vp, i32, vp, i32, i32, sz]),
     "gb_batch_prove_lockstep": (i32, [vp, vp, i32, vp, i32, i32, sz]),
+    "gb_lockstep_last_timing": (None, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "gb_matmul_proof_len": (sz, [i32, i32, i32, i32]),
     "gb_matmul_hbm_bytes": (sz, [i32, i32, i32]),
     "gb_prove_matmul": (i32, [vp, vp, vp, i32, vp]),

@@ -34,39 +34,11 @@ namespace gb {
 // 2x2 per-variable transforms applied to K consecutive bits [b, b+K) in registers
 // MAT 0: T = (e1, 2 e0 - e1)   1: Moebius (e0, e1 - e0)   2: WHT (e0 + e1, e0 - e1)
 // ===========================================================================
-template <int MAT>
-__device__ __forceinline__ void bf_butterfly(u64& x0, u64& x1) {
-    if (MAT == 0) {
-        u64 t = gl_sub(gl_double(x0), x1);
-        x0 = x1;
-        x1 = t;
-    } else if (MAT == 1) {
-        x1 = gl_sub(x1, x0);
-    } else {
-        u64 a = gl_add(x0, x1), b = gl_sub(x0, x1);
-        x0 = a;
-        x1 = b;
-    }
-}
-
 template <int MAT, int K>
 __global__ void bf_transform_pass_kernel(const u64* __restrict__ in, u64* __restrict__ out, int b, size_t groups) {
     size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (g >= groups) return;
-    size_t low = g & (((size_t)1 << b) - 1), high = g >> b;
-    size_t base = (high << (b + K)) | low;
-    u64 v[1 << K];
-#pragma unroll
-    for (int j = 0; j < (1 << K); j++) v[j] = in[base + ((size_t)j << b)];
-#pragma unroll
-    for (int l = 0; l < K; l++) {
-#pragma unroll
-        for (int j = 0; j < (1 << K); j++) {
-            if (!(j & (1 << l))) bf_butterfly<MAT>(v[j], v[j | (1 << l)]);
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < (1 << K); j++) out[base + ((size_t)j << b)] = v[j];
+    bf_transform_group<MAT, K>(in, out, b, g);
 }
 
 // apply the transform on all n bits; in may equal out
@@ -95,7 +67,6 @@ static int bf_transform(const u64* in, u64* out, int n) {
     return GB_OK;
 }
 
-__device__ __forceinline__ size_t bitrev_dev(size_t x, int bits) { return bits ? (__brevll(x) >> (64 - bits)) : 0; }
 
 // out[j] = in[bitrev_n(j mod 2^n)] for j < 2^(n+reps_log)
 __global__ void bitrev_replicate_kernel(const u64* __restrict__ in, u64* __restrict__ out, int n, size_t total) {

@@ -13,6 +13,7 @@
 // Every proof is bit-identical to gb_prove_instance's.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -173,6 +174,58 @@ __global__ void ls_fold_final_kernel(const LsSeg* __restrict__ segs, int nseg, u
     }
 }
 
+// ---- commits (commit_device, basefold.cu) for all polynomials ----
+// transform pass over bits [c0, c0 + K): a = in, c = out (may equal a), items = groups
+template <int K>
+__global__ void __launch_bounds__(LS_THREADS) ls_transform_pass_kernel(const LsSeg* __restrict__ segs, int nseg) {
+    LS_SEG_PROLOGUE
+    const u64 g = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
+    if (g >= sg.items) return;
+    bf_transform_group<0, K>(sg.a, sg.c, (int)sg.c0, g);
+}
+
+// codeword[j] = u[bitrev_n(j mod 2^n)]: a = u, c = codeword, items = L, c0 = n
+__global__ void __launch_bounds__(LS_THREADS) ls_bitrev_replicate_kernel(const LsSeg* __restrict__ segs, int nseg) {
+    LS_SEG_PROLOGUE
+    const u64 j = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
+    if (j >= sg.items) return;
+    const int n = (int)sg.c0;
+    sg.c[j] = __ldg(sg.a + bitrev_dev(j & (((u64)1 << n) - 1), n));
+}
+
+// leaf i = P2(cw[2i], cw[2i+1], 0, ...) for the first copy's leaves: a = codeword, d = tree
+__global__ void __launch_bounds__(LS_THREADS) ls_hash_leaves_kernel(const LsSeg* __restrict__ segs, int nseg) {
+    LS_SEG_PROLOGUE
+    const u64 i = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
+    if (i >= sg.items) return;
+    ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(sg.a) + i);
+    u64 st[8] = {v.x, v.y, 0, 0, 0, 0, 0, 0};
+    p2_permute(st);
+    st_digest(sg.d + 4 * i, st);
+}
+
+// copies of the first copy's subtree on every layer (replicate_layers_kernel, merkle.cu):
+// c = tree, items = copied words, c0 = leaves of the full tree, c1 = leaves of one copy (2 copies)
+__global__ void __launch_bounds__(LS_THREADS) ls_replicate_kernel(const LsSeg* __restrict__ segs, int nseg) {
+    LS_SEG_PROLOGUE
+    u64 t = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
+    if (t >= sg.items) return;
+    u64 off = 0, nodes = sg.c0, n = sg.c1;
+    for (;;) {
+        const u64 words = 4 * n;  // (copies - 1) = 1
+        if (t < words) {
+            u64* layer = sg.c + off;
+            layer[4 * n + t] = layer[t % (4 * n)];
+            return;
+        }
+        t -= words;
+        off += 4 * nodes;
+        nodes >>= 1;
+        n >>= 1;
+        if (n == 0) return;
+    }
+}
+
 // all polynomials' queries: block (query k, polynomial p)
 __global__ void ls_query_kernel(const QueryJob* __restrict__ jobs, const u64* __restrict__ idx, int q,
                                 u64* const* __restrict__ outs, const u64* __restrict__ per_query) {
@@ -184,6 +237,24 @@ __global__ void ls_query_kernel(const QueryJob* __restrict__ jobs, const u64* __
 // host side
 // ---------------------------------------------------------------------------
 static size_t align2(size_t w) { return (w + 1) & ~(size_t)1; }  // 16-byte multiples of words
+
+// fn(i) for i in [0, count) on up to 16 host threads (each polynomial's transcript is its own,
+// so the per-polynomial steps between rounds run in parallel)
+template <typename F>
+static void ls_parallel(size_t count, F fn) {
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min<size_t>(std::min<size_t>(hw, 16), (count + 63) / 64);
+    if (nt <= 1) {
+        for (size_t i = 0; i < count; i++) fn(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; t++)
+        th.emplace_back([&, t] {
+            for (size_t i = t * count / nt; i < (t + 1) * count / nt; i++) fn(i);
+        });
+    for (auto& x : th) x.join();
+}
 
 struct LsPoly {
     int n = 0;
@@ -266,10 +337,11 @@ class LsRunner {
         // preamble: root and point into each transcript; eq tables
         {
             std::vector<u64> pts;
-            for (auto& p : P) {
-                for (int k = 0; k < 4; k++) tr_append_u64(&p.t, "", p.com->root[k]);
+            ls_parallel(P.size(), [&](size_t k) {
+                LsPoly& p = P[k];
+                for (int w = 0; w < 4; w++) tr_append_u64(&p.t, "", p.com->root[w]);
                 for (int i = 0; i < p.n; i++) tr_append_ext2(&p.t, "", E2{canon(p.point[2 * i]), canon(p.point[2 * i + 1])});
-            }
+            });
             for (auto& p : P) {
                 std::vector<u64> v(2 * p.n);
                 for (int i = 0; i < 2 * p.n; i++) v[i] = canon(p.point[i]);
@@ -297,9 +369,9 @@ class LsRunner {
             ls_reduce_kernel<<<(unsigned)((np * 32 + 255) / 256), 256, 0, s>>>(ds, np, d_partials_, d_recs_);
             GB_LAUNCH_CHECK("ls_reduce_kernel");
             LS_RC(read_recs(np));
-            for (int k = 0; k < np; k++) {
+            ls_parallel(np, [&](size_t k) {
                 LsPoly& p = P[k];
-                const u64* rec = h_recs_ + (size_t)k * LS_REC;
+                const u64* rec = h_recs_ + k * LS_REC;
                 E2 c0{rec[0], rec[1]};
                 E2 s1 = put_oracle(p, 0, rec);
                 E2 ev = e2add(c0, s1);
@@ -309,7 +381,7 @@ class LsRunner {
                 p.bh_cur = p.com->d_evals;
                 p.pp = 0;
                 p.sc = p.N;
-            }
+            });
         }
         // rounds
         std::vector<E2> ch(np);
@@ -317,9 +389,11 @@ class LsRunner {
             std::vector<int> mid, last;  // still folding with a tree / final fold
             for (int k = 0; k < np; k++) {
                 if (rd >= P[k].n) continue;
-                ch[k] = tr_challenge_ext2(&P[k].t, "");
                 (rd < P[k].n - 1 ? mid : last).push_back(k);
             }
+            ls_parallel(np, [&](size_t k) {
+                if (rd < P[k].n) ch[k] = tr_challenge_ext2(&P[k].t, "");
+            });
             if (!mid.empty()) {
                 // eq/bh folds + next oracle
                 u64 nb = 0;
@@ -401,7 +475,7 @@ class LsRunner {
                 ls_root_kernel<<<(unsigned)((mid.size() + 127) / 128), 128, 0, s>>>(ds, (int)mid.size(), d_recs_);
                 GB_LAUNCH_CHECK("ls_root_kernel");
                 LS_RC(read_recs((int)mid.size()));
-                for (size_t m = 0; m < mid.size(); m++) {
+                ls_parallel(mid.size(), [&](size_t m) {
                     LsPoly& p = P[mid[m]];
                     const u64* rec = h_recs_ + m * LS_REC;
                     put_oracle(p, rd + 1, rec);
@@ -410,7 +484,7 @@ class LsRunner {
                         root[k] = rec[8 + k];
                         tr_append_u64(&p.t, "", root[k]);
                     }
-                }
+                });
             }
             if (!last.empty()) {
                 LsSeg* hs = next_slot(); if (!hs) return GB_EINVAL;
@@ -440,9 +514,12 @@ class LsRunner {
             std::vector<const u64*> ptrs;
             std::vector<size_t> out_off(np);
             size_t out_words = 0;
+            ls_parallel(np, [&](size_t k) {
+                LsPoly& p = P[k];
+                for (int j = 0; j < q_; j++) idx[k * q_ + j] = tr_challenge(&p.t, "") % (u64)(p.L / 2);
+            });
             for (int k = 0; k < np; k++) {
                 LsPoly& p = P[k];
-                for (int j = 0; j < q_; j++) idx[(size_t)k * q_ + j] = tr_challenge(&p.t, "") % (u64)(p.L / 2);
                 size_t pw = 0;
                 for (int r = 0; r < p.n; r++) pw += (size_t)(p.n + lr - 1 - r);
                 per_q[k] = 1 + (size_t)p.n * 4 + pw * 4;
@@ -561,6 +638,176 @@ class LsRunner {
     u64* d_partials_ = nullptr;
     size_t seg_cap_ = 0, np_max_ = 1, slot_ = 0;
 };
+
+// Commits of a batch of polynomials (rate 1/2, two copies of one subtree), as commit_device:
+// T-transform -> bit-reverse + replicate -> leaf hashes of one copy -> its layers -> copies ->
+// top layer.  Each step is one launch for all polynomials.  The commitments' buffers are carved
+// from `ws` (see ls_commit_words); d_evals points at the caller's evaluations.
+struct LsCommitJob {
+    int n = 0;
+    const u64* evals = nullptr;
+    BfCommitment com;
+};
+
+static size_t ls_commit_words(int n) {
+    size_t N = (size_t)1 << n, L = 2 * N;
+    return N /* transform scratch */ + L /* codeword */ + 4 * (2 * N - 1) + 2 /* tree */;
+}
+
+class LsCommitter {
+  public:
+    int commit(std::vector<LsCommitJob>& J, u64* ws) {
+        cudaStream_t s = stream();
+        const int nj = (int)J.size();
+        if (!nj) return GB_OK;
+        int maxn = 0;
+        for (auto& j : J) maxn = std::max(maxn, j.n);
+        std::vector<u64*> tmp(nj);
+        {
+            u64* cur = ws;
+            for (int k = 0; k < nj; k++) {
+                size_t N = (size_t)1 << J[k].n;
+                tmp[k] = cur;
+                cur += N;
+                J[k].com.num_vars = J[k].n;
+                J[k].com.log_rate = 1;
+                J[k].com.d_evals = const_cast<u64*>(J[k].evals);
+                J[k].com.d_codeword = cur;
+                cur += 2 * N;
+                J[k].com.d_tree = cur;
+                cur += 4 * (2 * N - 1) + 2;
+            }
+        }
+        const size_t cap = (size_t)nj * ((maxn + 3) / 4 * 4 + maxn + 8);
+        GB_CUDA_TRY(cudaMallocAsync(&d_segs_, cap * sizeof(LsSeg), s));
+        GB_CUDA_TRY(cudaMallocAsync(&d_recs_, (size_t)nj * LS_REC * 8, s));
+        GB_CUDA_TRY(cudaMallocHost(&h_segs_, cap * sizeof(LsSeg)));
+        GB_CUDA_TRY(cudaMallocHost(&h_recs_, (size_t)nj * LS_REC * 8));
+        size_t used = 0;
+        auto launch = [&](auto kernel, int count, u64 nb) -> int {
+            LsSeg* hs = h_segs_ + used;
+            GB_CUDA_TRY(cudaMemcpyAsync(d_segs_ + used, hs, (size_t)count * sizeof(LsSeg), cudaMemcpyHostToDevice, s));
+            kernel<<<(unsigned)nb, LS_THREADS, 0, s>>>(d_segs_ + used, count);
+            used += count;
+            return check_launch("ls_commit");
+        };
+        // 1. transform passes: pass p covers bits [4p, 4p + K) with K = min(4, n - 4p)
+        for (int b = 0; b < maxn; b += 4) {
+            for (int K = 1; K <= 4; K++) {
+                int cnt = 0;
+                u64 nb = 0;
+                LsSeg* hs = h_segs_ + used;
+                for (int k = 0; k < nj; k++) {
+                    const int n = J[k].n;
+                    if (n <= b || std::min(4, n - b) != K) continue;
+                    const u64 groups = ((u64)1 << n) >> K;
+                    hs[cnt++] = LsSeg{b == 0 ? J[k].evals : tmp[k], nullptr, tmp[k], nullptr, (u64)b, 0, groups, nb};
+                    nb += blocks(groups);
+                }
+                if (!cnt) continue;
+                int rc = K == 4   ? launch(ls_transform_pass_kernel<4>, cnt, nb)
+                         : K == 3 ? launch(ls_transform_pass_kernel<3>, cnt, nb)
+                         : K == 2 ? launch(ls_transform_pass_kernel<2>, cnt, nb)
+                                  : launch(ls_transform_pass_kernel<1>, cnt, nb);
+                if (rc) return rc;
+            }
+        }
+        // 2. codeword, 3. first copy's leaves
+        {
+            LsSeg* hs = h_segs_ + used;
+            u64 nb = 0;
+            for (int k = 0; k < nj; k++) {
+                const u64 L = (u64)2 << J[k].n;
+                hs[k] = LsSeg{tmp[k], nullptr, J[k].com.d_codeword, nullptr, (u64)J[k].n, 0, L, nb};
+                nb += blocks(L);
+            }
+            LS_RC(launch(ls_bitrev_replicate_kernel, nj, nb));
+            hs = h_segs_ + used;
+            nb = 0;
+            for (int k = 0; k < nj; k++) {
+                const u64 sub = (u64)1 << (J[k].n - 1);
+                hs[k] = LsSeg{J[k].com.d_codeword, nullptr, nullptr, J[k].com.d_tree, 0, 0, sub, nb};
+                nb += blocks(sub);
+            }
+            LS_RC(launch(ls_hash_leaves_kernel, nj, nb));
+        }
+        // 4. the first copy's layers (full-tree offsets: layer l holds N >> l nodes)
+        for (int l = 0;; l++) {
+            int cnt = 0;
+            u64 nb = 0;
+            LsSeg* hs = h_segs_ + used;
+            for (int k = 0; k < nj; k++) {
+                const u64 N = (u64)1 << J[k].n, sub = N / 2;
+                const u64 parents = sub >> (l + 1);
+                if (!parents) continue;
+                u64 off = 0;
+                for (int t = 0; t < l; t++) off += N >> t;
+                u64* layer = J[k].com.d_tree + 4 * off;
+                hs[cnt++] = LsSeg{layer, nullptr, layer + 4 * (N >> l), nullptr, 0, 0, parents, nb};
+                nb += blocks(parents);
+            }
+            if (!cnt) break;
+            LS_RC(launch(ls_merkle_level_kernel, cnt, nb));
+        }
+        // 5. the second copy on every layer
+        {
+            LsSeg* hs = h_segs_ + used;
+            u64 nb = 0;
+            for (int k = 0; k < nj; k++) {
+                const u64 N = (u64)1 << J[k].n, sub = N / 2;
+                u64 total = 0;
+                for (u64 m = sub; m >= 1; m >>= 1) total += 4 * m;
+                hs[k] = LsSeg{nullptr, nullptr, J[k].com.d_tree, nullptr, N, sub, total, nb};
+                nb += blocks(total);
+            }
+            LS_RC(launch(ls_replicate_kernel, nj, nb));
+        }
+        // 6. the top layer: two copy roots -> the root
+        {
+            LsSeg* hs = h_segs_ + used;
+            u64 nb = 0;
+            for (int k = 0; k < nj; k++) {
+                const int n = J[k].n;
+                const u64 N = (u64)1 << n;
+                u64 off = 0;
+                for (int t = 0; t < n - 1; t++) off += N >> t;  // the layer of 2 nodes
+                u64* layer = J[k].com.d_tree + 4 * off;
+                hs[k] = LsSeg{layer, nullptr, layer + 8, nullptr, 0, 0, 1, nb};
+                nb += 1;
+            }
+            LS_RC(launch(ls_merkle_level_kernel, nj, nb));
+            hs = h_segs_ + used;
+            for (int k = 0; k < nj; k++) {
+                const u64 N = (u64)1 << J[k].n;
+                hs[k] = LsSeg{J[k].com.d_tree + 4 * (2 * N - 2), nullptr, nullptr, nullptr, 0, 0, 0, 0};
+            }
+            GB_CUDA_TRY(cudaMemcpyAsync(d_segs_ + used, hs, (size_t)nj * sizeof(LsSeg), cudaMemcpyHostToDevice, s));
+            ls_root_kernel<<<(unsigned)((nj + 127) / 128), 128, 0, s>>>(d_segs_ + used, nj, d_recs_);
+            GB_LAUNCH_CHECK("ls_root_kernel");
+        }
+        GB_CUDA_TRY(cudaMemcpyAsync(h_recs_, d_recs_, (size_t)nj * LS_REC * 8, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int k = 0; k < nj; k++)
+            for (int w = 0; w < 4; w++) J[k].com.root[w] = h_recs_[(size_t)k * LS_REC + 8 + w];
+        return GB_OK;
+    }
+    ~LsCommitter() {
+        cudaStream_t s = stream();
+        if (d_segs_) cudaFreeAsync(d_segs_, s);
+        if (d_recs_) cudaFreeAsync(d_recs_, s);
+        cudaStreamSynchronize(s);
+        if (h_segs_) cudaFreeHost(h_segs_);
+        if (h_recs_) cudaFreeHost(h_recs_);
+    }
+
+  private:
+    static u64 blocks(u64 items) { return items ? (items + LS_THREADS - 1) / LS_THREADS : 1; }
+    LsSeg* d_segs_ = nullptr;
+    LsSeg* h_segs_ = nullptr;
+    u64* d_recs_ = nullptr;
+    u64* h_recs_ = nullptr;
+};
+
 // ---------------------------------------------------------------------------
 // driver: waves of instances; commits + sumchecks on worker threads, openings in lockstep
 // ---------------------------------------------------------------------------
@@ -571,32 +818,21 @@ static size_t inst_proof_words_before_opens(int n, int d) {
 
 static size_t ls_inst_bytes(const gb_instance& in) {
     size_t N = (size_t)1 << in.num_vars;
-    // uploaded inputs, commitments (evaluations, codeword, tree), the sumcheck's levels and the
-    // opening workspace, per polynomial
-    return (size_t)in.degree * (N * (8 + 8 + 16 + 64 + 16) + ls_poly_words(in.num_vars, 1) * 8) + ((size_t)1 << 20);
+    // uploaded inputs, commitment workspace, the sumcheck's levels and the opening workspace,
+    // per polynomial
+    return (size_t)in.degree * (N * (8 + 16) + (ls_commit_words(in.num_vars) + ls_poly_words(in.num_vars, 1)) * 8) +
+           ((size_t)1 << 20);
 }
 
-static int ls_commit_and_sumcheck(const u64 seed[2], const gb_instance& in, std::vector<void*>& com, u64*& owned) {
+// the product sumcheck of one instance (roots already in its proof), on the calling thread's stream
+static int ls_sumcheck(const u64 seed[2], const gb_instance& in, const u64* polys) {
     using namespace host;
     const int n = in.num_vars, d = in.degree;
-    const size_t N = (size_t)1 << n;
-    cudaStream_t s = stream();
-    const u64* polys = in.d_polys;
-    if (in.h_polys) {
-        GB_CUDA_TRY(cudaMallocAsync(&owned, N * d * 8, s));
-        GB_CUDA_TRY(cudaMemcpyAsync(owned, in.h_polys, N * d * 8, cudaMemcpyHostToDevice, s));
-        polys = owned;
-    }
     u64* roots = in.h_proof;
     u64* msgs = roots + (size_t)d * 4;
     u64* chal = msgs + (size_t)n * (d + 1) * 2;
     u64* finals = chal + (size_t)n * 2;
     u64* fe = finals + (size_t)d * 2;
-    com.assign(d, nullptr);
-    for (int j = 0; j < d; j++) {
-        int rc = gb_basefold_commit(polys + (size_t)j * N, nullptr, n, 1, &com[j], roots + 4 * j);
-        if (rc) return rc;
-    }
     gb_transcript t;
     gb_transcript_new(&t, "sumcheck");
     tr_append_ext2(&t, "", E2{canon(seed[0]), canon(seed[1])});
@@ -604,6 +840,9 @@ static int ls_commit_and_sumcheck(const u64 seed[2], const gb_instance& in, std:
     for (int k = 0; k < 4 * d; k++) tr_append_u64(&t, "", roots[k]);
     return gb_sumcheck_prove_ext2(&t, n, d, polys, nullptr, msgs, chal, finals, fe);
 }
+
+// wall time of the last lockstep batch on this thread: commits + sumchecks, openings
+static thread_local double t_ls_ms[2] = {0, 0};
 
 static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instance* insts, int count, int workers,
                           size_t budget) {
@@ -628,6 +867,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
     int dev = 0;
     GB_CUDA_TRY(cudaGetDevice(&dev));
     const size_t coop = gb_get_coop_threshold(), top = gb_get_merkle_top_nodes();
+    t_ls_ms[0] = t_ls_ms[1] = 0;
     size_t next = 0;
     while (next < order.size()) {
         // the wave: largest remaining first, as many as fit the budget (at least one)
@@ -637,40 +877,94 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
             used += ls_inst_bytes(insts[order[next]]);
             wave.push_back(order[next++]);
         }
-        std::vector<std::vector<void*>> com(wave.size());
+        auto t0 = std::chrono::steady_clock::now();
+        cudaStream_t s = stream();
+        // inputs on the device
+        std::vector<const u64*> polys(wave.size());
         std::vector<u64*> owned(wave.size(), nullptr);
+        int rc = GB_OK;
+        for (size_t k = 0; k < wave.size() && !rc; k++) {
+            const gb_instance& in = insts[wave[k]];
+            if (in.h_polys) {
+                size_t bytes = ((size_t)in.degree << in.num_vars) * 8;
+                cudaError_t e = cudaMallocAsync(&owned[k], bytes, s);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(owned[k], in.h_polys, bytes, cudaMemcpyHostToDevice, s);
+                if (e != cudaSuccess) {
+                    set_error("input upload", e);
+                    rc = GB_ECUDA;
+                }
+                polys[k] = owned[k];
+            } else {
+                polys[k] = in.d_polys;
+            }
+        }
+        // commits of every polynomial of the wave, in lockstep
+        std::vector<LsCommitJob> jobs;
+        std::vector<size_t> first_job(wave.size());
+        size_t cwords = 0;
+        for (size_t k = 0; k < wave.size(); k++) {
+            const gb_instance& in = insts[wave[k]];
+            first_job[k] = jobs.size();
+            for (int j = 0; j < in.degree; j++) {
+                LsCommitJob cj;
+                cj.n = in.num_vars;
+                cj.evals = polys[k] + ((size_t)j << in.num_vars);
+                jobs.push_back(cj);
+                cwords += ls_commit_words(in.num_vars);
+            }
+        }
+        u64* cws = nullptr;
+        if (!rc) {
+            cudaError_t e = cudaMallocAsync(&cws, std::max<size_t>(cwords, 2) * 8, s);
+            if (e != cudaSuccess) {
+                set_error("commit workspace", e);
+                rc = GB_ECUDA;
+            }
+        }
+        if (!rc) {
+            LsCommitter committer;
+            rc = committer.commit(jobs, cws);
+        }
+        if (!rc)
+            for (size_t k = 0; k < wave.size(); k++) {
+                const gb_instance& in = insts[wave[k]];
+                for (int j = 0; j < in.degree; j++)
+                    for (int w = 0; w < 4; w++) in.h_proof[4 * j + w] = jobs[first_job[k] + j].com.root[w];
+            }
+        // product sumchecks on the worker threads
         std::vector<int> rcs(wave.size(), GB_OK);
         std::vector<std::string> errs(wave.size());
-        std::atomic<size_t> cursor{0};
-        const int nt = (int)std::min<size_t>((size_t)workers, wave.size());
-        std::vector<std::thread> th;
-        for (int w = 0; w < nt; w++)
-            th.emplace_back([&] {
-                cudaStream_t st = nullptr;
-                if (cudaSetDevice(dev) != cudaSuccess || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
-                    st = nullptr;
-                if (st) gb_set_stream(st);
-                gb_set_coop_threshold(coop);
-                gb_set_merkle_top_nodes(top);
-                for (size_t k; (k = cursor.fetch_add(1)) < wave.size();) {
-                    int rc = st ? ls_commit_and_sumcheck(seed, insts[wave[k]], com[k], owned[k]) : GB_ECUDA;
-                    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = GB_ECUDA;
-                    rcs[k] = rc;
-                    if (rc) errs[k] = st ? gb_last_error() : "stream creation failed";
+        if (!rc) {
+            std::atomic<size_t> cursor{0};
+            const int nt = (int)std::min<size_t>((size_t)workers, wave.size());
+            std::vector<std::thread> th;
+            for (int w = 0; w < nt; w++)
+                th.emplace_back([&] {
+                    cudaStream_t st = nullptr;
+                    if (cudaSetDevice(dev) != cudaSuccess ||
+                        cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+                        st = nullptr;
+                    if (st) gb_set_stream(st);
+                    for (size_t k; (k = cursor.fetch_add(1)) < wave.size();) {
+                        int r = st ? ls_sumcheck(seed, insts[wave[k]], polys[k]) : GB_ECUDA;
+                        rcs[k] = r;
+                        if (r) errs[k] = st ? gb_last_error() : "stream creation failed";
+                    }
+                    if (st) {
+                        cudaStreamSynchronize(st);
+                        gb_set_stream(nullptr);
+                        cudaStreamDestroy(st);
+                    }
+                });
+            for (auto& t : th) t.join();
+            for (size_t k = 0; k < wave.size() && !rc; k++)
+                if (rcs[k]) {
+                    rc = rcs[k];
+                    set_error_msg(errs[k]);
                 }
-                if (st) {
-                    cudaStreamSynchronize(st);
-                    gb_set_stream(nullptr);
-                    cudaStreamDestroy(st);
-                }
-            });
-        for (auto& t : th) t.join();
-        int rc = GB_OK;
-        for (size_t k = 0; k < wave.size() && !rc; k++)
-            if (rcs[k]) {
-                rc = rcs[k];
-                set_error_msg(errs[k]);
-            }
+        }
+        auto t1 = std::chrono::steady_clock::now();
+        t_ls_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
         if (!rc) {
             // openings of every polynomial of the wave, in lockstep
             std::vector<LsPoly> P;
@@ -685,7 +979,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
                     p.n = n;
                     p.N = (size_t)1 << n;
                     p.L = p.N << 1;
-                    p.com = (const BfCommitment*)com[k][j];
+                    p.com = &jobs[first_job[k] + j].com;
                     p.point = chal;
                     gb_transcript_new(&p.t, "bf-open");
                     tr_append_ext2(&p.t, "", E2{canon(seed[0]), canon(seed[1])});
@@ -694,15 +988,15 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
                     P.push_back(std::move(p));
                 }
             }
-            LsRunner runner(tab, q);
-            rc = runner.open(P);
+            {
+                LsRunner runner(tab, q);
+                rc = runner.open(P);
+            }
+            t_ls_ms[1] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
         }
-        cudaStream_t s = stream();
-        for (size_t k = 0; k < wave.size(); k++) {
-            for (void* c : com[k])
-                if (c) gb_basefold_commitment_destroy(c);
+        if (cws) cudaFreeAsync(cws, s);
+        for (size_t k = 0; k < wave.size(); k++)
             if (owned[k]) cudaFreeAsync(owned[k], s);
-        }
         if (rc) return rc;
         GB_CUDA_TRY(cudaStreamSynchronize(s));
     }
@@ -718,6 +1012,11 @@ extern "C" {
 int gb_batch_prove_lockstep(void* table, const uint64_t master_seed[2], int num_queries, const gb_instance* insts,
                             int count, int workers, size_t hbm_budget) {
     return lockstep_prove(table, master_seed, num_queries, insts, count, workers, hbm_budget);
+}
+
+void gb_lockstep_last_timing(double* commit_sumcheck_ms, double* open_ms) {
+    if (commit_sumcheck_ms) *commit_sumcheck_ms = t_ls_ms[0];
+    if (open_ms) *open_ms = t_ls_ms[1];
 }
 
 }  // extern "C"
