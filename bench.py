@@ -240,6 +240,16 @@ def run_batched(args, summary=False):
         torch.cuda.synchronize()
         return time.perf_counter() - t0
 
+    if getattr(args, "quick", False):
+        # the lockstep engine alone at the settled schedule (for profiling captures)
+        L.gb_set_coop_threshold(4096)
+        for _ in range(args.warmup):
+            batch.batch_prove(table, seed, insts, 16, 160 << 30, engine="lockstep")
+        times = [wall(lambda: batch.batch_prove(table, seed, insts, 16, 160 << 30, engine="lockstep"))
+                 for _ in range(args.steps)]
+        print(json.dumps({"metric": "proofs/sec (mixed batch, lockstep only)", "value": count / statistics.mean(times),
+                          "unit": "proofs/s", "instances": count, "ms_per_step": statistics.mean(times) * 1e3}))
+        return
     # per-call path: a few warm-up instances, then every instance alone, in order
     for i in insts[:8]:
         batch.prove_instance(table, seed, i)
@@ -429,6 +439,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the roofline probes and the CPU baseline")
     ap.add_argument("--instances", type=int, default=512, help="batched workload: number of instances")
     ap.add_argument("--per-call-steps", type=int, default=1, help="batched workload: passes of the per-call path")
+    ap.add_argument("--quick", action="store_true", help="batched workload: the lockstep engine only (profiling)")
     ap.add_argument("--jobs", type=int, default=200, help="served workload: number of jobs")
     ap.add_argument("--rate", type=float, default=200.0, help="served workload: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")

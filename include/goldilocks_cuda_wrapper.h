@@ -128,6 +128,17 @@ int sumcheck_round_message_ext2_ffi(const uint64_t *d_polys, uint64_t *d_partial
 int sumcheck_fold_ext2_ffi(const uint64_t *d_input, uint64_t *d_output, uint64_t challenge_c0,
                            uint64_t challenge_c1, int d, size_t original_size, size_t half);
 
+/* ---- Monolith-12 Merkle trees (goldilocks-cuda-rs/src/ffi.rs:565-582; the crate's default Merkle
+ * hash, Cargo.toml:22-24; semantics of src/cpu_monolith.rs): leaf i = H(cw[2i], cw[2i+1]) (gl) or
+ * H(cw[4i..4i+3]) (ext2), parents H(left || right), digests the first 4 words (canonical),
+ * layout as the Poseidon2 trees.  Synchronising.  monolith_permute_test_ffi permutes one
+ * 12-word host state on the device.  monolith_cuda_init has nothing to set up (constants are
+ * compiled in). */
+int monolith_cuda_init(void);
+int monolith_merkle_tree_gl_ffi(const uint64_t *d_codeword, uint64_t *d_tree, int num_leaves);
+int monolith_merkle_tree_ext2_ffi(const uint64_t *d_codeword, uint64_t *d_tree, int num_leaves);
+int monolith_permute_test_ffi(const uint64_t *h_input, uint64_t *h_output);
+
 /* ---- Fiat-Shamir challengers on the device (goldilocks-cuda-rs/src/ffi.rs:314-372; semantics of
  * cuda/challenger.cuh:37-222): n independent duplex sponges over Poseidon2-w8, rate 4.  A state
  * is challenger_state_size() = 136 bytes (sponge[8], input[4], output[4] u64, input_count,

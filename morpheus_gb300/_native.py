@@ -58,6 +58,10 @@ SIGNATURES = {
     "sumcheck_fold_ffi": (i32, [vp, vp, u64, i32, sz, sz]),
     "sumcheck_round_message_ext2_ffi": (i32, [vp, vp, i32, sz, sz, i32]),
     "sumcheck_fold_ext2_ffi": (i32, [vp, vp, u64, u64, i32, sz, sz]),
+    "monolith_cuda_init": (i32, []),
+    "monolith_merkle_tree_gl_ffi": (i32, [vp, vp, i32]),
+    "monolith_merkle_tree_ext2_ffi": (i32, [vp, vp, i32]),
+    "monolith_permute_test_ffi": (i32, [vp, vp]),
     "challenger_state_size": (i32, []),
     "challenger_alloc_states": (i32, [ctypes.POINTER(vp), i32]),
     "challenger_init_states": (i32, [vp, i32]),

@@ -84,6 +84,9 @@ def lib():
             ("or_agl_sub", u64, [u64, u64]),
             ("or_agl_mul", u64, [u64, u64]),
             ("or_aext2_mul", None, [_u64p, _u64p, _u64p]),
+            ("or_monolith_permute", None, [_u64p]),
+            ("or_monolith_tree_gl", None, [_u64p, ctypes.c_size_t, _u64p]),
+            ("or_monolith_tree_ext2", None, [_u64p, ctypes.c_size_t, _u64p]),
             ("or_chacha8_block", None, [_u32p, _c.c_uint32, _u32p, _u32p]),
             ("or_ajtai_ring_elem", None, [_u32p, _c.c_uint32, u64, _u64p]),
             ("or_ajtai_commit_wide", None, [_u32p, _u64p, u64, u64, i32, i32, _u64p]),
@@ -153,6 +156,28 @@ def aext2_mul(a, b):
     out = np.zeros(2, np.uint64)
     lib().or_aext2_mul(_a(a), _a(b), out)
     return out
+
+
+def monolith_permute(state):
+    s = _a(state).copy()
+    lib().or_monolith_permute(s)
+    return s
+
+
+def monolith_tree_gl(cw):
+    cw = _a(cw)
+    leaves = cw.size // 2
+    tree = np.zeros((2 * leaves - 1) * 4, np.uint64)
+    lib().or_monolith_tree_gl(cw, leaves, tree)
+    return tree
+
+
+def monolith_tree_ext2(cw):
+    cw = _a(cw).reshape(-1)
+    leaves = cw.size // 4
+    tree = np.zeros((2 * leaves - 1) * 4, np.uint64)
+    lib().or_monolith_tree_ext2(cw, leaves, tree)
+    return tree
 
 
 def poseidon2_permute(state):

@@ -1021,3 +1021,94 @@ void or_ajtai_commit_u8_batch(const uint32_t key[8], const uint8_t *z8, u64 N, i
     }
     free(M);
 }
+
+/* ======================================================================
+ * Monolith-12 (goldilocks-cuda-rs/src/cpu_monolith.rs:13-139): concrete = circulant MDS with
+ * first row MO_C plus round constants, fully reduced; bars = the byte-wise chi-like S-box on the
+ * first 4 limbs; bricks = s[i] += s[i-1]^2 for i = 11 .. 1 (with the old s[i-1]).
+ * The round constants are the published Monolith-64 ones (LOOKUP_BITS = 8).
+ * ====================================================================== */
+static const u64 MO_C[12] = {7, 23, 8, 26, 13, 10, 9, 7, 6, 22, 21, 8};
+static const u64 MO_RC[7][12] = {
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+    {13596126580325903823ull, 5676126986831820406ull, 11349149288412960427ull, 3368797843020733411ull,
+     16240671731749717664ull, 9273190757374900239ull, 14446552112110239438ull, 4033077683985131644ull,
+     4291229347329361293ull, 13231607645683636062ull, 1383651072186713277ull, 8898815177417587567ull},
+    {2383619671172821638ull, 6065528368924797662ull, 16737578966352303081ull, 2661700069680749654ull,
+     7414030722730336790ull, 18124970299993404776ull, 9169923000283400738ull, 15832813151034110977ull,
+     16245117847613094506ull, 11056181639108379773ull, 10546400734398052938ull, 8443860941261719174ull},
+    {15799082741422909885ull, 13421235861052008152ull, 15448208253823605561ull, 2540286744040770964ull,
+     2895626806801935918ull, 8644593510196221619ull, 17722491003064835823ull, 5166255496419771636ull,
+     1015740739405252346ull, 4400043467547597488ull, 5176473243271652644ull, 4517904634837939508ull},
+    {18341030605319882173ull, 13366339881666916534ull, 6291492342503367536ull, 10004214885638819819ull,
+     4748655089269860551ull, 1520762444865670308ull, 8393589389936386108ull, 11025183333304586284ull,
+     5993305003203422738ull, 458912836931247573ull, 5947003897778655410ull, 17184667486285295106ull},
+    {15710528677110011358ull, 8929476121507374707ull, 2351989866172789037ull, 11264145846854799752ull,
+     14924075362538455764ull, 10107004551857451916ull, 18325221206052792232ull, 16751515052585522105ull,
+     15305034267720085905ull, 15639149412312342017ull, 14624541102106656564ull, 3542311898554959098ull},
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+};
+
+static u64 mo_bar(u64 x) {
+    u64 l1 = ((~x & 0x8080808080808080ull) >> 7) | ((~x & 0x7F7F7F7F7F7F7F7Full) << 1);
+    u64 l2 = ((x & 0xC0C0C0C0C0C0C0C0ull) >> 6) | ((x & 0x3F3F3F3F3F3F3F3Full) << 2);
+    u64 l3 = ((x & 0xE0E0E0E0E0E0E0E0ull) >> 5) | ((x & 0x1F1F1F1F1F1F1F1Full) << 3);
+    u64 t = x ^ (l1 & l2 & l3);
+    return ((t & 0x8080808080808080ull) >> 7) | ((t & 0x7F7F7F7F7F7F7F7Full) << 1);
+}
+
+static void mo_concrete(u64 s[12], int round) {
+    u64 out[12];
+    for (int r = 0; r < 12; r++) {
+        u128 acc = MO_RC[round][r];
+        for (int c = 0; c < 12; c++) acc += (u128)s[c] * MO_C[(c - r + 12) % 12];
+        out[r] = gl_reduce128(acc);
+    }
+    memcpy(s, out, sizeof(out));
+}
+
+void or_monolith_permute(u64 s[12]) {
+    for (int i = 0; i < 12; i++) s[i] = gl_canon(s[i]);
+    mo_concrete(s, 0);
+    for (int r = 1; r <= 6; r++) {
+        for (int i = 0; i < 4; i++) s[i] = mo_bar(s[i]);
+        for (int i = 11; i >= 1; i--) s[i] = gl_add(s[i], gl_mul(s[i - 1], s[i - 1]));
+        mo_concrete(s, r);
+    }
+}
+
+static void mo_tree_up(u64 *tree, size_t leaves) {
+    size_t off = 0, nodes = leaves;
+    while (nodes > 1) {
+        u64 *layer = tree + 4 * off, *up = layer + 4 * nodes;
+        for (size_t j = 0; j < nodes / 2; j++) {
+            u64 st[12] = {0};
+            memcpy(st, layer + 8 * j, 8 * sizeof(u64));
+            or_monolith_permute(st);
+            memcpy(up + 4 * j, st, 4 * sizeof(u64));
+        }
+        off += nodes;
+        nodes /= 2;
+    }
+}
+
+void or_monolith_tree_gl(const u64 *cw, size_t leaves, u64 *tree) {
+    for (size_t i = 0; i < leaves; i++) {
+        u64 st[12] = {0};
+        st[0] = cw[2 * i];
+        st[1] = cw[2 * i + 1];
+        or_monolith_permute(st);
+        memcpy(tree + 4 * i, st, 4 * sizeof(u64));
+    }
+    mo_tree_up(tree, leaves);
+}
+
+void or_monolith_tree_ext2(const u64 *cw, size_t leaves, u64 *tree) {
+    for (size_t i = 0; i < leaves; i++) {
+        u64 st[12] = {0};
+        memcpy(st, cw + 4 * i, 4 * sizeof(u64));
+        or_monolith_permute(st);
+        memcpy(tree + 4 * i, st, 4 * sizeof(u64));
+    }
+    mo_tree_up(tree, leaves);
+}

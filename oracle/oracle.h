@@ -111,6 +111,15 @@ int or_basefold_verify_ext2(const uint64_t root[4], int n, int log_rate, const u
                             const uint64_t *table_entries, const uint64_t *level_offsets,
                             or_transcript *t);
 
+/* ---- Monolith-12 over Goldilocks (goldilocks-cuda-rs/src/cpu_monolith.rs:13-226) ---- */
+/* The permutation (concrete layer, then 6 rounds of bars, bricks, concrete); canonical in/out. */
+void or_monolith_permute(uint64_t s[12]);
+/* Merkle trees with the Monolith leaf hash and compression, layout as or_merkle_tree_gl:
+ * leaves (4 words each), then each layer up to the root.  gl: leaf i = H(cw[2i], cw[2i+1]);
+ * ext2: leaf i = H(cw[4i..4i+3]). */
+void or_monolith_tree_gl(const uint64_t *cw, size_t leaves, uint64_t *tree);
+void or_monolith_tree_ext2(const uint64_t *cw, size_t leaves, uint64_t *tree);
+
 /* ---- almost-Goldilocks (q = 2^64 - 2^32 - 31) + Ext2 (X^2 - 3) ---- */
 uint64_t or_agl_add(uint64_t a, uint64_t b);
 uint64_t or_agl_sub(uint64_t a, uint64_t b);

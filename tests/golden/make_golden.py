@@ -94,6 +94,24 @@ def text_vectors(ref):
     out["sumcheck_h70"] = {"source": f"zk-torch-3/src/sumcheck/linear_prover.rs:{ln}",
                            "p1": [1, 2, 3, 4], "p2": [5, 6, 7, 8], "sum": 70,
                            "labels": {"base": "test", "ext2": "test_cpu_ext2"}}
+    # Monolith-12 permutation KAT and the Merkle test codewords of the reference's CPU tests
+    f = os.path.join(ref, "goldilocks-cuda-rs/src/cpu_monolith.rs")
+    src = open(f).read()
+    m = re.search(r"let expected: \[u64; 12\] = \[(.*?)\];", src, re.S)
+    kat = [int(x) for x in re.findall(r"\d+", m.group(1))]
+    assert len(kat) == 12
+    m = re.search(r"let codeword: Vec<u64> = vec!\[(.*?)\];", src, re.S)
+    big = [int(x, 16) for x in re.findall(r"0x[0-9A-Fa-f]+", m.group(1))]
+    assert len(big) == 32
+    m = re.search(r"let cw: Vec<u64> = vec!\[(.*?)\];", src, re.S)
+    specific = [int(x) for x in re.findall(r"\d+", m.group(1))]
+    out["monolith_kat"] = {"source": f"goldilocks-cuda-rs/src/cpu_monolith.rs:{find_line(f, 'let expected: [u64; 12]')}",
+                           "input": list(range(12)), "expected": kat}
+    out["monolith_tree_inputs"] = {
+        "source": f"goldilocks-cuda-rs/src/cpu_monolith.rs:{find_line(f, 'fn test_monolith_gpu_vs_cpu_merkle()')}",
+        "codewords": [list(range(100, 108)), list(range(1, 33)), specific, big],
+        "ext2_codeword": [10, 20, 30, 40, 50, 60, 70, 80],
+        "large_value_state": [8, P - 8] + [0] * 10}
     f = os.path.join(ref, "zk-torch-3/src/commit/basefold.rs")
     ln = find_line(f, "num_queries: 34")
     out["basefold_key_default"] = {"source": f"zk-torch-3/src/commit/basefold.rs:{ln}",

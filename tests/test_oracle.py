@@ -197,3 +197,20 @@ def test_agl_ext2_test_restatement_matches_pinned_oracle():
         a = [int(x) for x in rng.integers(0, O.Q_AGL, 2, dtype=np.uint64)]
         b = [int(x) for x in rng.integers(0, O.Q_AGL, 2, dtype=np.uint64)]
         assert list(tag.e2mul(a, b)) == [int(x) for x in O.aext2_mul(a, b)]
+
+
+def test_monolith_oracle_matches_reference_kat(golden):
+    """cpu_monolith.rs test vector: Monolith-12 of (0, 1, ..., 11)."""
+    g = golden["monolith_kat"]
+    assert [int(x) for x in O.monolith_permute(np.array(g["input"], np.uint64))] == g["expected"]
+
+
+def test_monolith_oracle_tree_structure():
+    """The oracle's trees: leaves are truncated permutations, parents compress their children."""
+    cw = np.arange(100, 108, dtype=np.uint64)
+    tree = O.monolith_tree_gl(cw).reshape(-1, 4)
+    leaf0 = O.monolith_permute(np.array([100, 101] + [0] * 10, np.uint64))[:4]
+    assert np.array_equal(tree[0], leaf0)
+    parent = O.monolith_permute(np.concatenate([tree[0], tree[1], np.zeros(4, np.uint64)]))[:4]
+    assert np.array_equal(tree[4], parent)
+    assert tree.shape[0] == 7
