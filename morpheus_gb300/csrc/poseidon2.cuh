@@ -206,19 +206,49 @@ __device__ __forceinline__ u64 p2_coop_external_linear(u64 x) {
     return gl_add(out, gl_add(out, shfl_xor64(out, 4)));
 }
 
+// Latency-oriented multiply for the cooperative form, whose cost is the S-box chain's latency,
+// not its instruction count: two independent 64-bit products and the compare-based reduction
+// (fewer dependent steps than the carry-chain product that the throughput kernels use).
+__device__ __forceinline__ u64 gl_mul_lat(u64 a, u64 b) {
+    u64 lo = a * b, hi = __umul64hi(a, b);
+    u64 h1 = hi >> 32, h0 = hi & GL_EPS;
+    u64 t0 = lo - h1;
+    if (lo < h1) t0 -= GL_EPS;
+    u64 t1 = (h0 << 32) - h0;
+    u64 r = t0 + t1;
+    if (r < t1) r += GL_EPS;
+    return r;
+}
+__device__ __forceinline__ u64 p2_sbox_lat(u64 x) {
+    u64 x2 = gl_mul_lat(x, x);
+    u64 x3 = gl_mul_lat(x2, x), x4 = gl_mul_lat(x2, x2);
+    return gl_mul_lat(x4, x3);
+}
+__device__ __forceinline__ glw shfl_xor_glw(glw v, int m) {
+    glw r;
+    r.lo = shfl_xor64(v.lo, m);
+    r.hi = __shfl_xor_sync(0xffffffffu, v.hi, m);
+    return r;
+}
+
+// Internal rounds: the 8-lane sum is kept lazy (64 bits + carries) through the all-reduce and
+// enters the lane's multiply-add unreduced; lane 0 also folds in the next round's constant.
 __device__ __forceinline__ u64 p2_permute_coop(u64 x, int l, const P2Lane& c) {
 #pragma unroll
-    for (int r = 0; r < 4; r++) x = p2_coop_external_linear(p2_sbox(gl_add(x, c.ext[r])));
+    for (int r = 0; r < 4; r++) x = p2_coop_external_linear(p2_sbox_lat(gl_add(x, c.ext[r])));
+    if (l == 0) x = gl_add(x, c_p2_int[0]);
 #pragma unroll
     for (int r = 0; r < 22; r++) {
-        if (l == 0) x = p2_sbox(gl_add(x, c_p2_int[r]));
-        u64 t = gl_add(x, shfl_xor64(x, 1));
-        t = gl_add(t, shfl_xor64(t, 2));
-        t = gl_add(t, shfl_xor64(t, 4));
-        x = gl_add(gl_mul(x, c.diag), t);
+        if (l == 0) x = p2_sbox_lat(x);
+        glw t = glw_of(x);
+        t = glw_add(t, shfl_xor_glw(t, 1));
+        t = glw_add(t, shfl_xor_glw(t, 2));
+        t = glw_add(t, shfl_xor_glw(t, 4));
+        if (l == 0 && r < 21) t = glw_add(t, c_p2_int[r + 1]);
+        x = gl_mul_add(x, c.diag, t);
     }
 #pragma unroll
-    for (int r = 4; r < 8; r++) x = p2_coop_external_linear(p2_sbox(gl_add(x, c.ext[r])));
+    for (int r = 4; r < 8; r++) x = p2_coop_external_linear(p2_sbox_lat(gl_add(x, c.ext[r])));
     return x;
 }
 

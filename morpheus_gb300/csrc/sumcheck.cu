@@ -328,6 +328,94 @@ __global__ void __launch_bounds__(RED_THREADS) sc_fold_round_e2_lazy_kernel(cons
     grid_reduce_finish<W>(acc, partials, msg, counter);
 }
 
+// D == 2: the lazy round with the next pair's loads issued before the current pair is folded
+// (register double buffering; two resident blocks per SM leave room for the extra registers).
+// Same outputs as sc_fold_round_e2_lazy_kernel.
+template <int D>  // D == 2 only (the message's last factor is the second polynomial)
+__global__ void __launch_bounds__(RED_THREADS, 2) sc_fold_round_e2_pf_kernel(const u64* __restrict__ in, size_t in_stride, u64* __restrict__ out,
+                                                          size_t out_stride, size_t quarter, u64 r0_, u64 r1_,
+                                                          u64* __restrict__ partials, u64* __restrict__ msg,
+                                                          unsigned* __restrict__ counter) {
+    constexpr int W = 2 * (D + 1);
+    const u64 r0 = gl_canon(r0_), r1 = gl_canon(r1_), r1x7 = gl_canon(gl_mul7(r1));
+    gl3 A[D + 1], C[D + 1];
+#pragma unroll
+    for (int c = 0; c <= D; c++) A[c] = C[c] = gl3_zero();
+    const size_t step = (size_t)gridDim.x * blockDim.x;
+    size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    e2 nx[D][4];
+    if (y < quarter) {
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            const u64* p = in + (size_t)i * 2 * in_stride + 8 * y;
+#pragma unroll
+            for (int k = 0; k < 4; k++) nx[i][k] = ld_e2(p + 2 * k, true);
+        }
+    }
+    for (; y < quarter; y += step) {
+        e2 x[D][4];
+#pragma unroll
+        for (int i = 0; i < D; i++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) x[i][k] = nx[i][k];
+        const size_t yn = y + step;
+        if (yn < quarter) {
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+                const u64* p = in + (size_t)i * 2 * in_stride + 8 * yn;
+#pragma unroll
+                for (int k = 0; k < 4; k++) nx[i][k] = ld_e2(p + 2 * k, true);
+            }
+        }
+        e2 e[D], dl[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            e2 f[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                u64 d0 = gl_sub(x[i][2 * h + 1].c0, x[i][2 * h].c0), d1 = gl_sub(x[i][2 * h + 1].c1, x[i][2 * h].c1);
+                gl3 c0 = gl3_zero(), c1 = gl3_zero();
+                c0.lo = x[i][2 * h].c0;
+                c1.lo = x[i][2 * h].c1;
+                gl3_add_prod(c0, r0, d0);
+                gl3_add_prod(c0, r1x7, d1);
+                gl3_add_prod(c1, r0, d1);
+                gl3_add_prod(c1, r1, d0);
+                f[h] = e2_make(gl3_reduce(c0), gl3_reduce(c1));
+            }
+            u64* q = out + (size_t)i * 2 * out_stride + 4 * y;
+            e2_st(q, f[0]);
+            e2_st(q + 2, f[1]);
+            e[i] = f[0];
+            dl[i] = e2_sub(f[1], f[0]);
+        }
+        e2 v[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) v[i] = e[i];
+#pragma unroll
+        for (int c = 0; c <= D; c++) {
+            e2 pre = v[0];
+#pragma unroll
+            for (int i = 1; i + 1 < D; i++) pre = e2_mul(pre, v[i]);
+            const e2 last = v[D - 1];
+            gl3_add_prod(A[c], pre.c0, last.c0);
+            gl3_add_prod(A[c], pre.c1, gl_mul7(last.c1));
+            gl3_add_prod(C[c], pre.c0, last.c1);
+            gl3_add_prod(C[c], pre.c1, last.c0);
+            if (c < D)
+#pragma unroll
+                for (int i = 0; i < D; i++) v[i] = e2_add(v[i], dl[i]);
+        }
+    }
+    u64 acc[W];
+#pragma unroll
+    for (int c = 0; c <= D; c++) {
+        acc[2 * c] = gl3_reduce(A[c]);
+        acc[2 * c + 1] = gl3_reduce(C[c]);
+    }
+    grid_reduce_finish<W>(acc, partials, msg, counter);
+}
+
 // Round k >= 1, base-field challenge (LinearSumcheckProver).
 template <int D>
 __global__ void __launch_bounds__(RED_THREADS) sc_fold_round_base_kernel(const u64* __restrict__ in, size_t in_stride,
@@ -442,6 +530,9 @@ struct FoldRoundE2 {
         if (base_in)
             sc_fold_round_e2_kernel<D, true><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
                                                                                  r0, r1, part, msg, ctr);
+        else if constexpr (D == 2)
+            sc_fold_round_e2_pf_kernel<D><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
+                                                                              r0, r1, part, msg, ctr);
         else if constexpr (D <= 4)
             sc_fold_round_e2_lazy_kernel<D><<<grid, RED_THREADS, 0, stream()>>>(in, in_stride, out, out_stride, quarter,
                                                                                 r0, r1, part, msg, ctr);
