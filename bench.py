@@ -187,6 +187,20 @@ def run_side_workload(args):
             GpuLinearSumcheckProver(n, d, t).prove((polys, d), t)
         unit, metric, work = "Melem/s", "sumcheck Melem/s", d * (1 << n) / 1e6
         cfg = {"workload": "product sumcheck, 2 polys x 2^20 Goldilocks, Ext2 challenges, 20 rounds"}
+    elif args.workload == "fold":
+        nf = 24
+        src_buf = DeviceBuffer.from_numpy(rng.integers(0, P, size=2 * 2 * (1 << nf), dtype=np.uint64))
+        dst_buf = DeviceBuffer(2 * 2 * (1 << (nf - 1)))
+        msg = DeviceBuffer(16)
+        work_buf = DeviceBuffer.from_numpy(np.zeros(L.gb_sumcheck_round_workspace_words(), np.uint64))
+
+        def step():
+            Nn.check(L.gb_sumcheck_fold_round_ext2(src_buf.ptr, 0, 1 << nf, dst_buf.ptr, 1 << (nf - 1), 2,
+                                                   1 << (nf - 2), 5, 7, msg.ptr, work_buf.ptr), "fold round")
+        unit, metric = "GB/s", "fused fold round GB/s"
+        work = (2 * (1 << nf) * 16 + 2 * (1 << (nf - 1)) * 16) / 1e9
+        cfg = {"workload": "sumcheck fold round: 2 polys x 2^24 Ext2 folded with an Ext2 challenge to 2 x 2^23, "
+                           "next round's degree-2 message", "l2": "flushed between timed launches"}
     else:
         n_ring, Bw, rows = 1024, 256, 16
         key = np.array([0x5EED, 1, 2, 3, 4, 5, 6, 7], np.uint32)
@@ -206,8 +220,12 @@ def run_side_workload(args):
     ms = statistics.mean(times)
     line = {"metric": metric, "value": work / (ms * 1e-3), "unit": unit, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u64" if args.workload == "sumcheck" else "bf16 limbs (exact), u64 out",
+            "vs_baseline": None, "dtype": "bf16 limbs (exact), u64 out" if args.workload == "ajtai" else "u64",
             "data": "synthetic", "config": cfg, "step_ms_all": [round(t, 4) for t in times]}
+    if args.workload == "fold":
+        peak, src = measured_peaks()
+        line["roofline"] = {"bound": "hbm", "achieved": line["value"], "peak": peak, "unit": "GB/s",
+                            "frac": line["value"] / peak, "peak_source": src}
     if args.workload == "ajtai":
         line["tensor_tflops_equiv"] = 2.0 * 8 * rows * 64 * Bw * n_ring * 64 / (ms * 1e-3) / 1e12
     print(json.dumps(line))
@@ -444,8 +462,9 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="served workload: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")
     ap.add_argument("--hbm-budget-gb", type=int, default=96, help="served workload: admission budget")
-    ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "ajtai", "batched", "served"],
+    ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "ajtai", "batched", "served"],
                     help="basefold (headline): commit+open proofs; sumcheck: 2 x 2^20 product sumcheck; "
+                         "fold: one fused fold round over 2 x 2^24 Ext2; "
                          "ajtai: 256 witnesses x 16 rows x 2^16 coefficients")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -578,7 +597,7 @@ def main():
         fr_ms = min(ev_time(fr) for _ in range(5))
         fbytes = 2 * (1 << nf) * 16 + 2 * (1 << (nf - 1)) * 16
         extras["roofline_hbm"] = {
-            "kernel": "sc_fold_round_e2_lazy_kernel (fold 2 x 2^24 Ext2 + next round message)",
+            "kernel": "sc_fold_round_e2_pf_kernel (fold 2 x 2^24 Ext2 + next round message)",
             "bound": "hbm", "achieved": fbytes / (fr_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
             "frac": fbytes / (fr_ms * 1e-3) / 1e9 / hbm_peak, "peak_source": src, "bytes_per_launch": fbytes,
             "launch_ms": fr_ms,

@@ -159,7 +159,30 @@ __device__ __forceinline__ void gl3_add(gl3& a, u64 x) {
         : "+l"(a.lo), "+l"(a.hi), "+r"(a.top)
         : "l"(x));
 }
-__device__ __forceinline__ u64 gl3_reduce(gl3 a) { return gl_sub(gl_reduce(a.lo, a.hi), (u64)a.top << 32); }
+// lo + 2^64 (h1 2^32 + h0) + 2^128 top == lo - (top 2^32 + h1) + h0 (2^32 - 1)  (2^128 == -2^32):
+// gl_reduce with the top word as the high half of the subtracted word.  For top <= 2^32 - 2 a
+// borrow still leaves at least EPS, so one -EPS correction remains enough.
+__device__ __forceinline__ u64 gl3_reduce(gl3 a) {
+    u32 l0 = (u32)a.lo, l1 = (u32)(a.lo >> 32), h0 = (u32)a.hi, h1 = (u32)(a.hi >> 32);
+    u32 s0, s1;
+    asm("{\n\t.reg .u32 b, t0, t1, c, m;\n\t"
+        "sub.cc.u32 %0, %2, %5;\n\t"
+        "subc.cc.u32 %1, %3, %6;\n\t"
+        "subc.u32 b, 0, 0;\n\t"
+        "sub.cc.u32 %0, %0, b;\n\t"
+        "subc.u32 %1, %1, 0;\n\t"
+        "sub.cc.u32 t0, 0, %4;\n\t"
+        "subc.u32 t1, %4, 0;\n\t"
+        "add.cc.u32 %0, %0, t0;\n\t"
+        "addc.cc.u32 %1, %1, t1;\n\t"
+        "addc.u32 c, 0, 0;\n\t"
+        "sub.u32 m, 0, c;\n\t"
+        "add.cc.u32 %0, %0, m;\n\t"
+        "addc.u32 %1, %1, 0;\n\t}"
+        : "=r"(s0), "=r"(s1)
+        : "r"(l0), "r"(l1), "r"(h0), "r"(h1), "r"(a.top));
+    return ((u64)s1 << 32) | s0;
+}
 
 // a b + c reduced, for b < p: the product's high word is then below 2^64 - 2^32, so adding
 // c (hi < 2^32) cannot carry out of 128 bits

@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(RED_THREADS, 2) sc_fold_round_e2_pf_kernel(con
                                                           size_t out_stride, size_t quarter, u64 r0_, u64 r1_,
                                                           u64* __restrict__ partials, u64* __restrict__ msg,
                                                           unsigned* __restrict__ counter) {
+    static_assert(D == 2, "the prefetching fold round is the degree-2 form");
     constexpr int W = 2 * (D + 1);
     const u64 r0 = gl_canon(r0_), r1 = gl_canon(r1_), r1x7 = gl_canon(gl_mul7(r1));
     gl3 A[D + 1], C[D + 1];
@@ -367,7 +368,7 @@ __global__ void __launch_bounds__(RED_THREADS, 2) sc_fold_round_e2_pf_kernel(con
                 for (int k = 0; k < 4; k++) nx[i][k] = ld_e2(p + 2 * k, true);
             }
         }
-        e2 e[D], dl[D];
+        e2 e[D], f1[D], dl[D];
 #pragma unroll
         for (int i = 0; i < D; i++) {
             e2 f[2];
@@ -387,32 +388,29 @@ __global__ void __launch_bounds__(RED_THREADS, 2) sc_fold_round_e2_pf_kernel(con
             e2_st(q, f[0]);
             e2_st(q + 2, f[1]);
             e[i] = f[0];
+            f1[i] = f[1];
             dl[i] = e2_sub(f[1], f[0]);
         }
-        e2 v[D];
+        // the product at 0, at 1, and its leading coefficient (the product of the slopes)
+        const e2 pts[3][2] = {{e[0], e[1]}, {f1[0], f1[1]}, {dl[0], dl[1]}};
 #pragma unroll
-        for (int i = 0; i < D; i++) v[i] = e[i];
-#pragma unroll
-        for (int c = 0; c <= D; c++) {
-            e2 pre = v[0];
-#pragma unroll
-            for (int i = 1; i + 1 < D; i++) pre = e2_mul(pre, v[i]);
-            const e2 last = v[D - 1];
+        for (int c = 0; c < 3; c++) {
+            const e2 pre = pts[c][0], last = pts[c][1];
             gl3_add_prod(A[c], pre.c0, last.c0);
             gl3_add_prod(A[c], pre.c1, gl_mul7(last.c1));
             gl3_add_prod(C[c], pre.c0, last.c1);
             gl3_add_prod(C[c], pre.c1, last.c0);
-            if (c < D)
-#pragma unroll
-                for (int i = 0; i < D; i++) v[i] = e2_add(v[i], dl[i]);
         }
     }
+    // s(2) = 2 s(1) - s(0) + 2 lead (the second difference of a quadratic is twice its lead)
     u64 acc[W];
 #pragma unroll
-    for (int c = 0; c <= D; c++) {
+    for (int c = 0; c < 3; c++) {
         acc[2 * c] = gl3_reduce(A[c]);
         acc[2 * c + 1] = gl3_reduce(C[c]);
     }
+#pragma unroll
+    for (int k = 0; k < 2; k++) acc[4 + k] = gl_sub(gl_add(gl_double(acc[2 + k]), gl_double(acc[4 + k])), acc[k]);
     grid_reduce_finish<W>(acc, partials, msg, counter);
 }
 
