@@ -154,6 +154,24 @@ def cpu_baseline_sample():
     return {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port", "sample": sample}
 
 
+def batch_open_cpu_sample(num_claims, sample_vars=12, n=20):
+    """The C restatement of batch_open_ext2 (one core) on 8 polys x 2^sample_vars at 2 points,
+    time scaled by 2^(n - sample_vars) to the 2^n workload."""
+    import oracle as O
+    O.build(ref=False)
+    rng = np.random.default_rng(7)
+    comms = [O.basefold_commit(rng.integers(0, P, size=1 << sample_vars, dtype=np.uint64), LOG_RATE) for _ in range(8)]
+    points = [rng.integers(0, P, size=(sample_vars, 2), dtype=np.uint64) for _ in range(2)]
+    claims = [(j, k, rng.integers(0, P, size=2, dtype=np.uint64)) for j in range(8) for k in range(2)]
+    table = O.basefold_table(sample_vars, LOG_RATE, sample_vars, TABLE_SEED)
+    t0 = time.perf_counter()
+    O.basefold_batch_open_ext2(comms, points, claims, table, O.Transcript(b"bf-batch"), QUERIES)
+    wall = (time.perf_counter() - t0) * (1 << (n - sample_vars))
+    return {"value": num_claims / wall, "unit": "claims/s", "cores": 1, "kind": "port",
+            "sample": f"one batch opening of 8 polys x 2^{sample_vars} at 2 points (C restatement, one core), "
+                      f"time scaled x{1 << (n - sample_vars)} to 2^{n}"}
+
+
 def run_side_workload(args):
     """Configs other than the headline, each on one GPU with inputs resident in HBM."""
     import torch
@@ -187,6 +205,22 @@ def run_side_workload(args):
             GpuLinearSumcheckProver(n, d, t).prove((polys, d), t)
         unit, metric, work = "Melem/s", "sumcheck Melem/s", d * (1 << n) / 1e6
         cfg = {"workload": "product sumcheck, 2 polys x 2^20 Goldilocks, Ext2 challenges, 20 rounds"}
+    elif args.workload == "batch_open":
+        from morpheus_gb300.basefold import BasefoldCommitment, BasefoldTable, batch_open_ext2
+        from morpheus_gb300.sumcheck import Transcript
+        n, npoly, npts, q = 20, 8, 2, QUERIES
+        tab = BasefoldTable.generate(n, LOG_RATE, n, TABLE_SEED)
+        comms = [BasefoldCommitment.commit(rng.integers(0, P, size=1 << n, dtype=np.uint64), n, LOG_RATE)
+                 for _ in range(npoly)]
+        points = [rng.integers(0, P, size=(n, 2), dtype=np.uint64) for _ in range(npts)]
+        claims = [(j, k, rng.integers(0, P, size=2, dtype=np.uint64)) for j in range(npoly) for k in range(npts)]
+
+        def step():
+            t = Transcript(b"bf-batch")
+            batch_open_ext2(comms, points, claims, tab, t, q)
+        unit, metric, work = "claims/s", "batch_open_ext2 claims/s", float(len(claims))
+        cfg = {"workload": f"batch_open_ext2: {npoly} polys x 2^{n}, {npts} points, {len(claims)} claims, "
+                           f"rate 1/2, {q} queries", "l2": "flushed between timed steps"}
     elif args.workload == "fold":
         nf = 24
         src_buf = DeviceBuffer.from_numpy(rng.integers(0, P, size=2 * 2 * (1 << nf), dtype=np.uint64))
@@ -222,6 +256,8 @@ def run_side_workload(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16 limbs (exact), u64 out" if args.workload == "ajtai" else "u64",
             "data": "synthetic", "config": cfg, "step_ms_all": [round(t, 4) for t in times]}
+    if args.workload == "batch_open":
+        line["cpu_baseline"] = batch_open_cpu_sample(len(claims))
     if args.workload == "fold":
         peak, src = measured_peaks()
         line["roofline"] = {"bound": "hbm", "achieved": line["value"], "peak": peak, "unit": "GB/s",
@@ -462,9 +498,10 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="served workload: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")
     ap.add_argument("--hbm-budget-gb", type=int, default=96, help="served workload: admission budget")
-    ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "ajtai", "batched", "served"],
+    ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "batch_open", "ajtai", "batched", "served"],
                     help="basefold (headline): commit+open proofs; sumcheck: 2 x 2^20 product sumcheck; "
                          "fold: one fused fold round over 2 x 2^24 Ext2; "
+                         "batch_open: 8 polys x 2^20 opened at 2 points; "
                          "ajtai: 256 witnesses x 16 rows x 2^16 coefficients")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -254,6 +254,23 @@ size_t gb_basefold_proof_len(int num_vars, int log_rate, int num_queries);
 int gb_basefold_open_ext2(void *commitment, void *table, const uint64_t *h_point, gb_transcript *t,
                           int num_queries, uint64_t *h_proof);
 
+/* batch_open_ext2 (goldilocks-cuda-rs/src/basefold.rs:1202-1532; BatchBasefoldProofExt2,
+ * :192-210): num_commitments commitments of equal num_vars and log_rate, opened at num_points
+ * Ext2 points (h_points: num_points x num_vars Ext2).  Evaluation i claims that polynomial
+ * eval_poly[i] at point eval_point[i] equals h_eval_values[2i..2i+1]; its transcript absorbs every
+ * root, point and claim, as the reference does.  h_proof (gb_basefold_batch_proof_len words,
+ * canonical): outer oracles [n][3][2] | combined root [4] | inner eval [2] | inner oracles
+ * [n][3][2] | folded roots [n-1][4] | final codeword [2^lr][2] | num_queries combined queries in
+ * the gb_basefold_open_ext2 query layout (round-0 values Ext2) | num_queries x num_evals
+ * individual queries (base pair [2] + path [n+lr-1][4]).  Returns 0 or GB_EINVAL (empty input,
+ * unequal shapes, an index out of range, a table that does not cover the commitments).
+ * Synchronising. */
+size_t gb_basefold_batch_proof_len(int num_vars, int log_rate, int num_queries, int num_evals);
+int gb_basefold_batch_open_ext2(void *const *commitments, int num_commitments, const uint64_t *h_points,
+                                int num_points, const int *eval_poly, const int *eval_point,
+                                const uint64_t *h_eval_values, int num_evals, void *table, gb_transcript *t,
+                                int num_queries, uint64_t *h_proof);
+
 /* ---- Batched and served proving (no reference counterpart) ----
  * An instance is `degree` multilinear polynomials of 2^num_vars base-field values, proven by
  * (1) Basefold commit of each (log_rate 1), (2) the product sumcheck with Ext2 challenges on

@@ -128,6 +128,9 @@ SIGNATURES = {
     "gb_basefold_commitment_info": (i32, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), vp]),
     "gb_basefold_proof_len": (sz, [i32, i32, i32]),
     "gb_basefold_open_ext2": (i32, [vp, vp, vp, ctypes.POINTER(GbTranscript), i32, vp]),
+    "gb_basefold_batch_proof_len": (sz, [i32, i32, i32, i32]),
+    "gb_basefold_batch_open_ext2": (i32, [vp, i32, vp, i32, vp, vp, vp, i32, vp, ctypes.POINTER(GbTranscript), i32,
+                                          vp]),
     "gb_instance_proof_len": (sz, [i32, i32, i32]),
     "gb_instance_hbm_bytes": (sz, [i32, i32]),
     "gb_prove_instance": (i32, [vp, vp, i32, vp]),

@@ -149,3 +149,55 @@ def split_proof(proof, n, lr, q):
         queries.append({"index": idx, "values": vals, "paths": paths})
     assert o == len(p)
     return {"eval": eval_, "oracles": oracles, "folded_roots": roots, "final_codeword": final, "queries": queries}
+
+
+def batch_proof_len(num_vars, log_rate, num_queries, num_evals):
+    return N.lib().gb_basefold_batch_proof_len(num_vars, log_rate, num_queries, num_evals)
+
+
+def batch_open_ext2(comms, points, evals, table, transcript, num_queries):
+    """batch_open_ext2 (goldilocks-cuda-rs/src/basefold.rs:1202-1532): open the commitments at Ext2
+    points.  evals: (poly, point, value) triples, value an Ext2 pair; returns the flat proof
+    (gb_basefold_batch_open_ext2 layout, see split_batch_proof)."""
+    n, lr = comms[0].num_vars, comms[0].log_rate
+    pts = np.ascontiguousarray(np.asarray(points, dtype=np.uint64).reshape(-1))
+    assert pts.size == 2 * n * len(points)
+    handles = (ctypes.c_void_p * len(comms))(*[c.handle for c in comms])
+    poly = np.ascontiguousarray([e[0] for e in evals], dtype=np.int32)
+    point = np.ascontiguousarray([e[1] for e in evals], dtype=np.int32)
+    vals = np.ascontiguousarray(np.asarray([np.asarray(e[2], np.uint64) for e in evals], np.uint64).reshape(-1))
+    L = batch_proof_len(n, lr, num_queries, max(len(evals), 1))
+    proof = np.zeros(max(L, 1), np.uint64)
+    rc = N.lib().gb_basefold_batch_open_ext2(ctypes.cast(handles, ctypes.c_void_p), len(comms), pts.ctypes.data,
+                                             len(points), poly.ctypes.data, point.ctypes.data, vals.ctypes.data,
+                                             len(evals), table.handle, ctypes.byref(transcript.state), num_queries,
+                                             proof.ctypes.data)
+    N.check(rc, "gb_basefold_batch_open_ext2")
+    return proof
+
+
+def split_batch_proof(proof, n, lr, q, num_evals):
+    """Structured view of a flat batch proof (BatchBasefoldProofExt2 field order)."""
+    p = np.asarray(proof)
+    o = 0
+
+    def take(k):
+        nonlocal o
+        v = p[o:o + k]
+        o += k
+        return v
+    out = {"outer_oracles": take(n * 6).reshape(n, 3, 2), "combined_root": take(4), "inner_eval": take(2),
+           "inner_oracles": take(n * 6).reshape(n, 3, 2), "folded_roots": take((n - 1) * 4).reshape(n - 1, 4),
+           "final_codeword": take(2 << lr).reshape(-1, 2)}
+    depths = [n + lr - 1 - r for r in range(n)]
+    cq = []
+    for _ in range(q):
+        idx = int(take(1)[0])
+        vals = take(n * 4).reshape(n, 2, 2)
+        cq.append({"index": idx, "values": vals, "paths": [take(d * 4).reshape(d, 4) for d in depths]})
+    iq = [[{"values": take(2), "path": take((n + lr - 1) * 4).reshape(-1, 4)} for _ in range(num_evals)]
+          for _ in range(q)]
+    assert o == len(p)
+    out["combined_queries"] = cq
+    out["individual_queries"] = iq
+    return out

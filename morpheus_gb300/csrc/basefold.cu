@@ -18,6 +18,7 @@
 // fold of round r writes the folded codeword and hashes its leaves in the same
 // launch.  Per round the host receives 10 canonical words (oracle + root), runs the
 // transcript and launches the next round.  Queries are gathered by one kernel.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -263,12 +264,16 @@ __global__ void __launch_bounds__(RED_THREADS) dot_product_kernel(const u64* __r
 
 // Round 0 oracle on (bh base, eq Ext2) at full size: acc = (c0, s1, c2) with
 // s1 = sum eq_o bh_o = c0 + c1 + c2.  Also the pairs' eval = c0 + s1.
+// BH_BASE: base evaluations (a commitment's); else Ext2 (a batch opening's combined ones).
+template <bool BH_BASE>
 __global__ void __launch_bounds__(RED_THREADS) open_round0_kernel(const u64* __restrict__ bh, const u64* __restrict__ eq,
                                                                   size_t pairs, u64* __restrict__ partials,
                                                                   u64* __restrict__ out, unsigned* __restrict__ counter) {
     u64 acc[6] = {0, 0, 0, 0, 0, 0};
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x)
-        open_round0_item(bh, eq, i, acc);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x) {
+        if (BH_BASE) open_round0_item(bh, eq, i, acc);
+        else open_round0_e2_item(bh, eq, i, acc);
+    }
     grid_reduce_finish<6>(acc, partials, out, counter);
 }
 
@@ -342,6 +347,117 @@ __global__ void query_gather_kernel(QueryJob job, const u64* __restrict__ leaf_i
     int q = blockIdx.x;
     if (q >= num_queries) return;
     query_gather_block(job, leaf_idx[q], out + (size_t)q * per_query);
+}
+
+// ===========================================================================
+// batch opening kernels (batch_open_ext2, basefold.rs:1202-1532)
+// ===========================================================================
+
+// One scaled source of a linear combination: src (base) times (c0, c1).
+struct BoTerm {
+    const u64* src;
+    u64 c0, c1;
+};
+
+// g_p[k] = sum of the point's terms c0 * src[k]  (blockIdx.y = point; terms start[p] .. start[p+1])
+__global__ void bo_accum_g_kernel(const BoTerm* __restrict__ terms, const int* __restrict__ start, size_t N,
+                                  u64* __restrict__ g) {
+    const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int p = blockIdx.y;
+    gl3 a = gl3_zero();
+    for (int j = start[p]; j < start[p + 1]; j++) gl3_add_prod(a, terms[j].c0, __ldg(terms[j].src + k));
+    g[(size_t)p * N + k] = gl3_reduce(a);
+}
+
+// Outer sumcheck round 0 over all points at once (blockIdx.y = point): g_p base at g + p N,
+// eq_p Ext2 at eq + 2 p N; one message summed over every point's pairs.
+__global__ void __launch_bounds__(RED_THREADS) bo_round0_kernel(const u64* __restrict__ g, const u64* __restrict__ eq,
+                                                                size_t N, u64* __restrict__ partials,
+                                                                u64* __restrict__ out, unsigned* __restrict__ counter) {
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    const u64* gp = g + (size_t)blockIdx.y * N;
+    const u64* ep = eq + (size_t)blockIdx.y * 2 * N;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N / 2; i += (size_t)gridDim.x * blockDim.x)
+        open_round0_item(gp, ep, i, acc);
+    grid_reduce_finish_n<6>(acc, partials, out, counter, blockIdx.y * gridDim.x + blockIdx.x, gridDim.x * gridDim.y);
+}
+
+// Outer round k >= 1 over all points: fold eq_p, g_p (base when BH_BASE) with ch; strides in words.
+template <bool BH_BASE>
+__global__ void __launch_bounds__(RED_THREADS) bo_round_kernel(const u64* __restrict__ eq_in, size_t eq_stride,
+                                                               const u64* __restrict__ g_in, size_t g_stride,
+                                                               u64* __restrict__ eq_out, u64* __restrict__ g_out,
+                                                               size_t out_stride, size_t quarter, u64 c0, u64 c1,
+                                                               u64* __restrict__ partials, u64* __restrict__ out,
+                                                               unsigned* __restrict__ counter) {
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    const e2 ch = e2_make(c0, c1);
+    const size_t p = blockIdx.y;
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < quarter; y += (size_t)gridDim.x * blockDim.x)
+        open_round_item<BH_BASE>(eq_in + p * eq_stride, g_in + p * g_stride, eq_out + p * out_stride,
+                                 g_out + p * out_stride, y, ch, acc);
+    grid_reduce_finish_n<6>(acc, partials, out, counter, blockIdx.y * gridDim.x + blockIdx.x, gridDim.x * gridDim.y);
+}
+
+// Combined Ext2 codeword sum_j scalar_j cw_j fused with its leaf hashes: leaf i = P2(ccw[2i] || ccw[2i+1]).
+__global__ void __launch_bounds__(128) bo_combine_leaves_kernel(const BoTerm* __restrict__ terms, int num_terms,
+                                                                u64* __restrict__ ccw, u64* __restrict__ tree,
+                                                                size_t leaves) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= leaves) return;
+    gl3 a[4] = {gl3_zero(), gl3_zero(), gl3_zero(), gl3_zero()};
+    for (int j = 0; j < num_terms; j++) {
+        const BoTerm tm = terms[j];
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(tm.src) + i);
+        gl3_add_prod(a[0], tm.c0, v.x);
+        gl3_add_prod(a[1], tm.c1, v.x);
+        gl3_add_prod(a[2], tm.c0, v.y);
+        gl3_add_prod(a[3], tm.c1, v.y);
+    }
+    u64 s[8] = {gl3_reduce(a[0]), gl3_reduce(a[1]), gl3_reduce(a[2]), gl3_reduce(a[3]), 0, 0, 0, 0};
+    e2_st(ccw + 4 * i, e2_make(s[0], s[1]));
+    e2_st(ccw + 4 * i + 2, e2_make(s[2], s[3]));
+    p2_permute(s);
+    st_digest(tree + 4 * i, s);
+}
+
+// Combined Ext2 evaluations sum_j scalar_j evals_j (natural order).
+__global__ void bo_combine_evals_kernel(const BoTerm* __restrict__ terms, int num_terms, u64* __restrict__ out,
+                                        size_t N) {
+    const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    gl3 a0 = gl3_zero(), a1 = gl3_zero();
+    for (int j = 0; j < num_terms; j++) {
+        const BoTerm tm = terms[j];
+        const u64 v = __ldg(tm.src + k);
+        gl3_add_prod(a0, tm.c0, v);
+        gl3_add_prod(a1, tm.c1, v);
+    }
+    e2_st(out + 2 * k, e2_make(gl3_reduce(a0), gl3_reduce(a1)));
+}
+
+// Individual query (q, j) (block q * E + j): the committed pair of evaluation j's codeword at the
+// query's leaf and its authentication path, canonical: 2 + 4 depth words.
+__global__ void bo_indiv_query_kernel(const u64* const* __restrict__ cws, const u64* const* __restrict__ trees,
+                                      const u64* __restrict__ leaf_idx, int num_evals, int depth, size_t leaves0,
+                                      u64* __restrict__ out) {
+    const int q = blockIdx.x / num_evals, j = blockIdx.x % num_evals;
+    const size_t leaf = leaf_idx[q];
+    u64* d = out + (size_t)blockIdx.x * (2 + 4 * (size_t)depth);
+    if (threadIdx.x == 0) {
+        d[0] = gl_canon(cws[j][2 * leaf]);
+        d[1] = gl_canon(cws[j][2 * leaf + 1]);
+    }
+    for (int l = threadIdx.x; l < depth; l += blockDim.x) {
+        size_t off = 0, sz = leaves0;
+        for (int k = 0; k < l; k++) {
+            off += sz;
+            sz >>= 1;
+        }
+        const u64* dg = trees[j] + 4 * (off + ((leaf >> l) ^ 1));
+        for (int k = 0; k < 4; k++) d[2 + 4 * l + k] = gl_canon(dg[k]);
+    }
 }
 
 // ===========================================================================
@@ -479,23 +595,29 @@ static int table_create(int num_vars, int log_rate, int num_rounds, u64 seed, Bf
     return GB_OK;
 }
 
-// BasefoldCommitment::open_ext2 (basefold.rs:578-870) into the flat proof layout.
-static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_point, gb_transcript* t, int num_queries,
-                     u64* h_proof) {
+// The rounds and queries of open_ext2 from its eq table onwards (basefold.rs:640-870), shared by
+// the single opening (base evaluations and codeword) and the inner phase of a batch opening
+// (their Ext2 linear combinations).
+struct OpenRounds {
+    const u64* bh;  // round-0 evaluations, natural order: base, or Ext2 when !bh_base
+    bool bh_base;
+    const u64* cw;  // round-0 codeword, 2^(n+lr) elements: base, or Ext2 when !cw_base
+    bool cw_base;
+    const u64* tree;  // its Merkle tree
+    int n, lr;
+};
+
+// Writes eval (2 words), n oracles, n-1 folded roots, the final codeword (2^lr Ext2) and the
+// queries; *d_leaf_idx receives the device array of the query leaves (num_queries > 0).
+static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, gb_transcript* t, int num_queries,
+                       u64* p_eval, u64* p_oracles, u64* p_roots, u64* p_final, u64* p_queries, DevMem& m,
+                       u64** d_leaf_idx) {
     using namespace host;
-    const int n = c->num_vars, lr = c->log_rate;
-    if (n < 2 || num_queries < 0 || !tab->d_entries || tab->num_rounds < n || tab->log_rate != lr ||
-        tab->num_vars < n) {
-        set_error_msg("gb_basefold_open_ext2: table does not cover this commitment (or num_vars < 2)");
-        return GB_EINVAL;
-    }
     cudaStream_t s = stream();
+    const int n = in.n, lr = in.lr;
     const size_t N = (size_t)1 << n, L = N << lr;
-    DevMem m;
-    u64 *d_point, *eq, *eqA, *eqB, *bhA, *bhB, *partials, *rec;
+    u64 *eqA, *eqB, *bhA, *bhB, *partials, *rec;
     unsigned* counter;
-    RC_TRY(m.alloc(&d_point, (size_t)n * 16));
-    RC_TRY(m.alloc(&eq, N * 16));
     RC_TRY(m.alloc(&eqA, N * 8));  // N/2 Ext2
     RC_TRY(m.alloc(&eqB, N * 8));
     RC_TRY(m.alloc(&bhA, N * 8));
@@ -514,24 +636,6 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
     }
     u64* stage = pinned(64);
     if (!stage) return GB_ECUDA;
-
-    u64* pp = h_proof;
-    u64* p_eval = pp;
-    u64* p_oracles = pp + 2;
-    u64* p_roots = p_oracles + (size_t)n * 6;
-    u64* p_final = p_roots + (size_t)(n - 1) * 4;
-    u64* p_queries = p_final + ((size_t)2 << lr);
-
-    // transcript preamble
-    for (int k = 0; k < 4; k++) tr_append_u64(t, "", c->root[k]);
-    std::vector<u64> pt(2 * n);
-    for (int i = 0; i < n; i++) {
-        pt[2 * i] = canon(h_point[2 * i]);
-        pt[2 * i + 1] = canon(h_point[2 * i + 1]);
-        tr_append_ext2(t, "", E2{pt[2 * i], pt[2 * i + 1]});
-    }
-    GB_CUDA_TRY(cudaMemcpyAsync(d_point, pt.data(), (size_t)n * 16, cudaMemcpyHostToDevice, s));
-    RC_TRY(eq_table(d_point, n, true, eq));
 
     auto read_rec = [&](int words) -> int {
         GB_CUDA_TRY(cudaMemcpyAsync(stage, rec, (size_t)words * 8, cudaMemcpyDeviceToHost, s));
@@ -555,8 +659,11 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
         return s1;
     };
 
-    // round 0 oracle (bh = evals base, eq Ext2); eval = c0 + s1
-    open_round0_kernel<<<red_grid(N / 2), RED_THREADS, 0, s>>>(c->d_evals, eq, N / 2, partials, rec, counter);
+    // round 0 oracle over (bh, eq); eval = c0 + s1
+    if (in.bh_base)
+        open_round0_kernel<true><<<red_grid(N / 2), RED_THREADS, 0, s>>>(in.bh, eq, N / 2, partials, rec, counter);
+    else
+        open_round0_kernel<false><<<red_grid(N / 2), RED_THREADS, 0, s>>>(in.bh, eq, N / 2, partials, rec, counter);
     GB_LAUNCH_CHECK("open_round0_kernel");
     RC_TRY(read_rec(6));
     {
@@ -568,7 +675,7 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
     }
 
     const u64* eq_cur = eq;
-    const u64* bh_cur = c->d_evals;
+    const u64* bh_cur = in.bh;
     u64* eq_bufs[2] = {eqA, eqB};
     u64* bh_bufs[2] = {bhA, bhB};
     int pp_i = 0;
@@ -580,7 +687,7 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
             u64* eo = eq_bufs[pp_i];
             u64* bo = bh_bufs[pp_i];
             unsigned g = red_grid(quarter);
-            if (rd == 0)
+            if (rd == 0 && in.bh_base)
                 open_round_kernel<true><<<g, RED_THREADS, 0, s>>>(eq_cur, bh_cur, eo, bo, quarter, ch.c0, ch.c1, partials,
                                                                   rec, counter);
             else
@@ -593,20 +700,21 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
             sc /= 2;
         }
         const u64* lvl = tab->d_entries + 2 * tab->level_offsets[rd];
-        const u64* cw_in = rd == 0 ? c->d_codeword : fcw[rd - 1];
+        const u64* cw_in = rd == 0 ? in.cw : fcw[rd - 1];
+        const bool base_in = rd == 0 && in.cw_base;
         size_t pairs = L >> (rd + 1);
         if (rd < n - 1) {
             size_t leaves = pairs / 2;
             if (leaves < mk_coop_below()) {
                 int th = coop_threads(leaves);
                 unsigned g = grid_for(leaves * 8, th);
-                if (rd == 0)
+                if (base_in)
                     fold_hash_leaves_coop_kernel<true><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
                                                                          leaves);
                 else
                     fold_hash_leaves_coop_kernel<false><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
                                                                           leaves);
-            } else if (rd == 0) {
+            } else if (base_in) {
                 fold_hash_leaves_kernel<true><<<grid_for(leaves, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
                                                                                      ftree[rd], leaves);
             } else {
@@ -623,7 +731,7 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
                 tr_append_u64(t, "", root[k]);
             }
         } else {
-            fold_final_kernel<<<grid_for(pairs, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], pairs, rd == 0);
+            fold_final_kernel<<<grid_for(pairs, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], pairs, base_in);
             GB_LAUNCH_CHECK("fold_final_kernel");
         }
     }
@@ -647,10 +755,293 @@ static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_poi
         }
         GB_CUDA_TRY(cudaMemcpyAsync(d_idx, idx.data(), (size_t)num_queries * 8, cudaMemcpyHostToDevice, s));
         GB_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), ptrs.size() * sizeof(u64*), cudaMemcpyHostToDevice, s));
-        QueryJob job{c->d_codeword, c->d_tree, d_ptrs, d_ptrs + n, n, lr};
+        QueryJob job{in.cw, in.tree, d_ptrs, d_ptrs + n, n, lr, !in.cw_base};
         query_gather_kernel<<<num_queries, 128, 0, s>>>(job, d_idx, num_queries, per_q, d_out);
         GB_LAUNCH_CHECK("query_gather_kernel");
         GB_CUDA_TRY(cudaMemcpyAsync(p_queries, d_out, (size_t)num_queries * per_q * 8, cudaMemcpyDeviceToHost, s));
+        if (d_leaf_idx) *d_leaf_idx = d_idx;
+    }
+    return GB_OK;
+}
+
+static bool table_covers(const BfTable* tab, int n, int lr) {
+    return tab && tab->d_entries && tab->num_rounds >= n && tab->log_rate == lr && tab->num_vars >= n;
+}
+
+// BasefoldCommitment::open_ext2 (basefold.rs:578-870) into the flat proof layout.
+static int open_ext2(const BfCommitment* c, const BfTable* tab, const u64* h_point, gb_transcript* t, int num_queries,
+                     u64* h_proof) {
+    using namespace host;
+    const int n = c->num_vars, lr = c->log_rate;
+    if (n < 2 || num_queries < 0 || !table_covers(tab, n, lr)) {
+        set_error_msg("gb_basefold_open_ext2: table does not cover this commitment (or num_vars < 2)");
+        return GB_EINVAL;
+    }
+    cudaStream_t s = stream();
+    const size_t N = (size_t)1 << n;
+    DevMem m;
+    u64 *d_point, *eq;
+    RC_TRY(m.alloc(&d_point, (size_t)n * 16));
+    RC_TRY(m.alloc(&eq, N * 16));
+
+    u64* p_eval = h_proof;
+    u64* p_oracles = h_proof + 2;
+    u64* p_roots = p_oracles + (size_t)n * 6;
+    u64* p_final = p_roots + (size_t)(n - 1) * 4;
+    u64* p_queries = p_final + ((size_t)2 << lr);
+
+    // transcript preamble
+    for (int k = 0; k < 4; k++) tr_append_u64(t, "", c->root[k]);
+    std::vector<u64> pt(2 * n);
+    for (int i = 0; i < n; i++) {
+        pt[2 * i] = canon(h_point[2 * i]);
+        pt[2 * i + 1] = canon(h_point[2 * i + 1]);
+        tr_append_ext2(t, "", E2{pt[2 * i], pt[2 * i + 1]});
+    }
+    GB_CUDA_TRY(cudaMemcpyAsync(d_point, pt.data(), (size_t)n * 16, cudaMemcpyHostToDevice, s));
+    RC_TRY(eq_table(d_point, n, true, eq));
+    OpenRounds in{c->d_evals, true, c->d_codeword, true, c->d_tree, n, lr};
+    RC_TRY(open_rounds(in, tab, eq, t, num_queries, p_eval, p_oracles, p_roots, p_final, p_queries, m, nullptr));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return GB_OK;
+}
+
+static inline size_t batch_proof_len(int n, int lr, int q, int num_evals) {
+    size_t per_q = 1 + (size_t)n * 4 + path_words_total(n, lr);
+    size_t indiv = 2 + (size_t)(n + lr - 1) * 4;
+    return (size_t)n * 6 + 4 + 2 + (size_t)n * 6 + (size_t)(n - 1) * 4 + ((size_t)2 << lr) + (size_t)q * per_q +
+           (size_t)q * num_evals * indiv;
+}
+
+// batch_open_ext2 (basefold.rs:1202-1532).  Outer sumcheck over sum_p eq_p g_p with every point's
+// pairs in one launch per round (blockIdx.y = point); the combined codeword is formed and its
+// leaves hashed in one launch; the inner phase runs the open rounds on the combined Ext2
+// codeword and evaluations at the outer challenges r.
+static int batch_open_ext2(BfCommitment* const* comms, int num_comms, const u64* h_points, int num_points,
+                           const int* ev_poly, const int* ev_point, const u64* ev_vals, int num_evals,
+                           const BfTable* tab, gb_transcript* t, int num_queries, u64* h_proof) {
+    using namespace host;
+    if (!comms || num_comms < 1 || !h_points || num_points < 1 || !ev_poly || !ev_point || !ev_vals ||
+        num_evals < 1 || num_queries < 0 || !t || !h_proof) {
+        set_error_msg("gb_basefold_batch_open_ext2: empty or null argument");
+        return GB_EINVAL;
+    }
+    for (int c = 0; c < num_comms; c++)
+        if (!comms[c]) return GB_EINVAL;
+    const int n = comms[0]->num_vars, lr = comms[0]->log_rate;
+    for (int c = 1; c < num_comms; c++)
+        if (comms[c]->num_vars != n || comms[c]->log_rate != lr) {
+            set_error_msg("gb_basefold_batch_open_ext2: commitments differ in num_vars or log_rate");
+            return GB_EINVAL;
+        }
+    for (int i = 0; i < num_evals; i++)
+        if (ev_poly[i] < 0 || ev_poly[i] >= num_comms || ev_point[i] < 0 || ev_point[i] >= num_points) {
+            set_error_msg("gb_basefold_batch_open_ext2: evaluation index out of range");
+            return GB_EINVAL;
+        }
+    if (n < 2 || !table_covers(tab, n, lr)) {
+        set_error_msg("gb_basefold_batch_open_ext2: table does not cover the commitments (or num_vars < 2)");
+        return GB_EINVAL;
+    }
+    cudaStream_t s = stream();
+    const size_t N = (size_t)1 << n, L = N << lr, P = (size_t)num_points, E = (size_t)num_evals;
+    u64* p_outer = h_proof;
+    u64* p_croot = p_outer + (size_t)n * 6;
+    u64* p_ieval = p_croot + 4;
+    u64* p_inner = p_ieval + 2;
+    u64* p_roots = p_inner + (size_t)n * 6;
+    u64* p_final = p_roots + (size_t)(n - 1) * 4;
+    u64* p_cq = p_final + ((size_t)2 << lr);
+    const size_t per_q = 1 + (size_t)n * 4 + path_words_total(n, lr);
+    u64* p_iq = p_cq + (size_t)num_queries * per_q;
+
+    // 1. transcript: roots, points, claimed values
+    std::vector<u64> pts(P * n * 2);
+    for (size_t k = 0; k < pts.size(); k++) pts[k] = canon(h_points[k]);
+    for (int c = 0; c < num_comms; c++)
+        for (int k = 0; k < 4; k++) tr_append_u64(t, "", comms[c]->root[k]);
+    for (size_t k = 0; k < P * n; k++) tr_append_ext2(t, "", E2{pts[2 * k], pts[2 * k + 1]});
+    for (int i = 0; i < num_evals; i++) tr_append_ext2(t, "", E2{canon(ev_vals[2 * i]), canon(ev_vals[2 * i + 1])});
+    // 2. weights eq(t, i), t_0 on the top index bit (basefold.rs:3008-3026)
+    int ell = 0;
+    while (((size_t)1 << ell) < E) ell++;
+    if (E <= 1) ell = 1;
+    std::vector<u64> w((size_t)1 << ell, 0);
+    w[0] = 1;
+    for (int i = 0; i < ell; i++) {
+        u64 ti = tr_challenge(t, "");
+        u64 omt = sub(1, ti);
+        for (size_t j = (size_t)1 << i; j-- > 0;) {
+            u64 v = w[j];
+            w[2 * j] = mul(v, omt);
+            w[2 * j + 1] = mul(v, ti);
+        }
+    }
+
+    DevMem m;
+    u64 *d_pts, *g, *eq, *eqA, *eqB, *gA, *gB, *partials, *rec;
+    unsigned* counter;
+    BoTerm* d_terms;
+    int* d_start;
+    RC_TRY(m.alloc(&d_pts, P * n * 16));
+    RC_TRY(m.alloc(&g, P * N * 8));
+    RC_TRY(m.alloc(&eq, P * N * 16));
+    RC_TRY(m.alloc(&eqA, P * N * 8));  // per point N/2 Ext2 (stride N words)
+    RC_TRY(m.alloc(&eqB, P * N * 8));
+    RC_TRY(m.alloc(&gA, P * N * 8));
+    RC_TRY(m.alloc(&gB, P * N * 8));
+    const unsigned gx = (unsigned)std::max<size_t>(1, (red_grid(N / 2) + P - 1) / P);
+    RC_TRY(m.alloc(&partials, (size_t)gx * P * 6 * 8));
+    RC_TRY(m.alloc(&rec, 16 * 8));
+    RC_TRY(m.alloc(&counter, 16));
+    RC_TRY(m.alloc(&d_terms, E * sizeof(BoTerm)));
+    RC_TRY(m.alloc(&d_start, (P + 1) * sizeof(int)));
+    GB_CUDA_TRY(cudaMemsetAsync(counter, 0, 16, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_pts, pts.data(), P * n * 16, cudaMemcpyHostToDevice, s));
+    u64* stage = pinned(64);
+    if (!stage) return GB_ECUDA;
+
+    // 3. g_p = sum over the point's evaluations of w_i evals_i (terms grouped by point)
+    std::vector<BoTerm> terms;
+    std::vector<int> start(P + 1, 0);
+    for (size_t p = 0; p < P; p++) {
+        start[p] = (int)terms.size();
+        for (size_t i = 0; i < E; i++)
+            if ((size_t)ev_point[i] == p) terms.push_back(BoTerm{comms[ev_poly[i]]->d_evals, w[i], 0});
+    }
+    start[P] = (int)terms.size();
+    GB_CUDA_TRY(cudaMemcpyAsync(d_terms, terms.data(), E * sizeof(BoTerm), cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_start, start.data(), (P + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    bo_accum_g_kernel<<<dim3(grid_for(N, 256), (unsigned)P), 256, 0, s>>>(d_terms, d_start, N, g);
+    GB_LAUNCH_CHECK("bo_accum_g_kernel");
+    // 4. eq tables
+    for (size_t p = 0; p < P; p++) RC_TRY(eq_table(d_pts + p * n * 2, n, true, eq + p * N * 2));
+
+    // 5-7. outer sumcheck: n oracles, n challenges r
+    auto read_rec = [&](int words) -> int {
+        GB_CUDA_TRY(cudaMemcpyAsync(stage, rec, (size_t)words * 8, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        return GB_OK;
+    };
+    auto put_oracle = [&](u64* o) {
+        E2 c0{stage[0], stage[1]}, s1{stage[2], stage[3]}, c2{stage[4], stage[5]};
+        E2 c1 = e2sub(e2sub(s1, c0), c2);
+        o[0] = c0.c0;
+        o[1] = c0.c1;
+        o[2] = c1.c0;
+        o[3] = c1.c1;
+        o[4] = c2.c0;
+        o[5] = c2.c1;
+        tr_append_ext2(t, "", c0);
+        tr_append_ext2(t, "", c1);
+        tr_append_ext2(t, "", c2);
+    };
+    std::vector<E2> r(n);
+    bo_round0_kernel<<<dim3(gx, (unsigned)P), RED_THREADS, 0, s>>>(g, eq, N, partials, rec, counter);
+    GB_LAUNCH_CHECK("bo_round0_kernel");
+    RC_TRY(read_rec(6));
+    put_oracle(p_outer);
+    r[0] = tr_challenge_ext2(t, "");
+    {
+        const u64* eq_cur = eq;
+        const u64* g_cur = g;
+        size_t eq_stride = 2 * N, g_stride = N;
+        u64* eq_bufs[2] = {eqA, eqB};
+        u64* g_bufs[2] = {gA, gB};
+        size_t sc = N;
+        for (int rd = 1; rd < n; rd++) {
+            const size_t quarter = sc / 4;
+            const unsigned gq = (unsigned)std::max<size_t>(1, (red_grid(quarter) + P - 1) / P);
+            u64* eo = eq_bufs[rd & 1];
+            u64* go = g_bufs[rd & 1];
+            if (rd == 1)
+                bo_round_kernel<true><<<dim3(gq, (unsigned)P), RED_THREADS, 0, s>>>(
+                    eq_cur, eq_stride, g_cur, g_stride, eo, go, N, quarter, r[rd - 1].c0, r[rd - 1].c1, partials, rec,
+                    counter);
+            else
+                bo_round_kernel<false><<<dim3(gq, (unsigned)P), RED_THREADS, 0, s>>>(
+                    eq_cur, eq_stride, g_cur, g_stride, eo, go, N, quarter, r[rd - 1].c0, r[rd - 1].c1, partials, rec,
+                    counter);
+            GB_LAUNCH_CHECK("bo_round_kernel");
+            RC_TRY(read_rec(6));
+            put_oracle(p_outer + (size_t)rd * 6);
+            r[rd] = tr_challenge_ext2(t, "");
+            eq_cur = eo;
+            g_cur = go;
+            eq_stride = g_stride = N;
+            sc /= 2;
+        }
+    }
+
+    // 8. scalars eq(r, point_i) w_i; combined codeword (+ leaves) and evaluations
+    std::vector<E2> eqr(P);
+    for (size_t p = 0; p < P; p++) {
+        E2 acc{1, 0}, one{1, 0};
+        for (int i = 0; i < n; i++) {
+            E2 pi{pts[(p * n + i) * 2], pts[(p * n + i) * 2 + 1]};
+            E2 term = e2add(e2mul(r[i], pi), e2mul(e2sub(one, r[i]), e2sub(one, pi)));
+            acc = e2mul(acc, term);
+        }
+        eqr[p] = acc;
+    }
+    std::vector<BoTerm> cw_terms(E), ev_terms(E);
+    for (size_t i = 0; i < E; i++) {
+        E2 sc = e2mul(eqr[ev_point[i]], E2{w[i], 0});
+        cw_terms[i] = BoTerm{comms[ev_poly[i]]->d_codeword, sc.c0, sc.c1};
+        ev_terms[i] = BoTerm{comms[ev_poly[i]]->d_evals, sc.c0, sc.c1};
+    }
+    BoTerm *d_cw_terms, *d_ev_terms;
+    u64 *ccw, *ctree, *cev, *ieq;
+    const size_t leaves0 = L / 2;
+    RC_TRY(m.alloc(&d_cw_terms, E * sizeof(BoTerm)));
+    RC_TRY(m.alloc(&d_ev_terms, E * sizeof(BoTerm)));
+    RC_TRY(m.alloc(&ccw, L * 16));
+    RC_TRY(m.alloc(&ctree, (2 * leaves0 - 1) * 32));
+    RC_TRY(m.alloc(&cev, N * 16));
+    RC_TRY(m.alloc(&ieq, N * 16));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_cw_terms, cw_terms.data(), E * sizeof(BoTerm), cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_ev_terms, ev_terms.data(), E * sizeof(BoTerm), cudaMemcpyHostToDevice, s));
+    bo_combine_leaves_kernel<<<grid_for(leaves0, 128), 128, 0, s>>>(d_cw_terms, num_evals, ccw, ctree, leaves0);
+    GB_LAUNCH_CHECK("bo_combine_leaves_kernel");
+    bo_combine_evals_kernel<<<grid_for(N, 256), 256, 0, s>>>(d_ev_terms, num_evals, cev, N);
+    GB_LAUNCH_CHECK("bo_combine_evals_kernel");
+    // 9. combined tree and root
+    RC_TRY(merkle_build_from_leaves(ctree, leaves0, rec + 8));
+    RC_TRY(read_rec(12));
+    for (int k = 0; k < 4; k++) {
+        p_croot[k] = canon(stage[8 + k]);
+        tr_append_u64(t, "", p_croot[k]);
+    }
+    // 10. inner phase at r
+    std::vector<u64> rr(2 * n);
+    for (int i = 0; i < n; i++) {
+        rr[2 * i] = r[i].c0;
+        rr[2 * i + 1] = r[i].c1;
+    }
+    u64* d_r = d_pts;  // the points are no longer needed on the device
+    GB_CUDA_TRY(cudaMemcpyAsync(d_r, rr.data(), (size_t)n * 16, cudaMemcpyHostToDevice, s));
+    RC_TRY(eq_table(d_r, n, true, ieq));
+    OpenRounds in{cev, false, ccw, false, ctree, n, lr};
+    u64* d_leaf = nullptr;
+    RC_TRY(open_rounds(in, tab, ieq, t, num_queries, p_ieval, p_inner, p_roots, p_final, p_cq, m, &d_leaf));
+    // 11. individual queries
+    if (num_queries > 0) {
+        const int depth = n + lr - 1;
+        const size_t indiv = 2 + 4 * (size_t)depth;
+        std::vector<const u64*> ptrs(2 * E);
+        for (size_t i = 0; i < E; i++) {
+            ptrs[i] = comms[ev_poly[i]]->d_codeword;
+            ptrs[E + i] = comms[ev_poly[i]]->d_tree;
+        }
+        const u64** d_ptrs;
+        u64* d_out;
+        RC_TRY(m.alloc(&d_ptrs, 2 * E * sizeof(u64*)));
+        RC_TRY(m.alloc(&d_out, (size_t)num_queries * E * indiv * 8));
+        GB_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), 2 * E * sizeof(u64*), cudaMemcpyHostToDevice, s));
+        bo_indiv_query_kernel<<<(unsigned)(num_queries * E), 64, 0, s>>>(d_ptrs, d_ptrs + E, d_leaf, num_evals, depth,
+                                                                         leaves0, d_out);
+        GB_LAUNCH_CHECK("bo_indiv_query_kernel");
+        GB_CUDA_TRY(cudaMemcpyAsync(p_iq, d_out, (size_t)num_queries * E * indiv * 8, cudaMemcpyDeviceToHost, s));
     }
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     return GB_OK;
@@ -877,6 +1268,20 @@ int gb_basefold_open_ext2(void* commitment, void* table, const uint64_t* h_point
                           uint64_t* h_proof) {
     if (!commitment || !table || !h_point || !t || !h_proof) return GB_EINVAL;
     return open_ext2((BfCommitment*)commitment, (BfTable*)table, h_point, t, num_queries, h_proof);
+}
+
+size_t gb_basefold_batch_proof_len(int num_vars, int log_rate, int num_queries, int num_evals) {
+    if (num_vars < 2 || log_rate < 0 || num_queries < 0 || num_evals < 1) return 0;
+    return batch_proof_len(num_vars, log_rate, num_queries, num_evals);
+}
+
+int gb_basefold_batch_open_ext2(void* const* commitments, int num_commitments, const uint64_t* h_points,
+                                int num_points, const int* eval_poly, const int* eval_point,
+                                const uint64_t* h_eval_values, int num_evals, void* table, gb_transcript* t,
+                                int num_queries, uint64_t* h_proof) {
+    if (!table) return GB_EINVAL;
+    return batch_open_ext2(reinterpret_cast<BfCommitment* const*>(commitments), num_commitments, h_points, num_points,
+                           eval_poly, eval_point, h_eval_values, num_evals, (BfTable*)table, t, num_queries, h_proof);
 }
 
 }  // extern "C"

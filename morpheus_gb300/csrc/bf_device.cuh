@@ -82,6 +82,20 @@ __device__ __forceinline__ void open_round0_item(const u64* __restrict__ bh, con
     acc[5] = gl_add(acc[5], t2.c1);
 }
 
+// Same over Ext2 evaluations (the combined evaluations of a batch opening)
+__device__ __forceinline__ void open_round0_e2_item(const u64* __restrict__ bh, const u64* __restrict__ eq, size_t i,
+                                                    u64 (&acc)[6]) {
+    e2 be = e2_ld(bh + 4 * i), bo = e2_ld(bh + 4 * i + 2);
+    e2 ee = e2_ld(eq + 4 * i), eo = e2_ld(eq + 4 * i + 2);
+    e2 t0 = e2_mul(ee, be), t1 = e2_mul(eo, bo), t2 = e2_mul(e2_sub(eo, ee), e2_sub(bo, be));
+    acc[0] = gl_add(acc[0], t0.c0);
+    acc[1] = gl_add(acc[1], t0.c1);
+    acc[2] = gl_add(acc[2], t1.c0);
+    acc[3] = gl_add(acc[3], t1.c1);
+    acc[4] = gl_add(acc[4], t2.c0);
+    acc[5] = gl_add(acc[5], t2.c1);
+}
+
 // Open round r >= 1, output pair y: fold eq (Ext2) and bh (base when BH_BASE) with ch, store
 // the folded pair of each, add the new pair's oracle terms.
 template <bool BH_BASE>
@@ -144,11 +158,12 @@ __device__ __forceinline__ void fold_leaf_item(const u64* __restrict__ cw, const
 // index, values of every round (initial pair lifted to Ext2, then the folded pairs) and all
 // authentication paths, written canonical into the flat proof layout.
 struct QueryJob {
-    const u64* cw0;           // base codeword
+    const u64* cw0;           // round-0 codeword: base, or Ext2 when cw0_ext2
     const u64* tree0;         // its tree
     const u64* const* fcw;    // folded codewords r = 0..n-2 (device array of pointers)
     const u64* const* ftree;  // their trees
     int n, lr;
+    bool cw0_ext2;
 };
 
 // One query, gathered by the calling block into o (per_query words).
@@ -158,10 +173,14 @@ __device__ __forceinline__ void query_gather_block(const QueryJob& job, size_t l
     u64* paths = vals + (size_t)n * 4;
     if (threadIdx.x == 0) {
         o[0] = leaf;
-        vals[0] = gl_canon(job.cw0[2 * leaf]);
-        vals[1] = 0;
-        vals[2] = gl_canon(job.cw0[2 * leaf + 1]);
-        vals[3] = 0;
+        if (job.cw0_ext2) {
+            for (int k = 0; k < 4; k++) vals[k] = gl_canon(job.cw0[4 * leaf + k]);
+        } else {
+            vals[0] = gl_canon(job.cw0[2 * leaf]);
+            vals[1] = 0;
+            vals[2] = gl_canon(job.cw0[2 * leaf + 1]);
+            vals[3] = 0;
+        }
     }
     for (int r = threadIdx.x; r + 1 < n; r += blockDim.x) {
         size_t pi = leaf >> (r + 1);

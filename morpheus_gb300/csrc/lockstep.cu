@@ -547,7 +547,7 @@ class LsRunner {
             for (int k = 0; k < np; k++) {
                 LsPoly& p = P[k];
                 const u64* const* base = d_ptrs + ptr_off[k];
-                jobs[k] = QueryJob{p.com->d_codeword, p.com->d_tree, base, base + (p.n - 1), p.n, lr};
+                jobs[k] = QueryJob{p.com->d_codeword, p.com->d_tree, base, base + (p.n - 1), p.n, lr, false};
                 outs[k] = d_out + out_off[k];
             }
             GB_CUDA_TRY(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * 8, cudaMemcpyHostToDevice, s));

@@ -35,17 +35,18 @@ __device__ __forceinline__ void block_reduce(u64 (&acc)[W]) {
 
 // Per-block partials to partials[blockIdx.x * W + w]; the last block sums all of
 // them and writes the canonical total to out[w], then re-arms the counter.
+// bid / nblocks: this block's index among the nblocks blocks that share the reduction.
 template <int W>
-__device__ __forceinline__ void grid_reduce_finish(u64 (&acc)[W], u64* __restrict__ partials, u64* __restrict__ out,
-                                                   unsigned* __restrict__ counter) {
+__device__ __forceinline__ void grid_reduce_finish_n(u64 (&acc)[W], u64* __restrict__ partials, u64* __restrict__ out,
+                                                     unsigned* __restrict__ counter, unsigned bid, unsigned nblocks) {
     __shared__ bool s_last;
     block_reduce<W>(acc);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int w = 0; w < W; w++) partials[(size_t)blockIdx.x * W + w] = acc[w];
+        for (int w = 0; w < W; w++) partials[(size_t)bid * W + w] = acc[w];
         __threadfence();
         unsigned t = atomicAdd(counter, 1u);
-        s_last = (t == gridDim.x - 1);
+        s_last = (t == nblocks - 1);
     }
     __syncthreads();
     if (!s_last) return;
@@ -53,7 +54,7 @@ __device__ __forceinline__ void grid_reduce_finish(u64 (&acc)[W], u64* __restric
     u64 tot[W];
 #pragma unroll
     for (int w = 0; w < W; w++) tot[w] = 0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    for (unsigned b = threadIdx.x; b < nblocks; b += blockDim.x) {
 #pragma unroll
         for (int w = 0; w < W; w++) tot[w] = gl_add(tot[w], __ldcg(reinterpret_cast<const unsigned long long*>(partials) + (size_t)b * W + w));
     }
@@ -63,6 +64,11 @@ __device__ __forceinline__ void grid_reduce_finish(u64 (&acc)[W], u64* __restric
         for (int w = 0; w < W; w++) out[w] = gl_canon(tot[w]);
         *counter = 0;
     }
+}
+template <int W>
+__device__ __forceinline__ void grid_reduce_finish(u64 (&acc)[W], u64* __restrict__ partials, u64* __restrict__ out,
+                                                   unsigned* __restrict__ counter) {
+    grid_reduce_finish_n<W>(acc, partials, out, counter, blockIdx.x, gridDim.x);
 }
 
 // Per-block partials only (the reference ABI leaves the final sum to the caller).

@@ -25,6 +25,7 @@ Q_AGL = 0xFFFFFFFEFFFFFFE1
 _u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
 _u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
 _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _c = ctypes
 
 
@@ -80,6 +81,11 @@ def lib():
             ("or_basefold_open_ext2", i32, [_u64p, _u64p, _u64p, _u64p, i32, i32, _u64p, _u64p, _u64p,
                                             vp, i32, _u64p]),
             ("or_basefold_verify_ext2", i32, [_u64p, i32, i32, _u64p, _u64p, i32, _u64p, _u64p, vp]),
+            ("or_basefold_batch_proof_len", sz, [i32, i32, i32, i32]),
+            ("or_basefold_batch_open_ext2", i32, [vp, vp, vp, _u64p, i32, i32, i32, _u64p, i32, _i32p, _i32p, _u64p,
+                                                  i32, _u64p, _u64p, vp, i32, _u64p]),
+            ("or_basefold_batch_verify_ext2", i32, [_u64p, i32, i32, i32, _u64p, i32, _i32p, _i32p, _u64p, i32,
+                                                    _u64p, i32, _u64p, _u64p, vp]),
             ("or_agl_add", u64, [u64, u64]),
             ("or_agl_sub", u64, [u64, u64]),
             ("or_agl_mul", u64, [u64, u64]),
@@ -321,6 +327,45 @@ def basefold_verify_ext2(root, n, log_rate, point, proof, num_queries, table, tr
     ent, off = table
     return bool(lib().or_basefold_verify_ext2(_a(root), n, log_rate, _a(point).reshape(-1), _a(proof),
                                               num_queries, ent.reshape(-1), off, transcript.ptr))
+
+
+def basefold_batch_proof_len(n, log_rate, q, num_evals):
+    return lib().or_basefold_batch_proof_len(n, log_rate, q, num_evals)
+
+
+def _evals_arrays(evals):
+    poly = _a([e[0] for e in evals], np.int32)
+    point = _a([e[1] for e in evals], np.int32)
+    vals = _a([np.asarray(e[2], np.uint64) for e in evals]).reshape(-1)
+    return poly, point, vals
+
+
+def basefold_batch_open_ext2(comms, points, evals, table, transcript, num_queries):
+    """batch_open_ext2: comms are basefold_commit dicts, points a list of n-long Ext2 arrays,
+    evals a list of (poly, point, value) with value an Ext2 pair."""
+    n, lr = comms[0]["num_vars"], comms[0]["log_rate"]
+    ent, off = table
+    keep = [(_a(c["codeword"]), _a(c["bh_evals"]), _a(c["tree"])) for c in comms]
+    ptrs = [(_c.c_void_p * len(comms))(*[k[j].ctypes.data for k in keep]) for j in range(3)]
+    roots = _a([c["root"] for c in comms]).reshape(-1)
+    pts = _a(points).reshape(-1)
+    poly, point, vals = _evals_arrays(evals)
+    proof = np.zeros(basefold_batch_proof_len(n, lr, num_queries, len(evals)), np.uint64)
+    rc = lib().or_basefold_batch_open_ext2(_c.cast(ptrs[0], _c.c_void_p), _c.cast(ptrs[1], _c.c_void_p),
+                                           _c.cast(ptrs[2], _c.c_void_p), roots, len(comms), n, lr, pts, len(points),
+                                           poly, point, vals, len(evals), ent.reshape(-1), off, transcript.ptr,
+                                           num_queries, proof)
+    assert rc == 0
+    return proof
+
+
+def basefold_batch_verify_ext2(roots, n, log_rate, points, evals, proof, num_queries, table, transcript):
+    ent, off = table
+    poly, point, vals = _evals_arrays(evals)
+    roots = _a(roots).reshape(-1)
+    return bool(lib().or_basefold_batch_verify_ext2(roots, roots.size // 4, n, log_rate, _a(points).reshape(-1),
+                                                    len(points), poly, point, vals, len(evals), _a(proof),
+                                                    num_queries, ent.reshape(-1), off, transcript.ptr))
 
 
 def ajtai_ring_elem(key, row, j):

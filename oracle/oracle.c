@@ -902,6 +902,383 @@ int or_basefold_verify_ext2(const u64 root[4], int n, int lr, const u64 *point, 
 }
 
 /* ======================================================================
+ * Batch opening of several committed polynomials at Ext2 points
+ * (batch_open_ext2, goldilocks-cuda-rs/src/basefold.rs:1202-1532; verifier
+ * batch_verify_ext2, :1931-2220).  Flat proof layout:
+ *   outer oracles n x (c0, c1, c2) Ext2 | combined root 4 | inner eval 2 |
+ *   inner oracles n x 6 | folded roots (n-1) x 4 | final codeword 2^lr Ext2 |
+ *   q combined queries (the open_ext2 query layout, Ext2 values in round 0) |
+ *   q x E individual queries: (v0, v1) base + path of depth n+lr-1.
+ * ====================================================================== */
+
+size_t or_basefold_batch_proof_len(int n, int lr, int q, int num_evals) {
+    size_t per_q = 1 + (size_t)n * 4 + path_words_total(n, lr);
+    size_t indiv = 2 + (size_t)(n + lr - 1) * 4;
+    return (size_t)n * 6 + 4 + 2 + (size_t)n * 6 + (size_t)(n - 1) * 4 + ((size_t)2 << lr) + (size_t)q * per_q +
+           (size_t)q * num_evals * indiv;
+}
+
+/* batching weights: eq(t, .) with t_0 on the most significant index bit (basefold.rs:3008-3026);
+ * ell = 1 for a single evaluation, else log2 of the next power of two */
+static int batch_ell(int num_evals) {
+    int ell = 0;
+    while (((size_t)1 << ell) < (size_t)num_evals) ell++;
+    return num_evals <= 1 ? 1 : ell;
+}
+static void batch_weights(or_transcript *t, int num_evals, u64 *w) {
+    int ell = batch_ell(num_evals);
+    size_t sz = (size_t)1 << ell;
+    u64 *res = (u64 *)calloc(sz, 8);
+    res[0] = 1;
+    for (int i = 0; i < ell; i++) {
+        u64 ti = bt_sample(t);
+        u64 omt = gl_sub(1, ti);
+        size_t half = (size_t)1 << i;
+        for (size_t j = half; j-- > 0;) {
+            u64 v = res[j];
+            res[2 * j] = gl_mul(v, omt);
+            res[2 * j + 1] = gl_mul(v, ti);
+        }
+    }
+    for (int i = 0; i < num_evals; i++) w[i] = res[i];
+    free(res);
+}
+
+/* eq(r, pt) = prod_i (r_i pt_i + (1 - r_i)(1 - pt_i))  (basefold.rs:3218-3230) */
+static e2 eq_eval_ext2(const e2 *r, const u64 *pt, int n) {
+    e2 one = e2_base(1), acc = one;
+    for (int i = 0; i < n; i++) {
+        e2 p = e2_mk(pt[2 * i], pt[2 * i + 1]);
+        e2 term = e2_add(e2_mul(r[i], p), e2_mul(e2_sub(one, r[i]), e2_sub(one, p)));
+        acc = e2_mul(acc, term);
+    }
+    return acc;
+}
+
+static void put_oracle(u64 *dst, const e2 o[3], or_transcript *t) {
+    for (int c = 0; c < 3; c++) {
+        put_e2(dst + 2 * c, o[c]);
+        bt_observe_ext2(t, o[c]);
+    }
+}
+
+int or_basefold_batch_open_ext2(const u64 *const *codewords, const u64 *const *bh_evals, const u64 *const *trees,
+                                const u64 *roots, int num_comms, int n, int lr, const u64 *points, int num_points,
+                                const int *ev_poly, const int *ev_point, const u64 *ev_vals, int num_evals,
+                                const u64 *tab, const u64 *lvl_off, or_transcript *t, int num_queries, u64 *proof) {
+    if (n < 2 || num_comms < 1 || num_points < 1 || num_evals < 1) return -1;
+    for (int i = 0; i < num_evals; i++)
+        if (ev_poly[i] < 0 || ev_poly[i] >= num_comms || ev_point[i] < 0 || ev_point[i] >= num_points) return -1;
+    const size_t N = (size_t)1 << n, L = (size_t)1 << (n + lr);
+    u64 *outer = proof;
+    u64 *croot = outer + (size_t)n * 6;
+    u64 *ieval = croot + 4;
+    u64 *inner = ieval + 2;
+    u64 *froots = inner + (size_t)n * 6;
+    u64 *final_cw = froots + (size_t)(n - 1) * 4;
+    u64 *cq = final_cw + ((size_t)2 << lr);
+    const size_t per_q = 1 + (size_t)n * 4 + path_words_total(n, lr);
+    u64 *iq = cq + (size_t)num_queries * per_q;
+
+    /* 1. transcript: every root, every point, every claimed value */
+    for (int c = 0; c < num_comms; c++) bt_observe_hash(t, roots + 4 * c);
+    for (int p = 0; p < num_points; p++)
+        for (int i = 0; i < n; i++) bt_observe_ext2(t, e2_mk(points[((size_t)p * n + i) * 2], points[((size_t)p * n + i) * 2 + 1]));
+    for (int i = 0; i < num_evals; i++) bt_observe_ext2(t, e2_mk(ev_vals[2 * i], ev_vals[2 * i + 1]));
+    /* 2. weights */
+    u64 *w = (u64 *)malloc(8 * (size_t)num_evals);
+    batch_weights(t, num_evals, w);
+    /* 3. g_p = sum over the point's evaluations of w_i * evals (natural order = bit-reversed bh_evals) */
+    e2 *g = (e2 *)malloc(sizeof(e2) * N * num_points);
+    e2 *eq = (e2 *)malloc(sizeof(e2) * N * num_points);
+    for (size_t k = 0; k < N * num_points; k++) g[k] = e2_base(0);
+    for (int i = 0; i < num_evals; i++) {
+        e2 *gp = g + N * ev_point[i];
+        const u64 *bh = bh_evals[ev_poly[i]];
+        for (size_t k = 0; k < N; k++) gp[k] = e2_add(gp[k], e2_base(gl_mul(w[i], bh[bitrev(k, n)])));
+    }
+    /* 4. eq tables of the points */
+    e2 *pt = (e2 *)malloc(sizeof(e2) * n);
+    for (int p = 0; p < num_points; p++) {
+        for (int i = 0; i < n; i++) pt[i] = e2_mk(points[((size_t)p * n + i) * 2], points[((size_t)p * n + i) * 2 + 1]);
+        eq_table_ext2(pt, n, eq + N * p);
+    }
+    /* 5-7. outer sumcheck over sum_p eq_p g_p: n oracles, n challenges */
+    e2 *r = (e2 *)malloc(sizeof(e2) * n);
+    size_t sz = N;
+    for (int rd = 0; rd < n; rd++) {
+        if (rd > 0) {
+            e2 ch = r[rd - 1];
+            size_t half = sz / 2;
+            for (int p = 0; p < num_points; p++) {
+                e2 *gp = g + N * p, *ep = eq + N * p;
+                for (size_t j = 0; j < half; j++) {
+                    gp[j] = e2_add(gp[2 * j], e2_mul(ch, e2_sub(gp[2 * j + 1], gp[2 * j])));
+                    ep[j] = e2_add(ep[2 * j], e2_mul(ch, e2_sub(ep[2 * j + 1], ep[2 * j])));
+                }
+            }
+            sz = half;
+        }
+        e2 tot[3] = {e2_base(0), e2_base(0), e2_base(0)};
+        for (int p = 0; p < num_points; p++) {
+            e2 o[3];
+            oracle_from_pairs(g + N * p, eq + N * p, sz, o);
+            for (int c = 0; c < 3; c++) tot[c] = e2_add(tot[c], o[c]);
+        }
+        put_oracle(outer + (size_t)rd * 6, tot, t);
+        r[rd] = bt_sample_ext2(t);
+    }
+    /* 8. combined codeword and evaluations with scalar_i = eq(r, point_i) w_i */
+    e2 *eqr = (e2 *)malloc(sizeof(e2) * num_points);
+    for (int p = 0; p < num_points; p++) eqr[p] = eq_eval_ext2(r, points + (size_t)p * n * 2, n);
+    e2 *sc = (e2 *)malloc(sizeof(e2) * num_evals);
+    for (int i = 0; i < num_evals; i++) sc[i] = e2_mul(eqr[ev_point[i]], e2_base(w[i]));
+    e2 *ccw = (e2 *)malloc(sizeof(e2) * L);
+    e2 *cbh = (e2 *)malloc(sizeof(e2) * N);
+    for (size_t k = 0; k < L; k++) ccw[k] = e2_base(0);
+    for (size_t k = 0; k < N; k++) cbh[k] = e2_base(0);
+    for (int i = 0; i < num_evals; i++) {
+        const u64 *cw = codewords[ev_poly[i]], *bh = bh_evals[ev_poly[i]];
+        for (size_t k = 0; k < L; k++) ccw[k] = e2_add(ccw[k], e2_scale(sc[i], cw[k]));
+        for (size_t k = 0; k < N; k++) cbh[k] = e2_add(cbh[k], e2_scale(sc[i], bh[bitrev(k, n)]));
+    }
+    /* 9. combined tree */
+    size_t leaves0 = L / 2;
+    u64 *ctree = (u64 *)malloc((2 * leaves0 - 1) * 32);
+    or_merkle_tree_ext2((const u64 *)ccw, leaves0, ctree);
+    memcpy(croot, ctree + tree_root_off(leaves0), 32);
+    bt_observe_hash(t, croot);
+    /* 10. inner phase: open_ext2's rounds on the Ext2 codeword and evaluations at r */
+    e2 *ieq = (e2 *)malloc(sizeof(e2) * N);
+    eq_table_ext2(r, n, ieq);
+    e2 o[3];
+    oracle_from_pairs(cbh, ieq, N, o);
+    e2 iev = e2_add(o[0], e2_add(o[0], e2_add(o[1], o[2])));
+    put_e2(ieval, iev);
+    put_oracle(inner, o, t);
+    e2 **fcw = (e2 **)calloc(n, sizeof(e2 *));
+    u64 **ftree = (u64 **)calloc(n, sizeof(u64 *));
+    sz = N;
+    for (int rd = 0; rd < n; rd++) {
+        e2 ch = bt_sample_ext2(t);
+        if (rd < n - 1) {
+            size_t half = sz / 2;
+            for (size_t j = 0; j < half; j++) {
+                ieq[j] = e2_add(ieq[2 * j], e2_mul(ch, e2_sub(ieq[2 * j + 1], ieq[2 * j])));
+                cbh[j] = e2_add(cbh[2 * j], e2_mul(ch, e2_sub(cbh[2 * j + 1], cbh[2 * j])));
+            }
+            sz = half;
+            oracle_from_pairs(cbh, ieq, sz, o);
+            put_oracle(inner + (size_t)(rd + 1) * 6, o, t);
+        }
+        size_t pairs = L >> (rd + 1);
+        const u64 *lv = tab + 2 * lvl_off[rd];
+        const e2 *in = rd == 0 ? ccw : fcw[rd - 1];
+        e2 *out = (e2 *)malloc(sizeof(e2) * pairs);
+        for (size_t i = 0; i < pairs; i++) out[i] = fold_one(in[2 * i], in[2 * i + 1], lv[2 * i], lv[2 * i + 1], ch);
+        fcw[rd] = out;
+        if (rd < n - 1) {
+            size_t lv_leaves = pairs / 2;
+            ftree[rd] = (u64 *)malloc((2 * lv_leaves - 1) * 32);
+            or_merkle_tree_ext2((const u64 *)out, lv_leaves, ftree[rd]);
+            memcpy(froots + 4 * rd, ftree[rd] + tree_root_off(lv_leaves), 32);
+            bt_observe_hash(t, froots + 4 * rd);
+        }
+    }
+    for (size_t i = 0; i < ((size_t)1 << lr); i++) put_e2(final_cw + 2 * i, fcw[n - 1][i]);
+    /* 11. queries: combined (Ext2) then individual (base) */
+    size_t *leaf_of = (size_t *)malloc(sizeof(size_t) * (num_queries > 0 ? num_queries : 1));
+    for (int q = 0; q < num_queries; q++) {
+        size_t leaf = (size_t)(bt_sample(t) % (u64)leaves0);
+        leaf_of[q] = leaf;
+        u64 *qq = cq + (size_t)q * per_q;
+        qq[0] = leaf;
+        u64 *vals = qq + 1;
+        put_e2(vals, ccw[2 * leaf]);
+        put_e2(vals + 2, ccw[2 * leaf + 1]);
+        size_t idx = leaf / 2;
+        for (int rr = 0; rr + 1 < n; rr++) {
+            put_e2(vals + 4 * (rr + 1), fcw[rr][2 * idx]);
+            put_e2(vals + 4 * (rr + 1) + 2, fcw[rr][2 * idx + 1]);
+            idx /= 2;
+        }
+        u64 *paths = vals + (size_t)n * 4;
+        tree_path(ctree, leaves0, leaf, paths);
+        paths += (size_t)(n + lr - 1) * 4;
+        idx = leaf / 2;
+        for (int rr = 0; rr + 1 < n; rr++) {
+            tree_path(ftree[rr], (L >> (rr + 1)) / 2, idx, paths);
+            paths += (size_t)(n + lr - 2 - rr) * 4;
+            idx /= 2;
+        }
+    }
+    const size_t indiv = 2 + (size_t)(n + lr - 1) * 4;
+    for (int q = 0; q < num_queries; q++) {
+        for (int i = 0; i < num_evals; i++) {
+            u64 *d = iq + ((size_t)q * num_evals + i) * indiv;
+            const u64 *cw = codewords[ev_poly[i]];
+            d[0] = gl_canon(cw[2 * leaf_of[q]]);
+            d[1] = gl_canon(cw[2 * leaf_of[q] + 1]);
+            tree_path(trees[ev_poly[i]], leaves0, leaf_of[q], d + 2);
+        }
+    }
+    for (int rd = 0; rd < n; rd++) {
+        free(fcw[rd]);
+        free(ftree[rd]);
+    }
+    free(fcw);
+    free(ftree);
+    free(leaf_of);
+    free(ieq);
+    free(ctree);
+    free(ccw);
+    free(cbh);
+    free(sc);
+    free(eqr);
+    free(r);
+    free(pt);
+    free(eq);
+    free(g);
+    free(w);
+    return 0;
+}
+
+static e2 oracle_at(const u64 *o, e2 x) {
+    e2 c0 = e2_mk(o[0], o[1]), c1 = e2_mk(o[2], o[3]), c2 = e2_mk(o[4], o[5]);
+    return e2_add(c0, e2_add(e2_mul(c1, x), e2_mul(c2, e2_mul(x, x))));
+}
+static e2 oracle_sum(const u64 *o) {
+    e2 c0 = e2_mk(o[0], o[1]), c1 = e2_mk(o[2], o[3]), c2 = e2_mk(o[4], o[5]);
+    return e2_add(c0, e2_add(c0, e2_add(c1, c2)));
+}
+static void observe_oracle(or_transcript *t, const u64 *o) {
+    for (int c = 0; c < 3; c++) bt_observe_ext2(t, e2_mk(o[2 * c], o[2 * c + 1]));
+}
+
+int or_basefold_batch_verify_ext2(const u64 *roots, int num_comms, int n, int lr, const u64 *points, int num_points,
+                                  const int *ev_poly, const int *ev_point, const u64 *ev_vals, int num_evals,
+                                  const u64 *proof, int num_queries, const u64 *tab, const u64 *lvl_off,
+                                  or_transcript *t) {
+    if (n < 2 || num_comms < 1 || num_points < 1 || num_evals < 1) return 0;
+    for (int i = 0; i < num_evals; i++)
+        if (ev_poly[i] < 0 || ev_poly[i] >= num_comms || ev_point[i] < 0 || ev_point[i] >= num_points) return 0;
+    const size_t L = (size_t)1 << (n + lr);
+    const u64 *outer = proof;
+    const u64 *croot = outer + (size_t)n * 6;
+    const u64 *ieval = croot + 4;
+    const u64 *inner = ieval + 2;
+    const u64 *froots = inner + (size_t)n * 6;
+    const u64 *final_cw = froots + (size_t)(n - 1) * 4;
+    const u64 *cq = final_cw + ((size_t)2 << lr);
+    const size_t per_q = 1 + (size_t)n * 4 + path_words_total(n, lr);
+    const u64 *iq = cq + (size_t)num_queries * per_q;
+    const size_t indiv = 2 + (size_t)(n + lr - 1) * 4;
+    int ok = 1;
+
+    for (int c = 0; c < num_comms; c++) bt_observe_hash(t, roots + 4 * c);
+    for (int p = 0; p < num_points; p++)
+        for (int i = 0; i < n; i++) bt_observe_ext2(t, e2_mk(points[((size_t)p * n + i) * 2], points[((size_t)p * n + i) * 2 + 1]));
+    for (int i = 0; i < num_evals; i++) bt_observe_ext2(t, e2_mk(ev_vals[2 * i], ev_vals[2 * i + 1]));
+    u64 *w = (u64 *)malloc(8 * (size_t)num_evals);
+    batch_weights(t, num_evals, w);
+    e2 claimed = e2_base(0);
+    for (int i = 0; i < num_evals; i++) claimed = e2_add(claimed, e2_scale(e2_mk(ev_vals[2 * i], ev_vals[2 * i + 1]), w[i]));
+    e2 *r = (e2 *)malloc(sizeof(e2) * n);
+    e2 *ich = (e2 *)malloc(sizeof(e2) * n);
+    e2 *sc = (e2 *)malloc(sizeof(e2) * num_evals);
+    /* outer sumcheck */
+    if (!e2_eq(oracle_sum(outer), claimed)) ok = 0;
+    if (ok) {
+        observe_oracle(t, outer);
+        for (int rd = 0; rd + 1 < n && ok; rd++) {
+            r[rd] = bt_sample_ext2(t);
+            if (!e2_eq(oracle_at(outer + (size_t)rd * 6, r[rd]), oracle_sum(outer + (size_t)(rd + 1) * 6))) ok = 0;
+            else observe_oracle(t, outer + (size_t)(rd + 1) * 6);
+        }
+    }
+    if (ok) {
+        r[n - 1] = bt_sample_ext2(t);
+        if (!e2_eq(oracle_at(outer + (size_t)(n - 1) * 6, r[n - 1]), e2_mk(ieval[0], ieval[1]))) ok = 0;
+    }
+    /* inner sumcheck with the folded roots */
+    if (ok) {
+        bt_observe_hash(t, croot);
+        if (!e2_eq(oracle_sum(inner), e2_mk(ieval[0], ieval[1]))) ok = 0;
+    }
+    if (ok) {
+        observe_oracle(t, inner);
+        for (int rd = 0; rd + 1 < n && ok; rd++) {
+            ich[rd] = bt_sample_ext2(t);
+            if (!e2_eq(oracle_at(inner + (size_t)rd * 6, ich[rd]), oracle_sum(inner + (size_t)(rd + 1) * 6))) ok = 0;
+            else {
+                observe_oracle(t, inner + (size_t)(rd + 1) * 6);
+                bt_observe_hash(t, froots + 4 * rd);
+            }
+        }
+    }
+    if (ok) ich[n - 1] = bt_sample_ext2(t);
+    /* queries */
+    if (ok && num_queries > 0) {
+        for (int i = 0; i < num_evals; i++)
+            sc[i] = e2_mul(eq_eval_ext2(r, points + (size_t)ev_point[i] * n * 2, n), e2_base(w[i]));
+        size_t *idx = (size_t *)malloc(sizeof(size_t) * num_queries);
+        for (int q = 0; q < num_queries; q++) idx[q] = (size_t)(bt_sample(t) % (u64)(L / 2));
+        for (int q = 0; q < num_queries && ok; q++) {
+            const u64 *qq = cq + (size_t)q * per_q;
+            size_t leaf = idx[q];
+            if (qq[0] != leaf) {
+                ok = 0;
+                break;
+            }
+            const u64 *vals = qq + 1;
+            const u64 *paths = vals + (size_t)n * 4;
+            u64 lh[4];
+            or_poseidon2_hash_ext2_leaf(vals, vals + 2, lh);
+            if (!verify_path(lh, paths, n + lr - 1, leaf, croot)) {
+                ok = 0;
+                break;
+            }
+            const u64 *pth = paths + (size_t)(n + lr - 1) * 4;
+            size_t fidx = leaf;
+            for (int rd = 0; rd < n && ok; rd++) {
+                e2 v0 = e2_mk(vals[4 * rd], vals[4 * rd + 1]), v1 = e2_mk(vals[4 * rd + 2], vals[4 * rd + 3]);
+                const u64 *ent = tab + 2 * (lvl_off[rd] + fidx);
+                e2 f = e2_add(v0, e2_mul(e2_mul(e2_sub(ich[rd], e2_base(ent[0])), e2_sub(v1, v0)), e2_base(ent[1])));
+                if (rd < n - 1) {
+                    const u64 *nv = vals + 4 * (rd + 1);
+                    e2 exp = (fidx & 1) ? e2_mk(nv[2], nv[3]) : e2_mk(nv[0], nv[1]);
+                    u64 nh[4];
+                    or_poseidon2_hash_ext2_leaf(nv, nv + 2, nh);
+                    int depth = n + lr - 2 - rd;
+                    if (!e2_eq(f, exp) || !verify_path(nh, pth, depth, fidx / 2, froots + 4 * rd)) ok = 0;
+                    pth += (size_t)depth * 4;
+                } else {
+                    const u64 *e = final_cw + ((fidx / 2) * 2 + (fidx & 1)) * 2;
+                    if (!e2_eq(f, e2_mk(e[0], e[1]))) ok = 0;
+                }
+                fidx /= 2;
+            }
+            e2 a0 = e2_base(0), a1 = e2_base(0);
+            for (int i = 0; i < num_evals && ok; i++) {
+                const u64 *d = iq + ((size_t)q * num_evals + i) * indiv;
+                u64 ih[4];
+                or_poseidon2_hash_gl_leaf(d[0], d[1], ih);
+                if (!verify_path(ih, d + 2, n + lr - 1, leaf, roots + 4 * ev_poly[i])) ok = 0;
+                a0 = e2_add(a0, e2_scale(sc[i], d[0]));
+                a1 = e2_add(a1, e2_scale(sc[i], d[1]));
+            }
+            if (ok && (!e2_eq(a0, e2_mk(vals[0], vals[1])) || !e2_eq(a1, e2_mk(vals[2], vals[3])))) ok = 0;
+        }
+        free(idx);
+    }
+    free(sc);
+    free(ich);
+    free(r);
+    free(w);
+    return ok;
+}
+
+/* ======================================================================
  * almost-Goldilocks q = 2^64 - 2^32 - 31, Ext2 = F_q[X]/(X^2 - 3)
  * (cuda_almost_goldilocks/almost_goldilocks.cuh, almost_extension.cuh)
  * ====================================================================== */

@@ -111,6 +111,25 @@ int or_basefold_verify_ext2(const uint64_t root[4], int n, int log_rate, const u
                             const uint64_t *table_entries, const uint64_t *level_offsets,
                             or_transcript *t);
 
+/* batch_open_ext2 (goldilocks-cuda-rs/src/basefold.rs:1202-1532): several committed polynomials
+ * (same num_vars, log_rate) opened at Ext2 points.  Commitment c: codewords[c], bh_evals[c],
+ * trees[c], roots[4c..4c+3]; points: num_points x n Ext2; evaluation i claims poly ev_poly[i] at
+ * point ev_point[i] equals ev_vals[2i..2i+1].  Proof layout: or_basefold_batch_proof_len words
+ * (outer oracles | combined root | inner eval | inner oracles | folded roots | final codeword |
+ * combined queries | individual queries). */
+size_t or_basefold_batch_proof_len(int n, int log_rate, int num_queries, int num_evals);
+int or_basefold_batch_open_ext2(const uint64_t *const *codewords, const uint64_t *const *bh_evals,
+                                const uint64_t *const *trees, const uint64_t *roots, int num_comms, int n,
+                                int log_rate, const uint64_t *points, int num_points, const int *ev_poly,
+                                const int *ev_point, const uint64_t *ev_vals, int num_evals,
+                                const uint64_t *table_entries, const uint64_t *level_offsets, or_transcript *t,
+                                int num_queries, uint64_t *proof);
+/* BasefoldVerifier::batch_verify_ext2 (goldilocks-cuda-rs/src/basefold.rs:1931-2220): 1 accepts. */
+int or_basefold_batch_verify_ext2(const uint64_t *roots, int num_comms, int n, int log_rate, const uint64_t *points,
+                                  int num_points, const int *ev_poly, const int *ev_point, const uint64_t *ev_vals,
+                                  int num_evals, const uint64_t *proof, int num_queries,
+                                  const uint64_t *table_entries, const uint64_t *level_offsets, or_transcript *t);
+
 /* ---- Monolith-12 over Goldilocks (goldilocks-cuda-rs/src/cpu_monolith.rs:13-226) ---- */
 /* The permutation (concrete layer, then 6 rounds of bars, bricks, concrete); canonical in/out. */
 void or_monolith_permute(uint64_t s[12]);

@@ -214,3 +214,36 @@ def test_monolith_oracle_tree_structure():
     parent = O.monolith_permute(np.concatenate([tree[0], tree[1], np.zeros(4, np.uint64)]))[:4]
     assert np.array_equal(tree[4], parent)
     assert tree.shape[0] == 7
+
+
+def _bp_ref_point(a, b, n):
+    return np.array([[((i + 1) * a) % O.P, ((i + 1) * b) % O.P] for i in range(n)], np.uint64)
+
+
+@pytest.mark.parametrize("case", ["single", "same_point", "different_points"])
+def test_batch_open_restatement_on_reference_tests(case):
+    """batch_open_ext2 restated (basefold.rs:1202-1532) on the reference's own tests
+    (basefold.rs:3908-4110): its restated verifier (:1931-2220) accepts, and rejects a wrong
+    claim (the reference's tamper test, :4113-4170) and a flipped proof word."""
+    n, lr, q = 4, 1, 4
+    table = O.basefold_table(n, lr, n, 42)
+    ea, eb = np.arange(1, 17, dtype=np.uint64), np.arange(100, 116, dtype=np.uint64)
+    pa, pb = _bp_ref_point(111, 222, n), _bp_ref_point(333, 444, n)
+    if case == "single":
+        evals, points, pairs = [ea], [pa], [(0, 0)]
+    elif case == "same_point":
+        evals, points, pairs = [ea, eb], [pa], [(0, 0), (1, 0)]
+    else:
+        evals, points, pairs = [ea, eb], [pa, pb], [(0, 0), (1, 1)]
+    comms = [O.basefold_commit(e, lr) for e in evals]
+    claims = [(a, b, O.ml_eval_ext2(evals[a], points[b])) for a, b in pairs]
+    proof = O.basefold_batch_open_ext2(comms, points, claims, table, O.Transcript(b"t"), q)
+    assert proof.size == O.basefold_batch_proof_len(n, lr, q, len(claims))
+    roots = [c["root"] for c in comms]
+    assert O.basefold_batch_verify_ext2(roots, n, lr, points, claims, proof, q, table, O.Transcript(b"t"))
+    bad = [(a, b, np.array([(int(v[0]) + 1) % O.P, int(v[1])], np.uint64)) for a, b, v in claims]
+    assert not O.basefold_batch_verify_ext2(roots, n, lr, points, bad, proof, q, table, O.Transcript(b"t"))
+    for k in (3, proof.size // 2, proof.size - 3):
+        flip = proof.copy()
+        flip[k] ^= np.uint64(1)
+        assert not O.basefold_batch_verify_ext2(roots, n, lr, points, claims, flip, q, table, O.Transcript(b"t"))
