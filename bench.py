@@ -221,6 +221,24 @@ def run_side_workload(args):
         unit, metric, work = "claims/s", "batch_open_ext2 claims/s", float(len(claims))
         cfg = {"workload": f"batch_open_ext2: {npoly} polys x 2^{n}, {npts} points, {len(claims)} claims, "
                            f"rate 1/2, {q} queries", "l2": "flushed between timed steps"}
+    elif args.workload == "peval":
+        from morpheus_gb300 import partial_eval as PE
+        n, m = 26, 14  # einsum A input 2^14 x 2^12, its halves swapped, the 2^14 side summed
+        ranges = [(12, 26), (0, 12)]
+        half = n // 2
+        lo, hi = PE.build_split_luts(n, ranges, half)
+        d_ev = DeviceBuffer.from_numpy(rng.integers(0, P, size=1 << n, dtype=np.uint64))
+        d_lo, d_hi = DeviceBuffer.from_numpy(lo), DeviceBuffer.from_numpy(hi)
+        d_eq, keep = PE.eq_table_ext2_device(rng.integers(0, P, size=(m, 2), dtype=np.uint64))
+        d_out = DeviceBuffer(2 << (n - m))
+
+        def step():
+            Nn.check(L.fused_permute_partial_eval_ffi(d_ev.ptr, d_out.ptr, d_eq.ptr, d_lo.ptr, d_hi.ptr, n, m, half,
+                                                      1 << (n - m), 0), "fused")
+        unit, metric = "GB/s", "fused permute + partial eval GB/s"
+        work = ((1 << n) * 8 + (1 << m) * 16 + (2 << (n - m)) * 8) / 1e9
+        cfg = {"workload": f"fused_permute_partial_eval: 2^{n} evaluations (2^14 x 2^12 einsum input, halves "
+                           f"swapped), {m} variables fixed at Ext2 challenges", "l2": "flushed between timed steps"}
     elif args.workload == "fold":
         nf = 24
         src_buf = DeviceBuffer.from_numpy(rng.integers(0, P, size=2 * 2 * (1 << nf), dtype=np.uint64))
@@ -258,7 +276,17 @@ def run_side_workload(args):
             "data": "synthetic", "config": cfg, "step_ms_all": [round(t, 4) for t in times]}
     if args.workload == "batch_open":
         line["cpu_baseline"] = batch_open_cpu_sample(len(claims))
-    if args.workload == "fold":
+    if args.workload == "peval":
+        # the unfused path on the same evaluations (no permutation): partial_eval_ext2_from_gl
+        d_r = DeviceBuffer.from_numpy(rng.integers(0, P, size=2 * m, dtype=np.uint64))
+        d_half = DeviceBuffer(2 << (n - 1))
+        pe = lambda: Nn.check(L.partial_eval_ext2_from_gl_ffi(d_ev.ptr, d_half.ptr, d_r.ptr, n, m), "peval")
+        pe()
+        pe_ms = min(ev_time(pe) for _ in range(5))
+        pe_bytes = (1 << n) * 8 + (2 << (n - 4)) * 8 * 2  # first pass reads 2^n, writes 2^(n-4) Ext2
+        line["partial_eval_ext2"] = {"ms": pe_ms, "GB_s": pe_bytes / (pe_ms * 1e-3) / 1e9,
+                                     "workload": f"partial_eval_ext2_from_gl_ffi, 2^{n} evaluations, {m} variables"}
+    if args.workload in ("fold", "peval"):
         peak, src = measured_peaks()
         line["roofline"] = {"bound": "hbm", "achieved": line["value"], "peak": peak, "unit": "GB/s",
                             "frac": line["value"] / peak, "peak_source": src}
@@ -498,10 +526,11 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="served workload: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")
     ap.add_argument("--hbm-budget-gb", type=int, default=96, help="served workload: admission budget")
-    ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "batch_open", "ajtai", "batched", "served"],
+    ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "batch_open", "peval", "ajtai", "batched", "served"],
                     help="basefold (headline): commit+open proofs; sumcheck: 2 x 2^20 product sumcheck; "
                          "fold: one fused fold round over 2 x 2^24 Ext2; "
                          "batch_open: 8 polys x 2^20 opened at 2 points; "
+                         "peval: fused permute + partial eval of 2^26 evaluations; "
                          "ajtai: 256 witnesses x 16 rows x 2^16 coefficients")
     args = ap.parse_args()
     if args.impl == "reference":

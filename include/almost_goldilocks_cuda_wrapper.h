@@ -137,6 +137,17 @@ int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses,
 int ajtai_commit_wide_noalloc_ffi(const uint32_t *d_key, const uint64_t *d_z_wide, uint64_t N, uint64_t col_offset,
                                   int chunk, uint64_t *d_out);
 
+/* ---- Partial evaluation and bit permutation over q (almost-goldilocks-cuda-rs/src/ffi.rs:113-119,
+ * :198-226; wrapper.cu:713-805, :1061-1085).  Same arguments and results as the Goldilocks forms
+ * (goldilocks_cuda_wrapper.h), over q = 2^64 - 2^32 - 31 and its Ext2 (X^2 - 3). ---- */
+int agl_partial_eval_ffi(uint64_t *d_data, const uint64_t *d_r, int log_n, int m);
+int agl_partial_eval_ext2_from_base_ffi(const uint64_t *d_input, uint64_t *d_output, const uint64_t *d_r, int log_n,
+                                        int m);
+int agl_bit_permute_ffi(const uint64_t *d_input, uint64_t *d_output, const int *d_perm_map, int n_bits, int total);
+int agl_fused_permute_partial_eval_ffi(const uint64_t *d_evals, uint64_t *d_output, const uint64_t *d_eq_table,
+                                       const uint32_t *d_lo_lut, const uint32_t *d_hi_lut, int n, int m, int half,
+                                       int output_size, int smem_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -364,6 +364,29 @@ int gb_prove_matmul(void *table, void *ajtai_key, const uint64_t master_seed[2],
 int gb_prover_set_ajtai_key(void *prover, void *ajtai_key);
 int gb_prover_submit_matmul(void *prover, const gb_matmul_job *job, uint64_t *ticket); /* non-blocking */
 
+/* ===================== Part 1 (continued): reference ABI =====================
+ * Partial evaluation and bit permutation (the einsum input preparation). */
+/* partial_eval_gl_ffi (ffi.rs:377-382, wrapper.cu:1166-1184): fix the low m of log_n variables of
+ * d_data (2^log_n base values) at the m base values d_r, LSB first; the 2^(log_n-m) results replace
+ * the front of d_data (canonical).  m <= 0 does nothing.  Scratch comes from the stream's pool. */
+int partial_eval_gl_ffi(uint64_t *d_data, const uint64_t *d_r, int log_n, int m);
+/* partial_eval_ext2_from_gl_ffi (ffi.rs:384-390, wrapper.cu:1186-1210): the same at m Ext2 values
+ * d_r; d_output (room for 2^(log_n-1) Ext2) receives the 2^(log_n-m) Ext2 results at its front. */
+int partial_eval_ext2_from_gl_ffi(const uint64_t *d_input, uint64_t *d_output, const uint64_t *d_r, int log_n, int m);
+/* bit_permute_gl_ffi (ffi.rs:644-650, wrapper.cu:1824-1851): d_output[new] = d_input[old] with old
+ * bit d_perm_map[k] taken from new bit k (the inverse permutation, as field.rs:195-224 passes it);
+ * total = 2^n_bits.  Returns -2 for a map that is not a permutation.  Synchronising (the map is
+ * read on the host to plan the tiles). */
+int bit_permute_gl_ffi(const uint64_t *d_input, uint64_t *d_output, const int *d_perm_map, int n_bits, int total);
+/* fused_permute_partial_eval_ffi (ffi.rs:657-668, wrapper.cu:1857-1885, fused_permute_peval.cuh):
+ * d_output[j] = sum_{b < 2^m} d_evals[lo_lut[i & (2^half - 1)] | hi_lut[i >> half]] * d_eq_table[b],
+ * i = j 2^m + b, for j < output_size <= 2^(n-m); d_eq_table holds 2^m Ext2 values, d_output
+ * output_size Ext2 (canonical).  smem_bytes is accepted and unused (the LUTs are read through the
+ * cache).  Asynchronous like the reference. */
+int fused_permute_partial_eval_ffi(const uint64_t *d_evals, uint64_t *d_output, const uint64_t *d_eq_table,
+                                   const uint32_t *d_lo_lut, const uint32_t *d_hi_lut, int n, int m, int half,
+                                   int output_size, int smem_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -171,6 +171,14 @@ SIGNATURES = {
     "aext2_eq_dp_all_batched_ffi": (i32, [vp, vp, vp, i32, i32, sz, ctypes.POINTER(vp), vp]),
     "ajtai_commit_wide_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
     "ajtai_commit_wide_noalloc_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
+    "partial_eval_gl_ffi": (i32, [vp, vp, i32, i32]),
+    "partial_eval_ext2_from_gl_ffi": (i32, [vp, vp, vp, i32, i32]),
+    "bit_permute_gl_ffi": (i32, [vp, vp, vp, i32, i32]),
+    "fused_permute_partial_eval_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32, i32, i32, i32]),
+    "agl_partial_eval_ffi": (i32, [vp, vp, i32, i32]),
+    "agl_partial_eval_ext2_from_base_ffi": (i32, [vp, vp, vp, i32, i32]),
+    "agl_bit_permute_ffi": (i32, [vp, vp, vp, i32, i32]),
+    "agl_fused_permute_partial_eval_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32, i32, i32, i32]),
     "ajtai_commit_dense_batched_ffi": (i32, [vp, vp, u64, i32, i32, vp]),
     "ajtai_commit_dense_batched_at_ffi": (i32, [vp, vp, u64, i32, i32, u64, vp]),
     "ajtai_commit_ternary_ffi": (i32, [vp, vp, vp, u64, i32, vp]),

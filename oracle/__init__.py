@@ -86,6 +86,10 @@ def lib():
                                                   i32, _u64p, _u64p, vp, i32, _u64p]),
             ("or_basefold_batch_verify_ext2", i32, [_u64p, i32, i32, i32, _u64p, i32, _i32p, _i32p, _u64p, i32,
                                                     _u64p, i32, _u64p, _u64p, vp]),
+            ("or_partial_eval_base", None, [i32, _u64p, i32, _u64p, i32, _u64p]),
+            ("or_partial_eval_ext2", None, [i32, _u64p, i32, _u64p, i32, _u64p]),
+            ("or_bit_permute", None, [_u64p, _u64p, _i32p, i32]),
+            ("or_fused_permute_peval", None, [i32, _u64p, i32, i32, i32, _u64p, _u32p, _u32p, _u64p]),
             ("or_agl_add", u64, [u64, u64]),
             ("or_agl_sub", u64, [u64, u64]),
             ("or_agl_mul", u64, [u64, u64]),
@@ -366,6 +370,41 @@ def basefold_batch_verify_ext2(roots, n, log_rate, points, evals, proof, num_que
     return bool(lib().or_basefold_batch_verify_ext2(roots, roots.size // 4, n, log_rate, _a(points).reshape(-1),
                                                     len(points), poly, point, vals, len(evals), _a(proof),
                                                     num_queries, ent.reshape(-1), off, transcript.ptr))
+
+
+_FIELD = {"gl": 0, "agl": 1}
+
+
+def partial_eval_base(evals, r, field="gl"):
+    evals = _a(evals)
+    log_n = evals.size.bit_length() - 1
+    r = _a(r).reshape(-1)
+    out = np.zeros(1 << (log_n - r.size), np.uint64)
+    lib().or_partial_eval_base(_FIELD[field], evals, log_n, r if r.size else np.zeros(1, np.uint64), r.size, out)
+    return out
+
+
+def partial_eval_ext2(evals, r, field="gl"):
+    evals = _a(evals)
+    log_n = evals.size.bit_length() - 1
+    r = _a(r).reshape(-1, 2)
+    out = np.zeros((1 << (log_n - r.shape[0]), 2), np.uint64)
+    lib().or_partial_eval_ext2(_FIELD[field], evals, log_n, r.reshape(-1), r.shape[0], out.reshape(-1))
+    return out
+
+
+def bit_permute(x, inv):
+    x = _a(x)
+    out = np.zeros_like(x)
+    lib().or_bit_permute(x, out, _a(inv, np.int32), len(inv))
+    return out
+
+
+def fused_permute_peval(evals, n, m, half, eq, lo, hi, field="gl"):
+    out = np.zeros((1 << (n - m), 2), np.uint64)
+    lib().or_fused_permute_peval(_FIELD[field], _a(evals), n, m, half, _a(eq).reshape(-1), _a(lo, np.uint32),
+                                 _a(hi, np.uint32), out.reshape(-1))
+    return out
 
 
 def ajtai_ring_elem(key, row, j):

@@ -1300,6 +1300,101 @@ void or_aext2_mul(const u64 a[2], const u64 b[2], u64 out[2]) {
 }
 
 /* ======================================================================
+ * Partial evaluation, bit permutation, fused permute + partial evaluation
+ * (cuda/partial_eval.cuh, goldilocks-cuda-rs/src/partial_eval.rs:406-520 CPU helpers;
+ * cuda/fused_permute_peval.cuh; wrapper.cu:1824-1841; almost-goldilocks forms
+ * cuda_almost_goldilocks/almost_partial_eval.cuh, almost_fused_permute_peval.cuh).
+ * field 0: Goldilocks (Ext2 X^2 - 7), 1: almost-Goldilocks (Ext2 X^2 - 3).
+ * ====================================================================== */
+typedef struct { u64 c0, c1; } fe2;
+static u64 f_add(int f, u64 a, u64 b) { return f ? agl_add(a, b) : gl_add(gl_canon(a), gl_canon(b)); }
+static u64 f_sub(int f, u64 a, u64 b) { return f ? agl_sub(a, b) : gl_sub(gl_canon(a), gl_canon(b)); }
+static u64 f_mul(int f, u64 a, u64 b) { return f ? agl_mul(a, b) : gl_mul(a, b); }
+static u64 f_canon(int f, u64 a) { return f ? agl_canon(a) : gl_canon(a); }
+static fe2 fe2_mul(int f, fe2 a, fe2 b) {
+    fe2 r;
+    u64 w = f ? 3 : 7;
+    r.c0 = f_add(f, f_mul(f, a.c0, b.c0), f_mul(f, w, f_mul(f, a.c1, b.c1)));
+    r.c1 = f_add(f, f_mul(f, a.c0, b.c1), f_mul(f, a.c1, b.c0));
+    return r;
+}
+
+/* fix the low m variables at base r: out[j] = in[2j] + r_i (in[2j+1] - in[2j]) per level */
+void or_partial_eval_base(int field, const u64 *evals, int log_n, const u64 *r, int m, u64 *out) {
+    size_t sz = (size_t)1 << log_n;
+    u64 *d = (u64 *)malloc(sz * 8);
+    for (size_t k = 0; k < sz; k++) d[k] = f_canon(field, evals[k]);
+    for (int i = 0; i < m; i++) {
+        size_t half = sz / 2;
+        for (size_t j = 0; j < half; j++)
+            d[j] = f_add(field, d[2 * j], f_mul(field, r[i], f_sub(field, d[2 * j + 1], d[2 * j])));
+        sz = half;
+    }
+    for (size_t k = 0; k < sz; k++) out[k] = f_canon(field, d[k]);
+    free(d);
+}
+
+/* the same at Ext2 r (m >= 1): the first level mixed, then Ext2 levels; out: 2^(log_n-m) Ext2 */
+void or_partial_eval_ext2(int field, const u64 *evals, int log_n, const u64 *r, int m, u64 *out) {
+    size_t sz = (size_t)1 << log_n;
+    fe2 *d = (fe2 *)malloc(sizeof(fe2) * (sz / 2 + 1));
+    size_t half = sz / 2;
+    for (size_t j = 0; j < half; j++) {
+        u64 a = f_canon(field, evals[2 * j]), b = f_canon(field, evals[2 * j + 1]);
+        u64 diff = f_sub(field, b, a);
+        d[j].c0 = f_add(field, a, f_mul(field, r[0], diff));
+        d[j].c1 = f_mul(field, r[1], diff);
+    }
+    sz = half;
+    for (int i = 1; i < m; i++) {
+        fe2 ri = {r[2 * i], r[2 * i + 1]};
+        half = sz / 2;
+        for (size_t j = 0; j < half; j++) {
+            fe2 a = d[2 * j], b = d[2 * j + 1];
+            fe2 diff = {f_sub(field, b.c0, a.c0), f_sub(field, b.c1, a.c1)};
+            fe2 t = fe2_mul(field, ri, diff);
+            d[j].c0 = f_add(field, a.c0, t.c0);
+            d[j].c1 = f_add(field, a.c1, t.c1);
+        }
+        sz = half;
+    }
+    for (size_t k = 0; k < sz; k++) {
+        out[2 * k] = f_canon(field, d[k].c0);
+        out[2 * k + 1] = f_canon(field, d[k].c1);
+    }
+    free(d);
+}
+
+/* out[new] = in[old], old bit inv[k] <- new bit k  (wrapper.cu:1824-1841) */
+void or_bit_permute(const u64 *in, u64 *out, const int *inv, int n_bits) {
+    size_t total = (size_t)1 << n_bits;
+    for (size_t nw = 0; nw < total; nw++) {
+        size_t old = 0;
+        for (int k = 0; k < n_bits; k++)
+            if ((nw >> k) & 1) old |= (size_t)1 << inv[k];
+        out[nw] = in[old];
+    }
+}
+
+/* out[j] = sum_{b < 2^m} evals[lo[i & (2^half-1)] | hi[i >> half]] eq[b], i = j 2^m + b
+ * (fused_permute_peval.cuh), for j < 2^(n-m) */
+void or_fused_permute_peval(int field, const u64 *evals, int n, int m, int half, const u64 *eq, const uint32_t *lo,
+                            const uint32_t *hi, u64 *out) {
+    size_t outs = (size_t)1 << (n - m), inner = (size_t)1 << m, lo_mask = ((size_t)1 << half) - 1;
+    for (size_t j = 0; j < outs; j++) {
+        u64 a0 = 0, a1 = 0;
+        for (size_t b = 0; b < inner; b++) {
+            size_t i = (j << m) + b;
+            u64 v = f_canon(field, evals[lo[i & lo_mask] | hi[i >> half]]);
+            a0 = f_add(field, a0, f_mul(field, v, eq[2 * b]));
+            a1 = f_add(field, a1, f_mul(field, v, eq[2 * b + 1]));
+        }
+        out[2 * j] = f_canon(field, a0);
+        out[2 * j + 1] = f_canon(field, a1);
+    }
+}
+
+/* ======================================================================
  * Ajtai: ChaCha8 matrix PRG (cuda_almost_goldilocks/ajtai_chacha8.cuh:60-178)
  * and the wide commitment (ajtai.cuh:216-275, ajtai_cpu_reference.cuh:57-186)
  * ====================================================================== */

@@ -145,6 +145,17 @@ uint64_t or_agl_sub(uint64_t a, uint64_t b);
 uint64_t or_agl_mul(uint64_t a, uint64_t b);
 void or_aext2_mul(const uint64_t a[2], const uint64_t b[2], uint64_t out[2]);
 
+/* ---- partial evaluation / bit permutation (field 0: Goldilocks, 1: almost-Goldilocks) ---- */
+/* cuda/partial_eval.cuh (goldilocks-cuda-rs/src/partial_eval.rs:449-520 CPU helpers):
+ * fix the low m variables, LSB first; canonical outputs. */
+void or_partial_eval_base(int field, const uint64_t *evals, int log_n, const uint64_t *r, int m, uint64_t *out);
+void or_partial_eval_ext2(int field, const uint64_t *evals, int log_n, const uint64_t *r, int m, uint64_t *out);
+/* wrapper.cu:1824-1841: out[new] = in[old], old bit inv[k] <- new bit k. */
+void or_bit_permute(const uint64_t *in, uint64_t *out, const int *inv, int n_bits);
+/* cuda/fused_permute_peval.cuh: out[j] = sum_b evals[lo[i & mask] | hi[i >> half]] eq[b], i = j 2^m + b. */
+void or_fused_permute_peval(int field, const uint64_t *evals, int n, int m, int half, const uint64_t *eq,
+                            const uint32_t *lo, const uint32_t *hi, uint64_t *out);
+
 /* ---- Ajtai commitment ---- */
 void or_chacha8_block(const uint32_t key[8], uint32_t counter, const uint32_t nonce[3], uint32_t out[16]);
 void or_ajtai_ring_elem(const uint32_t key[8], uint32_t row, uint64_t j, uint64_t out[64]);

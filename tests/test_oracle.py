@@ -247,3 +247,49 @@ def test_batch_open_restatement_on_reference_tests(case):
         flip = proof.copy()
         flip[k] ^= np.uint64(1)
         assert not O.basefold_batch_verify_ext2(roots, n, lr, points, claims, flip, q, table, O.Transcript(b"t"))
+
+
+def test_partial_eval_restatement_reference_cases():
+    """The oracle's partial evaluation against the reference's CPU helpers restated in Python
+    (goldilocks-cuda-rs/src/partial_eval.rs:449-520) on its own test inputs, and the reference's
+    edge cases (:650-720)."""
+    P = O.P
+    for log_n in (4, 8):
+        ev = [((i + 1) * 0xDEADBEEFCAFEBABE % 2**64) % P for i in range(1 << log_n)]
+        for m in (1, log_n // 2, log_n):
+            r = [((i + 1) * 12345678901234567 % 2**64) % P for i in range(m)]
+            rc = [((i + 1) * 98765432109876543 % 2**64) % P for i in range(m)]
+            d = list(ev)
+            for ri in r:
+                d = [(d[2 * j] + ri * (d[2 * j + 1] - d[2 * j])) % P for j in range(len(d) // 2)]
+            assert O.partial_eval_base(np.array(ev, np.uint64), np.array(r, np.uint64)).tolist() == d
+            e = [((ev[2 * j] + r[0] * (ev[2 * j + 1] - ev[2 * j])) % P, rc[0] * (ev[2 * j + 1] - ev[2 * j]) % P)
+                 for j in range(len(ev) // 2)]
+            for a, b in zip(r[1:], rc[1:]):
+                nxt = []
+                for j in range(len(e) // 2):
+                    x, y = e[2 * j], e[2 * j + 1]
+                    d0, d1 = (y[0] - x[0]) % P, (y[1] - x[1]) % P
+                    nxt.append(((x[0] + a * d0 + 7 * b * d1) % P, (x[1] + a * d1 + b * d0) % P))
+                e = nxt
+            got = O.partial_eval_ext2(np.array(ev, np.uint64), np.array(list(zip(r, rc)), np.uint64))
+            assert [tuple(int(v) for v in row) for row in got] == e
+    ev = np.array([1, 2, 3, 4], np.uint64)
+    assert O.partial_eval_base(ev, [0, 0]).tolist() == [1] and O.partial_eval_base(ev, [1, 1]).tolist() == [4]
+    assert O.partial_eval_ext2(ev, [[7, 0]])[:, 0].tolist() == O.partial_eval_base(ev, [7]).tolist()
+
+
+def test_fused_restatement_is_permute_then_partial_eval():
+    rng = np.random.default_rng(5)
+    n, m, half = 9, 4, 4
+    ev = rng.integers(0, O.P, size=1 << n, dtype=np.uint64)
+    ch = rng.integers(0, O.P, size=(m, 2), dtype=np.uint64)
+    perm = list(rng.permutation(n))
+    inv = [0] * n
+    for old, new in enumerate(perm):
+        inv[new] = old
+    lo = np.array([sum(1 << inv[k] for k in range(half) if (x >> k) & 1) for x in range(1 << half)], np.uint32)
+    hi = np.array([sum(1 << inv[half + k] for k in range(n - half) if (x >> k) & 1) for x in range(1 << (n - half))],
+                  np.uint32)
+    got = O.fused_permute_peval(ev, n, m, half, O.eq_table_ext2(ch), lo, hi)
+    assert np.array_equal(got, O.partial_eval_ext2(O.bit_permute(ev, inv), ch))
