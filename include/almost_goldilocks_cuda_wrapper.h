@@ -44,10 +44,50 @@ int ajtai_commit_dense_batched_ffi(const uint32_t *d_key, const uint64_t *d_z, u
                                    uint64_t *d_out);
 int ajtai_commit_dense_batched_at_ffi(const uint32_t *d_key, const uint64_t *d_z, uint64_t N, int B, int chunk,
                                       uint64_t col_offset, uint64_t *d_out);
-/* Ternary witness (almost wrapper.cu:1642-1660): coefficient l of ring element j is
- * bit l of d_pos[j] minus bit l of d_neg[j]; d_out [KAPPA][64].  Synchronising. */
+/* Ternary witnesses of a split (commit_ternary_kernel, ajtai.cuh:1262-1370; almost
+ * wrapper.cu:1642-1660): 13 witnesses, coefficient l of ring element j of witness i is bit l of
+ * d_pos[i N_ring + j] minus bit l of d_neg[i N_ring + j]; d_out [13][KAPPA][64].  Synchronising. */
 int ajtai_commit_ternary_ffi(const uint32_t *d_key, const uint64_t *d_pos, const uint64_t *d_neg, uint64_t N_ring,
                              int chunk, uint64_t *d_out);
+/* ajtai_materialize_m_ffi (ajtai_premat.cuh:35-85, almost wrapper.cu:1662-1670): d_M[j][i][0..63] =
+ * M_{i,j} for j < N, i < KAPPA (7680 N bytes).  ajtai_commit_ternary_premat_ffi: the ternary commit
+ * reading that matrix instead of generating it (same result as ajtai_commit_ternary_ffi).
+ * The commit is synchronising. */
+int ajtai_materialize_m_ffi(const uint32_t *d_chacha_key, uint64_t *d_M, uint64_t N);
+int ajtai_commit_ternary_premat_ffi(const uint64_t *d_M, const uint64_t *d_pos, const uint64_t *d_neg, uint64_t N_ring,
+                                    int chunk, uint64_t *d_out);
+
+/* ---- Fold tree (ajtai.cuh:700-1260; almost wrapper.cu:1468-1620, :1717-1740).  r: 64 int8
+ * challenge coefficients; r . z is the product in R_q = F_q[X]/(X^64 + 1).  Witnesses are u64
+ * bitmasks per ring element ([instance][N_ring]); ternary ones are (pos, neg) pairs. ---- */
+/* out[j] = z1[j] + r . z2[j], canonical F_q [N_ring][64]; r_coeffs on the host; chunk as the
+ * other commits (-3 otherwise). */
+int ajtai_fold_witness_ffi(const uint64_t *d_z1, const uint64_t *d_z2, const int8_t *r_coeffs, uint64_t N_ring,
+                           int chunk, uint64_t *d_out);
+/* out[j] = sum_i r_i . z_i[j] as int16 [N_ring][64] (the int32 sum cast to int16); d_r_all
+ * [num_instances][64] on the device.  chunk_size only has to be nonzero. */
+int ajtai_multifold_witness_ffi(const uint64_t *d_z_packed, const int8_t *d_r_all, int16_t *d_out, int num_instances,
+                                uint64_t N_ring, uint64_t chunk_size);
+/* binary instances then ternary ones: r_all [(num_binary + num_ternary)][64] */
+int ajtai_multifold_mixed_witness_ffi(const uint64_t *d_z_bin_packed, const uint64_t *d_pos_packed,
+                                      const uint64_t *d_neg_packed, const int8_t *d_r_all, int16_t *d_out,
+                                      int num_binary, int num_ternary, uint64_t N_ring, uint64_t chunk_size);
+/* The reference's tensor-core forms of the mixed fold (same result); here all three run the
+ * plane-popcount kernel. */
+int ajtai_multifold_mixed_witness_tc_ffi(const uint64_t *d_z_bin_packed, const uint64_t *d_pos_packed,
+                                         const uint64_t *d_neg_packed, const int8_t *d_r_all, int16_t *d_out,
+                                         int num_binary, int num_ternary, uint64_t N_ring);
+int ajtai_multifold_mixed_witness_tc_fused_ffi(const uint64_t *d_z_bin_packed, const uint64_t *d_pos_packed,
+                                               const uint64_t *d_neg_packed, const int8_t *d_r_all, int16_t *d_out,
+                                               int num_binary, int num_ternary, uint64_t N_ring);
+/* int16 witness [N_ring][64] -> 13 ternary chunks: v = sum_i 2^i (pos_i - neg_i), bits of |v|
+ * routed by sign; d_pos_chunks / d_neg_chunks [13][N_ring]. */
+int ajtai_split_witness_ffi(const int16_t *d_z_wide, uint64_t *d_pos_chunks, uint64_t *d_neg_chunks, uint64_t N_ring);
+/* c = sum_i r_i . c_i over [KAPPA][64] rows (d_c_packed [num_instances][KAPPA][64], d_r_all on
+ * the device); fold: c1 + r . c2 with r_coeffs on the host.  Canonical outputs. */
+int ajtai_multifold_commitment_ffi(const uint64_t *d_c_packed, const int8_t *d_r_all, int num_instances,
+                                   uint64_t *d_out);
+int ajtai_fold_commitment_ffi(const uint64_t *d_c1, const uint64_t *d_c2, const int8_t *r_coeffs, uint64_t *d_out);
 /* Sparse binary witness (commit_sparse_partial_kernel, ajtai.cuh:382-440; almost wrapper.cu:1741-1756):
  * d_positions holds K coefficient indices 64 j + l with value 1 (a repeated index counts once
  * per occurrence); d_out [KAPPA][64].  Synchronising. */

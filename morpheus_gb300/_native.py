@@ -171,6 +171,16 @@ SIGNATURES = {
     "aext2_eq_dp_all_batched_ffi": (i32, [vp, vp, vp, i32, i32, sz, ctypes.POINTER(vp), vp]),
     "ajtai_commit_wide_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
     "ajtai_commit_wide_noalloc_ffi": (i32, [vp, vp, u64, u64, i32, vp]),
+    "ajtai_materialize_m_ffi": (i32, [vp, vp, u64]),
+    "ajtai_commit_ternary_premat_ffi": (i32, [vp, vp, vp, u64, i32, vp]),
+    "ajtai_fold_witness_ffi": (i32, [vp, vp, vp, u64, i32, vp]),
+    "ajtai_multifold_witness_ffi": (i32, [vp, vp, vp, i32, u64, u64]),
+    "ajtai_multifold_mixed_witness_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32, u64, u64]),
+    "ajtai_multifold_mixed_witness_tc_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32, u64]),
+    "ajtai_multifold_mixed_witness_tc_fused_ffi": (i32, [vp, vp, vp, vp, vp, i32, i32, u64]),
+    "ajtai_split_witness_ffi": (i32, [vp, vp, vp, u64]),
+    "ajtai_multifold_commitment_ffi": (i32, [vp, vp, i32, vp]),
+    "ajtai_fold_commitment_ffi": (i32, [vp, vp, vp, vp]),
     "partial_eval_gl_ffi": (i32, [vp, vp, i32, i32]),
     "partial_eval_ext2_from_gl_ffi": (i32, [vp, vp, vp, i32, i32]),
     "bit_permute_gl_ffi": (i32, [vp, vp, vp, i32, i32]),

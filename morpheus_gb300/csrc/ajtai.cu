@@ -35,6 +35,7 @@ namespace gb {
 
 constexpr int AJ_D = 64;
 constexpr int AJ_KAPPA = 42;
+constexpr int AJ_SPLIT_K = 13;  // ternary chunks of a split witness (ajtai.cuh:1185)
 constexpr u64 AJ_HALF_Q = AGL_Q / 2;  // centred representatives: m > q/2 maps to m - q
 
 // ---------------------------------------------------------------------------
@@ -582,17 +583,20 @@ __device__ __forceinline__ void wide_fill_rows(const u32* ksh, int tile, u64 j, 
     }
 }
 
-// pos/neg: [B][N] bitmasks (neg may be null); partial [chunk][B][KAPPA][D]
+// pos/neg: [B][N] bitmasks (neg may be null); partial [chunk][B][KAPPA][D].  With Mg (a
+// materialized matrix [N][KAPPA][64], ajtai_materialize_m_ffi) the rows are read from it
+// instead of being generated.
 __global__ void __launch_bounds__(WIDE_ROWS * AJ_D) ajtai_bits_kernel(const u32* __restrict__ key,
                                                                     const u64* __restrict__ pos,
                                                                     const u64* __restrict__ neg, u64 N, int B,
-                                                                    u64 col_offset, u64* __restrict__ partial) {
+                                                                    u64 col_offset, u64* __restrict__ partial,
+                                                                    const u64* __restrict__ Mg) {
     __shared__ u64 Msh[WIDE_ROWS * AJ_D];
     __shared__ u64 psh[BITS_MAX_B], nsh[BITS_MAX_B];
     __shared__ u32 ksh[8];
     const int t = threadIdx.x, il = t / AJ_D, r = t % AJ_D;
     const int chunk = blockIdx.x, tile = blockIdx.y, row = tile * WIDE_ROWS + il;
-    if (t < 8) ksh[t] = key[t];
+    if (t < 8 && !Mg) ksh[t] = key[t];
     u64 acc[BITS_MAX_B];
 #pragma unroll
     for (int b = 0; b < BITS_MAX_B; b++) acc[b] = 0;
@@ -603,7 +607,12 @@ __global__ void __launch_bounds__(WIDE_ROWS * AJ_D) ajtai_bits_kernel(const u32*
             psh[t] = pos[(u64)t * N + j];
             nsh[t] = neg ? neg[(u64)t * N + j] : 0;
         }
-        wide_fill_rows(ksh, tile, j + col_offset, Msh, t);
+        if (Mg) {
+            const int rr = tile * WIDE_ROWS + il;
+            Msh[t] = rr < AJ_KAPPA ? Mg[((j + col_offset) * AJ_KAPPA + rr) * AJ_D + r] : 0;
+        } else {
+            wide_fill_rows(ksh, tile, j + col_offset, Msh, t);
+        }
         __syncthreads();
         const u64* m = Msh + il * AJ_D;
 #pragma unroll
@@ -676,14 +685,14 @@ static bool chunk_ok(int chunk) {
 }
 
 static int commit_bits(const u32* d_key, const u64* d_pos, const u64* d_neg, u64 N, int B, u64 col_offset,
-                       u64* d_out, const char* name) {
-    if (N == 0 || B < 1 || B > BITS_MAX_B || !d_key || !d_pos || !d_out) return GB_EINVAL;
+                       u64* d_out, const char* name, const u64* d_M = nullptr) {
+    if (N == 0 || B < 1 || B > BITS_MAX_B || !(d_key || d_M) || !d_pos || !d_out) return GB_EINVAL;
     cudaStream_t s = stream();
     const int nchunks = (int)((N + WIDE_CHUNK - 1) / WIDE_CHUNK);
     u64* partial = nullptr;
     GB_CUDA_TRY(cudaMallocAsync(&partial, (size_t)nchunks * B * AJ_KAPPA * AJ_D * 8, s));
     dim3 g((unsigned)nchunks, (unsigned)((AJ_KAPPA + WIDE_ROWS - 1) / WIDE_ROWS));
-    ajtai_bits_kernel<<<g, WIDE_ROWS * AJ_D, 0, s>>>(d_key, d_pos, d_neg, N, B, col_offset, partial);
+    ajtai_bits_kernel<<<g, WIDE_ROWS * AJ_D, 0, s>>>(d_key, d_pos, d_neg, N, B, col_offset, partial, d_M);
     int rc = check_launch(name);
     if (!rc) {
         ajtai_reduce_b_kernel<<<grid_for((size_t)B * AJ_KAPPA * AJ_D, 256), 256, 0, s>>>(partial, nchunks, B, d_out);
@@ -799,7 +808,39 @@ int ajtai_commit_ternary_ffi(const uint32_t* d_key, const uint64_t* d_pos, const
                              int chunk, uint64_t* d_out) {
     if (!chunk_ok(chunk)) return GB_EUNSUPPORTED;
     if (!d_neg) return GB_EINVAL;
-    return commit_bits(d_key, d_pos, d_neg, N_ring, 1, 0, d_out, "ajtai_commit_ternary_ffi");
+    return commit_bits(d_key, d_pos, d_neg, N_ring, AJ_SPLIT_K, 0, d_out, "ajtai_commit_ternary_ffi");
+}
+
+// M[j][i][0..63] = M_{i,j} for j < N, i < KAPPA (ajtai_premat.cuh:35-85)
+__global__ void ajtai_materialize_kernel(const u32* __restrict__ key, u64 N, u64* __restrict__ M) {
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)N * AJ_KAPPA * 8) return;
+    u32 k[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) k[q] = __ldg(key + q);
+    const u32 blk = (u32)(t & 7);
+    const size_t ji = t >> 3;  // j * KAPPA + i
+    const u64 j = ji / AJ_KAPPA;
+    const int i = (int)(ji % AJ_KAPPA);
+    u64 out[8];
+    ajtai_prg_block(k, (u32)i, j, blk, out);
+    u64* dst = M + ji * AJ_D + 8 * blk;
+#pragma unroll
+    for (int q = 0; q < 8; q++) dst[q] = out[q];
+}
+
+int ajtai_materialize_m_ffi(const uint32_t* d_chacha_key, uint64_t* d_M, uint64_t N) {
+    if (!d_chacha_key || !d_M || N == 0) return GB_EINVAL;
+    cudaStream_t s = stream();
+    ajtai_materialize_kernel<<<grid_for((size_t)N * AJ_KAPPA * 8, 256), 256, 0, s>>>(d_chacha_key, N, d_M);
+    return check_launch("ajtai_materialize_kernel");
+}
+
+int ajtai_commit_ternary_premat_ffi(const uint64_t* d_M, const uint64_t* d_pos, const uint64_t* d_neg, uint64_t N_ring,
+                                    int chunk, uint64_t* d_out) {
+    if (!chunk_ok(chunk)) return GB_EUNSUPPORTED;
+    if (!d_neg || !d_M) return GB_EINVAL;
+    return commit_bits(nullptr, d_pos, d_neg, N_ring, AJ_SPLIT_K, 0, d_out, "ajtai_commit_ternary_premat_ffi", d_M);
 }
 
 int ajtai_commit_sparse_ffi(const uint32_t* d_key, const uint64_t* d_positions, uint64_t K, int chunk,

@@ -98,6 +98,8 @@ struct FAgl {
 // builds E in shared memory by doubling; lanes read 32 consecutive inputs (coalesced) and
 // accumulate lazily; lanes of one output are combined by shuffles.
 // MODE 0: base in, base r.  1: base in, Ext2 r.  2: Ext2 in, Ext2 r.  Outputs canonical.
+constexpr int PE_BATCH = 8;
+
 template <class F, int MODE, bool FULL>
 __global__ void __launch_bounds__(256) pe_dot_kernel(const u64* __restrict__ in, u64* __restrict__ out,
                                                      const u64* __restrict__ r, int lvl0, int K, size_t outs) {
@@ -151,8 +153,32 @@ __global__ void __launch_bounds__(256) pe_dot_kernel(const u64* __restrict__ in,
         const size_t base = task * 32 * (size_t)steps;
         typename F::Acc acc;
         acc.zero();
-#pragma unroll 4
-        for (int i = 0; i < steps; i++) {
+        int i = 0;
+        if (FULL) {
+            // PE_BATCH independent loads in flight per lane before they are multiplied in
+            for (; i + PE_BATCH <= steps; i += PE_BATCH) {
+                u64 v0[PE_BATCH], v1[PE_BATCH];
+#pragma unroll
+                for (int u = 0; u < PE_BATCH; u++) {
+                    const size_t e = base + (size_t)(i + u) * 32 + lane;
+                    if (MODE == 2) {
+                        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(in) + e);
+                        v0[u] = v.x;
+                        v1[u] = v.y;
+                    } else {
+                        v0[u] = __ldg(in + e);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < PE_BATCH; u++) {
+                    const int b = (i + u) * 32 + lane;
+                    if (MODE == 0) acc.add1(v0[u], e0[b]);
+                    else if (MODE == 1) acc.add(v0[u], e0[b], e1[b]);
+                    else acc.add2(v0[u], v1[u], e0[b], e1[b], e1w[b]);
+                }
+            }
+        }
+        for (; i < steps; i++) {
             const int b = FULL ? i * 32 + lane : (lane & (S - 1));
             const size_t e = base + (size_t)i * 32 + lane;
             if (FULL || e < total) {

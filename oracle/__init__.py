@@ -407,6 +407,71 @@ def fused_permute_peval(evals, n, m, half, eq, lo, hi, field="gl"):
     return out
 
 
+# ---- Ajtai fold-tree operations (cuda_almost_goldilocks/ajtai.cuh:700-1260), numpy restatement ----
+def negacyclic_matrix(r):
+    """T with (r . z)[k] = sum_l z[l] T[l, k]: T[l, k] = r[(k - l) mod 64], negated when l > k."""
+    r = np.asarray(r, np.int64)
+    l = np.arange(64)[:, None]
+    k = np.arange(64)[None, :]
+    idx = (k - l) % 64
+    return np.where(l > k, -r[idx], r[idx])
+
+
+def bits64(words):
+    """[N] u64 -> [N, 64] int64 bits (bit l of word j at [j, l])."""
+    w = np.asarray(words, np.uint64).reshape(-1)
+    return ((w[:, None] >> np.arange(64, dtype=np.uint64)[None, :]) & np.uint64(1)).astype(np.int64)
+
+
+def ajtai_multifold_mixed(zb, pos, neg, r_all):
+    """multifold_mixed_witness_kernel (ajtai.cuh:1040-1122): zb [nb][N], pos/neg [nt][N] u64 masks,
+    r_all [(nb + nt)][64] int8 -> [N][64] int16 (the i32 sum cast to i16)."""
+    zb = np.asarray(zb, np.uint64).reshape(-1, np.asarray(zb).shape[-1]) if len(zb) else np.zeros((0, 0), np.uint64)
+    r_all = np.asarray(r_all, np.int64).reshape(-1, 64)
+    n = zb.shape[1] if zb.size else np.asarray(pos).shape[-1]
+    acc = np.zeros((n, 64), np.int64)
+    nb = zb.shape[0] if zb.size else 0
+    for i in range(nb):
+        acc += bits64(zb[i]) @ negacyclic_matrix(r_all[i])
+    for t in range(len(pos)):
+        acc += (bits64(pos[t]) - bits64(neg[t])) @ negacyclic_matrix(r_all[nb + t])
+    return acc.astype(np.int16)
+
+
+def ajtai_fold_witness(z1, z2, r):
+    """fold_witness_kernel (ajtai.cuh:715-760): z1 + r . z2 in F_q, canonical [N][64]."""
+    acc = bits64(z1) + bits64(z2) @ negacyclic_matrix(r)
+    neg = acc < 0
+    out = acc.astype(np.uint64)
+    out[neg] = np.uint64(Q_AGL) - (-acc[neg]).astype(np.uint64)
+    return out
+
+
+def ajtai_split_witness(z):
+    """split_witness_kernel (ajtai.cuh:1185-1243): [N][64] i16 -> pos, neg [13][N] u64."""
+    z = np.asarray(z, np.int64).reshape(-1, 64)
+    a = np.abs(z)
+    pos = np.zeros((13, z.shape[0]), np.uint64)
+    neg = np.zeros((13, z.shape[0]), np.uint64)
+    w = (np.uint64(1) << np.arange(64, dtype=np.uint64))[None, :]
+    for i in range(13):
+        b = ((a >> i) & 1).astype(bool)
+        pos[i] = np.bitwise_or.reduce(np.where(b & (z > 0), w, np.uint64(0)), axis=1)
+        neg[i] = np.bitwise_or.reduce(np.where(b & (z < 0), w, np.uint64(0)), axis=1)
+    return pos, neg
+
+
+def ajtai_fold_commitments(c_first, c_all, r_all):
+    """fold_commitment_kernel / multifold_commitment_kernel (ajtai.cuh:784-830, :1123-1147):
+    c_first (or zero) + sum_i r_i . c_i over [KAPPA][64] rows of F_q, canonical."""
+    c_all = [np.asarray(c, np.uint64).reshape(-1, 64) for c in c_all]
+    out = np.zeros_like(c_all[0], dtype=object) if c_first is None else np.asarray(c_first, np.uint64).reshape(-1, 64).astype(object)
+    for c, r in zip(c_all, np.asarray(r_all, np.int64).reshape(-1, 64)):
+        T = negacyclic_matrix(r).astype(object)
+        out = out + c.astype(object) @ T
+    return (out % Q_AGL).astype(np.uint64)
+
+
 def ajtai_ring_elem(key, row, j):
     out = np.zeros(64, np.uint64)
     lib().or_ajtai_ring_elem(_a(key, np.uint32), row, j, out)

@@ -150,12 +150,24 @@ def test_ternary_and_sparse_vs_oracle(gpu_lib):
     rng = np.random.default_rng(8)
     key = np.array([9, 9, 8, 8, 7, 7, 6, 6], np.uint32)
     n = 21
-    pos = rng.integers(0, 1 << 63, size=n, dtype=np.uint64)
-    neg = rng.integers(0, 1 << 63, size=n, dtype=np.uint64) & ~pos
-    d_key, d_out = _dev(key), _dev(np.zeros(42 * 64, np.uint64))
+    # the 13 ternary chunks of a split witness, committed together (ajtai.cuh:1262-1370)
+    pos = rng.integers(0, 1 << 63, size=(13, n), dtype=np.uint64)
+    neg = rng.integers(0, 1 << 63, size=(13, n), dtype=np.uint64) & ~pos
+    d_key, d_out = _dev(key), _dev(np.zeros(13 * 42 * 64, np.uint64))
     d_pos, d_neg = _dev(pos), _dev(neg)
     assert L.ajtai_commit_ternary_ffi(d_key.ptr, d_pos.ptr, d_neg.ptr, n, 1024, d_out.ptr) == 0
-    assert np.array_equal(d_out.to_numpy().reshape(42, 64), O.ajtai_commit_wide(key, _bits_to_coeffs(pos, neg), 0, 0, 42))
+    got = d_out.to_numpy().reshape(13, 42, 64)
+    for i in (0, 6, 12):
+        assert np.array_equal(got[i], O.ajtai_commit_wide(key, _bits_to_coeffs(pos[i], neg[i]), 0, 0, 42))
+    # the same against a materialized matrix (ajtai_premat.cuh)
+    d_M = _dev(np.zeros(n * 42 * 64, np.uint64))
+    assert L.ajtai_materialize_m_ffi(d_key.ptr, d_M.ptr, n) == 0
+    M = d_M.to_numpy().reshape(n, 42, 64)
+    assert np.array_equal(M[5, 3], O.ajtai_ring_elem(key, 3, 5)) and np.array_equal(M[20, 41], O.ajtai_ring_elem(key, 41, 20))
+    d_out2 = _dev(np.zeros(13 * 42 * 64, np.uint64))
+    assert L.ajtai_commit_ternary_premat_ffi(d_M.ptr, d_pos.ptr, d_neg.ptr, n, 256, d_out2.ptr) == 0
+    assert np.array_equal(d_out2.to_numpy(), d_out.to_numpy())
+    assert L.ajtai_commit_ternary_premat_ffi(d_M.ptr, d_pos.ptr, d_neg.ptr, n, 100, d_out2.ptr) == -3
     # sparse positions (ascending with gaps, one repeated index counted twice) across > 1 chunk
     cols = 700
     p = np.sort(rng.choice(cols * 64, size=300, replace=False)).astype(np.uint64)
@@ -164,6 +176,7 @@ def test_ternary_and_sparse_vs_oracle(gpu_lib):
     for x in p:
         coeff[int(x)] += 1
     d_p = _dev(p)
+    d_out = _dev(np.zeros(42 * 64, np.uint64))
     assert L.ajtai_commit_sparse_ffi(d_key.ptr, d_p.ptr, len(p), 64, d_out.ptr) == 0
     assert np.array_equal(d_out.to_numpy().reshape(42, 64), O.ajtai_commit_wide(key, coeff, 0, 0, 42))
     assert L.ajtai_commit_sparse_ffi(d_key.ptr, d_p.ptr, 0, 64, d_out.ptr) == 0 and not d_out.to_numpy().any()
