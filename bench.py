@@ -292,6 +292,20 @@ def run_side_workload(args):
                             "frac": line["value"] / peak, "peak_source": src}
     if args.workload == "ajtai":
         line["tensor_tflops_equiv"] = 2.0 * 8 * rows * 64 * Bw * n_ring * 64 / (ms * 1e-3) / 1e12
+        # the fold tree at the SuperNeo shape: 50 binary + 13 ternary witnesses of 2^14 ring elements
+        nb, nt, nr = 50, 13, 1 << 14
+        zb = DeviceBuffer.from_numpy(rng.integers(0, 2**63, size=nb * nr, dtype=np.uint64))
+        pn = rng.integers(0, 2**63, size=(2, nt * nr), dtype=np.uint64)
+        d_pos, d_neg = DeviceBuffer.from_numpy(pn[0]), DeviceBuffer.from_numpy(pn[1] & ~pn[0])
+        r = rng.choice(np.array([-1, 0, 1, 2], np.int8), size=(nb + nt) * 64)
+        d_r = DeviceBuffer.from_numpy(r)
+        d_o = DeviceBuffer(nr * 64, np.int16)
+        mf = lambda: Nn.check(L.ajtai_multifold_mixed_witness_ffi(zb.ptr, d_pos.ptr, d_neg.ptr, d_r.ptr, d_o.ptr, nb, nt,
+                                                                   nr, 256), "multifold")
+        mf()
+        mf_ms = min(ev_time(mf) for _ in range(5))
+        line["multifold_mixed"] = {"ms": mf_ms, "workload": f"{nb} binary + {nt} ternary witnesses x {nr} ring "
+                                                             "elements, challenges in {-1, 0, 1, 2}"}
     print(json.dumps(line))
 
 

@@ -177,6 +177,34 @@ int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses,
 int ajtai_commit_wide_noalloc_ffi(const uint32_t *d_key, const uint64_t *d_z_wide, uint64_t N, uint64_t col_offset,
                                   int chunk, uint64_t *d_out);
 
+/* ---- Element-wise ops over q and its Ext2 (almost-goldilocks-cuda-rs/src/ffi.rs:95-140;
+ * almost wrapper.cu:420-640): canonical outputs, Ext2 = F_q[X]/(X^2 - 3) as (c0, c1), inverses of
+ * zero are zero. ---- */
+int agl_batch_add_ffi(const uint64_t *a, const uint64_t *b, uint64_t *r, int n);
+int agl_batch_sub_ffi(const uint64_t *a, const uint64_t *b, uint64_t *r, int n);
+int agl_batch_mul_ffi(const uint64_t *a, const uint64_t *b, uint64_t *r, int n);
+int agl_batch_div_ffi(const uint64_t *a, const uint64_t *b, uint64_t *r, int n);
+int agl_batch_inverse_ffi(const uint64_t *a, uint64_t *r, int n);
+int agl_batch_mul_scalar_ffi(uint64_t scalar, const uint64_t *a, uint64_t *r, int n);
+int agl_batch_neg_ffi(const uint64_t *a, uint64_t *r, int n);
+int agl_batch_square_ffi(const uint64_t *a, uint64_t *r, int n);
+int agl_batch_double_ffi(const uint64_t *a, uint64_t *r, int n);
+int agl_batch_exp_ffi(const uint64_t *a, uint64_t exp, uint64_t *r, int n);
+int aext2_batch_add_ffi(const uint64_t *a, const uint64_t *b, uint64_t *r, int n);
+int aext2_batch_sub_ffi(const uint64_t *a, const uint64_t *b, uint64_t *r, int n);
+int aext2_batch_mul_ffi(const uint64_t *a, const uint64_t *b, uint64_t *r, int n);
+int aext2_batch_inverse_ffi(const uint64_t *a, uint64_t *r, int n);
+int aext2_batch_mul_scalar_ffi(uint64_t scalar, const uint64_t *a, uint64_t *r, int n);
+int aext2_batch_neg_ffi(const uint64_t *a, uint64_t *r, int n);
+int aext2_batch_square_ffi(const uint64_t *a, uint64_t *r, int n);
+int aext2_batch_frobenius_ffi(const uint64_t *a, uint64_t *r, int n);
+int aext2_batch_conjugate_ffi(const uint64_t *a, uint64_t *r, int n);
+int aext2_batch_exp_ffi(const uint64_t *a, uint64_t exp, uint64_t *r, int n);
+int aext2_scale_accumulate_ffi(uint64_t scalar_c0, uint64_t scalar_c1, const uint64_t *d_src, uint64_t *d_acc, int n);
+int agl_to_aext2_batch_ffi(const uint64_t *in, uint64_t *out, int n);
+int aext2_to_agl_batch_ffi(const uint64_t *in, uint64_t *out, int n);
+int agl_zero_buffer_ffi(uint64_t *d_buf, int n);
+
 /* ---- Partial evaluation and bit permutation over q (almost-goldilocks-cuda-rs/src/ffi.rs:113-119,
  * :198-226; wrapper.cu:713-805, :1061-1085).  Same arguments and results as the Goldilocks forms
  * (goldilocks_cuda_wrapper.h), over q = 2^64 - 2^32 - 31 and its Ext2 (X^2 - 3). ---- */

@@ -62,6 +62,41 @@ int gl_batch_inverse(const uint64_t *d_a, uint64_t *d_result, int n);
 int ext2_batch_add_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
 int ext2_batch_sub_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
 int ext2_batch_mul_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+/* The rest of the element-wise ops (ffi.rs:105-131, :163-280, :633-639; wrapper.cu:180-858,
+ * :1790-1815, :2282, :2446), canonical outputs; Ext2 = F_p[X]/(X^2 - 7) as (c0, c1), Ext5 =
+ * F_p[X]/(X^5 - 3) as (c0..c4); inverses (and divisions) by zero give zero.  The quantisation
+ * helpers gl_scale_up/down and gl_decompose_bits32 belong to the einsum/ReLU basic blocks and are
+ * not part of this library. */
+int gl_batch_div(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int gl_batch_mul_scalar(uint64_t scalar, const uint64_t *d_a, uint64_t *d_result, int n);
+int gl_batch_neg(const uint64_t *d_a, uint64_t *d_result, int n);
+int gl_batch_square(const uint64_t *d_a, uint64_t *d_result, int n);
+int gl_batch_double(const uint64_t *d_a, uint64_t *d_result, int n);
+int gl_batch_exp(const uint64_t *d_a, uint64_t exp, uint64_t *d_result, int n);
+int ext2_batch_inverse_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext2_batch_mul_scalar_ffi(uint64_t scalar, const uint64_t *d_a, uint64_t *d_result, int n);
+int ext2_batch_neg_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext2_batch_square_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext2_batch_frobenius_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext2_batch_conjugate_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext2_batch_exp_ffi(const uint64_t *d_a, uint64_t exp, uint64_t *d_result, int n);
+/* d_acc[i] += (scalar_c0 + scalar_c1 X) d_src[i], Ext2 */
+int ext2_scale_accumulate_ffi(uint64_t scalar_c0, uint64_t scalar_c1, const uint64_t *d_src, uint64_t *d_acc, int n);
+int ext5_batch_add_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int ext5_batch_sub_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int ext5_batch_mul_ffi(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_result, int n);
+int ext5_batch_inverse_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext5_batch_mul_scalar_ffi(uint64_t scalar, const uint64_t *d_a, uint64_t *d_result, int n);
+int ext5_batch_neg_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext5_batch_square_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext5_batch_frobenius_ffi(const uint64_t *d_a, uint64_t *d_result, int n);
+int ext5_batch_exp_ffi(const uint64_t *d_a, uint64_t exp, uint64_t *d_result, int n);
+int gl_to_ext2_batch_ffi(const uint64_t *d_input, uint64_t *d_output, int n);
+int ext2_to_gl_batch_ffi(const uint64_t *d_input, uint64_t *d_output, int n);
+int gl_to_ext5_batch_ffi(const uint64_t *d_input, uint64_t *d_output, int n);
+int ext5_to_gl_batch_ffi(const uint64_t *d_input, uint64_t *d_output, int n);
+int gl_memset_zero(uint64_t *d_buf, size_t n_u64);
+int gl_zero_buffer(uint64_t *d_buf, int n);
 
 /* Poseidon2 width 8 (ffi.rs:287-300; wrapper.cu:864-962).
  * hash_batch: full permutation of n 8-element states; compress/merkle_layer: 2-to-1. */

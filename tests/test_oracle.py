@@ -1,4 +1,6 @@
 """The CPU oracle against the reference's golden vectors and its own code (CPU only)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -293,3 +295,15 @@ def test_fused_restatement_is_permute_then_partial_eval():
                   np.uint32)
     got = O.fused_permute_peval(ev, n, m, half, O.eq_table_ext2(ch), lo, hi)
     assert np.array_equal(got, O.partial_eval_ext2(O.bit_permute(ev, inv), ch))
+
+
+def test_ext5_frobenius_constants():
+    """The Ext5 Frobenius multipliers compiled into the library are the powers of 3^((p-1)/5),
+    and 7, 3 are quadratic non-residues (their Frobenius multiplier is -1)."""
+    import re
+    src = open(os.path.join(os.path.dirname(__file__), "..", "morpheus_gb300", "csrc", "field_ops.cu")).read()
+    m = re.search(r"c_frob_gl5\[5\] = \{([^}]*)\}", src)
+    vals = [int(v.strip().rstrip("ull")) for v in m.group(1).split(",")]
+    d = pow(3, (O.P - 1) // 5, O.P)
+    assert vals == [pow(d, i, O.P) for i in range(5)]
+    assert pow(7, (O.P - 1) // 2, O.P) == O.P - 1 and pow(3, (O.Q_AGL - 1) // 2, O.Q_AGL) == O.Q_AGL - 1
