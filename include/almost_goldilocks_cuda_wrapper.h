@@ -177,6 +177,34 @@ int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses,
 int ajtai_commit_wide_noalloc_ffi(const uint32_t *d_key, const uint64_t *d_z_wide, uint64_t N, uint64_t col_offset,
                                   int chunk, uint64_t *d_out);
 
+/* ---- Binary round 0 and lifts of the batched same-point sumcheck (almost-goldilocks-cuda-rs
+ * GpuBatchedSamePointState, src/sumcheck_prover.rs:468-1006; almost_sumcheck_prover.cuh:709-1005;
+ * almost wrapper.cu:862-1060).  Layout as aext2_sumcheck_batched_*: leaf l's eq then f, each
+ * original_size Ext2, at d_polys + 4 l original_size; bit i of leaf l's binary f is bit i % 64 of
+ * d_packed[l packed_size_u64 + i / 64].  Same grid shapes as the reference (partials
+ * [num_blocks_x][leaf][c][2]). ---- */
+/* round 0 with f binary: c = 0: sum e0 f0, c = 1: sum e1 f1, c = 2: sum (2 e1 - e0)(2 f1 - f0) */
+int aext2_sumcheck_batched_round0_binary_msg_ffi(const uint64_t *d_polys, const uint64_t *d_packed,
+                                                 uint64_t *d_partial, size_t original_size, size_t half,
+                                                 int num_leaves, int num_blocks_x, size_t packed_size_u64);
+/* the fold of that round: eq and the lifted f folded with the challenge into d_output (same layout) */
+int aext2_sumcheck_batched_round0_binary_fold_ffi(const uint64_t *d_polys, const uint64_t *d_packed,
+                                                  uint64_t *d_output, uint64_t challenge_c0, uint64_t challenge_c1,
+                                                  size_t original_size, size_t half, int num_leaves,
+                                                  size_t packed_size_u64);
+/* lift binary (or ternary pos - neg) bits into the f slot of each leaf, Ext2 (bit, 0) */
+int aext2_batched_lift_binary_ffi(const uint64_t *d_packed, uint64_t *d_polys, size_t original_size, int num_leaves,
+                                  size_t packed_size_u64);
+int aext2_batched_lift_ternary_single_ffi(const uint64_t *d_pos, const uint64_t *d_neg, uint64_t *d_polys,
+                                          size_t original_size, int num_leaves, size_t packed_size_u64);
+/* the same into a contiguous [leaf][original_size] Ext2 array */
+int aext2_lift_binary_contig_ffi(const uint64_t *d_packed, uint64_t *d_f, size_t original_size, int num_leaves,
+                                 size_t packed_size_u64);
+/* per-(block, plane) partial sums of the shared eq table over each plane's set bits
+ * (almost_sumcheck_prover.cuh:920-970; almost-goldilocks-cuda-rs/src/eq_lagrange.rs) */
+int aext2_selective_add_batched_planes_ffi(const uint64_t *d_eq, const uint64_t *d_packed_planes, uint64_t *d_partial,
+                                           size_t total, int n_planes, size_t packed_size_u64, int num_blocks_x);
+
 /* ---- Element-wise ops over q and its Ext2 (almost-goldilocks-cuda-rs/src/ffi.rs:95-140;
  * almost wrapper.cu:420-640): canonical outputs, Ext2 = F_q[X]/(X^2 - 3) as (c0, c1), inverses of
  * zero are zero. ---- */

@@ -145,6 +145,111 @@ __global__ void __launch_bounds__(AGL_BLOCK) aext2_batched_msg_kernel(const u64*
     }
 }
 
+// Round 0 with a binary f (packed bits of leaf l at packed + l * packed_words; the eq slot of
+// polys is read, the f slot ignored): c = 0: e0 f0, c = 1: e1 f1, c = 2: (2 e1 - e0)(2 f1 - f0),
+// by selective additions (almost_sumcheck_prover.cuh:709-800).  Partials as the batched message.
+__global__ void __launch_bounds__(AGL_BLOCK) aext2_round0_binary_msg_kernel(const u64* __restrict__ polys,
+                                                                            const u64* __restrict__ packed,
+                                                                            u64* __restrict__ partial,
+                                                                            size_t original_size, size_t half,
+                                                                            int leaves, size_t packed_words) {
+    __shared__ u64 sh[(AGL_BLOCK / 32) * 6];
+    const int leaf = blockIdx.y;
+    const u64* lp = polys + (size_t)leaf * 4 * original_size;
+    const u64* bits = packed + (size_t)leaf * packed_words;
+    u64 acc[6] = {0, 0, 0, 0, 0, 0};
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < half; y += (size_t)gridDim.x * blockDim.x) {
+        const ae2 e0 = ae2_make(lp[4 * y], lp[4 * y + 1]), e1 = ae2_make(lp[4 * y + 2], lp[4 * y + 3]);
+        const u64 w = bits[(2 * y) >> 6] >> ((2 * y) & 63);
+        const int f0 = (int)(w & 1), f1 = (int)((w >> 1) & 1);
+        if (f0) {
+            acc[0] = agl_add(acc[0], e0.c0);
+            acc[1] = agl_add(acc[1], e0.c1);
+        }
+        if (f1) {
+            acc[2] = agl_add(acc[2], e1.c0);
+            acc[3] = agl_add(acc[3], e1.c1);
+        }
+        const int f2 = 2 * f1 - f0;  // in {-1, 0, 1, 2}
+        if (f2) {
+            ae2 e2v = ae2_sub(ae2_add(e1, e1), e0);
+            if (f2 == 2) e2v = ae2_add(e2v, e2v);
+            if (f2 < 0) {
+                acc[4] = agl_sub(acc[4], e2v.c0);
+                acc[5] = agl_sub(acc[5], e2v.c1);
+            } else {
+                acc[4] = agl_add(acc[4], e2v.c0);
+                acc[5] = agl_add(acc[5], e2v.c1);
+            }
+        }
+    }
+    agl_block_sum<6>(acc, sh);
+    if (threadIdx.x == 0) {
+        u64* o = partial + ((size_t)blockIdx.x * leaves + leaf) * 6;
+#pragma unroll
+        for (int w = 0; w < 6; w++) o[w] = acc[w];
+    }
+}
+
+// the matching fold: eq' = e0 + r (e1 - e0); f' = f0 + r (f1 - f0) in {0, r, 1 - r, 1}
+__global__ void aext2_round0_binary_fold_kernel(const u64* __restrict__ in, const u64* __restrict__ packed,
+                                                u64* __restrict__ out, u64 r0, u64 r1, size_t original_size,
+                                                size_t half, size_t packed_words) {
+    const int leaf = blockIdx.y;
+    const u64* il = in + (size_t)leaf * 4 * original_size;
+    const u64* bits = packed + (size_t)leaf * packed_words;
+    u64* ol = out + (size_t)leaf * 4 * original_size;
+    const ae2 r = ae2_make(r0, r1);
+    const ae2 omr = ae2_sub(ae2_make(1, 0), r);
+    for (size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x; y < half; y += (size_t)gridDim.x * blockDim.x) {
+        const ae2 a = ae2_make(il[4 * y], il[4 * y + 1]), b = ae2_make(il[4 * y + 2], il[4 * y + 3]);
+        const ae2 e = ae2_canon(ae2_add(a, ae2_mul(r, ae2_sub(b, a))));
+        ol[2 * y] = e.c0;
+        ol[2 * y + 1] = e.c1;
+        const u64 w = bits[(2 * y) >> 6] >> ((2 * y) & 63);
+        const int f0 = (int)(w & 1), f1 = (int)((w >> 1) & 1);
+        const ae2 f = f0 ? (f1 ? ae2_make(1, 0) : omr) : (f1 ? r : ae2_make(0, 0));
+        const ae2 fc = ae2_canon(f);
+        ol[2 * original_size + 2 * y] = fc.c0;
+        ol[2 * original_size + 2 * y + 1] = fc.c1;
+    }
+}
+
+// binary (or ternary pos - neg) bits of leaf l lifted to Ext2 at dst + l * leaf_words + off
+__global__ void aext2_lift_kernel(const u64* __restrict__ pos, const u64* __restrict__ neg, u64* __restrict__ dst,
+                                  size_t original_size, size_t packed_words, size_t leaf_words, size_t off) {
+    const int leaf = blockIdx.y;
+    const u64* pl = pos + (size_t)leaf * packed_words;
+    const u64* nl = neg ? neg + (size_t)leaf * packed_words : nullptr;
+    u64* d = dst + (size_t)leaf * leaf_words + off;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < original_size; i += (size_t)gridDim.x * blockDim.x) {
+        const u64 p = (pl[i >> 6] >> (i & 63)) & 1, n = nl ? (nl[i >> 6] >> (i & 63)) & 1 : 0;
+        d[2 * i] = agl_sub(p, n);  // 0, 1 or q - 1 (pos and neg disjoint)
+        d[2 * i + 1] = 0;
+    }
+}
+
+// per-(block, plane) partial sums of eq[i] over the set bits of each plane (shared eq table)
+__global__ void __launch_bounds__(AGL_BLOCK) aext2_selective_add_kernel(const u64* __restrict__ eq,
+                                                                        const u64* __restrict__ planes,
+                                                                        u64* __restrict__ partial, size_t total,
+                                                                        int n_planes, size_t packed_words) {
+    __shared__ u64 sh[(AGL_BLOCK / 32) * 2];
+    const int plane = blockIdx.y;
+    const u64* pb = planes + (size_t)plane * packed_words;
+    u64 acc[2] = {0, 0};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+        if ((pb[i >> 6] >> (i & 63)) & 1) {
+            acc[0] = agl_add(acc[0], eq[2 * i]);
+            acc[1] = agl_add(acc[1], eq[2 * i + 1]);
+        }
+    agl_block_sum<2>(acc, sh);
+    if (threadIdx.x == 0) {
+        partial[((size_t)blockIdx.x * n_planes + plane) * 2] = acc[0];
+        partial[((size_t)blockIdx.x * n_planes + plane) * 2 + 1] = acc[1];
+    }
+}
+
 __global__ void aext2_batched_fold_kernel(const u64* __restrict__ in, u64* __restrict__ out, u64 r0, u64 r1,
                                           size_t original_size, size_t half) {
     const int leaf = blockIdx.y;
@@ -331,6 +436,62 @@ int aext2_sumcheck_batched_fold_ffi(const uint64_t* d_input, uint64_t* d_output,
     aext2_batched_fold_kernel<<<dim3(fold_grid(half), num_leaves), AGL_BLOCK, 0, stream()>>>(d_input, d_output, c0,
                                                                                              c1, original_size, half);
     return check_launch("aext2_sumcheck_batched_fold_ffi");
+}
+
+int aext2_sumcheck_batched_round0_binary_msg_ffi(const uint64_t* d_polys, const uint64_t* d_packed,
+                                                 uint64_t* d_partial, size_t original_size, size_t half,
+                                                 int num_leaves, int num_blocks_x, size_t packed_size_u64) {
+    if (num_leaves < 0 || num_blocks_x <= 0) return GB_EINVAL;
+    if (num_leaves == 0) return GB_OK;
+    aext2_round0_binary_msg_kernel<<<dim3(num_blocks_x, num_leaves), AGL_BLOCK, 0, stream()>>>(
+        d_polys, d_packed, d_partial, original_size, half, num_leaves, packed_size_u64);
+    return check_launch("aext2_sumcheck_batched_round0_binary_msg_ffi");
+}
+
+int aext2_sumcheck_batched_round0_binary_fold_ffi(const uint64_t* d_polys, const uint64_t* d_packed,
+                                                  uint64_t* d_output, uint64_t c0, uint64_t c1, size_t original_size,
+                                                  size_t half, int num_leaves, size_t packed_size_u64) {
+    if (num_leaves < 0) return GB_EINVAL;
+    if (num_leaves == 0 || half == 0) return GB_OK;
+    aext2_round0_binary_fold_kernel<<<dim3(fold_grid(half), num_leaves), AGL_BLOCK, 0, stream()>>>(
+        d_polys, d_packed, d_output, c0, c1, original_size, half, packed_size_u64);
+    return check_launch("aext2_sumcheck_batched_round0_binary_fold_ffi");
+}
+
+int aext2_batched_lift_binary_ffi(const uint64_t* d_packed, uint64_t* d_polys, size_t original_size, int num_leaves,
+                                  size_t packed_size_u64) {
+    if (num_leaves < 0) return GB_EINVAL;
+    if (num_leaves == 0 || original_size == 0) return GB_OK;
+    aext2_lift_kernel<<<dim3(fold_grid(original_size), num_leaves), AGL_BLOCK, 0, stream()>>>(
+        d_packed, nullptr, d_polys, original_size, packed_size_u64, 4 * original_size, 2 * original_size);
+    return check_launch("aext2_batched_lift_binary_ffi");
+}
+
+int aext2_batched_lift_ternary_single_ffi(const uint64_t* d_pos, const uint64_t* d_neg, uint64_t* d_polys,
+                                          size_t original_size, int num_leaves, size_t packed_size_u64) {
+    if (num_leaves < 0 || !d_neg) return GB_EINVAL;
+    if (num_leaves == 0 || original_size == 0) return GB_OK;
+    aext2_lift_kernel<<<dim3(fold_grid(original_size), num_leaves), AGL_BLOCK, 0, stream()>>>(
+        d_pos, d_neg, d_polys, original_size, packed_size_u64, 4 * original_size, 2 * original_size);
+    return check_launch("aext2_batched_lift_ternary_single_ffi");
+}
+
+int aext2_lift_binary_contig_ffi(const uint64_t* d_packed, uint64_t* d_f, size_t original_size, int num_leaves,
+                                 size_t packed_size_u64) {
+    if (num_leaves < 0) return GB_EINVAL;
+    if (num_leaves == 0 || original_size == 0) return GB_OK;
+    aext2_lift_kernel<<<dim3(fold_grid(original_size), num_leaves), AGL_BLOCK, 0, stream()>>>(
+        d_packed, nullptr, d_f, original_size, packed_size_u64, 2 * original_size, 0);
+    return check_launch("aext2_lift_binary_contig_ffi");
+}
+
+int aext2_selective_add_batched_planes_ffi(const uint64_t* d_eq, const uint64_t* d_packed_planes, uint64_t* d_partial,
+                                           size_t total, int n_planes, size_t packed_size_u64, int num_blocks_x) {
+    if (n_planes < 0 || num_blocks_x <= 0) return GB_EINVAL;
+    if (n_planes == 0) return GB_OK;
+    aext2_selective_add_kernel<<<dim3(num_blocks_x, n_planes), AGL_BLOCK, 0, stream()>>>(
+        d_eq, d_packed_planes, d_partial, total, n_planes, packed_size_u64);
+    return check_launch("aext2_selective_add_batched_planes_ffi");
 }
 
 // eq tables: like the reference's ping-pong DP, the table ends in d_buf_a when log_n is even

@@ -20,9 +20,22 @@ def e2mul(a, b):
     return ((a[0] * b[0] + 3 * a[1] * b[1]) % Q, (a[0] * b[1] + a[1] * b[0]) % Q)
 
 
+_KEEP = []
+
+
+@pytest.fixture(autouse=True)
+def _release_buffers():
+    """Buffers made by dev() live until the test ends (a temporary passed as dev(x).ptr would
+    otherwise be freed, and its memory reused, before the kernel that reads it runs)."""
+    yield
+    _KEEP.clear()
+
+
 def dev(arr):
     from morpheus_gb300.memory import DeviceBuffer
-    return DeviceBuffer.from_numpy(np.ascontiguousarray(arr, dtype=np.uint64).reshape(-1))
+    buf = DeviceBuffer.from_numpy(np.ascontiguousarray(arr, dtype=np.uint64).reshape(-1))
+    _KEEP.append(buf)
+    return buf
 
 
 def block_of(y, blocks):
@@ -193,3 +206,78 @@ def test_memory_and_stream_entry_points(gpu_lib):
     assert L.cuda_sync_mine() == 0
     assert L.agl_cuda_error_string(0) == b"no error"
     assert L.agl_cached_bytes() >= 0
+
+
+@pytest.mark.parametrize("leaves,half,blocks", [(1, 5, 1), (3, 300, 2), (2, 1024, 3)])
+def test_batched_round0_binary_and_lifts(gpu_lib, leaves, half, blocks):
+    """Round 0 of the batched same-point sumcheck with a binary f (almost_sumcheck_prover.cuh:709-860):
+    the partials are the batched message over the lifted f, block by block, and the fold equals the
+    batched fold of the lifted polynomials.  The lifts write (bit, 0) / (pos - neg, 0)."""
+    from morpheus_gb300 import _native as N
+    L = N.lib()
+    rng = np.random.default_rng(leaves * 13 + half)
+    orig = 2 * half
+    words = (orig + 63) // 64
+    polys = rng.integers(0, Q, size=(leaves, 2, orig, 2), dtype=np.uint64)
+    packed = rng.integers(0, 2**63, size=(leaves, words), dtype=np.uint64) * np.uint64(2) + \
+        rng.integers(0, 2, size=(leaves, words), dtype=np.uint64)
+    d_pk = dev(packed)
+    # the lift into the f slots, then the ordinary batched message on the result
+    d_lifted = dev(polys)
+    N.check(L.aext2_batched_lift_binary_ffi(d_pk.ptr, d_lifted.ptr, orig, leaves, words), "lift")
+    lifted = d_lifted.to_numpy().reshape(leaves, 2, orig, 2)
+    bits = ((packed[:, :, None] >> np.arange(64, dtype=np.uint64)) & np.uint64(1)).reshape(leaves, -1)[:, :orig]
+    assert np.array_equal(lifted[:, 0], polys[:, 0]) and np.array_equal(lifted[:, 1, :, 0], bits) and not lifted[:, 1, :, 1].any()
+    d_ref = dev(np.zeros(blocks * leaves * 6, np.uint64))
+    N.check(L.aext2_sumcheck_batched_round_message_ffi(d_lifted.ptr, d_ref.ptr, orig, half, leaves, blocks), "msg")
+    d_bin = dev(np.zeros(blocks * leaves * 6, np.uint64))
+    d_p = dev(polys)
+    N.check(L.aext2_sumcheck_batched_round0_binary_msg_ffi(d_p.ptr, d_pk.ptr, d_bin.ptr, orig, half, leaves, blocks,
+                                                           words), "msg0")
+    assert np.array_equal(d_bin.to_numpy(), d_ref.to_numpy())
+    r = [int(x) for x in rng.integers(0, Q, 2, dtype=np.uint64)]
+    d_o1, d_o2 = dev(np.zeros_like(polys)), dev(np.zeros_like(polys))
+    N.check(L.aext2_sumcheck_batched_fold_ffi(d_lifted.ptr, d_o1.ptr, r[0], r[1], orig, half, leaves), "fold")
+    N.check(L.aext2_sumcheck_batched_round0_binary_fold_ffi(d_p.ptr, d_pk.ptr, d_o2.ptr, r[0], r[1], orig, half, leaves,
+                                                            words), "fold0")
+    o1 = d_o1.to_numpy().reshape(leaves, 2, orig, 2)[:, :, :half]
+    o2 = d_o2.to_numpy().reshape(leaves, 2, orig, 2)[:, :, :half]
+    assert np.array_equal(o1, o2)
+    # a spot check of the fold against the definition
+    a, b = [int(x) for x in lifted[0, 1, 0]], [int(x) for x in lifted[0, 1, 1]]
+    rd = e2mul(r, [(b[w] - a[w]) % Q for w in range(2)])
+    assert [int(x) for x in o2[0, 1, 0]] == [(a[w] + rd[w]) % Q for w in range(2)]
+    # ternary lift and the contiguous lift
+    neg = rng.integers(0, 2**63, size=(leaves, words), dtype=np.uint64) & ~packed
+    d_t = dev(np.zeros_like(polys))
+    d_neg = dev(neg)
+    N.check(L.aext2_batched_lift_ternary_single_ffi(d_pk.ptr, d_neg.ptr, d_t.ptr, orig, leaves, words), "tern")
+    nbits = ((neg[:, :, None] >> np.arange(64, dtype=np.uint64)) & np.uint64(1)).reshape(leaves, -1)[:, :orig]
+    t = d_t.to_numpy().reshape(leaves, 2, orig, 2)[:, 1, :, 0]
+    assert [[int(v) for v in row] for row in t] == [[(int(p) - int(n)) % Q for p, n in zip(pr, nr)] for pr, nr in zip(bits, nbits)]
+    d_c = dev(np.zeros(leaves * orig * 2, np.uint64))
+    N.check(L.aext2_lift_binary_contig_ffi(d_pk.ptr, d_c.ptr, orig, leaves, words), "contig")
+    c = d_c.to_numpy().reshape(leaves, orig, 2)
+    assert np.array_equal(c[:, :, 0], bits) and not c[:, :, 1].any()
+
+
+def test_selective_add_batched_planes(gpu_lib):
+    from morpheus_gb300 import _native as N
+    L = N.lib()
+    rng = np.random.default_rng(9)
+    total, planes, blocks = 3000, 5, 3
+    words = (total + 63) // 64
+    eq = rng.integers(0, Q, size=(total, 2), dtype=np.uint64)
+    pk = rng.integers(0, 2**63, size=(planes, words), dtype=np.uint64)
+    d_part = dev(np.zeros(blocks * planes * 2, np.uint64))
+    d_eq, d_pk = dev(eq), dev(pk)  # held until the kernel has run
+    N.check(L.aext2_selective_add_batched_planes_ffi(d_eq.ptr, d_pk.ptr, d_part.ptr, total, planes, words, blocks),
+            "sel")
+    got = d_part.to_numpy().reshape(blocks, planes, 2)
+    for p in range(planes):
+        want = [[0, 0] for _ in range(blocks)]
+        for i in range(total):
+            if (int(pk[p, i // 64]) >> (i % 64)) & 1:
+                b = block_of(i, blocks)
+                want[b] = [(want[b][w] + int(eq[i, w])) % Q for w in range(2)]
+        assert [[int(x) for x in got[b, p]] for b in range(blocks)] == want

@@ -14,9 +14,22 @@ pytestmark = pytest.mark.gpu
 Q = O.Q_AGL
 
 
+_KEEP = []
+
+
+@pytest.fixture(autouse=True)
+def _release_buffers():
+    """Buffers made by dev() live until the test ends (a temporary passed as dev(x).ptr would
+    otherwise be freed, and its memory reused, before the kernel that reads it runs)."""
+    yield
+    _KEEP.clear()
+
+
 def dev(a):
     from morpheus_gb300.memory import DeviceBuffer
-    return DeviceBuffer.from_numpy(np.ascontiguousarray(a))
+    buf = DeviceBuffer.from_numpy(np.ascontiguousarray(a))
+    _KEEP.append(buf)
+    return buf
 
 
 def masks(rng, shape, density=0.5):
