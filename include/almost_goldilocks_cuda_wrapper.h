@@ -205,6 +205,53 @@ int aext2_lift_binary_contig_ffi(const uint64_t *d_packed, uint64_t *d_f, size_t
 int aext2_selective_add_batched_planes_ffi(const uint64_t *d_eq, const uint64_t *d_packed_planes, uint64_t *d_partial,
                                            size_t total, int n_planes, size_t packed_size_u64, int num_blocks_x);
 
+/* ---- The fold tree's other sumcheck provers (almost-goldilocks-cuda-rs/src/sumcheck_prover.rs,
+ * ffi.rs:141-160, :319-400; almost_sumcheck_prover.cuh:360-700; almost wrapper.cu:931-1028,
+ * :2652-2980).  Same launch shapes as the reference (partials per (block, unique / leaf / term)).
+ * ---- */
+/* F_u[x] = sum over leaves d_leaf_idx_sorted[d_unique_offsets[u] .. d_unique_offsets[u+1]) of
+ * alpha_leaf * bit (binary) or * (pos bit - neg bit) (ternary); d_Fu [num_unique][original_size] Ext2 */
+int aext2_build_fu_ffi(const uint64_t *d_packed, const uint64_t *d_alphas, const int *d_leaf_idx_sorted,
+                       const int *d_unique_offsets, uint64_t *d_Fu, size_t original_size, int num_unique,
+                       size_t packed_size_u64);
+int aext2_build_fu_ternary_ffi(const uint64_t *d_pos, const uint64_t *d_neg, const uint64_t *d_alphas,
+                               const int *d_leaf_idx_sorted, const int *d_unique_offsets, uint64_t *d_Fu,
+                               size_t original_size, int num_unique, size_t packed_size_u64);
+/* i16 witness [n_ring][64] -> k_chunks signed bit planes [k][n_ring] (pos, neg); *d_err = 1 when
+ * some |v| >= 2^k_chunks; k_chunks > 16 returns -1 */
+int aext2_wide_to_ternary_ffi(const int16_t *d_wide, uint64_t *d_pos, uint64_t *d_neg, int *d_err, size_t n_ring,
+                              int k_chunks);
+/* all suffix tables eqsuf_t (t = log_n .. 1) of each unique point's r (d_r_all [u][log_n] Ext2):
+ * eqsuf_t at element offset 2^(log_n-t) - 1 of the unique's region (stride eqsuf_stride_u64 words) */
+int aext2_eq_suffix_dp_ffi(const uint64_t *d_r_all, uint64_t *d_eqsuf, int log_n, int num_unique,
+                           size_t eqsuf_stride_u64);
+/* partials [block][u][A, B]: A = sum_y eqsuf[y] F_u[2y], B = sum_y eqsuf[y] F_u[2y+1] */
+int aext2_sharedeq_factored_msg_ffi(const uint64_t *d_eqsuf, const uint64_t *d_fu, uint64_t *d_partial,
+                                    size_t eqsuf_off_elems, size_t eqsuf_stride_u64, size_t poly_stride_u64,
+                                    size_t half, int num_unique, int num_blocks_x);
+/* partials [block][leaf][c][2] of the degree-2 message of eq[leaf_to_unique[leaf]] * f[leaf] */
+int aext2_sharedeq_msg_ffi(const uint64_t *d_eq, const uint64_t *d_f, const int *d_leaf_to_unique,
+                           uint64_t *d_partial, size_t original_size, size_t half, int num_leaves, int num_blocks_x);
+/* fold count independent Ext2 polynomials (stride original_size) by one challenge */
+int aext2_fold_single_ffi(const uint64_t *d_in, uint64_t *d_out, uint64_t challenge_c0, uint64_t challenge_c1,
+                          size_t original_size, size_t half, int count);
+/* Sparse boolean check: n entries (d_idx, d_val Ext2) grouped into n_terms terms by d_term_off.
+ * init: every value (1, 0).  round_msg: flags (first entry of each pair {2y, 2y+1}), their exclusive
+ * scan into d_gid (d_scan_scratch: at least 4 ceil(n / 256) + 8 words), h_msg = the degree-3
+ * message sum_t w_t v (v - 1) eq at 0..3 (4 Ext2, canonical), *h_total = number of pairs.
+ * fold: each pair folded to position d_gid of d_out_idx / d_out_val, new term offsets.  finish:
+ * d_out[t] = the value at position 0 of term t (or 0).  All synchronising. */
+int agl_bool_init_val_ffi(uint64_t *d_val, size_t n);
+int agl_bool_round_msg_ffi(const uint32_t *d_idx, const uint64_t *d_val, const uint32_t *d_term_off,
+                           const uint64_t *d_w, const uint64_t *d_eq, int n_terms, size_t n, uint32_t *d_flags,
+                           uint32_t *d_gid, uint64_t *d_partial, int grid_x, uint32_t *d_scan_scratch,
+                           size_t scan_scratch_len, uint64_t *h_msg, uint32_t *h_total);
+int agl_bool_fold_ffi(const uint32_t *d_idx, const uint64_t *d_val, const uint32_t *d_flags, const uint32_t *d_gid,
+                      const uint32_t *d_term_off, int n_terms, size_t n, uint64_t r0, uint64_t r1, uint32_t total,
+                      int grid_x, uint32_t *d_out_idx, uint64_t *d_out_val, uint32_t *d_new_off);
+int agl_bool_finish_ffi(const uint32_t *d_idx, const uint64_t *d_val, const uint32_t *d_term_off, int n_terms, size_t n,
+                        uint64_t *d_out);
+
 /* ---- Element-wise ops over q and its Ext2 (almost-goldilocks-cuda-rs/src/ffi.rs:95-140;
  * almost wrapper.cu:420-640): canonical outputs, Ext2 = F_q[X]/(X^2 - 3) as (c0, c1), inverses of
  * zero are zero. ---- */
