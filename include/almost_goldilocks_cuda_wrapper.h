@@ -252,6 +252,15 @@ int agl_bool_fold_ffi(const uint32_t *d_idx, const uint64_t *d_val, const uint32
 int agl_bool_finish_ffi(const uint32_t *d_idx, const uint64_t *d_val, const uint32_t *d_term_off, int n_terms, size_t n,
                         uint64_t *d_out);
 
+/* ---- Runtime helpers (almost wrapper.cu:268-279, :327-328, :2989-2997, :3943-3958) ---- */
+int cuda_memcpy_peer(void *dst, int dst_dev, const void *src, int src_dev, size_t size);
+int cuda_enable_peer_access(int peer); /* 0 when enabled or already enabled, else -1 */
+void agl_nvtx_push(const char *name);  /* NVTX profiler range */
+void agl_nvtx_pop(void);
+int agl_i64_to_i32(const int64_t *s, int32_t *d, uint64_t n);   /* d = (i32) s; synchronising */
+int agl_add_i32_i64(int64_t *d, const int32_t *s, uint64_t n);  /* d += (i64) s; synchronising */
+int agl_gauss_low_priority(int on); /* the calling thread's low-priority stream on or off */
+
 /* ---- Element-wise ops over q and its Ext2 (almost-goldilocks-cuda-rs/src/ffi.rs:95-140;
  * almost wrapper.cu:420-640): canonical outputs, Ext2 = F_q[X]/(X^2 - 3) as (c0, c1), inverses of
  * zero are zero. ---- */

@@ -11,6 +11,7 @@
 #include "../../include/goldilocks_cuda_wrapper.h"
 #include "common.cuh"
 #include "host_field.hpp"
+#include <nvtx3/nvToolsExt.h>
 
 namespace gb {
 
@@ -136,6 +137,15 @@ static int e2_batch(const u64* a, const u64* b, u64* r, int n, const char* name)
     return check_launch(name);
 }
 
+__global__ void i64_to_i32_kernel(const int64_t* __restrict__ s, int32_t* __restrict__ d, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        d[i] = (int32_t)s[i];
+}
+__global__ void add_i32_i64_kernel(int64_t* __restrict__ d, const int32_t* __restrict__ s, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        d[i] += (int64_t)s[i];
+}
+
 // Throughput ceiling of this file's Goldilocks multiplication: every thread runs
 // 8 independent chains of `iters` multiplications (no memory traffic).
 __global__ void __launch_bounds__(256) mulmod_probe_kernel(u64* out, int iters) {
@@ -206,6 +216,23 @@ int cuda_get_last_error(void) { return (int)cudaGetLastError(); }
 int cuda_peek_at_last_error(void) { return (int)cudaPeekAtLastError(); }
 int cuda_mem_get_info(size_t* f, size_t* t) { return cudaMemGetInfo(f, t) == cudaSuccess ? 0 : -1; }
 const char* agl_cuda_error_string(int code) { return cudaGetErrorString((cudaError_t)code); }
+// Peer access between devices (almost wrapper.cu:268-279): best effort, an already enabled peer is
+// success.  A one-GPU process has no peer, so enabling one reports -1 as the reference does.
+int cuda_memcpy_peer(void* dst, int dst_dev, const void* src, int src_dev, size_t size) {
+    return cudaMemcpyPeer(dst, dst_dev, src, src_dev, size) == cudaSuccess ? 0 : -1;
+}
+int cuda_enable_peer_access(int peer) {
+    const cudaError_t e = cudaDeviceEnablePeerAccess(peer, 0);
+    if (e == cudaSuccess || e == cudaErrorPeerAccessAlreadyEnabled) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaGetLastError();
+    return -1;
+}
+// Profiler ranges (almost wrapper.cu:327-328)
+void agl_nvtx_push(const char* name) { nvtxRangePushA(name); }
+void agl_nvtx_pop(void) { nvtxRangePop(); }
 int cuda_memset(void* dst, int value, size_t size) {
     return cudaMemsetAsync(dst, value, size, stream()) == cudaSuccess && cudaStreamSynchronize(stream()) == cudaSuccess
                ? 0
@@ -299,4 +326,37 @@ void gb_transcript_challenge_ext2(gb_transcript* t, const char* label, uint64_t 
     out[1] = c.c1;
 }
 
+
+// Integer helpers of the Morpheus authentication path (almost wrapper.cu:3943-3958): d = (i32) s,
+// d += (i64) s.  Synchronising.
+int agl_i64_to_i32(const int64_t* s, int32_t* d, uint64_t n) {
+    if (!n) return 0;
+    i64_to_i32_kernel<<<grid_for(n, 256), 256, 0, stream()>>>(s, d, n);
+    const cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? (int)e : (int)cudaStreamSynchronize(stream());
+}
+int agl_add_i32_i64(int64_t* d, const int32_t* s, uint64_t n) {
+    if (!n) return 0;
+    add_i32_i64_kernel<<<grid_for(n, 256), 256, 0, stream()>>>(d, s, n);
+    const cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? (int)e : (int)cudaStreamSynchronize(stream());
+}
+// The calling thread's low-priority stream toggle of the Gaussian sampler (almost wrapper.cu:2989-2997).
+// The sampler itself is not part of this library; the toggle keeps its contract (0, or -1 when the
+// stream cannot be created).
+static thread_local cudaStream_t t_low_stream = nullptr;
+int agl_gauss_low_priority(int on) {
+    if (on && !t_low_stream) {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (cudaStreamCreateWithPriority(&t_low_stream, cudaStreamNonBlocking, lo) != cudaSuccess) {
+            t_low_stream = nullptr;
+            return -1;
+        }
+    } else if (!on && t_low_stream) {
+        cudaStreamDestroy(t_low_stream);
+        t_low_stream = nullptr;
+    }
+    return 0;
+}
 }  // extern "C"

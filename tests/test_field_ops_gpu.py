@@ -152,3 +152,24 @@ def test_scale_accumulate_conversions_and_zero(gpu_lib):
     L.cuda_sync_mine()
     assert not buf.to_numpy().any()
     assert L.gl_batch_neg(buf.ptr, buf.ptr, -1) == -2
+
+
+def test_runtime_helpers(gpu_lib):
+    """Peer copies on one device, NVTX ranges, the i64/i32 helpers and the stream toggle."""
+    from morpheus_gb300 import _native as N_
+    from morpheus_gb300.memory import DeviceBuffer
+    L = N_.lib()
+    src = DeviceBuffer.from_numpy(np.arange(100, dtype=np.uint64))
+    dst = DeviceBuffer(100)
+    assert L.cuda_memcpy_peer(dst.ptr, 0, src.ptr, 0, 800) == 0
+    assert (dst.to_numpy() == np.arange(100)).all()
+    assert L.cuda_enable_peer_access(0) == -1  # a device is not its own peer
+    L.agl_nvtx_push(b"range")
+    L.agl_nvtx_pop()
+    s = DeviceBuffer.from_numpy(np.array([1, -2, 2**40 + 5, -(2**33)], np.int64))
+    d = DeviceBuffer(4, np.int32)
+    assert L.agl_i64_to_i32(s.ptr, d.ptr, 4) == 0
+    assert d.to_numpy().tolist() == [1, -2, 5, 0]
+    assert L.agl_add_i32_i64(s.ptr, d.ptr, 4) == 0
+    assert s.to_numpy().tolist() == [2, -4, 2**40 + 10, -(2**33)]
+    assert L.agl_gauss_low_priority(1) == 0 and L.agl_gauss_low_priority(0) == 0
