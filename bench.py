@@ -40,6 +40,22 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
 
 
+def max_over_ranks(values, dist, device):
+    """Each value's maximum over the ranks (the slowest rank's time), through the default process
+    group when dist (nccl on the GPUs, gloo in the CPU tests)."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if dist:
+        import torch.distributed as tdist
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_throughput(world, ms_max):
+    """Proofs per second of world replicas that each prove one proof per step of ms_max."""
+    return world * 1000.0 / ms_max
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -631,13 +647,8 @@ def main():
             c.open_ext2(pt, table, Transcript(b"bf-open"), QUERIES)
             e2e_times.append(time.perf_counter() - t0)
             del c
-    ms = statistics.mean(times)
-    tmax = torch.tensor([ms], device=dev)
-    if dist:
-        tdist.all_reduce(tmax, op=tdist.ReduceOp.MAX)
-    ms_max = float(tmax.item())
-    value = world * 1000.0 / ms_max
-    e2e_ms = statistics.mean(e2e_times) * 1e3
+    ms_max, e2e_ms = max_over_ranks([statistics.mean(times), statistics.mean(e2e_times) * 1e3], dist, dev)
+    value = replica_throughput(world, ms_max)
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -707,7 +718,7 @@ def main():
             "config": {"workload": f"basefold commit+open_ext2, 2^{n} evals, rate 1/2, {QUERIES} queries",
                        "num_vars": n, "log_rate": LOG_RATE, "num_queries": QUERIES, "table_seed": TABLE_SEED,
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
-            "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "proofs/s", "h2d_bytes_per_step": 8 << n,
+            "e2e": {"value": replica_throughput(world, e2e_ms), "unit": "proofs/s", "h2d_bytes_per_step": 8 << n,
                     "d2h_bytes_per_step": 8 * int(proof_len)},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
