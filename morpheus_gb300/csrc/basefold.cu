@@ -295,8 +295,8 @@ __global__ void __launch_bounds__(RED_THREADS) open_round_kernel(const u64* __re
 // Codeword fold of one round fused with hashing the folded codeword's leaves:
 // leaf i = P2(f[2i], f[2i+1]) with f[k] = fold(cw[2k], cw[2k+1], table[k]).
 // BASE_IN: the input codeword is the base-field committed one (mixed fold).
-template <bool BASE_IN>
-__global__ void __launch_bounds__(128) fold_hash_leaves_kernel(const u64* __restrict__ cw, const u64* __restrict__ tab,
+template <bool BASE_IN, int T>
+__global__ void P2_BOUNDS(T) fold_hash_leaves_kernel(const u64* __restrict__ cw, const u64* __restrict__ tab,
                                                                u64 c0, u64 c1, u64* __restrict__ folded,
                                                                u64* __restrict__ tree, size_t leaves) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -401,7 +401,9 @@ __global__ void __launch_bounds__(RED_THREADS) bo_round_kernel(const u64* __rest
 }
 
 // Combined Ext2 codeword sum_j scalar_j cw_j fused with its leaf hashes: leaf i = P2(ccw[2i] || ccw[2i+1]).
-__global__ void __launch_bounds__(128) bo_combine_leaves_kernel(const BoTerm* __restrict__ terms, int num_terms,
+// (Up to 64 registers: the four three-word accumulators do not fit the P2_BOUNDS budget.)
+template <int T>
+__global__ void __launch_bounds__(T, (T) == 512 ? 2 : 4) bo_combine_leaves_kernel(const BoTerm* __restrict__ terms, int num_terms,
                                                                 u64* __restrict__ ccw, u64* __restrict__ tree,
                                                                 size_t leaves) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -714,12 +716,22 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
                 else
                     fold_hash_leaves_coop_kernel<false><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
                                                                           leaves);
-            } else if (base_in) {
-                fold_hash_leaves_kernel<true><<<grid_for(leaves, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
-                                                                                     ftree[rd], leaves);
             } else {
-                fold_hash_leaves_kernel<false><<<grid_for(leaves, 128), 128, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
-                                                                                      ftree[rd], leaves);
+                const bool wide = p2_wide(leaves);
+                const int th = wide ? P2_WIDE : P2_NARROW;
+                const unsigned g = grid_for(leaves, th);
+                if (base_in && wide)
+                    fold_hash_leaves_kernel<true, P2_WIDE><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                            ftree[rd], leaves);
+                else if (base_in)
+                    fold_hash_leaves_kernel<true, P2_NARROW><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                              ftree[rd], leaves);
+                else if (wide)
+                    fold_hash_leaves_kernel<false, P2_WIDE><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                             ftree[rd], leaves);
+                else
+                    fold_hash_leaves_kernel<false, P2_NARROW><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                               ftree[rd], leaves);
             }
             GB_LAUNCH_CHECK("fold_hash_leaves_kernel");
             RC_TRY(merkle_build_from_leaves(ftree[rd], leaves, rec + 8));
@@ -1001,7 +1013,12 @@ static int batch_open_ext2(BfCommitment* const* comms, int num_comms, const u64*
     RC_TRY(m.alloc(&ieq, N * 16));
     GB_CUDA_TRY(cudaMemcpyAsync(d_cw_terms, cw_terms.data(), E * sizeof(BoTerm), cudaMemcpyHostToDevice, s));
     GB_CUDA_TRY(cudaMemcpyAsync(d_ev_terms, ev_terms.data(), E * sizeof(BoTerm), cudaMemcpyHostToDevice, s));
-    bo_combine_leaves_kernel<<<grid_for(leaves0, 128), 128, 0, s>>>(d_cw_terms, num_evals, ccw, ctree, leaves0);
+    if (p2_wide(leaves0))
+        bo_combine_leaves_kernel<P2_WIDE><<<grid_for(leaves0, P2_WIDE), P2_WIDE, 0, s>>>(d_cw_terms, num_evals, ccw,
+                                                                                       ctree, leaves0);
+    else
+        bo_combine_leaves_kernel<P2_NARROW><<<grid_for(leaves0, P2_NARROW), P2_NARROW, 0, s>>>(d_cw_terms, num_evals,
+                                                                                             ccw, ctree, leaves0);
     GB_LAUNCH_CHECK("bo_combine_leaves_kernel");
     bo_combine_evals_kernel<<<grid_for(N, 256), 256, 0, s>>>(d_ev_terms, num_evals, cev, N);
     GB_LAUNCH_CHECK("bo_combine_evals_kernel");

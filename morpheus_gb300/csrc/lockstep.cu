@@ -67,6 +67,20 @@ __device__ __forceinline__ int ls_find(const LsSeg* __restrict__ segs, int nseg,
     __syncthreads();                                          \
     const LsSeg sg = segs[s_seg];
 
+// CTA size of a segmented Poseidon2 launch, and each segment's first block for it: the wide
+// shape (P2_BOUNDS) when the launch is large and its segments average at least one wide CTA.
+static int ls_p2_assign(LsSeg* hs, int cnt, u64& nb) {
+    u64 total = 0;
+    for (int k = 0; k < cnt; k++) total += hs[k].items;
+    const int T = (p2_wide(total) && total >= (u64)cnt * P2_WIDE) ? P2_WIDE : P2_NARROW;
+    nb = 0;
+    for (int k = 0; k < cnt; k++) {
+        hs[k].block0 = nb;
+        nb += hs[k].items ? (hs[k].items + T - 1) / T : 1;
+    }
+    return T;
+}
+
 // round 0 oracle partials: a = bh (base), b = eq (Ext2), items = pairs
 __global__ void __launch_bounds__(LS_RED_THREADS) ls_round0_kernel(const LsSeg* __restrict__ segs, int nseg,
                                                                    u64* __restrict__ partials) {
@@ -122,8 +136,8 @@ __global__ void ls_reduce_kernel(const LsSeg* __restrict__ segs, int nseg, const
 }
 
 // codeword fold + leaf hash: a = codeword in, b = table level, c = folded out, d = tree leaves
-template <bool BASE_IN>
-__global__ void __launch_bounds__(LS_THREADS) ls_fold_hash_kernel(const LsSeg* __restrict__ segs, int nseg) {
+template <bool BASE_IN, int T>
+__global__ void P2_BOUNDS(T) ls_fold_hash_kernel(const LsSeg* __restrict__ segs, int nseg) {
     LS_SEG_PROLOGUE
     const u64 i = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
     if (i >= sg.items) return;
@@ -137,7 +151,8 @@ __global__ void __launch_bounds__(LS_THREADS) ls_fold_hash_kernel(const LsSeg* _
 }
 
 // one Merkle layer: a = children, c = parents
-__global__ void __launch_bounds__(LS_THREADS) ls_merkle_level_kernel(const LsSeg* __restrict__ segs, int nseg) {
+template <int T>
+__global__ void P2_BOUNDS(T) ls_merkle_level_kernel(const LsSeg* __restrict__ segs, int nseg) {
     LS_SEG_PROLOGUE
     const u64 j = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
     if (j >= sg.items) return;
@@ -194,7 +209,8 @@ __global__ void __launch_bounds__(LS_THREADS) ls_bitrev_replicate_kernel(const L
 }
 
 // leaf i = P2(cw[2i], cw[2i+1], 0, ...) for the first copy's leaves: a = codeword, d = tree
-__global__ void __launch_bounds__(LS_THREADS) ls_hash_leaves_kernel(const LsSeg* __restrict__ segs, int nseg) {
+template <int T>
+__global__ void P2_BOUNDS(T) ls_hash_leaves_kernel(const LsSeg* __restrict__ segs, int nseg) {
     LS_SEG_PROLOGUE
     const u64 i = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
     if (i >= sg.items) return;
@@ -434,10 +450,16 @@ class LsRunner {
                                   ch[mid[m]].c0, ch[mid[m]].c1, leaves, nb};
                     nb += blocks(leaves);
                 }
+                const int th = ls_p2_assign(hs, (int)mid.size(), nb);
                 ds = upload(hs, (int)mid.size());
                 if (!ds) return GB_ECUDA;
-                if (rd == 0) ls_fold_hash_kernel<true><<<(unsigned)nb, LS_THREADS, 0, s>>>(ds, (int)mid.size());
-                else ls_fold_hash_kernel<false><<<(unsigned)nb, LS_THREADS, 0, s>>>(ds, (int)mid.size());
+                if (th == P2_WIDE) {
+                    if (rd == 0) ls_fold_hash_kernel<true, P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, (int)mid.size());
+                    else ls_fold_hash_kernel<false, P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, (int)mid.size());
+                } else {
+                    if (rd == 0) ls_fold_hash_kernel<true, P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, (int)mid.size());
+                    else ls_fold_hash_kernel<false, P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, (int)mid.size());
+                }
                 GB_LAUNCH_CHECK("ls_fold_hash_kernel");
                 // Merkle layers, all trees at once
                 for (int lvl = 0;; lvl++) {
@@ -459,9 +481,11 @@ class LsRunner {
                         unslot();
                         break;
                     }
+                    const int th = ls_p2_assign(hs, cnt, nb);
                     ds = upload(hs, cnt);
                     if (!ds) return GB_ECUDA;
-                    ls_merkle_level_kernel<<<(unsigned)nb, LS_THREADS, 0, s>>>(ds, cnt);
+                    if (th == P2_WIDE) ls_merkle_level_kernel<P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
+                    else ls_merkle_level_kernel<P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
                     GB_LAUNCH_CHECK("ls_merkle_level_kernel");
                 }
                 hs = next_slot(); if (!hs) return GB_EINVAL;
@@ -684,12 +708,19 @@ class LsCommitter {
         GB_CUDA_TRY(cudaMallocHost(&h_segs_, cap * sizeof(LsSeg)));
         GB_CUDA_TRY(cudaMallocHost(&h_recs_, (size_t)nj * LS_REC * 8));
         size_t used = 0;
-        auto launch = [&](auto kernel, int count, u64 nb) -> int {
+        auto launch_t = [&](auto kernel, int count, u64 nb, int threads) -> int {
             LsSeg* hs = h_segs_ + used;
             GB_CUDA_TRY(cudaMemcpyAsync(d_segs_ + used, hs, (size_t)count * sizeof(LsSeg), cudaMemcpyHostToDevice, s));
-            kernel<<<(unsigned)nb, LS_THREADS, 0, s>>>(d_segs_ + used, count);
+            kernel<<<(unsigned)nb, threads, 0, s>>>(d_segs_ + used, count);
             used += count;
             return check_launch("ls_commit");
+        };
+        auto launch = [&](auto kernel, int count, u64 nb) -> int { return launch_t(kernel, count, nb, LS_THREADS); };
+        // a Poseidon2 kernel (template on its CTA size) over the segments at h_segs_ + used
+        auto launch_p2 = [&](auto wide_kernel, auto narrow_kernel, int count) -> int {
+            u64 nb = 0;
+            const int th = ls_p2_assign(h_segs_ + used, count, nb);
+            return th == P2_WIDE ? launch_t(wide_kernel, count, nb, th) : launch_t(narrow_kernel, count, nb, th);
         };
         // 1. transform passes: pass p covers bits [4p, 4p + K) with K = min(4, n - 4p)
         for (int b = 0; b < maxn; b += 4) {
@@ -729,7 +760,7 @@ class LsCommitter {
                 hs[k] = LsSeg{J[k].com.d_codeword, nullptr, nullptr, J[k].com.d_tree, 0, 0, sub, nb};
                 nb += blocks(sub);
             }
-            LS_RC(launch(ls_hash_leaves_kernel, nj, nb));
+            LS_RC(launch_p2(ls_hash_leaves_kernel<P2_WIDE>, ls_hash_leaves_kernel<P2_NARROW>, nj));
         }
         // 4. the first copy's layers (full-tree offsets: layer l holds N >> l nodes)
         for (int l = 0;; l++) {
@@ -747,7 +778,7 @@ class LsCommitter {
                 nb += blocks(parents);
             }
             if (!cnt) break;
-            LS_RC(launch(ls_merkle_level_kernel, cnt, nb));
+            LS_RC(launch_p2(ls_merkle_level_kernel<P2_WIDE>, ls_merkle_level_kernel<P2_NARROW>, cnt));
         }
         // 5. the second copy on every layer
         {
@@ -775,7 +806,7 @@ class LsCommitter {
                 hs[k] = LsSeg{layer, nullptr, layer + 8, nullptr, 0, 0, 1, nb};
                 nb += 1;
             }
-            LS_RC(launch(ls_merkle_level_kernel, nj, nb));
+            LS_RC(launch_p2(ls_merkle_level_kernel<P2_WIDE>, ls_merkle_level_kernel<P2_NARROW>, nj));
             hs = h_segs_ + used;
             for (int k = 0; k < nj; k++) {
                 const u64 N = (u64)1 << J[k].n;

@@ -15,8 +15,8 @@ namespace gb {
 constexpr int MK_THREADS = 128;
 constexpr int MK_COOP_THREADS = 256;
 
-__global__ void __launch_bounds__(MK_THREADS) merkle_level_kernel(const u64* __restrict__ in, u64* __restrict__ out,
-                                                                  size_t nodes) {
+template <int T>
+__global__ void P2_BOUNDS(T) merkle_level_kernel(const u64* __restrict__ in, u64* __restrict__ out, size_t nodes) {
     size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (j >= nodes) return;
     u64 s[8];
@@ -110,8 +110,8 @@ __global__ void __launch_bounds__(MK_COOP_THREADS) hash_leaves_coop_kernel(const
     if (live && l < 4) tree[4 * g + l] = x;
 }
 
-__global__ void __launch_bounds__(MK_THREADS) hash_leaves_gl_kernel(const u64* __restrict__ cw, u64* __restrict__ tree,
-                                                                    size_t leaves) {
+template <int T>
+__global__ void P2_BOUNDS(T) hash_leaves_gl_kernel(const u64* __restrict__ cw, u64* __restrict__ tree, size_t leaves) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= leaves) return;
     ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(cw) + i);
@@ -120,8 +120,8 @@ __global__ void __launch_bounds__(MK_THREADS) hash_leaves_gl_kernel(const u64* _
     st_digest(tree + 4 * i, s);
 }
 
-__global__ void __launch_bounds__(MK_THREADS) hash_leaves_ext2_kernel(const u64* __restrict__ cw, u64* __restrict__ tree,
-                                                                      size_t leaves) {
+template <int T>
+__global__ void P2_BOUNDS(T) hash_leaves_ext2_kernel(const u64* __restrict__ cw, u64* __restrict__ tree, size_t leaves) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= leaves) return;
     u64 s[8];
@@ -146,7 +146,10 @@ size_t mk_coop_below() { return t_coop_below; }
 static int merkle_level(const u64* in, u64* out, size_t half) {
     cudaStream_t s = stream();
     if (half >= mk_coop_below()) {
-        merkle_level_kernel<<<grid_for(half, MK_THREADS), MK_THREADS, 0, s>>>(in, out, half);
+        if (p2_wide(half))
+            merkle_level_kernel<P2_WIDE><<<grid_for(half, P2_WIDE), P2_WIDE, 0, s>>>(in, out, half);
+        else
+            merkle_level_kernel<P2_NARROW><<<grid_for(half, P2_NARROW), P2_NARROW, 0, s>>>(in, out, half);
         return check_launch("merkle_level_kernel");
     }
     int threads = coop_threads(half);
@@ -185,7 +188,10 @@ int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves) {
         hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 2);
         return check_launch("hash_leaves_coop_kernel");
     }
-    hash_leaves_gl_kernel<<<grid_for(leaves, MK_THREADS), MK_THREADS, 0, stream()>>>(cw, tree, leaves);
+    if (p2_wide(leaves))
+        hash_leaves_gl_kernel<P2_WIDE><<<grid_for(leaves, P2_WIDE), P2_WIDE, 0, stream()>>>(cw, tree, leaves);
+    else
+        hash_leaves_gl_kernel<P2_NARROW><<<grid_for(leaves, P2_NARROW), P2_NARROW, 0, stream()>>>(cw, tree, leaves);
     return check_launch("hash_leaves_gl_kernel");
 }
 
@@ -195,7 +201,10 @@ int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves) {
         hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 4);
         return check_launch("hash_leaves_coop_kernel");
     }
-    hash_leaves_ext2_kernel<<<grid_for(leaves, MK_THREADS), MK_THREADS, 0, stream()>>>(cw, tree, leaves);
+    if (p2_wide(leaves))
+        hash_leaves_ext2_kernel<P2_WIDE><<<grid_for(leaves, P2_WIDE), P2_WIDE, 0, stream()>>>(cw, tree, leaves);
+    else
+        hash_leaves_ext2_kernel<P2_NARROW><<<grid_for(leaves, P2_NARROW), P2_NARROW, 0, stream()>>>(cw, tree, leaves);
     return check_launch("hash_leaves_ext2_kernel");
 }
 
@@ -228,7 +237,8 @@ int merkle_tree_gl_replicated(const u64* cw, u64* tree, size_t leaves, int copie
     return merkle_build_from_leaves(tree + off, layer_nodes);
 }
 
-__global__ void permute_batch_kernel(const u64* __restrict__ in, u64* __restrict__ out, int n) {
+template <int T>
+__global__ void P2_BOUNDS(T) permute_batch_kernel(const u64* __restrict__ in, u64* __restrict__ out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     u64 s[8];
@@ -239,7 +249,9 @@ __global__ void permute_batch_kernel(const u64* __restrict__ in, u64* __restrict
     for (int k = 0; k < 8; k++) out[8 * (size_t)i + k] = s[k];
 }
 
-__global__ void compress_batch_kernel(const u64* __restrict__ l, const u64* __restrict__ r, u64* __restrict__ out, int n) {
+template <int T>
+__global__ void P2_BOUNDS(T) compress_batch_kernel(const u64* __restrict__ l, const u64* __restrict__ r,
+                                                   u64* __restrict__ out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     u64 s[8];
@@ -276,14 +288,21 @@ size_t gb_get_merkle_top_nodes(void) { return t_top_nodes; }
 int poseidon2_hash_batch_ffi(const uint64_t* d_input, uint64_t* d_output, int n) {
     if (n < 0) return GB_EINVAL;
     if (n == 0) return GB_OK;
-    permute_batch_kernel<<<grid_for(n, MK_THREADS), MK_THREADS, 0, stream()>>>(d_input, d_output, n);
+    if (p2_wide((size_t)n))
+        permute_batch_kernel<P2_WIDE><<<grid_for(n, P2_WIDE), P2_WIDE, 0, stream()>>>(d_input, d_output, n);
+    else
+        permute_batch_kernel<P2_NARROW><<<grid_for(n, P2_NARROW), P2_NARROW, 0, stream()>>>(d_input, d_output, n);
     return check_launch("poseidon2_hash_batch_ffi");
 }
 
 int poseidon2_compress_batch_ffi(const uint64_t* d_left, const uint64_t* d_right, uint64_t* d_output, int n) {
     if (n < 0) return GB_EINVAL;
     if (n == 0) return GB_OK;
-    compress_batch_kernel<<<grid_for(n, MK_THREADS), MK_THREADS, 0, stream()>>>(d_left, d_right, d_output, n);
+    if (p2_wide((size_t)n))
+        compress_batch_kernel<P2_WIDE><<<grid_for(n, P2_WIDE), P2_WIDE, 0, stream()>>>(d_left, d_right, d_output, n);
+    else
+        compress_batch_kernel<P2_NARROW><<<grid_for(n, P2_NARROW), P2_NARROW, 0, stream()>>>(d_left, d_right, d_output,
+                                                                                            n);
     return check_launch("poseidon2_compress_batch_ffi");
 }
 
@@ -295,7 +314,10 @@ int poseidon2_merkle_layer_ffi(const uint64_t* d_input, uint64_t* d_output, int 
         merkle_level_scalar_kernel<<<grid_for(n, MK_THREADS), MK_THREADS, 0, stream()>>>(d_input, d_output, (size_t)n);
         return check_launch("poseidon2_merkle_layer_ffi");
     }
-    merkle_level_kernel<<<grid_for(n, MK_THREADS), MK_THREADS, 0, stream()>>>(d_input, d_output, (size_t)n);
+    if (p2_wide((size_t)n))
+        merkle_level_kernel<P2_WIDE><<<grid_for(n, P2_WIDE), P2_WIDE, 0, stream()>>>(d_input, d_output, (size_t)n);
+    else
+        merkle_level_kernel<P2_NARROW><<<grid_for(n, P2_NARROW), P2_NARROW, 0, stream()>>>(d_input, d_output, (size_t)n);
     return check_launch("poseidon2_merkle_layer_ffi");
 }
 

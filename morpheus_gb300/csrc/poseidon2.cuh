@@ -231,19 +231,24 @@ __device__ __forceinline__ glw shfl_xor_glw(glw v, int m) {
     return r;
 }
 
-// Internal rounds: the 8-lane sum is kept lazy (64 bits + carries) through the all-reduce and
-// enters the lane's multiply-add unreduced; lane 0 also folds in the next round's constant.
+// Internal rounds: the sum of lanes 1..7 is all-reduced while lane 0 computes its S-box (lane 0
+// adds 0), then lane 0's S-box output is broadcast and added, so the shuffles leave the S-box
+// chain.  The sum stays lazy (64 bits + carries) and enters the lane's multiply-add unreduced;
+// lane 0 also folds in the next round's constant.
 __device__ __forceinline__ u64 p2_permute_coop(u64 x, int l, const P2Lane& c) {
+    const int lane0 = (threadIdx.x & 31) & ~7;
 #pragma unroll
     for (int r = 0; r < 4; r++) x = p2_coop_external_linear(p2_sbox_lat(gl_add(x, c.ext[r])));
     if (l == 0) x = gl_add(x, c_p2_int[0]);
 #pragma unroll
     for (int r = 0; r < 22; r++) {
-        if (l == 0) x = p2_sbox_lat(x);
-        glw t = glw_of(x);
+        glw t = glw_of(l == 0 ? 0ull : x);
         t = glw_add(t, shfl_xor_glw(t, 1));
         t = glw_add(t, shfl_xor_glw(t, 2));
         t = glw_add(t, shfl_xor_glw(t, 4));
+        const u64 y = p2_sbox_lat(x);
+        if (l == 0) x = y;
+        t = glw_add(t, shfl_idx64(y, lane0));
         if (l == 0 && r < 21) t = glw_add(t, c_p2_int[r + 1]);
         x = gl_mul_add(x, c.diag, t);
     }
