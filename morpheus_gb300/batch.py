@@ -277,7 +277,7 @@ def mixed_workload(count, seed, min_vars=10, max_vars=20, degrees=(2, 3, 4), num
     return out
 
 
-def autotune(table, master_seed, instances, workers=(8, 12, 16, 24), coop_thresholds=(32768, 4096),
+def autotune(table, master_seed, instances, workers=(8, 12, 16, 24), coop_thresholds=(16384, 4096),
              top_nodes=(16, 256, 2048), hbm_budget=64 << 30):
     """Schedule (workers, cooperative threshold, top size) for this batch by coordinate search:
     after a warm-up run, the worker count at the default Merkle schedule, then the

@@ -310,6 +310,33 @@ __global__ void P2_BOUNDS(T) fold_hash_leaves_kernel(const u64* __restrict__ cw,
     st_digest(tree + 4 * i, s);
 }
 
+// Same in the pair form (p2_permute_pair): lane 0 of a pair folds and holds the leaf's four
+// elements, lane 1 the zero half of the state.
+template <bool BASE_IN, int T>
+__global__ void P2_PAIR_BOUNDS(T) fold_hash_leaves_pair_kernel(const u64* __restrict__ cw,
+                                                               const u64* __restrict__ tab, u64 c0, u64 c1,
+                                                               u64* __restrict__ folded, u64* __restrict__ tree,
+                                                               size_t leaves) {
+    const size_t i = (blockIdx.x * (size_t)T + threadIdx.x) >> 1;
+    const int h = threadIdx.x & 1;
+    const bool live = i < leaves;
+    u64 s[4] = {0, 0, 0, 0};
+    if (h == 0) {
+        e2 f0, f1;
+        fold_leaf_item<BASE_IN>(cw, tab, live ? i : 0, c0, c1, f0, f1);
+        if (live) {
+            e2_st(folded + 4 * i, f0);
+            e2_st(folded + 4 * i + 2, f1);
+        }
+        s[0] = f0.c0;
+        s[1] = f0.c1;
+        s[2] = f1.c0;
+        s[3] = f1.c1;
+    }
+    p2_permute_pair(s, h);
+    if (live && h == 0) st_digest(tree + 4 * i, s);
+}
+
 // Same with 8 lanes per leaf (latency-bound rounds, see mk_coop_below): every lane of a
 // group folds both elements, lane l takes state element l, lanes 0..3 store.
 template <bool BASE_IN>
@@ -707,7 +734,23 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
         size_t pairs = L >> (rd + 1);
         if (rd < n - 1) {
             size_t leaves = pairs / 2;
-            if (leaves < mk_coop_below()) {
+            const P2Form form = p2_form(leaves);
+            if (form == P2_PAIR) {
+                const int th = p2_pair_threads(leaves);
+                const unsigned g = grid_for(2 * leaves, th);
+                if (base_in && th == 256)
+                    fold_hash_leaves_pair_kernel<true, 256><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                             ftree[rd], leaves);
+                else if (base_in)
+                    fold_hash_leaves_pair_kernel<true, 128><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                             ftree[rd], leaves);
+                else if (th == 256)
+                    fold_hash_leaves_pair_kernel<false, 256><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                              ftree[rd], leaves);
+                else
+                    fold_hash_leaves_pair_kernel<false, 128><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                              ftree[rd], leaves);
+            } else if (form == P2_COOP) {
                 int th = coop_threads(leaves);
                 unsigned g = grid_for(leaves * 8, th);
                 if (base_in)
@@ -717,21 +760,13 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
                     fold_hash_leaves_coop_kernel<false><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
                                                                           leaves);
             } else {
-                const bool wide = p2_wide(leaves);
-                const int th = wide ? P2_WIDE : P2_NARROW;
-                const unsigned g = grid_for(leaves, th);
-                if (base_in && wide)
-                    fold_hash_leaves_kernel<true, P2_WIDE><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
-                                                                            ftree[rd], leaves);
-                else if (base_in)
-                    fold_hash_leaves_kernel<true, P2_NARROW><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
-                                                                              ftree[rd], leaves);
-                else if (wide)
-                    fold_hash_leaves_kernel<false, P2_WIDE><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
-                                                                             ftree[rd], leaves);
+                const unsigned g = grid_for(leaves, P2_WIDE);
+                if (base_in)
+                    fold_hash_leaves_kernel<true, P2_WIDE><<<g, P2_WIDE, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                                 ftree[rd], leaves);
                 else
-                    fold_hash_leaves_kernel<false, P2_NARROW><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
-                                                                               ftree[rd], leaves);
+                    fold_hash_leaves_kernel<false, P2_WIDE><<<g, P2_WIDE, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd],
+                                                                                  ftree[rd], leaves);
             }
             GB_LAUNCH_CHECK("fold_hash_leaves_kernel");
             RC_TRY(merkle_build_from_leaves(ftree[rd], leaves, rec + 8));

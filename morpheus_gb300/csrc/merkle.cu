@@ -38,6 +38,20 @@ __global__ void __launch_bounds__(MK_THREADS) merkle_level_scalar_kernel(const u
     for (int k = 0; k < 4; k++) out[4 * j + k] = s[k];
 }
 
+// One parent per lane pair (p2_permute_pair): lane h loads child 2j + h.  Pairs past the end
+// compute parent 0 and store nothing: their warp still takes part in the exchanges.
+template <int T>
+__global__ void P2_PAIR_BOUNDS(T) merkle_level_pair_kernel(const u64* __restrict__ in, u64* __restrict__ out,
+                                                           size_t nodes) {
+    const size_t j = (blockIdx.x * (size_t)T + threadIdx.x) >> 1;
+    const int h = threadIdx.x & 1;
+    const bool live = j < nodes;
+    u64 s[4];
+    ld_digest(in + 8 * (live ? j : 0) + 4 * h, s);
+    p2_permute_pair(s, h);
+    if (live && h == 0) st_digest(out + 4 * j, s);
+}
+
 // One parent per 8-lane group.  Groups past the end compute node 0 and store nothing:
 // their warp still has to take part in the shuffles.
 __global__ void __launch_bounds__(MK_COOP_THREADS) merkle_level_coop_kernel(const u64* __restrict__ in,
@@ -97,6 +111,30 @@ __global__ void replicate_layers_kernel(u64* __restrict__ tree, size_t leaves, s
     }
 }
 
+// Leaf hashes in the pair form: lane 0 of a pair holds the leaf's `width` (2 or 4) elements,
+// lane 1 the zero half of the state.
+template <int T>
+__global__ void P2_PAIR_BOUNDS(T) hash_leaves_pair_kernel(const u64* __restrict__ cw, u64* __restrict__ tree,
+                                                          size_t leaves, int width) {
+    const size_t i = (blockIdx.x * (size_t)T + threadIdx.x) >> 1;
+    const int h = threadIdx.x & 1;
+    const bool live = i < leaves;
+    u64 s[4] = {0, 0, 0, 0};
+    if (h == 0) {
+        const ulonglong2* p = reinterpret_cast<const ulonglong2*>(cw + (size_t)width * (live ? i : 0));
+        ulonglong2 v = __ldg(p);
+        s[0] = v.x;
+        s[1] = v.y;
+        if (width == 4) {
+            v = __ldg(p + 1);
+            s[2] = v.x;
+            s[3] = v.y;
+        }
+    }
+    p2_permute_pair(s, h);
+    if (live && h == 0) st_digest(tree + 4 * i, s);
+}
+
 __global__ void __launch_bounds__(MK_COOP_THREADS) hash_leaves_coop_kernel(const u64* __restrict__ cw,
                                                                          u64* __restrict__ tree, size_t leaves,
                                                                          int width) {
@@ -145,12 +183,17 @@ size_t mk_coop_below() { return t_coop_below; }
 // one layer: `half` parents from the 2*half digests at `in`
 static int merkle_level(const u64* in, u64* out, size_t half) {
     cudaStream_t s = stream();
-    if (half >= mk_coop_below()) {
-        if (p2_wide(half))
-            merkle_level_kernel<P2_WIDE><<<grid_for(half, P2_WIDE), P2_WIDE, 0, s>>>(in, out, half);
-        else
-            merkle_level_kernel<P2_NARROW><<<grid_for(half, P2_NARROW), P2_NARROW, 0, s>>>(in, out, half);
+    const P2Form f = p2_form(half);
+    if (f == P2_ONE) {
+        merkle_level_kernel<P2_WIDE><<<grid_for(half, P2_WIDE), P2_WIDE, 0, s>>>(in, out, half);
         return check_launch("merkle_level_kernel");
+    }
+    if (f == P2_PAIR) {
+        if (p2_pair_threads(half) == 256)
+            merkle_level_pair_kernel<256><<<grid_for(2 * half, 256), 256, 0, s>>>(in, out, half);
+        else
+            merkle_level_pair_kernel<128><<<grid_for(2 * half, 128), 128, 0, s>>>(in, out, half);
+        return check_launch("merkle_level_pair_kernel");
     }
     int threads = coop_threads(half);
     merkle_level_coop_kernel<<<grid_for(half * 8, threads), threads, 0, s>>>(in, out, half);
@@ -183,28 +226,38 @@ int merkle_build_from_leaves(u64* tree, size_t leaves, u64* root_out) {
 }
 
 int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves) {
-    if (leaves < mk_coop_below()) {
+    const P2Form f = p2_form(leaves);
+    if (f == P2_COOP) {
         int t = coop_threads(leaves);
         hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 2);
         return check_launch("hash_leaves_coop_kernel");
     }
-    if (p2_wide(leaves))
-        hash_leaves_gl_kernel<P2_WIDE><<<grid_for(leaves, P2_WIDE), P2_WIDE, 0, stream()>>>(cw, tree, leaves);
-    else
-        hash_leaves_gl_kernel<P2_NARROW><<<grid_for(leaves, P2_NARROW), P2_NARROW, 0, stream()>>>(cw, tree, leaves);
+    if (f == P2_PAIR) {
+        if (p2_pair_threads(leaves) == 256)
+            hash_leaves_pair_kernel<256><<<grid_for(2 * leaves, 256), 256, 0, stream()>>>(cw, tree, leaves, 2);
+        else
+            hash_leaves_pair_kernel<128><<<grid_for(2 * leaves, 128), 128, 0, stream()>>>(cw, tree, leaves, 2);
+        return check_launch("hash_leaves_pair_kernel");
+    }
+    hash_leaves_gl_kernel<P2_WIDE><<<grid_for(leaves, P2_WIDE), P2_WIDE, 0, stream()>>>(cw, tree, leaves);
     return check_launch("hash_leaves_gl_kernel");
 }
 
 int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves) {
-    if (leaves < mk_coop_below()) {
+    const P2Form f = p2_form(leaves);
+    if (f == P2_COOP) {
         int t = coop_threads(leaves);
         hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 4);
         return check_launch("hash_leaves_coop_kernel");
     }
-    if (p2_wide(leaves))
-        hash_leaves_ext2_kernel<P2_WIDE><<<grid_for(leaves, P2_WIDE), P2_WIDE, 0, stream()>>>(cw, tree, leaves);
-    else
-        hash_leaves_ext2_kernel<P2_NARROW><<<grid_for(leaves, P2_NARROW), P2_NARROW, 0, stream()>>>(cw, tree, leaves);
+    if (f == P2_PAIR) {
+        if (p2_pair_threads(leaves) == 256)
+            hash_leaves_pair_kernel<256><<<grid_for(2 * leaves, 256), 256, 0, stream()>>>(cw, tree, leaves, 4);
+        else
+            hash_leaves_pair_kernel<128><<<grid_for(2 * leaves, 128), 128, 0, stream()>>>(cw, tree, leaves, 4);
+        return check_launch("hash_leaves_pair_kernel");
+    }
+    hash_leaves_ext2_kernel<P2_WIDE><<<grid_for(leaves, P2_WIDE), P2_WIDE, 0, stream()>>>(cw, tree, leaves);
     return check_launch("hash_leaves_ext2_kernel");
 }
 
@@ -314,11 +367,7 @@ int poseidon2_merkle_layer_ffi(const uint64_t* d_input, uint64_t* d_output, int 
         merkle_level_scalar_kernel<<<grid_for(n, MK_THREADS), MK_THREADS, 0, stream()>>>(d_input, d_output, (size_t)n);
         return check_launch("poseidon2_merkle_layer_ffi");
     }
-    if (p2_wide((size_t)n))
-        merkle_level_kernel<P2_WIDE><<<grid_for(n, P2_WIDE), P2_WIDE, 0, stream()>>>(d_input, d_output, (size_t)n);
-    else
-        merkle_level_kernel<P2_NARROW><<<grid_for(n, P2_NARROW), P2_NARROW, 0, stream()>>>(d_input, d_output, (size_t)n);
-    return check_launch("poseidon2_merkle_layer_ffi");
+    return merkle_level(d_input, d_output, (size_t)n);
 }
 
 int poseidon2_merkle_tree_gl_ffi(const uint64_t* d_codeword, uint64_t* d_tree, int num_leaves) {

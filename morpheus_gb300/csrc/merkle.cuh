@@ -49,7 +49,7 @@ __device__ __forceinline__ void ld_digest(const u64* p, u64* s) {
 // permutation is a long serial chain, so those launches use 8 lanes per state (at about
 // half the throughput of one state per thread).  The threshold belongs to the calling
 // thread (gb_set_coop_threshold); many concurrent proofs favour a lower one.
-constexpr size_t MK_COOP_BELOW_DEFAULT = 32768;
+constexpr size_t MK_COOP_BELOW_DEFAULT = 16384;
 size_t mk_coop_below();
 // Once a layer has at most this many nodes, the layers above it are finished by one CTA
 // (default; the calling thread can raise it with gb_set_merkle_top_nodes: fewer launches,
@@ -66,6 +66,20 @@ constexpr int P2_WIDE = 512, P2_NARROW = 128;
 constexpr size_t P2_WIDE_FROM = (size_t)1 << 19;
 #define P2_BOUNDS(T) __launch_bounds__(T, (T) == 512 ? 3 : 10)
 inline bool p2_wide(size_t items) { return items >= P2_WIDE_FROM; }
+
+// Form of a single-tree launch of `items` permutations, by the per-launch times measured on
+// GB300 (a 2^21-leaf tree's chain of levels down to 16 nodes: 1.32 ms against 1.50 ms with
+// the one-thread form from the cooperative threshold up): the 8-lane cooperative form below
+// mk_coop_below(), the pair form (p2_permute_pair) below P2_ONE_FROM, and one permutation per
+// thread in 512-thread CTAs from there.
+constexpr size_t P2_ONE_FROM = (size_t)1 << 16;
+enum P2Form { P2_COOP, P2_PAIR, P2_ONE };
+inline P2Form p2_form(size_t items) {
+    return items < mk_coop_below() ? P2_COOP : items < P2_ONE_FROM ? P2_PAIR : P2_ONE;
+}
+// pair-form CTA size (2 threads per permutation) and its bounds (up to 64 registers)
+inline int p2_pair_threads(size_t items) { return items >= ((size_t)1 << 15) ? 256 : 128; }
+#define P2_PAIR_BOUNDS(T) __launch_bounds__(T, (T) == 256 ? 4 : 8)
 
 // CTA size for a cooperative launch over `groups` 8-lane groups: small launches use
 // 64-thread CTAs so that the work spreads over as many SMs as there are CTAs.

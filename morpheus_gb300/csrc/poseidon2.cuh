@@ -257,6 +257,86 @@ __device__ __forceinline__ u64 p2_permute_coop(u64 x, int l, const P2Lane& c) {
     return x;
 }
 
+// ---------------------------------------------------------------------------
+// Pair form: 2 adjacent lanes hold one state, lane h (h = lane & 1) holding s[4h .. 4h+3].
+// The external circulant stays within a lane; the column sums and the internal rounds'
+// sum take one exchange with the partner.  It issues about as many instructions per
+// permutation as the one-thread form, in warp streams half as long, which suits layers too
+// small to fill the GPU with one-thread permutations.  All 32 lanes of a warp must call it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ u64 p2_sel(int h, u64 lo, u64 hi) { return h ? hi : lo; }
+
+// this lane's half of the external layer, plus add[] (the next round's constants) when has_add
+__device__ __forceinline__ void p2_pair_external(u64* x, const u64* add, bool has_add) {
+    glw a = glw_of(x[0]), b = glw_of(x[1]), c = glw_of(x[2]), d = glw_of(x[3]);
+    glw t01 = glw_add(a, b), t23 = glw_add(c, d);
+    glw t0123 = glw_add(t01, t23);
+    glw t01123 = glw_add(t0123, b), t01233 = glw_add(t0123, d);
+    u64 o[4] = {glw_reduce(glw_add(t01123, t01)), glw_reduce(glw_add(t01123, glw_add(c, c))),
+                glw_reduce(glw_add(t01233, t23)), glw_reduce(glw_add(t01233, glw_add(a, a)))};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        glw v = glw_add(glw_add(glw_of(o[i]), o[i]), shfl_xor64(o[i], 1));  // 2 o_i + partner's o_i
+        if (has_add) v = glw_add(v, add[i]);
+        x[i] = glw_reduce(v);
+    }
+}
+
+__device__ __forceinline__ void p2_permute_pair(u64* s, int h) {
+    u64 rc[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) s[i] = p2_sbox(glw_reduce(glw_add(glw_of(s[i]), p2_sel(h, p2_rc_ext(0, i), p2_rc_ext(0, 4 + i)))));
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        if (r < 3) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) rc[i] = p2_sel(h, p2_rc_ext(r + 1, i), p2_rc_ext(r + 1, 4 + i));
+            p2_pair_external(s, rc, true);
+#pragma unroll
+            for (int i = 0; i < 4; i++) s[i] = p2_sbox(s[i]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++) rc[i] = (i == 0 && h == 0) ? p2_rc_int(0) : 0;
+            p2_pair_external(s, rc, true);
+        }
+    }
+    u64 dg[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) dg[i] = p2_sel(h, p2_diag(i), p2_diag(4 + i));
+    // internal rounds: lane 0 of the pair holds s0 (already plus rc_int[r]); both lanes run the
+    // S-box on their s[0], lane 1 keeps its own value
+#pragma unroll
+    for (int r = 0; r < 22; r++) {
+        const u64 y = p2_sbox(s[0]);
+        if (h == 0) s[0] = y;
+        glw loc = glw_add(glw_add(glw_of(s[0]), glw_of(s[1])), glw_add(glw_of(s[2]), glw_of(s[3])));
+        glw sum = glw_add(loc, shfl_xor_glw(loc, 1));
+        if (r < 21) {
+            s[0] = gl_mul_add(s[0], dg[0], h == 0 ? glw_add(sum, p2_rc_int(r + 1)) : sum);
+#pragma unroll
+            for (int i = 1; i < 4; i++) s[i] = gl_mul_add(s[i], dg[i], sum);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                s[i] = gl_mul_add(s[i], dg[i], glw_add(sum, p2_sel(h, p2_rc_ext(4, i), p2_rc_ext(4, 4 + i))));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) s[i] = p2_sbox(s[i]);
+#pragma unroll
+    for (int r = 4; r < 8; r++) {
+        if (r < 7) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) rc[i] = p2_sel(h, p2_rc_ext(r + 1, i), p2_rc_ext(r + 1, 4 + i));
+            p2_pair_external(s, rc, true);
+#pragma unroll
+            for (int i = 0; i < 4; i++) s[i] = p2_sbox(s[i]);
+        } else {
+            p2_pair_external(s, rc, false);
+        }
+    }
+}
+
 // 2-to-1 compression P2(l || r)[0..4]
 __device__ __forceinline__ void p2_compress(const u64* l, const u64* r, u64* out) {
     u64 s[8] = {l[0], l[1], l[2], l[3], r[0], r[1], r[2], r[3]};

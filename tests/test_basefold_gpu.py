@@ -47,7 +47,7 @@ def test_poseidon2_batch_matches_reference_code(gpu_lib, golden):
     assert got.tolist() == [c[1] for c in cases]
 
 
-@pytest.mark.parametrize("leaves", [1, 2, 8, 1024, 4096, 1 << 15])
+@pytest.mark.parametrize("leaves", [1, 2, 8, 1024, 4096, 1 << 15, 1 << 17])
 def test_merkle_tree_gl_and_ext2(gpu_lib, leaves):
     from morpheus_gb300.memory import DeviceBuffer
     cw = rnd(leaves, 2 * leaves)
@@ -57,6 +57,20 @@ def test_merkle_tree_gl_and_ext2(gpu_lib, leaves):
     cw2 = rnd(leaves + 1, 4 * leaves)
     assert gpu_lib.poseidon2_merkle_tree_ext2_ffi(dev(cw2).ptr, tree.ptr, leaves) == 0
     assert np.array_equal(canon(tree.to_numpy()), O.merkle_tree_ext2(cw2))
+
+
+@pytest.mark.parametrize("parents", [1 << 13, 1 << 14, 1 << 15, 1 << 16])
+def test_merkle_layer_every_form(gpu_lib, parents):
+    """One layer at the sizes where the launch switches form (cooperative, pair, one thread)."""
+    from morpheus_gb300.memory import DeviceBuffer
+    layer = rnd(parents, 2 * parents, 4)
+    out = DeviceBuffer(4 * parents)
+    assert gpu_lib.poseidon2_merkle_layer_ffi(dev(layer).ptr, out.ptr, parents) == 0
+    got = canon(out.to_numpy().reshape(parents, 4))
+    for j in (0, 1, parents // 2 + 3, parents - 1):
+        r = np.zeros(4, np.uint64)
+        O.lib().or_poseidon2_compress(layer[2 * j].copy(), layer[2 * j + 1].copy(), r)
+        assert np.array_equal(got[j], r), j
 
 
 def test_merkle_layer_and_compress(gpu_lib):
@@ -236,8 +250,9 @@ def test_table_matches_oracle(gpu_lib):
     assert np.array_equal(t.level_offsets(), off)
 
 
+# n = 16 folds 2^15- and 2^14-leaf rounds (the pair-form launches) and 2^16-parent layers
 @pytest.mark.parametrize("n,lr,q,table_nv", [(2, 1, 3, 2), (4, 1, 4, 6), (6, 3, 10, 9), (9, 1, 34, 9), (12, 1, 34, 14),
-                                             (11, 2, 7, 11)])
+                                             (11, 2, 7, 11), (16, 1, 34, 16)])
 def test_open_ext2_matches_oracle(gpu_lib, n, lr, q, table_nv):
     from morpheus_gb300.basefold import BasefoldCommitment, BasefoldTable
     from morpheus_gb300.sumcheck import Transcript
