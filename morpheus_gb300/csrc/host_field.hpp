@@ -70,42 +70,59 @@ inline E2 e2mul(E2 a, E2 b) {
     return E2{add(m0, mul(7, m1)), add(mul(a.c0, b.c1), mul(a.c1, b.c0))};
 }
 
+// Poseidon2 (width 8) on the host, branch-free: values stay any u64 congruent mod p inside the
+// permutation, sums are lazy 128-bit, and every reduction selects its corrections arithmetically
+// (data-dependent branches on random field elements mispredict about half the time).  The
+// output is canonical, equal to the canonical-throughout form of the same rounds.
+inline u64 red128(u128 x) {  // any 128-bit value -> a u64 congruent to it
+    const u64 lo = (u64)x, hi = (u64)(x >> 64);
+    const u64 h1 = hi >> 32, h0 = hi & GL_EPS;
+    u64 t0 = lo - h1;
+    t0 -= ((u64)0 - (u64)(lo < h1)) & GL_EPS;  // a borrow is worth 2^64 == EPS: take it back
+    const u64 t1 = (h0 << 32) - h0;
+    u64 r = t0 + t1;
+    r += ((u64)0 - (u64)(r < t1)) & GL_EPS;  // a carry is worth EPS (no second carry is possible)
+    return r;
+}
+inline u64 mulr(u64 a, u64 b) { return red128((u128)a * b); }
+
 inline void p2_permute(u64 s[8]) {
     auto sbox = [](u64 x) {
-        u64 x2 = mul(x, x), x4 = mul(x2, x2), x3 = mul(x2, x);
-        return mul(x4, x3);
+        const u64 x2 = mulr(x, x), x4 = mulr(x2, x2), x3 = mulr(x2, x);
+        return mulr(x4, x3);
     };
+    // external layer: per half the circulant [2 3 1 1], then each output plus its column sum
     auto ext = [](u64* v) {
+        u128 o[8];
         for (int h = 0; h < 8; h += 4) {
-            u64 a = v[h], b = v[h + 1], c = v[h + 2], d = v[h + 3];
-            u64 ab = add(a, b), cd = add(c, d), all = add(ab, cd);
-            u64 all_b = add(all, b), all_d = add(all, d);
-            v[h] = add(all_b, ab);
-            v[h + 1] = add(all_b, add(c, c));
-            v[h + 2] = add(all_d, cd);
-            v[h + 3] = add(all_d, add(a, a));
+            const u128 a = v[h], b = v[h + 1], c = v[h + 2], d = v[h + 3];
+            const u128 ab = a + b, cd = c + d, all = ab + cd;
+            o[h] = all + b + ab;
+            o[h + 1] = all + b + c + c;
+            o[h + 2] = all + d + cd;
+            o[h + 3] = all + d + a + a;
         }
         for (int i = 0; i < 4; i++) {
-            u64 col = add(v[i], v[i + 4]);
-            v[i] = add(v[i], col);
-            v[i + 4] = add(v[i + 4], col);
+            const u128 col = o[i] + o[i + 4];
+            v[i] = red128(o[i] + col);
+            v[i + 4] = red128(o[i + 4] + col);
         }
     };
-    for (int i = 0; i < 8; i++) s[i] = canon(s[i]);
     for (int r = 0; r < 4; r++) {
-        for (int i = 0; i < 8; i++) s[i] = sbox(add(s[i], P2Const::ext[r][i]));
+        for (int i = 0; i < 8; i++) s[i] = sbox(red128((u128)s[i] + P2Const::ext[r][i]));
         ext(s);
     }
     for (int r = 0; r < 22; r++) {
-        s[0] = sbox(add(s[0], P2Const::inner[r]));
-        u64 sum = 0;
-        for (int i = 0; i < 8; i++) sum = add(sum, s[i]);
-        for (int i = 0; i < 8; i++) s[i] = add(mul(s[i], P2Const::diag[i]), sum);
+        s[0] = sbox(red128((u128)s[0] + P2Const::inner[r]));
+        u128 sum = 0;
+        for (int i = 0; i < 8; i++) sum += s[i];
+        for (int i = 0; i < 8; i++) s[i] = red128((u128)s[i] * P2Const::diag[i] + sum);
     }
     for (int r = 4; r < 8; r++) {
-        for (int i = 0; i < 8; i++) s[i] = sbox(add(s[i], P2Const::ext[r][i]));
+        for (int i = 0; i < 8; i++) s[i] = sbox(red128((u128)s[i] + P2Const::ext[r][i]));
         ext(s);
     }
+    for (int i = 0; i < 8; i++) s[i] = canon(s[i]);
 }
 
 // ---- transcript ----
