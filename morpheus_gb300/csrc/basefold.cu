@@ -529,6 +529,12 @@ struct DevMem {
 };
 
 static u64* pinned(size_t words) { return thread_pinned(1, words); }
+// Device address of pinned staging: the kernels write each round's record there directly, so
+// reading it back takes a stream synchronisation and no copy.
+static u64* mapped(u64* host) {
+    void* d = nullptr;
+    return host && cudaHostGetDevicePointer(&d, host, 0) == cudaSuccess ? (u64*)d : nullptr;
+}
 
 #define RC_TRY(x)                 \
     do {                          \
@@ -645,7 +651,7 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
     cudaStream_t s = stream();
     const int n = in.n, lr = in.lr;
     const size_t N = (size_t)1 << n, L = N << lr;
-    u64 *eqA, *eqB, *bhA, *bhB, *partials, *rec;
+    u64 *eqA, *eqB, *bhA, *bhB, *partials;
     unsigned* counter;
     RC_TRY(m.alloc(&eqA, N * 8));  // N/2 Ext2
     RC_TRY(m.alloc(&eqB, N * 8));
@@ -653,7 +659,6 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
     RC_TRY(m.alloc(&bhB, N * 8));
     const unsigned gmax = red_grid(N / 2);
     RC_TRY(m.alloc(&partials, (size_t)gmax * 6 * 8));
-    RC_TRY(m.alloc(&rec, 16 * 8));
     RC_TRY(m.alloc(&counter, 16));
     GB_CUDA_TRY(cudaMemsetAsync(counter, 0, 16, s));
     // folded codewords r = 0..n-1 (L >> (r+1) Ext2 each) and trees r = 0..n-2
@@ -664,10 +669,10 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
         RC_TRY(m.alloc(&ftree[r], (2 * leaves - 1) * 32));
     }
     u64* stage = pinned(64);
-    if (!stage) return GB_ECUDA;
+    u64* rec = mapped(stage);  // records: oracle words 0..5, root 8..11
+    if (!rec) return GB_ECUDA;
 
-    auto read_rec = [&](int words) -> int {
-        GB_CUDA_TRY(cudaMemcpyAsync(stage, rec, (size_t)words * 8, cudaMemcpyDeviceToHost, s));
+    auto read_rec = [&](int) -> int {  // the record's words are in `stage` once the stream is idle
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         return GB_OK;
     };
@@ -926,7 +931,7 @@ static int batch_open_ext2(BfCommitment* const* comms, int num_comms, const u64*
     }
 
     DevMem m;
-    u64 *d_pts, *g, *eq, *eqA, *eqB, *gA, *gB, *partials, *rec;
+    u64 *d_pts, *g, *eq, *eqA, *eqB, *gA, *gB, *partials;
     unsigned* counter;
     BoTerm* d_terms;
     int* d_start;
@@ -939,14 +944,14 @@ static int batch_open_ext2(BfCommitment* const* comms, int num_comms, const u64*
     RC_TRY(m.alloc(&gB, P * N * 8));
     const unsigned gx = (unsigned)std::max<size_t>(1, (red_grid(N / 2) + P - 1) / P);
     RC_TRY(m.alloc(&partials, (size_t)gx * P * 6 * 8));
-    RC_TRY(m.alloc(&rec, 16 * 8));
     RC_TRY(m.alloc(&counter, 16));
     RC_TRY(m.alloc(&d_terms, E * sizeof(BoTerm)));
     RC_TRY(m.alloc(&d_start, (P + 1) * sizeof(int)));
     GB_CUDA_TRY(cudaMemsetAsync(counter, 0, 16, s));
     GB_CUDA_TRY(cudaMemcpyAsync(d_pts, pts.data(), P * n * 16, cudaMemcpyHostToDevice, s));
     u64* stage = pinned(64);
-    if (!stage) return GB_ECUDA;
+    u64* rec = mapped(stage);  // records: oracle words 0..5, root 8..11
+    if (!rec) return GB_ECUDA;
 
     // 3. g_p = sum over the point's evaluations of w_i evals_i (terms grouped by point)
     std::vector<BoTerm> terms;
@@ -965,8 +970,7 @@ static int batch_open_ext2(BfCommitment* const* comms, int num_comms, const u64*
     for (size_t p = 0; p < P; p++) RC_TRY(eq_table(d_pts + p * n * 2, n, true, eq + p * N * 2));
 
     // 5-7. outer sumcheck: n oracles, n challenges r
-    auto read_rec = [&](int words) -> int {
-        GB_CUDA_TRY(cudaMemcpyAsync(stage, rec, (size_t)words * 8, cudaMemcpyDeviceToHost, s));
+    auto read_rec = [&](int) -> int {  // the record's words are in `stage` once the stream is idle
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         return GB_OK;
     };

@@ -220,7 +220,7 @@ int merkle_build_from_leaves(u64* tree, size_t leaves, u64* root_out) {
         merkle_top_coop_kernel<<<1, threads, 0, stream()>>>(layer, nodes, root_out);
         GB_LAUNCH_CHECK("merkle_top_coop_kernel");
     } else if (root_out) {
-        GB_CUDA_TRY(cudaMemcpyAsync(root_out, layer, 32, cudaMemcpyDeviceToDevice, stream()));
+        GB_CUDA_TRY(cudaMemcpyAsync(root_out, layer, 32, cudaMemcpyDefault, stream()));  // root_out may be mapped host memory
     }
     return GB_OK;
 }

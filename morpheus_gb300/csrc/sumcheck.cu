@@ -568,7 +568,6 @@ struct ScWork {
     u64* a = nullptr;     // ping
     u64* b = nullptr;     // pong
     u64* partials = nullptr;
-    u64* out = nullptr;   // message / finals staging (device)
     unsigned* counter = nullptr;
     ~ScWork() {
         cudaStream_t s = stream();
@@ -576,7 +575,6 @@ struct ScWork {
         if (a) cudaFreeAsync(a, s);
         if (b) cudaFreeAsync(b, s);
         if (partials) cudaFreeAsync(partials, s);
-        if (out) cudaFreeAsync(out, s);
         if (counter) cudaFreeAsync(counter, s);
     }
 };
@@ -607,13 +605,16 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
         polys = w.base;
     }
     u64* stage = pinned_staging(2 * (SC_MAX_D + 1) + 2 * SC_MAX_D);
-    if (!stage) {
+    // the round kernels write each message (and the final values) straight into the pinned
+    // staging through its device address, so reading it back is a stream synchronisation
+    void* stage_dev = nullptr;
+    if (!stage || cudaHostGetDevicePointer(&stage_dev, stage, 0) != cudaSuccess) {
         set_error_msg("gb_sumcheck_prove: pinned staging allocation failed");
         return GB_ECUDA;
     }
+    u64* msg_out = (u64*)stage_dev;
     const unsigned max_grid = round_grid(N / 2 > 0 ? N / 2 : 1);
     GB_CUDA_TRY(cudaMallocAsync(&w.partials, (size_t)max_grid * 2 * (SC_MAX_D + 1) * 8, s));
-    GB_CUDA_TRY(cudaMallocAsync(&w.out, 2 * (SC_MAX_D + 1) * 8, s));
     GB_CUDA_TRY(cudaMallocAsync(&w.counter, sizeof(unsigned), s));
     GB_CUDA_TRY(cudaMemsetAsync(w.counter, 0, sizeof(unsigned), s));
     const size_t lvl_stride = N / 2 > 0 ? N / 2 : 1;  // elements per poly in the ping/pong buffers
@@ -642,16 +643,16 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
             int rc;
             if (k == 0) {
                 unsigned g = round_grid(level / 2);
-                rc = in_ext ? dispatch_d<Round0E2In>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter)
-                     : ext  ? dispatch_d<Round0E2>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter)
-                            : dispatch_d<Round0Base>(d, cur, cur_stride, level / 2, g, w.partials, w.out, w.counter);
+                rc = in_ext ? dispatch_d<Round0E2In>(d, cur, cur_stride, level / 2, g, w.partials, msg_out, w.counter)
+                     : ext  ? dispatch_d<Round0E2>(d, cur, cur_stride, level / 2, g, w.partials, msg_out, w.counter)
+                            : dispatch_d<Round0Base>(d, cur, cur_stride, level / 2, g, w.partials, msg_out, w.counter);
             } else {
                 u64* dst = bufs[pp];
                 size_t quarter = level / 2;  // output pairs
                 unsigned g = round_grid(quarter);
                 rc = ext ? dispatch_d<FoldRoundE2>(d, base_in, cur, cur_stride, dst, lvl_stride, quarter, g, r0, r1,
-                                                   w.partials, w.out, w.counter)
-                         : dispatch_d<FoldRoundBase>(d, cur, cur_stride, dst, lvl_stride, quarter, g, r0, w.partials, w.out,
+                                                   w.partials, msg_out, w.counter)
+                         : dispatch_d<FoldRoundBase>(d, cur, cur_stride, dst, lvl_stride, quarter, g, r0, w.partials, msg_out,
                                                      w.counter);
                 cur = dst;
                 cur_stride = lvl_stride;
@@ -660,7 +661,6 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
             }
             if (rc) return rc;
             const int words = W * (d + 1);
-            GB_CUDA_TRY(cudaMemcpyAsync(stage, w.out, words * 8, cudaMemcpyDeviceToHost, s));
             GB_CUDA_TRY(cudaStreamSynchronize(s));
             u64* m = h_msgs + (size_t)k * words;
             for (int i = 0; i < words; i++) m[i] = stage[i];
@@ -679,14 +679,13 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
         }
         if (ext) {
             if (base_in)
-                sc_final_kernel<true, true><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, w.out);
+                sc_final_kernel<true, true><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, msg_out);
             else
-                sc_final_kernel<true, false><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, w.out);
+                sc_final_kernel<true, false><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, msg_out);
         } else {
-            sc_final_kernel<false, true><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, w.out);
+            sc_final_kernel<false, true><<<1, 32, 0, s>>>(cur, cur_stride, d, r0, r1, msg_out);
         }
         GB_LAUNCH_CHECK("sc_final");
-        GB_CUDA_TRY(cudaMemcpyAsync(stage, w.out, (size_t)W * d * 8, cudaMemcpyDeviceToHost, s));
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         for (int i = 0; i < W * d; i++) finals[i] = stage[i];
     }
