@@ -343,9 +343,14 @@ class LsRunner {
         np_max_ = (size_t)np;
         seg_cap_ = (size_t)np * (maxn + 8);  // one round's launches (layers + 4) never need more slots
         GB_CUDA_TRY(cudaMallocAsync(&d_segs_, seg_cap_ * sizeof(LsSeg), s));
-        GB_CUDA_TRY(cudaMallocAsync(&d_recs_, (size_t)np * LS_REC * 8, s));
         GB_CUDA_TRY(cudaMallocHost(&h_segs_, seg_cap_ * sizeof(LsSeg)));
         GB_CUDA_TRY(cudaMallocHost(&h_recs_, (size_t)np * LS_REC * 8));
+        {
+            // the kernels write the records straight into the pinned array (its device address)
+            void* d = nullptr;
+            GB_CUDA_TRY(cudaHostGetDevicePointer(&d, h_recs_, 0));
+            d_recs_ = (u64*)d;
+        }
         size_t max_blocks = 0;
         for (auto& p : P) max_blocks += (p.N / 2 + LS_RED_THREADS * LS_ITEMS - 1) / (LS_RED_THREADS * LS_ITEMS) + 1;
         GB_CUDA_TRY(cudaMallocAsync(&d_partials_, max_blocks * 6 * 8, s));
@@ -600,7 +605,6 @@ class LsRunner {
         cudaStream_t s = stream();
         if (ws_) cudaFreeAsync(ws_, s);
         if (d_segs_) cudaFreeAsync(d_segs_, s);
-        if (d_recs_) cudaFreeAsync(d_recs_, s);
         if (d_partials_) cudaFreeAsync(d_partials_, s);
         cudaStreamSynchronize(s);
         if (h_segs_) cudaFreeHost(h_segs_);
@@ -628,8 +632,7 @@ class LsRunner {
             return nullptr;
         return d_segs_ + off;
     }
-    int read_recs(int count) {
-        GB_CUDA_TRY(cudaMemcpyAsync(h_recs_, d_recs_, (size_t)count * LS_REC * 8, cudaMemcpyDeviceToHost, stream()));
+    int read_recs(int) {  // the records are in h_recs_ once the stream is idle
         GB_CUDA_TRY(cudaStreamSynchronize(stream()));
         slot_ = 0;
         return GB_OK;
@@ -657,7 +660,7 @@ class LsRunner {
     u64* ws_ = nullptr;
     LsSeg* d_segs_ = nullptr;
     LsSeg* h_segs_ = nullptr;
-    u64* d_recs_ = nullptr;
+    u64* d_recs_ = nullptr;  // device address of h_recs_ (mapped pinned memory)
     u64* h_recs_ = nullptr;
     u64* d_partials_ = nullptr;
     size_t seg_cap_ = 0, np_max_ = 1, slot_ = 0;
