@@ -344,6 +344,7 @@ __global__ void __launch_bounds__(256) fold_hash_leaves_coop_kernel(const u64* _
                                                                     const u64* __restrict__ tab, u64 c0, u64 c1,
                                                                     u64* __restrict__ folded, u64* __restrict__ tree,
                                                                     size_t leaves) {
+    pdl_enter();
     size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 3;
     const int l = threadIdx.x & 7;
     const bool live = g < leaves;
@@ -759,11 +760,11 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
                 int th = coop_threads(leaves);
                 unsigned g = grid_for(leaves * 8, th);
                 if (base_in)
-                    fold_hash_leaves_coop_kernel<true><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
-                                                                         leaves);
+                    GB_CUDA_TRY(launch_pdl(fold_hash_leaves_coop_kernel<true>, g, th, s, cw_in, lvl, ch.c0, ch.c1,
+                                           fcw[rd], ftree[rd], leaves));
                 else
-                    fold_hash_leaves_coop_kernel<false><<<g, th, 0, s>>>(cw_in, lvl, ch.c0, ch.c1, fcw[rd], ftree[rd],
-                                                                          leaves);
+                    GB_CUDA_TRY(launch_pdl(fold_hash_leaves_coop_kernel<false>, g, th, s, cw_in, lvl, ch.c0, ch.c1,
+                                           fcw[rd], ftree[rd], leaves));
             } else {
                 const unsigned g = grid_for(leaves, P2_WIDE);
                 if (base_in)

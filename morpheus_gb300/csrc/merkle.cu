@@ -56,6 +56,7 @@ __global__ void P2_PAIR_BOUNDS(T) merkle_level_pair_kernel(const u64* __restrict
 // their warp still has to take part in the shuffles.
 __global__ void __launch_bounds__(MK_COOP_THREADS) merkle_level_coop_kernel(const u64* __restrict__ in,
                                                                           u64* __restrict__ out, size_t nodes) {
+    pdl_enter();
     size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 3;
     int l = threadIdx.x & 7;
     bool live = g < nodes;
@@ -71,6 +72,7 @@ __global__ void __launch_bounds__(MK_COOP_THREADS) merkle_level_coop_kernel(cons
 // written to root_out when given.
 __global__ void __launch_bounds__(1024) merkle_top_coop_kernel(u64* __restrict__ layer, size_t nodes,
                                                                u64* __restrict__ root_out) {
+    pdl_enter();
     const int groups = blockDim.x >> 3, grp = threadIdx.x >> 3, l = threadIdx.x & 7;
     P2Lane c = p2_lane_consts(l);
     while (nodes > 1) {
@@ -138,6 +140,7 @@ __global__ void P2_PAIR_BOUNDS(T) hash_leaves_pair_kernel(const u64* __restrict_
 __global__ void __launch_bounds__(MK_COOP_THREADS) hash_leaves_coop_kernel(const u64* __restrict__ cw,
                                                                          u64* __restrict__ tree, size_t leaves,
                                                                          int width) {
+    pdl_enter();
     size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 3;
     int l = threadIdx.x & 7;
     bool live = g < leaves;
@@ -196,7 +199,7 @@ static int merkle_level(const u64* in, u64* out, size_t half) {
         return check_launch("merkle_level_pair_kernel");
     }
     int threads = coop_threads(half);
-    merkle_level_coop_kernel<<<grid_for(half * 8, threads), threads, 0, s>>>(in, out, half);
+    GB_CUDA_TRY(launch_pdl(merkle_level_coop_kernel, grid_for(half * 8, threads), threads, s, in, out, half));
     return check_launch("merkle_level_coop_kernel");
 }
 
@@ -217,7 +220,7 @@ int merkle_build_from_leaves(u64* tree, size_t leaves, u64* root_out) {
         size_t half = nodes >> 1;
         int threads = (int)(8 * (half < 128 ? half : 128));
         threads = threads < 64 ? 64 : (threads + 31) / 32 * 32;
-        merkle_top_coop_kernel<<<1, threads, 0, stream()>>>(layer, nodes, root_out);
+        GB_CUDA_TRY(launch_pdl(merkle_top_coop_kernel, 1, threads, stream(), layer, nodes, root_out));
         GB_LAUNCH_CHECK("merkle_top_coop_kernel");
     } else if (root_out) {
         GB_CUDA_TRY(cudaMemcpyAsync(root_out, layer, 32, cudaMemcpyDefault, stream()));  // root_out may be mapped host memory
@@ -229,7 +232,7 @@ int merkle_hash_leaves_gl(const u64* cw, u64* tree, size_t leaves) {
     const P2Form f = p2_form(leaves);
     if (f == P2_COOP) {
         int t = coop_threads(leaves);
-        hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 2);
+        GB_CUDA_TRY(launch_pdl(hash_leaves_coop_kernel, grid_for(leaves * 8, t), t, stream(), cw, tree, leaves, 2));
         return check_launch("hash_leaves_coop_kernel");
     }
     if (f == P2_PAIR) {
@@ -247,7 +250,7 @@ int merkle_hash_leaves_ext2(const u64* cw, u64* tree, size_t leaves) {
     const P2Form f = p2_form(leaves);
     if (f == P2_COOP) {
         int t = coop_threads(leaves);
-        hash_leaves_coop_kernel<<<grid_for(leaves * 8, t), t, 0, stream()>>>(cw, tree, leaves, 4);
+        GB_CUDA_TRY(launch_pdl(hash_leaves_coop_kernel, grid_for(leaves * 8, t), t, stream(), cw, tree, leaves, 4));
         return check_launch("hash_leaves_coop_kernel");
     }
     if (f == P2_PAIR) {

@@ -63,7 +63,7 @@ constexpr size_t MK_TOP_NODES = 16;
 // 128-thread CTAs.  Launches below P2_WIDE_FROM permutations keep 128-thread CTAs, so that a
 // launch of less than a wave still spreads over every SM.
 constexpr int P2_WIDE = 512, P2_NARROW = 128;
-constexpr size_t P2_WIDE_FROM = (size_t)1 << 19;
+constexpr size_t P2_WIDE_FROM = (size_t)1 << 16;
 #define P2_BOUNDS(T) __launch_bounds__(T, (T) == 512 ? 3 : 10)
 inline bool p2_wide(size_t items) { return items >= P2_WIDE_FROM; }
 
@@ -80,6 +80,31 @@ inline P2Form p2_form(size_t items) {
 // pair-form CTA size (2 threads per permutation) and its bounds (up to 64 registers)
 inline int p2_pair_threads(size_t items) { return items >= ((size_t)1 << 15) ? 256 : 128; }
 #define P2_PAIR_BOUNDS(T) __launch_bounds__(T, (T) == 256 ? 4 : 8)
+
+// Programmatic dependent launch for the latency-bound cooperative kernels: launched with
+// launch_pdl, such a kernel may be scheduled while the kernel before it on the stream drains;
+// pdl_enter (its first statement) lets the next such kernel be scheduled in turn and waits for
+// the previous kernel's completion and memory before anything is read.  Without the launch
+// attribute both instructions return at once.  Only these small, single-wave kernels use it:
+// an early-scheduled kernel holds SM slots while it waits.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+template <typename... Params, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(Params...), unsigned grid, int block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 
 // CTA size for a cooperative launch over `groups` 8-lane groups: small launches use
 // 64-thread CTAs so that the work spreads over as many SMs as there are CTAs.
