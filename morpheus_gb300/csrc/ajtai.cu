@@ -163,7 +163,7 @@ __global__ void ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows
 //   warp 0: TMA producer   warp 1: MMA issuer (one thread)   warps 2..9: epilogue, warp w owning
 //   TMEM lanes 32 (w % 4) .. +31 and columns 64 ((w - 2) / 4) .. +63 of each accumulator
 // ---------------------------------------------------------------------------
-constexpr int GM_BM = 128, GM_BN = 128, GM_BK = 64, GM_STAGES = 4, GM_CHUNK_TILES = 16;
+constexpr int GM_BM = 128, GM_BN = 128, GM_BK = 64, GM_STAGES = 6, GM_CHUNK_TILES = 16;
 constexpr int GM_TILE_BYTES = GM_BM * GM_BK * 2;  // 16 KB (A and B tiles are the same size)
 constexpr int GM_STAGE_BYTES = 2 * GM_TILE_BYTES;
 constexpr int GM_EPI_WARPS = 8;  // two warps per TMEM lane quarter, one per 64-column half
