@@ -140,15 +140,20 @@ __global__ void ajtai_zprep_kernel(const uint8_t* __restrict__ z, int B, size_t 
     zc[t] = __int2bfloat16_rn(v);
 }
 
-// c[b][i][r] = sum_p 256^p S[(p, i, r)][b] + 128 rowsum[i][r]  mod q, canonical
-__global__ void ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows, int B, const u64* __restrict__ RS,
-                                     u64* __restrict__ out) {
+// c[b][i][r] = sum_p 256^p S[(p, i, r)][b] + 128 rowsum[i][r]  mod q, canonical; S is the sum of
+// the split-K partial arrays (split_stride ints apart)
+__global__ void ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows, int B, int splits,
+                                     size_t split_stride, const u64* __restrict__ RS, u64* __restrict__ out) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= B * rows * AJ_D) return;
     int b = t / (rows * AJ_D), ir = t % (rows * AJ_D);
     __int128 acc = 0;
-#pragma unroll
-    for (int p = 7; p >= 0; p--) acc = acc * 256 + (__int128)S[((size_t)p * rows * AJ_D + ir) * Bp + b];
+    for (int p = 7; p >= 0; p--) {
+        const int* sp = S + ((size_t)p * rows * AJ_D + ir) * Bp + b;
+        long long part = 0;  // |each split| < 2^31, at most 152 splits
+        for (int q = 0; q < splits; q++) part += sp[(size_t)q * split_stride];
+        acc = acc * 256 + (__int128)part;
+    }
     const __int128 Q = (__int128)AGL_Q;
     __int128 m = acc % Q;
     if (m < 0) m += Q;
@@ -158,15 +163,18 @@ __global__ void ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows
 
 // ---------------------------------------------------------------------------
 // tcgen05 GEMM:  S[m][n] = sum_k A[m][k] B[n][k]   (bf16, K-major both, fp32 in TMEM,
-// exact per 1024-K chunk, int32 totals), M tile 128, N tile 128, K tile 64 (128-byte
-// swizzled rows), 4-stage TMA pipeline.
-//   warp 0: TMA producer   warp 1: MMA issuer (one thread)   warps 2..9: epilogue, warp w owning
+// exact per 1024-K chunk, int32 totals), M tile 128, N tile 256 (every witness of a batch of
+// 256 in one tile, so each key tile is loaded once), K tile 64 (128-byte swizzled rows),
+// 4-stage TMA pipeline of 48 KB stages.  blockIdx.y splits the K chunks (split-K): each split
+// writes its own int32 partial sums, which the combine adds.
+//   warp 0: TMA producer   warp 1: MMA issuer (one thread)   warps 2..17: epilogue, warp w owning
 //   TMEM lanes 32 (w % 4) .. +31 and columns 64 ((w - 2) / 4) .. +63 of each accumulator
 // ---------------------------------------------------------------------------
-constexpr int GM_BM = 128, GM_BN = 128, GM_BK = 64, GM_STAGES = 6, GM_CHUNK_TILES = 16;
-constexpr int GM_TILE_BYTES = GM_BM * GM_BK * 2;  // 16 KB (A and B tiles are the same size)
-constexpr int GM_STAGE_BYTES = 2 * GM_TILE_BYTES;
-constexpr int GM_EPI_WARPS = 8;  // two warps per TMEM lane quarter, one per 64-column half
+constexpr int GM_BM = 128, GM_BN = 256, GM_BK = 64, GM_STAGES = 4, GM_CHUNK_TILES = 16;
+constexpr int GM_A_BYTES = GM_BM * GM_BK * 2;  // 16 KB
+constexpr int GM_B_BYTES = GM_BN * GM_BK * 2;  // 32 KB
+constexpr int GM_STAGE_BYTES = GM_A_BYTES + GM_B_BYTES;
+constexpr int GM_EPI_WARPS = 16;  // four warps per TMEM lane quarter, one per 64-column group
 constexpr int GM_THREADS = 64 + 32 * GM_EPI_WARPS;
 constexpr int GM_SMEM = GM_STAGES * GM_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr unsigned long long GM_SPIN_LIMIT = 1ull << 26;  // bounded waits (seconds at worst)
@@ -222,20 +230,25 @@ __device__ __forceinline__ u64 umma_desc_sw128(u32 saddr) {
     return d;
 }
 
-// instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 128
+// instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 256
 constexpr u32 GM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(GM_BN >> 3) << 17) | ((u32)(GM_BM >> 4) << 24);
 
 __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                    const __grid_constant__ CUtensorMap tmB, int k_tiles,
-                                                                   int* __restrict__ S, int ldS, int* __restrict__ err) {
+                                                                   int chunks_per_split, int* __restrict__ S, int ldS,
+                                                                   size_t split_stride, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + GM_STAGES * GM_STAGE_BYTES);
     // bars: full[S], empty[S], acc_full[2], acc_empty[2], mma_done; tmem base address after them
     u32* tmem_slot = (u32*)(bars + 2 * GM_STAGES + 5);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * GM_BM, n0 = blockIdx.y * GM_BN;
-    const int chunks = k_tiles / GM_CHUNK_TILES;
+    const int m0 = blockIdx.x * GM_BM, n0 = blockIdx.z * GM_BN;
+    // this split's K chunks [c_begin, c_begin + chunks); the host makes every split non-empty
+    const int all_chunks = k_tiles / GM_CHUNK_TILES;
+    const int c_begin = blockIdx.y * chunks_per_split;
+    const int chunks = min(chunks_per_split, all_chunks - c_begin);
+    const int kt0 = c_begin * GM_CHUNK_TILES;
 
     auto full = [&](int s) { return smem_u32(bars + s); };
     auto empty = [&](int s) { return smem_u32(bars + GM_STAGES + s); };
@@ -255,8 +268,8 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
         mbar_init(mma_done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 1) {  // TMEM: two 128-column fp32 accumulators
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+    if (warp == 1) {  // TMEM: two 256-column fp32 accumulators (all 512 columns; one CTA per SM)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -266,15 +279,17 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
 
     if (warp == 0) {
         if (lane == 0) {
+            // kt counts this split's K tiles from 0 (stage and phase); the K coordinate is kt0 + kt
+            const int my_tiles = chunks * GM_CHUNK_TILES;
             int issued = 0;
-            for (int kt = 0; kt < k_tiles; kt++) {
+            for (int kt = 0; kt < my_tiles; kt++) {
                 int s = kt % GM_STAGES;
                 u32 ph = (kt / GM_STAGES) & 1;
                 if (!mbar_wait(empty(s), ph ^ 1, err, 1)) break;
                 mbar_expect_tx(full(s), GM_STAGE_BYTES);
                 uint8_t* sa = smem + s * GM_STAGE_BYTES;
-                tma_load_2d(smem_u32(sa), &tmA, kt * GM_BK, m0, full(s));
-                tma_load_2d(smem_u32(sa + GM_TILE_BYTES), &tmB, kt * GM_BK, n0, full(s));
+                tma_load_2d(smem_u32(sa), &tmA, (kt0 + kt) * GM_BK, m0, full(s));
+                tma_load_2d(smem_u32(sa + GM_A_BYTES), &tmB, (kt0 + kt) * GM_BK, n0, full(s));
                 issued = kt + 1;
             }
             // loads still in flight land in shared memory: wait (bounded) for every issued stage
@@ -299,7 +314,7 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     u32 sa = smem_u32(smem + s * GM_STAGE_BYTES);
-                    u64 adesc = umma_desc_sw128(sa), bdesc = umma_desc_sw128(sa + GM_TILE_BYTES);
+                    u64 adesc = umma_desc_sw128(sa), bdesc = umma_desc_sw128(sa + GM_A_BYTES);
 #pragma unroll
                     for (int k = 0; k < GM_BK / 16; k++) {
                         u32 acc = (t > 0 || k > 0) ? 1u : 0u;
@@ -324,9 +339,9 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
     } else {
         // epilogue: int32 totals of one TMEM row (lane) x 64 columns in registers
         const int quarter = warp & 3;
-        const int half = (warp - 2) >> 2;
+        const int half = (warp - 2) >> 2;  // 64-column group 0..3
         const int row = quarter * 32 + lane;
-        constexpr int COLS = GM_BN / 2;
+        constexpr int COLS = 64;
         int acc[COLS];
 #pragma unroll
         for (int q = 0; q < COLS; q++) acc[q] = 0;
@@ -340,34 +355,31 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-            for (int cb = 0; cb < COLS; cb += 32) {
-                u32 v[32];
+            for (int cb = 0; cb < COLS; cb += 16) {
+                u32 v[16];
                 u32 taddr = tmem + ((u32)(quarter * 32) << 16) + (u32)(a * GM_BN + half * COLS + cb);
                 asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-                    "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
-                    "[%32];"
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];"
                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
                       "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                      "=r"(v[15])
                     : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int e = 0; e < 32; e++) acc[cb + e] += __float2int_rn(__uint_as_float(v[e]));
+                for (int e = 0; e < 16; e++) acc[cb + e] += __float2int_rn(__uint_as_float(v[e]));
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
             mbar_arrive(acc_empty(a));
         }
-        int* dst = S + (size_t)(m0 + row) * ldS + n0 + half * COLS;
+        int* dst = S + blockIdx.y * split_stride + (size_t)(m0 + row) * ldS + n0 + half * COLS;
 #pragma unroll
         for (int q = 0; q < COLS; q += 4) *reinterpret_cast<int4*>(dst + q) = make_int4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
-    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
 // ---------------------------------------------------------------------------
@@ -379,8 +391,8 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// 2D bf16 tensor map, inner dimension contiguous, 64 x 128 boxes with 128-byte swizzle
-static int make_map(CUtensorMap* map, void* base, u64 inner, u64 outer) {
+// 2D bf16 tensor map, inner dimension contiguous, 64 x box_rows boxes with 128-byte swizzle
+static int make_map(CUtensorMap* map, void* base, u64 inner, u64 outer, u32 box_rows) {
     static const EncodeTiledFn encode = [] {  // resolved once (thread-safe static init)
         void* fn = nullptr;
         cudaDriverEntryPointQueryResult q;
@@ -395,7 +407,7 @@ static int make_map(CUtensorMap* map, void* base, u64 inner, u64 outer) {
     }
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {inner * 2};
-    cuuint32_t box[2] = {GM_BK, GM_BM};
+    cuuint32_t box[2] = {GM_BK, box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -452,7 +464,7 @@ static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* 
     GB_LAUNCH_CHECK("ajtai_rowsum_kernel");
     cudaFreeAsync(d_key, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
-    return make_map(&k->mapA, k->d_T, k->Kp, Mrows);
+    return make_map(&k->mapA, k->d_T, k->Kp, Mrows, GM_BM);
 }
 
 static void key_free(AjtaiKey* k) {
@@ -469,31 +481,41 @@ static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out
     cudaStream_t s = stream();
     const int Bp = (int)round_up((size_t)B, GM_BN);
     const size_t Mrows = (size_t)8 * k->rows * AJ_D;
+    // split-K: as many K splits as keep one CTA on every SM, each split a whole number of chunks
+    const int chunks = (int)(k->Kp / ((size_t)GM_BK * GM_CHUNK_TILES));
+    const int tiles = (int)(Mrows / GM_BM) * (Bp / GM_BN);
+    int splits = num_sms() / tiles;
+    splits = splits < 1 ? 1 : splits > chunks ? chunks : splits;
+    const int per_split = (chunks + splits - 1) / splits;
+    splits = (chunks + per_split - 1) / per_split;  // no empty split
+    const size_t split_stride = Mrows * (size_t)Bp;
     __nv_bfloat16* zc = nullptr;
     int* S = nullptr;
     int* err = nullptr;
     GB_CUDA_TRY(cudaMallocAsync(&zc, (size_t)Bp * k->Kp * 2, s));
-    GB_CUDA_TRY(cudaMallocAsync(&S, Mrows * Bp * 4, s));
+    GB_CUDA_TRY(cudaMallocAsync(&S, split_stride * splits * 4, s));
     GB_CUDA_TRY(cudaMallocAsync(&err, 4, s));
     GB_CUDA_TRY(cudaMemsetAsync(err, 0, 4, s));
     ajtai_zprep_kernel<<<grid_for((size_t)Bp * k->Kp, 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
     int rc = check_launch("ajtai_zprep_kernel");
     CUtensorMap mapB;
-    if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp);
+    if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp, GM_BN);
     if (!rc) {
         static bool attr = false;
         if (!attr) {
             cudaFuncSetAttribute(ajtai_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GM_SMEM);
             attr = true;
         }
-        dim3 grid((unsigned)(Mrows / GM_BM), (unsigned)(Bp / GM_BN));
+        dim3 grid((unsigned)(Mrows / GM_BM), (unsigned)splits, (unsigned)(Bp / GM_BN));
         int k_tiles = (int)(k->Kp / GM_BK);
-        ajtai_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, s>>>(k->mapA, mapB, k_tiles, S, Bp, err);
+        ajtai_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, s>>>(k->mapA, mapB, k_tiles, per_split, S, Bp, split_stride,
+                                                            err);
         rc = check_launch("ajtai_gemm_kernel");
     }
     if (!rc) {
         int total = B * k->rows * AJ_D;
-        ajtai_combine_kernel<<<grid_for(total, 256), 256, 0, s>>>(S, Bp, k->rows, B, k->d_RS, d_out);
+        ajtai_combine_kernel<<<grid_for(total, 256), 256, 0, s>>>(S, Bp, k->rows, B, splits, split_stride, k->d_RS,
+                                                                  d_out);
         rc = check_launch("ajtai_combine_kernel");
     }
     int h_err = 0;
