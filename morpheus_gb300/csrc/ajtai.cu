@@ -130,9 +130,28 @@ __global__ void ajtai_rowsum_kernel(const u64* __restrict__ M, int rows, u64 N, 
     RS[t] = agl_canon(acc);
 }
 
-// z'[b][k] = z[b][k] - 128 (bf16); padded witnesses / columns are 0
+// z'[b][k] = z[b][k] - 128 (bf16); padded witnesses / columns are 0.  Eight coefficients per
+// thread: one 8-byte load (K and Kp are multiples of 64; the host checks z's alignment) and one
+// 16-byte store.
 __global__ void ajtai_zprep_kernel(const uint8_t* __restrict__ z, int B, size_t K, int Bp, size_t Kp,
                                    __nv_bfloat16* __restrict__ zc) {
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t per_row = Kp / 8;
+    if (t >= (size_t)Bp * per_row) return;
+    const size_t b = t / per_row, k = (t % per_row) * 8;
+    uint2 raw = make_uint2(0x80808080u, 0x80808080u);  // 128 - 128 = 0 for padding
+    if (b < (size_t)B && k < K) raw = __ldg(reinterpret_cast<const uint2*>(z + b * K + k));
+    __align__(16) __nv_bfloat16 w[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+        const u32 word = e < 4 ? raw.x : raw.y;
+        w[e] = __int2bfloat16_rn((int)((word >> (8 * (e & 3))) & 0xFF) - 128);
+    }
+    *reinterpret_cast<uint4*>(zc + b * Kp + k) = *reinterpret_cast<const uint4*>(w);
+}
+// the same, one coefficient per thread, for witness arrays that are not 8-byte aligned
+__global__ void ajtai_zprep_scalar_kernel(const uint8_t* __restrict__ z, int B, size_t K, int Bp, size_t Kp,
+                                          __nv_bfloat16* __restrict__ zc) {
     size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (t >= (size_t)Bp * Kp) return;
     size_t b = t / Kp, k = t % Kp;
@@ -141,24 +160,40 @@ __global__ void ajtai_zprep_kernel(const uint8_t* __restrict__ z, int B, size_t 
 }
 
 // c[b][i][r] = sum_p 256^p S[(p, i, r)][b] + 128 rowsum[i][r]  mod q, canonical; S is the sum of
-// the split-K partial arrays (split_stride ints apart)
-__global__ void ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows, int B, int splits,
-                                     size_t split_stride, const u64* __restrict__ RS, u64* __restrict__ out) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= B * rows * AJ_D) return;
-    int b = t / (rows * AJ_D), ir = t % (rows * AJ_D);
-    __int128 acc = 0;
-    for (int p = 7; p >= 0; p--) {
-        const int* sp = S + ((size_t)p * rows * AJ_D + ir) * Bp + b;
-        long long part = 0;  // |each split| < 2^31, at most 152 splits
-        for (int q = 0; q < splits; q++) part += sp[(size_t)q * split_stride];
-        acc = acc * 256 + (__int128)part;
-    }
+// the split-K partial arrays (split_stride ints apart).  A block takes 32 witnesses x 32 output
+// coefficients through shared memory, so that it reads S along b and writes out along (i, r).
+constexpr int AJ_CB = 32;
+__global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows, int B,
+                                                            int splits, size_t split_stride,
+                                                            const u64* __restrict__ RS, u64* __restrict__ out) {
+    __shared__ u64 tile[AJ_CB][AJ_CB + 1];
+    const int IR = rows * AJ_D;
+    const int b0 = blockIdx.x * AJ_CB, ir0 = blockIdx.y * AJ_CB;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of 32
     const __int128 Q = (__int128)AGL_Q;
-    __int128 m = acc % Q;
-    if (m < 0) m += Q;
-    u64 rs128 = agl_mul(__ldg(RS + ir), 128);
-    out[t] = agl_canon(agl_add((u64)m, agl_canon(rs128)));
+    for (int j = ty; j < AJ_CB; j += 8) {
+        const int ir = ir0 + j, b = b0 + tx;
+        u64 val = 0;
+        if (ir < IR && b < B) {
+            __int128 acc = 0;
+            for (int p = 7; p >= 0; p--) {
+                const int* sp = S + ((size_t)p * IR + ir) * Bp + b;
+                long long part = 0;  // |each split| < 2^31, at most a few hundred splits
+                for (int q = 0; q < splits; q++) part += sp[(size_t)q * split_stride];
+                acc = acc * 256 + (__int128)part;
+            }
+            __int128 m = acc % Q;
+            if (m < 0) m += Q;
+            const u64 rs128 = agl_mul(__ldg(RS + ir), 128);
+            val = agl_canon(agl_add((u64)m, agl_canon(rs128)));
+        }
+        tile[j][tx] = val;
+    }
+    __syncthreads();
+    for (int j = ty; j < AJ_CB; j += 8) {
+        const int b = b0 + j, ir = ir0 + tx;
+        if (b < B && ir < IR) out[(size_t)b * IR + ir] = tile[tx][j];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -496,7 +531,10 @@ static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out
     GB_CUDA_TRY(cudaMallocAsync(&S, split_stride * splits * 4, s));
     GB_CUDA_TRY(cudaMallocAsync(&err, 4, s));
     GB_CUDA_TRY(cudaMemsetAsync(err, 0, 4, s));
-    ajtai_zprep_kernel<<<grid_for((size_t)Bp * k->Kp, 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+    if (((uintptr_t)d_z & 7) == 0)
+        ajtai_zprep_kernel<<<grid_for((size_t)Bp * (k->Kp / 8), 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+    else
+        ajtai_zprep_scalar_kernel<<<grid_for((size_t)Bp * k->Kp, 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
     int rc = check_launch("ajtai_zprep_kernel");
     CUtensorMap mapB;
     if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp, GM_BN);
@@ -513,9 +551,8 @@ static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out
         rc = check_launch("ajtai_gemm_kernel");
     }
     if (!rc) {
-        int total = B * k->rows * AJ_D;
-        ajtai_combine_kernel<<<grid_for(total, 256), 256, 0, s>>>(S, Bp, k->rows, B, splits, split_stride, k->d_RS,
-                                                                  d_out);
+        dim3 cg((unsigned)((B + AJ_CB - 1) / AJ_CB), (unsigned)((k->rows * AJ_D + AJ_CB - 1) / AJ_CB));
+        ajtai_combine_kernel<<<cg, 256, 0, s>>>(S, Bp, k->rows, B, splits, split_stride, k->d_RS, d_out);
         rc = check_launch("ajtai_combine_kernel");
     }
     int h_err = 0;
