@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -159,13 +160,29 @@ __global__ void ajtai_zprep_scalar_kernel(const uint8_t* __restrict__ z, int B, 
     zc[t] = __int2bfloat16_rn(v);
 }
 
-// c[b][i][r] = sum_p 256^p S[(p, i, r)][b] + 128 rowsum[i][r]  mod q, canonical; S is the sum of
-// the split-K partial arrays (split_stride ints apart).  A block takes 32 witnesses x 32 output
-// coefficients through shared memory, so that it reads S along b and writes out along (i, r).
+constexpr int GM_BM_C = 128, GM_BN_C = 256;  // the GEMM's M and N tiles (GM_BM, GM_BN below)
+
+// Persistent schedule of the GEMM: the (tile, K chunk) units, tile-major (tile t = nt tiles_m +
+// mt), split into `ctas` equal contiguous ranges, one per CTA.  A tile's partial sums come from
+// the CTAs whose range meets it, each writing its own slot of the tile: slot k of tile t belongs
+// to CTA gm_cta_of(t chunks) + k.
+struct GmSched {
+    int tiles_m, chunks;  // M tiles; K chunks per tile
+    long long units;      // tiles x chunks
+    int ctas, slots;      // grid size; slots per tile (the most CTAs meeting one tile)
+};
+__host__ __device__ inline long long gm_unit_begin(const GmSched& g, long long c) { return c * g.units / g.ctas; }
+__host__ __device__ inline int gm_cta_of(const GmSched& g, long long u) {  // the CTA whose range holds u
+    return (int)(((u + 1) * g.ctas - 1) / g.units);
+}
+
+// c[b][i][r] = sum_p 256^p S[(p, i, r)][b] + 128 rowsum[i][r]  mod q, canonical; S[(p, i, r)][b]
+// is the sum of the slots of its tile.  A block takes 32 witnesses x 32 output coefficients
+// through shared memory, so that it reads the slots along b and writes out along (i, r).
 constexpr int AJ_CB = 32;
-__global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restrict__ S, int Bp, int rows, int B,
-                                                            int splits, size_t split_stride,
-                                                            const u64* __restrict__ RS, u64* __restrict__ out) {
+__global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restrict__ S, GmSched sched, int rows,
+                                                            int B, const u64* __restrict__ RS,
+                                                            u64* __restrict__ out) {
     __shared__ u64 tile[AJ_CB][AJ_CB + 1];
     const int IR = rows * AJ_D;
     const int b0 = blockIdx.x * AJ_CB, ir0 = blockIdx.y * AJ_CB;
@@ -176,10 +193,14 @@ __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restric
         u64 val = 0;
         if (ir < IR && b < B) {
             __int128 acc = 0;
+            const int nt = b / GM_BN_C, col = b % GM_BN_C;
             for (int p = 7; p >= 0; p--) {
-                const int* sp = S + ((size_t)p * IR + ir) * Bp + b;
-                long long part = 0;  // |each split| < 2^31, at most a few hundred splits
-                for (int q = 0; q < splits; q++) part += sp[(size_t)q * split_stride];
+                const int m = p * IR + ir;
+                const long long t = (long long)nt * sched.tiles_m + m / GM_BM_C;
+                const int k_end = gm_cta_of(sched, (t + 1) * sched.chunks - 1) - gm_cta_of(sched, t * sched.chunks);
+                const int* sp = S + ((size_t)t * sched.slots * GM_BM_C + m % GM_BM_C) * GM_BN_C + col;
+                long long part = 0;  // |each slot| < 2^31
+                for (int k = 0; k <= k_end; k++) part += sp[(size_t)k * GM_BM_C * GM_BN_C];
                 acc = acc * 256 + (__int128)part;
             }
             __int128 m = acc % Q;
@@ -200,12 +221,14 @@ __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restric
 // tcgen05 GEMM:  S[m][n] = sum_k A[m][k] B[n][k]   (bf16, K-major both, fp32 in TMEM,
 // exact per 1024-K chunk, int32 totals), M tile 128, N tile 256 (every witness of a batch of
 // 256 in one tile, so each key tile is loaded once), K tile 64 (128-byte swizzled rows),
-// 4-stage TMA pipeline of 48 KB stages.  blockIdx.y splits the K chunks (split-K): each split
-// writes its own int32 partial sums, which the combine adds.
+// 4-stage TMA pipeline of 48 KB stages.  Persistent: CTA c takes the (tile, K chunk) units of
+// its GmSched range, which may span tiles; at each tile's last unit it writes its int32 sums to
+// its slot of that tile, and the combine adds the slots.
 //   warp 0: TMA producer   warp 1: MMA issuer (one thread)   warps 2..17: epilogue, warp w owning
 //   TMEM lanes 32 (w % 4) .. +31 and columns 64 ((w - 2) / 4) .. +63 of each accumulator
 // ---------------------------------------------------------------------------
 constexpr int GM_BM = 128, GM_BN = 256, GM_BK = 64, GM_STAGES = 4, GM_CHUNK_TILES = 16;
+static_assert(GM_BM == GM_BM_C && GM_BN == GM_BN_C, "combine tile sizes");
 constexpr int GM_A_BYTES = GM_BM * GM_BK * 2;  // 16 KB
 constexpr int GM_B_BYTES = GM_BN * GM_BK * 2;  // 32 KB
 constexpr int GM_STAGE_BYTES = GM_A_BYTES + GM_B_BYTES;
@@ -270,20 +293,23 @@ constexpr u32 GM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(GM_BN >> 3)
 
 __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                    const __grid_constant__ CUtensorMap tmB, int k_tiles,
-                                                                   int chunks_per_split, int* __restrict__ S, int ldS,
-                                                                   size_t split_stride, int* __restrict__ err) {
+                                                                   GmSched sched, int* __restrict__ S,
+                                                                   int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + GM_STAGES * GM_STAGE_BYTES);
     // bars: full[S], empty[S], acc_full[2], acc_empty[2], mma_done; tmem base address after them
     u32* tmem_slot = (u32*)(bars + 2 * GM_STAGES + 5);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * GM_BM, n0 = blockIdx.z * GM_BN;
-    // this split's K chunks [c_begin, c_begin + chunks); the host makes every split non-empty
-    const int all_chunks = k_tiles / GM_CHUNK_TILES;
-    const int c_begin = blockIdx.y * chunks_per_split;
-    const int chunks = min(chunks_per_split, all_chunks - c_begin);
-    const int kt0 = c_begin * GM_CHUNK_TILES;
+    // this CTA's units [u0, u0 + chunks) (at least one: the host launches at most `units` CTAs)
+    const long long u0 = gm_unit_begin(sched, blockIdx.x);
+    const int chunks = (int)(gm_unit_begin(sched, blockIdx.x + 1) - u0);
+    // unit -> tile and its operand rows, and the unit's first K tile
+    auto unit_tile = [&](int lu) { return (u0 + lu) / sched.chunks; };
+    auto unit_m0 = [&](int lu) { return (int)(unit_tile(lu) % sched.tiles_m) * GM_BM; };
+    auto unit_n0 = [&](int lu) { return (int)(unit_tile(lu) / sched.tiles_m) * GM_BN; };
+    auto unit_k0 = [&](int lu) { return (int)((u0 + lu) % sched.chunks) * GM_CHUNK_TILES; };
+    (void)k_tiles;
 
     auto full = [&](int s) { return smem_u32(bars + s); };
     auto empty = [&](int s) { return smem_u32(bars + GM_STAGES + s); };
@@ -314,7 +340,7 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
 
     if (warp == 0) {
         if (lane == 0) {
-            // kt counts this split's K tiles from 0 (stage and phase); the K coordinate is kt0 + kt
+            // kt counts this CTA's K tiles from 0 (stage and phase); unit kt / 16 gives the coordinates
             const int my_tiles = chunks * GM_CHUNK_TILES;
             int issued = 0;
             for (int kt = 0; kt < my_tiles; kt++) {
@@ -323,8 +349,9 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
                 if (!mbar_wait(empty(s), ph ^ 1, err, 1)) break;
                 mbar_expect_tx(full(s), GM_STAGE_BYTES);
                 uint8_t* sa = smem + s * GM_STAGE_BYTES;
-                tma_load_2d(smem_u32(sa), &tmA, (kt0 + kt) * GM_BK, m0, full(s));
-                tma_load_2d(smem_u32(sa + GM_A_BYTES), &tmB, (kt0 + kt) * GM_BK, n0, full(s));
+                const int lu = kt / GM_CHUNK_TILES, x = (unit_k0(lu) + kt % GM_CHUNK_TILES) * GM_BK;
+                tma_load_2d(smem_u32(sa), &tmA, x, unit_m0(lu), full(s));
+                tma_load_2d(smem_u32(sa + GM_A_BYTES), &tmB, x, unit_n0(lu), full(s));
                 issued = kt + 1;
             }
             // loads still in flight land in shared memory: wait (bounded) for every issued stage
@@ -406,10 +433,18 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
             mbar_arrive(acc_empty(a));
-        }
-        int* dst = S + blockIdx.y * split_stride + (size_t)(m0 + row) * ldS + n0 + half * COLS;
+            // the tile's last unit of this CTA: its sums go to this CTA's slot of the tile
+            const long long t = unit_tile(c);
+            if (c + 1 == chunks || unit_tile(c + 1) != t) {
+                const int k = (int)blockIdx.x - gm_cta_of(sched, t * sched.chunks);
+                int* dst = S + (((size_t)t * sched.slots + k) * GM_BM + row) * GM_BN + half * COLS;
 #pragma unroll
-        for (int q = 0; q < COLS; q += 4) *reinterpret_cast<int4*>(dst + q) = make_int4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
+                for (int q = 0; q < COLS; q += 4) {
+                    *reinterpret_cast<int4*>(dst + q) = make_int4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
+                    acc[q] = acc[q + 1] = acc[q + 2] = acc[q + 3] = 0;
+                }
+            }
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -516,19 +551,23 @@ static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out
     cudaStream_t s = stream();
     const int Bp = (int)round_up((size_t)B, GM_BN);
     const size_t Mrows = (size_t)8 * k->rows * AJ_D;
-    // split-K: as many K splits as keep one CTA on every SM, each split a whole number of chunks
-    const int chunks = (int)(k->Kp / ((size_t)GM_BK * GM_CHUNK_TILES));
-    const int tiles = (int)(Mrows / GM_BM) * (Bp / GM_BN);
-    int splits = num_sms() / tiles;
-    splits = splits < 1 ? 1 : splits > chunks ? chunks : splits;
-    const int per_split = (chunks + splits - 1) / splits;
-    splits = (chunks + per_split - 1) / per_split;  // no empty split
-    const size_t split_stride = Mrows * (size_t)Bp;
+    // persistent schedule: one CTA per SM (or per unit, when there are fewer), equal unit ranges
+    GmSched sched;
+    sched.tiles_m = (int)(Mrows / GM_BM);
+    sched.chunks = (int)(k->Kp / ((size_t)GM_BK * GM_CHUNK_TILES));
+    const long long tiles = (long long)sched.tiles_m * (Bp / GM_BN);
+    sched.units = tiles * sched.chunks;
+    sched.ctas = (int)std::min<long long>(num_sms(), sched.units);
+    sched.slots = 1;
+    for (long long t = 0; t < tiles; t++)
+        sched.slots = std::max(sched.slots, gm_cta_of(sched, (t + 1) * sched.chunks - 1) -
+                                                gm_cta_of(sched, t * sched.chunks) + 1);
+    const size_t s_ints = (size_t)tiles * sched.slots * GM_BM * GM_BN;
     __nv_bfloat16* zc = nullptr;
     int* S = nullptr;
     int* err = nullptr;
     GB_CUDA_TRY(cudaMallocAsync(&zc, (size_t)Bp * k->Kp * 2, s));
-    GB_CUDA_TRY(cudaMallocAsync(&S, split_stride * splits * 4, s));
+    GB_CUDA_TRY(cudaMallocAsync(&S, s_ints * 4, s));
     GB_CUDA_TRY(cudaMallocAsync(&err, 4, s));
     GB_CUDA_TRY(cudaMemsetAsync(err, 0, 4, s));
     if (((uintptr_t)d_z & 7) == 0)
@@ -544,15 +583,13 @@ static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out
             cudaFuncSetAttribute(ajtai_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GM_SMEM);
             attr = true;
         }
-        dim3 grid((unsigned)(Mrows / GM_BM), (unsigned)splits, (unsigned)(Bp / GM_BN));
         int k_tiles = (int)(k->Kp / GM_BK);
-        ajtai_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, s>>>(k->mapA, mapB, k_tiles, per_split, S, Bp, split_stride,
-                                                            err);
+        ajtai_gemm_kernel<<<sched.ctas, GM_THREADS, GM_SMEM, s>>>(k->mapA, mapB, k_tiles, sched, S, err);
         rc = check_launch("ajtai_gemm_kernel");
     }
     if (!rc) {
         dim3 cg((unsigned)((B + AJ_CB - 1) / AJ_CB), (unsigned)((k->rows * AJ_D + AJ_CB - 1) / AJ_CB));
-        ajtai_combine_kernel<<<cg, 256, 0, s>>>(S, Bp, k->rows, B, splits, split_stride, k->d_RS, d_out);
+        ajtai_combine_kernel<<<cg, 256, 0, s>>>(S, sched, k->rows, B, k->d_RS, d_out);
         rc = check_launch("ajtai_combine_kernel");
     }
     int h_err = 0;
