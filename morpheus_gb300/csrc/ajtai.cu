@@ -76,9 +76,13 @@ __device__ __forceinline__ void centred_digits(u64 m, int* d) {
     d[7] = (int)v;  // |d7| <= 128
 }
 
-// T[(p, i, r)][(j, l)] = s(r,l) d_p(M[i][j][(r-l) mod 64]) as bf16, K padded with zeros to Kp.
-// One block per (i, j), 64 threads (thread r writes 8 rows x 64 columns).
-__global__ void __launch_bounds__(64) ajtai_expand_kernel(const u64* __restrict__ M, int rows, u64 N, size_t Kp,
+// T[(p, i, r)][(j, l)] = s(r,l) d_p(M[i][j][(r-l) mod 64]) as bf16, stored tile by tile as the
+// GEMM reads it: the 128 x 64 tile (m / 128, j) of row m = (p rows + i) 64 + r is 16 KB contiguous
+// at ((m / 128) KT + j) 16 KB, already in the 128-byte swizzled layout (16-byte chunk c of tile
+// row R at (R / 8) 1024 + (R mod 8) 128 + (c ^ (R mod 8)) 16), so that one bulk copy moves it.
+// Tiles past the last ring column (K padded to Kp) are zero.  One block per (i, j), 64 threads
+// (thread r writes 8 rows x 64 columns).
+__global__ void __launch_bounds__(64) ajtai_expand_kernel(const u64* __restrict__ M, int rows, u64 N, size_t KT,
                                                           __nv_bfloat16* __restrict__ T) {
     __shared__ short dig[AJ_D][8];  // the top digit can be +128: not a signed char
     const u64 j = blockIdx.x;
@@ -94,7 +98,9 @@ __global__ void __launch_bounds__(64) ajtai_expand_kernel(const u64* __restrict_
     const size_t row_stride = (size_t)rows * AJ_D;  // rows per digit
 #pragma unroll 1
     for (int p = 0; p < 8; p++) {
-        __nv_bfloat16* dst = T + ((size_t)p * row_stride + (size_t)i * AJ_D + r) * Kp + j * AJ_D;
+        const size_t m = (size_t)p * row_stride + (size_t)i * AJ_D + r;
+        const int R = (int)(m & 127);
+        uint8_t* tile = reinterpret_cast<uint8_t*>(T) + ((m >> 7) * KT + j) * 16384 + (R >> 3) * 1024 + (R & 7) * 128;
 #pragma unroll
         for (int v = 0; v < 8; v++) {
             __align__(16) __nv_bfloat16 w[8];
@@ -105,17 +111,9 @@ __global__ void __launch_bounds__(64) ajtai_expand_kernel(const u64* __restrict_
                 int val = dig[k][p];
                 w[e] = __int2bfloat16_rn(l <= r ? val : -val);
             }
-            *reinterpret_cast<uint4*>(dst + v * 8) = *reinterpret_cast<uint4*>(w);
+            *reinterpret_cast<uint4*>(tile + ((v ^ (R & 7)) << 4)) = *reinterpret_cast<uint4*>(w);
         }
     }
-}
-
-// zero the padded K columns [K, Kp) of every row
-__global__ void ajtai_pad_cols_kernel(__nv_bfloat16* __restrict__ T, size_t nrows, size_t K, size_t Kp) {
-    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    size_t w = Kp - K;
-    if (t >= nrows * w) return;
-    T[(t / w) * Kp + K + t % w] = __int2bfloat16_rn(0);
 }
 
 // rowsum(T)[i][r] mod q = sum_j (2 prefix_r(M_ij) - total(M_ij)), one thread per (i, r)
@@ -184,23 +182,29 @@ __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restric
                                                             int B, const u64* __restrict__ RS,
                                                             u64* __restrict__ out) {
     __shared__ u64 tile[AJ_CB][AJ_CB + 1];
+    __shared__ const int* s_base[8];  // per digit plane: the block's first output row in slot 0 of its tile
+    __shared__ int s_slots[8];        // and how many slots that tile has
     const int IR = rows * AJ_D;
     const int b0 = blockIdx.x * AJ_CB, ir0 = blockIdx.y * AJ_CB;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of 32
     const __int128 Q = (__int128)AGL_Q;
+    if (threadIdx.x < 8) {
+        // rows p IR + ir0 .. +31 lie in one 128-row tile (IR is a multiple of 64, ir0 of 32)
+        const int p = threadIdx.x, m = p * IR + ir0, nt = b0 / GM_BN_C;
+        const long long t = (long long)nt * sched.tiles_m + m / GM_BM_C;
+        s_slots[p] = gm_cta_of(sched, (t + 1) * sched.chunks - 1) - gm_cta_of(sched, t * sched.chunks) + 1;
+        s_base[p] = S + ((size_t)t * sched.slots * GM_BM_C + m % GM_BM_C) * GM_BN_C + b0 % GM_BN_C;
+    }
+    __syncthreads();
     for (int j = ty; j < AJ_CB; j += 8) {
         const int ir = ir0 + j, b = b0 + tx;
         u64 val = 0;
         if (ir < IR && b < B) {
             __int128 acc = 0;
-            const int nt = b / GM_BN_C, col = b % GM_BN_C;
             for (int p = 7; p >= 0; p--) {
-                const int m = p * IR + ir;
-                const long long t = (long long)nt * sched.tiles_m + m / GM_BM_C;
-                const int k_end = gm_cta_of(sched, (t + 1) * sched.chunks - 1) - gm_cta_of(sched, t * sched.chunks);
-                const int* sp = S + ((size_t)t * sched.slots * GM_BM_C + m % GM_BM_C) * GM_BN_C + col;
+                const int* sp = s_base[p] + (size_t)j * GM_BN_C + tx;  // row ir0 + j, witness b0 + tx
                 long long part = 0;  // |each slot| < 2^31
-                for (int k = 0; k <= k_end; k++) part += sp[(size_t)k * GM_BM_C * GM_BN_C];
+                for (int k = 0; k < s_slots[p]; k++) part += sp[(size_t)k * GM_BM_C * GM_BN_C];
                 acc = acc * 256 + (__int128)part;
             }
             __int128 m = acc % Q;
@@ -277,6 +281,13 @@ __device__ __forceinline__ void tma_load_2d(u32 dst, const CUtensorMap* map, int
         : "memory");
 }
 
+// one contiguous global -> shared copy by the async proxy (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(u32 dst, const void* src, u32 bytes, u32 bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
 __device__ __forceinline__ u64 umma_desc_sw128(u32 saddr) {
     u64 d = 0;
@@ -291,7 +302,7 @@ __device__ __forceinline__ u64 umma_desc_sw128(u32 saddr) {
 // instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 256
 constexpr u32 GM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(GM_BN >> 3) << 17) | ((u32)(GM_BM >> 4) << 24);
 
-__global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bfloat16* __restrict__ A_tiled,
                                                                    const __grid_constant__ CUtensorMap tmB, int k_tiles,
                                                                    GmSched sched, int* __restrict__ S,
                                                                    int* __restrict__ err) {
@@ -309,7 +320,6 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
     auto unit_m0 = [&](int lu) { return (int)(unit_tile(lu) % sched.tiles_m) * GM_BM; };
     auto unit_n0 = [&](int lu) { return (int)(unit_tile(lu) / sched.tiles_m) * GM_BN; };
     auto unit_k0 = [&](int lu) { return (int)((u0 + lu) % sched.chunks) * GM_CHUNK_TILES; };
-    (void)k_tiles;
 
     auto full = [&](int s) { return smem_u32(bars + s); };
     auto empty = [&](int s) { return smem_u32(bars + GM_STAGES + s); };
@@ -350,7 +360,9 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __grid_
                 mbar_expect_tx(full(s), GM_STAGE_BYTES);
                 uint8_t* sa = smem + s * GM_STAGE_BYTES;
                 const int lu = kt / GM_CHUNK_TILES, x = (unit_k0(lu) + kt % GM_CHUNK_TILES) * GM_BK;
-                tma_load_2d(smem_u32(sa), &tmA, x, unit_m0(lu), full(s));
+                // the key tile (m0 / 128, x / 64) is 16 KB contiguous and already swizzled
+                bulk_load(smem_u32(sa), A_tiled + ((size_t)(unit_m0(lu) / GM_BM) * k_tiles + x / GM_BK) * (GM_A_BYTES / 2),
+                          GM_A_BYTES, full(s));
                 tma_load_2d(smem_u32(sa + GM_A_BYTES), &tmB, x, unit_n0(lu), full(s));
                 issued = kt + 1;
             }
@@ -496,9 +508,8 @@ struct AjtaiKey {
     u64 N = 0;        // ring columns
     size_t K = 0, Kp = 0;
     u64* d_M = nullptr;              // [rows][N][64]
-    __nv_bfloat16* d_T = nullptr;    // [8 * rows * 64][Kp]
+    __nv_bfloat16* d_T = nullptr;    // 8 * rows * 64 x Kp, tile by tile (ajtai_expand_kernel)
     u64* d_RS = nullptr;             // [rows][64]
-    CUtensorMap mapA;
 };
 
 static size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
@@ -522,19 +533,15 @@ static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* 
     size_t tasks = (size_t)rows * N * 8;
     ajtai_prg_kernel<<<grid_for(tasks, 256), 256, 0, s>>>(d_key, row_lo, rows, 0, N, k->d_M);
     GB_LAUNCH_CHECK("ajtai_prg_kernel");
+    if (k->Kp > k->K) GB_CUDA_TRY(cudaMemsetAsync(k->d_T, 0, Mrows * k->Kp * 2, s));  // the padding tiles
     dim3 g((unsigned)N, (unsigned)rows);
-    ajtai_expand_kernel<<<g, 64, 0, s>>>(k->d_M, rows, N, k->Kp, k->d_T);
+    ajtai_expand_kernel<<<g, 64, 0, s>>>(k->d_M, rows, N, k->Kp / GM_BK, k->d_T);
     GB_LAUNCH_CHECK("ajtai_expand_kernel");
-    if (k->Kp > k->K) {
-        size_t work = Mrows * (k->Kp - k->K);
-        ajtai_pad_cols_kernel<<<grid_for(work, 256), 256, 0, s>>>(k->d_T, Mrows, k->K, k->Kp);
-        GB_LAUNCH_CHECK("ajtai_pad_cols_kernel");
-    }
     ajtai_rowsum_kernel<<<grid_for((size_t)rows * AJ_D, 64), 64, 0, s>>>(k->d_M, rows, N, k->d_RS);
     GB_LAUNCH_CHECK("ajtai_rowsum_kernel");
     cudaFreeAsync(d_key, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
-    return make_map(&k->mapA, k->d_T, k->Kp, Mrows, GM_BM);
+    return GB_OK;
 }
 
 static void key_free(AjtaiKey* k) {
@@ -584,7 +591,7 @@ static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out
             attr = true;
         }
         int k_tiles = (int)(k->Kp / GM_BK);
-        ajtai_gemm_kernel<<<sched.ctas, GM_THREADS, GM_SMEM, s>>>(k->mapA, mapB, k_tiles, sched, S, err);
+        ajtai_gemm_kernel<<<sched.ctas, GM_THREADS, GM_SMEM, s>>>(k->d_T, mapB, k_tiles, sched, S, err);
         rc = check_launch("ajtai_gemm_kernel");
     }
     if (!rc) {
