@@ -52,7 +52,10 @@ def test_batched_matches_reference(gpu_lib, golden):
     assert [int(x) for x in out.reshape(-1)] == g["out"]
 
 
-@pytest.mark.parametrize("n_ring,B,row_lo,rows", [(16, 3, 0, 16), (40, 5, 0, 16), (8, 130, 3, 2), (33, 1, 40, 2)])
+# shapes cover one and several K chunks per tile, tiles whose chunks span many CTAs of the
+# persistent schedule (1 row x 1024 ring columns: 38 slots), two witness tiles (B > 256) and K padding
+@pytest.mark.parametrize("n_ring,B,row_lo,rows", [(16, 3, 0, 16), (40, 5, 0, 16), (8, 130, 3, 2), (33, 1, 40, 2),
+                                                  (1024, 2, 0, 1), (64, 300, 5, 1)])
 def test_batched_vs_oracle(gpu_lib, n_ring, B, row_lo, rows):
     from morpheus_gb300.ajtai import AjtaiKey
     key = np.array([9, 8, 7, 6, 5, 4, 3, 2], np.uint32)
@@ -80,6 +83,27 @@ def test_batched_extremes_and_batch_invariance(gpu_lib):
     # a witness's commitment does not depend on its batch position or companions
     out2 = k.commit_u8_batched(z[[2, 3, 1]])
     assert np.array_equal(out2, out[[2, 3, 1]])
+
+
+def test_batched_unaligned_witness_pointer(gpu_lib):
+    """A witness array that is not 8-byte aligned takes the one-coefficient-per-thread prep."""
+    import ctypes
+    from morpheus_gb300.ajtai import AjtaiKey
+    from morpheus_gb300.memory import DeviceBuffer
+    key = np.array([3, 1, 4, 1, 5, 9, 2, 6], np.uint32)
+    n_ring, B = 16, 3
+    z8 = np.random.default_rng(5).integers(0, 256, size=(B, n_ring * 64), dtype=np.uint8)
+    raw = np.zeros(B * n_ring * 64 + 8, np.uint8)
+    raw[1:1 + z8.size] = z8.reshape(-1)
+    buf = DeviceBuffer.from_numpy(raw)
+
+    class _At:  # a device address one byte into the buffer
+        ptr = ctypes.c_void_p(buf.ptr.value + 1)
+
+    k = AjtaiKey(key, 0, 2, n_ring)
+    out = k.commit_u8_batched((_At(), B))
+    assert np.array_equal(out, k.commit_u8_batched(z8))
+    assert np.array_equal(out[[0, 2]], O.ajtai_commit_u8_batch(key, z8[[0, 2]], row_lo=0, nrows=2))
 
 
 def test_batched_equals_wide_rows(gpu_lib):
