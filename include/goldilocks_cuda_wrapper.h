@@ -359,16 +359,19 @@ int gb_prover_destroy(void *prover);
 int gb_batch_prove(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *insts, int count,
                    int workers, size_t hbm_budget);
 
-/* The same batch as gb_batch_prove with the openings run round-synchronously: commits and
- * sumchecks on `workers` threads, then every round of every polynomial's opening as one launch
- * per step for all polynomials (and one per Merkle layer), with one host round trip per round.
+/* The same batch as gb_batch_prove, round-synchronously: the commits of all polynomials, then
+ * every round of every instance's product sumcheck as one launch per degree, then every round
+ * of every polynomial's opening as one launch per step for all polynomials (and one per Merkle
+ * layer), with one host round trip per round; the host steps of the per-instance transcripts
+ * run on up to 16 threads.  `workers` must be >= 1 and is otherwise unused by this engine.
  * Instances that do not fit hbm_budget together run in waves, largest first.  Proofs are
  * identical to gb_prove_instance's.  table: log_rate 1.  Synchronising. */
 int gb_batch_prove_lockstep(void *table, const uint64_t master_seed[2], int num_queries, const gb_instance *insts,
                             int count, int workers, size_t hbm_budget);
 /* Host wall time of the calling thread's last gb_batch_prove_lockstep: the commit + sumcheck
- * phase and the opening phase, summed over its waves (either pointer may be NULL). */
-void gb_lockstep_last_timing(double *commit_sumcheck_ms, double *open_ms);
+ * phase, the opening phase and the sumcheck part of the first, summed over its waves (any
+ * pointer may be NULL). */
+void gb_lockstep_last_timing(double *commit_sumcheck_ms, double *open_ms, double *sumcheck_ms);
 
 /* A quantized matmul layer C = A B as a served job (no reference counterpart; the field work
  * of zk-torch-3/src/basicblock/einsum.rs:807-1000): A is m x k, B is k x n (row-major int8),

@@ -1,8 +1,10 @@
 // Round-synchronous batch prover: many instances (gb_instance, the protocol of batch.cu) with
 // their Basefold openings run in lockstep, so that every step of a round is ONE launch over
 // all polynomials (ragged segment tables) instead of one launch per polynomial:
-//   1. commits and product sumchecks: a pool of worker threads, a stream each (as in the
-//      prover service), keeping every commitment resident;
+//   1. commits in lockstep (transform passes, codewords, leaf hashes, layers), then the product
+//      sumchecks in lockstep: for round k, one launch per degree over every instance still in
+//      its protocol, one reduce launch for all the messages and one host round trip in which
+//      every instance's transcript advances; every commitment stays resident;
 //   2. openings: for round r = 0, 1, ... on the calling thread's stream, one launch each for
 //      the eq/bh fold + oracle partials, their per-polynomial reduction, the codeword fold +
 //      leaf hash, every Merkle layer, the roots and the final folds of all polynomials still
@@ -14,7 +16,10 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <thread>
@@ -26,6 +31,7 @@
 #include "host_field.hpp"
 #include "merkle.cuh"
 #include "reduce.cuh"
+#include "sc_device.cuh"
 
 namespace gb {
 
@@ -254,22 +260,90 @@ __global__ void ls_query_kernel(const QueryJob* __restrict__ jobs, const u64* __
 // ---------------------------------------------------------------------------
 static size_t align2(size_t w) { return (w + 1) & ~(size_t)1; }  // 16-byte multiples of words
 
-// fn(i) for i in [0, count) on up to 16 host threads (each polynomial's transcript is its own,
-// so the per-polynomial steps between rounds run in parallel)
+// Host threads for the per-polynomial steps between rounds (each polynomial's transcript is its
+// own, so they run in parallel).  The threads are started once and wait between jobs: a round
+// trip of the engine should not pay for thread creation.  One job at a time (jobs are issued
+// by the calling thread of a batch, and concurrent batches take turns).
+class LsPool {
+  public:
+    static LsPool& get() {
+        static LsPool pool;
+        return pool;
+    }
+    // fn(i) for i in [0, count), split into ranges among the pool and the calling thread
+    void run(size_t count, const std::function<void(size_t)>& fn) {
+        const size_t nt = std::min<size_t>(workers_.size() + 1, (count + 63) / 64);
+        if (nt <= 1) {
+            for (size_t i = 0; i < count; i++) fn(i);
+            return;
+        }
+        std::lock_guard<std::mutex> job_lock(job_);
+        {
+            std::lock_guard<std::mutex> l(m_);
+            fn_ = &fn;
+            count_ = count;
+            parts_ = nt;
+            next_part_ = 1;  // part 0 is the calling thread's
+            done_ = 0;
+            gen_++;
+        }
+        cv_.notify_all();
+        part(0);
+        std::unique_lock<std::mutex> l(m_);
+        done_cv_.wait(l, [&] { return done_ == parts_ - 1; });
+        fn_ = nullptr;
+    }
+    ~LsPool() {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            stop_ = true;
+            gen_++;
+        }
+        cv_.notify_all();
+        for (auto& t : workers_) t.join();
+    }
+
+  private:
+    LsPool() {
+        const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+        const size_t n = std::min<size_t>(hw, 16) - 1;
+        for (size_t t = 0; t < n; t++) workers_.emplace_back([this] { loop(); });
+    }
+    void part(size_t k) {
+        for (size_t i = k * count_ / parts_; i < (k + 1) * count_ / parts_; i++) (*fn_)(i);
+    }
+    void loop() {
+        unsigned long long seen = 0;
+        for (;;) {
+            size_t k;
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [&] { return stop_ || (gen_ != seen && next_part_ < parts_); });
+                if (stop_) return;
+                k = next_part_++;
+                if (next_part_ >= parts_) seen = gen_;
+            }
+            part(k);
+            {
+                std::lock_guard<std::mutex> l(m_);
+                done_++;
+            }
+            done_cv_.notify_one();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex job_, m_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t)>* fn_ = nullptr;
+    size_t count_ = 0, parts_ = 0, next_part_ = 0, done_ = 0;
+    unsigned long long gen_ = 0;
+    bool stop_ = false;
+};
+
 template <typename F>
 static void ls_parallel(size_t count, F fn) {
-    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-    const size_t nt = std::min<size_t>(std::min<size_t>(hw, 16), (count + 63) / 64);
-    if (nt <= 1) {
-        for (size_t i = 0; i < count; i++) fn(i);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (size_t t = 0; t < nt; t++)
-        th.emplace_back([&, t] {
-            for (size_t i = t * count / nt; i < (t + 1) * count / nt; i++) fn(i);
-        });
-    for (auto& x : th) x.join();
+    const std::function<void(size_t)> f = fn;
+    LsPool::get().run(count, f);
 }
 
 struct LsPoly {
@@ -843,6 +917,371 @@ class LsCommitter {
 };
 
 // ---------------------------------------------------------------------------
+// Product sumchecks of a wave in lockstep.  Round k of every instance still in its protocol is
+// one launch per degree (block -> instance by binary search over the segment table), then one
+// reduce launch writes every instance's message into mapped pinned records, then one host round
+// trip advances every instance's own transcript; the final folds are one launch.  Each instance's
+// transcript steps and arithmetic are those of gb_sumcheck_prove_ext2 (sumcheck.cu), so its
+// proof is identical to the per-call one.
+// ---------------------------------------------------------------------------
+constexpr int LSC_MAX_D = 8;
+constexpr int LSC_W = 2 * (LSC_MAX_D + 1);  // message words of the largest degree (partials stride)
+constexpr int LSC_FIN = 2 * LSC_MAX_D;      // final-value words per instance
+constexpr int LSC_ITEMS = 2;                // pairs per thread
+
+struct ScSeg {
+    const u64* in;               // this round's input level (the base polynomials in rounds 0 and 1)
+    u64* out;                    // the folded level (rounds >= 1)
+    u64 in_stride, out_stride;   // elements per polynomial
+    u64 r0, r1;                  // the previous round's challenge (rounds >= 1; the last one for the finals)
+    u64 items;                   // pairs: input pairs in round 0, output pairs later
+    u64 block0;                  // first block of this instance in its launch
+    u64 pblock0;                 // its first row of the round's partials
+    u64 rec;                     // record slot (position in the wave)
+    u64 d;                       // degree
+};
+
+__device__ __forceinline__ int sc_find(const ScSeg* __restrict__ segs, int nseg, u64 block) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].block0 <= block) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// MODE 0: round 0 (base input, message only); 1: round 1 (fold the base input into Ext2, message);
+// 2: rounds >= 2 (fold Ext2, message).  Same per-pair math as sc_round0_kernel<D, true> and
+// sc_fold_round_e2_kernel<D, BASE_IN>.
+template <int D, int MODE>
+__global__ void __launch_bounds__(RED_THREADS) ls_sc_round_kernel(const ScSeg* __restrict__ segs, int nseg,
+                                                                  u64* __restrict__ partials) {
+    __shared__ int s_seg;
+    if (threadIdx.x == 0) s_seg = sc_find(segs, nseg, blockIdx.x);
+    __syncthreads();
+    const ScSeg sg = segs[s_seg];
+    constexpr int W = 2 * (D + 1);
+    u64 acc[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    const bool vec = aligned16(sg.in);
+    const e2 r = e2_make(sg.r0, sg.r1);
+    const u64 base = (blockIdx.x - sg.block0) * (u64)RED_THREADS * LSC_ITEMS;
+#pragma unroll
+    for (int it = 0; it < LSC_ITEMS; it++) {
+        const u64 y = base + (u64)it * RED_THREADS + threadIdx.x;
+        if (y >= sg.items) continue;
+        if constexpr (MODE == 0) {
+            u64 e[D], dl[D];
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+                u64 a, b;
+                ld_pair(sg.in + (size_t)i * sg.in_stride + 2 * y, vec, a, b);
+                e[i] = a;
+                dl[i] = gl_sub(b, a);
+            }
+            u64 bacc[D + 1];
+#pragma unroll
+            for (int c = 0; c <= D; c++) bacc[c] = 0;
+            accum_base<D>(e, dl, bacc);
+#pragma unroll
+            for (int c = 0; c <= D; c++) acc[2 * c] = gl_add(acc[2 * c], bacc[c]);
+        } else {
+            e2 e[D], dl[D];
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+                e2 a, b;
+                if constexpr (MODE == 1) {
+                    const u64* p = sg.in + (size_t)i * sg.in_stride + 4 * y;
+                    u64 x0, x1, x2, x3;
+                    ld_pair(p, vec, x0, x1);
+                    ld_pair(p + 2, vec, x2, x3);
+                    const u64 d0 = gl_sub(x1, x0), d1 = gl_sub(x3, x2);
+                    a = e2_make(gl_add(x0, gl_mul(sg.r0, d0)), gl_mul(sg.r1, d0));
+                    b = e2_make(gl_add(x2, gl_mul(sg.r0, d1)), gl_mul(sg.r1, d1));
+                } else {
+                    const u64* p = sg.in + (size_t)i * 2 * sg.in_stride + 8 * y;
+                    const e2 x0 = ld_e2(p, true), x1 = ld_e2(p + 2, true), x2 = ld_e2(p + 4, true),
+                             x3 = ld_e2(p + 6, true);
+                    a = e2_add(x0, e2_mul(r, e2_sub(x1, x0)));
+                    b = e2_add(x2, e2_mul(r, e2_sub(x3, x2)));
+                }
+                u64* q = sg.out + (size_t)i * 2 * sg.out_stride + 4 * y;
+                e2_st(q, a);
+                e2_st(q + 2, b);
+                e[i] = a;
+                dl[i] = e2_sub(b, a);
+            }
+            accum_e2<D>(e, dl, acc);
+        }
+    }
+    block_reduce<W>(acc);
+    if (threadIdx.x == 0) {
+        u64* dst = partials + (sg.pblock0 + (blockIdx.x - sg.block0)) * LSC_W;
+#pragma unroll
+        for (int w = 0; w < W; w++) dst[w] = acc[w];
+    }
+}
+
+static u64 lsc_blocks(u64 items) {
+    const u64 per = (u64)RED_THREADS * LSC_ITEMS;
+    return items ? (items + per - 1) / per : 1;
+}
+
+// each instance's message: the sum of its blocks' partials, canonical; one warp per instance
+__global__ void ls_sc_reduce_kernel(const ScSeg* __restrict__ segs, int nseg, const u64* __restrict__ partials,
+                                    u64* __restrict__ recs) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nseg) return;
+    const ScSeg sg = segs[w];
+    const u64 per = (u64)RED_THREADS * LSC_ITEMS;
+    const u64 nb = sg.items ? (sg.items + per - 1) / per : 1;
+    const int words = 2 * ((int)sg.d + 1);
+    u64 acc[LSC_W];
+#pragma unroll
+    for (int k = 0; k < LSC_W; k++) acc[k] = 0;
+    for (u64 b = lane; b < nb; b += 32)
+#pragma unroll
+        for (int k = 0; k < LSC_W; k++)
+            if (k < words) acc[k] = gl_add(acc[k], partials[(sg.pblock0 + b) * LSC_W + k]);
+#pragma unroll
+    for (int k = 0; k < LSC_W; k++) {
+        const u64 v = gl_warp_sum(acc[k]);
+        if (lane == 0 && k < words) recs[sg.rec * LSC_W + k] = gl_canon(v);
+    }
+}
+
+// each instance's final values: its last level (2 elements per polynomial) folded with its last
+// challenge; one block per instance, thread i folds polynomial i (as sc_final_kernel<true, false>)
+__global__ void ls_sc_final_kernel(const ScSeg* __restrict__ segs, int nseg, u64* __restrict__ fins) {
+    if ((int)blockIdx.x >= nseg) return;
+    const ScSeg sg = segs[blockIdx.x];
+    const int i = threadIdx.x;
+    if (i >= (int)sg.d) return;
+    const u64* p = sg.in + (size_t)i * 2 * sg.in_stride;
+    const e2 a = e2_make(p[0], p[1]), b = e2_make(p[2], p[3]);
+    const e2 f = e2_canon(e2_add(a, e2_mul(e2_make(sg.r0, sg.r1), e2_sub(b, a))));
+    fins[sg.rec * LSC_FIN + 2 * i] = f.c0;
+    fins[sg.rec * LSC_FIN + 2 * i + 1] = f.c1;
+}
+
+template <int D>
+static void lsc_launch(int mode, unsigned blocks, const ScSeg* segs, int nseg, u64* partials, cudaStream_t s) {
+    if (mode == 0) ls_sc_round_kernel<D, 0><<<blocks, RED_THREADS, 0, s>>>(segs, nseg, partials);
+    else if (mode == 1) ls_sc_round_kernel<D, 1><<<blocks, RED_THREADS, 0, s>>>(segs, nseg, partials);
+    else ls_sc_round_kernel<D, 2><<<blocks, RED_THREADS, 0, s>>>(segs, nseg, partials);
+}
+static void lsc_launch_d(int d, int mode, unsigned blocks, const ScSeg* segs, int nseg, u64* partials, cudaStream_t s) {
+    switch (d) {
+        case 1: lsc_launch<1>(mode, blocks, segs, nseg, partials, s); break;
+        case 2: lsc_launch<2>(mode, blocks, segs, nseg, partials, s); break;
+        case 3: lsc_launch<3>(mode, blocks, segs, nseg, partials, s); break;
+        case 4: lsc_launch<4>(mode, blocks, segs, nseg, partials, s); break;
+        case 5: lsc_launch<5>(mode, blocks, segs, nseg, partials, s); break;
+        case 6: lsc_launch<6>(mode, blocks, segs, nseg, partials, s); break;
+        case 7: lsc_launch<7>(mode, blocks, segs, nseg, partials, s); break;
+        default: lsc_launch<8>(mode, blocks, segs, nseg, partials, s); break;
+    }
+}
+
+// The product sumchecks of the wave's instances (their roots already in their proofs), all
+// rounds in lockstep.  polys[k]: instance wave[k]'s d base polynomials of 2^n values on the device.
+static int ls_sumchecks(const u64 seed[2], const gb_instance* insts, const std::vector<int>& wave,
+                        const std::vector<const u64*>& polys) {
+    using namespace host;
+    cudaStream_t s = stream();
+    const int nw = (int)wave.size();
+    if (!nw) return GB_OK;
+    struct St {
+        int n = 0, d = 0;
+        u64 N = 0;
+        u64* buf[2] = {nullptr, nullptr};
+        const u64* cur = nullptr;
+        u64 cur_stride = 0;
+        int pp = 0;
+        E2 r{0, 0};
+        gb_transcript t;
+    };
+    std::vector<St> st(nw);
+    size_t ws_words = 0, max_blocks = 1;
+    int maxn = 0;
+    for (int k = 0; k < nw; k++) {
+        const gb_instance& in = insts[wave[k]];
+        St& x = st[k];
+        x.n = in.num_vars;
+        x.d = in.degree;
+        x.N = (u64)1 << x.n;
+        maxn = std::max(maxn, x.n);
+        ws_words += 2 * (size_t)x.d * x.N;  // two levels of d x N/2 Ext2 values
+        max_blocks += lsc_blocks(x.N >> 1);
+    }
+    u64 *ws = nullptr, *partials = nullptr, *h_recs = nullptr, *d_recs = nullptr;
+    ScSeg *h_segs = nullptr, *d_segs = nullptr;
+    int rc = GB_OK;
+    auto cleanup = [&] {
+        if (ws) cudaFreeAsync(ws, s);
+        if (partials) cudaFreeAsync(partials, s);
+        if (d_segs) cudaFreeAsync(d_segs, s);
+        cudaStreamSynchronize(s);
+        if (h_recs) cudaFreeHost(h_recs);
+        if (h_segs) cudaFreeHost(h_segs);
+    };
+    auto fail = [&](const char* where, cudaError_t e) {
+        set_error(where, e);
+        cleanup();
+        return GB_ECUDA;
+    };
+    cudaError_t e = cudaMallocAsync(&ws, ws_words * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&partials, max_blocks * LSC_W * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_segs, (size_t)nw * sizeof(ScSeg), s);
+    if (e == cudaSuccess) e = cudaMallocHost(&h_recs, (size_t)nw * (LSC_W + LSC_FIN) * 8);
+    if (e == cudaSuccess) e = cudaMallocHost(&h_segs, (size_t)nw * sizeof(ScSeg));
+    if (e == cudaSuccess) {
+        void* d = nullptr;
+        e = cudaHostGetDevicePointer(&d, h_recs, 0);
+        d_recs = (u64*)d;
+    }
+    if (e != cudaSuccess) return fail("lockstep sumcheck workspace", e);
+    u64* h_fins = h_recs + (size_t)nw * LSC_W;
+    u64* d_fins = d_recs + (size_t)nw * LSC_W;
+    {
+        u64* cur = ws;
+        for (int k = 0; k < nw; k++) {
+            St& x = st[k];
+            x.buf[0] = cur;
+            cur += (size_t)x.d * x.N;
+            x.buf[1] = cur;
+            cur += (size_t)x.d * x.N;
+            x.cur = polys[k];
+            x.cur_stride = x.N;
+        }
+    }
+    // each instance's transcript, up to its first round (ls_sumcheck, gb_sumcheck_prove_ext2)
+    ls_parallel(nw, [&](size_t k) {
+        const gb_instance& in = insts[wave[k]];
+        St& x = st[k];
+        gb_transcript_new(&x.t, "sumcheck");
+        tr_append_ext2(&x.t, "", E2{canon(seed[0]), canon(seed[1])});
+        tr_append_u64(&x.t, "", in.index);
+        for (int w = 0; w < 4 * x.d; w++) tr_append_u64(&x.t, "", in.h_proof[w]);
+        tr_append_u64(&x.t, "num_var", (u64)x.n);
+        tr_append_u64(&x.t, "num_poly", (u64)x.d);
+    });
+    std::vector<int> active;
+    for (int k = 0; k < maxn && !rc; k++) {
+        // the instances still in the protocol, grouped by degree
+        active.clear();
+        for (int dd = 1; dd <= LSC_MAX_D; dd++)
+            for (int w = 0; w < nw; w++)
+                if (st[w].d == dd && st[w].n > k) active.push_back(w);
+        const int mode = k == 0 ? 0 : k == 1 ? 1 : 2;
+        u64 pblock = 0;
+        for (size_t a = 0; a < active.size(); a++) {
+            St& x = st[active[a]];
+            ScSeg& g = h_segs[a];
+            g.in = x.cur;
+            g.in_stride = x.cur_stride;
+            g.out = k == 0 ? nullptr : x.buf[x.pp];
+            g.out_stride = x.N >> 1;
+            g.r0 = x.r.c0;
+            g.r1 = x.r.c1;
+            g.items = x.N >> (k + 1);
+            g.pblock0 = pblock;
+            g.rec = (u64)active[a];
+            g.d = (u64)x.d;
+            pblock += lsc_blocks(g.items);
+        }
+        // block0 is relative to the launch of the segment's degree
+        for (size_t a = 0; a < active.size();) {
+            size_t b = a;
+            u64 nb = 0;
+            while (b < active.size() && st[active[b]].d == st[active[a]].d) {
+                h_segs[b].block0 = nb;
+                nb += lsc_blocks(h_segs[b].items);
+                b++;
+            }
+            a = b;
+        }
+        e = cudaMemcpyAsync(d_segs, h_segs, active.size() * sizeof(ScSeg), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return fail("lockstep sumcheck segments", e);
+        for (size_t a = 0; a < active.size();) {
+            size_t b = a;
+            u64 nb = 0;
+            while (b < active.size() && st[active[b]].d == st[active[a]].d) nb += lsc_blocks(h_segs[b++].items);
+            lsc_launch_d(st[active[a]].d, mode, (unsigned)nb, d_segs + a, (int)(b - a), partials, s);
+            rc = check_launch("ls_sc_round_kernel");
+            if (rc) break;
+            a = b;
+        }
+        if (rc) break;
+        ls_sc_reduce_kernel<<<(unsigned)((active.size() * 32 + 255) / 256), 256, 0, s>>>(d_segs, (int)active.size(),
+                                                                                        partials, d_recs);
+        rc = check_launch("ls_sc_reduce_kernel");
+        if (rc) break;
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail("lockstep sumcheck round", e);
+        ls_parallel(active.size(), [&](size_t a) {
+            const int w = active[a];
+            St& x = st[w];
+            const gb_instance& in = insts[wave[w]];
+            const int words = 2 * (x.d + 1);
+            const u64* m = h_recs + (size_t)w * LSC_W;
+            u64* msgs = in.h_proof + (size_t)x.d * 4 + (size_t)k * words;
+            for (int c = 0; c < words; c++) msgs[c] = m[c];
+            for (int c = 0; c <= x.d; c++) tr_append_ext2(&x.t, "round_message", E2{m[2 * c], m[2 * c + 1]});
+            x.r = tr_challenge_ext2(&x.t, "challenge");
+            u64* chal = in.h_proof + (size_t)x.d * 4 + (size_t)x.n * words;
+            chal[2 * k] = x.r.c0;
+            chal[2 * k + 1] = x.r.c1;
+            if (k >= 1) {
+                x.cur = x.buf[x.pp];
+                x.cur_stride = x.N >> 1;
+                x.pp ^= 1;
+            }
+        });
+    }
+    if (!rc) {
+        // the final values: every instance's last level folded with its last challenge
+        for (int w = 0; w < nw; w++) {
+            St& x = st[w];
+            ScSeg& g = h_segs[w];
+            g = ScSeg{};
+            g.in = x.cur;
+            g.in_stride = x.cur_stride;
+            g.r0 = x.r.c0;
+            g.r1 = x.r.c1;
+            g.rec = (u64)w;
+            g.d = (u64)x.d;
+        }
+        e = cudaMemcpyAsync(d_segs, h_segs, (size_t)nw * sizeof(ScSeg), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return fail("lockstep sumcheck finals", e);
+        ls_sc_final_kernel<<<(unsigned)nw, 32, 0, s>>>(d_segs, nw, d_fins);
+        rc = check_launch("ls_sc_final_kernel");
+        if (!rc) {
+            e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return fail("lockstep sumcheck finals", e);
+            for (int w = 0; w < nw; w++) {
+                St& x = st[w];
+                const gb_instance& in = insts[wave[w]];
+                const int words = 2 * (x.d + 1);
+                u64* finals = in.h_proof + (size_t)x.d * 4 + (size_t)x.n * words + (size_t)x.n * 2;
+                E2 fe{1, 0};
+                for (int i = 0; i < x.d; i++) {
+                    finals[2 * i] = h_fins[(size_t)w * LSC_FIN + 2 * i];
+                    finals[2 * i + 1] = h_fins[(size_t)w * LSC_FIN + 2 * i + 1];
+                    fe = e2mul(fe, E2{finals[2 * i], finals[2 * i + 1]});
+                }
+                finals[2 * x.d] = fe.c0;
+                finals[2 * x.d + 1] = fe.c1;
+            }
+        }
+    }
+    cleanup();
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
 // driver: waves of instances; commits + sumchecks on worker threads, openings in lockstep
 // ---------------------------------------------------------------------------
 // words of an instance proof before its openings (batch.cu's layout)
@@ -858,25 +1297,8 @@ static size_t ls_inst_bytes(const gb_instance& in) {
            ((size_t)1 << 20);
 }
 
-// the product sumcheck of one instance (roots already in its proof), on the calling thread's stream
-static int ls_sumcheck(const u64 seed[2], const gb_instance& in, const u64* polys) {
-    using namespace host;
-    const int n = in.num_vars, d = in.degree;
-    u64* roots = in.h_proof;
-    u64* msgs = roots + (size_t)d * 4;
-    u64* chal = msgs + (size_t)n * (d + 1) * 2;
-    u64* finals = chal + (size_t)n * 2;
-    u64* fe = finals + (size_t)d * 2;
-    gb_transcript t;
-    gb_transcript_new(&t, "sumcheck");
-    tr_append_ext2(&t, "", E2{canon(seed[0]), canon(seed[1])});
-    tr_append_u64(&t, "", in.index);
-    for (int k = 0; k < 4 * d; k++) tr_append_u64(&t, "", roots[k]);
-    return gb_sumcheck_prove_ext2(&t, n, d, polys, nullptr, msgs, chal, finals, fe);
-}
-
 // wall time of the last lockstep batch on this thread: commits + sumchecks, openings
-static thread_local double t_ls_ms[2] = {0, 0};
+static thread_local double t_ls_ms[3] = {0, 0, 0};  // commit + sumcheck, open, of which sumcheck
 
 static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instance* insts, int count, int workers,
                           size_t budget) {
@@ -898,10 +1320,8 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return ls_inst_bytes(insts[a]) > ls_inst_bytes(insts[b]); });
-    int dev = 0;
-    GB_CUDA_TRY(cudaGetDevice(&dev));
     const size_t coop = gb_get_coop_threshold(), top = gb_get_merkle_top_nodes();
-    t_ls_ms[0] = t_ls_ms[1] = 0;
+    t_ls_ms[0] = t_ls_ms[1] = t_ls_ms[2] = 0;
     size_t next = 0;
     while (next < order.size()) {
         // the wave: largest remaining first, as many as fit the budget (at least one)
@@ -965,38 +1385,10 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
                 for (int j = 0; j < in.degree; j++)
                     for (int w = 0; w < 4; w++) in.h_proof[4 * j + w] = jobs[first_job[k] + j].com.root[w];
             }
-        // product sumchecks on the worker threads
-        std::vector<int> rcs(wave.size(), GB_OK);
-        std::vector<std::string> errs(wave.size());
-        if (!rc) {
-            std::atomic<size_t> cursor{0};
-            const int nt = (int)std::min<size_t>((size_t)workers, wave.size());
-            std::vector<std::thread> th;
-            for (int w = 0; w < nt; w++)
-                th.emplace_back([&] {
-                    cudaStream_t st = nullptr;
-                    if (cudaSetDevice(dev) != cudaSuccess ||
-                        cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
-                        st = nullptr;
-                    if (st) gb_set_stream(st);
-                    for (size_t k; (k = cursor.fetch_add(1)) < wave.size();) {
-                        int r = st ? ls_sumcheck(seed, insts[wave[k]], polys[k]) : GB_ECUDA;
-                        rcs[k] = r;
-                        if (r) errs[k] = st ? gb_last_error() : "stream creation failed";
-                    }
-                    if (st) {
-                        cudaStreamSynchronize(st);
-                        gb_set_stream(nullptr);
-                        cudaStreamDestroy(st);
-                    }
-                });
-            for (auto& t : th) t.join();
-            for (size_t k = 0; k < wave.size() && !rc; k++)
-                if (rcs[k]) {
-                    rc = rcs[k];
-                    set_error_msg(errs[k]);
-                }
-        }
+        // product sumchecks of the wave, all rounds in lockstep
+        const auto ts = std::chrono::steady_clock::now();
+        if (!rc) rc = ls_sumchecks(seed, insts, wave, polys);
+        t_ls_ms[2] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ts).count();
         auto t1 = std::chrono::steady_clock::now();
         t_ls_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
         if (!rc) {
@@ -1048,9 +1440,10 @@ int gb_batch_prove_lockstep(void* table, const uint64_t master_seed[2], int num_
     return lockstep_prove(table, master_seed, num_queries, insts, count, workers, hbm_budget);
 }
 
-void gb_lockstep_last_timing(double* commit_sumcheck_ms, double* open_ms) {
+void gb_lockstep_last_timing(double* commit_sumcheck_ms, double* open_ms, double* sumcheck_ms) {
     if (commit_sumcheck_ms) *commit_sumcheck_ms = t_ls_ms[0];
     if (open_ms) *open_ms = t_ls_ms[1];
+    if (sumcheck_ms) *sumcheck_ms = t_ls_ms[2];
 }
 
 }  // extern "C"

@@ -146,6 +146,7 @@ def test_lockstep_engine_equals_alone(tables, budget, device):
     gt, ot = tables
     rng = np.random.default_rng(21)
     specs = [(int(rng.integers(2, TABLE_NV + 1)), int(rng.integers(1, 5))) for _ in range(20)] + [(2, 1), (TABLE_NV, 4)]
+    specs += [(3, 8), (6, 5)]  # the largest degrees of the sumcheck's lockstep kernels
     alone = [make(n, d, k, 300 + k) for k, (n, d) in enumerate(specs)]
     for inst in alone:
         batch.prove_instance(gt, SEED, inst)
