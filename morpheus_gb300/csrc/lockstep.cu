@@ -1219,6 +1219,9 @@ static int ls_sumchecks(const u64 seed[2], const gb_instance* insts, const std::
                                                                                         partials, d_recs);
         rc = check_launch("ls_sc_reduce_kernel");
         if (rc) break;
+        // every instance's first message label does not depend on the message: absorb it while the
+        // round runs on the device (the absorb sequence is unchanged)
+        ls_parallel(active.size(), [&](size_t a) { tr_label(&st[active[a]].t, "round_message"); });
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return fail("lockstep sumcheck round", e);
         ls_parallel(active.size(), [&](size_t a) {
@@ -1229,7 +1232,9 @@ static int ls_sumchecks(const u64 seed[2], const gb_instance* insts, const std::
             const u64* m = h_recs + (size_t)w * LSC_W;
             u64* msgs = in.h_proof + (size_t)x.d * 4 + (size_t)k * words;
             for (int c = 0; c < words; c++) msgs[c] = m[c];
-            for (int c = 0; c <= x.d; c++) tr_append_ext2(&x.t, "round_message", E2{m[2 * c], m[2 * c + 1]});
+            tr_absorb(&x.t, m[0]);
+            tr_absorb(&x.t, m[1]);
+            for (int c = 1; c <= x.d; c++) tr_append_ext2(&x.t, "round_message", E2{m[2 * c], m[2 * c + 1]});
             x.r = tr_challenge_ext2(&x.t, "challenge");
             u64* chal = in.h_proof + (size_t)x.d * 4 + (size_t)x.n * words;
             chal[2 * k] = x.r.c0;

@@ -595,18 +595,24 @@ static int prove(gb_transcript* t, int n, int d, const u64* d_polys, const u64* 
             }
             if (rc) return rc;
             const int words = W * (d + 1);
+            // the first message's label does not depend on the message: absorb it while the
+            // round runs on the device (the absorb sequence is unchanged)
+            tr_label(t, "round_message");
             GB_CUDA_TRY(cudaStreamSynchronize(s));
             u64* m = h_msgs + (size_t)k * words;
             for (int i = 0; i < words; i++) m[i] = stage[i];
             if (ext) {
-                for (int c = 0; c <= d; c++) tr_append_ext2(t, "round_message", E2{m[2 * c], m[2 * c + 1]});
+                tr_absorb(t, m[0]);
+                tr_absorb(t, m[1]);
+                for (int c = 1; c <= d; c++) tr_append_ext2(t, "round_message", E2{m[2 * c], m[2 * c + 1]});
                 E2 ch = tr_challenge_ext2(t, "challenge");
                 r0 = ch.c0;
                 r1 = ch.c1;
                 h_ch[2 * k] = r0;
                 h_ch[2 * k + 1] = r1;
             } else {
-                for (int c = 0; c <= d; c++) tr_append_u64(t, "round_message", m[c]);
+                tr_absorb(t, m[0]);
+                for (int c = 1; c <= d; c++) tr_append_u64(t, "round_message", m[c]);
                 r0 = tr_challenge(t, "challenge");
                 h_ch[k] = r0;
             }
