@@ -308,6 +308,20 @@ def run_side_workload(args):
                             "frac": line["value"] / peak, "peak_source": src}
     if args.workload == "ajtai":
         line["tensor_tflops_equiv"] = 2.0 * 8 * rows * 64 * Bw * n_ring * 64 / (ms * 1e-3) / 1e12
+        # whole batch (digit prep, GEMM, combine) against the HBM bound of the GEMM's operand
+        # stream: the key's 8 digit planes (bf16) once, plus the witness digits (bf16)
+        peak, src = measured_peaks()
+        op_bytes = 8 * rows * 64 * n_ring * 64 * 2 + Bw * n_ring * 64 * 2
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                tpeak = json.load(f).get("bf16_tflops", 1900.0)
+        except Exception:
+            tpeak = 1900.0
+        line["roofline"] = {"bound": "hbm", "kernel": "ajtai_gemm_kernel (whole batch timed)",
+                            "achieved": op_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                            "frac": op_bytes / (ms * 1e-3) / 1e9 / peak, "peak_source": src,
+                            "bytes_per_launch": op_bytes, "tensor_frac": line["tensor_tflops_equiv"] / tpeak,
+                            "traffic": None}
         # the fold tree at the SuperNeo shape: 50 binary + 13 ternary witnesses of 2^14 ring elements
         nb, nt, nr = 50, 13, 1 << 14
         zb = DeviceBuffer.from_numpy(rng.integers(0, 2**63, size=nb * nr, dtype=np.uint64))
