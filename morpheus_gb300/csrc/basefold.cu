@@ -306,7 +306,7 @@ __global__ void P2_BOUNDS(T) fold_hash_leaves_kernel(const u64* __restrict__ cw,
     e2_st(folded + 4 * i, f0);
     e2_st(folded + 4 * i + 2, f1);
     u64 s[8] = {f0.c0, f0.c1, f1.c0, f1.c1, 0, 0, 0, 0};
-    p2_permute(s);
+    p2_permute<4>(s);
     st_digest(tree + 4 * i, s);
 }
 
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(T, (T) == 512 ? 2 : 4) bo_combine_leaves_kerne
     u64 s[8] = {gl3_reduce(a[0]), gl3_reduce(a[1]), gl3_reduce(a[2]), gl3_reduce(a[3]), 0, 0, 0, 0};
     e2_st(ccw + 4 * i, e2_make(s[0], s[1]));
     e2_st(ccw + 4 * i + 2, e2_make(s[2], s[3]));
-    p2_permute(s);
+    p2_permute<4>(s);
     st_digest(tree + 4 * i, s);
 }
 

@@ -152,7 +152,7 @@ __global__ void P2_BOUNDS(T) ls_fold_hash_kernel(const LsSeg* __restrict__ segs,
     e2_st(sg.c + 4 * i, f0);
     e2_st(sg.c + 4 * i + 2, f1);
     u64 s[8] = {f0.c0, f0.c1, f1.c0, f1.c1, 0, 0, 0, 0};
-    p2_permute(s);
+    p2_permute<4>(s);
     st_digest(sg.d + 4 * i, s);
 }
 
@@ -222,7 +222,7 @@ __global__ void P2_BOUNDS(T) ls_hash_leaves_kernel(const LsSeg* __restrict__ seg
     if (i >= sg.items) return;
     ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(sg.a) + i);
     u64 st[8] = {v.x, v.y, 0, 0, 0, 0, 0, 0};
-    p2_permute(st);
+    p2_permute<2>(st);
     st_digest(sg.d + 4 * i, st);
 }
 

@@ -157,7 +157,7 @@ __global__ void P2_BOUNDS(T) hash_leaves_gl_kernel(const u64* __restrict__ cw, u
     if (i >= leaves) return;
     ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(cw) + i);
     u64 s[8] = {v.x, v.y, 0, 0, 0, 0, 0, 0};
-    p2_permute(s);
+    p2_permute<2>(s);
     st_digest(tree + 4 * i, s);
 }
 
@@ -168,7 +168,7 @@ __global__ void P2_BOUNDS(T) hash_leaves_ext2_kernel(const u64* __restrict__ cw,
     u64 s[8];
     ld_digest(cw + 4 * i, s);
     s[4] = s[5] = s[6] = s[7] = 0;
-    p2_permute(s);
+    p2_permute<4>(s);
     st_digest(tree + 4 * i, s);
 }
 

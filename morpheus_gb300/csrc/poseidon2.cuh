@@ -48,6 +48,14 @@ namespace gb {
     0x9177c73d8b7e929cull, 0x2a6fe8085797e791ull, 0x3de6e93329f8d5adull, 0x3f7af9125da962feull, \
     }
 
+// sbox(rc_ext[0][i]) = rc_ext[0][i]^7 mod p: the first round of a lane whose input is zero (leaf
+// hashes pad the state with zeros), precomputed
+#define GB_P2_SBOX_RC0 \
+    { \
+    0x387c7997ddb86b2dull, 0xeaef0e16d57a01b1ull, 0x56194e5f22b13d3full, 0xf1c2b617a3fb0d63ull, \
+    0x2cf5b8a51a6f0ae2ull, 0xcfa4b3786daf48b0ull, 0x1c4c56702fac6714ull, 0xcd56a4eb1f507954ull, \
+    }
+
 struct P2Const {
     static constexpr u64 ext[8][8] = GB_P2_RC_EXT;
     static constexpr u64 inner[22] = GB_P2_RC_INT;
@@ -69,6 +77,10 @@ __device__ __forceinline__ u64 p2_rc_int(int r) {
 }
 __device__ __forceinline__ u64 p2_diag(int i) {
     constexpr u64 t[8] = GB_P2_DIAG;
+    return t[i];
+}
+__device__ __forceinline__ u64 p2_sbox_rc0(int i) {
+    constexpr u64 t[8] = GB_P2_SBOX_RC0;
     return t[i];
 }
 
@@ -113,10 +125,14 @@ __device__ __forceinline__ void p2_external_linear_add(u64* x, const u64* add, b
 //   external round r: s <- E(sbox(s + rc_ext[r]));  internal round r: s0 <- sbox(s0 + rc_int[r]),
 //   s_i <- diag_i s_i + sum(s) -- computed as one multiply-add per lane with the sum (and the
 //   next round's constant) unreduced.
+// LIVE < 8: lanes LIVE..7 of the input are zero (a leaf hash), so their first S-box is a constant
+// and s[LIVE..7] are not read.
+template <int LIVE = 8>
 __device__ __forceinline__ void p2_permute(u64* s) {
     u64 rc[8];
 #pragma unroll
-    for (int i = 0; i < 8; i++) s[i] = p2_sbox(glw_reduce(glw_add(glw_of(s[i]), p2_rc_ext(0, i))));
+    for (int i = 0; i < 8; i++)
+        s[i] = i < LIVE ? p2_sbox(glw_reduce(glw_add(glw_of(s[i]), p2_rc_ext(0, i)))) : p2_sbox_rc0(i);
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         if (r < 3) {

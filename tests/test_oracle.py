@@ -307,3 +307,15 @@ def test_ext5_frobenius_constants():
     d = pow(3, (O.P - 1) // 5, O.P)
     assert vals == [pow(d, i, O.P) for i in range(5)]
     assert pow(7, (O.P - 1) // 2, O.P) == O.P - 1 and pow(3, (O.Q_AGL - 1) // 2, O.Q_AGL) == O.Q_AGL - 1
+
+
+def test_poseidon2_zero_lane_sbox_constants():
+    """The precomputed first-round S-boxes of zero lanes (leaf hashes) are rc_ext[0][i]^7 mod p."""
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "morpheus_gb300", "csrc",
+                            "poseidon2.cuh")).read()
+    rc = [int(x, 16) for x in re.findall(r"0x([0-9a-f]+)ull", src[src.index("#define GB_P2_RC_EXT"):
+                                                                   src.index("#define GB_P2_RC_INT")])][:8]
+    pre = [int(x, 16) for x in re.findall(r"0x([0-9a-f]+)ull", src[src.index("#define GB_P2_SBOX_RC0"):
+                                                                    src.index("struct P2Const")])]
+    assert pre == [pow(x % P, 7, P) for x in rc]
