@@ -1420,8 +1420,61 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
                 }
             }
             {
-                LsRunner runner(tab, q);
-                rc = runner.open(P);
+                // two halves of the polynomials (alternating in size order, so that both carry
+                // about the same work), each opened by its own runner: the second on a helper
+                // thread with its own stream, so that one half's host round trip between rounds
+                // overlaps the other half's device work
+                std::vector<size_t> idx(P.size());
+                std::iota(idx.begin(), idx.end(), 0);
+                std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return P[a].N > P[b].N; });
+                std::vector<LsPoly> A, B;
+                for (size_t k = 0; k < idx.size(); k++) (k % 2 ? B : A).push_back(std::move(P[idx[k]]));
+                if (B.empty()) {
+                    LsRunner runner(tab, q);
+                    rc = runner.open(A);
+                } else {
+                    int dev = 0, rc2 = GB_OK;
+                    std::string err2;
+                    cudaEvent_t ready = nullptr;
+                    cudaError_t e = cudaGetDevice(&dev);
+                    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+                    if (e == cudaSuccess) e = cudaEventRecord(ready, s);  // the commits and sumchecks
+                    if (e != cudaSuccess) {
+                        set_error("lockstep open helper", e);
+                        rc = GB_ECUDA;
+                    } else {
+                        std::thread helper([&] {
+                            cudaStream_t st = nullptr;
+                            cudaError_t he = cudaSetDevice(dev);
+                            if (he == cudaSuccess) he = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+                            if (he == cudaSuccess) he = cudaStreamWaitEvent(st, ready, 0);
+                            if (he != cudaSuccess) {
+                                rc2 = GB_ECUDA;
+                                err2 = std::string("lockstep open helper: ") + cudaGetErrorString(he);
+                            } else {
+                                gb_set_stream(st);
+                                {
+                                    LsRunner runner(tab, q);
+                                    rc2 = runner.open(B);
+                                }
+                                if (rc2) err2 = gb_last_error();
+                                cudaStreamSynchronize(st);
+                                gb_set_stream(nullptr);
+                            }
+                            if (st) cudaStreamDestroy(st);
+                        });
+                        {
+                            LsRunner runner(tab, q);
+                            rc = runner.open(A);
+                        }
+                        helper.join();
+                        if (!rc && rc2) {
+                            rc = rc2;
+                            set_error_msg(err2);
+                        }
+                    }
+                    if (ready) cudaEventDestroy(ready);
+                }
             }
             t_ls_ms[1] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
         }
