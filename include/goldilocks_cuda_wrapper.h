@@ -220,9 +220,9 @@ unsigned long long gb_launch_count(void);
 int gb_mulmod_probe(uint64_t *d_out, int blocks, int iters);
 
 /* Merkle scheduling knob of the calling thread: tree layers (and leaf hashes) of fewer than
- * `parents` permutations use 8 lanes per permutation (lower latency), larger ones one thread
- * per permutation (higher throughput).  Default 32768; results do not depend on it.  Returns
- * the previous value. */
+ * `parents` permutations use 8 lanes per permutation (lowest latency); from there up to 2^16
+ * permutations 2 lanes per permutation, and above that one thread per permutation (highest
+ * throughput).  Default 16384; results do not depend on it.  Returns the previous value. */
 size_t gb_set_coop_threshold(size_t parents);
 size_t gb_get_coop_threshold(void);
 /* Second Merkle knob of the calling thread: once a layer has at most `nodes` digests (2..2048,

@@ -56,12 +56,12 @@ size_t mk_coop_below();
 // a longer chain inside the one CTA).
 constexpr size_t MK_TOP_NODES = 16;
 
-// Launch shape of the one-permutation-per-thread kernels.  The unrolled permutation is about
-// 15 k instructions, and the warps of one CTA run through it together, so large CTAs keep an
-// SM's warps within a few regions of the instruction cache: 512-thread CTAs, three per SM
-// (at most 40 registers), measured 1.89 G permutations/s at 2^24 against 1.52-1.59 G with
-// 128-thread CTAs.  Launches below P2_WIDE_FROM permutations keep 128-thread CTAs, so that a
-// launch of less than a wave still spreads over every SM.
+// Launch shape of the one-permutation-per-thread kernels: 512-thread CTAs, three per SM (at
+// most 40 registers), measured 1.89 G permutations/s at 2^24 against 1.52-1.59 G with 128-thread
+// CTAs of the same code and register count.  The likely cause is instruction-cache locality:
+// the unrolled permutation is about 15 k instructions, and the warps of one CTA run through it
+// together.  Launches below P2_WIDE_FROM permutations keep 128-thread CTAs, so that a launch of
+// less than a wave still spreads over every SM.
 constexpr int P2_WIDE = 512, P2_NARROW = 128;
 constexpr size_t P2_WIDE_FROM = (size_t)1 << 16;
 #define P2_BOUNDS(T) __launch_bounds__(T, (T) == 512 ? 3 : 10)
