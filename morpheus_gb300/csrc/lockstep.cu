@@ -370,6 +370,64 @@ static size_t ls_poly_words(int n, int lr) {
     return w;
 }
 
+// eq(r, x) tables of every polynomial of a runner at once (the values of eq_table, eq.cu):
+// block 2k + h builds polynomial k's table over its low (h = 0) or high (h = 1) half of the
+// variables by the doubling loop; then one launch multiplies them out, block -> polynomial by
+// binary search over block0.
+struct EqSeg {
+    const u64* r;  // 2n words (Ext2 point)
+    u64* lo;       // 2^k Ext2 scratch
+    u64* hi;       // 2^(n-k) Ext2 scratch
+    u64* out;      // 2^n Ext2
+    u64 n, k, block0;
+};
+
+__global__ void __launch_bounds__(256) ls_eq_halves_kernel(const EqSeg* __restrict__ segs, int nseg) {
+    const int k = blockIdx.x >> 1, h = blockIdx.x & 1;
+    if (k >= nseg) return;
+    const EqSeg sg = segs[k];
+    u64* out = h ? sg.hi : sg.lo;
+    const int v0 = h ? (int)sg.k : 0, v1 = h ? (int)sg.n : (int)sg.k;
+    if (threadIdx.x == 0) {
+        out[0] = 1;
+        out[1] = 0;
+    }
+    __syncthreads();
+    for (int v = v0; v < v1; v++) {
+        const size_t half = (size_t)1 << (v - v0);
+        const e2 rv = e2_make(sg.r[2 * v], sg.r[2 * v + 1]);
+        for (size_t j = threadIdx.x; j < half; j += blockDim.x) {
+            const e2 a = e2_make(out[2 * j], out[2 * j + 1]);
+            const e2 ar = e2_mul(a, rv);
+            const e2 lo_v = e2_sub(a, ar);
+            out[2 * (j + half)] = ar.c0;
+            out[2 * (j + half) + 1] = ar.c1;
+            out[2 * j] = lo_v.c0;
+            out[2 * j + 1] = lo_v.c1;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) ls_eq_expand_kernel(const EqSeg* __restrict__ segs, int nseg) {
+    __shared__ int s_seg;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (segs[mid].block0 <= blockIdx.x) lo = mid;
+            else hi = mid - 1;
+        }
+        s_seg = lo;
+    }
+    __syncthreads();
+    const EqSeg sg = segs[s_seg];
+    const u64 x = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
+    if (x >= ((u64)1 << sg.n)) return;
+    const u64 xl = x & (((u64)1 << sg.k) - 1), xh = x >> sg.k;
+    e2_st(sg.out + 2 * x, e2_mul(e2_ld(sg.lo + 2 * xl), e2_ld(sg.hi + 2 * xh)));
+}
+
 class LsRunner {
   public:
     LsRunner(const BfTable* tab, int q) : tab_(tab), q_(q) {}
@@ -437,14 +495,50 @@ class LsRunner {
                 for (int w = 0; w < 4; w++) tr_append_u64(&p.t, "", p.com->root[w]);
                 for (int i = 0; i < p.n; i++) tr_append_ext2(&p.t, "", E2{canon(p.point[2 * i]), canon(p.point[2 * i + 1])});
             });
-            for (auto& p : P) {
-                std::vector<u64> v(2 * p.n);
-                for (int i = 0; i < 2 * p.n; i++) v[i] = canon(p.point[i]);
-                GB_CUDA_TRY(cudaMemcpyAsync(p.d_point, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s));
-                int rc = eq_table(p.d_point, p.n, true, p.eq);
-                if (rc) return rc;
+            // every point in one copy into one buffer, then every eq table in two launches
+            std::vector<size_t> poff(np);
+            size_t pwords = 0, scratch = 0;
+            for (int k = 0; k < np; k++) {
+                poff[k] = pwords;
+                pwords += align2(2 * (size_t)P[k].n);
+                scratch += 2 * (((size_t)1 << (P[k].n / 2)) + ((size_t)1 << (P[k].n - P[k].n / 2)));
             }
-            GB_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors above go out of scope
+            pts.assign(pwords, 0);
+            for (int k = 0; k < np; k++)
+                for (int i = 0; i < 2 * P[k].n; i++) pts[poff[k] + i] = canon(P[k].point[i]);
+            u64* d_pts = nullptr;
+            GB_CUDA_TRY(cudaMallocAsync(&d_pts, pwords * 8, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(d_pts, pts.data(), pwords * 8, cudaMemcpyHostToDevice, s));
+            u64* eqs = nullptr;
+            EqSeg* d_eqsegs = nullptr;
+            std::vector<EqSeg> eqsegs(np);
+            GB_CUDA_TRY(cudaMallocAsync(&eqs, scratch * 8, s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_eqsegs, (size_t)np * sizeof(EqSeg), s));
+            u64 nb = 0;
+            u64* cur = eqs;
+            for (int k = 0; k < np; k++) {
+                LsPoly& p = P[k];
+                EqSeg& g = eqsegs[k];
+                g.r = d_pts + poff[k];
+                g.n = (u64)p.n;
+                g.k = (u64)(p.n / 2);
+                g.lo = cur;
+                cur += 2 * ((size_t)1 << g.k);
+                g.hi = cur;
+                cur += 2 * ((size_t)1 << (g.n - g.k));
+                g.out = p.eq;
+                g.block0 = nb;
+                nb += ((u64)1 << p.n) / 256 + 1;
+            }
+            GB_CUDA_TRY(cudaMemcpyAsync(d_eqsegs, eqsegs.data(), (size_t)np * sizeof(EqSeg), cudaMemcpyHostToDevice, s));
+            ls_eq_halves_kernel<<<(unsigned)(2 * np), 256, 0, s>>>(d_eqsegs, np);
+            GB_LAUNCH_CHECK("ls_eq_halves_kernel");
+            ls_eq_expand_kernel<<<(unsigned)nb, 256, 0, s>>>(d_eqsegs, np);
+            GB_LAUNCH_CHECK("ls_eq_expand_kernel");
+            cudaFreeAsync(eqs, s);
+            cudaFreeAsync(d_eqsegs, s);
+            cudaFreeAsync(d_pts, s);
+            GB_CUDA_TRY(cudaStreamSynchronize(s));  // the host arrays above go out of scope
         }
         // round 0 oracle
         std::vector<int> all(np);
