@@ -130,7 +130,7 @@ def cpu_throughput(steps, warmup=0):
     2^14 sample to the 2^22 workload by the work ratio."""
     import multiprocessing as mp
     import oracle as O
-    O.build(ref=False)
+    O.build(ref_root="")
     cores = os.cpu_count() or 1
     scale = float(1 << (N_VARS - SAMPLE_VARS))
     rates = []
@@ -174,7 +174,7 @@ def batch_open_cpu_sample(num_claims, sample_vars=12, n=20):
     """The C restatement of batch_open_ext2 (one core) on 8 polys x 2^sample_vars at 2 points,
     time scaled by 2^(n - sample_vars) to the 2^n workload."""
     import oracle as O
-    O.build(ref=False)
+    O.build(ref_root="")
     rng = np.random.default_rng(7)
     comms = [O.basefold_commit(rng.integers(0, P, size=1 << sample_vars, dtype=np.uint64), LOG_RATE) for _ in range(8)]
     points = [rng.integers(0, P, size=(sample_vars, 2), dtype=np.uint64) for _ in range(2)]

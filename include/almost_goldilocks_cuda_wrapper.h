@@ -109,6 +109,9 @@ int cuda_memcpy_dtod_async(void *dst, const void *src, size_t size, void *stream
 int cuda_memcpy_htod_async(void *dst, const void *src, size_t size, void *stream);
 /* Device memory the stream-ordered pool of the current device holds (reserved, in use or not). */
 size_t agl_cached_bytes(void);
+/* High-water mark of the memory in use from that pool since the last reset (no counterpart in the
+ * reference).  reset != 0 then restarts the mark from the memory in use now.  (size_t)-1 on error. */
+size_t gb_pool_used_high(int reset);
 /* Synchronous copies through pinned staging (any host memory). */
 int agl_d2h_staged(void *h_dst, const void *d_src, size_t bytes);
 int agl_h2d_staged(void *d_dst, const void *h_src, size_t bytes);
@@ -168,8 +171,11 @@ int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses,
  * N returns -2 with a message in gb_last_error().  It is for callers that must not allocate
  * on their request path: a service that has reserved its whole HBM budget up front, where an
  * allocation inside the call could fail or wait on the memory pool.
- *   - The first call on each device (with that device current) looks the scratch address up
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call looks the scratch address up on the current device (cudaGetSymbolAddress).
+ *     The first call on each device is a warm-up: with lazy module loading it may load the
+ *     library's module and map its static device memory, this array included.  Make that call
+ *     before reserving the HBM budget, before serving starts and before any stream capture;
+ *     from the second call on nothing is allocated.
  *   - Calls share the one scratch: calls that overlap in time (other threads, other streams)
  *     race on it and must be serialised by the caller.
  *   - Nothing in the scratch needs clearing: every word read is written by the same call.

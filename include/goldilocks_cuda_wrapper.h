@@ -214,6 +214,9 @@ const char *gb_last_error(void);
 int gb_device_sm_count(void);
 /* Number of kernels this library has launched in the process (all threads). */
 unsigned long long gb_launch_count(void);
+/* cudaFuncAttributes::binaryVersion of this library's kernels on the current device (103 for
+ * sm_103a code), -1 on error. */
+int gb_binary_version(void);
 /* Measurement probe: blocks x 256 threads, each running 8 independent chains of `iters`
  * Goldilocks multiplications; d_out receives blocks*256 words.  Times the arithmetic
  * ceiling that the Poseidon2 kernels are compared against.  Launch only. */

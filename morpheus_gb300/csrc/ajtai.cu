@@ -850,24 +850,13 @@ constexpr u64 AJ_NOALLOC_MAX_RING = 4096;
 constexpr int AJ_NOALLOC_MAX_CHUNKS = (int)(AJ_NOALLOC_MAX_RING / WIDE_CHUNK);
 static __device__ __align__(256) u64 g_wide_noalloc_scratch[(size_t)AJ_NOALLOC_MAX_CHUNKS * AJ_KAPPA * AJ_D];
 
-// Device address of the scratch, looked up once per device (with that device current).
+// Device address of the scratch on the current device.  It is looked up on every call (a host-side
+// table lookup once the module is loaded), so no address outlives a context that a device reset
+// tore down.
 static int wide_noalloc_scratch(u64** out) {
-    constexpr int MAX_DEVICES = 64;
-    static std::mutex mu;
-    static u64* addr[MAX_DEVICES] = {};
-    int dev = 0;
-    GB_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= MAX_DEVICES) {
-        set_error_msg("ajtai_commit_wide_noalloc_ffi: device ordinal out of range");
-        return GB_EINVAL;
-    }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void* p = nullptr;
-        GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_wide_noalloc_scratch));
-        addr[dev] = static_cast<u64*>(p);
-    }
-    *out = addr[dev];
+    void* p = nullptr;
+    GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_wide_noalloc_scratch));
+    *out = static_cast<u64*>(p);
     return GB_OK;
 }
 }  // namespace gb

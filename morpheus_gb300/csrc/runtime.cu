@@ -184,6 +184,12 @@ int gb_mulmod_probe(uint64_t* d_out, int blocks, int iters) {
     return check_launch("gb_mulmod_probe");
 }
 
+int gb_binary_version(void) {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, mulmod_probe_kernel) != cudaSuccess) return -1;
+    return a.binaryVersion;
+}
+
 int goldilocks_cuda_init(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return -1;
@@ -261,6 +267,19 @@ size_t agl_cached_bytes(void) {
         cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess)
         return 0;
     return (size_t)reserved;
+}
+size_t gb_pool_used_high(int reset) {
+    int dev = 0;
+    cudaMemPool_t pool;
+    uint64_t high = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess ||
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &high) != cudaSuccess)
+        return (size_t)-1;
+    if (reset) {
+        uint64_t zero = 0;  // resets the mark to the memory in use now
+        if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero) != cudaSuccess) return (size_t)-1;
+    }
+    return (size_t)high;
 }
 // chunked copies through the thread's pinned staging buffer
 static int staged_copy(void* dst, const void* src, size_t bytes, bool to_host) {

@@ -29,13 +29,14 @@ _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _c = ctypes
 
 
-def build(ref=None):
-    """Compile liboracle.so (and _ref/ when the reference tree is present)."""
+def build(ref_root=None):
+    """Compile liboracle.so, and _ref/ from the reference checkout at ref_root (default: the
+    MORPHEUS_REFERENCE environment variable) when one is given and present."""
     subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
-    if ref is None:
-        ref = os.path.isdir("/root/reference/cuda_almost_goldilocks")
-    if ref:
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    if ref_root is None:
+        ref_root = os.environ.get("MORPHEUS_REFERENCE")
+    if ref_root and os.path.isdir(os.path.join(ref_root, "cuda_almost_goldilocks")):
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref_root}"], check=True)
 
 
 def lib():
@@ -43,7 +44,7 @@ def lib():
     if _LIB is None:
         path = os.path.join(_HERE, "liboracle.so")
         if not os.path.exists(path):
-            build(ref=False)
+            build(ref_root="")
         L = ctypes.CDLL(path)
         u64, i32, sz = _c.c_uint64, _c.c_int, _c.c_size_t
         vp = _c.c_void_p

@@ -2,7 +2,7 @@
 
 Run here (where the reference sources exist), never on the GPU machine:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>
 
 Two kinds of vectors are written:
 
@@ -201,9 +201,10 @@ def ref_vectors():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MORPHEUS_REFERENCE"),
+                    help="the reference checkout (default: $MORPHEUS_REFERENCE)")
     args = ap.parse_args()
-    if not os.path.isdir(args.ref):
+    if not args.ref or not os.path.isdir(args.ref):
         sys.exit("reference tree not found; fixtures are generated only where it exists")
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all", "ref", f"REF={args.ref}"], check=True)
     data = {"generated_by": "tests/golden/make_golden.py"}

@@ -52,3 +52,39 @@ def test_noalloc_at_its_maximum_and_beyond(gpu_lib):
     rc = N.lib().ajtai_commit_wide_noalloc_ffi(None, None, MAX_RING + 1, 0, 256, None)
     assert rc == -2
     assert b"exceeds" in N.lib().gb_last_error()
+
+
+def test_noalloc_call_allocates_nothing(gpu_lib):
+    """After a warm-up call, a call changes neither the free device memory nor the
+    stream-ordered pool's high-water mark: no allocation happens on the request path."""
+    import ctypes
+    from morpheus_gb300 import _native as N
+    from morpheus_gb300.memory import DeviceBuffer
+    L = N.lib()
+    key = np.array([4, 4, 2, 2, 1, 1, 0, 0], np.uint32)
+    z = np.random.default_rng(11).integers(0, O.Q_AGL, size=MAX_RING * 64, dtype=np.uint64)
+    d_key = DeviceBuffer.from_numpy(key)
+    d_z = DeviceBuffer.from_numpy(z)
+    d_out = DeviceBuffer(42 * 64)
+    try:
+        def call():
+            N.check(L.ajtai_commit_wide_noalloc_ffi(d_key.ptr, d_z.ptr, MAX_RING, 0, 256, d_out.ptr),
+                    "ajtai_commit_wide_noalloc_ffi")
+
+        def free_bytes():
+            f, t = ctypes.c_size_t(), ctypes.c_size_t()
+            N.check(L.cuda_mem_get_info(ctypes.byref(f), ctypes.byref(t)), "cuda_mem_get_info")
+            return f.value
+
+        call()  # warm-up: may load the module and its static memory
+        first = d_out.to_numpy()
+        assert L.gb_pool_used_high(1) != ctypes.c_size_t(-1).value
+        in_use = L.gb_pool_used_high(0)
+        free0 = free_bytes()
+        call()
+        assert free_bytes() == free0
+        assert L.gb_pool_used_high(0) == in_use
+        assert np.array_equal(d_out.to_numpy(), first)
+    finally:
+        for b in (d_key, d_z, d_out):
+            b.free()
