@@ -107,67 +107,108 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-SAMPLE_VARS = 14  # bounded CPU sample: 2^14-evaluation proofs, time scaled by 2^(22-14)
-
-
-def _cpu_proof(seed):
-    """One commit + open_ext2 of a 2^SAMPLE_VARS polynomial by the CPU restatement
-    of the reference prover (runs in a spawned worker)."""
-    import oracle as O
-    rng = np.random.default_rng(seed)
-    ev = rng.integers(0, P, size=1 << SAMPLE_VARS, dtype=np.uint64)
-    pt = rng.integers(0, P, size=(SAMPLE_VARS, 2), dtype=np.uint64)
-    table = O.basefold_table(SAMPLE_VARS, LOG_RATE, SAMPLE_VARS, TABLE_SEED)
-    t0 = time.perf_counter()
-    c = O.basefold_commit(ev, LOG_RATE)
-    O.basefold_open_ext2(c, pt, table, O.Transcript(b"bf-open"), QUERIES)
-    return time.perf_counter() - t0
-
-
-def cpu_throughput(steps, warmup=0):
-    """Proofs/s of the CPU restatement with one proof per host core in parallel (the
-    reference runs its CPU openings one per thread, many in parallel), scaled from the
-    2^14 sample to the 2^22 workload by the work ratio."""
-    import multiprocessing as mp
+def cpu_basefold_proofs(steps, warmup, n=N_VARS, seed=1234):
+    """Commit + open_ext2 proofs of 2^n evaluations by the C restatement of the reference's CPU
+    prover (cpu_full_open_ext2, zk-torch-3/src/commit/cpu_basefold.rs:235-425), each proof's large
+    loops (Merkle layers, transform layers, folds, sums) split over every host thread.  The folding
+    table is the key's, generated once outside the timed proofs, as BasefoldTable::generate is.
+    Returns the seconds of each timed proof, the thread count and the last proof."""
     import oracle as O
     O.build(ref_root="")
-    cores = os.cpu_count() or 1
-    scale = float(1 << (N_VARS - SAMPLE_VARS))
-    rates = []
-    with mp.get_context("spawn").Pool(cores) as pool:
-        for i in range(warmup + steps):
-            t0 = time.perf_counter()
-            pool.map(_cpu_proof, range(i * cores, (i + 1) * cores))
-            wall = time.perf_counter() - t0
-            if i >= warmup:
-                rates.append(cores / (wall * scale))
-    value = statistics.mean(rates)
-    return value, cores, (f"{steps} x {cores} parallel proofs of 2^{SAMPLE_VARS} evaluations "
-                          f"(C restatement, one per core), time scaled x{int(scale)} to 2^22")
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    rng = np.random.default_rng(seed)
+    ev = rng.integers(0, P, size=1 << n, dtype=np.uint64)
+    pt = rng.integers(0, P, size=(n, 2), dtype=np.uint64)
+    table = O.basefold_table(n, LOG_RATE, n, TABLE_SEED)
+
+    def one():
+        c = O.basefold_commit(ev, LOG_RATE)
+        return c, O.basefold_open_ext2(c, pt, table, O.Transcript(b"bf-open"), QUERIES)
+    for _ in range(warmup):
+        one()
+    secs, last = [], None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        last = one()
+        secs.append(time.perf_counter() - t0)
+    return secs, threads, last
 
 
 def run_reference(args):
     """The reference's CPU prover path, restated in C (the reference is Rust and no Rust
-    toolchain exists here or on the GPU machine), on all host cores.  Rank 0 only."""
+    toolchain exists here or on the GPU machine), at the full 2^22 configuration on all host
+    threads: each step is one real commit + open_ext2 proof.  Rank 0 only."""
     rank, world = env_rank()
     if rank != 0:
         return
-    value, cores, sample = cpu_throughput(args.steps, min(args.warmup, 1))
+    warm = min(args.warmup, 1)  # a CPU proof has no device state to warm; one untimed proof
+    secs, threads, _ = cpu_basefold_proofs(args.steps, warm)
+    step_s = statistics.mean(secs)
+    value = 1.0 / step_s
+    sample = (f"{args.steps} timed commit+open_ext2 proofs of 2^{N_VARS} evaluations (C restatement), "
+              f"each split over {threads} host threads, after {warm} untimed proof; table generated once")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic",
+        "steps": args.steps, "warmup": warm, "warmup_requested": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)",
+        "data": "synthetic",
         "config": {"workload": f"basefold commit+open_ext2, 2^{N_VARS} evals, rate 1/2, {QUERIES} queries",
                    "num_vars": N_VARS, "log_rate": LOG_RATE, "num_queries": QUERIES, "table_seed": TABLE_SEED},
-        "cpu_baseline": {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "proofs/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "proofs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "step_ms_all": [round(t * 1e3, 1) for t in secs],
     }
     print(json.dumps(line))
 
 
-def cpu_baseline_sample():
-    value, cores, sample = cpu_throughput(1, 0)
-    return {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port", "sample": sample}
+def cpu_baseline_sample(gpu_proof=None, seed=1234):
+    """One full-size CPU proof (after a small untimed one), on all host threads; the proof is
+    compared with the GPU's proof of the same inputs when one is given."""
+    cpu_basefold_proofs(0, 1, n=14)
+    secs, threads, (_, proof) = cpu_basefold_proofs(1, 0, seed=seed)
+    out = {"value": 1.0 / secs[0], "unit": "proofs/s", "cores": threads, "kind": "port",
+           "sample": f"1 commit+open_ext2 proof of 2^{N_VARS} evaluations (C restatement) split over {threads} "
+                     f"host threads, {secs[0]:.1f} s; table generated once, outside the timing"}
+    if gpu_proof is not None:
+        out["identical_to_gpu_proof"] = bool(np.array_equal(np.asarray(gpu_proof), proof))
+    return out
+
+
+def cpu_sumcheck_sample(polys, gpu_msgs=None, reps=3):
+    """CpuLinearSumcheckProverExt2 (zk-torch-3/src/sumcheck/cpu_ext2_prover.rs:13-110), single-threaded
+    like the reference's, restated in C: 2 x 2^20, whole proof with its transcript."""
+    import oracle as O
+    O.set_threads(1)
+    secs = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        ref = O.sumcheck_prove_ext2(O.Transcript(b"bench"), polys)
+        secs.append(time.perf_counter() - t0)
+    s = statistics.median(secs)
+    out = {"value": polys.size / s / 1e6, "unit": "Melem/s", "cores": 1, "kind": "port",
+           "sample": f"{reps} Ext2-challenge sumcheck proofs of 2 x 2^20 (C restatement, one thread as the "
+                     f"reference's CpuLinearSumcheckProverExt2), median {s * 1e3:.0f} ms"}
+    if gpu_msgs is not None:
+        out["identical_to_gpu_proof"] = bool(np.array_equal(np.asarray(gpu_msgs), ref["round_messages"]))
+    return out
+
+
+def cpu_ajtai_sample(key, z8, rows, gpu_out=None):
+    """The Ajtai commitment by the C restatement (ajtai_cpu_reference.cuh:57-186 semantics, exact
+    128-bit accumulation), witnesses split over every host thread."""
+    import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    t0 = time.perf_counter()
+    ref = O.ajtai_commit_u8_batch(key, z8, 0, rows)
+    s = time.perf_counter() - t0
+    out = {"value": z8.shape[0] / s, "unit": "commitments/s", "cores": threads, "kind": "port",
+           "sample": f"{z8.shape[0]} witnesses x {z8.shape[1]} coefficients, rows 0..{rows - 1} (C restatement, "
+                     f"witnesses over {threads} host threads, matrix generation included), {s:.2f} s"}
+    if gpu_out is not None:
+        out["identical_to_gpu"] = bool(np.array_equal(np.asarray(gpu_out).reshape(ref.shape), ref))
+    return out
 
 
 def batch_open_cpu_sample(num_claims, sample_vars=12, n=20):
@@ -337,6 +378,45 @@ def run_side_workload(args):
         line["multifold_mixed"] = {"ms": mf_ms, "workload": f"{nb} binary + {nt} ternary witnesses x {nr} ring "
                                                              "elements, challenges in {-1, 0, 1, 2}"}
     print(json.dumps(line))
+
+
+def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):
+    """Compact line for the Ajtai configuration: the whole 256-witness batch (digit prep, tensor-core
+    GEMM, combine), its tensor and HBM rooflines, and the C restatement on the host cores."""
+    n_ring, Bw, rows = 1024, 256, 16
+    key = np.array([0x5EED, 1, 2, 3, 4, 5, 6, 7], np.uint32)
+    z_host = np.random.default_rng(303).integers(0, 256, size=(Bw, n_ring * 64), dtype=np.uint8)
+    h = ctypes.c_void_p()
+    Nn.check(L.gb_ajtai_key_create(key.ctypes.data, 0, rows, n_ring, ctypes.byref(h)), "ajtai key")
+    z = DeviceBuffer.from_numpy(z_host.reshape(-1))
+    out = DeviceBuffer(Bw * rows * 64)
+    step = lambda: Nn.check(L.gb_ajtai_commit_u8_batched(h, z.ptr, Bw, out.ptr), "ajtai")
+    for _ in range(3):
+        step()
+    times = [ev_time(step) for _ in range(10)]
+    ms = statistics.median(times)
+    got = out.to_numpy()
+    Nn.check(L.gb_ajtai_key_destroy(h), "ajtai key destroy")
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    tpeak = peaks.get("bf16_tflops", 1900.0)
+    hpeak = peaks.get("hbm_gbs", 6800.0)
+    flop = 2.0 * 8 * rows * 64 * Bw * n_ring * 64  # 8 digit planes of the 1024 x 65536 x 256 product
+    alg_bytes = Bw * n_ring * 64 + rows * n_ring * 64 * 8 + Bw * rows * 64 * 8  # Z (u8) + M + out
+    tf = flop / (ms * 1e-3) / 1e12
+    return {"ms_per_batch": ms, "value": Bw / (ms * 1e-3), "unit": "commitments/s",
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": tpeak, "unit": "TFLOP/s", "frac": tf / tpeak,
+                         "peak_source": "measured (bf16 burst)" if peaks else "fallback",
+                         "hbm_algorithmic_GB_s": alg_bytes / (ms * 1e-3) / 1e9, "hbm_peak": hpeak,
+                         "algorithmic_bytes": alg_bytes},
+            "cpu_baseline": cpu_ajtai_sample(key, z_host[:64], rows, got.reshape(Bw, rows, 64)[:64]),
+            "step_ms_all": [round(t, 4) for t in times],
+            "workload": "256 witnesses x 2^16 coefficients in [0, 256), rows 0..15 of the ChaCha8 matrix, "
+                        "q = 2^64 - 2^32 - 31; python bench.py --workload ajtai for the full line"}
 
 
 def run_batched(args, summary=False):
@@ -637,13 +717,13 @@ def main():
     if dist:
         tdist.barrier()
 
-    times = []
+    times, last = [], []
     with ClockSampler() as clk:
         l0 = L.gb_launch_count()
         for _ in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
-            times.append(ev_time(step_device))
+            times.append(ev_time(lambda: last.__setitem__(slice(None), [step_device()])))
         launches = (L.gb_launch_count() - l0) // max(1, args.steps)
         torch.cuda.synchronize()
         if dist:
@@ -713,15 +793,20 @@ def main():
             "launch_ms": fr_ms,
         }
         # --- sumcheck Melem/s at the 2 x 2^20 shape (whole proof, host transcript)
-        polys = DeviceBuffer.from_numpy(rng.integers(0, P, size=2 << 20, dtype=np.uint64))
+        polys_host = rng.integers(0, P, size=(2, 1 << 20), dtype=np.uint64)
+        polys = DeviceBuffer.from_numpy(polys_host.reshape(-1))
+        sc_out = []
 
         def sc():
             t = Transcript(b"bench")
-            GpuLinearSumcheckProver(20, 2, t).prove((polys, 2), t)
+            sc_out.append(GpuLinearSumcheckProver(20, 2, t).prove((polys, 2), t))
         sc()
         sc_ms = statistics.median(ev_time(sc) for _ in range(5))
-        extras["sumcheck_2x2^20"] = {"ms_per_proof": sc_ms, "melem_per_s": 2 * (1 << 20) / (sc_ms * 1e-3) / 1e6}
-        extras["cpu_baseline"] = cpu_baseline_sample()
+        extras["sumcheck_2x2^20"] = {"ms_per_proof": sc_ms, "melem_per_s": 2 * (1 << 20) / (sc_ms * 1e-3) / 1e6,
+                                     "cpu_baseline": cpu_sumcheck_sample(polys_host, sc_out[-1].round_messages)}
+        # --- Ajtai commitment at its configuration: 256 witnesses x 2^16 coefficients, rows 0..15
+        extras["ajtai_c3"] = ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time)
+        extras["cpu_baseline"] = cpu_baseline_sample(gpu_proof=last[-1][1], seed=1234 + rank)
         # the batched (512 mixed instances) and served (Poisson matmul jobs) configurations, compact
         L.gb_set_stream(None)
         extras["batched_512"] = run_batched(argparse.Namespace(instances=512, steps=1, warmup=1, per_call_steps=1),

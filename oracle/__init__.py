@@ -49,6 +49,8 @@ def lib():
         u64, i32, sz = _c.c_uint64, _c.c_int, _c.c_size_t
         vp = _c.c_void_p
         for name, res, args in [
+            ("or_set_threads", None, [i32]),
+            ("or_get_threads", i32, []),
             ("or_gl_add", u64, [u64, u64]),
             ("or_gl_sub", u64, [u64, u64]),
             ("or_gl_mul", u64, [u64, u64]),
@@ -124,6 +126,15 @@ def ref_lib():
         R.ref_commit_binary.argtypes = [_u32p, _u64p, _c.c_uint64, _u64p]
         _REF = R
     return _REF
+
+
+def set_threads(k):
+    """Host threads for the large loops of one proof (results do not depend on them)."""
+    lib().or_set_threads(int(k))
+
+
+def get_threads():
+    return int(lib().or_get_threads())
 
 
 def _a(x, dt=np.uint64):

@@ -8,11 +8,64 @@
  */
 #include "oracle.h"
 
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
 typedef uint64_t u64;
 typedef unsigned __int128 u128;
+
+/* ----------------------------------------------------------------------
+ * Host threads for the CPU baseline.  The reference's CPU prover runs one
+ * opening per thread under rayon (zk-torch-3/src/dag/mod.rs:1120-1140); here
+ * the large element-wise loops of one proof (Merkle layers, transform layers,
+ * folds, sums) can instead be split over or_set_threads() threads.  Every split
+ * loop writes disjoint outputs or reduces exactly mod p, so results do not
+ * depend on the thread count.  Default: 1 thread.
+ * ---------------------------------------------------------------------- */
+#define OR_MAX_THREADS 256
+static int g_threads = 1;
+void or_set_threads(int k) { g_threads = k < 1 ? 1 : (k > OR_MAX_THREADS ? OR_MAX_THREADS : k); }
+int or_get_threads(void) { return g_threads; }
+
+typedef void (*or_range_fn)(void *ctx, size_t lo, size_t hi, int part);
+typedef struct { or_range_fn fn; void *ctx; size_t lo, hi; int part; } or_job;
+static void *or_job_run(void *a) {
+    or_job *j = (or_job *)a;
+    j->fn(j->ctx, j->lo, j->hi, j->part);
+    return NULL;
+}
+/* Runs fn over [0, n) in at most or_parts(n, min_chunk) contiguous parts (part = 0, 1, ...). */
+static int or_parts(size_t n, size_t min_chunk) {
+    size_t k = (size_t)g_threads;
+    if (min_chunk < 1) min_chunk = 1;
+    if (k > n / min_chunk) k = n / min_chunk;
+    return k < 1 ? 1 : (int)k;
+}
+static void par_for(size_t n, size_t min_chunk, or_range_fn fn, void *ctx) {
+    int k = or_parts(n, min_chunk);
+    if (k == 1) {
+        fn(ctx, 0, n, 0);
+        return;
+    }
+    pthread_t th[OR_MAX_THREADS];
+    or_job jobs[OR_MAX_THREADS] = {{0}};
+    int started[OR_MAX_THREADS];
+    for (int t = 0; t < k; t++) {
+        jobs[t].fn = fn;
+        jobs[t].ctx = ctx;
+        jobs[t].lo = n * (size_t)t / (size_t)k;
+        jobs[t].hi = n * (size_t)(t + 1) / (size_t)k;
+        jobs[t].part = t;
+        started[t] = t > 0 && pthread_create(&th[t], NULL, or_job_run, &jobs[t]) == 0;
+    }
+    or_job_run(&jobs[0]);
+    for (int t = 1; t < k; t++) {
+        if (started[t]) pthread_join(th[t], NULL);
+        else or_job_run(&jobs[t]); /* no thread available: run it here */
+    }
+}
+#define PAR_MIN 4096 /* elements per part below which a loop stays on one thread */
 
 /* ======================================================================
  * Goldilocks p = 2^64 - 2^32 + 1   (goldilocks-cuda-rs/src/field.rs:9-100,
@@ -465,17 +518,22 @@ void or_eq_table_base(const u64 *r, int n, u64 *out) {
     }
 }
 
+typedef struct { e2 *out; size_t half; e2 r, omr; } eq_layer_ctx;
+static void eq_layer_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    eq_layer_ctx *c = (eq_layer_ctx *)ctx;
+    for (size_t j = lo; j < hi; j++) {
+        c->out[j | c->half] = e2_mul(c->out[j], c->r);
+        c->out[j] = e2_mul(c->out[j], c->omr);
+    }
+}
 static void eq_table_ext2(const e2 *r, int n, e2 *out) {
     size_t N = (size_t)1 << n;
     for (size_t k = 0; k < N; k++) out[k] = e2_base(0);
     out[0] = e2_base(1);
     for (int i = 0; i < n; i++) {
-        size_t half = (size_t)1 << i;
-        e2 omr = e2_sub(e2_base(1), r[i]);
-        for (size_t j = half; j-- > 0;) {
-            out[j | half] = e2_mul(out[j], r[i]);
-            out[j] = e2_mul(out[j], omr);
-        }
+        eq_layer_ctx c = {out, (size_t)1 << i, r[i], e2_sub(e2_base(1), r[i])};
+        par_for(c.half, PAR_MIN, eq_layer_range, &c);
     }
 }
 
@@ -511,6 +569,12 @@ size_t or_basefold_table_entries(int num_vars, int log_rate, int num_rounds) {
     return tot;
 }
 
+static void table_invert_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    u64 *e = (u64 *)ctx;
+    for (size_t k = lo; k < hi; k++) e[2 * k + 1] = gl_inv(e[2 * k + 1]);
+}
+
 /* BasefoldTable::generate: xorshift64 (13, 7, 17), each draw reduced % p; x1 redrawn
  * while equal to x0; weight = 1 / (x1 - x0)  (goldilocks-cuda-rs/src/basefold.rs:281-321). */
 void or_basefold_table_generate(int num_vars, int log_rate, int num_rounds, u64 seed, u64 *entries,
@@ -526,11 +590,12 @@ void or_basefold_table_generate(int num_vars, int log_rate, int num_rounds, u64 
             u64 x1 = XS_NEXT();
             while (x1 == x0) x1 = XS_NEXT();
             entries[2 * pos] = x0;
-            entries[2 * pos + 1] = gl_inv(gl_sub(x1, x0));
+            entries[2 * pos + 1] = gl_sub(x1, x0);
             pos++;
         }
     }
 #undef XS_NEXT
+    par_for(pos, PAR_MIN, table_invert_range, entries);
 }
 
 static inline size_t bitrev(size_t x, int bits) {
@@ -543,31 +608,64 @@ static inline size_t bitrev(size_t x, int bits) {
 }
 
 /* in-place bit-reversal of 2^log_n items of stride_words u64 (basefold.cuh:57-90) */
-void or_bit_reverse_u64(u64 *data, int log_n, int stride_words) {
-    size_t N = (size_t)1 << log_n;
+typedef struct { u64 *data; int log_n, stride; } bitrev_ctx;
+/* each swap (i, j), i < j, is made by the part that owns i */
+static void bitrev_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    bitrev_ctx *c = (bitrev_ctx *)ctx;
     u64 tmp[8];
-    for (size_t i = 0; i < N; i++) {
-        size_t j = bitrev(i, log_n);
+    size_t w = (size_t)c->stride;
+    for (size_t i = lo; i < hi; i++) {
+        size_t j = bitrev(i, c->log_n);
         if (i < j) {
-            memcpy(tmp, data + i * stride_words, 8 * stride_words);
-            memcpy(data + i * stride_words, data + j * stride_words, 8 * stride_words);
-            memcpy(data + j * stride_words, tmp, 8 * stride_words);
+            memcpy(tmp, c->data + i * w, 8 * w);
+            memcpy(c->data + i * w, c->data + j * w, 8 * w);
+            memcpy(c->data + j * w, tmp, 8 * w);
         }
     }
+}
+void or_bit_reverse_u64(u64 *data, int log_n, int stride_words) {
+    bitrev_ctx c = {data, log_n, stride_words};
+    par_for((size_t)1 << log_n, PAR_MIN, bitrev_range, &c);
 }
 
 /* basefold_bhc_interpolate_ffi (goldilocks-cuda-rs/cuda/wrapper.cu:1242-1274 with
  * cuda/basefold.cuh:103-147): Moebius transform evals -> coeffs; bh_evals is the
  * bit-reversed copy of evals. */
+/* one butterfly layer over pairs p = (base, j): base = (p / h) 2h, lo = base + j, hi = lo + h */
+typedef struct { u64 *v; size_t h; int kind; } layer_ctx;
+static void layer_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    layer_ctx *c = (layer_ctx *)ctx;
+    size_t h = c->h;
+    for (size_t p = lo; p < hi; p++) {
+        size_t a = (p / h) * 2 * h + (p % h), b = a + h;
+        if (c->kind == 0) { /* Moebius: hi -= lo */
+            c->v[b] = gl_sub(c->v[b], c->v[a]);
+        } else { /* +-1 butterfly */
+            u64 x = c->v[a], y = c->v[b];
+            c->v[a] = gl_add(x, y);
+            c->v[b] = gl_sub(x, y);
+        }
+    }
+}
+typedef struct { u64 *dst; const u64 *src; int shift; } copy_ctx;
+static void canon_copy_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    copy_ctx *c = (copy_ctx *)ctx;
+    for (size_t k = lo; k < hi; k++) c->dst[k] = gl_canon(c->src[k >> c->shift]);
+}
+
 void or_bhc_interpolate(const u64 *evals, int n, u64 *coeffs, u64 *bh_evals) {
     size_t N = (size_t)1 << n;
-    for (size_t k = 0; k < N; k++) coeffs[k] = gl_canon(evals[k]);
+    copy_ctx cc = {coeffs, evals, 0};
+    par_for(N, PAR_MIN, canon_copy_range, &cc);
     for (int lvl = 0; lvl < n; lvl++) {
-        size_t h = (size_t)1 << lvl;
-        for (size_t base = 0; base < N; base += 2 * h)
-            for (size_t j = 0; j < h; j++) coeffs[base + h + j] = gl_sub(coeffs[base + h + j], coeffs[base + j]);
+        layer_ctx lc = {coeffs, (size_t)1 << lvl, 0};
+        par_for(N / 2, PAR_MIN, layer_range, &lc);
     }
-    for (size_t k = 0; k < N; k++) bh_evals[k] = gl_canon(evals[k]);
+    copy_ctx cb = {bh_evals, evals, 0};
+    par_for(N, PAR_MIN, canon_copy_range, &cb);
     or_bit_reverse_u64(bh_evals, n, 1);
 }
 
@@ -575,24 +673,38 @@ void or_bhc_interpolate(const u64 *evals, int n, u64 *coeffs, u64 *bh_evals) {
  * x 2^lr, n layers of (lo + hi, lo - hi) at half-chunk 2^(i+lr), then bit reversal. */
 void or_basefold_encode(const u64 *coeffs, int n, int log_rate, u64 *cw) {
     size_t L = (size_t)1 << (n + log_rate);
-    for (size_t k = 0; k < L; k++) cw[k] = gl_canon(coeffs[k >> log_rate]);
+    copy_ctx cc = {cw, coeffs, log_rate};
+    par_for(L, PAR_MIN, canon_copy_range, &cc);
     for (int i = 0; i < n; i++) {
-        size_t h = (size_t)1 << (i + log_rate);
-        for (size_t base = 0; base < L; base += 2 * h)
-            for (size_t j = 0; j < h; j++) {
-                u64 lo = cw[base + j], hi = cw[base + h + j];
-                cw[base + j] = gl_add(lo, hi);
-                cw[base + h + j] = gl_sub(lo, hi);
-            }
+        layer_ctx lc = {cw, (size_t)1 << (i + log_rate), 1};
+        par_for(L / 2, PAR_MIN, layer_range, &lc);
     }
     or_bit_reverse_u64(cw, n + log_rate, 1);
 }
 
+typedef struct { const u64 *in; u64 *out; } hash_ctx;
+static void compress_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    hash_ctx *c = (hash_ctx *)ctx;
+    for (size_t i = lo; i < hi; i++) or_poseidon2_compress(c->in + 8 * i, c->in + 8 * i + 4, c->out + 4 * i);
+}
+static void gl_leaf_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    hash_ctx *c = (hash_ctx *)ctx;
+    for (size_t i = lo; i < hi; i++) or_poseidon2_hash_gl_leaf(c->in[2 * i], c->in[2 * i + 1], c->out + 4 * i);
+}
+static void ext2_leaf_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    hash_ctx *c = (hash_ctx *)ctx;
+    for (size_t i = lo; i < hi; i++) or_poseidon2_hash_ext2_leaf(c->in + 4 * i, c->in + 4 * i + 2, c->out + 4 * i);
+}
+#define PAR_MIN_HASH 256 /* permutations per part */
+
 static void merkle_layers(u64 *tree, size_t num_leaves) {
     size_t off = 0, sz = num_leaves;
     while (sz > 1) {
-        for (size_t i = 0; i < sz / 2; i++)
-            or_poseidon2_compress(tree + (off + 2 * i) * 4, tree + (off + 2 * i + 1) * 4, tree + (off + sz + i) * 4);
+        hash_ctx c = {tree + off * 4, tree + (off + sz) * 4};
+        par_for(sz / 2, PAR_MIN_HASH, compress_range, &c);
         off += sz;
         sz /= 2;
     }
@@ -600,11 +712,13 @@ static void merkle_layers(u64 *tree, size_t num_leaves) {
 
 /* DeviceMerkleTree::build_from_gl_codeword (merkle.rs:34-60; cpu_basefold.rs:22-78) */
 void or_merkle_tree_gl(const u64 *cw, size_t num_leaves, u64 *tree) {
-    for (size_t i = 0; i < num_leaves; i++) or_poseidon2_hash_gl_leaf(cw[2 * i], cw[2 * i + 1], tree + 4 * i);
+    hash_ctx c = {cw, tree};
+    par_for(num_leaves, PAR_MIN_HASH, gl_leaf_range, &c);
     merkle_layers(tree, num_leaves);
 }
 void or_merkle_tree_ext2(const u64 *cw, size_t num_leaves, u64 *tree) {
-    for (size_t i = 0; i < num_leaves; i++) or_poseidon2_hash_ext2_leaf(cw + 4 * i, cw + 4 * i + 2, tree + 4 * i);
+    hash_ctx c = {cw, tree};
+    par_for(num_leaves, PAR_MIN_HASH, ext2_leaf_range, &c);
     merkle_layers(tree, num_leaves);
 }
 
@@ -644,16 +758,37 @@ size_t or_basefold_proof_len(int n, int lr, int q) {
     return 2 + (size_t)n * 6 + (size_t)(n - 1) * 4 + ((size_t)2 << lr) + (size_t)q * per_q;
 }
 
-/* sumcheck oracle in coefficient form from P(0), P(1), P(2) (cpu_basefold.rs:157-221) */
-static void oracle_from_pairs(const e2 *bh, const e2 *eq, size_t size, e2 out[3]) {
-    e2 two = e2_base(2), inv2 = e2_base(9223372034707292161ULL);
+/* P(0), P(1), P(2) partial sums of pairs [lo, hi), written to part's slot */
+typedef struct { const e2 *bh, *eq; e2 (*acc)[3]; } pairs_ctx;
+static void pairs_range(void *ctx, size_t lo, size_t hi, int part) {
+    pairs_ctx *c = (pairs_ctx *)ctx;
+    const e2 *eq = c->eq, *bh = c->bh;
+    e2 two = e2_base(2);
     e2 p0 = e2_base(0), p1 = e2_base(0), p2 = e2_base(0);
-    for (size_t j = 0; j < size / 2; j++) {
+    for (size_t j = lo; j < hi; j++) {
         p0 = e2_add(p0, e2_mul(eq[2 * j], bh[2 * j]));
         p1 = e2_add(p1, e2_mul(eq[2 * j + 1], bh[2 * j + 1]));
         e2 ei = e2_sub(e2_mul(two, eq[2 * j + 1]), eq[2 * j]);
         e2 bi = e2_sub(e2_mul(two, bh[2 * j + 1]), bh[2 * j]);
         p2 = e2_add(p2, e2_mul(ei, bi));
+    }
+    c->acc[part][0] = p0;
+    c->acc[part][1] = p1;
+    c->acc[part][2] = p2;
+}
+
+/* sumcheck oracle in coefficient form from P(0), P(1), P(2) (cpu_basefold.rs:157-221) */
+static void oracle_from_pairs(const e2 *bh, const e2 *eq, size_t size, e2 out[3]) {
+    e2 two = e2_base(2), inv2 = e2_base(9223372034707292161ULL);
+    e2 acc[OR_MAX_THREADS][3];
+    pairs_ctx pc = {bh, eq, acc};
+    int parts = or_parts(size / 2, PAR_MIN);
+    par_for(size / 2, PAR_MIN, pairs_range, &pc);
+    e2 p0 = e2_base(0), p1 = e2_base(0), p2 = e2_base(0);
+    for (int k = 0; k < parts; k++) {
+        p0 = e2_add(p0, acc[k][0]);
+        p1 = e2_add(p1, acc[k][1]);
+        p2 = e2_add(p2, acc[k][2]);
     }
     e2 c2 = e2_mul(e2_add(e2_sub(p0, e2_mul(two, p1)), p2), inv2);
     out[0] = p0;
@@ -670,6 +805,60 @@ static inline e2 fold_one(e2 v0, e2 v1, u64 x0, u64 w, e2 ch) {
 static void put_e2(u64 *p, e2 v) {
     p[0] = v.c0;
     p[1] = v.c1;
+}
+
+/* open-phase loops split over host threads */
+typedef struct { e2 *bh; const u64 *bh_evals; int n; } bh_init_ctx;
+static void bh_init_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    bh_init_ctx *c = (bh_init_ctx *)ctx;
+    for (size_t k = lo; k < hi; k++) c->bh[k] = e2_base(c->bh_evals[bitrev(k, c->n)]);
+}
+typedef struct { const e2 *a, *b; e2 *acc; } dot_ctx;
+static void dot_range(void *ctx, size_t lo, size_t hi, int part) {
+    dot_ctx *c = (dot_ctx *)ctx;
+    e2 s = e2_base(0);
+    for (size_t k = lo; k < hi; k++) s = e2_add(s, e2_mul(c->a[k], c->b[k]));
+    c->acc[part] = s;
+}
+static e2 dot_ext2(const e2 *a, const e2 *b, size_t n) {
+    e2 acc[OR_MAX_THREADS];
+    dot_ctx c = {a, b, acc};
+    int parts = or_parts(n, PAR_MIN);
+    par_for(n, PAR_MIN, dot_range, &c);
+    e2 s = e2_base(0);
+    for (int k = 0; k < parts; k++) s = e2_add(s, acc[k]);
+    return s;
+}
+/* eq and bh halves: dst[j] = src[2j] + ch (src[2j+1] - src[2j]), out of place */
+typedef struct { const e2 *eq, *bh; e2 *eq_out, *bh_out; e2 ch; } half_fold_ctx;
+static void half_fold_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    half_fold_ctx *c = (half_fold_ctx *)ctx;
+    for (size_t j = lo; j < hi; j++) {
+        e2 l = c->eq[2 * j], h = c->eq[2 * j + 1];
+        c->eq_out[j] = e2_add(l, e2_mul(c->ch, e2_sub(h, l)));
+        l = c->bh[2 * j];
+        h = c->bh[2 * j + 1];
+        c->bh_out[j] = e2_add(l, e2_mul(c->ch, e2_sub(h, l)));
+    }
+}
+/* codeword fold: out[i] = fold(v[2i], v[2i+1]) with level table entry i */
+typedef struct { const u64 *base_cw; const e2 *prev; const u64 *lv; e2 *out; e2 ch; } cw_fold_ctx;
+static void cw_fold_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    cw_fold_ctx *c = (cw_fold_ctx *)ctx;
+    for (size_t i = lo; i < hi; i++) {
+        e2 v0, v1;
+        if (c->base_cw) {
+            v0 = e2_base(c->base_cw[2 * i]);
+            v1 = e2_base(c->base_cw[2 * i + 1]);
+        } else {
+            v0 = c->prev[2 * i];
+            v1 = c->prev[2 * i + 1];
+        }
+        c->out[i] = fold_one(v0, v1, c->lv[2 * i], c->lv[2 * i + 1], c->ch);
+    }
 }
 
 int or_basefold_open_ext2(const u64 *cw0, const u64 *bh_evals, const u64 *tree0, const u64 root[4], int n,
@@ -689,10 +878,12 @@ int or_basefold_open_ext2(const u64 *cw0, const u64 *bh_evals, const u64 *tree0,
     e2 *eq = (e2 *)malloc(sizeof(e2) * N);
     eq_table_ext2(pt, n, eq);
     e2 *bh = (e2 *)malloc(sizeof(e2) * N);
-    for (size_t k = 0; k < N; k++) bh[k] = e2_base(bh_evals[bitrev(k, n)]);
+    bh_init_ctx bc = {bh, bh_evals, n};
+    par_for(N, PAR_MIN, bh_init_range, &bc);
+    e2 *eq_b = (e2 *)malloc(sizeof(e2) * (N / 2));
+    e2 *bh_b = (e2 *)malloc(sizeof(e2) * (N / 2));
 
-    e2 eval = e2_base(0);
-    for (size_t k = 0; k < N; k++) eval = e2_add(eval, e2_mul(bh[k], eq[k]));
+    e2 eval = dot_ext2(bh, eq, N);
     put_e2(pp, eval);
     pp += 2;
 
@@ -719,13 +910,13 @@ int or_basefold_open_ext2(const u64 *cw0, const u64 *bh_evals, const u64 *tree0,
         e2 ch = bt_sample_ext2(t);
         if (rd < n - 1) {
             size_t half = sc / 2;
-            for (size_t j = 0; j < half; j++) {
-                e2 lo = eq[2 * j], hi = eq[2 * j + 1];
-                eq[j] = e2_add(lo, e2_mul(ch, e2_sub(hi, lo)));
-                lo = bh[2 * j];
-                hi = bh[2 * j + 1];
-                bh[j] = e2_add(lo, e2_mul(ch, e2_sub(hi, lo)));
-            }
+            half_fold_ctx hc = {eq, bh, eq_b, bh_b, ch};
+            par_for(half, PAR_MIN, half_fold_range, &hc);
+            e2 *t0 = eq, *t1 = bh;
+            eq = eq_b;
+            bh = bh_b;
+            eq_b = t0;
+            bh_b = t1;
             sc = half;
             oracle_from_pairs(bh, eq, sc, o);
             for (int c = 0; c < 3; c++) {
@@ -737,17 +928,8 @@ int or_basefold_open_ext2(const u64 *cw0, const u64 *bh_evals, const u64 *tree0,
         size_t pairs = L >> (rd + 1);
         const u64 *lv = tab + 2 * lvl_off[rd];
         e2 *out = (e2 *)malloc(sizeof(e2) * pairs);
-        for (size_t i = 0; i < pairs; i++) {
-            e2 v0, v1;
-            if (rd == 0) {
-                v0 = e2_base(cw0[2 * i]);
-                v1 = e2_base(cw0[2 * i + 1]);
-            } else {
-                v0 = fcw[rd - 1][2 * i];
-                v1 = fcw[rd - 1][2 * i + 1];
-            }
-            out[i] = fold_one(v0, v1, lv[2 * i], lv[2 * i + 1], ch);
-        }
+        cw_fold_ctx fc = {rd == 0 ? cw0 : NULL, rd == 0 ? NULL : fcw[rd - 1], lv, out, ch};
+        par_for(pairs, PAR_MIN, cw_fold_range, &fc);
         fcw[rd] = out;
         if (rd < n - 1) {
             size_t leaves = pairs / 2;
@@ -794,6 +976,8 @@ int or_basefold_open_ext2(const u64 *cw0, const u64 *bh_evals, const u64 *tree0,
     free(pt);
     free(eq);
     free(bh);
+    free(eq_b);
+    free(bh_b);
     return 0;
 }
 
@@ -1468,29 +1652,45 @@ void or_ajtai_commit_wide(const uint32_t key[8], const u64 *z, u64 N, u64 col_of
     }
 }
 
-void or_ajtai_commit_u8_batch(const uint32_t key[8], const uint8_t *z8, u64 N, int B, int row_lo, int nrows,
-                              u64 *out) {
-    u64 *M = (u64 *)malloc(sizeof(u64) * (size_t)nrows * N * 64);
-    for (int i = 0; i < nrows; i++)
-        for (u64 j = 0; j < N; j++) or_ajtai_ring_elem(key, (uint32_t)(row_lo + i), j, M + ((size_t)i * N + j) * 64);
-    for (int b = 0; b < B; b++) {
-        const uint8_t *zb = z8 + (size_t)b * N * 64;
-        for (int i = 0; i < nrows; i++) {
+typedef struct { const uint32_t *key; int row_lo; u64 N; u64 *M; } ajtai_m_ctx;
+static void ajtai_m_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    ajtai_m_ctx *c = (ajtai_m_ctx *)ctx;
+    for (size_t k = lo; k < hi; k++)
+        or_ajtai_ring_elem(c->key, (uint32_t)(c->row_lo + (int)(k / c->N)), k % c->N, c->M + k * 64);
+}
+typedef struct { const u64 *M; const uint8_t *z8; u64 N; int nrows; u64 *out; } ajtai_w_ctx;
+static void ajtai_witness_range(void *ctx, size_t lo, size_t hi, int part) {
+    (void)part;
+    ajtai_w_ctx *c = (ajtai_w_ctx *)ctx;
+    u64 N = c->N;
+    for (size_t b = lo; b < hi; b++) {
+        const uint8_t *zb = c->z8 + b * N * 64;
+        for (int i = 0; i < c->nrows; i++) {
             /* positive and negative parts accumulated exactly in 128 bits:
              * each product < 2^72, at most N*64 <= 2^26 terms per coefficient */
             for (int r = 0; r < 64; r++) {
                 u128 pos = 0, neg = 0;
                 for (u64 j = 0; j < N; j++) {
-                    const u64 *Mij = M + ((size_t)i * N + j) * 64;
+                    const u64 *Mij = c->M + ((size_t)i * N + j) * 64;
                     const uint8_t *zj = zb + j * 64;
                     for (int l = 0; l <= r; l++) pos += (u128)Mij[r - l] * zj[l];
                     for (int l = r + 1; l < 64; l++) neg += (u128)Mij[r - l + 64] * zj[l];
                 }
                 u64 pm = (u64)(pos % AGL_Q), nm = (u64)(neg % AGL_Q);
-                out[((size_t)b * nrows + i) * 64 + r] = agl_sub(pm, nm);
+                c->out[(b * (size_t)c->nrows + i) * 64 + r] = agl_sub(pm, nm);
             }
         }
     }
+}
+/* witnesses split over the host threads (one witness per part at least) */
+void or_ajtai_commit_u8_batch(const uint32_t key[8], const uint8_t *z8, u64 N, int B, int row_lo, int nrows,
+                              u64 *out) {
+    u64 *M = (u64 *)malloc(sizeof(u64) * (size_t)nrows * N * 64);
+    ajtai_m_ctx mc = {key, row_lo, N, M};
+    par_for((size_t)nrows * N, 64, ajtai_m_range, &mc);
+    ajtai_w_ctx wc = {M, z8, N, nrows, out};
+    par_for((size_t)B, 1, ajtai_witness_range, &wc);
     free(M);
 }
 

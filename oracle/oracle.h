@@ -32,6 +32,11 @@
 extern "C" {
 #endif
 
+/* ---- Host threads for the large loops of one proof (results do not depend on them);
+ * default 1, at most 256 ---- */
+void or_set_threads(int k);
+int or_get_threads(void);
+
 /* ---- Goldilocks scalar + Ext2 (X^2 - 7) ---- */
 uint64_t or_gl_add(uint64_t a, uint64_t b);
 uint64_t or_gl_sub(uint64_t a, uint64_t b);

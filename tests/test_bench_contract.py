@@ -1,17 +1,21 @@
-"""The reference arm of bench.py on CPU: the JSON line it prints (one bounded step of the CPU
+"""The reference arm of bench.py on CPU: the JSON line it prints (one full-size step of the CPU
 restatement), and the silent exit of ranks other than 0 under a multi-rank launch."""
 import json
 import os
 import subprocess
 import sys
+import time
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _run(extra_env):
     env = dict(os.environ, **extra_env)
-    return subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
-                          cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    t0 = time.perf_counter()
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
+                         cwd=ROOT, env=env, capture_output=True, text=True, timeout=900)
+    out.wall_s = time.perf_counter() - t0
+    return out
 
 
 def test_reference_arm_line():
@@ -27,6 +31,9 @@ def test_reference_arm_line():
     assert line["e2e"] == {"value": line["value"], "unit": "proofs/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["num_vars"] == 22 and line["config"]["num_queries"] == 34
+    # each step is a measured full-size proof: the timed steps fit inside the process's own run
+    assert line["steps"] * line["ms_per_step"] / 1e3 <= out.wall_s
+    assert len(line["step_ms_all"]) == line["steps"]
 
 
 def test_reference_arm_other_ranks_exit_quietly():
