@@ -199,6 +199,44 @@ def ref_vectors():
     return out
 
 
+def _sha(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<u8").tobytes()).hexdigest()
+
+
+def basefold_kernel_vectors():
+    """Basefold commitments made by the reference's own kernels (cuda/basefold.cuh and the Merkle
+    kernels of goldilocks-cuda-rs/cuda/wrapper.cu) run on the host by oracle/_ref/libbasefold_ref.so,
+    on the seeded inputs of tests/seeded_inputs.py (so the GPU machine can regenerate the inputs)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import seeded_inputs as SI
+    u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+    R = ctypes.CDLL(os.path.join(REPO, "oracle/_ref/libbasefold_ref.so"))
+    R.ref_bf_init()
+    R.ref_basefold_commit.argtypes = [u64p, ctypes.c_int, ctypes.c_int, u64p, u64p, u64p, u64p]
+    cases = []
+    for n, lr in [(1, 1), (4, 1), (6, 3), (13, 1), (16, 2), (22, 1)]:
+        ev, _ = SI.c2_inputs(n)
+        L = 1 << (n + lr)
+        cw, bh = np.zeros(L, np.uint64), np.zeros(1 << n, np.uint64)
+        tree, root = np.zeros((L - 1) * 4, np.uint64), np.zeros(4, np.uint64)
+        R.ref_basefold_commit(ev, n, lr, cw, bh, tree, root)
+        P_ = np.uint64(P)
+        cw, bh, tree, root = cw % P_, bh % P_, tree % P_, root % P_  # canonical, as the reference compares
+        case = {"num_vars": n, "log_rate": lr, "evals_sha256": _sha(ev), "root": [int(x) for x in root],
+                "codeword_sha256": _sha(cw), "bh_evals_sha256": _sha(bh), "tree_sha256": _sha(tree)}
+        if L <= 64:
+            case["codeword"] = [int(x) for x in cw]
+        cases.append(case)
+    return {"source": "cuda/basefold.cuh:57-205 (bit reverse, interpolation, encode) and "
+                      "goldilocks-cuda-rs/cuda/wrapper.cu:934-960, 1604-1710 (leaf hashes, tree layers), "
+                      "launched as wrapper.cu:1242-1313 and :1653-1710 do and in the order of "
+                      "BasefoldCommitment::commit_device (goldilocks-cuda-rs/src/basefold.rs:380-410); "
+                      "run on the host by oracle/_ref/libbasefold_ref.so",
+            "inputs": "tests/seeded_inputs.py c2_inputs(num_vars)",
+            "cases": cases}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("MORPHEUS_REFERENCE"),
@@ -213,6 +251,10 @@ def main():
     with open(os.path.join(HERE, "reference_vectors.json"), "w") as f:
         json.dump(data, f, indent=0)
     print("wrote", os.path.join(HERE, "reference_vectors.json"))
+    with open(os.path.join(HERE, "reference_basefold.json"), "w") as f:
+        json.dump({"generated_by": "tests/golden/make_golden.py",
+                   "basefold_commit_ref": basefold_kernel_vectors()}, f, indent=0)
+    print("wrote", os.path.join(HERE, "reference_basefold.json"))
 
 
 if __name__ == "__main__":

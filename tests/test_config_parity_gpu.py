@@ -105,3 +105,21 @@ def test_c2_basefold_commit_open_matches_oracle_fixture(gpu_lib, goldens, key):
     assert [int(x) for x in c2.root] == g["root"]
     assert sha(c2.open_ext2(pt, table, S.Transcript(g["label"].encode()), q)) == g["proof_sha256"]
     d_ev.free()
+
+
+def _ref_commit_cases():
+    with open(os.path.join(HERE, "golden", "reference_basefold.json")) as f:
+        return json.load(f)["basefold_commit_ref"]["cases"]
+
+
+@pytest.mark.parametrize("case", _ref_commit_cases(), ids=lambda c: f"n{c['num_vars']}_lr{c['log_rate']}")
+def test_commit_equals_reference_kernels(gpu_lib, case):
+    """The commitment equals the one the reference's own Basefold and Merkle kernels made."""
+    from morpheus_gb300.basefold import BasefoldCommitment
+    n, lr = case["num_vars"], case["log_rate"]
+    ev, _ = SI.c2_inputs(n)
+    assert sha(ev) == case["evals_sha256"]
+    c = BasefoldCommitment.commit(ev, n, lr)
+    assert [int(x) for x in c.root] == case["root"]
+    assert sha(c.codeword()) == case["codeword_sha256"]
+    assert sha(c.tree()) == case["tree_sha256"]
