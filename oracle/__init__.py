@@ -505,3 +505,114 @@ def ajtai_commit_u8_batch(key, z8, row_lo=0, nrows=16):
     out = np.zeros((B, nrows, 64), np.uint64)
     lib().or_ajtai_commit_u8_batch(_a(key, np.uint32), z8.reshape(-1), N, B, row_lo, nrows, out.reshape(-1))
     return out
+
+
+# ---- The reference's own Basefold kernels run on the host (oracle/_ref/libbasefold_ref.so) ----
+_REF_BF = None
+_OBS = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64))
+_SAMP = ctypes.CFUNCTYPE(ctypes.c_uint64, ctypes.c_void_p)
+
+
+class _RefTranscript(ctypes.Structure):
+    _fields_ = [("ctx", ctypes.c_void_p), ("observe_ext2", _OBS), ("observe_hash", _OBS), ("sample", _SAMP),
+                ("sample_ext2", _OBS)]
+
+
+def ref_basefold_lib():
+    """The reference's Basefold/Merkle kernels built for the host, or None where the reference
+    checkout was not available to build them."""
+    global _REF_BF
+    if _REF_BF is None:
+        path = os.path.join(_HERE, "_ref", "libbasefold_ref.so")
+        if not os.path.exists(path):
+            return None
+        R = ctypes.CDLL(path)
+        R.ref_bf_init()
+        R.ref_basefold_commit.argtypes = [_u64p, _c.c_int, _c.c_int, _u64p, _u64p, _u64p, _u64p]
+        R.ref_merkle_tree_ext2.argtypes = [_u64p, _u64p, _c.c_int]
+        R.ref_basefold_open_ext2.argtypes = [_u64p, _u64p, _u64p, _u64p, _c.c_int, _c.c_int, _u64p, _u64p, _u64p,
+                                             ctypes.POINTER(_RefTranscript), _c.c_int, _u64p]
+        _REF_BF = R
+    return _REF_BF
+
+
+def ref_basefold_commit(evals, log_rate):
+    """BasefoldCommitment::commit_device made by the reference's kernels (canonical outputs)."""
+    R = ref_basefold_lib()
+    evals = _a(evals)
+    n = evals.size.bit_length() - 1
+    L = 1 << (n + log_rate)
+    cw, bh = np.zeros(L, np.uint64), np.zeros(1 << n, np.uint64)
+    tree, root = np.zeros((L - 1) * 4, np.uint64), np.zeros(4, np.uint64)
+    R.ref_basefold_commit(evals, n, log_rate, cw, bh, tree, root)
+    p = np.uint64(P)
+    return {"root": root % p, "codeword": cw % p, "bh_evals": bh % p, "tree": tree % p, "num_vars": n,
+            "log_rate": log_rate}
+
+
+def ref_basefold_open_ext2(comm, point, table, transcript, num_queries):
+    """open_ext2 (goldilocks-cuda-rs/src/basefold.rs:578-870) over the reference's kernels, the
+    Fiat-Shamir steps on `transcript` (a Transcript of this package, the BasefoldTranscript rules of
+    zk-torch-3/src/transcript.rs:331-350).  Returns the proof in the flat layout, canonical."""
+    R = ref_basefold_lib()
+    n, lr = comm["num_vars"], comm["log_rate"]
+    ent, off = table
+    t = transcript
+
+    def observe_ext2(_, v):
+        t.append_ext2(b"", np.array([v[0], v[1]], np.uint64))
+
+    def observe_hash(_, h):
+        for i in range(4):
+            t.append_scalar(b"", h[i])
+
+    def sample(_):
+        return t.challenge_scalar(b"")
+
+    def sample_ext2(_, out):
+        c = t.challenge_ext2(b"")
+        out[0], out[1] = int(c[0]), int(c[1])
+    cbs = (_OBS(observe_ext2), _OBS(observe_hash), _SAMP(sample), _OBS(sample_ext2))
+    rt = _RefTranscript(None, *cbs)
+    proof = np.zeros(basefold_proof_len(n, lr, num_queries), np.uint64)
+    rc = R.ref_basefold_open_ext2(_a(comm["codeword"]), _a(comm["bh_evals"]), _a(comm["tree"]), _a(comm["root"]), n,
+                                  lr, _a(point).reshape(-1), _a(ent).reshape(-1), _a(off), ctypes.byref(rt),
+                                  num_queries, proof)
+    assert rc == 0
+    return proof % np.uint64(P)
+
+
+class _RefSumcheckTranscript(ctypes.Structure):
+    _fields_ = [("ctx", ctypes.c_void_p), ("append_message", _OBS), ("challenge", _OBS)]
+
+
+def ref_sumcheck_prove_ext2(transcript, polys):
+    """GpuLinearSumcheckProver::new + prove (zk-torch-3/src/sumcheck/gpu_prover.rs:21-90) over the
+    reference's sumcheck kernels (cuda/sumcheck_prover.cuh) run on the host; the transcript is a
+    Transcript of this package.  Same result layout as sumcheck_prove_ext2."""
+    R = ref_basefold_lib()
+    R.ref_sumcheck_prove_ext2.argtypes = [_u64p, _c.c_int, _c.c_int, ctypes.POINTER(_RefSumcheckTranscript), _u64p,
+                                          _u64p, _u64p, _u64p]
+    polys = _a(polys)
+    d, N = polys.shape
+    n = N.bit_length() - 1
+    t = transcript
+    t.append_u64(b"num_var", n)
+    t.append_u64(b"num_poly", d)
+
+    def append_message(_, v):
+        t.append_ext2(b"round_message", np.array([v[0], v[1]], np.uint64))
+
+    def challenge(_, out):
+        c = t.challenge_ext2(b"challenge")
+        out[0], out[1] = int(c[0]), int(c[1])
+    cbs = (_OBS(append_message), _OBS(challenge))
+    rt = _RefSumcheckTranscript(None, *cbs)
+    msgs = np.zeros((n, d + 1, 2), np.uint64)
+    ch = np.zeros((n, 2), np.uint64)
+    finals = np.zeros((d, 2), np.uint64)
+    fe = np.zeros(2, np.uint64)
+    rc = R.ref_sumcheck_prove_ext2(polys.reshape(-1), n, d, ctypes.byref(rt), msgs.reshape(-1), ch.reshape(-1),
+                                   finals.reshape(-1), fe)
+    assert rc == 0
+    return {"round_messages": msgs, "challenges": ch, "final_evals": finals, "final_eval": fe}

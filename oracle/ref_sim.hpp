@@ -40,7 +40,7 @@ extern thread_local FiberBlock* t_block;
 // One block's threads as fibers.  The scheduler resumes every unfinished fiber in turn; a fiber
 // returns to it at each barrier and when its kernel body ends.
 struct FiberBlock {
-    static constexpr size_t STACK = 256 << 10;
+    static constexpr size_t STACK = 64 << 10;
     std::vector<ucontext_t> ctx;
     std::vector<char> stacks;
     std::vector<uint8_t> done;

@@ -237,6 +237,76 @@ def basefold_kernel_vectors():
             "cases": cases}
 
 
+def basefold_open_vectors():
+    """Openings made by the reference's kernels (open_ext2's launch sequence, basefold.rs:578-870,
+    restated around them; the transcript is the oracle's restatement of zk-torch-3's Transcript)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, REPO)
+    import oracle as O
+    import seeded_inputs as SI
+    O.set_threads(os.cpu_count() or 1)
+    cases = []
+
+    def record(name, evals, n, lr, point, table_vars, q, label, u64_after_label, explicit):
+        comm = O.ref_basefold_commit(evals, lr)
+        table = O.basefold_table(table_vars, lr, table_vars, 42)
+        t = O.Transcript(label)
+        if u64_after_label is not None:
+            t.append_u64(b"", u64_after_label)
+        proof = O.ref_basefold_open_ext2(comm, point, table, t, q)
+        head = 2 + 6 * n + 4 * (n - 1) + (2 << lr)
+        case = {"name": name, "num_vars": n, "log_rate": lr, "table_vars": table_vars, "table_seed": 42,
+                "num_queries": q, "label": label.decode(), "u64_after_label": u64_after_label,
+                "evals_sha256": _sha(evals), "point": [int(x) for x in np.asarray(point).reshape(-1)],
+                "root": [int(x) for x in comm["root"]], "proof_len": int(proof.size),
+                "proof_sha256": _sha(proof), "proof_head": [int(x) for x in proof[:head]]}
+        if explicit:
+            case["evals"] = [int(x) for x in evals]
+            case["proof"] = [int(x) for x in proof]
+        cases.append(case)
+
+    # the reference's own GPU-against-CPU opening test, its inputs exactly
+    # (zk-torch-3/src/commit/cpu_basefold.rs:433-509)
+    ev = np.array([(P - 1 - i * 1000 % P) % P for i in range(64)], np.uint64)
+    pt = np.array([[100 + i, 0] for i in range(6)], np.uint64)
+    record("cpu_vs_gpu_opening", ev, 6, 3, pt, 9, 10, b"test-open", 42, True)
+    # the C2 shape (seeded inputs of tests/seeded_inputs.py), rate 1/2, 34 queries
+    for n in (4, 13, 16, 22):
+        ev, pt = SI.c2_inputs(n)
+        record(f"c2_shape_n{n}", ev, n, 1, pt, n, 34, b"bf-open", None, n <= 4)
+    return {"source": "open_ext2 (goldilocks-cuda-rs/src/basefold.rs:578-870) with the reference's kernels "
+                      "(cuda/basefold.cuh, cuda/eq_lagrange.cuh, wrapper.cu Merkle kernels) run on the host by "
+                      "oracle/_ref/libbasefold_ref.so; launch sizes of wrapper.cu:1223-1600; commitment from "
+                      "the reference's kernels too",
+            "cases": cases}
+
+
+def sumcheck_vectors():
+    """Ext2-challenge product sumchecks made by the reference's kernels (cuda/sumcheck_prover.cuh,
+    launched as wrapper.cu:1751-1785 in GpuSumcheckStateExt2's sequence) on seeded inputs."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, REPO)
+    import oracle as O
+    import seeded_inputs as SI
+    cases = []
+    shapes = [("c1", SI.C1["seed"], 2, 20, SI.C1["label"]), ("d3_n12", 0x5C3, 3, 12, b"bench"),
+              ("d4_n10", 0x5C4, 4, 10, b"bench"), ("d8_n6", 0x5C8, 8, 6, b"bench")]
+    for name, seed, d, n, label in shapes:
+        polys = SI.field_elems(seed, d << n).reshape(d, 1 << n)
+        r = O.ref_sumcheck_prove_ext2(O.Transcript(label), polys)
+        cases.append({"name": name, "seed": seed, "degree": d, "num_vars": n, "label": label.decode(),
+                      "polys_sha256": _sha(polys),
+                      "round_messages": [int(x) for x in r["round_messages"].reshape(-1)],
+                      "challenges": [int(x) for x in r["challenges"].reshape(-1)],
+                      "final_evals": [int(x) for x in r["final_evals"].reshape(-1)],
+                      "final_eval": [int(x) for x in r["final_eval"]]})
+    return {"source": "GpuLinearSumcheckProver::prove (zk-torch-3/src/sumcheck/gpu_prover.rs:36-90) on "
+                      "GpuSumcheckStateExt2 (goldilocks-cuda-rs/src/sumcheck_prover.rs:215-410) with the "
+                      "reference's kernels run on the host by oracle/_ref/libbasefold_ref.so; inputs "
+                      "tests/seeded_inputs.py field_elems(seed, d << n)",
+            "cases": cases}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("MORPHEUS_REFERENCE"),
@@ -253,7 +323,9 @@ def main():
     print("wrote", os.path.join(HERE, "reference_vectors.json"))
     with open(os.path.join(HERE, "reference_basefold.json"), "w") as f:
         json.dump({"generated_by": "tests/golden/make_golden.py",
-                   "basefold_commit_ref": basefold_kernel_vectors()}, f, indent=0)
+                   "basefold_commit_ref": basefold_kernel_vectors(),
+                   "basefold_open_ref": basefold_open_vectors(),
+                   "sumcheck_ref": sumcheck_vectors()}, f, indent=0)
     print("wrote", os.path.join(HERE, "reference_basefold.json"))
 
 

@@ -123,3 +123,52 @@ def test_commit_equals_reference_kernels(gpu_lib, case):
     assert [int(x) for x in c.root] == case["root"]
     assert sha(c.codeword()) == case["codeword_sha256"]
     assert sha(c.tree()) == case["tree_sha256"]
+
+
+def _ref_open_cases():
+    with open(os.path.join(HERE, "golden", "reference_basefold.json")) as f:
+        return json.load(f)["basefold_open_ref"]["cases"]
+
+
+@pytest.mark.parametrize("case", _ref_open_cases(), ids=lambda c: c["name"])
+def test_open_equals_reference_kernels(gpu_lib, case):
+    """The whole proof equals the one open_ext2's sequence of the reference's own kernels made,
+    including the exact inputs of the reference's GPU-against-CPU opening test
+    (zk-torch-3/src/commit/cpu_basefold.rs:433-509: n = 6, table for 9 variables, rate 1/8)."""
+    from morpheus_gb300 import sumcheck as S
+    from morpheus_gb300.basefold import BasefoldCommitment, BasefoldTable
+    n, lr, q = case["num_vars"], case["log_rate"], case["num_queries"]
+    ev = np.array(case["evals"], np.uint64) if "evals" in case else SI.c2_inputs(n)[0]
+    pt = np.array(case["point"], np.uint64).reshape(-1, 2)
+    assert sha(ev) == case["evals_sha256"]
+    c = BasefoldCommitment.commit(ev, n, lr)
+    assert [int(x) for x in c.root] == case["root"]
+    table = BasefoldTable.generate(case["table_vars"], lr, case["table_vars"], case["table_seed"])
+    t = S.Transcript(case["label"].encode())
+    if case["u64_after_label"] is not None:
+        t.append_u64(b"", case["u64_after_label"])
+    proof = c.open_ext2(pt, table, t, q)
+    assert proof.size == case["proof_len"]
+    assert [int(x) for x in proof[:len(case["proof_head"])]] == case["proof_head"]
+    assert sha(proof) == case["proof_sha256"]
+
+
+def _ref_sumcheck_cases():
+    with open(os.path.join(HERE, "golden", "reference_basefold.json")) as f:
+        return json.load(f)["sumcheck_ref"]["cases"]
+
+
+@pytest.mark.parametrize("case", _ref_sumcheck_cases(), ids=lambda c: c["name"])
+def test_sumcheck_equals_reference_kernels(gpu_lib, case):
+    """Round messages, challenges and final evaluations equal those of the reference's own sumcheck
+    kernels in GpuLinearSumcheckProver's sequence (c1 = the 2 x 2^20 configuration)."""
+    from morpheus_gb300 import sumcheck as S
+    d, n = case["degree"], case["num_vars"]
+    polys = SI.field_elems(case["seed"], d << n).reshape(d, 1 << n)
+    assert sha(polys) == case["polys_sha256"]
+    t = S.Transcript(case["label"].encode())
+    pr = S.GpuLinearSumcheckProver(n, d, t).prove(polys, t)
+    assert [int(x) for x in pr.round_messages.reshape(-1)] == case["round_messages"]
+    assert [int(x) for x in pr.challenges.reshape(-1)] == case["challenges"]
+    assert [int(x) for x in pr.final_evals.reshape(-1)] == case["final_evals"]
+    assert [int(x) for x in pr.final_eval.reshape(-1)] == case["final_eval"]
