@@ -163,6 +163,12 @@ int gb_ajtai_key_info(void *handle, int *row_lo, int *rows, uint64_t *n_ring);
  * bytes (device); d_out is [num_witnesses][rows][64] canonical u64 (device).  Rows are those of
  * the key; the result equals ajtai_commit_wide_ffi restricted to those rows.  Synchronising. */
 int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses, uint64_t *d_out);
+/* Test switch of the calling thread for the GEMM's bounded waits: with on != 0 the following
+ * gb_ajtai_commit_u8_batched calls launch the tensor-core GEMM with its operand loads left out and
+ * short wait limits, so that its pipeline waits run out; the call then returns -1 with
+ * "pipeline wait timed out (code N)" in gb_last_error(), with no load in flight and TMEM
+ * released.  Returns the previous setting. */
+int gb_ajtai_test_starve(int on);
 
 /* ajtai_commit_wide_ffi without any device allocation (no counterpart in the reference).
  * Same arguments, result and return codes as ajtai_commit_wide_ffi, whose every call

@@ -168,6 +168,8 @@ struct GmSched {
     int tiles_m, chunks;  // M tiles; K chunks per tile
     long long units;      // tiles x chunks
     int ctas, slots;      // grid size; slots per tile (the most CTAs meeting one tile)
+    unsigned long long spin_limit;  // iterations of each bounded mbarrier wait
+    int starve;  // test mode: the producer issues no loads, so that every consumer wait runs out
 };
 __host__ __device__ inline long long gm_unit_begin(const GmSched& g, long long c) { return c * g.units / g.ctas; }
 __host__ __device__ inline int gm_cta_of(const GmSched& g, long long u) {  // the CTA whose range holds u
@@ -240,6 +242,7 @@ constexpr int GM_EPI_WARPS = 16;  // four warps per TMEM lane quarter, one per 6
 constexpr int GM_THREADS = 64 + 32 * GM_EPI_WARPS;
 constexpr int GM_SMEM = GM_STAGES * GM_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr unsigned long long GM_SPIN_LIMIT = 1ull << 26;  // bounded waits (seconds at worst)
+constexpr unsigned long long GM_SPIN_LIMIT_TEST = 1ull << 14;  // the starved test mode's limit
 
 __device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
 
@@ -264,8 +267,9 @@ __device__ __forceinline__ bool mbar_try_wait(u32 bar, u32 parity) {
     return ok != 0;
 }
 // bounded wait: false (and the error flag set) when the limit is reached
-__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity, int* err, int code) {
-    for (unsigned long long it = 0; it < GM_SPIN_LIMIT; it++) {
+__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity, int* err, int code,
+                                          unsigned long long limit = GM_SPIN_LIMIT) {
+    for (unsigned long long it = 0; it < limit; it++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 1023) == 1023 && *(volatile int*)err) return false;  // another role already gave up
     }
@@ -351,12 +355,12 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
     if (warp == 0) {
         if (lane == 0) {
             // kt counts this CTA's K tiles from 0 (stage and phase); unit kt / 16 gives the coordinates
-            const int my_tiles = chunks * GM_CHUNK_TILES;
+            const int my_tiles = sched.starve ? 0 : chunks * GM_CHUNK_TILES;
             int issued = 0;
             for (int kt = 0; kt < my_tiles; kt++) {
                 int s = kt % GM_STAGES;
                 u32 ph = (kt / GM_STAGES) & 1;
-                if (!mbar_wait(empty(s), ph ^ 1, err, 1)) break;
+                if (!mbar_wait(empty(s), ph ^ 1, err, 1, sched.spin_limit)) break;
                 mbar_expect_tx(full(s), GM_STAGE_BYTES);
                 uint8_t* sa = smem + s * GM_STAGE_BYTES;
                 const int lu = kt / GM_CHUNK_TILES, x = (unit_k0(lu) + kt % GM_CHUNK_TILES) * GM_BK;
@@ -368,7 +372,7 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
             }
             // loads still in flight land in shared memory: wait (bounded) for every issued stage
             for (int kt = issued - GM_STAGES < 0 ? 0 : issued - GM_STAGES; kt < issued; kt++)
-                mbar_wait(full(kt % GM_STAGES), (kt / GM_STAGES) & 1, err, 5);
+                mbar_wait(full(kt % GM_STAGES), (kt / GM_STAGES) & 1, err, 5, sched.spin_limit);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -376,13 +380,13 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
             for (int c = 0; c < chunks && ok; c++) {
                 int a = c & 1;
                 u32 use = (u32)(c >> 1);
-                if (!mbar_wait(acc_empty(a), (use & 1) ^ 1, err, 2)) break;
+                if (!mbar_wait(acc_empty(a), (use & 1) ^ 1, err, 2, sched.spin_limit)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const u32 d_tmem = tmem + (u32)(a * GM_BN);
                 for (int t = 0; t < GM_CHUNK_TILES; t++) {
                     int kt = c * GM_CHUNK_TILES + t;
                     int s = kt % GM_STAGES;
-                    if (!mbar_wait(full(s), (kt / GM_STAGES) & 1, err, 3)) {
+                    if (!mbar_wait(full(s), (kt / GM_STAGES) & 1, err, 3, sched.spin_limit)) {
                         ok = false;
                         break;
                     }
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
             }
             // every MMA this thread issued has completed before TMEM can be released
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done));
-            mbar_wait(mma_done, 0, err, 6);
+            mbar_wait(mma_done, 0, err, 6, sched.spin_limit);
         }
     } else {
         // epilogue: int32 totals of one TMEM row (lane) x 64 columns in registers
@@ -423,7 +427,7 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
         for (int c = 0; c < chunks && ok; c++) {
             int a = c & 1;
             u32 use = (u32)(c >> 1);
-            if (!mbar_wait(acc_full(a), use & 1, err, 4)) {
+            if (!mbar_wait(acc_full(a), use & 1, err, 4, sched.spin_limit)) {
                 ok = false;
                 break;
             }
@@ -553,6 +557,10 @@ static void key_free(AjtaiKey* k) {
     k->d_RS = nullptr;
 }
 
+// Test switch of the calling thread: the next GEMMs run starved (no operand loads, short wait
+// limits), so that their bounded waits run out and the call reports it; see gb_ajtai_test_starve.
+static thread_local int t_starve = 0;
+
 static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     if (B < 1) return GB_EINVAL;
     cudaStream_t s = stream();
@@ -566,6 +574,8 @@ static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out
     sched.units = tiles * sched.chunks;
     sched.ctas = (int)std::min<long long>(num_sms(), sched.units);
     sched.slots = 1;
+    sched.starve = t_starve;
+    sched.spin_limit = t_starve ? GM_SPIN_LIMIT_TEST : GM_SPIN_LIMIT;
     for (long long t = 0; t < tiles; t++)
         sched.slots = std::max(sched.slots, gm_cta_of(sched, (t + 1) * sched.chunks - 1) -
                                                 gm_cta_of(sched, t * sched.chunks) + 1);
@@ -992,6 +1002,12 @@ int gb_ajtai_commit_u8_batched(void* handle, const uint8_t* d_z, int num_witness
     AjtaiKey* k = (AjtaiKey*)handle;
     if (!k || !d_z || !d_out) return GB_EINVAL;
     return commit_batch(k, d_z, num_witnesses, d_out);
+}
+
+int gb_ajtai_test_starve(int on) {
+    int old = t_starve;
+    t_starve = on ? 1 : 0;
+    return old;
 }
 
 }  // extern "C"

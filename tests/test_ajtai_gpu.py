@@ -204,3 +204,29 @@ def test_ternary_and_sparse_vs_oracle(gpu_lib):
     assert L.ajtai_commit_sparse_ffi(d_key.ptr, d_p.ptr, len(p), 64, d_out.ptr) == 0
     assert np.array_equal(d_out.to_numpy().reshape(42, 64), O.ajtai_commit_wide(key, coeff, 0, 0, 42))
     assert L.ajtai_commit_sparse_ffi(d_key.ptr, d_p.ptr, 0, 64, d_out.ptr) == 0 and not d_out.to_numpy().any()
+
+
+def test_gemm_bounded_waits_time_out_and_the_context_recovers(gpu_lib):
+    """The tensor-core GEMM's mbarrier waits are bounded.  In the starved test mode the producer
+    issues no operand loads, so the MMA and epilogue waits can only run out: the call must return
+    -1 with the wait's code in gb_last_error(), and the next normal call on the same context must
+    be bit-exact (TMEM released, no copy left in flight)."""
+    import re
+    from morpheus_gb300 import ajtai, _native as N
+    L = N.lib()
+    key = np.array([3, 1, 4, 1, 5, 9, 2, 6], np.uint32)
+    k = ajtai.AjtaiKey(key, 0, 16, 64)
+    z8 = np.random.default_rng(31).integers(0, 256, size=(5, 64 * 64), dtype=np.uint8)
+    want = O.ajtai_commit_u8_batch(key, z8, 0, 16)
+    old = L.gb_ajtai_test_starve(1)
+    try:
+        with pytest.raises(N.NativeError) as exc:
+            k.commit_u8_batched(z8)
+        msg = L.gb_last_error().decode()
+        m = re.search(r"pipeline wait timed out \(code (\d)\)", msg)
+        assert m and 1 <= int(m.group(1)) <= 6, msg
+        assert "gb_ajtai_commit_u8_batched" in str(exc.value)
+    finally:
+        assert L.gb_ajtai_test_starve(old) == 1
+    for _ in range(2):
+        assert np.array_equal(k.commit_u8_batched(z8), want)
