@@ -557,9 +557,11 @@ def run_batched(args, summary=False):
 
 
 def run_served(args, summary=False):
-    """Served matmul-layer jobs arriving as a Poisson stream: the prover service (worker
-    streams, HBM-budget admission) against the per-call path (one job at a time, in arrival
-    order), both on the same arrival schedule; latency = arrival -> proof done."""
+    """Served matmul-layer jobs arriving as a Poisson stream.  The continuous prover service
+    (prologues on worker streams, every opening in flight batched round by round in the open
+    engines of its size class, HBM-budget admission) against the per-call path (one job at a time,
+    in arrival order), both on the same arrival schedule; latency = arrival -> proof done.  Each
+    offered load in `rates` gets its own schedule; the first is the headline load."""
     import torch
     from morpheus_gb300 import build as B
     B.build()
@@ -569,7 +571,6 @@ def run_served(args, summary=False):
     seed = (0x452821E638D01377 % P, 0xBE5466CF34E90C6C % P)
     table = BasefoldTable.generate(24, LOG_RATE, 24, TABLE_SEED)
     key = AjtaiKey(np.array([0xA11CE, 1, 2, 3, 4, 5, 6, 7], np.uint32), 0, 16, 1024)
-    jobs, arrivals = batch.matmul_stream(args.jobs, seed=7, rate_per_s=args.rate, num_queries=QUERIES)
     warm, _ = batch.matmul_stream(3, seed=8, rate_per_s=args.rate, num_queries=QUERIES)
     for j in warm:
         batch.prove_matmul(table, key, seed, j)
@@ -578,26 +579,24 @@ def run_served(args, summary=False):
     def pct(xs, q):
         return float(np.percentile(np.asarray(xs), q))
 
-    # per-call: one job at a time, each starting once it has arrived and the previous is done
-    lat_pc = []
-    t0 = time.perf_counter()
-    for j, a in zip(jobs, arrivals):
-        now = time.perf_counter() - t0
-        if now < a:
-            time.sleep(a - now)
-        batch.prove_matmul(table, key, seed, j)
-        lat_pc.append((time.perf_counter() - t0 - a) * 1e3)
-    span_pc = time.perf_counter() - t0
-    alone = [j.proof.copy() for j in jobs]
-    for j in jobs:
-        j.proof[:] = 0
+    def per_call(jobs, arrivals):
+        # one job at a time, each starting once it has arrived and the previous one is done
+        lat = []
+        t0 = time.perf_counter()
+        for j, a in zip(jobs, arrivals):
+            now = time.perf_counter() - t0
+            if now < a:
+                time.sleep(a - now)
+            batch.prove_matmul(table, key, seed, j)
+            lat.append((time.perf_counter() - t0 - a) * 1e3)
+        return time.perf_counter() - t0, lat
 
-    # served: submit at arrival, the service admits and overlaps the jobs
-    with batch.ProverService(table, seed, QUERIES, workers=args.workers, hbm_budget=args.hbm_budget_gb << 30) as svc:
-        svc.set_ajtai_key(key)
-        for j in warm:
-            svc.wait(svc.submit(j))
-        with ClockSampler() as clk:
+    def served(jobs, arrivals, continuous):
+        with batch.ProverService(table, seed, QUERIES, workers=args.workers, hbm_budget=args.hbm_budget_gb << 30,
+                                 continuous=continuous) as svc:
+            svc.set_ajtai_key(key)
+            for j in warm:
+                svc.wait(svc.submit(j))
             tickets = []
             t0 = time.perf_counter()
             for j, a in zip(jobs, arrivals):
@@ -607,17 +606,53 @@ def run_served(args, summary=False):
                 tickets.append(svc.submit(j))
             stats = [svc.wait(t)[1] for t in tickets]
             span = time.perf_counter() - t0
-    lat = [st["latency_ms"] for st in stats]
-    same = sum(np.array_equal(j.proof, a) for j, a in zip(jobs, alone))
-    h2d = sum(j.a.nbytes + j.b.nbytes for j in jobs)
+        return span, [st["latency_ms"] for st in stats]
+
+    rates = [args.rate] + [r for r in getattr(args, "low_rates", []) if r != args.rate]
+    runs = {}
+    clk = None
+    for rate in rates:
+        jobs, arrivals = batch.matmul_stream(args.jobs, seed=7, rate_per_s=rate, num_queries=QUERIES)
+        span_pc, lat_pc = per_call(jobs, arrivals)
+        alone = [j.proof.copy() for j in jobs]
+        for j in jobs:
+            j.proof[:] = 0
+        if rate == args.rate:
+            with ClockSampler() as clk:
+                span, lat = served(jobs, arrivals, True)
+        else:
+            span, lat = served(jobs, arrivals, True)
+        same = sum(np.array_equal(j.proof, a) for j, a in zip(jobs, alone))
+        run = {"offered_jobs_per_s": rate, "value": len(jobs) / span, "unit": "proofs/s",
+               "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "max_ms": max(lat),
+               "per_call": {"value": len(jobs) / span_pc, "p50_ms": pct(lat_pc, 50), "p99_ms": pct(lat_pc, 99)},
+               "served_over_per_call": span_pc / span, "identical_to_per_call": f"{same}/{len(jobs)}"}
+        if not summary:
+            # the whole-job service (a worker proves a job start to end on its stream), same schedule
+            for j in jobs:
+                j.proof[:] = 0
+            span_w, lat_w = served(jobs, arrivals, False)
+            run["whole_job_service"] = {"value": len(jobs) / span_w, "p50_ms": pct(lat_w, 50),
+                                        "p99_ms": pct(lat_w, 99),
+                                        "identical": f"{sum(np.array_equal(j.proof, a) for j, a in zip(jobs, alone))}/"
+                                                     f"{len(jobs)}"}
+        runs[rate] = (run, jobs)
+    head, jobs = runs[args.rate]
+    others = [runs[r][0] for r in rates[1:]]
+    workload = ("matmul-layer jobs (M, N, K in {256, 512, 1024, 4096}, int8), Poisson arrivals; continuous "
+                "service (openings batched round by round in one engine per size class); python bench.py "
+                "--workload served for the full run")
     if summary:
-        return {"value": len(jobs) / span, "unit": "proofs/s", "jobs": len(jobs), "offered_jobs_per_s": args.rate,
-                "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
-                "per_call": {"value": len(jobs) / span_pc, "p50_ms": pct(lat_pc, 50), "p99_ms": pct(lat_pc, 99)},
-                "identical_to_per_call": f"{same}/{len(jobs)}",
-                "workload": "matmul-layer jobs (M, N, K in {256, 512, 1024, 4096}, int8), Poisson arrivals; "
-                            "python bench.py --workload served for the full run"}
-    line = {"metric": "served proofs/sec", "value": len(jobs) / span, "unit": "proofs/s", "n_gpus": 1,
+        out = {k: head[k] for k in ("value", "unit", "p50_ms", "p99_ms", "per_call", "served_over_per_call",
+                                    "identical_to_per_call", "offered_jobs_per_s")}
+        out.update({"jobs": len(jobs), "engine": "continuous", "workload": workload,
+                    "below_capacity": [{k: o[k] for k in ("offered_jobs_per_s", "value", "p50_ms", "p99_ms",
+                                                          "served_over_per_call", "identical_to_per_call")}
+                                       for o in others]})
+        return out
+    h2d = sum(j.a.nbytes + j.b.nbytes for j in jobs)
+    span = len(jobs) / head["value"]
+    line = {"metric": "served proofs/sec", "value": head["value"], "unit": "proofs/s", "n_gpus": 1,
             "steps": len(jobs), "warmup": len(warm), "ms_per_step": span * 1e3 / len(jobs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)",
             "data": "synthetic",
@@ -625,18 +660,20 @@ def run_served(args, summary=False):
                                    "M, N, K uniform over {256, 512, 1024, 4096}, int8 values; per job: Basefold "
                                    "commit of A and B, partial evaluation, degree-2 sumcheck over K, open of A "
                                    "and B (34 queries), Ajtai commit of a 2^16 witness (16 rows)",
-                       "workers": args.workers, "hbm_budget_gb": args.hbm_budget_gb,
-                       "offered_load_jobs_per_s": args.rate, "table": "(24, 1, 24, seed 42)",
+                       "engine": "continuous (gb_prover_create_continuous)", "workers": args.workers,
+                       "hbm_budget_gb": args.hbm_budget_gb, "offered_load_jobs_per_s": args.rate,
+                       "table": "(24, 1, 24, seed 42)",
                        "timing": "host wall clock from the first arrival to the last proof",
                        "l2": "inputs larger than L2", "parallelism": "replicas x1"},
-            "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "max_ms": max(lat),
-            "per_call": {"value": len(jobs) / span_pc, "unit": "proofs/s", "p50_ms": pct(lat_pc, 50),
-                         "p99_ms": pct(lat_pc, 99)},
-            "served_over_per_call": span_pc / span,
-            "identical_to_per_call": f"{same}/{len(jobs)}",
-            "e2e": {"value": len(jobs) / span, "unit": "proofs/s", "h2d_bytes_per_step": int(h2d / len(jobs)),
+            "p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"], "max_ms": head["max_ms"],
+            "per_call": dict(head["per_call"], unit="proofs/s"),
+            "served_over_per_call": head["served_over_per_call"],
+            "identical_to_per_call": head["identical_to_per_call"],
+            "whole_job_service": head.get("whole_job_service"),
+            "other_loads": others,
+            "e2e": {"value": head["value"], "unit": "proofs/s", "h2d_bytes_per_step": int(h2d / len(jobs)),
                     "d2h_bytes_per_step": int(sum(j.proof.nbytes for j in jobs) / len(jobs))},
-            "clocks": clk.summary()}
+            "clocks": clk.summary() if clk else None}
     print(json.dumps(line))
 
 
@@ -653,6 +690,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="batched workload: the lockstep engine only (profiling)")
     ap.add_argument("--jobs", type=int, default=200, help="served workload: number of jobs")
     ap.add_argument("--rate", type=float, default=200.0, help="served workload: mean arrivals per second")
+    ap.add_argument("--low-rates", type=float, nargs="*", default=[80.0, 120.0],
+                    help="served workload: further offered loads reported beside --rate")
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")
     ap.add_argument("--hbm-budget-gb", type=int, default=96, help="served workload: admission budget")
     ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "batch_open", "peval", "ajtai", "batched", "served"],
@@ -811,8 +850,8 @@ def main():
         L.gb_set_stream(None)
         extras["batched_512"] = run_batched(argparse.Namespace(instances=512, steps=1, warmup=1, per_call_steps=1),
                                             summary=True)
-        extras["served"] = run_served(argparse.Namespace(jobs=100, rate=200.0, workers=8, hbm_budget_gb=96),
-                                      summary=True)
+        extras["served"] = run_served(argparse.Namespace(jobs=100, rate=200.0, low_rates=[80.0], workers=8,
+                                                         hbm_budget_gb=96), summary=True)
 
     if rank == 0:
         line = {

@@ -347,6 +347,23 @@ int gb_prove_instance(void *table, const uint64_t master_seed[2], int num_querie
  * host buffers must stay valid until gb_prover_wait returns for its ticket. */
 int gb_prover_create(void *table, const uint64_t master_seed[2], int num_queries, int workers, size_t hbm_budget,
                      void **handle);
+/* The continuous prover service (no reference counterpart): `workers` threads run each admitted
+ * job's steps before its openings (inputs, commits, sumcheck, partial evaluations, Ajtai) on their
+ * own streams, then hand its openings to open engines, one per size class of opening (n < 19,
+ * 19 <= n < 22, n >= 22), each a thread with a stream that keeps every opening of its class in
+ * flight and advances all of them one round per step: each round's work of all of them in one
+ * launch per kernel kind (and one per Merkle layer).  Openings join at their engine's next step
+ * once their job's prologue is done, and leave when their queries are gathered; the job is then
+ * complete and its budget share is freed.  A worker takes the next admitted job as soon as it has
+ * handed over the last one, so admission follows the HBM budget alone.  Proofs are identical to
+ * the per-call path's.  Same submit / wait / drain / destroy calls; table: log_rate 1. */
+int gb_prover_create_continuous(void *table, const uint64_t master_seed[2], int num_queries, int workers,
+                                size_t hbm_budget, void **handle);
+/* Jobs admitted and not yet complete (either service), -1 for a null handle. */
+int gb_prover_running(void *prover);
+/* Openings in the continuous service's open engines (waiting to join or in flight); 0 for the
+ * whole-job service. */
+size_t gb_prover_openings_in_flight(void *prover);
 int gb_prover_submit(void *prover, const gb_instance *inst, uint64_t *ticket); /* non-blocking */
 /* Blocks until the ticket's job is done; returns the job's return code (its message in
  * gb_last_error()); stats may be NULL.  Each ticket is waited for once. */

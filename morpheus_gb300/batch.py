@@ -205,15 +205,21 @@ def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30, c
 
 
 class ProverService:
-    """Continuous-batching prover: submit instances as they arrive; each runs as soon as a
-    worker is free and its estimated device footprint fits the HBM budget."""
+    """Prover service: submit instances or matmul jobs as they arrive; each is admitted as soon as
+    its estimated device footprint fits the HBM budget beside the jobs in flight.
+
+    continuous=False: a worker proves a job whole on its own stream (gb_prover_create).
+    continuous=True: workers run each job's steps before its openings, then its openings join the
+    service's open engines, which advance every opening in flight one round per step with one
+    launch per kernel kind for all of them (gb_prover_create_continuous)."""
 
     def __init__(self, table, master_seed, num_queries, workers=8, hbm_budget=64 << 30, coop_threshold=None,
-                 top_nodes=None):
+                 top_nodes=None, continuous=False):
         self.handle = ctypes.c_void_p()
         self.num_queries = num_queries
-        N.check(N.lib().gb_prover_create(table.handle, _seed(master_seed), num_queries, workers, hbm_budget,
-                                         ctypes.byref(self.handle)), "gb_prover_create")
+        fn = "gb_prover_create_continuous" if continuous else "gb_prover_create"
+        N.check(getattr(N.lib(), fn)(table.handle, _seed(master_seed), num_queries, workers, hbm_budget,
+                                     ctypes.byref(self.handle)), fn)
         if coop_threshold is not None:
             N.check(N.lib().gb_prover_set_coop_threshold(self.handle, coop_threshold), "gb_prover_set_coop_threshold")
         if top_nodes is not None:
@@ -237,6 +243,14 @@ class ProverService:
             N.check(N.lib().gb_prover_submit(self.handle, ctypes.byref(s), ctypes.byref(t)), "gb_prover_submit")
         self._live[t.value] = job  # keeps the host buffers alive until waited for
         return t.value
+
+    def running(self):
+        """Jobs admitted and not yet complete."""
+        return int(N.lib().gb_prover_running(self.handle))
+
+    def openings_in_flight(self):
+        """Openings in the continuous service's open engines (0 for the whole-job service)."""
+        return int(N.lib().gb_prover_openings_in_flight(self.handle))
 
     def wait(self, ticket):
         st = GbJobStats()

@@ -36,8 +36,12 @@
 #include "basefold.cuh"
 #include "common.cuh"
 #include "host_field.hpp"
+#include "open_engine.cuh"
 
 namespace gb {
+
+int matmul_prologue(void* table, void* ajtai_key, const u64 seed[2], int q, const gb_matmul_job* job,
+                    std::vector<OpenTask>* tasks, std::vector<void*>* coms);
 
 constexpr int INST_MAX_D = 8;
 constexpr int INST_LOG_RATE = 1;
@@ -59,15 +63,19 @@ static double ms_between(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
-// Prove one instance on the calling thread's stream.
-static int prove_instance(void* table, const u64 seed[2], int q, const gb_instance* in) {
+// Everything of one instance before its openings, on the calling thread's stream: the commits
+// and the product sumcheck.  On success the commitments (handles in *coms) and one OpenTask per
+// polynomial (its point, its "bf-open" transcript preamble, its place in the proof) are returned
+// and the stream is idle; the caller opens and then destroys the commitments.
+static int instance_prologue(void* table, const u64 seed[2], int q, const gb_instance* in,
+                             std::vector<OpenTask>* tasks, std::vector<void*>* coms) {
     using namespace host;
-    const int n = in->num_vars, d = in->degree;
-    if (!table || !in || n < 2 || n > 30 || d < 1 || d > INST_MAX_D || (!in->h_polys == !in->d_polys) ||
-        !in->h_proof || q < 0) {
+    if (!table || !in || in->num_vars < 2 || in->num_vars > 30 || in->degree < 1 || in->degree > INST_MAX_D ||
+        (!in->h_polys == !in->d_polys) || !in->h_proof || q < 0) {
         set_error_msg("gb_prove_instance: invalid argument");
         return GB_EINVAL;
     }
+    const int n = in->num_vars, d = in->degree;
     cudaStream_t s = stream();
     const size_t N = (size_t)1 << n;
     const u64* polys = in->d_polys;
@@ -103,16 +111,7 @@ static int prove_instance(void* table, const u64 seed[2], int q, const gb_instan
         for (int k = 0; k < 4 * d; k++) tr_append_u64(&t, "", roots[k]);
         rc = gb_sumcheck_prove_ext2(&t, n, d, polys, nullptr, msgs, chal, finals, final_eval);
     }
-    for (int j = 0; j < d && !rc; j++) {
-        gb_transcript t;
-        gb_transcript_new(&t, "bf-open");
-        tr_append_ext2(&t, "", E2{canon(seed[0]), canon(seed[1])});
-        tr_append_u64(&t, "", 8 * in->index + (u64)j);
-        rc = gb_basefold_open_ext2(com[j], table, chal, &t, q, opens + (size_t)j * plen);
-    }
-    for (int j = 0; j < d; j++)
-        if (com[j]) gb_basefold_commitment_destroy(com[j]);
-    if (owned) cudaFreeAsync(owned, s);
+    if (owned) cudaFreeAsync(owned, s);  // the commitments hold their own copies
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
@@ -120,7 +119,47 @@ static int prove_instance(void* table, const u64 seed[2], int q, const gb_instan
             rc = GB_ECUDA;
         }
     }
+    if (rc) {
+        for (int j = 0; j < d; j++)
+            if (com[j]) gb_basefold_commitment_destroy(com[j]);
+        return rc;
+    }
+    for (int j = 0; j < d; j++) {
+        OpenTask t;
+        t.com = (BfCommitment*)com[j];
+        t.point.assign(chal, chal + 2 * (size_t)n);
+        gb_transcript_new(&t.t, "bf-open");
+        tr_append_ext2(&t.t, "", E2{canon(seed[0]), canon(seed[1])});
+        tr_append_u64(&t.t, "", 8 * in->index + (u64)j);
+        t.proof = opens + (size_t)j * plen;
+        tasks->push_back(std::move(t));
+        coms->push_back(com[j]);
+    }
+    return GB_OK;
+}
+
+int open_tasks_inline(void* table, int q, std::vector<OpenTask>& tasks, std::vector<void*>& coms) {
+    int rc = GB_OK;
+    for (size_t k = 0; k < tasks.size() && !rc; k++)
+        rc = gb_basefold_open_ext2(coms[k], table, tasks[k].point.data(), &tasks[k].t, q, tasks[k].proof);
+    for (void* c : coms) gb_basefold_commitment_destroy(c);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(stream());
+        if (e != cudaSuccess) {
+            set_error("cudaStreamSynchronize", e);
+            rc = GB_ECUDA;
+        }
+    }
     return rc;
+}
+
+// Prove one instance on the calling thread's stream.
+static int prove_instance(void* table, const u64 seed[2], int q, const gb_instance* in) {
+    std::vector<OpenTask> tasks;
+    std::vector<void*> coms;
+    int rc = instance_prologue(table, seed, q, in, &tasks, &coms);
+    if (rc) return rc;
+    return open_tasks_inline(table, q, tasks, coms);
 }
 
 // ---------------------------------------------------------------------------
@@ -138,12 +177,36 @@ struct Job {
     std::string err;
 };
 
+// Two modes.  Whole-job: a worker runs a job from start to end on its stream.  Continuous: a
+// worker runs a job's prologue (inputs, commits, sumcheck, partial evaluations, Ajtai) on its
+// stream and hands the job's openings to the service's open engines, which batch them with the
+// openings of every other job in flight round by round (open_engine.cuh); the worker then takes
+// the next admitted job, and the job completes, and frees its share of the budget, when its
+// last opening leaves its engine.  There is one engine (thread and stream) per size class of
+// openings, so that a step of small openings does not wait for a large opening's round (a
+// 2^24-evaluation opening's first tree takes ~9 ms of permutations; a 2^16 one's whole opening
+// ~0.1 ms), and the classes' steps overlap on the device.
+constexpr int OPEN_CLASS_CUTS[] = {19, 22};  // classes n < 19, 19 <= n < 22, n >= 22
+constexpr int OPEN_CLASSES = 3;
+static int open_class(int n) {
+    int c = 0;
+    while (c < OPEN_CLASSES - 1 && n >= OPEN_CLASS_CUTS[c]) c++;
+    return c;
+}
+
 class Prover {
   public:
-    Prover(void* table, const u64 seed[2], int q, int workers, size_t budget, int device)
+    Prover(void* table, const u64 seed[2], int q, int workers, size_t budget, int device, bool continuous)
         : table_(table), q_(q), budget_(budget), device_(device) {
         seed_[0] = seed[0];
         seed_[1] = seed[1];
+        if (continuous)
+            for (int c = 0; c < OPEN_CLASSES && !start_rc_; c++) {
+                int rc = GB_OK;
+                OpenEngine* e = open_engine_create((const BfTable*)table, q, device, &rc);
+                if (!e) start_rc_ = rc ? rc : GB_EINVAL;
+                else engines_.push_back(e);
+            }
         for (int w = 0; w < workers; w++) threads_.emplace_back([this] { run(); });
     }
     ~Prover() {
@@ -153,6 +216,7 @@ class Prover {
         }
         cv_work_.notify_all();
         for (auto& t : threads_) t.join();
+        for (OpenEngine* e : engines_) open_engine_destroy(e);  // finishes the openings in flight
     }
     int start_error() {
         std::unique_lock<std::mutex> l(mu_);
@@ -212,6 +276,16 @@ class Prover {
         cv_done_.wait(l, [this] { return queue_.empty() && running_ == 0; });
         return GB_OK;
     }
+    size_t engine_in_flight() {
+        size_t k = 0;
+        for (OpenEngine* e : engines_) k += open_engine_in_flight(e);
+        return k;
+    }
+    // jobs admitted and not yet complete (in a prologue or with openings in an engine)
+    int running() {
+        std::lock_guard<std::mutex> l(mu_);
+        return running_;
+    }
 
   private:
     // the first queued job that fits the budget beside the running ones; a job larger than
@@ -251,21 +325,19 @@ class Prover {
             }
             gb_set_coop_threshold(coop_.load());
             gb_set_merkle_top_nodes(top_.load());
+            if (!engines_.empty() && !rc) {
+                std::vector<OpenTask> tasks;
+                std::vector<void*> coms;
+                int prc = j->kind == 0 ? instance_prologue(table_, seed_, q_, &j->inst, &tasks, &coms)
+                                       : matmul_prologue(table_, ajtai_key_, seed_, q_, &j->mm, &tasks, &coms);
+                if (!prc) hand_to_engines(j, tasks, coms);
+                else complete(j, prc, gb_last_error());
+                continue;
+            }
             int jrc = rc ? rc
                       : j->kind == 0 ? prove_instance(table_, seed_, q_, &j->inst)
                                      : gb_prove_matmul(table_, ajtai_key_, seed_, q_, &j->mm);
-            std::string err = jrc ? std::string(gb_last_error()) : std::string();
-            {
-                std::lock_guard<std::mutex> l(mu_);
-                j->finished = Clock::now();
-                j->rc = jrc;
-                j->err = err;
-                j->done = true;
-                in_use_ -= j->bytes;
-                running_--;
-            }
-            cv_done_.notify_all();
-            cv_work_.notify_all();  // freed budget may admit a waiting job
+            complete(j, jrc, jrc ? std::string(gb_last_error()) : std::string());
         }
         if (st) {
             cudaStreamSynchronize(st);
@@ -274,8 +346,52 @@ class Prover {
         }
     }
 
+    void complete(Job* j, int rc, const std::string& err) {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            j->finished = Clock::now();
+            j->rc = rc;
+            j->err = err;
+            j->done = true;
+            in_use_ -= j->bytes;
+            running_--;
+        }
+        cv_done_.notify_all();
+        cv_work_.notify_all();  // freed budget may admit a waiting job
+    }
+    // the job's openings into the engines of their size classes; the last one to finish
+    // completes the job (on an engine thread)
+    void hand_to_engines(Job* j, std::vector<OpenTask>& tasks, std::vector<void*>& coms) {
+        struct Pending {
+            std::mutex mu;
+            int left = 0, rc = GB_OK;
+            std::string err;
+        };
+        auto pend = std::make_shared<Pending>();
+        pend->left = (int)tasks.size();
+        for (size_t k = 0; k < tasks.size(); k++) {
+            void* com = coms[k];
+            OpenEngine* e = engines_[open_class(tasks[k].com->num_vars)];
+            tasks[k].done = [this, j, pend, com](int rc, const std::string& err) {
+                gb_basefold_commitment_destroy(com);
+                bool last;
+                {
+                    std::lock_guard<std::mutex> l(pend->mu);  // the engines are separate threads
+                    if (rc && !pend->rc) {
+                        pend->rc = rc;
+                        pend->err = err;
+                    }
+                    last = --pend->left == 0;
+                }
+                if (last) complete(j, pend->rc, pend->err);
+            };
+            open_engine_submit(e, std::move(tasks[k]));
+        }
+    }
+
     void* table_;
     void* ajtai_key_ = nullptr;
+    std::vector<OpenEngine*> engines_;  // continuous mode: one per size class
     std::atomic<size_t> coop_{gb_get_coop_threshold()};
     std::atomic<size_t> top_{gb_get_merkle_top_nodes()};
     u64 seed_[2];
@@ -310,23 +426,40 @@ int gb_prove_instance(void* table, const uint64_t master_seed[2], int num_querie
     return prove_instance(table, master_seed, num_queries, inst);
 }
 
-int gb_prover_create(void* table, const uint64_t master_seed[2], int num_queries, int workers, size_t hbm_budget,
-                     void** handle) {
-    if (!table || !master_seed || !handle || workers < 1 || workers > 256 || num_queries < 0) {
-        set_error_msg("gb_prover_create: invalid argument");
+static int prover_create(void* table, const uint64_t master_seed[2], int num_queries, int workers, size_t hbm_budget,
+                         bool continuous, void** handle) {
+    if (!table || !master_seed || !handle || workers < 1 || workers > 256 || num_queries < 0 ||
+        (continuous && ((const BfTable*)table)->log_rate != 1)) {
+        set_error_msg("gb_prover_create: invalid argument (the continuous service needs a log_rate 1 table)");
         return GB_EINVAL;
     }
     int dev = 0;
     GB_CUDA_TRY(cudaGetDevice(&dev));
-    Prover* p = new Prover(table, master_seed, num_queries, workers, hbm_budget, dev);
+    Prover* p = new Prover(table, master_seed, num_queries, workers, hbm_budget, dev, continuous);
     int rc = p->start_error();
     if (rc) {
         delete p;
-        set_error_msg("gb_prover_create: a worker could not create its stream");
+        set_error_msg("gb_prover_create: a worker or an open engine could not start");
         return rc;
     }
     *handle = p;
     return GB_OK;
+}
+
+int gb_prover_create(void* table, const uint64_t master_seed[2], int num_queries, int workers, size_t hbm_budget,
+                     void** handle) {
+    return prover_create(table, master_seed, num_queries, workers, hbm_budget, false, handle);
+}
+
+int gb_prover_create_continuous(void* table, const uint64_t master_seed[2], int num_queries, int workers,
+                                size_t hbm_budget, void** handle) {
+    return prover_create(table, master_seed, num_queries, workers, hbm_budget, true, handle);
+}
+
+int gb_prover_running(void* prover) { return prover ? static_cast<Prover*>(prover)->running() : -1; }
+
+size_t gb_prover_openings_in_flight(void* prover) {
+    return prover ? static_cast<Prover*>(prover)->engine_in_flight() : 0;
 }
 
 int gb_prover_submit(void* prover, const gb_instance* inst, uint64_t* ticket) {

@@ -19,6 +19,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -30,6 +31,7 @@
 #include "bf_device.cuh"
 #include "host_field.hpp"
 #include "merkle.cuh"
+#include "open_engine.cuh"
 #include "reduce.cuh"
 #include "sc_device.cuh"
 
@@ -1580,6 +1582,608 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
     }
     return GB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Continuous open engine (open_engine.cuh): the rounds of LsRunner::open, with every polynomial
+// at its own round.  Step = one round for all polynomials in flight: the eq/bh fold + oracle
+// partials and the codeword fold + leaf hash go out as one launch per input kind (round 0 reads
+// base-field inputs, later rounds Ext2), the Merkle layers as one launch per layer over every
+// tree, then roots and final folds; one host round trip advances each transcript.  Joining
+// polynomials get their eq tables and round-0 oracles at the step boundary; finished ones their
+// queries, in one gather launch.
+// ---------------------------------------------------------------------------
+struct EngPoly : LsPoly {
+    int rd = 0;
+    u64* ws = nullptr;
+    OpenTask task;
+};
+
+class OpenEngine {
+  public:
+    OpenEngine(const BfTable* tab, int q, int device) : tab_(tab), q_(q), device_(device) {
+        th_ = std::thread([this] { run(); });
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [this] { return started_; });
+    }
+    ~OpenEngine() {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        th_.join();
+    }
+    int start_rc() const { return start_rc_; }
+    void submit(OpenTask&& t) {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            intake_.push_back(std::move(t));
+            waiting_++;
+        }
+        cv_.notify_all();
+    }
+    size_t in_flight() {
+        std::lock_guard<std::mutex> l(mu_);
+        return waiting_;
+    }
+
+  private:
+    using PolyList = std::vector<EngPoly*>;
+
+    void run() {
+        cudaStream_t st = nullptr;
+        cudaError_t e = cudaSetDevice(device_);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            start_rc_ = e == cudaSuccess ? GB_OK : GB_ECUDA;
+            started_ = true;
+        }
+        cv_.notify_all();
+        if (e != cudaSuccess) return;
+        gb_set_stream(st);
+        for (;;) {
+            std::vector<OpenTask> in;
+            {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_.wait(l, [&] { return stop_ || !intake_.empty() || !active_.empty(); });
+                if (intake_.empty() && active_.empty()) break;  // stop, with nothing left
+                in.swap(intake_);
+            }
+            int rc = GB_OK;
+            if (!in.empty()) rc = join(in);
+            if (!rc && !active_.empty()) rc = step();
+            if (!rc) rc = finish();
+            if (rc) fail_all(rc, gb_last_error());
+        }
+        cudaStreamSynchronize(st);
+        release_buffers();
+        gb_set_stream(nullptr);
+        cudaStreamDestroy(st);
+    }
+
+    // carve one polynomial's workspace (the layout of LsRunner::open)
+    static void carve(EngPoly& p) {
+        u64* cur = p.ws;
+        p.d_point = cur;
+        cur += align2(2 * (size_t)p.n);
+        p.eq = cur;
+        cur += 2 * p.N;
+        p.bufs_eq[0] = cur;
+        cur += p.N;
+        p.bufs_eq[1] = cur;
+        cur += p.N;
+        p.bufs_bh[0] = cur;
+        cur += p.N;
+        p.bufs_bh[1] = cur;
+        cur += p.N;
+        p.fcw.assign(p.n, nullptr);
+        p.ftree.assign(p.n - 1, nullptr);
+        for (int r = 0; r < p.n; r++) {
+            p.fcw[r] = cur;
+            cur += align2(2 * (p.L >> (r + 1)));
+        }
+        for (int r = 0; r + 1 < p.n; r++) {
+            p.ftree[r] = cur;
+            cur += 4 * (2 * ((p.L >> (r + 1)) / 2) - 1) + 2;
+        }
+    }
+
+    // Per-step buffers sized for the polynomials in flight (called with the stream idle).
+    int reserve(size_t polys, int maxn, size_t partial_blocks) {
+        cudaStream_t s = stream();
+        const size_t segs = polys * (size_t)(maxn + 8);
+        if (segs > seg_cap_) {
+            if (d_segs_) cudaFreeAsync(d_segs_, s);
+            if (h_segs_) cudaFreeHost(h_segs_);
+            d_segs_ = nullptr;
+            h_segs_ = nullptr;
+            seg_cap_ = std::max(segs, 2 * seg_cap_);
+            GB_CUDA_TRY(cudaMallocAsync(&d_segs_, seg_cap_ * sizeof(LsSeg), s));
+            GB_CUDA_TRY(cudaMallocHost(&h_segs_, seg_cap_ * sizeof(LsSeg)));
+        }
+        if (polys > rec_cap_) {
+            if (h_recs_) cudaFreeHost(h_recs_);
+            h_recs_ = nullptr;
+            rec_cap_ = std::max(polys, 2 * rec_cap_);
+            GB_CUDA_TRY(cudaMallocHost(&h_recs_, rec_cap_ * LS_REC * 8));
+            void* d = nullptr;
+            GB_CUDA_TRY(cudaHostGetDevicePointer(&d, h_recs_, 0));
+            d_recs_ = (u64*)d;
+        }
+        if (partial_blocks > part_cap_) {
+            if (d_partials_) cudaFreeAsync(d_partials_, s);
+            d_partials_ = nullptr;
+            part_cap_ = std::max(partial_blocks, 2 * part_cap_);
+            GB_CUDA_TRY(cudaMallocAsync(&d_partials_, part_cap_ * 6 * 8, s));
+        }
+        seg_used_ = 0;
+        return GB_OK;
+    }
+    void release_buffers() {
+        cudaStream_t s = stream();
+        if (d_segs_) cudaFreeAsync(d_segs_, s);
+        if (d_partials_) cudaFreeAsync(d_partials_, s);
+        cudaStreamSynchronize(s);
+        if (h_segs_) cudaFreeHost(h_segs_);
+        if (h_recs_) cudaFreeHost(h_recs_);
+        d_segs_ = nullptr;
+        h_segs_ = nullptr;
+        h_recs_ = nullptr;
+        d_partials_ = nullptr;
+        seg_cap_ = rec_cap_ = part_cap_ = 0;
+    }
+    // descriptor entries for one launch (valid until the next synchronisation)
+    LsSeg* segs(size_t count) {
+        if (seg_used_ + count > seg_cap_) return nullptr;
+        LsSeg* p = h_segs_ + seg_used_;
+        seg_used_ += count;
+        return p;
+    }
+    const LsSeg* upload(const LsSeg* hs, size_t count) {
+        if (!hs) return nullptr;
+        const size_t off = (size_t)(hs - h_segs_);
+        if (cudaMemcpyAsync(d_segs_ + off, hs, count * sizeof(LsSeg), cudaMemcpyHostToDevice, stream()) != cudaSuccess)
+            return nullptr;
+        return d_segs_ + off;
+    }
+    static u64 blocks_red(u64 items) {
+        const u64 per = (u64)LS_RED_THREADS * LS_ITEMS;
+        return items ? (items + per - 1) / per : 1;
+    }
+    static host::E2 put_oracle(LsPoly& p, int r, const u64* rec) {
+        using namespace host;
+        E2 c0{rec[0], rec[1]}, s1{rec[2], rec[3]}, c2{rec[4], rec[5]};
+        E2 c1 = e2sub(e2sub(s1, c0), c2);
+        u64* o = p.proof + 2 + (size_t)r * 6;
+        o[0] = c0.c0;
+        o[1] = c0.c1;
+        o[2] = c1.c0;
+        o[3] = c1.c1;
+        o[4] = c2.c0;
+        o[5] = c2.c1;
+        tr_append_ext2(&p.t, "", c0);
+        tr_append_ext2(&p.t, "", c1);
+        tr_append_ext2(&p.t, "", c2);
+        return s1;
+    }
+    int sync() {
+        GB_CUDA_TRY(cudaStreamSynchronize(stream()));
+        seg_used_ = 0;
+        return GB_OK;
+    }
+    size_t partial_need() const {
+        size_t b = 0;
+        for (auto& p : active_) b += blocks_red(p->N / 2) + 1;
+        return b;
+    }
+    int max_vars() const {
+        int m = 1;
+        for (auto& p : active_) m = std::max(m, p->n);
+        return m;
+    }
+
+    // new openings: workspaces, transcript preambles, eq tables and round-0 oracles
+    int join(std::vector<OpenTask>& in) {
+        using namespace host;
+        cudaStream_t s = stream();
+        PolyList P;
+        // ownership moves to active_ first, so that a failure below reaches every callback
+        for (auto& t : in) {
+            auto p = std::make_unique<EngPoly>();
+            p->task = std::move(t);
+            p->n = p->task.com->num_vars;
+            p->N = (size_t)1 << p->n;
+            p->L = p->N << 1;
+            p->com = p->task.com;
+            p->point = p->task.point.data();
+            p->t = p->task.t;
+            p->proof = p->task.proof;
+            P.push_back(p.get());
+            active_.push_back(std::move(p));
+        }
+        for (auto* p : P) {
+            if (p->n < 2 || p->task.com->log_rate != 1 || p->task.point.size() != 2 * (size_t)p->n ||
+                tab_->num_rounds < p->n || tab_->num_vars < p->n) {
+                set_error_msg("open engine: invalid opening (n >= 2, log_rate 1, 2n point words, table covering n)");
+                return GB_EINVAL;
+            }
+            GB_CUDA_TRY(cudaMallocAsync(&p->ws, ls_poly_words(p->n, 1) * 8, s));
+            carve(*p);
+        }
+        LS_RC(reserve(active_.size(), max_vars(), partial_need()));
+        const int np = (int)P.size();
+        ls_parallel(P.size(), [&](size_t k) {
+            EngPoly& p = *P[k];
+            for (int w = 0; w < 4; w++) tr_append_u64(&p.t, "", p.com->root[w]);
+            for (int i = 0; i < p.n; i++) tr_append_ext2(&p.t, "", E2{canon(p.point[2 * i]), canon(p.point[2 * i + 1])});
+        });
+        // every joining point in one copy, then every eq table in two launches
+        std::vector<EqSeg> eqsegs(np);
+        size_t scratch = 0;
+        for (auto* p : P) scratch += 2 * (((size_t)1 << (p->n / 2)) + ((size_t)1 << (p->n - p->n / 2)));
+        std::vector<u64> pts;
+        for (auto* p : P)
+            for (int i = 0; i < 2 * p->n; i++) pts.push_back(canon(p->point[i]));
+        u64 *eqs = nullptr, *d_pts = nullptr;
+        EqSeg* d_eqsegs = nullptr;
+        GB_CUDA_TRY(cudaMallocAsync(&d_pts, pts.size() * 8, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(d_pts, pts.data(), pts.size() * 8, cudaMemcpyHostToDevice, s));
+        GB_CUDA_TRY(cudaMallocAsync(&eqs, scratch * 8, s));
+        GB_CUDA_TRY(cudaMallocAsync(&d_eqsegs, (size_t)np * sizeof(EqSeg), s));
+        {
+            u64 nb = 0;
+            u64* cur = eqs;
+            size_t po = 0;
+            for (int k = 0; k < np; k++) {
+                EngPoly& p = *P[k];
+                EqSeg& g = eqsegs[k];
+                g.r = d_pts + po;
+                po += 2 * (size_t)p.n;
+                g.n = (u64)p.n;
+                g.k = (u64)(p.n / 2);
+                g.lo = cur;
+                cur += 2 * ((size_t)1 << g.k);
+                g.hi = cur;
+                cur += 2 * ((size_t)1 << (g.n - g.k));
+                g.out = p.eq;
+                g.block0 = nb;
+                nb += ((u64)1 << p.n) / 256 + 1;
+            }
+            GB_CUDA_TRY(cudaMemcpyAsync(d_eqsegs, eqsegs.data(), (size_t)np * sizeof(EqSeg), cudaMemcpyHostToDevice, s));
+            ls_eq_halves_kernel<<<(unsigned)(2 * np), 256, 0, s>>>(d_eqsegs, np);
+            GB_LAUNCH_CHECK("ls_eq_halves_kernel");
+            ls_eq_expand_kernel<<<(unsigned)nb, 256, 0, s>>>(d_eqsegs, np);
+            GB_LAUNCH_CHECK("ls_eq_expand_kernel");
+        }
+        // round-0 oracles
+        {
+            LsSeg* hs = segs(np);
+            if (!hs) return GB_EINVAL;
+            u64 nb = 0;
+            for (int k = 0; k < np; k++) {
+                EngPoly& p = *P[k];
+                hs[k] = LsSeg{p.com->d_evals, p.eq, nullptr, nullptr, 0, 0, p.N / 2, nb};
+                nb += blocks_red(p.N / 2);
+            }
+            const LsSeg* ds = upload(hs, np);
+            if (!ds) return GB_ECUDA;
+            ls_round0_kernel<<<(unsigned)nb, LS_RED_THREADS, 0, s>>>(ds, np, d_partials_);
+            GB_LAUNCH_CHECK("ls_round0_kernel");
+            ls_reduce_kernel<<<(unsigned)((np * 32 + 255) / 256), 256, 0, s>>>(ds, np, d_partials_, d_recs_);
+            GB_LAUNCH_CHECK("ls_reduce_kernel");
+        }
+        cudaFreeAsync(eqs, s);
+        cudaFreeAsync(d_eqsegs, s);
+        cudaFreeAsync(d_pts, s);
+        LS_RC(sync());
+        ls_parallel(P.size(), [&](size_t k) {
+            EngPoly& p = *P[k];
+            const u64* rec = h_recs_ + k * LS_REC;
+            E2 ev = e2add(E2{rec[0], rec[1]}, put_oracle(p, 0, rec));
+            p.proof[0] = ev.c0;
+            p.proof[1] = ev.c1;
+            p.eq_cur = p.eq;
+            p.bh_cur = p.com->d_evals;
+            p.pp = 0;
+            p.sc = p.N;
+            p.rd = 0;
+        });
+        return GB_OK;
+    }
+
+    // one round of every opening in flight
+    int step() {
+        using namespace host;
+        cudaStream_t s = stream();
+        LS_RC(reserve(active_.size(), max_vars(), partial_need()));
+        const size_t na = active_.size();
+        std::vector<E2> ch(na);
+        ls_parallel(na, [&](size_t k) { ch[k] = tr_challenge_ext2(&active_[k]->t, ""); });
+        // `mid`: openings with a tree this round, round-0 ones first (they read base-field
+        // inputs); `last`: the final fold.  Every opening has n >= 2.
+        std::vector<size_t> mid, last;
+        for (size_t k = 0; k < na; k++)
+            if (active_[k]->rd == 0) mid.push_back(k);
+        const size_t mid0 = mid.size();
+        for (size_t k = 0; k < na; k++) {
+            const EngPoly& p = *active_[k];
+            if (p.rd >= 1 && p.rd < p.n - 1) mid.push_back(k);
+            else if (p.rd >= 1 && p.rd == p.n - 1) last.push_back(k);
+        }
+        if (!mid.empty()) {
+            // eq/bh folds + next oracles: record m of `mid` in mid order
+            u64 part_off = 0;
+            for (int g = 0; g < 2; g++) {
+                const size_t b = g ? mid0 : 0, e = g ? mid.size() : mid0;
+                if (b == e) continue;
+                LsSeg* hs = segs(e - b);
+                if (!hs) return GB_EINVAL;
+                u64 nb = 0;
+                for (size_t m = b; m < e; m++) {
+                    EngPoly& p = *active_[mid[m]];
+                    const size_t quarter = p.sc / 4;
+                    hs[m - b] = LsSeg{p.eq_cur, p.bh_cur, p.bufs_eq[p.pp], p.bufs_bh[p.pp], ch[mid[m]].c0,
+                                      ch[mid[m]].c1, quarter, nb};
+                    nb += blocks_red(quarter);
+                }
+                const LsSeg* ds = upload(hs, e - b);
+                if (!ds) return GB_ECUDA;
+                u64* part = d_partials_ + part_off * 6;
+                if (g == 0) ls_open_round_kernel<true><<<(unsigned)nb, LS_RED_THREADS, 0, s>>>(ds, (int)(e - b), part);
+                else ls_open_round_kernel<false><<<(unsigned)nb, LS_RED_THREADS, 0, s>>>(ds, (int)(e - b), part);
+                GB_LAUNCH_CHECK("ls_open_round_kernel");
+                ls_reduce_kernel<<<(unsigned)(((e - b) * 32 + 255) / 256), 256, 0, s>>>(ds, (int)(e - b), part,
+                                                                                        d_recs_ + b * LS_REC);
+                GB_LAUNCH_CHECK("ls_reduce_kernel");
+                part_off += nb;
+            }
+            for (size_t k : mid) {
+                EngPoly& p = *active_[k];
+                p.eq_cur = p.bufs_eq[p.pp];
+                p.bh_cur = p.bufs_bh[p.pp];
+                p.pp ^= 1;
+                p.sc /= 2;
+            }
+            // codeword folds + leaf hashes
+            for (int g = 0; g < 2; g++) {
+                const size_t b = g ? mid0 : 0, e = g ? mid.size() : mid0;
+                if (b == e) continue;
+                LsSeg* hs = segs(e - b);
+                if (!hs) return GB_EINVAL;
+                for (size_t m = b; m < e; m++) {
+                    EngPoly& p = *active_[mid[m]];
+                    const int rd = p.rd;
+                    const size_t leaves = (p.L >> (rd + 1)) / 2;
+                    const u64* cw_in = rd == 0 ? p.com->d_codeword : p.fcw[rd - 1];
+                    hs[m - b] = LsSeg{cw_in, tab_->d_entries + 2 * tab_->level_offsets[rd], p.fcw[rd], p.ftree[rd],
+                                      ch[mid[m]].c0, ch[mid[m]].c1, leaves, 0};
+                }
+                u64 nb = 0;
+                const int cnt = (int)(e - b);
+                const int th = ls_p2_assign(hs, cnt, nb);
+                const LsSeg* ds = upload(hs, e - b);
+                if (!ds) return GB_ECUDA;
+                if (th == P2_WIDE) {
+                    if (g == 0) ls_fold_hash_kernel<true, P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
+                    else ls_fold_hash_kernel<false, P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
+                } else {
+                    if (g == 0) ls_fold_hash_kernel<true, P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
+                    else ls_fold_hash_kernel<false, P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
+                }
+                GB_LAUNCH_CHECK("ls_fold_hash_kernel");
+            }
+            // Merkle layers of every tree, one launch per layer
+            for (int lvl = 0;; lvl++) {
+                LsSeg* hs = segs(mid.size());
+                if (!hs) return GB_EINVAL;
+                int cnt = 0;
+                for (size_t k : mid) {
+                    EngPoly& p = *active_[k];
+                    const size_t leaves = (p.L >> (p.rd + 1)) / 2;
+                    const size_t nodes = leaves >> lvl;
+                    if (nodes < 2) continue;
+                    size_t off = 0;
+                    for (int l = 0; l < lvl; l++) off += leaves >> l;
+                    u64* layer = p.ftree[p.rd] + 4 * off;
+                    hs[cnt++] = LsSeg{layer, nullptr, layer + 4 * nodes, nullptr, 0, 0, nodes / 2, 0};
+                }
+                if (!cnt) {
+                    seg_used_ -= mid.size();
+                    break;
+                }
+                u64 nb = 0;
+                const int th = ls_p2_assign(hs, cnt, nb);
+                const LsSeg* ds = upload(hs, cnt);
+                if (!ds) return GB_ECUDA;
+                if (th == P2_WIDE) ls_merkle_level_kernel<P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
+                else ls_merkle_level_kernel<P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
+                GB_LAUNCH_CHECK("ls_merkle_level_kernel");
+            }
+            // roots into records m of `mid`
+            LsSeg* hs = segs(mid.size());
+            if (!hs) return GB_EINVAL;
+            for (size_t m = 0; m < mid.size(); m++) {
+                EngPoly& p = *active_[mid[m]];
+                const size_t leaves = (p.L >> (p.rd + 1)) / 2;
+                hs[m] = LsSeg{p.ftree[p.rd] + 4 * (2 * leaves - 2), nullptr, nullptr, nullptr, 0, 0, 0, 0};
+            }
+            const LsSeg* ds = upload(hs, mid.size());
+            if (!ds) return GB_ECUDA;
+            ls_root_kernel<<<(unsigned)((mid.size() + 127) / 128), 128, 0, s>>>(ds, (int)mid.size(), d_recs_);
+            GB_LAUNCH_CHECK("ls_root_kernel");
+        }
+        if (!last.empty()) {
+            // final folds into records |mid| + m
+            LsSeg* hs = segs(last.size());
+            if (!hs) return GB_EINVAL;
+            for (size_t m = 0; m < last.size(); m++) {
+                EngPoly& p = *active_[last[m]];
+                const int rd = p.rd;
+                hs[m] = LsSeg{p.fcw[rd - 1], tab_->d_entries + 2 * tab_->level_offsets[rd], p.fcw[rd], nullptr,
+                              ch[last[m]].c0, ch[last[m]].c1, p.L >> (rd + 1), 0};
+            }
+            const LsSeg* ds = upload(hs, last.size());
+            if (!ds) return GB_ECUDA;
+            ls_fold_final_kernel<<<(unsigned)last.size(), 32, 0, s>>>(ds, (int)last.size(), d_recs_ + mid.size() * LS_REC);
+            GB_LAUNCH_CHECK("ls_fold_final_kernel");
+        }
+        LS_RC(sync());
+        ls_parallel(mid.size(), [&](size_t m) {
+            EngPoly& p = *active_[mid[m]];
+            const u64* rec = h_recs_ + m * LS_REC;
+            put_oracle(p, p.rd + 1, rec);
+            u64* root = p.proof + 2 + (size_t)p.n * 6 + (size_t)p.rd * 4;
+            for (int k = 0; k < 4; k++) {
+                root[k] = rec[8 + k];
+                tr_append_u64(&p.t, "", root[k]);
+            }
+        });
+        for (size_t m = 0; m < last.size(); m++) {
+            EngPoly& p = *active_[last[m]];
+            u64* fin = p.proof + 2 + (size_t)p.n * 6 + (size_t)(p.n - 1) * 4;
+            for (int k = 0; k < 4; k++) fin[k] = h_recs_[(mid.size() + m) * LS_REC + 12 + k];
+        }
+        for (auto& p : active_) p->rd++;
+        return GB_OK;
+    }
+
+    // queries of the openings that finished their rounds, then their callbacks
+    int finish() {
+        using namespace host;
+        cudaStream_t s = stream();
+        PolyList D;
+        for (auto& p : active_)
+            if (p->rd >= p->n) D.push_back(p.get());
+        if (D.empty()) return GB_OK;
+        const int np = (int)D.size(), lr = 1;
+        if (q_ > 0) {
+            std::vector<QueryJob> jobs(np);
+            std::vector<u64> idx((size_t)np * q_), per_q(np);
+            std::vector<const u64*> ptrs;
+            std::vector<size_t> out_off(np), ptr_off(np);
+            size_t out_words = 0;
+            ls_parallel(D.size(), [&](size_t k) {
+                EngPoly& p = *D[k];
+                for (int j = 0; j < q_; j++) idx[k * q_ + j] = tr_challenge(&p.t, "") % (u64)(p.L / 2);
+            });
+            for (int k = 0; k < np; k++) {
+                EngPoly& p = *D[k];
+                size_t pw = 0;
+                for (int r = 0; r < p.n; r++) pw += (size_t)(p.n + lr - 1 - r);
+                per_q[k] = 1 + (size_t)p.n * 4 + pw * 4;
+                out_off[k] = out_words;
+                out_words += per_q[k] * q_;
+                ptr_off[k] = ptrs.size();
+                for (int r = 0; r + 1 < p.n; r++) ptrs.push_back(p.fcw[r]);
+                for (int r = 0; r + 1 < p.n; r++) ptrs.push_back(p.ftree[r]);
+            }
+            u64 *d_idx = nullptr, *d_perq = nullptr, *d_out = nullptr;
+            const u64** d_ptrs = nullptr;
+            QueryJob* d_jobs = nullptr;
+            u64** d_outs = nullptr;
+            GB_CUDA_TRY(cudaMallocAsync(&d_idx, idx.size() * 8, s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_perq, per_q.size() * 8, s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_out, std::max<size_t>(out_words, 1) * 8, s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_ptrs, std::max<size_t>(ptrs.size(), 1) * sizeof(u64*), s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_jobs, (size_t)np * sizeof(QueryJob), s));
+            GB_CUDA_TRY(cudaMallocAsync(&d_outs, (size_t)np * sizeof(u64*), s));
+            std::vector<u64*> outs(np);
+            for (int k = 0; k < np; k++) {
+                EngPoly& p = *D[k];
+                const u64* const* base = d_ptrs + ptr_off[k];
+                jobs[k] = QueryJob{p.com->d_codeword, p.com->d_tree, base, base + (p.n - 1), p.n, lr, false};
+                outs[k] = d_out + out_off[k];
+            }
+            GB_CUDA_TRY(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * 8, cudaMemcpyHostToDevice, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(d_perq, per_q.data(), per_q.size() * 8, cudaMemcpyHostToDevice, s));
+            if (!ptrs.empty())
+                GB_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), ptrs.size() * sizeof(u64*), cudaMemcpyHostToDevice, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(QueryJob), cudaMemcpyHostToDevice, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(d_outs, outs.data(), outs.size() * sizeof(u64*), cudaMemcpyHostToDevice, s));
+            ls_query_kernel<<<dim3((unsigned)q_, (unsigned)np), 128, 0, s>>>(d_jobs, d_idx, q_, d_outs, d_perq);
+            GB_LAUNCH_CHECK("ls_query_kernel");
+            std::vector<u64> host_out(out_words);
+            GB_CUDA_TRY(cudaMemcpyAsync(host_out.data(), d_out, out_words * 8, cudaMemcpyDeviceToHost, s));
+            for (void* x : {(void*)d_idx, (void*)d_perq, (void*)d_out, (void*)d_ptrs, (void*)d_jobs, (void*)d_outs})
+                cudaFreeAsync(x, s);
+            LS_RC(sync());
+            for (int k = 0; k < np; k++) {
+                EngPoly& p = *D[k];
+                u64* dst = p.proof + 2 + (size_t)p.n * 6 + (size_t)(p.n - 1) * 4 + ((size_t)2 << lr);
+                std::memcpy(dst, host_out.data() + out_off[k], per_q[k] * q_ * 8);
+            }
+        }
+        for (auto* p : D) {
+            cudaFreeAsync(p->ws, s);
+            p->ws = nullptr;
+        }
+        LS_RC(sync());
+        // callbacks, then the finished polynomials leave the set
+        std::vector<std::unique_ptr<EngPoly>> keep, gone;
+        for (auto& p : active_) (p->rd >= p->n ? gone : keep).push_back(std::move(p));
+        active_.swap(keep);
+        for (auto& p : gone) {
+            if (p->task.done) p->task.done(GB_OK, std::string());
+            std::lock_guard<std::mutex> l(mu_);
+            waiting_--;
+        }
+        return GB_OK;
+    }
+
+    // a failed step: every opening in flight ends with the error
+    void fail_all(int rc, const std::string& err) {
+        cudaStream_t s = stream();
+        cudaStreamSynchronize(s);
+        std::vector<std::unique_ptr<EngPoly>> gone;
+        gone.swap(active_);
+        for (auto& p : gone) {
+            if (p->ws) cudaFreeAsync(p->ws, s);
+            if (p->task.done) p->task.done(rc, err);
+            std::lock_guard<std::mutex> l(mu_);
+            waiting_--;
+        }
+        cudaStreamSynchronize(s);
+        seg_used_ = 0;
+    }
+
+    const BfTable* tab_;
+    int q_, device_;
+    std::thread th_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::vector<OpenTask> intake_;
+    std::vector<std::unique_ptr<EngPoly>> active_;  // engine thread only
+    size_t waiting_ = 0;
+    bool stop_ = false, started_ = false;
+    int start_rc_ = GB_OK;
+    LsSeg* d_segs_ = nullptr;
+    LsSeg* h_segs_ = nullptr;
+    u64* d_recs_ = nullptr;
+    u64* h_recs_ = nullptr;
+    u64* d_partials_ = nullptr;
+    size_t seg_cap_ = 0, rec_cap_ = 0, part_cap_ = 0, seg_used_ = 0;
+};
+
+OpenEngine* open_engine_create(const BfTable* tab, int q, int device, int* rc) {
+    if (!tab || q < 0 || tab->log_rate != 1) {
+        set_error_msg("open engine: invalid table (log_rate must be 1) or query count");
+        if (rc) *rc = GB_EINVAL;
+        return nullptr;
+    }
+    auto* e = new OpenEngine(tab, q, device);
+    if (e->start_rc()) {
+        if (rc) *rc = e->start_rc();
+        set_error_msg("open engine: could not set the device or create its stream");
+        delete e;
+        return nullptr;
+    }
+    if (rc) *rc = GB_OK;
+    return e;
+}
+void open_engine_submit(OpenEngine* e, OpenTask&& task) { e->submit(std::move(task)); }
+size_t open_engine_in_flight(OpenEngine* e) { return e->in_flight(); }
+void open_engine_destroy(OpenEngine* e) { delete e; }
 
 }  // namespace gb
 

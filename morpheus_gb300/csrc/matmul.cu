@@ -20,6 +20,7 @@
 #include "basefold.cuh"
 #include "common.cuh"
 #include "host_field.hpp"
+#include "open_engine.cuh"
 
 namespace gb {
 
@@ -108,7 +109,11 @@ size_t matmul_hbm_bytes(int m, int n, int k) {
     return (a + b) * 130 + (a > b ? a : b) * 144 + ((size_t)8 << 20);
 }
 
-int prove_matmul(void* table, void* ajtai_key, const u64 seed[2], int q, const gb_matmul_job* job) {
+// Steps 1-4 and the Ajtai commitment of one job, on the calling thread's stream; on success the
+// stream is idle and the two openings (A at (r_k, r_i), B at (r_j, r_k)) are returned as tasks with
+// their commitments, for the caller to open and then destroy.
+int matmul_prologue(void* table, void* ajtai_key, const u64 seed[2], int q, const gb_matmul_job* job,
+                    std::vector<OpenTask>* tasks, std::vector<void*>* coms) {
     using namespace host;
     const int M = job->m, N = job->n, K = job->k;
     const int lm = log2_exact(M), ln = log2_exact(N), lk = log2_exact(K);
@@ -175,8 +180,6 @@ int prove_matmul(void* table, void* ajtai_key, const u64 seed[2], int q, const g
     void* comA = nullptr;
     void* comB = nullptr;
     auto finish = [&](int r) {
-        if (comA) gb_basefold_commitment_destroy(comA);
-        if (comB) gb_basefold_commitment_destroy(comB);
         cleanup();
         if (!r) {
             cudaError_t e = cudaStreamSynchronize(s);
@@ -184,6 +187,10 @@ int prove_matmul(void* table, void* ajtai_key, const u64 seed[2], int q, const g
                 set_error("cudaStreamSynchronize", e);
                 r = GB_ECUDA;
             }
+        }
+        if (r) {
+            if (comA) gb_basefold_commitment_destroy(comA);
+            if (comB) gb_basefold_commitment_destroy(comB);
         }
         return r;
     };
@@ -266,17 +273,32 @@ int prove_matmul(void* table, void* ajtai_key, const u64 seed[2], int q, const g
         ptB[2 * v] = pt[2 * (lm + v)];
         ptB[2 * v + 1] = pt[2 * (lm + v) + 1];
     }
-    for (int which = 0; which < 2; which++) {
-        gb_transcript to;
-        gb_transcript_new(&to, "bf-open");
-        tr_append_ext2(&to, "", E2{canon(seed[0]), canon(seed[1])});
-        tr_append_u64(&to, "", 8 * job->index + (u64)which);
-        MM_TRY(gb_basefold_open_ext2(which ? comB : comA, table, which ? ptB.data() : ptA.data(), &to, q,
-                                     which ? openB : openA));
+    {
+        int r = finish(GB_OK);
+        if (r) return r;
     }
-    return finish(GB_OK);
+    for (int which = 0; which < 2; which++) {
+        OpenTask t;
+        t.com = (BfCommitment*)(which ? comB : comA);
+        t.point = which ? ptB : ptA;
+        gb_transcript_new(&t.t, "bf-open");
+        tr_append_ext2(&t.t, "", E2{canon(seed[0]), canon(seed[1])});
+        tr_append_u64(&t.t, "", 8 * job->index + (u64)which);
+        t.proof = which ? openB : openA;
+        tasks->push_back(std::move(t));
+        coms->push_back(which ? comB : comA);
+    }
+    return GB_OK;
 #undef MM_TRY
 #undef MM_CUDA
+}
+
+int prove_matmul(void* table, void* ajtai_key, const u64 seed[2], int q, const gb_matmul_job* job) {
+    std::vector<OpenTask> tasks;
+    std::vector<void*> coms;
+    int rc = matmul_prologue(table, ajtai_key, seed, q, job, &tasks, &coms);
+    if (rc) return rc;
+    return open_tasks_inline(table, q, tasks, coms);
 }
 
 }  // namespace gb

@@ -143,3 +143,80 @@ def test_matmul_job_rejects_bad_shapes(env):
     job = make(64, 4, 64, 0, 0)  # m k = 2^12 < 2^16: no 2^16-entry witness
     with pytest.raises(N.NativeError, match="-2"):
         batch.prove_matmul(gt, key, SEED, job)
+
+
+@pytest.mark.parametrize("budget", [1, 8 << 30])
+def test_continuous_service_mix_equals_alone(env, budget):
+    """The continuous service (prologues on the workers, every opening in the open engines) gives
+    each matmul job and each instance the proof it gives alone; a 1-byte budget admits one job
+    at a time, a large one lets their openings share the engines' steps."""
+    from morpheus_gb300 import batch
+    gt, key, _ = env
+    jobs = [make(256, 16, 256, 300 + i, 70 + i) for i in range(2)] + [make(512, 8, 128, 400 + i, 80 + i)
+                                                                      for i in range(2)]
+    rng = np.random.default_rng(19)
+    insts = [batch.Instance(rng.integers(0, P, size=(1 + i % 3, 1 << (4 + 3 * i)), dtype=np.uint64), 600 + i, Q)
+             for i in range(4)]
+    alone = []
+    for x in jobs + insts:
+        (batch.prove_matmul(gt, key, SEED, x) if isinstance(x, batch.MatmulJob) else batch.prove_instance(gt, SEED, x))
+        alone.append(x.proof.copy())
+        x.proof[:] = 0
+    with batch.ProverService(gt, SEED, Q, workers=3, hbm_budget=budget, continuous=True) as svc:
+        svc.set_ajtai_key(key)
+        order = [x for pair in zip(jobs, insts) for x in pair]
+        tickets = [svc.submit(x) for x in order]
+        stats = [svc.wait(t)[1] for t in tickets]
+        assert svc.running() == 0 and svc.openings_in_flight() == 0
+    assert all(st["latency_ms"] >= st["run_ms"] > 0 for st in stats)
+    for x in order:
+        assert np.array_equal(x.proof, alone[(jobs + insts).index(x)])
+
+
+def test_continuous_service_jobs_join_openings_in_flight(env):
+    """Jobs submitted while another job's openings are in the engines join their steps, and every
+    proof is still its alone-run proof."""
+    import time
+    from morpheus_gb300 import batch
+    gt, key, _ = env
+    first = make(256, 64, 256, 700, 90)
+    late = [make(256, 8, 256, 701 + i, 91 + i) for i in range(3)]
+    rng = np.random.default_rng(23)
+    late_insts = [batch.Instance(rng.integers(0, P, size=(2, 1 << 12), dtype=np.uint64), 800 + i, Q) for i in range(2)]
+    alone = []
+    for x in [first] + late + late_insts:
+        (batch.prove_matmul(gt, key, SEED, x) if isinstance(x, batch.MatmulJob) else batch.prove_instance(gt, SEED, x))
+        alone.append(x.proof.copy())
+        x.proof[:] = 0
+    with batch.ProverService(gt, SEED, Q, workers=2, hbm_budget=8 << 30, continuous=True) as svc:
+        svc.set_ajtai_key(key)
+        t0 = svc.submit(first)
+        deadline = time.time() + 30
+        while svc.openings_in_flight() == 0 and svc.running() > 0 and time.time() < deadline:
+            time.sleep(0.0005)
+        tickets = [t0] + [svc.submit(x) for x in late + late_insts]
+        for t in tickets:
+            svc.wait(t)
+    for x, want in zip([first] + late + late_insts, alone):
+        assert np.array_equal(x.proof, want)
+
+
+def test_continuous_service_spans_size_classes(env):
+    """Instances whose openings fall in each of the engines' size classes (2^12, 2^19 and 2^22
+    evaluations) run together in the continuous service with their alone-run proofs."""
+    from morpheus_gb300 import batch
+    from morpheus_gb300.basefold import BasefoldTable
+    _, key, _ = env
+    gt = BasefoldTable.generate(22, 1, 22, 42)
+    rng = np.random.default_rng(29)
+    insts = [batch.Instance(rng.integers(0, P, size=(1, 1 << n), dtype=np.uint64), 900 + n, Q) for n in (22, 12, 19)]
+    alone = []
+    for x in insts:
+        batch.prove_instance(gt, SEED, x)
+        alone.append(x.proof.copy())
+        x.proof[:] = 0
+    with batch.ProverService(gt, SEED, Q, workers=3, hbm_budget=16 << 30, continuous=True) as svc:
+        for t in [svc.submit(x) for x in insts]:
+            svc.wait(t)
+    for x, want in zip(insts, alone):
+        assert np.array_equal(x.proof, want)
