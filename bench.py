@@ -591,9 +591,11 @@ def run_served(args, summary=False):
             lat.append((time.perf_counter() - t0 - a) * 1e3)
         return time.perf_counter() - t0, lat
 
+    slots = getattr(args, "slots", 0) or 0  # 0: no slot limit (the budget alone)
+
     def served(jobs, arrivals, continuous):
         with batch.ProverService(table, seed, QUERIES, workers=args.workers, hbm_budget=args.hbm_budget_gb << 30,
-                                 continuous=continuous) as svc:
+                                 continuous=continuous, slots=slots if continuous else None) as svc:
             svc.set_ajtai_key(key)
             for j in warm:
                 svc.wait(svc.submit(j))
@@ -661,6 +663,7 @@ def run_served(args, summary=False):
                                    "commit of A and B, partial evaluation, degree-2 sumcheck over K, open of A "
                                    "and B (34 queries), Ajtai commit of a 2^16 witness (16 rows)",
                        "engine": "continuous (gb_prover_create_continuous)", "workers": args.workers,
+                       "slots": slots,
                        "hbm_budget_gb": args.hbm_budget_gb, "offered_load_jobs_per_s": args.rate,
                        "table": "(24, 1, 24, seed 42)",
                        "timing": "host wall clock from the first arrival to the last proof",
@@ -690,6 +693,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="batched workload: the lockstep engine only (profiling)")
     ap.add_argument("--jobs", type=int, default=200, help="served workload: number of jobs")
     ap.add_argument("--rate", type=float, default=200.0, help="served workload: mean arrivals per second")
+    ap.add_argument("--slots", type=int, default=0, help="served workload: job slots of the continuous service "
+                                                        "(0: no limit beside the HBM budget)")
     ap.add_argument("--low-rates", type=float, nargs="*", default=[80.0, 120.0],
                     help="served workload: further offered loads reported beside --rate")
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")

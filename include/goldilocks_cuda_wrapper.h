@@ -359,6 +359,12 @@ int gb_prover_create(void *table, const uint64_t master_seed[2], int num_queries
  * the per-call path's.  Same submit / wait / drain / destroy calls; table: log_rate 1. */
 int gb_prover_create_continuous(void *table, const uint64_t master_seed[2], int num_queries, int workers,
                                 size_t hbm_budget, void **handle);
+/* Job slots (no reference counterpart): at most `slots` jobs are admitted and not yet complete at
+ * a time, beside the HBM budget; 0 (the default) lifts the limit.  In the continuous service the
+ * workers hand a job's openings over and take the next job at once, so without slots only the
+ * budget bounds the jobs sharing the device: the most throughput, each job finishing later.
+ * Fewer slots trade throughput for latency.  The whole-job service is bounded by its workers. */
+int gb_prover_set_slots(void *prover, int slots);
 /* Jobs admitted and not yet complete (either service), -1 for a null handle. */
 int gb_prover_running(void *prover);
 /* Openings in the continuous service's open engines (waiting to join or in flight); 0 for the

@@ -214,12 +214,14 @@ class ProverService:
     launch per kernel kind for all of them (gb_prover_create_continuous)."""
 
     def __init__(self, table, master_seed, num_queries, workers=8, hbm_budget=64 << 30, coop_threshold=None,
-                 top_nodes=None, continuous=False):
+                 top_nodes=None, continuous=False, slots=None):
         self.handle = ctypes.c_void_p()
         self.num_queries = num_queries
         fn = "gb_prover_create_continuous" if continuous else "gb_prover_create"
         N.check(getattr(N.lib(), fn)(table.handle, _seed(master_seed), num_queries, workers, hbm_budget,
                                      ctypes.byref(self.handle)), fn)
+        if slots is not None:
+            N.check(N.lib().gb_prover_set_slots(self.handle, slots), "gb_prover_set_slots")
         if coop_threshold is not None:
             N.check(N.lib().gb_prover_set_coop_threshold(self.handle, coop_threshold), "gb_prover_set_coop_threshold")
         if top_nodes is not None:

@@ -225,6 +225,13 @@ class Prover {
     }
     void set_coop(size_t v) { coop_.store(v); }
     void set_top(size_t v) { top_.store(v); }
+    void set_slots(int k) {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            slots_ = k;
+        }
+        cv_work_.notify_all();
+    }
     void set_ajtai_key(void* key) {
         std::lock_guard<std::mutex> l(mu_);
         ajtai_key_ = key;
@@ -291,6 +298,7 @@ class Prover {
     // the first queued job that fits the budget beside the running ones; a job larger than
     // the whole budget is taken only when nothing runs
     Job* take_locked() {
+        if (slots_ > 0 && running_ >= slots_) return nullptr;  // every slot holds a job in flight
         for (auto it = queue_.begin(); it != queue_.end(); ++it) {
             Job* j = *it;
             if (in_use_ + j->bytes <= budget_ || running_ == 0) {
@@ -405,6 +413,7 @@ class Prover {
     std::vector<std::thread> threads_;
     uint64_t next_ticket_ = 0;
     size_t in_use_ = 0;
+    int slots_ = 0;  // jobs in flight at most (0: the budget alone limits them)
     int running_ = 0, ready_ = 0, start_rc_ = 0;
     bool stop_ = false;
 };
@@ -482,6 +491,12 @@ int gb_prover_set_coop_threshold(void* prover, size_t parents) {
 int gb_prover_set_merkle_top_nodes(void* prover, size_t nodes) {
     if (!prover) return GB_EINVAL;
     static_cast<Prover*>(prover)->set_top(nodes);
+    return GB_OK;
+}
+
+int gb_prover_set_slots(void* prover, int slots) {
+    if (!prover || slots < 0) return GB_EINVAL;
+    static_cast<Prover*>(prover)->set_slots(slots);
     return GB_OK;
 }
 

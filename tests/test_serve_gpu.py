@@ -220,3 +220,34 @@ def test_continuous_service_spans_size_classes(env):
             svc.wait(t)
     for x, want in zip(insts, alone):
         assert np.array_equal(x.proof, want)
+
+
+def test_continuous_service_slots_bound_jobs_in_flight(env):
+    """With one job slot the continuous service never has more than one job admitted at a time,
+    whatever the budget, and the proofs are still the alone-run ones."""
+    import threading
+    from morpheus_gb300 import batch
+    gt, _, _ = env
+    rng = np.random.default_rng(37)
+    insts = [batch.Instance(rng.integers(0, P, size=(2, 1 << 11), dtype=np.uint64), 1000 + i, Q) for i in range(6)]
+    alone = []
+    for x in insts:
+        batch.prove_instance(gt, SEED, x)
+        alone.append(x.proof.copy())
+        x.proof[:] = 0
+    seen, stop = [], threading.Event()
+    with batch.ProverService(gt, SEED, Q, workers=3, hbm_budget=8 << 30, continuous=True, slots=1) as svc:
+        def watch():
+            while not stop.is_set():
+                seen.append(svc.running())
+        th = threading.Thread(target=watch)
+        th.start()
+        try:
+            for t in [svc.submit(x) for x in insts]:
+                svc.wait(t)
+        finally:
+            stop.set()
+            th.join()
+    assert max(seen) <= 1
+    for x, want in zip(insts, alone):
+        assert np.array_equal(x.proof, want)
