@@ -171,6 +171,54 @@ __global__ void P2_BOUNDS(T) ls_merkle_level_kernel(const LsSeg* __restrict__ se
     st_digest(sg.c + 4 * j, s);
 }
 
+// one Merkle layer in the 8-lane form (latency-bound layers): group g of a segment's blocks makes
+// parent g; a = children, c = parents.  Groups past a segment's end compute parent 0 and store
+// nothing (their warp takes part in the shuffles).
+constexpr int LS_COOP_THREADS = 128;
+__global__ void __launch_bounds__(LS_COOP_THREADS) ls_merkle_level_coop_kernel(const LsSeg* __restrict__ segs,
+                                                                               int nseg) {
+    LS_SEG_PROLOGUE
+    const u64 g = ((blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x) >> 3;
+    const int l = threadIdx.x & 7;
+    const bool live = g < sg.items;
+    const P2Lane c = p2_lane_consts(l);
+    const u64 x = p2_permute_coop(sg.a[8 * (live ? g : 0) + l], l, c);
+    if (live && l < 4) sg.c[4 * g + l] = x;
+}
+
+// The form of one segmented Merkle layer: the 8-lane form when its total parents are below
+// `coop` (the layer cannot fill the GPU, and one thread's permutation is a long serial chain),
+// else one permutation per thread in ls_p2_assign's CTA size.  The form is named, not read off
+// the CTA size: the 8-lane form and the narrow one-per-thread form both use 128 threads.
+enum class LsLayerForm { Coop, Wide, Narrow };
+static LsLayerForm ls_layer_assign(LsSeg* hs, int cnt, size_t coop, u64& nb) {
+    u64 total = 0;
+    for (int k = 0; k < cnt; k++) total += hs[k].items;
+    if (total < coop) {
+        nb = 0;
+        for (int k = 0; k < cnt; k++) {
+            hs[k].block0 = nb;
+            nb += (hs[k].items * 8 + LS_COOP_THREADS - 1) / LS_COOP_THREADS;
+        }
+        return LsLayerForm::Coop;
+    }
+    return ls_p2_assign(hs, cnt, nb) == P2_WIDE ? LsLayerForm::Wide : LsLayerForm::Narrow;
+}
+static int ls_layer_launch(LsLayerForm form, u64 nb, const LsSeg* ds, int cnt, cudaStream_t s) {
+    switch (form) {
+        case LsLayerForm::Coop:
+            ls_merkle_level_coop_kernel<<<(unsigned)nb, LS_COOP_THREADS, 0, s>>>(ds, cnt);
+            break;
+        case LsLayerForm::Wide:
+            ls_merkle_level_kernel<P2_WIDE><<<(unsigned)nb, P2_WIDE, 0, s>>>(ds, cnt);
+            break;
+        case LsLayerForm::Narrow:
+            ls_merkle_level_kernel<P2_NARROW><<<(unsigned)nb, P2_NARROW, 0, s>>>(ds, cnt);
+            break;
+    }
+    return check_launch("ls_merkle_level_kernel");
+}
+
 // recs[seg][8..11] = root digest at a (canonical); one thread per polynomial
 __global__ void ls_root_kernel(const LsSeg* __restrict__ segs, int nseg, u64* __restrict__ recs) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -432,7 +480,7 @@ __global__ void __launch_bounds__(256) ls_eq_expand_kernel(const EqSeg* __restri
 
 class LsRunner {
   public:
-    LsRunner(const BfTable* tab, int q) : tab_(tab), q_(q) {}
+    LsRunner(const BfTable* tab, int q, size_t coop) : tab_(tab), q_(q), coop_(coop) {}
 
     // openings of `polys` (transcripts already hold their "bf-open" preamble prefix)
     int open(std::vector<LsPoly>& P) {
@@ -656,12 +704,10 @@ class LsRunner {
                         unslot();
                         break;
                     }
-                    const int th = ls_p2_assign(hs, cnt, nb);
+                    const LsLayerForm form = ls_layer_assign(hs, cnt, coop_, nb);
                     ds = upload(hs, cnt);
                     if (!ds) return GB_ECUDA;
-                    if (th == P2_WIDE) ls_merkle_level_kernel<P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
-                    else ls_merkle_level_kernel<P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
-                    GB_LAUNCH_CHECK("ls_merkle_level_kernel");
+                    LS_RC(ls_layer_launch(form, nb, ds, cnt, s));
                 }
                 hs = next_slot(); if (!hs) return GB_EINVAL;
                 for (size_t m = 0; m < mid.size(); m++) {
@@ -827,6 +873,7 @@ class LsRunner {
 
     const BfTable* tab_;
     int q_;
+    size_t coop_;  // layers below this many parents run in the 8-lane form
     u64* ws_ = nullptr;
     LsSeg* d_segs_ = nullptr;
     LsSeg* h_segs_ = nullptr;
@@ -853,6 +900,7 @@ static size_t ls_commit_words(int n) {
 
 class LsCommitter {
   public:
+    explicit LsCommitter(size_t coop) : coop_(coop) {}
     int commit(std::vector<LsCommitJob>& J, u64* ws) {
         cudaStream_t s = stream();
         const int nj = (int)J.size();
@@ -889,6 +937,16 @@ class LsCommitter {
             return check_launch("ls_commit");
         };
         auto launch = [&](auto kernel, int count, u64 nb) -> int { return launch_t(kernel, count, nb, LS_THREADS); };
+        // a Merkle layer over the segments at h_segs_ + used, in the form ls_layer_assign picks
+        auto launch_layer = [&](int count) -> int {
+            u64 nb = 0;
+            LsSeg* hs = h_segs_ + used;
+            const LsLayerForm form = ls_layer_assign(hs, count, coop_, nb);
+            GB_CUDA_TRY(cudaMemcpyAsync(d_segs_ + used, hs, (size_t)count * sizeof(LsSeg), cudaMemcpyHostToDevice, s));
+            const int rc = ls_layer_launch(form, nb, d_segs_ + used, count, s);
+            used += count;
+            return rc;
+        };
         // a Poseidon2 kernel (template on its CTA size) over the segments at h_segs_ + used
         auto launch_p2 = [&](auto wide_kernel, auto narrow_kernel, int count) -> int {
             u64 nb = 0;
@@ -951,7 +1009,7 @@ class LsCommitter {
                 nb += blocks(parents);
             }
             if (!cnt) break;
-            LS_RC(launch_p2(ls_merkle_level_kernel<P2_WIDE>, ls_merkle_level_kernel<P2_NARROW>, cnt));
+            LS_RC(launch_layer(cnt));
         }
         // 5. the second copy on every layer
         {
@@ -979,7 +1037,7 @@ class LsCommitter {
                 hs[k] = LsSeg{layer, nullptr, layer + 8, nullptr, 0, 0, 1, nb};
                 nb += 1;
             }
-            LS_RC(launch_p2(ls_merkle_level_kernel<P2_WIDE>, ls_merkle_level_kernel<P2_NARROW>, nj));
+            LS_RC(launch_layer(nj));
             hs = h_segs_ + used;
             for (int k = 0; k < nj; k++) {
                 const u64 N = (u64)1 << J[k].n;
@@ -1005,6 +1063,7 @@ class LsCommitter {
     }
 
   private:
+    size_t coop_;  // layers below this many parents run in the 8-lane form
     static u64 blocks(u64 items) { return items ? (items + LS_THREADS - 1) / LS_THREADS : 1; }
     LsSeg* d_segs_ = nullptr;
     LsSeg* h_segs_ = nullptr;
@@ -1421,7 +1480,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return ls_inst_bytes(insts[a]) > ls_inst_bytes(insts[b]); });
-    const size_t coop = gb_get_coop_threshold(), top = gb_get_merkle_top_nodes();
+    const size_t coop = gb_get_coop_threshold();  // the 8-lane form below this many parents a layer
     t_ls_ms[0] = t_ls_ms[1] = t_ls_ms[2] = 0;
     size_t next = 0;
     while (next < order.size()) {
@@ -1477,7 +1536,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
             }
         }
         if (!rc) {
-            LsCommitter committer;
+            LsCommitter committer(coop);
             rc = committer.commit(jobs, cws);
         }
         if (!rc)
@@ -1526,7 +1585,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
                 std::vector<LsPoly> A, B;
                 for (size_t k = 0; k < idx.size(); k++) (k % 2 ? B : A).push_back(std::move(P[idx[k]]));
                 if (B.empty()) {
-                    LsRunner runner(tab, q);
+                    LsRunner runner(tab, q, coop);
                     rc = runner.open(A);
                 } else {
                     int dev = 0, rc2 = GB_OK;
@@ -1550,7 +1609,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
                             } else {
                                 gb_set_stream(st);
                                 {
-                                    LsRunner runner(tab, q);
+                                    LsRunner runner(tab, q, coop);
                                     rc2 = runner.open(B);
                                 }
                                 if (rc2) err2 = gb_last_error();
@@ -1560,7 +1619,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
                             if (st) cudaStreamDestroy(st);
                         });
                         {
-                            LsRunner runner(tab, q);
+                            LsRunner runner(tab, q, coop);
                             rc = runner.open(A);
                         }
                         helper.join();
@@ -1600,7 +1659,8 @@ struct EngPoly : LsPoly {
 
 class OpenEngine {
   public:
-    OpenEngine(const BfTable* tab, int q, int device) : tab_(tab), q_(q), device_(device) {
+    OpenEngine(const BfTable* tab, int q, int device)
+        : tab_(tab), q_(q), device_(device), coop_(gb_get_coop_threshold()) {
         th_ = std::thread([this] { run(); });
         std::unique_lock<std::mutex> l(mu_);
         cv_.wait(l, [this] { return started_; });
@@ -1993,12 +2053,10 @@ class OpenEngine {
                     break;
                 }
                 u64 nb = 0;
-                const int th = ls_p2_assign(hs, cnt, nb);
+                const LsLayerForm form = ls_layer_assign(hs, cnt, coop_, nb);
                 const LsSeg* ds = upload(hs, cnt);
                 if (!ds) return GB_ECUDA;
-                if (th == P2_WIDE) ls_merkle_level_kernel<P2_WIDE><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
-                else ls_merkle_level_kernel<P2_NARROW><<<(unsigned)nb, th, 0, s>>>(ds, cnt);
-                GB_LAUNCH_CHECK("ls_merkle_level_kernel");
+                LS_RC(ls_layer_launch(form, nb, ds, cnt, s));
             }
             // roots into records m of `mid`
             LsSeg* hs = segs(mid.size());
@@ -2149,6 +2207,7 @@ class OpenEngine {
 
     const BfTable* tab_;
     int q_, device_;
+    size_t coop_;  // the creating thread's cooperative threshold, for the Merkle layers
     std::thread th_;
     std::mutex mu_;
     std::condition_variable cv_;

@@ -158,3 +158,20 @@ def test_lockstep_engine_equals_alone(tables, budget, device):
     for a, b in zip(alone, together):
         assert np.array_equal(a.proof, b.proof)
     assert np.array_equal(alone[0].proof, oracle_instance_proof(alone[0].polys, alone[0].index, Q, ot))
+
+
+@pytest.mark.parametrize("coop", [0, 1 << 40, 700])
+def test_lockstep_layer_forms_do_not_change_proofs(tables, coop):
+    """The lockstep committer's and open runner's Merkle layers give the same trees in each form:
+    threshold 0 puts every layer in one permutation per thread (narrow CTAs for these small
+    trees), 2^40 puts every layer in the 8-lane form, 700 mixes them within one proof."""
+    from morpheus_gb300 import batch
+    gt, _ = tables
+    specs = [(TABLE_NV, 2), (12, 1), (9, 3), (5, 1), (TABLE_NV - 1, 1), (3, 2)]
+    alone = [make(n, d, k, 500 + k) for k, (n, d) in enumerate(specs)]
+    for inst in alone:
+        batch.prove_instance(gt, SEED, inst)
+    together = [make(n, d, k, 500 + k) for k, (n, d) in enumerate(specs)]
+    batch.batch_prove(gt, SEED, together, workers=2, engine="lockstep", coop_threshold=coop)
+    for a, b in zip(alone, together):
+        assert np.array_equal(a.proof, b.proof)

@@ -173,6 +173,32 @@ def test_continuous_service_mix_equals_alone(env, budget):
         assert np.array_equal(x.proof, alone[(jobs + insts).index(x)])
 
 
+@pytest.mark.parametrize("coop", [0, 1 << 40])
+def test_continuous_service_layer_forms_do_not_change_proofs(env, coop):
+    """The open engines take the creating thread's cooperative threshold for their Merkle
+    layers: 0 puts every layer in one permutation per thread, 2^40 every layer in the 8-lane
+    form; the proofs are the alone-run proofs either way."""
+    from morpheus_gb300 import batch
+    gt, key, _ = env
+    rng = np.random.default_rng(31)
+    insts = [batch.Instance(rng.integers(0, P, size=(1 + i % 2, 1 << n), dtype=np.uint64), 900 + i, Q)
+             for i, n in enumerate((TABLE_NV, 11, 7, 3))]
+    jobs = [make(256, 16, 256, 950, 97)]
+    alone = []
+    for x in jobs + insts:
+        (batch.prove_matmul(gt, key, SEED, x) if isinstance(x, batch.MatmulJob) else batch.prove_instance(gt, SEED, x))
+        alone.append(x.proof.copy())
+        x.proof[:] = 0
+    with batch.Schedule(coop, None):
+        svc = batch.ProverService(gt, SEED, Q, workers=2, hbm_budget=8 << 30, continuous=True)
+    with svc:
+        svc.set_ajtai_key(key)
+        for t in [svc.submit(x) for x in jobs + insts]:
+            svc.wait(t)
+    for x, a in zip(jobs + insts, alone):
+        assert np.array_equal(x.proof, a)
+
+
 def test_continuous_service_jobs_join_openings_in_flight(env):
     """Jobs submitted while another job's openings are in the engines join their steps, and every
     proof is still its alone-run proof."""
