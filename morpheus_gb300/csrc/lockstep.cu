@@ -1460,6 +1460,205 @@ static size_t ls_inst_bytes(const gb_instance& in) {
 // wall time of the last lockstep batch on this thread: commits + sumchecks, openings
 static thread_local double t_ls_ms[3] = {0, 0, 0};  // commit + sumcheck, open, of which sumcheck
 
+// Runs `side` on a helper thread with its own stream, ordered after the work already on the
+// calling thread's stream, while `main` runs on the calling thread.  Returns main's result if it
+// failed, else side's (side_rc and side_err, which `side` sets on failure).  Synchronising.
+template <class Side, class Main>
+static int ls_on_helper_stream(Side side, Main main, int& side_rc, std::string& side_err) {
+    cudaStream_t s = stream();
+    int dev = 0;
+    cudaEvent_t ready = nullptr;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ready, s);
+    if (e != cudaSuccess) {
+        if (ready) cudaEventDestroy(ready);
+        set_error("lockstep helper stream", e);
+        return GB_ECUDA;
+    }
+    std::thread helper([&] {
+        cudaStream_t st = nullptr;
+        cudaError_t he = cudaSetDevice(dev);
+        if (he == cudaSuccess) he = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (he == cudaSuccess) he = cudaStreamWaitEvent(st, ready, 0);
+        if (he != cudaSuccess) {
+            side_rc = GB_ECUDA;
+            side_err = std::string("lockstep helper stream: ") + cudaGetErrorString(he);
+        } else {
+            gb_set_stream(st);
+            side();
+            cudaStreamSynchronize(st);
+            gb_set_stream(nullptr);
+        }
+        if (st) cudaStreamDestroy(st);
+    });
+    int rc = main();
+    helper.join();
+    cudaEventDestroy(ready);
+    if (!rc && side_rc) {
+        rc = side_rc;
+        set_error_msg(side_err);
+    }
+    return rc;
+}
+
+// One group of a wave, on the calling thread's stream: inputs on the device, the commits of every
+// polynomial in lockstep (roots into the proofs), then `committed()` (called exactly once, also
+// on failure), the product sumchecks in lockstep and the openings in lockstep, in two halves on
+// two streams.  Synchronising.
+static int ls_prove_group(const BfTable* tab, const u64 seed[2], int q, const gb_instance* insts,
+                          const std::vector<int>& wave, size_t coop, const std::function<void()>& committed) {
+    using namespace host;
+    bool signalled = false;
+    auto signal = [&] {
+        if (!signalled) committed();
+        signalled = true;
+    };
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = stream();
+    // inputs on the device
+    std::vector<const u64*> polys(wave.size());
+    std::vector<u64*> owned(wave.size(), nullptr);
+    int rc = GB_OK;
+    for (size_t k = 0; k < wave.size() && !rc; k++) {
+        const gb_instance& in = insts[wave[k]];
+        if (in.h_polys) {
+            size_t bytes = ((size_t)in.degree << in.num_vars) * 8;
+            cudaError_t e = cudaMallocAsync(&owned[k], bytes, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(owned[k], in.h_polys, bytes, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) {
+                set_error("input upload", e);
+                rc = GB_ECUDA;
+            }
+            polys[k] = owned[k];
+        } else {
+            polys[k] = in.d_polys;
+        }
+    }
+    // commits of every polynomial of the group, in lockstep
+    std::vector<LsCommitJob> jobs;
+    std::vector<size_t> first_job(wave.size());
+    size_t cwords = 0;
+    for (size_t k = 0; k < wave.size(); k++) {
+        const gb_instance& in = insts[wave[k]];
+        first_job[k] = jobs.size();
+        for (int j = 0; j < in.degree; j++) {
+            LsCommitJob cj;
+            cj.n = in.num_vars;
+            cj.evals = polys[k] + ((size_t)j << in.num_vars);
+            jobs.push_back(cj);
+            cwords += ls_commit_words(in.num_vars);
+        }
+    }
+    u64* cws = nullptr;
+    if (!rc) {
+        cudaError_t e = cudaMallocAsync(&cws, std::max<size_t>(cwords, 2) * 8, s);
+        if (e != cudaSuccess) {
+            set_error("commit workspace", e);
+            rc = GB_ECUDA;
+        }
+    }
+    if (!rc) {
+        LsCommitter committer(coop);
+        rc = committer.commit(jobs, cws);
+    }
+    signal();
+    if (!rc)
+        for (size_t k = 0; k < wave.size(); k++) {
+            const gb_instance& in = insts[wave[k]];
+            for (int j = 0; j < in.degree; j++)
+                for (int w = 0; w < 4; w++) in.h_proof[4 * j + w] = jobs[first_job[k] + j].com.root[w];
+        }
+    // product sumchecks of the group, all rounds in lockstep
+    const auto ts = std::chrono::steady_clock::now();
+    if (!rc) {
+        // on a stream of the highest priority: the sumchecks are a chain of small launches and
+        // host round trips, which another group's commit or open launches would otherwise delay
+        int lo = 0, hi = 0;
+        cudaStream_t hs = nullptr;
+        cudaEvent_t inputs = nullptr;
+        cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&inputs, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(inputs, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(hs, inputs, 0);
+        if (e != cudaSuccess) {
+            set_error("lockstep sumcheck stream", e);
+            rc = GB_ECUDA;
+        } else {
+            gb_set_stream(hs);
+            rc = ls_sumchecks(seed, insts, wave, polys);  // synchronises hs before it returns
+            gb_set_stream(s);
+        }
+        if (inputs) cudaEventDestroy(inputs);
+        if (hs) cudaStreamDestroy(hs);
+    }
+    t_ls_ms[2] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ts).count();
+    auto t1 = std::chrono::steady_clock::now();
+    t_ls_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+    if (!rc) {
+        // openings of every polynomial of the group, in lockstep
+        std::vector<LsPoly> P;
+        for (size_t k = 0; k < wave.size(); k++) {
+            const gb_instance& in = insts[wave[k]];
+            const int n = in.num_vars, d = in.degree;
+            const size_t plen = gb_basefold_proof_len(n, 1, q);
+            const u64* chal = in.h_proof + (size_t)d * 4 + (size_t)n * (d + 1) * 2;
+            u64* opens = in.h_proof + inst_proof_words_before_opens(n, d);
+            for (int j = 0; j < d; j++) {
+                LsPoly p;
+                p.n = n;
+                p.N = (size_t)1 << n;
+                p.L = p.N << 1;
+                p.com = &jobs[first_job[k] + j].com;
+                p.point = chal;
+                gb_transcript_new(&p.t, "bf-open");
+                tr_append_ext2(&p.t, "", E2{canon(seed[0]), canon(seed[1])});
+                tr_append_u64(&p.t, "", 8 * in.index + (u64)j);
+                p.proof = opens + (size_t)j * plen;
+                P.push_back(std::move(p));
+            }
+        }
+        // two halves of the polynomials (alternating in size order, so that both carry about the
+        // same work), each opened by its own runner: the second on a helper thread with its own
+        // stream, so that one half's host round trip between rounds overlaps the other half's
+        // device work
+        std::vector<size_t> idx(P.size());
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return P[a].N > P[b].N; });
+        std::vector<LsPoly> A, B;
+        for (size_t k = 0; k < idx.size(); k++) (k % 2 ? B : A).push_back(std::move(P[idx[k]]));
+        if (B.empty()) {
+            LsRunner runner(tab, q, coop);
+            rc = runner.open(A);
+        } else {
+            int rc2 = GB_OK;
+            std::string err2;
+            rc = ls_on_helper_stream(
+                [&] {
+                    LsRunner runner(tab, q, coop);
+                    rc2 = runner.open(B);
+                    if (rc2) err2 = gb_last_error();
+                },
+                [&] {
+                    LsRunner runner(tab, q, coop);
+                    return runner.open(A);
+                },
+                rc2, err2);
+        }
+        t_ls_ms[1] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+    }
+    if (cws) cudaFreeAsync(cws, s);
+    for (size_t k = 0; k < wave.size(); k++)
+        if (owned[k]) cudaFreeAsync(owned[k], s);
+    if (rc) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return GB_OK;
+}
+
 static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instance* insts, int count, int workers,
                           size_t budget) {
     using namespace host;
@@ -1491,153 +1690,42 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
             used += ls_inst_bytes(insts[order[next]]);
             wave.push_back(order[next++]);
         }
-        auto t0 = std::chrono::steady_clock::now();
-        cudaStream_t s = stream();
-        // inputs on the device
-        std::vector<const u64*> polys(wave.size());
-        std::vector<u64*> owned(wave.size(), nullptr);
+        // Two groups (alternating in size order), staggered: the second group's commits start
+        // once the first group's are done, so they run beside the first group's sumchecks (a chain
+        // of host round trips with little device work), and the first group's openings beside the
+        // second group's sumchecks.  Each group's proofs are those it gives alone.
+        std::vector<int> g1, g2;
+        for (size_t k = 0; k < wave.size(); k++) (k % 2 ? g2 : g1).push_back(wave[k]);
         int rc = GB_OK;
-        for (size_t k = 0; k < wave.size() && !rc; k++) {
-            const gb_instance& in = insts[wave[k]];
-            if (in.h_polys) {
-                size_t bytes = ((size_t)in.degree << in.num_vars) * 8;
-                cudaError_t e = cudaMallocAsync(&owned[k], bytes, s);
-                if (e == cudaSuccess) e = cudaMemcpyAsync(owned[k], in.h_polys, bytes, cudaMemcpyHostToDevice, s);
-                if (e != cudaSuccess) {
-                    set_error("input upload", e);
-                    rc = GB_ECUDA;
-                }
-                polys[k] = owned[k];
-            } else {
-                polys[k] = in.d_polys;
-            }
-        }
-        // commits of every polynomial of the wave, in lockstep
-        std::vector<LsCommitJob> jobs;
-        std::vector<size_t> first_job(wave.size());
-        size_t cwords = 0;
-        for (size_t k = 0; k < wave.size(); k++) {
-            const gb_instance& in = insts[wave[k]];
-            first_job[k] = jobs.size();
-            for (int j = 0; j < in.degree; j++) {
-                LsCommitJob cj;
-                cj.n = in.num_vars;
-                cj.evals = polys[k] + ((size_t)j << in.num_vars);
-                jobs.push_back(cj);
-                cwords += ls_commit_words(in.num_vars);
-            }
-        }
-        u64* cws = nullptr;
-        if (!rc) {
-            cudaError_t e = cudaMallocAsync(&cws, std::max<size_t>(cwords, 2) * 8, s);
-            if (e != cudaSuccess) {
-                set_error("commit workspace", e);
-                rc = GB_ECUDA;
-            }
-        }
-        if (!rc) {
-            LsCommitter committer(coop);
-            rc = committer.commit(jobs, cws);
-        }
-        if (!rc)
-            for (size_t k = 0; k < wave.size(); k++) {
-                const gb_instance& in = insts[wave[k]];
-                for (int j = 0; j < in.degree; j++)
-                    for (int w = 0; w < 4; w++) in.h_proof[4 * j + w] = jobs[first_job[k] + j].com.root[w];
-            }
-        // product sumchecks of the wave, all rounds in lockstep
-        const auto ts = std::chrono::steady_clock::now();
-        if (!rc) rc = ls_sumchecks(seed, insts, wave, polys);
-        t_ls_ms[2] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ts).count();
-        auto t1 = std::chrono::steady_clock::now();
-        t_ls_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
-        if (!rc) {
-            // openings of every polynomial of the wave, in lockstep
-            std::vector<LsPoly> P;
-            for (size_t k = 0; k < wave.size(); k++) {
-                const gb_instance& in = insts[wave[k]];
-                const int n = in.num_vars, d = in.degree;
-                const size_t plen = gb_basefold_proof_len(n, 1, q);
-                const u64* chal = in.h_proof + (size_t)d * 4 + (size_t)n * (d + 1) * 2;
-                u64* opens = in.h_proof + inst_proof_words_before_opens(n, d);
-                for (int j = 0; j < d; j++) {
-                    LsPoly p;
-                    p.n = n;
-                    p.N = (size_t)1 << n;
-                    p.L = p.N << 1;
-                    p.com = &jobs[first_job[k] + j].com;
-                    p.point = chal;
-                    gb_transcript_new(&p.t, "bf-open");
-                    tr_append_ext2(&p.t, "", E2{canon(seed[0]), canon(seed[1])});
-                    tr_append_u64(&p.t, "", 8 * in.index + (u64)j);
-                    p.proof = opens + (size_t)j * plen;
-                    P.push_back(std::move(p));
-                }
-            }
-            {
-                // two halves of the polynomials (alternating in size order, so that both carry
-                // about the same work), each opened by its own runner: the second on a helper
-                // thread with its own stream, so that one half's host round trip between rounds
-                // overlaps the other half's device work
-                std::vector<size_t> idx(P.size());
-                std::iota(idx.begin(), idx.end(), 0);
-                std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return P[a].N > P[b].N; });
-                std::vector<LsPoly> A, B;
-                for (size_t k = 0; k < idx.size(); k++) (k % 2 ? B : A).push_back(std::move(P[idx[k]]));
-                if (B.empty()) {
-                    LsRunner runner(tab, q, coop);
-                    rc = runner.open(A);
-                } else {
-                    int dev = 0, rc2 = GB_OK;
-                    std::string err2;
-                    cudaEvent_t ready = nullptr;
-                    cudaError_t e = cudaGetDevice(&dev);
-                    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
-                    if (e == cudaSuccess) e = cudaEventRecord(ready, s);  // the commits and sumchecks
-                    if (e != cudaSuccess) {
-                        set_error("lockstep open helper", e);
-                        rc = GB_ECUDA;
-                    } else {
-                        std::thread helper([&] {
-                            cudaStream_t st = nullptr;
-                            cudaError_t he = cudaSetDevice(dev);
-                            if (he == cudaSuccess) he = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-                            if (he == cudaSuccess) he = cudaStreamWaitEvent(st, ready, 0);
-                            if (he != cudaSuccess) {
-                                rc2 = GB_ECUDA;
-                                err2 = std::string("lockstep open helper: ") + cudaGetErrorString(he);
-                            } else {
-                                gb_set_stream(st);
-                                {
-                                    LsRunner runner(tab, q, coop);
-                                    rc2 = runner.open(B);
-                                }
-                                if (rc2) err2 = gb_last_error();
-                                cudaStreamSynchronize(st);
-                                gb_set_stream(nullptr);
-                            }
-                            if (st) cudaStreamDestroy(st);
-                        });
-                        {
-                            LsRunner runner(tab, q, coop);
-                            rc = runner.open(A);
-                        }
-                        helper.join();
-                        if (!rc && rc2) {
-                            rc = rc2;
-                            set_error_msg(err2);
-                        }
+        if (g2.empty()) {
+            rc = ls_prove_group(tab, seed, q, insts, g1, coop, [] {});
+        } else {
+            std::mutex mu;
+            std::condition_variable cv;
+            bool committed = false;
+            int rc2 = GB_OK;
+            std::string err2;
+            rc = ls_on_helper_stream(
+                [&] {
+                    {
+                        std::unique_lock<std::mutex> l(mu);
+                        cv.wait(l, [&] { return committed; });
                     }
-                    if (ready) cudaEventDestroy(ready);
-                }
-            }
-            t_ls_ms[1] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+                    rc2 = ls_prove_group(tab, seed, q, insts, g2, coop, [] {});
+                    if (rc2) err2 = gb_last_error();
+                },
+                [&] {
+                    return ls_prove_group(tab, seed, q, insts, g1, coop, [&] {
+                        {
+                            std::lock_guard<std::mutex> l(mu);
+                            committed = true;
+                        }
+                        cv.notify_all();
+                    });
+                },
+                rc2, err2);
         }
-        if (cws) cudaFreeAsync(cws, s);
-        for (size_t k = 0; k < wave.size(); k++)
-            if (owned[k]) cudaFreeAsync(owned[k], s);
         if (rc) return rc;
-        GB_CUDA_TRY(cudaStreamSynchronize(s));
     }
     return GB_OK;
 }
@@ -2177,14 +2265,17 @@ class OpenEngine {
             p->ws = nullptr;
         }
         LS_RC(sync());
-        // callbacks, then the finished polynomials leave the set
+        // the finished polynomials leave the set, then their callbacks run (a callback may
+        // complete the job, and whoever waits on it may count the openings in flight at once)
         std::vector<std::unique_ptr<EngPoly>> keep, gone;
         for (auto& p : active_) (p->rd >= p->n ? gone : keep).push_back(std::move(p));
         active_.swap(keep);
         for (auto& p : gone) {
+            {
+                std::lock_guard<std::mutex> l(mu_);
+                waiting_--;
+            }
             if (p->task.done) p->task.done(GB_OK, std::string());
-            std::lock_guard<std::mutex> l(mu_);
-            waiting_--;
         }
         return GB_OK;
     }
@@ -2197,9 +2288,11 @@ class OpenEngine {
         gone.swap(active_);
         for (auto& p : gone) {
             if (p->ws) cudaFreeAsync(p->ws, s);
+            {
+                std::lock_guard<std::mutex> l(mu_);
+                waiting_--;
+            }
             if (p->task.done) p->task.done(rc, err);
-            std::lock_guard<std::mutex> l(mu_);
-            waiting_--;
         }
         cudaStreamSynchronize(s);
         seg_used_ = 0;
