@@ -493,14 +493,23 @@ def run_batched(args, summary=False):
     if summary:
         times_svc, launches_svc, clk_svc = [float("inf")], 0, None
     budget = 160 << 30
-    batch.batch_prove(table, seed, insts, best, budget, engine="lockstep")
-    l1 = L.gb_launch_count()
-    with ClockSampler() as clk_ls:
-        times_ls = [wall(lambda: batch.batch_prove(table, seed, insts, best, budget, engine="lockstep"))
-                    for _ in range(args.steps)]
-    launches_ls = (L.gb_launch_count() - l1) // max(1, args.steps)
-    phase = (ctypes.c_double(), ctypes.c_double(), ctypes.c_double())
-    L.gb_lockstep_last_timing(*(ctypes.byref(x) for x in phase))
+    # the lockstep engine's schedule (staggered groups, open parts, cooperative threshold), tuned
+    # on this batch; these runs are its warm-up
+    (ls_groups, ls_parts, ls_coop), tune_ls = batch.autotune_lockstep(
+        table, seed, insts, groups=(2, 1, 3, 4), open_parts=(2, 1, 3), coop_thresholds=(4096, 16384, 8192, 2048),
+        hbm_budget=budget)
+    ls_sched = batch.Schedule(ls_coop, None, ls_groups, ls_parts)
+    with ls_sched:
+        batch.batch_prove(table, seed, insts, best, budget, engine="lockstep")
+        l1 = L.gb_launch_count()
+        with ClockSampler() as clk_ls:
+            times_ls = [wall(lambda: batch.batch_prove(table, seed, insts, best, budget, engine="lockstep"))
+                        for _ in range(args.steps)]
+        launches_ls = (L.gb_launch_count() - l1) // max(1, args.steps)
+        phase = (ctypes.c_double(), ctypes.c_double(), ctypes.c_double())
+        L.gb_lockstep_last_timing(*(ctypes.byref(x) for x in phase))
+    lockstep_schedule = {"groups": ls_groups, "open_parts": ls_parts, "coop_threshold": ls_coop,
+                         "autotune_s": {f"{k[0]}g/{k[1]}p/{k[2]}": round(v, 4) for k, v in tune_ls.items()}}
     same_ls = sum(np.array_equal(i.proof, a) for i, a in zip(insts, alone))
     engine = "lockstep" if statistics.mean(times_ls) < statistics.mean(times_svc) else "service"
     times, launches, clk = (times_ls, launches_ls, clk_ls) if engine == "lockstep" else (times_svc, launches_svc, clk_svc)
@@ -510,6 +519,7 @@ def run_batched(args, summary=False):
                 "per_call": {"value": count / per_call_s, "unit": "proofs/s", "ms_per_batch": per_call_s * 1e3},
                 "batched_over_per_call": per_call_s / statistics.mean(times),
                 "identical_to_per_call": f"{same_ls}/{count}", "gpu_launches": int(launches),
+                "lockstep_schedule": lockstep_schedule,
                 "workload": "512 instances, 2^10..2^20 evaluations (log-uniform), degree 2..4, sumcheck + "
                             "commit/open of each polynomial; python bench.py --workload batched for the full run"}
     # end to end: the same batch from pinned host memory (host->device copies inside)
@@ -521,9 +531,10 @@ def run_batched(args, summary=False):
         pinned[o:o + k] = i.polys.reshape(-1)
         host_insts.append(batch.Instance(pinned[o:o + k].reshape(i.polys.shape), i.index, QUERIES))
         o += k
-    batch.batch_prove(table, seed, host_insts, best, budget, engine=engine)
-    e2e_times = [wall(lambda: batch.batch_prove(table, seed, host_insts, best, budget, engine=engine))
-                 for _ in range(args.steps)]
+    with ls_sched:
+        batch.batch_prove(table, seed, host_insts, best, budget, engine=engine)
+        e2e_times = [wall(lambda: batch.batch_prove(table, seed, host_insts, best, budget, engine=engine))
+                     for _ in range(args.steps)]
     same_e2e = sum(np.array_equal(h.proof, a) for h, a in zip(host_insts, alone))
 
     step_s = statistics.mean(times)
@@ -546,7 +557,7 @@ def run_batched(args, summary=False):
             "engines": {"service": {"ms_per_step": statistics.mean(times_svc) * 1e3, "gpu_launches": int(launches_svc)},
                         "lockstep": {"ms_per_step": statistics.mean(times_ls) * 1e3, "gpu_launches": int(launches_ls),
                                      "commit_sumcheck_ms": phase[0].value, "open_ms": phase[1].value,
-                                     "sumcheck_ms": phase[2].value},
+                                     "sumcheck_ms": phase[2].value, "schedule": lockstep_schedule},
                         "chosen": engine},
             "e2e": {"value": count / statistics.mean(e2e_times), "unit": "proofs/s",
                     "h2d_bytes_per_step": int(total),

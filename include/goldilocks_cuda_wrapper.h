@@ -398,6 +398,13 @@ int gb_batch_prove_lockstep(void *table, const uint64_t master_seed[2], int num_
  * phase, the opening phase and the sumcheck part of the first, summed over its waves (any
  * pointer may be NULL). */
 void gb_lockstep_last_timing(double *commit_sumcheck_ms, double *open_ms, double *sumcheck_ms);
+/* Schedule of the calling thread's gb_batch_prove_lockstep calls (no reference counterpart; the
+ * autotuner's knobs, results never depend on them): a wave's instances are dealt out in size
+ * order to `groups` staggered groups (group k + 1's commits start once group k's are done, each
+ * group on its own stream and host thread), and each group's polynomials to `open_parts` parts
+ * opened side by side on their own streams.  Both in [1, 8], else -2.  Default 2 and 2. */
+int gb_set_lockstep_schedule(int groups, int open_parts);
+void gb_get_lockstep_schedule(int *groups, int *open_parts);
 
 /* A quantized matmul layer C = A B as a served job (no reference counterpart; the field work
  * of zk-torch-3/src/basicblock/einsum.rs:807-1000): A is m x k, B is k x n (row-major int8),

@@ -165,41 +165,49 @@ def prove_instance(table, master_seed, inst):
 
 
 class Schedule:
-    """Per-thread Merkle scheduling knobs (results never depend on them): the cooperative
-    threshold (gb_set_coop_threshold) and the single-CTA top size (gb_set_merkle_top_nodes).
-    A context manager that sets them on the calling thread and restores the previous ones."""
+    """Per-thread scheduling knobs (results never depend on them): the Merkle cooperative threshold
+    (gb_set_coop_threshold), the single-CTA top size (gb_set_merkle_top_nodes) and the lockstep
+    engine's staggered groups and open parts (gb_set_lockstep_schedule).  A context manager that
+    sets the given ones on the calling thread and restores the previous ones."""
 
-    def __init__(self, coop_threshold=None, top_nodes=None):
-        self.coop, self.top = coop_threshold, top_nodes
+    def __init__(self, coop_threshold=None, top_nodes=None, groups=None, open_parts=None):
+        self.coop, self.top, self.groups, self.parts = coop_threshold, top_nodes, groups, open_parts
 
     def __enter__(self):
         L = N.lib()
-        self._old = (L.gb_get_coop_threshold(), L.gb_get_merkle_top_nodes())
+        g, p = ctypes.c_int(), ctypes.c_int()
+        L.gb_get_lockstep_schedule(ctypes.byref(g), ctypes.byref(p))
+        self._old = (L.gb_get_coop_threshold(), L.gb_get_merkle_top_nodes(), g.value, p.value)
         if self.coop is not None:
             L.gb_set_coop_threshold(self.coop)
         if self.top is not None:
             L.gb_set_merkle_top_nodes(self.top)
+        if self.groups is not None or self.parts is not None:
+            N.check(L.gb_set_lockstep_schedule(self.groups if self.groups is not None else g.value,
+                                               self.parts if self.parts is not None else p.value),
+                    "gb_set_lockstep_schedule")
         return self
 
     def __exit__(self, *a):
         L = N.lib()
         L.gb_set_coop_threshold(self._old[0])
         L.gb_set_merkle_top_nodes(self._old[1])
+        L.gb_set_lockstep_schedule(self._old[2], self._old[3])
 
 
 def batch_prove(table, master_seed, instances, workers=8, hbm_budget=64 << 30, coop_threshold=None, top_nodes=None,
-                engine="service"):
+                engine="service", groups=None, open_parts=None):
     """All instances at once.  engine "service": the prover service, whole instances on worker
-    streams, largest first; "lockstep": commits and sumchecks on workers, then every
-    opening round-synchronously (one launch per step for all polynomials).  The Merkle schedule
-    (None keeps the calling thread's) applies to both; proofs are the same either way."""
+    streams, largest first; "lockstep": the round-synchronous engine (commits, sumcheck rounds and
+    opening rounds of all instances in lockstep) in `groups` staggered groups whose openings run in
+    `open_parts` parts.  The schedule (None keeps the calling thread's) never changes the proofs."""
     if not instances:
         return
     q = instances[0].num_queries
     assert all(i.num_queries == q for i in instances)
     arr = (GbInstance * len(instances))(*[i.struct() for i in instances])
     fn = {"service": N.lib().gb_batch_prove, "lockstep": N.lib().gb_batch_prove_lockstep}[engine]
-    with Schedule(coop_threshold, top_nodes):
+    with Schedule(coop_threshold, top_nodes, groups, open_parts):
         N.check(fn(table.handle, _seed(master_seed), q, arr, len(instances), workers, hbm_budget),
                 "gb_batch_prove" if engine == "service" else "gb_batch_prove_lockstep")
 
@@ -291,6 +299,36 @@ def mixed_workload(count, seed, min_vars=10, max_vars=20, degrees=(2, 3, 4), num
         polys = rng.integers(0, P, size=(int(degs[k]), 1 << int(sizes[k])), dtype=np.uint64)
         out.append(Instance(polys, k, num_queries))
     return out
+
+
+def autotune_lockstep(table, master_seed, instances, groups=(2, 1, 3, 4), open_parts=(2, 1, 3),
+                      coop_thresholds=(16384, 8192, 32768), hbm_budget=64 << 30, repeats=1):
+    """Schedule (groups, open parts, cooperative threshold) of the lockstep engine for this batch,
+    by coordinate search in that order from the first value of each axis, each candidate timed
+    by wall clock (the best of `repeats` runs) after one warm-up run.  Returns
+    ((groups, open_parts, coop), {schedule: seconds})."""
+    def run(g, p, c):
+        best_t = None
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            batch_prove(table, master_seed, instances, 1, hbm_budget, coop_threshold=c, engine="lockstep",
+                        groups=g, open_parts=p)
+            t = time.perf_counter() - t0
+            best_t = t if best_t is None else min(best_t, t)
+        return best_t
+
+    best = (groups[0], open_parts[0], coop_thresholds[0])
+    run(*best)
+    times = {}
+    for axis, values in ((0, groups), (1, open_parts), (2, coop_thresholds)):
+        for v in values:
+            cand = list(best)
+            cand[axis] = v
+            cand = tuple(cand)
+            if cand not in times:
+                times[cand] = run(*cand)
+        best = min(times, key=times.get)
+    return best, times
 
 
 def autotune(table, master_seed, instances, workers=(8, 12, 16, 24), coop_thresholds=(16384, 4096),

@@ -1460,11 +1460,12 @@ static size_t ls_inst_bytes(const gb_instance& in) {
 // wall time of the last lockstep batch on this thread: commits + sumchecks, openings
 static thread_local double t_ls_ms[3] = {0, 0, 0};  // commit + sumcheck, open, of which sumcheck
 
-// Runs `side` on a helper thread with its own stream, ordered after the work already on the
-// calling thread's stream, while `main` runs on the calling thread.  Returns main's result if it
-// failed, else side's (side_rc and side_err, which `side` sets on failure).  Synchronising.
-template <class Side, class Main>
-static int ls_on_helper_stream(Side side, Main main, int& side_rc, std::string& side_err) {
+// parts[0] on the calling thread and its stream; parts[k] (k >= 1) on helper thread k with a stream
+// of its own that starts after the work already queued on the caller's stream.  Synchronising;
+// returns the first failing part's code (in part order) with its message.
+static int ls_on_streams(const std::vector<std::function<int()>>& parts) {
+    if (parts.empty()) return GB_OK;
+    if (parts.size() == 1) return parts[0]();
     cudaStream_t s = stream();
     int dev = 0;
     cudaEvent_t ready = nullptr;
@@ -1473,41 +1474,59 @@ static int ls_on_helper_stream(Side side, Main main, int& side_rc, std::string& 
     if (e == cudaSuccess) e = cudaEventRecord(ready, s);
     if (e != cudaSuccess) {
         if (ready) cudaEventDestroy(ready);
-        set_error("lockstep helper stream", e);
+        set_error("lockstep helper streams", e);
         return GB_ECUDA;
     }
-    std::thread helper([&] {
-        cudaStream_t st = nullptr;
-        cudaError_t he = cudaSetDevice(dev);
-        if (he == cudaSuccess) he = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-        if (he == cudaSuccess) he = cudaStreamWaitEvent(st, ready, 0);
-        if (he != cudaSuccess) {
-            side_rc = GB_ECUDA;
-            side_err = std::string("lockstep helper stream: ") + cudaGetErrorString(he);
-        } else {
-            gb_set_stream(st);
-            side();
-            cudaStreamSynchronize(st);
-            gb_set_stream(nullptr);
-        }
-        if (st) cudaStreamDestroy(st);
-    });
-    int rc = main();
-    helper.join();
+    const size_t n = parts.size();
+    std::vector<int> rcs(n, GB_OK);
+    std::vector<std::string> errs(n);
+    std::vector<std::thread> helpers;
+    for (size_t k = 1; k < n; k++)
+        helpers.emplace_back([&, k] {
+            cudaStream_t st = nullptr;
+            cudaError_t he = cudaSetDevice(dev);
+            if (he == cudaSuccess) he = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            if (he == cudaSuccess) he = cudaStreamWaitEvent(st, ready, 0);
+            if (he != cudaSuccess) {
+                // the part still runs (on this thread's default stream), so that what it signals to
+                // the other parts happens; the failure is reported
+                if (st) cudaStreamDestroy(st);
+                st = nullptr;
+                parts[k]();
+                rcs[k] = GB_ECUDA;
+                errs[k] = std::string("lockstep helper stream: ") + cudaGetErrorString(he);
+            } else {
+                gb_set_stream(st);
+                rcs[k] = parts[k]();
+                if (rcs[k]) errs[k] = gb_last_error();
+                cudaStreamSynchronize(st);
+                gb_set_stream(nullptr);
+            }
+            if (st) cudaStreamDestroy(st);
+        });
+    rcs[0] = parts[0]();
+    if (rcs[0]) errs[0] = gb_last_error();
+    for (auto& t : helpers) t.join();
     cudaEventDestroy(ready);
-    if (!rc && side_rc) {
-        rc = side_rc;
-        set_error_msg(side_err);
-    }
-    return rc;
+    for (size_t k = 0; k < n; k++)
+        if (rcs[k]) {
+            set_error_msg(errs[k]);
+            return rcs[k];
+        }
+    return GB_OK;
 }
+
+// Schedule of the calling thread's lockstep batches (gb_set_lockstep_schedule): the wave's
+// instances in this many staggered groups, each group's openings in this many parts.
+static thread_local int t_ls_groups = 2, t_ls_open_parts = 2;
 
 // One group of a wave, on the calling thread's stream: inputs on the device, the commits of every
 // polynomial in lockstep (roots into the proofs), then `committed()` (called exactly once, also
-// on failure), the product sumchecks in lockstep and the openings in lockstep, in two halves on
-// two streams.  Synchronising.
+// on failure), the product sumchecks in lockstep and the openings in lockstep, in `open_parts`
+// parts on as many streams.  Synchronising.
 static int ls_prove_group(const BfTable* tab, const u64 seed[2], int q, const gb_instance* insts,
-                          const std::vector<int>& wave, size_t coop, const std::function<void()>& committed) {
+                          const std::vector<int>& wave, size_t coop, int open_parts,
+                          const std::function<void()>& committed) {
     using namespace host;
     bool signalled = false;
     auto signal = [&] {
@@ -1619,33 +1638,23 @@ static int ls_prove_group(const BfTable* tab, const u64 seed[2], int q, const gb
                 P.push_back(std::move(p));
             }
         }
-        // two halves of the polynomials (alternating in size order, so that both carry about the
-        // same work), each opened by its own runner: the second on a helper thread with its own
-        // stream, so that one half's host round trip between rounds overlaps the other half's
-        // device work
+        // open_parts parts of the polynomials (dealt out in size order, so that each carries about
+        // the same work), each opened by its own runner: part 0 on this thread, the others on
+        // helper threads with streams of their own, so that one part's host round trip between
+        // rounds overlaps the others' device work
         std::vector<size_t> idx(P.size());
         std::iota(idx.begin(), idx.end(), 0);
         std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return P[a].N > P[b].N; });
-        std::vector<LsPoly> A, B;
-        for (size_t k = 0; k < idx.size(); k++) (k % 2 ? B : A).push_back(std::move(P[idx[k]]));
-        if (B.empty()) {
-            LsRunner runner(tab, q, coop);
-            rc = runner.open(A);
-        } else {
-            int rc2 = GB_OK;
-            std::string err2;
-            rc = ls_on_helper_stream(
-                [&] {
-                    LsRunner runner(tab, q, coop);
-                    rc2 = runner.open(B);
-                    if (rc2) err2 = gb_last_error();
-                },
-                [&] {
-                    LsRunner runner(tab, q, coop);
-                    return runner.open(A);
-                },
-                rc2, err2);
-        }
+        const size_t np = std::max<size_t>(1, std::min<size_t>((size_t)open_parts, P.size()));
+        std::vector<std::vector<LsPoly>> part(np);
+        for (size_t k = 0; k < idx.size(); k++) part[k % np].push_back(std::move(P[idx[k]]));
+        std::vector<std::function<int()>> runs;
+        for (size_t k = 0; k < np; k++)
+            runs.push_back([&, k] {
+                LsRunner runner(tab, q, coop);
+                return runner.open(part[k]);
+            });
+        rc = ls_on_streams(runs);
         t_ls_ms[1] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
     }
     if (cws) cudaFreeAsync(cws, s);
@@ -1680,6 +1689,7 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return ls_inst_bytes(insts[a]) > ls_inst_bytes(insts[b]); });
     const size_t coop = gb_get_coop_threshold();  // the 8-lane form below this many parents a layer
+    const int groups = t_ls_groups, open_parts = t_ls_open_parts;
     t_ls_ms[0] = t_ls_ms[1] = t_ls_ms[2] = 0;
     size_t next = 0;
     while (next < order.size()) {
@@ -1690,41 +1700,32 @@ static int lockstep_prove(void* table, const u64 seed[2], int q, const gb_instan
             used += ls_inst_bytes(insts[order[next]]);
             wave.push_back(order[next++]);
         }
-        // Two groups (alternating in size order), staggered: the second group's commits start
-        // once the first group's are done, so they run beside the first group's sumchecks (a chain
-        // of host round trips with little device work), and the first group's openings beside the
-        // second group's sumchecks.  Each group's proofs are those it gives alone.
-        std::vector<int> g1, g2;
-        for (size_t k = 0; k < wave.size(); k++) (k % 2 ? g2 : g1).push_back(wave[k]);
-        int rc = GB_OK;
-        if (g2.empty()) {
-            rc = ls_prove_group(tab, seed, q, insts, g1, coop, [] {});
-        } else {
-            std::mutex mu;
-            std::condition_variable cv;
-            bool committed = false;
-            int rc2 = GB_OK;
-            std::string err2;
-            rc = ls_on_helper_stream(
-                [&] {
+        // `groups` groups (dealt out in size order), staggered: group k + 1's commits start once
+        // group k's are done, so they run beside group k's sumchecks (a chain of host round trips
+        // with little device work), and group k's openings beside group k + 1's sumchecks.  Each
+        // group's proofs are those it gives alone.
+        const int G = std::max(1, std::min(groups, (int)wave.size()));
+        std::vector<std::vector<int>> grp(G);
+        for (size_t k = 0; k < wave.size(); k++) grp[k % G].push_back(wave[k]);
+        std::mutex mu;
+        std::condition_variable cv;
+        int committed = 0;  // groups whose commits are done
+        std::vector<std::function<int()>> parts;
+        for (int k = 0; k < G; k++)
+            parts.push_back([&, k] {
+                if (k > 0) {
+                    std::unique_lock<std::mutex> l(mu);
+                    cv.wait(l, [&] { return committed >= k; });
+                }
+                return ls_prove_group(tab, seed, q, insts, grp[k], coop, open_parts, [&, k] {
                     {
-                        std::unique_lock<std::mutex> l(mu);
-                        cv.wait(l, [&] { return committed; });
+                        std::lock_guard<std::mutex> l(mu);
+                        committed = std::max(committed, k + 1);
                     }
-                    rc2 = ls_prove_group(tab, seed, q, insts, g2, coop, [] {});
-                    if (rc2) err2 = gb_last_error();
-                },
-                [&] {
-                    return ls_prove_group(tab, seed, q, insts, g1, coop, [&] {
-                        {
-                            std::lock_guard<std::mutex> l(mu);
-                            committed = true;
-                        }
-                        cv.notify_all();
-                    });
-                },
-                rc2, err2);
-        }
+                    cv.notify_all();
+                });
+            });
+        const int rc = ls_on_streams(parts);
         if (rc) return rc;
     }
     return GB_OK;
@@ -2346,6 +2347,21 @@ extern "C" {
 int gb_batch_prove_lockstep(void* table, const uint64_t master_seed[2], int num_queries, const gb_instance* insts,
                             int count, int workers, size_t hbm_budget) {
     return lockstep_prove(table, master_seed, num_queries, insts, count, workers, hbm_budget);
+}
+
+int gb_set_lockstep_schedule(int groups, int open_parts) {
+    if (groups < 1 || groups > 8 || open_parts < 1 || open_parts > 8) {
+        set_error_msg("gb_set_lockstep_schedule: groups and open_parts must lie in [1, 8]");
+        return GB_EINVAL;
+    }
+    t_ls_groups = groups;
+    t_ls_open_parts = open_parts;
+    return GB_OK;
+}
+
+void gb_get_lockstep_schedule(int* groups, int* open_parts) {
+    if (groups) *groups = t_ls_groups;
+    if (open_parts) *open_parts = t_ls_open_parts;
 }
 
 void gb_lockstep_last_timing(double* commit_sumcheck_ms, double* open_ms, double* sumcheck_ms) {

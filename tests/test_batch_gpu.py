@@ -175,3 +175,32 @@ def test_lockstep_layer_forms_do_not_change_proofs(tables, coop):
     batch.batch_prove(gt, SEED, together, workers=2, engine="lockstep", coop_threshold=coop)
     for a, b in zip(alone, together):
         assert np.array_equal(a.proof, b.proof)
+
+
+@pytest.mark.parametrize("groups,parts", [(1, 1), (3, 2), (4, 3), (8, 8)])
+def test_lockstep_schedule_does_not_change_proofs(tables, groups, parts):
+    """Staggered groups and open parts (the lockstep autotuner's knobs) leave every proof its
+    alone-run proof, including more groups or parts than there are instances or polynomials; the
+    calling thread's schedule is restored afterwards."""
+    import ctypes
+    from morpheus_gb300 import batch, _native as N
+    gt, _ = tables
+    specs = [(TABLE_NV, 2), (10, 3), (7, 1), (4, 2), (TABLE_NV - 2, 1)]
+    alone = [make(n, d, k, 700 + k) for k, (n, d) in enumerate(specs)]
+    for inst in alone:
+        batch.prove_instance(gt, SEED, inst)
+    together = [make(n, d, k, 700 + k) for k, (n, d) in enumerate(specs)]
+    batch.batch_prove(gt, SEED, together, workers=1, engine="lockstep", groups=groups, open_parts=parts)
+    for a, b in zip(alone, together):
+        assert np.array_equal(a.proof, b.proof)
+    g, p = ctypes.c_int(), ctypes.c_int()
+    N.lib().gb_get_lockstep_schedule(ctypes.byref(g), ctypes.byref(p))
+    assert (g.value, p.value) == (2, 2)
+
+
+def test_lockstep_schedule_rejects_out_of_range(gpu_lib):
+    from morpheus_gb300 import _native as N
+    L = N.lib()
+    for g, p in [(0, 1), (1, 0), (9, 1), (1, 9)]:
+        assert L.gb_set_lockstep_schedule(g, p) == -2
+    assert L.gb_set_lockstep_schedule(2, 2) == 0
