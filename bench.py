@@ -447,16 +447,20 @@ def run_batched(args, summary=False):
         return time.perf_counter() - t0
 
     if getattr(args, "quick", False):
-        # the lockstep engine alone at the settled schedule (for profiling captures)
-        L.gb_set_coop_threshold(4096)
-        for _ in range(args.warmup):
-            batch.batch_prove(table, seed, insts, 16, 160 << 30, engine="lockstep")
-        times = [wall(lambda: batch.batch_prove(table, seed, insts, 16, 160 << 30, engine="lockstep"))
-                 for _ in range(args.steps)]
-        phase = (ctypes.c_double(), ctypes.c_double(), ctypes.c_double())
-        L.gb_lockstep_last_timing(*(ctypes.byref(x) for x in phase))
+        # the lockstep engine alone at the schedule its autotuner settles on for this batch
+        # (3 staggered groups, 2 open parts, cooperative threshold 4096), for profiling captures
+        with batch.Schedule(4096, None, 3, 2):
+            for _ in range(args.warmup):
+                batch.batch_prove(table, seed, insts, 16, 160 << 30, engine="lockstep")
+            l0 = L.gb_launch_count()
+            times = [wall(lambda: batch.batch_prove(table, seed, insts, 16, 160 << 30, engine="lockstep"))
+                     for _ in range(args.steps)]
+            launches = (L.gb_launch_count() - l0) // max(1, args.steps)
+            phase = (ctypes.c_double(), ctypes.c_double(), ctypes.c_double())
+            L.gb_lockstep_last_timing(*(ctypes.byref(x) for x in phase))
         print(json.dumps({"metric": "proofs/sec (mixed batch, lockstep only)", "value": count / statistics.mean(times),
                           "unit": "proofs/s", "instances": count, "ms_per_step": statistics.mean(times) * 1e3,
+                          "gpu_launches": int(launches),
                           "commit_sumcheck_ms": phase[0].value, "open_ms": phase[1].value,
                           "sumcheck_ms": phase[2].value}))
         return
