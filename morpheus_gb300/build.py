@@ -1,11 +1,12 @@
 """In-tree build of the CUDA C-ABI library for sm_103a.
 
 Every ``csrc/*.cu`` is compiled by nvcc in parallel into ``_build/`` and linked
-into ``libmorpheus_gb300.so``.  The two library names the reference crates link
+into ``libmorpheus_gb300.so``; the same objects also go into the static archive
+``libmorpheus_gb300.a``.  The two library names the reference crates link
 (``goldilocks_cuda_wrapper``, ``almost_goldilocks_cuda_wrapper``, see
 goldilocks-cuda-rs/build.rs:157-164 and almost-goldilocks-cuda-rs/build.rs:115-117)
-are provided as symlinks to it, so a crate's ``cargo:rustc-link-lib`` line can
-point at this directory unchanged.
+are provided as symlinks to each, so a crate's ``cargo:rustc-link-lib`` line (static or
+dynamic) can point at this directory unchanged.
 """
 import concurrent.futures as cf
 import glob
@@ -19,6 +20,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmorpheus_gb300.so")
 ALIASES = ["libgoldilocks_cuda_wrapper.so", "libalmost_goldilocks_cuda_wrapper.so"]
+# The same objects as a static archive, under the names the crates link statically
+# (cargo:rustc-link-lib=static=goldilocks_cuda_wrapper beside static=cudart_static, stdc++, dl, rt,
+# pthread: goldilocks-cuda-rs/build.rs:157-168, almost-goldilocks-cuda-rs/build.rs:115-121).
+ARCHIVE = os.path.join(HERE, "libmorpheus_gb300.a")
+ARCHIVE_ALIASES = ["libgoldilocks_cuda_wrapper.a", "libalmost_goldilocks_cuda_wrapper.a"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--default-stream", "per-thread", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
@@ -67,11 +73,19 @@ def build(verbose=False, extra=()):
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{p.stdout}\n{p.stderr}")
-    for alias in ALIASES:
-        path = os.path.join(HERE, alias)
-        if os.path.islink(path) or os.path.exists(path):
-            os.remove(path)
-        os.symlink(os.path.basename(LIB), path)
+    if not os.path.exists(ARCHIVE) or os.path.getmtime(ARCHIVE) < newest:
+        if os.path.exists(ARCHIVE):
+            os.remove(ARCHIVE)
+        ar = shutil.which("ar") or "ar"
+        p = subprocess.run([ar, "rcs", ARCHIVE] + objs, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"ar failed: {p.stdout}\n{p.stderr}")
+    for target, aliases in ((LIB, ALIASES), (ARCHIVE, ARCHIVE_ALIASES)):
+        for alias in aliases:
+            path = os.path.join(HERE, alias)
+            if os.path.islink(path) or os.path.exists(path):
+                os.remove(path)
+            os.symlink(os.path.basename(target), path)
     return LIB
 
 

@@ -63,3 +63,32 @@ def test_built_for_sm103a_only():
 def test_loaded_kernels_are_sm103_binaries(gpu_lib):
     from morpheus_gb300 import _native
     assert _native.lib().gb_binary_version() == 103
+
+
+def test_static_archive_links_with_the_crates_link_line(libpath, tmp_path):
+    """The static archive, under the crates' library names, links a C program that takes the
+    address of every declared function, with the link line the crates' build scripts emit
+    (static=goldilocks_cuda_wrapper, static=cudart_static, stdc++, dl, rt, pthread).  Link only:
+    the program is not run."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cudart = "/usr/local/cuda/lib64/libcudart_static.a"
+    if not cc or not os.path.exists(cudart):
+        pytest.skip("no C compiler or static CUDA runtime")
+    d = os.path.dirname(libpath)
+    for alias in ("libgoldilocks_cuda_wrapper.a", "libalmost_goldilocks_cuda_wrapper.a"):
+        assert os.path.exists(os.path.join(d, alias))
+    names = declared_functions()
+    src = ["#include <stdint.h>", "#include <stddef.h>",
+           '#include "goldilocks_cuda_wrapper.h"', '#include "almost_goldilocks_cuda_wrapper.h"',
+           "void *fns[] = {"] + [f"    (void *)&{n}," for n in names] + [
+           "};", "int main(void) { return fns[0] == 0; }"]
+    c = tmp_path / "link_all.c"
+    c.write_text("\n".join(src) + "\n")
+    for lib in ("goldilocks_cuda_wrapper", "almost_goldilocks_cuda_wrapper"):
+        out = tmp_path / f"link_{lib}"
+        cmd = [cc, str(c), "-I", os.path.join(ROOT, "include"), "-o", str(out), "-L", d, f"-l:lib{lib}.a",
+               "-L", "/usr/local/cuda/lib64", "-lcudart_static", "-lstdc++", "-ldl", "-lrt", "-lpthread"]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        assert p.returncode == 0, p.stderr[-3000:]
