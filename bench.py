@@ -311,17 +311,20 @@ def run_side_workload(args):
         cfg = {"workload": "sumcheck fold round: 2 polys x 2^24 Ext2 folded with an Ext2 challenge to 2 x 2^23, "
                            "next round's degree-2 message", "l2": "flushed between timed launches"}
     else:
-        n_ring, Bw, rows = 1024, 256, 16
+        n_ring, Bw, rows = 1024, args.witnesses, 16
         key = np.array([0x5EED, 1, 2, 3, 4, 5, 6, 7], np.uint32)
         h = ctypes.c_void_p()
         Nn.check(L.gb_ajtai_key_create(key.ctypes.data, 0, rows, n_ring, ctypes.byref(h)), "key")
+        L.gb_ajtai_set_batch_form(args.ajtai_form)
         z = DeviceBuffer.from_numpy(rng.integers(0, 256, size=Bw * n_ring * 64, dtype=np.uint8))
         out = DeviceBuffer(Bw * rows * 64)
 
         def step():
             Nn.check(L.gb_ajtai_commit_u8_batched(h, z.ptr, Bw, out.ptr), "ajtai")
         unit, metric, work = "commitments/s", "ajtai witness commitments/s", float(Bw)
-        cfg = {"workload": "ajtai commit, 256 witnesses x 2^16 coefficients in [0,256), rows 0..15, q = 2^64-2^32-31"}
+        cfg = {"workload": f"ajtai commit, {Bw} witnesses x 2^16 coefficients in [0,256), rows 0..15, "
+                           "q = 2^64-2^32-31", "form": ["by batch size", "witness-circulant", "key-Toeplitz"][args.ajtai_form],
+               "l2": "flushed between timed steps"}
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -352,13 +355,19 @@ def run_side_workload(args):
         # whole batch (digit prep, GEMM, combine) against the HBM bound of the GEMM's operand
         # stream: the key's 8 digit planes (bf16) once, plus the witness digits (bf16)
         peak, src = measured_peaks()
-        op_bytes = 8 * rows * 64 * n_ring * 64 * 2 + Bw * n_ring * 64 * 2
+        circulant = args.ajtai_form == 1 or (args.ajtai_form == 0 and Bw <= 128)
+        if circulant:  # the key's digit planes once (16 MB) plus the witness bytes
+            op_bytes = 8 * rows * n_ring * 64 * 2 + Bw * n_ring * 64
+        else:  # the key's Toeplitz expansion once (1.07 GB) plus the witness digits
+            op_bytes = 8 * rows * 64 * n_ring * 64 * 2 + Bw * n_ring * 64 * 2
         try:
             with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
                 tpeak = json.load(f).get("bf16_tflops", 1900.0)
         except Exception:
             tpeak = 1900.0
-        line["roofline"] = {"bound": "hbm", "kernel": "ajtai_gemm_kernel (whole batch timed)",
+        line["roofline"] = {"bound": "hbm",
+                            "kernel": ("ajtai_gemm_wc_kernel" if circulant else "ajtai_gemm_kernel") +
+                                      " (whole batch timed)",
                             "achieved": op_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                             "frac": op_bytes / (ms * 1e-3) / 1e9 / peak, "peak_source": src,
                             "bytes_per_launch": op_bytes, "tensor_frac": line["tensor_tflops_equiv"] / tpeak,
@@ -380,9 +389,11 @@ def run_side_workload(args):
     print(json.dumps(line))
 
 
-def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):
+def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):  # ev_time flushes L2 before it times
     """Compact line for the Ajtai configuration: the whole 256-witness batch (digit prep, tensor-core
-    GEMM, combine), its tensor and HBM rooflines, and the C restatement on the host cores."""
+    GEMM, combine), its tensor and HBM rooflines, and the C restatement on the host cores; beside
+    it one witness alone (the served jobs' commitment) in both GEMM forms.  L2 flushed before
+    every timed call."""
     n_ring, Bw, rows = 1024, 256, 16
     key = np.array([0x5EED, 1, 2, 3, 4, 5, 6, 7], np.uint32)
     z_host = np.random.default_rng(303).integers(0, 256, size=(Bw, n_ring * 64), dtype=np.uint8)
@@ -390,12 +401,24 @@ def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):
     Nn.check(L.gb_ajtai_key_create(key.ctypes.data, 0, rows, n_ring, ctypes.byref(h)), "ajtai key")
     z = DeviceBuffer.from_numpy(z_host.reshape(-1))
     out = DeviceBuffer(Bw * rows * 64)
+    timed = ev_time  # flushes L2 on the launch stream, then times
     step = lambda: Nn.check(L.gb_ajtai_commit_u8_batched(h, z.ptr, Bw, out.ptr), "ajtai")
     for _ in range(3):
         step()
-    times = [ev_time(step) for _ in range(10)]
+    times = [timed(step) for _ in range(10)]
     ms = statistics.median(times)
     got = out.to_numpy()
+    # one witness: the automatic form (witness-circulant) against the key-Toeplitz form
+    one = {}
+    for name, form in (("auto", 0), ("toeplitz", 2)):
+        old = L.gb_ajtai_set_batch_form(form)
+        step1 = lambda: Nn.check(L.gb_ajtai_commit_u8_batched(h, z.ptr, 1, out.ptr), "ajtai one")
+        for _ in range(3):
+            step1()
+        one[name] = statistics.median(timed(step1) for _ in range(10))
+        one[name + "_out"] = out.to_numpy()[:rows * 64].copy()
+        L.gb_ajtai_set_batch_form(old)
+    assert np.array_equal(one["auto_out"], one["toeplitz_out"]) and np.array_equal(one["auto_out"], got[:rows * 64])
     Nn.check(L.gb_ajtai_key_destroy(h), "ajtai key destroy")
     peaks = {}
     try:
@@ -413,6 +436,10 @@ def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):
                          "peak_source": "measured (bf16 burst)" if peaks else "fallback",
                          "hbm_algorithmic_GB_s": alg_bytes / (ms * 1e-3) / 1e9, "hbm_peak": hpeak,
                          "algorithmic_bytes": alg_bytes},
+            "single_witness": {"ms_witness_circulant": one["auto"], "ms_key_toeplitz": one["toeplitz"],
+                               "identical": True, "note": "one 2^16-coefficient witness, as in a served job; "
+                                                         "the automatic choice takes the witness-circulant "
+                                                         "form up to 128 witnesses"},
             "cpu_baseline": cpu_ajtai_sample(key, z_host[:64], rows, got.reshape(Bw, rows, 64)[:64]),
             "step_ms_all": [round(t, 4) for t in times],
             "workload": "256 witnesses x 2^16 coefficients in [0, 256), rows 0..15 of the ChaCha8 matrix, "
@@ -714,6 +741,9 @@ def main():
                     help="served workload: further offered loads reported beside --rate")
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")
     ap.add_argument("--hbm-budget-gb", type=int, default=96, help="served workload: admission budget")
+    ap.add_argument("--witnesses", type=int, default=256, help="ajtai workload: witnesses per batch (1..256)")
+    ap.add_argument("--ajtai-form", type=int, default=0, choices=[0, 1, 2],
+                    help="ajtai workload: 0 by batch size, 1 witness-circulant GEMM, 2 key-Toeplitz GEMM")
     ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "batch_open", "peval", "ajtai", "batched", "served"],
                     help="basefold (headline): commit+open proofs; sumcheck: 2 x 2^20 product sumcheck; "
                          "fold: one fused fold round over 2 x 2^24 Ext2; "
@@ -864,7 +894,14 @@ def main():
         extras["sumcheck_2x2^20"] = {"ms_per_proof": sc_ms, "melem_per_s": 2 * (1 << 20) / (sc_ms * 1e-3) / 1e6,
                                      "cpu_baseline": cpu_sumcheck_sample(polys_host, sc_out[-1].round_messages)}
         # --- Ajtai commitment at its configuration: 256 witnesses x 2^16 coefficients, rows 0..15
-        extras["ajtai_c3"] = ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+        def ev_time_flushed(fn):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            return ev_time(fn)
+        extras["ajtai_c3"] = ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time_flushed)
+        del flush
         extras["cpu_baseline"] = cpu_baseline_sample(gpu_proof=last[-1][1], seed=1234 + rank)
         # the batched (512 mixed instances) and served (Poisson matmul jobs) configurations, compact
         L.gb_set_stream(None)

@@ -31,8 +31,27 @@ def commit_wide(seed, z_wide, col_offset=0, chunk=None):
     return d_out.to_numpy().reshape(KAPPA, RING_DIM)
 
 
+class batch_form:
+    """Context manager: the calling thread's form of AjtaiKey.commit_u8_batched (0 by batch size,
+    1 witness-circulant GEMM, 2 key-Toeplitz GEMM; gb_ajtai_set_batch_form).  Results never
+    depend on it."""
+
+    def __init__(self, form):
+        self.form = form
+
+    def __enter__(self):
+        self._old = N.lib().gb_ajtai_set_batch_form(self.form)
+        N.check(self._old if self._old < 0 else 0, "gb_ajtai_set_batch_form")
+        return self
+
+    def __exit__(self, *a):
+        N.lib().gb_ajtai_set_batch_form(self._old)
+
+
 class AjtaiKey:
-    """Rows [row_lo, row_lo + rows) of the matrix over n_ring columns, expanded once."""
+    """Rows [row_lo, row_lo + rows) of the matrix over n_ring columns, with both GEMM operands
+    built once: the digit planes (16 MB for 16 rows x 1024 columns) and their Toeplitz expansion
+    (1.07 GB)."""
 
     def __init__(self, seed, row_lo, rows, n_ring):
         self.rows, self.n_ring = rows, n_ring

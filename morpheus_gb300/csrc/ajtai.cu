@@ -5,8 +5,9 @@
 // with M[i][j] drawn by the ChaCha8 PRG keyed by the seed (ajtai_chacha8.cuh:115-178).
 //
 // Batched small-witness path (witness coefficients in [0, 256)): one exact GEMM on the
-// tcgen05 tensor cores.  sm_103a has no integer MMA (ptxas rejects tcgen05 kind::i8), so
-// the contraction runs in bf16 with fp32 accumulation, kept exact by construction:
+// tcgen05 tensor cores, in one of two forms chosen by batch size (below).  sm_103a has no
+// integer MMA (ptxas rejects tcgen05 kind::i8), so the contraction runs in bf16 with fp32
+// accumulation, kept exact by construction:
 //   * every matrix coefficient m is centred (v = m or m - q, |v| < q/2) and split into
 //     8 balanced base-256 digits d_p with |d_p| <= 128 (v = sum_p d_p 256^p);
 //   * witness coefficients are centred, z' = z - 128 in [-128, 127];
@@ -14,9 +15,14 @@
 //     fp32 represents exactly.  The K dimension is cut into 1024-long chunks; after each
 //     chunk the fp32 accumulator (TMEM) is drained into int32 registers (|sum| <= 2^30 over
 //     K = 2^16) while the tensor core fills the other accumulator buffer.
-//   The GEMM is S_p = T_p . Z'^T with T_p the negacyclic Toeplitz expansion of digit p
-//   (rows (p, i, r), columns (j, l)), and c = sum_p 256^p S_p + 128 * rowsum(T) mod q.
-// The digit-expanded matrix is built once per (key, rows, columns) and kept in HBM.
+//   Key-Toeplitz form (large batches): S_p = T_p . Z'^T with T_p the negacyclic Toeplitz
+//   expansion of digit p (rows (p, i, r), columns (j, l)), and c = sum_p 256^p S_p +
+//   128 * rowsum(T) mod q.  M128 x N256 MMAs over every witness of a 256-witness tile; the
+//   1.07 GB expansion (16 rows x 1024 columns) is streamed once per batch whatever its size.
+//   Witness-circulant form (batches up to AJ_WC_MAX_AUTO): the Toeplitz structure on the
+//   witness side (ajtai_gemm_wc_kernel), the key as its plain 16 MB of digit planes; one N = 64
+//   MMA per witness and K step, so the work follows the batch size.
+// Both key operands are built once per (key, rows, columns) and kept in HBM.
 //
 // The full-width entry point ajtai_commit_wide_ffi (arbitrary field coefficients) runs
 // on the CUDA cores with modular multiplications.
@@ -114,6 +120,33 @@ __global__ void __launch_bounds__(64) ajtai_expand_kernel(const u64* __restrict_
             *reinterpret_cast<uint4*>(tile + ((v ^ (R & 7)) << 4)) = *reinterpret_cast<uint4*>(w);
         }
     }
+}
+
+// Key operand of the witness-circulant GEMM: A[m][(j, kappa)] = d_p(M[i][j][63 - kappa]) as bf16,
+// m = 16 p + (i mod 16) in the 128-row tile i / 16, stored tile by tile like ajtai_expand_kernel's
+// output (tile (i / 16, j) 16 KB contiguous at ((i / 16) KT + j) 16 KB, 128-byte swizzled).  Rows
+// of absent ring rows and tiles past the last ring column stay zero.  One block per (i, j):
+// thread k takes the digits of M[i][j][k], then thread (p, c) writes row 16 p + (i mod 16),
+// 16-byte chunk c (kappa = 8c .. 8c + 7).
+__global__ void __launch_bounds__(64) ajtai_planes_kernel(const u64* __restrict__ M, u64 N, size_t KT,
+                                                          __nv_bfloat16* __restrict__ A) {
+    __shared__ short dig[AJ_D][8];
+    const u64 j = blockIdx.x;
+    const int i = blockIdx.y;
+    {
+        int d[8];
+        centred_digits(M[((size_t)i * N + j) * AJ_D + threadIdx.x], d);
+#pragma unroll
+        for (int p = 0; p < 8; p++) dig[threadIdx.x][p] = (short)d[p];
+    }
+    __syncthreads();
+    const int p = threadIdx.x >> 3, c = threadIdx.x & 7;
+    const int R = 16 * p + (i & 15);
+    __align__(16) __nv_bfloat16 w[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) w[e] = __int2bfloat16_rn(dig[63 - (8 * c + e)][p]);
+    uint8_t* tile = reinterpret_cast<uint8_t*>(A) + ((size_t)(i >> 4) * KT + j) * 16384 + (R >> 3) * 1024 + (R & 7) * 128;
+    *reinterpret_cast<uint4*>(tile + ((c ^ (R & 7)) << 4)) = *reinterpret_cast<uint4*>(w);
 }
 
 // rowsum(T)[i][r] mod q = sum_j (2 prefix_r(M_ij) - total(M_ij)), one thread per (i, r)
@@ -469,6 +502,316 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
 }
 
 // ---------------------------------------------------------------------------
+// Witness-circulant tcgen05 GEMM.  The negacyclic structure moves to the witness side:
+//   c_i[r] = sum_j sum_k M_ij[k] s'(r,k) z_j[(r-k) mod 64],   s' = -1 when k > r,
+// so the key operand is the plain digit planes: A rows m = 16 p + (i mod 16) (digit plane p, ring
+// row i; 128 rows per 16 ring rows), K = (j, kappa) with kappa = 63 - k reversed inside each ring
+// column, 16 MB for 16 rows x 1024 columns, read through L2.  Witness z contributes, per ring
+// column j, the 64 x 64 circulant
+//   W[r][kappa] = G[r + kappa - 63],   G[t] = z'[t] (t >= 0), -z'[t + 64] (t < 0),   z' = z - 128.
+// In the K-major no-swizzle layout the 8 x 8 core matrix (rows 8a.., columns 8b..) of W depends
+// only on a + b: its row rho is G[8(a + b) + rho - 63 .. +7].  So W has 15 distinct core matrices,
+// stored 128 bytes apart, and the MMA reads them in place through a descriptor whose leading- and
+// stride-dimension offsets are both 128 bytes: one witness is one N = 64 MMA per K step, 1920
+// bytes of shared memory per ring column instead of 8 KB.  A CTA's N tile is 4 witnesses (256
+// TMEM columns), the accumulator pair fills TMEM.  Exactness as in ajtai_gemm_kernel:
+// |d_p| <= 128, |G| <= 128, fp32 chunks 1024 deep, int32 totals.
+//   warp 0: bulk-copy producer (the stage's key tile; each unit's witness bytes, 1 KB per witness)
+//   warp 1: MMA issuer (one thread)
+//   warps 2..17: build each stage's circulants (one 16-byte core-matrix row per thread) and drain
+//     the accumulators (warp w: TMEM lanes 32 (w % 4) .. +31, the 64 columns of witness (w - 2) / 4)
+// ---------------------------------------------------------------------------
+constexpr int WC_WIT = 4;                  // witnesses per N tile
+constexpr int WC_BN = WC_WIT * AJ_D;       // accumulator columns (witness, r)
+constexpr int WC_STAGES = 8;
+constexpr int WC_LAG = 4;                  // a chunk is drained this many stages into the next one
+static_assert(WC_LAG % 4 == 0 && WC_LAG + 3 < 16, "each build group drains at one of its own stages");
+constexpr int WC_A_BYTES = GM_BM * GM_BK * 2;            // 16 KB key tile
+constexpr int WC_WIN_BYTES = 2048;                       // one circulant: 15 core matrices (1920 B)
+constexpr int WC_ROWS_W = 120;                           // 16-byte core-matrix rows of one circulant
+constexpr int WC_STAGE_BYTES = WC_A_BYTES + WC_WIT * WC_WIN_BYTES;  // 24 KB
+constexpr int WC_ZUNIT = WC_WIT * GM_CHUNK_TILES * AJ_D;  // a unit's witness bytes: 4 KB
+constexpr int WC_BUILDERS = 512;
+constexpr int WC_THREADS = 64 + WC_BUILDERS;
+constexpr int WC_NBAR = 3 * WC_STAGES + 9;
+constexpr int WC_SMEM = WC_STAGES * WC_STAGE_BYTES + 2 * WC_ZUNIT + 1024 /*align*/ + 512 /*barriers*/;
+static_assert(WC_WIT * WC_ROWS_W <= 4 * 128, "four core-matrix rows per thread of a build group");
+// instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 64
+constexpr u32 WC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(AJ_D >> 3) << 17) | ((u32)(GM_BM >> 4) << 24);
+
+// shared-memory descriptor of a circulant: K-major, no swizzle, core matrices 128 bytes apart along
+// both K (leading dimension) and N (stride dimension)
+__device__ __forceinline__ u64 umma_desc_circ(u32 saddr) {
+    u64 d = (u64)((saddr & 0x3FFFF) >> 4);
+    d |= (u64)(128 >> 4) << 16;
+    d |= (u64)(128 >> 4) << 32;
+    d |= (u64)1 << 46;  // descriptor version for tcgen05; layout 0 = no swizzle
+    return d;
+}
+
+__device__ __forceinline__ u32 bf16x2_of(int lo, int hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn((float)lo, (float)hi);  // |lo|, |hi| <= 128: exact
+    return *reinterpret_cast<u32*>(&v);
+}
+
+__global__ void __launch_bounds__(WC_THREADS, 1) ajtai_gemm_wc_kernel(const __nv_bfloat16* __restrict__ A_tiled,
+                                                                      const uint8_t* __restrict__ z, int B, u64 n_ring,
+                                                                      int k_tiles, GmSched sched, int* __restrict__ S,
+                                                                      int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* zs = smem + WC_STAGES * WC_STAGE_BYTES;  // two units' witness bytes
+    uint64_t* bars = (uint64_t*)(zs + 2 * WC_ZUNIT);
+    // bars: full[S] (key tile landed), ready[S] (circulants built), empty[S] (MMAs done with the
+    // stage), zfull[2], zempty[2], acc_full[2], acc_empty[2], mma_done; TMEM base address after them
+    u32* tmem_slot = (u32*)(bars + WC_NBAR);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long u0 = gm_unit_begin(sched, blockIdx.x);
+    const int chunks = (int)(gm_unit_begin(sched, blockIdx.x + 1) - u0);
+    const int T = chunks * GM_CHUNK_TILES;  // this CTA's stages, one ring column each
+    auto unit_tile = [&](int lu) { return (u0 + lu) / sched.chunks; };
+    auto unit_mt = [&](int lu) { return (int)(unit_tile(lu) % sched.tiles_m); };
+    auto unit_b0 = [&](int lu) { return (int)(unit_tile(lu) / sched.tiles_m) * WC_WIT; };
+    auto unit_j0 = [&](int lu) { return (u64)((u0 + lu) % sched.chunks) * GM_CHUNK_TILES; };
+    auto full = [&](int s) { return smem_u32(bars + s); };
+    auto ready = [&](int s) { return smem_u32(bars + WC_STAGES + s); };
+    auto empty = [&](int s) { return smem_u32(bars + 2 * WC_STAGES + s); };
+    auto zfull = [&](int b) { return smem_u32(bars + 3 * WC_STAGES + b); };
+    auto zempty = [&](int b) { return smem_u32(bars + 3 * WC_STAGES + 2 + b); };
+    auto acc_full = [&](int a) { return smem_u32(bars + 3 * WC_STAGES + 4 + a); };
+    auto acc_empty = [&](int a) { return smem_u32(bars + 3 * WC_STAGES + 6 + a); };
+    const u32 mma_done = smem_u32(bars + 3 * WC_STAGES + 8);
+    const unsigned long long lim = sched.spin_limit;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < WC_STAGES; s++) {
+            mbar_init(full(s), 1);
+            mbar_init(ready(s), 4);  // the four warps of the stage's build group
+            mbar_init(empty(s), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(zfull(b), 1);
+            mbar_init(zempty(b), WC_BUILDERS / 32);  // one arrival per warp
+            mbar_init(acc_full(b), 1);
+            mbar_init(acc_empty(b), WC_BUILDERS / 32);
+        }
+        mbar_init(mma_done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const u32 tmem = *(volatile u32*)tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const int my_tiles = sched.starve ? 0 : T;
+            int issued = 0, zissued = 0;
+            size_t a_tile = 0;  // the unit's first key tile
+            for (int kt = 0; kt < my_tiles; kt++) {
+                const int lu = kt / GM_CHUNK_TILES, jl = kt % GM_CHUNK_TILES;
+                if (jl == 0) {  // the unit's witness bytes: 16 ring columns of each valid witness
+                    const int zb = lu & 1;
+                    if (!mbar_wait(zempty(zb), ((lu >> 1) & 1) ^ 1, err, 1, lim)) break;
+                    const int b0 = unit_b0(lu);
+                    const u64 j0 = unit_j0(lu);
+                    a_tile = (size_t)unit_mt(lu) * k_tiles + j0;
+                    const u32 nb = (u32)(min((u64)GM_CHUNK_TILES, n_ring - j0) * AJ_D);
+                    const int nw = min(WC_WIT, B - b0);
+                    mbar_expect_tx(zfull(zb), nb * (u32)nw);
+                    for (int w = 0; w < nw; w++)
+                        bulk_load(smem_u32(zs + zb * WC_ZUNIT + w * (GM_CHUNK_TILES * AJ_D)),
+                                  z + (size_t)(b0 + w) * (n_ring * AJ_D) + j0 * AJ_D, nb, zfull(zb));
+                    zissued = lu + 1;
+                }
+                const int s = kt % WC_STAGES;
+                if (!mbar_wait(empty(s), ((kt / WC_STAGES) & 1) ^ 1, err, 1, lim)) break;
+                mbar_expect_tx(full(s), WC_A_BYTES);
+                bulk_load(smem_u32(smem + s * WC_STAGE_BYTES),
+                          A_tiled + (a_tile + jl) * (WC_A_BYTES / 2), WC_A_BYTES,
+                          full(s));
+                issued = kt + 1;
+            }
+            // copies still in flight land in shared memory before the CTA exits
+            for (int kt = issued - WC_STAGES < 0 ? 0 : issued - WC_STAGES; kt < issued; kt++)
+                mbar_wait(full(kt % WC_STAGES), (kt / WC_STAGES) & 1, err, 5, lim);
+            for (int lu = zissued - 2 < 0 ? 0 : zissued - 2; lu < zissued; lu++)
+                mbar_wait(zfull(lu & 1), (lu >> 1) & 1, err, 5, lim);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            bool ok = true;
+            for (int c = 0; c < chunks && ok; c++) {
+                const int a = c & 1;
+                if (!mbar_wait(acc_empty(a), ((c >> 1) & 1) ^ 1, err, 2, lim)) break;
+                const int nw = min(WC_WIT, B - unit_b0(c));  // the tile's witnesses (>= 1)
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                for (int t = 0; t < GM_CHUNK_TILES; t++) {
+                    const int kt = c * GM_CHUNK_TILES + t, s = kt % WC_STAGES;
+                    const u32 ph = (kt / WC_STAGES) & 1;
+                    if (!mbar_wait(full(s), ph, err, 3, lim) || !mbar_wait(ready(s), ph, err, 3, lim)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const u32 sa = smem_u32(smem + s * WC_STAGE_BYTES);
+                    const u64 adesc = umma_desc_sw128(sa);
+                    // K step k, witness w: 32 bytes along the swizzled key rows, two core matrices
+                    // (256 bytes) along the circulant
+                    auto mma = [&](int k, int w) {
+                        const u32 acc = (t > 0 || k > 0) ? 1u : 0u;
+                        const u64 ad = adesc + (u64)((k * 32) >> 4);
+                        const u64 bd = umma_desc_circ(sa + WC_A_BYTES + w * WC_WIN_BYTES + k * 256);
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                                tmem + (u32)(a * WC_BN + w * AJ_D)),
+                            "l"(ad), "l"(bd), "r"(WC_IDESC), "r"(acc));
+                    };
+                    if (nw == WC_WIT) {  // a full tile: the issue sequence fully unrolled
+#pragma unroll
+                        for (int k = 0; k < GM_BK / 16; k++)
+#pragma unroll
+                            for (int w = 0; w < WC_WIT; w++) mma(k, w);
+                    } else {  // the batch's last tile: its witnesses only
+                        for (int k = 0; k < GM_BK / 16; k++)
+                            for (int w = 0; w < nw; w++) mma(k, w);
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        empty(s)));
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    acc_full(a)));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done));
+            mbar_wait(mma_done, 0, err, 6, lim);
+        }
+    } else {
+        // Group g = (warp - 2) / 4 of four warps (one per TMEM lane quarter) builds the stages
+        // kt = g (mod 4), so that four stages are built at once; every warp also drains its
+        // (lane quarter, witness g) block of the accumulators.
+        const int quarter = warp & 3, g = (warp - 2) >> 2, row = quarter * 32 + lane;
+        // build tasks of this thread: core-matrix rows row + 128 q (q < 4) of the stage's 480; row
+        // crow of witness bw holds entries u .. u + 7 (u = crow + 1) of
+        //   Gs[x] = 128 - z[x] (x < 64),  z[x - 64] - 128 (x >= 64):
+        // bytes z[(u + e) mod 64], the first nneg of them negated.
+        int acc[AJ_D];
+#pragma unroll
+        for (int q = 0; q < AJ_D; q++) acc[q] = 0;
+        auto drain = [&](int c) -> bool {
+            const int a = c & 1;
+            if (!mbar_wait(acc_full(a), (c >> 1) & 1, err, 4, lim)) return false;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const bool live = g < B - unit_b0(c);  // this warp's witness is in the batch (warp-uniform)
+#pragma unroll
+            for (int cb = 0; cb < AJ_D; cb += 8) {
+                if (!live) break;
+                u32 v[8];
+                const u32 taddr = tmem + ((u32)(quarter * 32) << 16) + (u32)(a * WC_BN + g * AJ_D + cb);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                               "=r"(v[7])
+                             : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int e = 0; e < 8; e++) acc[cb + e] += __float2int_rn(__uint_as_float(v[e]));
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty(a));
+            const long long t = unit_tile(c);
+            if (c + 1 == chunks || unit_tile(c + 1) != t) {  // this CTA's last unit of the tile
+                const int k = (int)blockIdx.x - gm_cta_of(sched, t * sched.chunks);
+                int* dst = S + (((size_t)t * sched.slots + k) * GM_BM + row) * WC_BN + g * AJ_D;
+#pragma unroll
+                for (int q = 0; q < AJ_D; q += 4) {
+                    *reinterpret_cast<int4*>(dst + q) = make_int4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
+                    acc[q] = acc[q + 1] = acc[q + 2] = acc[q + 3] = 0;
+                }
+            }
+            return true;
+        };
+        bool ok = true;
+        int ntask = 0;  // core-matrix rows to build per stage in the current unit
+        for (int kt = g; kt < T && ok; kt += 4) {
+            const int lu = kt / GM_CHUNK_TILES, jl = kt % GM_CHUNK_TILES, s = kt % WC_STAGES;
+            if (jl == g) {  // this group's first stage of the unit
+                if (!mbar_wait(zfull(lu & 1), (lu >> 1) & 1, err, 4, lim)) break;
+                ntask = min(WC_WIT, B - unit_b0(lu)) * WC_ROWS_W;  // the tile's witnesses only
+            }
+            // the MMAs of this stage's previous use are done with its circulants
+            if (!mbar_wait(empty(s), ((kt / WC_STAGES) & 1) ^ 1, err, 4, lim)) break;
+            const uint8_t* zu = zs + (lu & 1) * WC_ZUNIT + jl * AJ_D;
+            uint8_t* bst = smem + s * WC_STAGE_BYTES + WC_A_BYTES;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int task = row + 128 * q;
+                if (task >= ntask) continue;
+                const int bw = task / WC_ROWS_W, crow = task - bw * WC_ROWS_W, u = crow + 1;
+                const int w0 = (u >> 3) & 7, nneg = min(8, max(0, 64 - u)), sh = (u & 7) * 8;
+                const uint8_t* zw = zu + bw * (GM_CHUNK_TILES * AJ_D);
+                const u64 lo = *reinterpret_cast<const u64*>(zw + 8 * w0);
+                const u64 hi = *reinterpret_cast<const u64*>(zw + 8 * ((w0 + 1) & 7));
+                const u64 x = sh ? (lo >> sh) | (hi << (64 - sh)) : lo;
+                u32 pk[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int b0 = (int)((x >> (16 * e)) & 255), b1 = (int)((x >> (16 * e + 8)) & 255);
+                    pk[e] = bf16x2_of(2 * e < nneg ? 128 - b0 : b0 - 128, 2 * e + 1 < nneg ? 128 - b1 : b1 - 128);
+                }
+                asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(smem_u32(bst + bw * WC_WIN_BYTES + crow * 16)), "r"(pk[0]),
+                             "r"(pk[1]), "r"(pk[2]), "r"(pk[3])
+                             : "memory");
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // visible to the tensor core
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(ready(s));
+                if (jl >= GM_CHUNK_TILES - 4) mbar_arrive(zempty(lu & 1));  // the group's last stage of the unit
+            }
+            if (jl == WC_LAG + g && lu >= 1 && !drain(lu - 1)) ok = false;
+        }
+        if (ok && chunks > 0) drain(chunks - 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+}
+
+// c[b][i][r] = sum_p 256^p S[16 p + (i mod 16)][(b mod 4) 64 + r] + 128 rowsum[i][r]  mod q,
+// canonical; S summed over the slots of tile (b / 4, i / 16).  One thread per output coefficient,
+// r fastest: the slot reads and the output writes are both contiguous.
+__global__ void __launch_bounds__(256) ajtai_combine_wc_kernel(const int* __restrict__ S, GmSched sched, int rows,
+                                                               int B, const u64* __restrict__ RS,
+                                                               u64* __restrict__ out) {
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int IR = rows * AJ_D;
+    if (t >= (size_t)B * IR) return;
+    const int b = (int)(t / IR), ir = (int)(t % IR), i = ir / AJ_D, r = ir % AJ_D;
+    const long long tile = (long long)(b / WC_WIT) * sched.tiles_m + i / 16;
+    const int c0 = gm_cta_of(sched, tile * sched.chunks);
+    const int ns = gm_cta_of(sched, (tile + 1) * sched.chunks - 1) - c0 + 1;
+    const int* base = S + ((size_t)tile * sched.slots * GM_BM + (i & 15)) * WC_BN + (b % WC_WIT) * AJ_D + r;
+    __int128 acc = 0;
+    for (int p = 7; p >= 0; p--) {
+        long long part = 0;  // |total over the slots| <= 2^30
+        for (int k = 0; k < ns; k++) part += __ldg(base + ((size_t)k * GM_BM + 16 * p) * WC_BN);
+        acc = acc * 256 + (__int128)part;
+    }
+    const __int128 Q = (__int128)AGL_Q;
+    __int128 m = acc % Q;
+    if (m < 0) m += Q;
+    const u64 rs128 = agl_mul(__ldg(RS + ir), 128);
+    out[(size_t)b * IR + ir] = agl_canon(agl_add((u64)m, agl_canon(rs128)));
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 // The driver's tensor-map encoder, resolved at run time so that loading the library
@@ -513,6 +856,7 @@ struct AjtaiKey {
     size_t K = 0, Kp = 0;
     u64* d_M = nullptr;              // [rows][N][64]
     __nv_bfloat16* d_T = nullptr;    // 8 * rows * 64 x Kp, tile by tile (ajtai_expand_kernel)
+    __nv_bfloat16* d_A = nullptr;    // ceil(rows / 16) * 128 x Kp, tile by tile (ajtai_planes_kernel)
     u64* d_RS = nullptr;             // [rows][64]
 };
 
@@ -541,6 +885,13 @@ static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* 
     dim3 g((unsigned)N, (unsigned)rows);
     ajtai_expand_kernel<<<g, 64, 0, s>>>(k->d_M, rows, N, k->Kp / GM_BK, k->d_T);
     GB_LAUNCH_CHECK("ajtai_expand_kernel");
+    {
+        const size_t tiles_m = (size_t)(rows + 15) / 16;
+        GB_CUDA_TRY(cudaMalloc(&k->d_A, tiles_m * GM_BM * k->Kp * 2));
+        GB_CUDA_TRY(cudaMemsetAsync(k->d_A, 0, tiles_m * GM_BM * k->Kp * 2, s));
+        ajtai_planes_kernel<<<g, 64, 0, s>>>(k->d_M, N, k->Kp / GM_BK, k->d_A);
+        GB_LAUNCH_CHECK("ajtai_planes_kernel");
+    }
     ajtai_rowsum_kernel<<<grid_for((size_t)rows * AJ_D, 64), 64, 0, s>>>(k->d_M, rows, N, k->d_RS);
     GB_LAUNCH_CHECK("ajtai_rowsum_kernel");
     cudaFreeAsync(d_key, s);
@@ -551,9 +902,11 @@ static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* 
 static void key_free(AjtaiKey* k) {
     if (k->d_M) cudaFree(k->d_M);
     if (k->d_T) cudaFree(k->d_T);
+    if (k->d_A) cudaFree(k->d_A);
     if (k->d_RS) cudaFree(k->d_RS);
     k->d_M = nullptr;
     k->d_T = nullptr;
+    k->d_A = nullptr;
     k->d_RS = nullptr;
 }
 
@@ -561,8 +914,74 @@ static void key_free(AjtaiKey* k) {
 // limits), so that their bounded waits run out and the call reports it; see gb_ajtai_test_starve.
 static thread_local int t_starve = 0;
 
+// Witness-circulant GEMM: one persistent launch over the (tile, 1024-deep chunk) units, tile =
+// (4 witnesses, 16 ring rows), then the combine.
+static int commit_batch_wc(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
+    cudaStream_t s = stream();
+    GmSched sched;
+    sched.tiles_m = (k->rows + 15) / 16;
+    sched.chunks = (int)(k->Kp / ((size_t)GM_BK * GM_CHUNK_TILES));
+    const long long tiles = (long long)sched.tiles_m * ((B + WC_WIT - 1) / WC_WIT);
+    sched.units = tiles * sched.chunks;
+    sched.ctas = (int)std::min<long long>(num_sms(), sched.units);
+    sched.slots = 1;
+    sched.starve = t_starve;
+    sched.spin_limit = t_starve ? GM_SPIN_LIMIT_TEST : GM_SPIN_LIMIT;
+    for (long long t = 0; t < tiles; t++)
+        sched.slots = std::max(sched.slots, gm_cta_of(sched, (t + 1) * sched.chunks - 1) -
+                                                gm_cta_of(sched, t * sched.chunks) + 1);
+    const size_t s_ints = (size_t)tiles * sched.slots * GM_BM * WC_BN;
+    uint8_t* zal = nullptr;
+    int* S = nullptr;
+    int* err = nullptr;
+    if ((uintptr_t)d_z & 15) {  // the bulk copies read 16-byte aligned rows: realign the batch once
+        GB_CUDA_TRY(cudaMallocAsync(&zal, (size_t)B * k->K, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(zal, d_z, (size_t)B * k->K, cudaMemcpyDeviceToDevice, s));
+        d_z = zal;
+    }
+    GB_CUDA_TRY(cudaMallocAsync(&S, s_ints * 4, s));
+    GB_CUDA_TRY(cudaMallocAsync(&err, 4, s));
+    GB_CUDA_TRY(cudaMemsetAsync(err, 0, 4, s));
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(ajtai_gemm_wc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, WC_SMEM);
+        attr = true;
+    }
+    ajtai_gemm_wc_kernel<<<sched.ctas, WC_THREADS, WC_SMEM, s>>>(k->d_A, d_z, B, k->N, (int)(k->Kp / GM_BK), sched,
+                                                                S, err);
+    int rc = check_launch("ajtai_gemm_wc_kernel");
+    if (!rc) {
+        ajtai_combine_wc_kernel<<<grid_for((size_t)B * k->rows * AJ_D, 256), 256, 0, s>>>(S, sched, k->rows, B,
+                                                                                       k->d_RS, d_out);
+        rc = check_launch("ajtai_combine_wc_kernel");
+    }
+    int h_err = 0;
+    if (!rc) {
+        cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) rc = GB_ECUDA;
+    }
+    if (zal) cudaFreeAsync(zal, s);
+    cudaFreeAsync(S, s);
+    cudaFreeAsync(err, s);
+    if (!rc && h_err) {
+        set_error_msg("ajtai_gemm_wc_kernel: pipeline wait timed out (code " + std::to_string(h_err) + ")");
+        rc = GB_ECUDA;
+    }
+    return rc;
+}
+
+// Form of the calling thread's batched commitments (gb_ajtai_set_batch_form): 0 by batch size,
+// 1 the witness-circulant GEMM, 2 the key-Toeplitz GEMM.  Results never depend on it.
+static thread_local int t_batch_form = 0;
+// Largest batch that the automatic choice gives the witness-circulant GEMM.  Its work grows with
+// the batch (one N = 64 MMA per witness and K step), while the key-Toeplitz GEMM streams the
+// 1.07 GB key expansion whatever the batch.
+constexpr int AJ_WC_MAX_AUTO = 128;
+
 static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     if (B < 1) return GB_EINVAL;
+    const int form = t_batch_form ? t_batch_form : (B <= AJ_WC_MAX_AUTO ? 1 : 2);
+    if (form == 1) return commit_batch_wc(k, d_z, B, d_out);
     cudaStream_t s = stream();
     const int Bp = (int)round_up((size_t)B, GM_BN);
     const size_t Mrows = (size_t)8 * k->rows * AJ_D;
@@ -1002,6 +1421,16 @@ int gb_ajtai_commit_u8_batched(void* handle, const uint8_t* d_z, int num_witness
     AjtaiKey* k = (AjtaiKey*)handle;
     if (!k || !d_z || !d_out) return GB_EINVAL;
     return commit_batch(k, d_z, num_witnesses, d_out);
+}
+
+int gb_ajtai_set_batch_form(int form) {
+    if (form < 0 || form > 2) {
+        set_error_msg("gb_ajtai_set_batch_form: form must be 0 (by batch size), 1 or 2");
+        return GB_EINVAL;
+    }
+    const int old = t_batch_form;
+    t_batch_form = form;
+    return old;
 }
 
 int gb_ajtai_test_starve(int on) {

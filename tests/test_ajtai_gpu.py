@@ -8,6 +8,14 @@ Q = O.Q_AGL
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=[1, 2], ids=["circulant", "toeplitz"])
+def form(request, gpu_lib):
+    """Runs the test once with each tensor-core form of the batched commitment."""
+    from morpheus_gb300.ajtai import batch_form
+    with batch_form(request.param):
+        yield request.param
+
+
 def test_commit_wide_matches_reference(gpu_lib, golden):
     from morpheus_gb300 import ajtai
     g = golden["ajtai_commit_wide_ref"]
@@ -44,7 +52,7 @@ def test_commit_wide_rejects_unsupported_chunk(gpu_lib):
         assert N.lib().ajtai_commit_wide_ffi(None, None, 1, 0, chunk, None) == -3
 
 
-def test_batched_matches_reference(gpu_lib, golden):
+def test_batched_matches_reference(gpu_lib, form, golden):
     from morpheus_gb300.ajtai import AjtaiKey
     g = golden["ajtai_commit_u8_ref"]
     k = AjtaiKey(g["key"], 0, g["rows"], g["N"])
@@ -56,7 +64,7 @@ def test_batched_matches_reference(gpu_lib, golden):
 # persistent schedule (1 row x 1024 ring columns: 38 slots), two witness tiles (B > 256) and K padding
 @pytest.mark.parametrize("n_ring,B,row_lo,rows", [(16, 3, 0, 16), (40, 5, 0, 16), (8, 130, 3, 2), (33, 1, 40, 2),
                                                   (1024, 2, 0, 1), (64, 300, 5, 1)])
-def test_batched_vs_oracle(gpu_lib, n_ring, B, row_lo, rows):
+def test_batched_vs_oracle(gpu_lib, form, n_ring, B, row_lo, rows):
     from morpheus_gb300.ajtai import AjtaiKey
     key = np.array([9, 8, 7, 6, 5, 4, 3, 2], np.uint32)
     z8 = np.random.default_rng(n_ring + B).integers(0, 256, size=(B, n_ring * 64), dtype=np.uint8)
@@ -67,7 +75,7 @@ def test_batched_vs_oracle(gpu_lib, n_ring, B, row_lo, rows):
     assert np.array_equal(out[pick], ref)
 
 
-def test_batched_extremes_and_batch_invariance(gpu_lib):
+def test_batched_extremes_and_batch_invariance(gpu_lib, form):
     from morpheus_gb300.ajtai import AjtaiKey
     key = np.array([1, 2, 3, 4, 5, 6, 7, 8], np.uint32)
     n_ring = 32
@@ -85,7 +93,7 @@ def test_batched_extremes_and_batch_invariance(gpu_lib):
     assert np.array_equal(out2, out[[2, 3, 1]])
 
 
-def test_batched_unaligned_witness_pointer(gpu_lib):
+def test_batched_unaligned_witness_pointer(gpu_lib, form):
     """A witness array that is not 8-byte aligned takes the one-coefficient-per-thread prep."""
     import ctypes
     from morpheus_gb300.ajtai import AjtaiKey
@@ -106,7 +114,7 @@ def test_batched_unaligned_witness_pointer(gpu_lib):
     assert np.array_equal(out[[0, 2]], O.ajtai_commit_u8_batch(key, z8[[0, 2]], row_lo=0, nrows=2))
 
 
-def test_batched_equals_wide_rows(gpu_lib):
+def test_batched_equals_wide_rows(gpu_lib, form):
     from morpheus_gb300 import ajtai
     key = np.array([11, 22, 33, 44, 55, 66, 77, 88], np.uint32)
     n_ring = 16
@@ -116,7 +124,7 @@ def test_batched_equals_wide_rows(gpu_lib):
         assert np.array_equal(out[b], ajtai.commit_wide(key, z8[b].astype(np.uint64)))
 
 
-def test_full_size_config(gpu_lib):
+def test_full_size_config(gpu_lib, form):
     """16 rows x 2^16 coefficients (1024 ring columns), 256 witnesses in [0, 256)."""
     from morpheus_gb300.ajtai import AjtaiKey
     key = np.array([0xC0FFEE, 1, 2, 3, 4, 5, 6, 7], np.uint32)
@@ -206,7 +214,7 @@ def test_ternary_and_sparse_vs_oracle(gpu_lib):
     assert L.ajtai_commit_sparse_ffi(d_key.ptr, d_p.ptr, 0, 64, d_out.ptr) == 0 and not d_out.to_numpy().any()
 
 
-def test_gemm_bounded_waits_time_out_and_the_context_recovers(gpu_lib):
+def test_gemm_bounded_waits_time_out_and_the_context_recovers(gpu_lib, form):
     """The tensor-core GEMM's mbarrier waits are bounded.  In the starved test mode the producer
     issues no operand loads, so the MMA and epilogue waits can only run out: the call must return
     -1 with the wait's code in gb_last_error(), and the next normal call on the same context must
@@ -230,3 +238,28 @@ def test_gemm_bounded_waits_time_out_and_the_context_recovers(gpu_lib):
         assert L.gb_ajtai_test_starve(old) == 1
     for _ in range(2):
         assert np.array_equal(k.commit_u8_batched(z8), want)
+
+
+@pytest.mark.parametrize("B", [1, 4, 5, 128, 129, 300])
+def test_batch_forms_agree(gpu_lib, B):
+    """Both tensor-core forms and the automatic choice (witness-circulant up to 128 witnesses) give
+    the same commitments, on either side of the threshold and over several witness tiles."""
+    from morpheus_gb300.ajtai import AjtaiKey, batch_form
+    key = np.array([2, 7, 1, 8, 2, 8, 1, 8], np.uint32)
+    n_ring = 48
+    z8 = np.random.default_rng(B).integers(0, 256, size=(B, n_ring * 64), dtype=np.uint8)
+    k = AjtaiKey(key, 1, 16, n_ring)
+    outs = []
+    for f in (0, 1, 2):
+        with batch_form(f):
+            outs.append(k.commit_u8_batched(z8))
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
+    pick = sorted({0, B - 1})
+    assert np.array_equal(outs[0][pick], O.ajtai_commit_u8_batch(key, z8[pick], row_lo=1, nrows=16))
+
+
+def test_batch_form_rejects_out_of_range(gpu_lib):
+    from morpheus_gb300 import _native as N
+    L = N.lib()
+    assert L.gb_ajtai_set_batch_form(3) == -2 and L.gb_ajtai_set_batch_form(-1) == -2
+    assert L.gb_ajtai_set_batch_form(0) == 0
