@@ -38,6 +38,8 @@
 #include "agl.cuh"
 #include "common.cuh"
 
+extern "C" const char* gb_last_error(void);  // the calling thread's message (runtime.cu)
+
 namespace gb {
 
 constexpr int AJ_D = 64;
@@ -855,9 +857,13 @@ struct AjtaiKey {
     u64 N = 0;        // ring columns
     size_t K = 0, Kp = 0;
     u64* d_M = nullptr;              // [rows][N][64]
-    __nv_bfloat16* d_T = nullptr;    // 8 * rows * 64 x Kp, tile by tile (ajtai_expand_kernel)
+    __nv_bfloat16* d_T = nullptr;    // 8 * rows * 64 x Kp, tile by tile (ajtai_expand_kernel); built
+                                     // by the first batch that takes the key-Toeplitz form
     __nv_bfloat16* d_A = nullptr;    // ceil(rows / 16) * 128 x Kp, tile by tile (ajtai_planes_kernel)
     u64* d_RS = nullptr;             // [rows][64]
+    std::once_flag t_once;           // the expansion's one build (any thread may commit)
+    int t_rc = GB_OK;                // its outcome
+    std::string t_err;
 };
 
 static size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
@@ -871,20 +877,15 @@ static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* 
     k->N = N;
     k->K = (size_t)N * AJ_D;
     k->Kp = round_up(k->K, (size_t)GM_BK * GM_CHUNK_TILES);
-    const size_t Mrows = (size_t)8 * rows * AJ_D;
     u32* d_key = nullptr;
     GB_CUDA_TRY(cudaMalloc(&k->d_M, (size_t)rows * N * AJ_D * 8));
-    GB_CUDA_TRY(cudaMalloc(&k->d_T, Mrows * k->Kp * 2));
     GB_CUDA_TRY(cudaMalloc(&k->d_RS, (size_t)rows * AJ_D * 8));
     GB_CUDA_TRY(cudaMallocAsync(&d_key, 32, s));
     GB_CUDA_TRY(cudaMemcpyAsync(d_key, h_seed, 32, cudaMemcpyHostToDevice, s));
     size_t tasks = (size_t)rows * N * 8;
     ajtai_prg_kernel<<<grid_for(tasks, 256), 256, 0, s>>>(d_key, row_lo, rows, 0, N, k->d_M);
     GB_LAUNCH_CHECK("ajtai_prg_kernel");
-    if (k->Kp > k->K) GB_CUDA_TRY(cudaMemsetAsync(k->d_T, 0, Mrows * k->Kp * 2, s));  // the padding tiles
     dim3 g((unsigned)N, (unsigned)rows);
-    ajtai_expand_kernel<<<g, 64, 0, s>>>(k->d_M, rows, N, k->Kp / GM_BK, k->d_T);
-    GB_LAUNCH_CHECK("ajtai_expand_kernel");
     {
         const size_t tiles_m = (size_t)(rows + 15) / 16;
         GB_CUDA_TRY(cudaMalloc(&k->d_A, tiles_m * GM_BM * k->Kp * 2));
@@ -897,6 +898,33 @@ static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* 
     cudaFreeAsync(d_key, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     return GB_OK;
+}
+
+// The key-Toeplitz form's operand: the digit-expanded Toeplitz matrix of the key's rows, 1.07 GB
+// for 16 rows x 1024 ring columns.  Built once, on the calling thread's stream, by the first batch
+// that needs it; later calls (from any thread) wait for that build and reuse it.
+static int key_expand(AjtaiKey* k) {
+    std::call_once(k->t_once, [k] {
+        cudaStream_t s = stream();
+        const size_t bytes = (size_t)8 * k->rows * AJ_D * k->Kp * 2;
+        int rc = GB_OK;
+        cudaError_t e = cudaMalloc(&k->d_T, bytes);
+        if (e == cudaSuccess && k->Kp > k->K) e = cudaMemsetAsync(k->d_T, 0, bytes, s);  // the padding tiles
+        if (e == cudaSuccess) {
+            dim3 g((unsigned)k->N, (unsigned)k->rows);
+            ajtai_expand_kernel<<<g, 64, 0, s>>>(k->d_M, k->rows, k->N, k->Kp / GM_BK, k->d_T);
+            rc = check_launch("ajtai_expand_kernel");
+            if (!rc) e = cudaStreamSynchronize(s);
+        }
+        if (e != cudaSuccess) {
+            set_error("ajtai key expansion", e);
+            rc = GB_ECUDA;
+        }
+        k->t_rc = rc;
+        if (rc) k->t_err = gb_last_error();
+    });
+    if (k->t_rc) set_error_msg(k->t_err);
+    return k->t_rc;
 }
 
 static void key_free(AjtaiKey* k) {
@@ -916,7 +944,7 @@ static thread_local int t_starve = 0;
 
 // Witness-circulant GEMM: one persistent launch over the (tile, 1024-deep chunk) units, tile =
 // (4 witnesses, 16 ring rows), then the combine.
-static int commit_batch_wc(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
+static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     cudaStream_t s = stream();
     GmSched sched;
     sched.tiles_m = (k->rows + 15) / 16;
@@ -978,10 +1006,11 @@ static thread_local int t_batch_form = 0;
 // 1.07 GB key expansion whatever the batch.
 constexpr int AJ_WC_MAX_AUTO = 128;
 
-static int commit_batch(const AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
+static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     if (B < 1) return GB_EINVAL;
     const int form = t_batch_form ? t_batch_form : (B <= AJ_WC_MAX_AUTO ? 1 : 2);
     if (form == 1) return commit_batch_wc(k, d_z, B, d_out);
+    if (int rc = key_expand(k)) return rc;
     cudaStream_t s = stream();
     const int Bp = (int)round_up((size_t)B, GM_BN);
     const size_t Mrows = (size_t)8 * k->rows * AJ_D;

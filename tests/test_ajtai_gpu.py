@@ -263,3 +263,32 @@ def test_batch_form_rejects_out_of_range(gpu_lib):
     L = N.lib()
     assert L.gb_ajtai_set_batch_form(3) == -2 and L.gb_ajtai_set_batch_form(-1) == -2
     assert L.gb_ajtai_set_batch_form(0) == 0
+
+
+def test_key_expansion_is_built_on_first_large_batch(gpu_lib):
+    """A key that only ever commits small batches holds its 16 MB of digit planes, not the 1.07 GB
+    Toeplitz expansion; the first batch in the key-Toeplitz form builds the expansion, and both
+    forms stay bit-exact around it."""
+    import ctypes
+    from morpheus_gb300 import _native as N
+    from morpheus_gb300.ajtai import AjtaiKey, batch_form
+    L = N.lib()
+
+    def free_bytes():
+        f, t = ctypes.c_size_t(), ctypes.c_size_t()
+        assert L.cuda_mem_get_info(ctypes.byref(f), ctypes.byref(t)) == 0
+        return f.value
+
+    key = np.array([4, 4, 2, 2, 1, 1, 0, 7], np.uint32)
+    z8 = np.random.default_rng(77).integers(0, 256, size=(3, 1024 * 64), dtype=np.uint8)
+    want = O.ajtai_commit_u8_batch(key, z8[:1], 0, 16)
+    f0 = free_bytes()
+    k = AjtaiKey(key, 0, 16, 1024)
+    assert np.array_equal(k.commit_u8_batched(z8[:1]), want)
+    assert f0 - free_bytes() < (512 << 20)
+    with batch_form(2):
+        out = k.commit_u8_batched(z8)
+    assert f0 - free_bytes() > (1 << 30)
+    assert np.array_equal(out[:1], want)
+    with batch_form(1):
+        assert np.array_equal(k.commit_u8_batched(z8), out)
