@@ -165,7 +165,7 @@ int gb_ajtai_key_info(void *handle, int *row_lo, int *rows, uint64_t *n_ring);
 int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses, uint64_t *d_out);
 /* Form of the calling thread's gb_ajtai_commit_u8_batched calls (no reference counterpart):
  * 0 chooses by batch size (the default), 1 the witness-circulant tensor-core GEMM (work
- * proportional to the batch; the automatic choice up to 128 witnesses), 2 the key-Toeplitz
+ * proportional to the batch; the automatic choice up to 192 witnesses), 2 the key-Toeplitz
  * tensor-core GEMM (streams the key's 1.07 GB expansion once per batch of up to 256 witnesses).
  * Results never depend on it.  Returns the previous form, or -2 for a form outside 0..2. */
 int gb_ajtai_set_batch_form(int form);

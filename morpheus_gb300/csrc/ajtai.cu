@@ -519,7 +519,9 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
 // TMEM columns), the accumulator pair fills TMEM.  Exactness as in ajtai_gemm_kernel:
 // |d_p| <= 128, |G| <= 128, fp32 chunks 1024 deep, int32 totals.
 //   warp 0: bulk-copy producer (the stage's key tile; each unit's witness bytes, 1 KB per witness)
-//   warp 1: MMA issuer (one thread)
+//   warps 1 and 18: MMA issuers (one thread each), witnesses 0-1 and 2-3 of the tile.  An N = 64
+//     MMA costs its issuing thread about 100 cycles, three times its tensor work, so two issuers
+//     (measured: 0.35 against 0.44 ms for 256 witnesses; four: 0.33 ms, with register spills)
 //   warps 2..17: build each stage's circulants (one 16-byte core-matrix row per thread) and drain
 //     the accumulators (warp w: TMEM lanes 32 (w % 4) .. +31, the 64 columns of witness (w - 2) / 4)
 // ---------------------------------------------------------------------------
@@ -534,8 +536,9 @@ constexpr int WC_ROWS_W = 120;                           // 16-byte core-matrix 
 constexpr int WC_STAGE_BYTES = WC_A_BYTES + WC_WIT * WC_WIN_BYTES;  // 24 KB
 constexpr int WC_ZUNIT = WC_WIT * GM_CHUNK_TILES * AJ_D;  // a unit's witness bytes: 4 KB
 constexpr int WC_BUILDERS = 512;
-constexpr int WC_THREADS = 64 + WC_BUILDERS;
-constexpr int WC_NBAR = 3 * WC_STAGES + 9;
+constexpr int WC_ISSUERS = 2;  // MMA-issuing warps (1 and 18), two witnesses each
+constexpr int WC_THREADS = 64 + WC_BUILDERS + 32 * (WC_ISSUERS - 1);
+constexpr int WC_NBAR = 3 * WC_STAGES + 8 + WC_ISSUERS;
 constexpr int WC_SMEM = WC_STAGES * WC_STAGE_BYTES + 2 * WC_ZUNIT + 1024 /*align*/ + 512 /*barriers*/;
 static_assert(WC_WIT * WC_ROWS_W <= 4 * 128, "four core-matrix rows per thread of a build group");
 // instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 64
@@ -565,7 +568,8 @@ __global__ void __launch_bounds__(WC_THREADS, 1) ajtai_gemm_wc_kernel(const __nv
     uint8_t* zs = smem + WC_STAGES * WC_STAGE_BYTES;  // two units' witness bytes
     uint64_t* bars = (uint64_t*)(zs + 2 * WC_ZUNIT);
     // bars: full[S] (key tile landed), ready[S] (circulants built), empty[S] (MMAs done with the
-    // stage), zfull[2], zempty[2], acc_full[2], acc_empty[2], mma_done; TMEM base address after them
+    // stage, one arrival per issuer), zfull[2], zempty[2], acc_full[2] (one arrival per issuer),
+    // acc_empty[2], mma_done[issuers]; TMEM base address after them
     u32* tmem_slot = (u32*)(bars + WC_NBAR);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long u0 = gm_unit_begin(sched, blockIdx.x);
@@ -582,22 +586,22 @@ __global__ void __launch_bounds__(WC_THREADS, 1) ajtai_gemm_wc_kernel(const __nv
     auto zempty = [&](int b) { return smem_u32(bars + 3 * WC_STAGES + 2 + b); };
     auto acc_full = [&](int a) { return smem_u32(bars + 3 * WC_STAGES + 4 + a); };
     auto acc_empty = [&](int a) { return smem_u32(bars + 3 * WC_STAGES + 6 + a); };
-    const u32 mma_done = smem_u32(bars + 3 * WC_STAGES + 8);
+    auto mma_done = [&](int q) { return smem_u32(bars + 3 * WC_STAGES + 8 + q); };
     const unsigned long long lim = sched.spin_limit;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < WC_STAGES; s++) {
             mbar_init(full(s), 1);
             mbar_init(ready(s), 4);  // the four warps of the stage's build group
-            mbar_init(empty(s), 1);
+            mbar_init(empty(s), WC_ISSUERS);
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(zfull(b), 1);
             mbar_init(zempty(b), WC_BUILDERS / 32);  // one arrival per warp
-            mbar_init(acc_full(b), 1);
+            mbar_init(acc_full(b), WC_ISSUERS);
             mbar_init(acc_empty(b), WC_BUILDERS / 32);
         }
-        mbar_init(mma_done, 1);
+        for (int q = 0; q < WC_ISSUERS; q++) mbar_init(mma_done(q), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -644,13 +648,15 @@ __global__ void __launch_bounds__(WC_THREADS, 1) ajtai_gemm_wc_kernel(const __nv
             for (int lu = zissued - 2 < 0 ? 0 : zissued - 2; lu < zissued; lu++)
                 mbar_wait(zfull(lu & 1), (lu >> 1) & 1, err, 5, lim);
         }
-    } else if (warp == 1) {
+    } else if (warp == 1 || warp == 18) {
+        const int iss = warp == 1 ? 0 : 1;  // issues the MMAs of witnesses 2 iss, 2 iss + 1
         if (lane == 0) {
             bool ok = true;
             for (int c = 0; c < chunks && ok; c++) {
                 const int a = c & 1;
                 if (!mbar_wait(acc_empty(a), ((c >> 1) & 1) ^ 1, err, 2, lim)) break;
-                const int nw = min(WC_WIT, B - unit_b0(c));  // the tile's witnesses (>= 1)
+                // this issuer's witnesses of the tile: [w_lo, w_hi), possibly none in the last tile
+                const int w_lo = 2 * iss, w_hi = min(min(WC_WIT, B - unit_b0(c)), w_lo + 2);
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 for (int t = 0; t < GM_CHUNK_TILES; t++) {
                     const int kt = c * GM_CHUNK_TILES + t, s = kt % WC_STAGES;
@@ -674,14 +680,15 @@ __global__ void __launch_bounds__(WC_THREADS, 1) ajtai_gemm_wc_kernel(const __nv
                                 tmem + (u32)(a * WC_BN + w * AJ_D)),
                             "l"(ad), "l"(bd), "r"(WC_IDESC), "r"(acc));
                     };
-                    if (nw == WC_WIT) {  // a full tile: the issue sequence fully unrolled
+                    if (w_hi == w_lo + 2) {  // both witnesses: the issue sequence fully unrolled
 #pragma unroll
-                        for (int k = 0; k < GM_BK / 16; k++)
+                        for (int k = 0; k < GM_BK / 16; k++) {
+                            mma(k, w_lo);
+                            mma(k, w_lo + 1);
+                        }
+                    } else if (w_hi > w_lo) {
 #pragma unroll
-                            for (int w = 0; w < WC_WIT; w++) mma(k, w);
-                    } else {  // the batch's last tile: its witnesses only
-                        for (int k = 0; k < GM_BK / 16; k++)
-                            for (int w = 0; w < nw; w++) mma(k, w);
+                        for (int k = 0; k < GM_BK / 16; k++) mma(k, w_lo);
                     }
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                         empty(s)));
@@ -690,8 +697,9 @@ __global__ void __launch_bounds__(WC_THREADS, 1) ajtai_gemm_wc_kernel(const __nv
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                     acc_full(a)));
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done));
-            mbar_wait(mma_done, 0, err, 6, lim);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                mma_done(iss)));
+            mbar_wait(mma_done(iss), 0, err, 6, lim);
         }
     } else {
         // Group g = (warp - 2) / 4 of four warps (one per TMEM lane quarter) builds the stages
@@ -1004,7 +1012,7 @@ static thread_local int t_batch_form = 0;
 // Largest batch that the automatic choice gives the witness-circulant GEMM.  Its work grows with
 // the batch (one N = 64 MMA per witness and K step), while the key-Toeplitz GEMM streams the
 // 1.07 GB key expansion whatever the batch.
-constexpr int AJ_WC_MAX_AUTO = 128;
+constexpr int AJ_WC_MAX_AUTO = 192;
 
 static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     if (B < 1) return GB_EINVAL;

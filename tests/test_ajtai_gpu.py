@@ -240,9 +240,9 @@ def test_gemm_bounded_waits_time_out_and_the_context_recovers(gpu_lib, form):
         assert np.array_equal(k.commit_u8_batched(z8), want)
 
 
-@pytest.mark.parametrize("B", [1, 4, 5, 128, 129, 300])
+@pytest.mark.parametrize("B", [1, 4, 5, 6, 192, 193, 300])
 def test_batch_forms_agree(gpu_lib, B):
-    """Both tensor-core forms and the automatic choice (witness-circulant up to 128 witnesses) give
+    """Both tensor-core forms and the automatic choice (witness-circulant up to 192 witnesses) give
     the same commitments, on either side of the threshold and over several witness tiles."""
     from morpheus_gb300.ajtai import AjtaiKey, batch_form
     key = np.array([2, 7, 1, 8, 2, 8, 1, 8], np.uint32)
