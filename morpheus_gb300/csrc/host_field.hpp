@@ -86,6 +86,12 @@ inline u64 red128(u128 x) {  // any 128-bit value -> a u64 congruent to it
 }
 inline u64 mulr(u64 a, u64 b) { return red128((u128)a * b); }
 
+// x + c for any u64 x and c < p: on a carry the wrapped sum is below c, and 2^64 == EPS (mod p)
+inline u64 add_rc(u64 x, u64 c) {
+    const u64 s = x + c;
+    return s + (((u64)0 - (u64)(s < c)) & GL_EPS);
+}
+
 inline void p2_permute(u64 s[8]) {
     auto sbox = [](u64 x) {
         const u64 x2 = mulr(x, x), x4 = mulr(x2, x2), x3 = mulr(x2, x);
@@ -109,17 +115,26 @@ inline void p2_permute(u64 s[8]) {
         }
     };
     for (int r = 0; r < 4; r++) {
-        for (int i = 0; i < 8; i++) s[i] = sbox(red128((u128)s[i] + P2Const::ext[r][i]));
+        for (int i = 0; i < 8; i++) s[i] = sbox(add_rc(s[i], P2Const::ext[r][i]));
         ext(s);
     }
+    // Internal round: x = s0 + rc, tot = x^7 + s1 + .. + s7, s_i' = s_i d_i + tot.  Lane 0 is the
+    // round's dependency chain, so s0' = x^7 (d0 + 1) + (s1 + .. + s7) is formed as
+    // x4 * (x2 * (x (d0 + 1))): three dependent multiplications from x instead of four.  The host
+    // transcript's permutations run back to back between rounds, so this chain is their latency.
+    static_assert(P2Const::diag[0] + 1 < GL_P, "d0 + 1 is a canonical constant");
+    const u64 d0p1 = P2Const::diag[0] + 1;
     for (int r = 0; r < 22; r++) {
-        s[0] = sbox(red128((u128)s[0] + P2Const::inner[r]));
-        u128 sum = 0;
-        for (int i = 0; i < 8; i++) sum += s[i];
-        for (int i = 0; i < 8; i++) s[i] = red128((u128)s[i] * P2Const::diag[i] + sum);
+        const u128 rest = (u128)s[1] + s[2] + s[3] + s[4] + s[5] + s[6] + s[7];
+        const u64 x = add_rc(s[0], P2Const::inner[r]);
+        const u64 x2 = mulr(x, x), xc = mulr(x, d0p1);
+        const u64 x4 = mulr(x2, x2), x3 = mulr(x2, x), x3c = mulr(x2, xc);
+        const u128 tot = rest + mulr(x4, x3);
+        s[0] = red128((u128)x4 * x3c + rest);
+        for (int i = 1; i < 8; i++) s[i] = red128((u128)s[i] * P2Const::diag[i] + tot);
     }
     for (int r = 4; r < 8; r++) {
-        for (int i = 0; i < 8; i++) s[i] = sbox(red128((u128)s[i] + P2Const::ext[r][i]));
+        for (int i = 0; i < 8; i++) s[i] = sbox(add_rc(s[i], P2Const::ext[r][i]));
         ext(s);
     }
     for (int i = 0; i < 8; i++) s[i] = canon(s[i]);
