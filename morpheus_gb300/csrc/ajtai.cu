@@ -978,11 +978,8 @@ static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     GB_CUDA_TRY(cudaMallocAsync(&S, s_ints * 4, s));
     GB_CUDA_TRY(cudaMallocAsync(&err, 4, s));
     GB_CUDA_TRY(cudaMemsetAsync(err, 0, 4, s));
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(ajtai_gemm_wc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, WC_SMEM);
-        attr = true;
-    }
+    // set on every call: idempotent, per device, and free of shared state between threads
+    cudaFuncSetAttribute(ajtai_gemm_wc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, WC_SMEM);
     ajtai_gemm_wc_kernel<<<sched.ctas, WC_THREADS, WC_SMEM, s>>>(k->d_A, d_z, B, k->N, (int)(k->Kp / GM_BK), sched,
                                                                 S, err);
     int rc = check_launch("ajtai_gemm_wc_kernel");
@@ -1051,11 +1048,8 @@ static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     CUtensorMap mapB;
     if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp, GM_BN);
     if (!rc) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(ajtai_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GM_SMEM);
-            attr = true;
-        }
+        // set on every call: idempotent, per device, and free of shared state between threads
+        cudaFuncSetAttribute(ajtai_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GM_SMEM);
         int k_tiles = (int)(k->Kp / GM_BK);
         ajtai_gemm_kernel<<<sched.ctas, GM_THREADS, GM_SMEM, s>>>(k->d_T, mapB, k_tiles, sched, S, err);
         rc = check_launch("ajtai_gemm_kernel");
