@@ -643,6 +643,33 @@ struct OpenRounds {
     int n, lr;
 };
 
+// A second stream of the calling thread (created on first use, per device), with two events for
+// ordering it against the thread's launch stream.
+struct HelperStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int dev = -1;
+    ~HelperStream() { release(); }
+    void release() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e), e = nullptr;
+        if (s) cudaStreamDestroy(s), s = nullptr;
+    }
+    int get(cudaStream_t* out) {
+        int d = 0;
+        GB_CUDA_TRY(cudaGetDevice(&d));
+        if (!s || d != dev) {
+            release();
+            dev = d;
+            GB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            for (auto& e : ev) GB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        *out = s;
+        return GB_OK;
+    }
+};
+static thread_local HelperStream t_helper;
+
 // Writes eval (2 words), n oracles, n-1 folded roots, the final codeword (2^lr Ext2) and the
 // queries; *d_leaf_idx receives the device array of the query leaves (num_queries > 0).
 static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, gb_transcript* t, int num_queries,
@@ -673,7 +700,24 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
     u64* rec = mapped(stage);  // records: oracle words 0..5, root 8..11
     if (!rec) return GB_ECUDA;
 
-    auto read_rec = [&](int) -> int {  // the record's words are in `stage` once the stream is idle
+    // Round rd + 1's eq/bh fold and oracle (open_round_kernel) need only round rd's challenge, as do
+    // round rd's codeword fold and tree: they run on the helper stream s2, beside the tree, and the
+    // host reads the round's record once both streams are idle.  s2 starts after the work already
+    // queued on s, and s waits for s2 before this function returns (on every path), so the caller's
+    // later work and frees stay ordered after it.
+    cudaStream_t s2 = nullptr;
+    RC_TRY(t_helper.get(&s2));
+    GB_CUDA_TRY(cudaEventRecord(t_helper.ev[0], s));
+    GB_CUDA_TRY(cudaStreamWaitEvent(s2, t_helper.ev[0], 0));
+    struct JoinHelper {
+        cudaStream_t s, s2;
+        cudaEvent_t ev;
+        ~JoinHelper() {
+            if (cudaEventRecord(ev, s2) == cudaSuccess) cudaStreamWaitEvent(s, ev, 0);
+        }
+    } join{s, s2, t_helper.ev[1]};
+    auto read_rec = [&](int) -> int {  // the record's words are in `stage` once both streams are idle
+        GB_CUDA_TRY(cudaStreamSynchronize(s2));
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         return GB_OK;
     };
@@ -723,11 +767,11 @@ static int open_rounds(const OpenRounds& in, const BfTable* tab, const u64* eq, 
             u64* bo = bh_bufs[pp_i];
             unsigned g = red_grid(quarter);
             if (rd == 0 && in.bh_base)
-                open_round_kernel<true><<<g, RED_THREADS, 0, s>>>(eq_cur, bh_cur, eo, bo, quarter, ch.c0, ch.c1, partials,
-                                                                  rec, counter);
-            else
-                open_round_kernel<false><<<g, RED_THREADS, 0, s>>>(eq_cur, bh_cur, eo, bo, quarter, ch.c0, ch.c1,
+                open_round_kernel<true><<<g, RED_THREADS, 0, s2>>>(eq_cur, bh_cur, eo, bo, quarter, ch.c0, ch.c1,
                                                                    partials, rec, counter);
+            else
+                open_round_kernel<false><<<g, RED_THREADS, 0, s2>>>(eq_cur, bh_cur, eo, bo, quarter, ch.c0, ch.c1,
+                                                                    partials, rec, counter);
             GB_LAUNCH_CHECK("open_round_kernel");
             eq_cur = eo;
             bh_cur = bo;
