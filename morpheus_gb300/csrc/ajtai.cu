@@ -950,6 +950,23 @@ static void key_free(AjtaiKey* k) {
 // limits), so that their bounded waits run out and the call reports it; see gb_ajtai_test_starve.
 static thread_local int t_starve = 0;
 
+// Waits for the calling thread's stream and reads the device word at d (the GEMMs' wait-error
+// flag) through the thread's pinned staging, a plain DMA (a pageable destination would add a
+// staged copy to every call).
+static int read_flag(const int* d, int* out) {
+    cudaStream_t s = stream();
+    u64* pin = thread_pinned(2, 1);
+    if (!pin) {
+        set_error_msg("ajtai: no pinned staging for the error flag");
+        return GB_ECUDA;
+    }
+    *reinterpret_cast<volatile int*>(pin) = 0;
+    if (cudaMemcpyAsync(pin, d, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+        return GB_ECUDA;
+    *out = *reinterpret_cast<volatile int*>(pin);
+    return GB_OK;
+}
+
 // Witness-circulant GEMM: one persistent launch over the (tile, 1024-deep chunk) units, tile =
 // (4 witnesses, 16 ring rows), then the combine.
 static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
@@ -989,10 +1006,7 @@ static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
         rc = check_launch("ajtai_combine_wc_kernel");
     }
     int h_err = 0;
-    if (!rc) {
-        cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) rc = GB_ECUDA;
-    }
+    if (!rc) rc = read_flag(err, &h_err);
     if (zal) cudaFreeAsync(zal, s);
     cudaFreeAsync(S, s);
     cudaFreeAsync(err, s);
@@ -1060,10 +1074,7 @@ static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
         rc = check_launch("ajtai_combine_kernel");
     }
     int h_err = 0;
-    if (!rc) {
-        cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) rc = GB_ECUDA;
-    }
+    if (!rc) rc = read_flag(err, &h_err);
     cudaFreeAsync(zc, s);
     cudaFreeAsync(S, s);
     cudaFreeAsync(err, s);
