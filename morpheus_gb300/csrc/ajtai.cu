@@ -193,6 +193,19 @@ __global__ void ajtai_zprep_scalar_kernel(const uint8_t* __restrict__ z, int B, 
     zc[t] = __int2bfloat16_rn(v);
 }
 
+// Canonical residue mod q of a signed 128-bit value x with |x| < 2^88 (the GEMMs' digit-plane
+// combinations: 8 planes of int32 sums, sum_p 256^p S_p).  Adding q 2^25 makes it positive and
+// below 2^90; then 2^64 == 2^32 + 31 (mod q) folds the high word in twice.
+__device__ __forceinline__ u64 agl_from_i128(__int128 x) {
+    const unsigned __int128 a = (unsigned __int128)(x + ((__int128)AGL_Q << 25));
+    const u64 lo = (u64)a, hi = (u64)(a >> 64);  // hi < 2^26
+    constexpr u64 C = (1ull << 32) + 31;         // 2^64 mod q
+    const unsigned __int128 r = (unsigned __int128)lo + (unsigned __int128)hi * C;  // < 2^64 + 2^59
+    const u64 r_lo = (u64)r, r_hi = (u64)(r >> 64);  // r_hi <= 1, and r_lo < 2^59 when it is 1
+    const u64 v = r_lo + r_hi * C;
+    return v >= AGL_Q ? v - AGL_Q : v;
+}
+
 constexpr int GM_BM_C = 128, GM_BN_C = 256;  // the GEMM's M and N tiles (GM_BM, GM_BN below)
 
 // Persistent schedule of the GEMM: the (tile, K chunk) units, tile-major (tile t = nt tiles_m +
@@ -224,7 +237,6 @@ __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restric
     const int IR = rows * AJ_D;
     const int b0 = blockIdx.x * AJ_CB, ir0 = blockIdx.y * AJ_CB;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of 32
-    const __int128 Q = (__int128)AGL_Q;
     if (threadIdx.x < 8) {
         // rows p IR + ir0 .. +31 lie in one 128-row tile (IR is a multiple of 64, ir0 of 32)
         const int p = threadIdx.x, m = p * IR + ir0, nt = b0 / GM_BN_C;
@@ -233,21 +245,39 @@ __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restric
         s_base[p] = S + ((size_t)t * sched.slots * GM_BM_C + m % GM_BM_C) * GM_BN_C + b0 % GM_BN_C;
     }
     __syncthreads();
+    // up to 4 slots per tile (any full 256-witness batch of 16 rows): every load of a plane's
+    // slots unrolled, so that all of a thread's loads are in flight together
+    bool few = true;
+#pragma unroll
+    for (int p = 0; p < 8; p++) few = few && s_slots[p] <= 4;
+    const size_t slot = (size_t)GM_BM_C * GM_BN_C;
     for (int j = ty; j < AJ_CB; j += 8) {
         const int ir = ir0 + j, b = b0 + tx;
         u64 val = 0;
         if (ir < IR && b < B) {
-            __int128 acc = 0;
-            for (int p = 7; p >= 0; p--) {
-                const int* sp = s_base[p] + (size_t)j * GM_BN_C + tx;  // row ir0 + j, witness b0 + tx
-                long long part = 0;  // |each slot| < 2^31
-                for (int k = 0; k < s_slots[p]; k++) part += sp[(size_t)k * GM_BM_C * GM_BN_C];
-                acc = acc * 256 + (__int128)part;
+            long long part[8];  // |each slot| < 2^31
+            if (few) {
+#pragma unroll
+                for (int p = 0; p < 8; p++) {
+                    const int* sp = s_base[p] + (size_t)j * GM_BN_C + tx;  // row ir0 + j, witness b0 + tx
+                    const int ns = s_slots[p];
+                    const long long v0 = __ldg(sp), v1 = ns > 1 ? __ldg(sp + slot) : 0;
+                    const long long v2 = ns > 2 ? __ldg(sp + 2 * slot) : 0, v3 = ns > 3 ? __ldg(sp + 3 * slot) : 0;
+                    part[p] = v0 + v1 + v2 + v3;
+                }
+            } else {
+                for (int p = 0; p < 8; p++) {
+                    const int* sp = s_base[p] + (size_t)j * GM_BN_C + tx;
+                    long long sum = 0;
+                    for (int k = 0; k < s_slots[p]; k++) sum += __ldg(sp + (size_t)k * slot);
+                    part[p] = sum;
+                }
             }
-            __int128 m = acc % Q;
-            if (m < 0) m += Q;
+            __int128 acc = 0;
+#pragma unroll
+            for (int p = 7; p >= 0; p--) acc = acc * 256 + (__int128)part[p];
             const u64 rs128 = agl_mul(__ldg(RS + ir), 128);
-            val = agl_canon(agl_add((u64)m, agl_canon(rs128)));
+            val = agl_canon(agl_add(agl_from_i128(acc), agl_canon(rs128)));
         }
         tile[j][tx] = val;
     }
@@ -795,30 +825,45 @@ __global__ void __launch_bounds__(WC_THREADS, 1) ajtai_gemm_wc_kernel(const __nv
 }
 
 // c[b][i][r] = sum_p 256^p S[16 p + (i mod 16)][(b mod 4) 64 + r] + 128 rowsum[i][r]  mod q,
-// canonical; S summed over the slots of tile (b / 4, i / 16).  One thread per output coefficient,
-// r fastest: the slot reads and the output writes are both contiguous.
+// canonical; S summed over the slots of tile (b / 4, i / 16).  A block takes 32 consecutive
+// outputs (consecutive r): warp p sums digit plane p over the slots (coalesced along r, four loads
+// in flight), and warp 0 combines the planes.  A small batch spreads one tile's K chunks over
+// many CTAs (64 slots for one witness), so the slot sums are the combine's work.
 __global__ void __launch_bounds__(256) ajtai_combine_wc_kernel(const int* __restrict__ S, GmSched sched, int rows,
                                                                int B, const u64* __restrict__ RS,
                                                                u64* __restrict__ out) {
-    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    __shared__ long long part[8][32];
     const int IR = rows * AJ_D;
-    if (t >= (size_t)B * IR) return;
-    const int b = (int)(t / IR), ir = (int)(t % IR), i = ir / AJ_D, r = ir % AJ_D;
-    const long long tile = (long long)(b / WC_WIT) * sched.tiles_m + i / 16;
-    const int c0 = gm_cta_of(sched, tile * sched.chunks);
-    const int ns = gm_cta_of(sched, (tile + 1) * sched.chunks - 1) - c0 + 1;
-    const int* base = S + ((size_t)tile * sched.slots * GM_BM + (i & 15)) * WC_BN + (b % WC_WIT) * AJ_D + r;
-    __int128 acc = 0;
-    for (int p = 7; p >= 0; p--) {
-        long long part = 0;  // |total over the slots| <= 2^30
-        for (int k = 0; k < ns; k++) part += __ldg(base + ((size_t)k * GM_BM + 16 * p) * WC_BN);
-        acc = acc * 256 + (__int128)part;
+    const int p = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t o = (size_t)blockIdx.x * 32 + lane;  // output b IR + ir
+    const bool valid = o < (size_t)B * IR;
+    const int b = valid ? (int)(o / IR) : 0, ir = valid ? (int)(o % IR) : 0, i = ir / AJ_D, r = ir % AJ_D;
+    long long sum = 0;
+    if (valid) {
+        const long long tile = (long long)(b / WC_WIT) * sched.tiles_m + i / 16;
+        const int ns = gm_cta_of(sched, (tile + 1) * sched.chunks - 1) - gm_cta_of(sched, tile * sched.chunks) + 1;
+        const int* base = S + ((size_t)tile * sched.slots * GM_BM + 16 * p + (i & 15)) * WC_BN + (b % WC_WIT) * AJ_D + r;
+        const size_t stride = (size_t)GM_BM * WC_BN;  // one slot
+        long long s0 = 0, s1 = 0, s2 = 0, s3 = 0;  // |total over the slots| <= 2^30
+        int k = 0;
+        for (; k + 4 <= ns; k += 4) {
+            s0 += __ldg(base + (size_t)k * stride);
+            s1 += __ldg(base + (size_t)(k + 1) * stride);
+            s2 += __ldg(base + (size_t)(k + 2) * stride);
+            s3 += __ldg(base + (size_t)(k + 3) * stride);
+        }
+        for (; k < ns; k++) s0 += __ldg(base + (size_t)k * stride);
+        sum = s0 + s1 + s2 + s3;
     }
-    const __int128 Q = (__int128)AGL_Q;
-    __int128 m = acc % Q;
-    if (m < 0) m += Q;
-    const u64 rs128 = agl_mul(__ldg(RS + ir), 128);
-    out[(size_t)b * IR + ir] = agl_canon(agl_add((u64)m, agl_canon(rs128)));
+    part[p][lane] = sum;
+    __syncthreads();
+    if (p == 0 && valid) {
+        __int128 acc = 0;
+#pragma unroll
+        for (int q = 7; q >= 0; q--) acc = acc * 256 + (__int128)part[q][lane];
+        const u64 rs128 = agl_mul(__ldg(RS + ir), 128);
+        out[o] = agl_canon(agl_add(agl_from_i128(acc), agl_canon(rs128)));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1001,8 +1046,8 @@ static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
                                                                 S, err);
     int rc = check_launch("ajtai_gemm_wc_kernel");
     if (!rc) {
-        ajtai_combine_wc_kernel<<<grid_for((size_t)B * k->rows * AJ_D, 256), 256, 0, s>>>(S, sched, k->rows, B,
-                                                                                       k->d_RS, d_out);
+        ajtai_combine_wc_kernel<<<grid_for((size_t)B * k->rows * AJ_D, 32), 256, 0, s>>>(S, sched, k->rows, B,
+                                                                                      k->d_RS, d_out);
         rc = check_launch("ajtai_combine_wc_kernel");
     }
     int h_err = 0;
