@@ -151,10 +151,12 @@ int aext2_eq_dp_all_batched_ffi(const uint64_t *d_r_all, uint64_t *d_buf_a_all, 
 
 /* ===================== Part 2: GB300 additions (no reference counterpart) ===================== */
 
-/* Matrix rows [row_lo, row_lo + rows) over n_ring ring columns of the ChaCha8 key h_seed,
- * expanded once into the device-resident operand of the tensor-core commitment (8 bf16 digit
- * planes of the negacyclic expansion: 8 * rows * 64 * roundup(64 n_ring, 1024) * 2 bytes).
- * Synchronising. */
+/* Matrix rows [row_lo, row_lo + rows) over n_ring ring columns of the ChaCha8 key h_seed, with
+ * the device-resident operands of the tensor-core commitments: the 8 bf16 digit planes
+ * (ceil(rows / 16) * 128 * roundup(64 n_ring, 1024) * 2 bytes, 16 MB for 16 rows x 1024 columns),
+ * built here, and their negacyclic expansion (8 * rows * 64 * roundup(64 n_ring, 1024) * 2 bytes,
+ * 1.07 GB), built by the first gb_ajtai_commit_u8_batched call that takes the key-Toeplitz form
+ * (that call then synchronises for it; concurrent callers wait for the one build).  Synchronising. */
 int gb_ajtai_key_create(const uint32_t *h_seed, int row_lo, int rows, uint64_t n_ring, void **handle);
 int gb_ajtai_key_destroy(void *handle);
 /* The key's first row, row count and ring columns (any output pointer may be NULL). */
