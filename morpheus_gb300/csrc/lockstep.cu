@@ -171,6 +171,21 @@ __global__ void P2_BOUNDS(T) ls_merkle_level_kernel(const LsSeg* __restrict__ se
     st_digest(sg.c + 4 * j, s);
 }
 
+// one Merkle layer in the pair form (mid-size layers): lanes 2j, 2j + 1 of a segment's blocks make
+// parent j, each holding half the state; a = children, c = parents.  Pairs past a segment's end
+// compute parent 0 and store nothing (their warp takes part in the exchanges).
+template <int T>
+__global__ void P2_PAIR_BOUNDS(T) ls_merkle_level_pair_kernel(const LsSeg* __restrict__ segs, int nseg) {
+    LS_SEG_PROLOGUE
+    const u64 j = ((blockIdx.x - sg.block0) * (u64)T + threadIdx.x) >> 1;
+    const int h = threadIdx.x & 1;
+    const bool live = j < sg.items;
+    u64 st[4];
+    ld_digest(sg.a + 8 * (live ? j : 0) + 4 * h, st);
+    p2_permute_pair(st, h);
+    if (live && h == 0) st_digest(sg.c + 4 * j, st);
+}
+
 // one Merkle layer in the 8-lane form (latency-bound layers): group g of a segment's blocks makes
 // parent g; a = children, c = parents.  Groups past a segment's end compute parent 0 and store
 // nothing (their warp takes part in the shuffles).
@@ -186,21 +201,30 @@ __global__ void __launch_bounds__(LS_COOP_THREADS) ls_merkle_level_coop_kernel(c
     if (live && l < 4) sg.c[4 * g + l] = x;
 }
 
-// The form of one segmented Merkle layer: the 8-lane form when its total parents are below
-// `coop` (the layer cannot fill the GPU, and one thread's permutation is a long serial chain),
-// else one permutation per thread in ls_p2_assign's CTA size.  The form is named, not read off
-// the CTA size: the 8-lane form and the narrow one-per-thread form both use 128 threads.
-enum class LsLayerForm { Coop, Wide, Narrow };
+// The form of one segmented Merkle layer, by its total parents, as the per-call trees choose
+// (p2_form): the 8-lane form below `coop` (the layer cannot fill the GPU, and one thread's
+// permutation is a long serial chain), the pair form below P2_ONE_FROM (two lanes per parent,
+// 128- or 256-thread CTAs), else one permutation per thread in ls_p2_assign's CTA size.  The form
+// is named, not read off the CTA size: several forms use 128 threads.
+enum class LsLayerForm { Coop, Pair128, Pair256, Wide, Narrow };
 static LsLayerForm ls_layer_assign(LsSeg* hs, int cnt, size_t coop, u64& nb) {
     u64 total = 0;
     for (int k = 0; k < cnt; k++) total += hs[k].items;
-    if (total < coop) {
+    auto blocks = [&](u64 threads_per_item, int T) {
         nb = 0;
         for (int k = 0; k < cnt; k++) {
             hs[k].block0 = nb;
-            nb += (hs[k].items * 8 + LS_COOP_THREADS - 1) / LS_COOP_THREADS;
+            nb += (hs[k].items * threads_per_item + T - 1) / T;  // no block for an empty segment
         }
+    };
+    if (total < coop) {
+        blocks(8, LS_COOP_THREADS);
         return LsLayerForm::Coop;
+    }
+    if (total < P2_ONE_FROM) {
+        const int T = p2_pair_threads(total);
+        blocks(2, T);
+        return T == 256 ? LsLayerForm::Pair256 : LsLayerForm::Pair128;
     }
     return ls_p2_assign(hs, cnt, nb) == P2_WIDE ? LsLayerForm::Wide : LsLayerForm::Narrow;
 }
@@ -208,6 +232,12 @@ static int ls_layer_launch(LsLayerForm form, u64 nb, const LsSeg* ds, int cnt, c
     switch (form) {
         case LsLayerForm::Coop:
             ls_merkle_level_coop_kernel<<<(unsigned)nb, LS_COOP_THREADS, 0, s>>>(ds, cnt);
+            break;
+        case LsLayerForm::Pair128:
+            ls_merkle_level_pair_kernel<128><<<(unsigned)nb, 128, 0, s>>>(ds, cnt);
+            break;
+        case LsLayerForm::Pair256:
+            ls_merkle_level_pair_kernel<256><<<(unsigned)nb, 256, 0, s>>>(ds, cnt);
             break;
         case LsLayerForm::Wide:
             ls_merkle_level_kernel<P2_WIDE><<<(unsigned)nb, P2_WIDE, 0, s>>>(ds, cnt);
