@@ -145,7 +145,7 @@ __global__ void ls_reduce_kernel(const LsSeg* __restrict__ segs, int nseg, const
 
 // codeword fold + leaf hash: a = codeword in, b = table level, c = folded out, d = tree leaves
 template <bool BASE_IN, int T>
-__global__ void P2_BOUNDS(T) ls_fold_hash_kernel(const LsSeg* __restrict__ segs, int nseg) {
+__global__ void P2_SEG_BOUNDS(T) ls_fold_hash_kernel(const LsSeg* __restrict__ segs, int nseg) {
     LS_SEG_PROLOGUE
     const u64 i = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
     if (i >= sg.items) return;
@@ -160,7 +160,7 @@ __global__ void P2_BOUNDS(T) ls_fold_hash_kernel(const LsSeg* __restrict__ segs,
 
 // one Merkle layer: a = children, c = parents
 template <int T>
-__global__ void P2_BOUNDS(T) ls_merkle_level_kernel(const LsSeg* __restrict__ segs, int nseg) {
+__global__ void P2_SEG_BOUNDS(T) ls_merkle_level_kernel(const LsSeg* __restrict__ segs, int nseg) {
     LS_SEG_PROLOGUE
     const u64 j = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
     if (j >= sg.items) return;
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(LS_THREADS) ls_bitrev_replicate_kernel(const L
 
 // leaf i = P2(cw[2i], cw[2i+1], 0, ...) for the first copy's leaves: a = codeword, d = tree
 template <int T>
-__global__ void P2_BOUNDS(T) ls_hash_leaves_kernel(const LsSeg* __restrict__ segs, int nseg) {
+__global__ void P2_SEG_BOUNDS(T) ls_hash_leaves_kernel(const LsSeg* __restrict__ segs, int nseg) {
     LS_SEG_PROLOGUE
     const u64 i = (blockIdx.x - sg.block0) * (u64)blockDim.x + threadIdx.x;
     if (i >= sg.items) return;

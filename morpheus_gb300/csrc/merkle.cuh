@@ -56,15 +56,18 @@ size_t mk_coop_below();
 // a longer chain inside the one CTA).
 constexpr size_t MK_TOP_NODES = 16;
 
-// Launch shape of the one-permutation-per-thread kernels: 512-thread CTAs, three per SM (at
-// most 40 registers), measured 1.89 G permutations/s at 2^24 against 1.52-1.59 G with 128-thread
-// CTAs of the same code and register count.  The likely cause is instruction-cache locality:
-// the unrolled permutation is about 15 k instructions, and the warps of one CTA run through it
-// together.  Launches below P2_WIDE_FROM permutations keep 128-thread CTAs, so that a launch of
-// less than a wave still spreads over every SM.
+// Launch shape of the one-permutation-per-thread kernels: 512-thread CTAs, four per SM (at most
+// 32 registers; 8-16 bytes spill), measured 1.917 G permutations/s on a 2^21-parent layer against
+// 1.891 G with three per SM (40 registers), and 1.52-1.59 G with 128-thread CTAs of the same code.
+// The likely cause of the CTA-size effect is instruction-cache locality: the unrolled permutation
+// is about 15 k instructions, and the warps of one CTA run through it together.  Launches below
+// P2_WIDE_FROM permutations keep 128-thread CTAs, so that a launch of less than a wave still
+// spreads over every SM.  The segmented kernels of the batched engine (P2_SEG_BOUNDS) keep three
+// CTAs per SM: at 32 registers their segment bookkeeping spills (784 bytes in one of them).
 constexpr int P2_WIDE = 512, P2_NARROW = 128;
 constexpr size_t P2_WIDE_FROM = (size_t)1 << 16;
-#define P2_BOUNDS(T) __launch_bounds__(T, (T) == 512 ? 3 : 10)
+#define P2_BOUNDS(T) __launch_bounds__(T, (T) == 512 ? 4 : 10)
+#define P2_SEG_BOUNDS(T) __launch_bounds__(T, (T) == 512 ? 3 : 10)
 inline bool p2_wide(size_t items) { return items >= P2_WIDE_FROM; }
 
 // Form of a single-tree launch of `items` permutations, by the per-launch times measured on
