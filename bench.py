@@ -323,7 +323,8 @@ def run_side_workload(args):
             Nn.check(L.gb_ajtai_commit_u8_batched(h, z.ptr, Bw, out.ptr), "ajtai")
         unit, metric, work = "commitments/s", "ajtai witness commitments/s", float(Bw)
         cfg = {"workload": f"ajtai commit, {Bw} witnesses x 2^16 coefficients in [0,256), rows 0..15, "
-                           "q = 2^64-2^32-31", "form": ["by batch size", "witness-circulant", "key-Toeplitz"][args.ajtai_form],
+                           "q = 2^64-2^32-31", "form": ["by batch size", "witness-circulant", "key-Toeplitz",
+                                                                "key-Toeplitz on CTA pairs"][args.ajtai_form],
                "l2": "flushed between timed steps"}
     for _ in range(args.warmup):
         step()
@@ -356,6 +357,7 @@ def run_side_workload(args):
         # stream: the key's 8 digit planes (bf16) once, plus the witness digits (bf16)
         peak, src = measured_peaks()
         circulant = args.ajtai_form == 1 or (args.ajtai_form == 0 and Bw <= 192)
+        pair = args.ajtai_form == 3 or (args.ajtai_form == 0 and Bw > 192)
         if circulant:  # the key's digit planes once (16 MB) plus the witness bytes
             op_bytes = 8 * rows * n_ring * 64 * 2 + Bw * n_ring * 64
         else:  # the key's Toeplitz expansion once (1.07 GB) plus the witness digits
@@ -366,7 +368,8 @@ def run_side_workload(args):
         except Exception:
             tpeak = 1900.0
         line["roofline"] = {"bound": "hbm",
-                            "kernel": ("ajtai_gemm_wc_kernel" if circulant else "ajtai_gemm_kernel") +
+                            "kernel": ("ajtai_gemm_wc_kernel" if circulant else
+                                       "ajtai_gemm_pair_kernel" if pair else "ajtai_gemm_kernel") +
                                       " (whole batch timed)",
                             "achieved": op_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                             "frac": op_bytes / (ms * 1e-3) / 1e9 / peak, "peak_source": src,
@@ -408,6 +411,13 @@ def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):  # ev_time flushes L2 before
     times = [timed(step) for _ in range(10)]
     ms = statistics.median(times)
     got = out.to_numpy()
+    # the same batch in the one-CTA key-Toeplitz form (the automatic choice takes CTA pairs)
+    old = L.gb_ajtai_set_batch_form(2)
+    for _ in range(2):
+        step()
+    ms_one_cta = statistics.median(timed(step) for _ in range(10))
+    assert np.array_equal(out.to_numpy(), got)
+    L.gb_ajtai_set_batch_form(old)
     # one witness: the automatic form (witness-circulant) against the key-Toeplitz form
     one = {}
     for name, form in (("auto", 0), ("toeplitz", 2)):
@@ -432,6 +442,7 @@ def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):  # ev_time flushes L2 before
     alg_bytes = Bw * n_ring * 64 + rows * n_ring * 64 * 8 + Bw * rows * 64 * 8  # Z (u8) + M + out
     tf = flop / (ms * 1e-3) / 1e12
     return {"ms_per_batch": ms, "value": Bw / (ms * 1e-3), "unit": "commitments/s",
+            "form": "key-Toeplitz GEMM on CTA pairs (ajtai_gemm_pair_kernel)", "ms_one_cta_form": ms_one_cta,
             "roofline": {"bound": "tensor", "achieved": tf, "peak": tpeak, "unit": "TFLOP/s", "frac": tf / tpeak,
                          "peak_source": "measured (bf16 burst)" if peaks else "fallback",
                          "hbm_algorithmic_GB_s": alg_bytes / (ms * 1e-3) / 1e9, "hbm_peak": hpeak,
@@ -742,8 +753,9 @@ def main():
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")
     ap.add_argument("--hbm-budget-gb", type=int, default=96, help="served workload: admission budget")
     ap.add_argument("--witnesses", type=int, default=256, help="ajtai workload: witnesses per batch (1..256)")
-    ap.add_argument("--ajtai-form", type=int, default=0, choices=[0, 1, 2],
-                    help="ajtai workload: 0 by batch size, 1 witness-circulant GEMM, 2 key-Toeplitz GEMM")
+    ap.add_argument("--ajtai-form", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="ajtai workload: 0 by batch size, 1 witness-circulant GEMM, 2 key-Toeplitz GEMM, "
+                         "3 key-Toeplitz GEMM on CTA pairs")
     ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "batch_open", "peval", "ajtai", "batched", "served"],
                     help="basefold (headline): commit+open proofs; sumcheck: 2 x 2^20 product sumcheck; "
                          "fold: one fused fold round over 2 x 2^24 Ext2; "

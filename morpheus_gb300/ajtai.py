@@ -33,8 +33,8 @@ def commit_wide(seed, z_wide, col_offset=0, chunk=None):
 
 class batch_form:
     """Context manager: the calling thread's form of AjtaiKey.commit_u8_batched (0 by batch size,
-    1 witness-circulant GEMM, 2 key-Toeplitz GEMM; gb_ajtai_set_batch_form).  Results never
-    depend on it."""
+    1 witness-circulant GEMM, 2 key-Toeplitz GEMM, 3 key-Toeplitz GEMM on CTA pairs;
+    gb_ajtai_set_batch_form).  Results never depend on it."""
 
     def __init__(self, form):
         self.form = form

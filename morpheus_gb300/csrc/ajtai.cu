@@ -215,9 +215,10 @@ constexpr int GM_BM_C = 128, GM_BN_C = 256;  // the GEMM's M and N tiles (GM_BM,
 struct GmSched {
     int tiles_m, chunks;  // M tiles; K chunks per tile
     long long units;      // tiles x chunks
-    int ctas, slots;      // grid size; slots per tile (the most CTAs meeting one tile)
+    int ctas, slots;      // grid size (CTAs, or CTA pairs); slots per tile (the most CTAs meeting one tile)
     unsigned long long spin_limit;  // iterations of each bounded mbarrier wait
     int starve;  // test mode: the producer issues no loads, so that every consumer wait runs out
+    int pair = 0;  // 1: an M tile is 256 rows, two 128-row halves, one per CTA of a pair
 };
 __host__ __device__ inline long long gm_unit_begin(const GmSched& g, long long c) { return c * g.units / g.ctas; }
 __host__ __device__ inline int gm_cta_of(const GmSched& g, long long u) {  // the CTA whose range holds u
@@ -238,11 +239,14 @@ __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restric
     const int b0 = blockIdx.x * AJ_CB, ir0 = blockIdx.y * AJ_CB;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of 32
     if (threadIdx.x < 8) {
-        // rows p IR + ir0 .. +31 lie in one 128-row tile (IR is a multiple of 64, ir0 of 32)
+        // rows p IR + ir0 .. +31 lie in one 128-row tile (IR is a multiple of 64, ir0 of 32); with
+        // pairs, 128-row tile mt is half mt % 2 of the schedule's tile mt / 2, and the halves of
+        // one tile keep their slots one after the other
         const int p = threadIdx.x, m = p * IR + ir0, nt = b0 / GM_BN_C;
-        const long long t = (long long)nt * sched.tiles_m + m / GM_BM_C;
+        const int w = sched.pair ? 2 : 1, mt = m / GM_BM_C;
+        const long long t = (long long)nt * sched.tiles_m + mt / w;
         s_slots[p] = gm_cta_of(sched, (t + 1) * sched.chunks - 1) - gm_cta_of(sched, t * sched.chunks) + 1;
-        s_base[p] = S + ((size_t)t * sched.slots * GM_BM_C + m % GM_BM_C) * GM_BN_C + b0 % GM_BN_C;
+        s_base[p] = S + (((size_t)t * w + mt % w) * sched.slots * GM_BM_C + m % GM_BM_C) * GM_BN_C + b0 % GM_BN_C;
     }
     __syncthreads();
     // up to 4 slots per tile (any full 256-witness batch of 16 rows): every load of a plane's
@@ -357,6 +361,21 @@ __device__ __forceinline__ void bulk_load(u32 dst, const void* src, u32 bytes, u
                  : "memory");
 }
 
+// the same copy with an L2 eviction-priority policy (a createpolicy value)
+__device__ __forceinline__ void bulk_load_hint(u32 dst, const void* src, u32 bytes, u32 bar, u64 policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar), "l"(policy)
+        : "memory");
+}
+// L2 policy for data read once while other data should stay: evicted first
+__device__ __forceinline__ u64 l2_evict_first() {
+    u64 p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
 __device__ __forceinline__ u64 umma_desc_sw128(u32 saddr) {
     u64 d = 0;
@@ -421,6 +440,9 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
         if (lane == 0) {
             // kt counts this CTA's K tiles from 0 (stage and phase); unit kt / 16 gives the coordinates
             const int my_tiles = sched.starve ? 0 : chunks * GM_CHUNK_TILES;
+            // the key expansion is read once: evicted first, so that the witness digits (read
+            // once per M tile) stay in L2
+            const u64 pol_key = l2_evict_first();
             int issued = 0;
             for (int kt = 0; kt < my_tiles; kt++) {
                 int s = kt % GM_STAGES;
@@ -430,8 +452,9 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
                 uint8_t* sa = smem + s * GM_STAGE_BYTES;
                 const int lu = kt / GM_CHUNK_TILES, x = (unit_k0(lu) + kt % GM_CHUNK_TILES) * GM_BK;
                 // the key tile (m0 / 128, x / 64) is 16 KB contiguous and already swizzled
-                bulk_load(smem_u32(sa), A_tiled + ((size_t)(unit_m0(lu) / GM_BM) * k_tiles + x / GM_BK) * (GM_A_BYTES / 2),
-                          GM_A_BYTES, full(s));
+                bulk_load_hint(smem_u32(sa),
+                               A_tiled + ((size_t)(unit_m0(lu) / GM_BM) * k_tiles + x / GM_BK) * (GM_A_BYTES / 2),
+                               GM_A_BYTES, full(s), pol_key);
                 tma_load_2d(smem_u32(sa + GM_A_BYTES), &tmB, x, unit_n0(lu), full(s));
                 issued = kt + 1;
             }
@@ -531,6 +554,278 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+}
+
+// ---------------------------------------------------------------------------
+// The same GEMM on CTA pairs (clusters of 2, `tcgen05.mma.cta_group::2`): an M tile is 256 key
+// rows, rows 0..127 in the even CTA's shared memory and 128..255 in the odd one's, and the 256
+// witnesses of the N tile are split the same way, 0..127 and 128..255.  One thread of the even
+// CTA issues M = 256 MMAs; each CTA's TMEM receives its 128 rows x all 256 witnesses.  So each
+// SM loads half of the witness tile (the batch's witness digits are read from L2 once per 256
+// key rows instead of once per 128) and a stage is 32 KB, six in flight.
+//   Both CTAs: warp 0 loads the CTA's halves into its stages; warps 2..17 drain the CTA's TMEM
+//   exactly as ajtai_gemm_kernel does and arrive on the even CTA's accumulator-empty barriers.
+//   Even CTA, warp 1: the MMA issuer; it waits for its own stage and for the odd CTA's relay,
+//   and its commits arrive on the stage-empty and accumulator-full barriers of both CTAs.
+//   Odd CTA, warp 1: the relay; each of the CTA's stages, once loaded, is passed on as one
+//   arrival on the even CTA's pair-full barrier of that stage.
+// The arrivals on the other CTA's barriers are relaxed: each is made only after the arriving
+// thread's own wait has seen what it reports complete (the stage's bytes landed, or the TMEM
+// reads done with tcgen05.wait::ld), and shared memory has no cache to publish.  A release arrival
+// per stage (a cluster-scope fence in the relay) held the pair to 0.44 ms per 256-witness batch
+// against 0.29 ms relaxed.  The issuer's wait on the relay is what keeps the odd CTA's stage
+// phases in step with the MMAs: it is not optional.
+// Every wait is bounded.  Every thread of both CTAs passes the same two cluster barriers at the
+// start and one at the end (none returns early), both CTAs allocate and free TMEM together, and
+// each CTA waits for the arrivals the other still owes it before the last barrier.
+// ---------------------------------------------------------------------------
+constexpr int GP_STAGES = 6;
+constexpr int GP_BN_HALF = GM_BN / 2;                    // witnesses of one CTA
+constexpr int GP_B_BYTES = GP_BN_HALF * GM_BK * 2;       // 16 KB
+constexpr int GP_STAGE_BYTES = GM_A_BYTES + GP_B_BYTES;  // 32 KB
+constexpr int GP_NBAR = 3 * GP_STAGES + 5;               // full, empty, pair-full, accumulators x 4, mma_done
+constexpr int GP_SMEM = GP_STAGES * GP_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+static_assert(GP_NBAR * 8 + 8 <= 256, "barrier area");
+// instruction descriptor: D f32, A/B bf16, both K-major, M = 256 (the pair), N = 256
+constexpr u32 GP_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(GM_BN >> 3) << 17) | ((u32)(256 >> 4) << 24);
+
+__device__ __forceinline__ u32 cluster_rank() {
+    u32 r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// the shared::cluster address of the same shared-memory offset in CTA `cta` of the cluster
+__device__ __forceinline__ u32 peer_addr(u32 local, u32 cta) {
+    u32 r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(cta));
+    return r;
+}
+// relaxed arrival on a barrier of the other CTA of the pair (see the ordering note above)
+__device__ __forceinline__ void mbar_arrive_remote(u32 cluster_addr) {
+    asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cluster(u32 bar, u32 parity) {
+    u32 ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait on a barrier that the other CTA of the pair arrives on
+__device__ __forceinline__ bool mbar_wait_cluster(u32 bar, u32 parity, int* err, int code, unsigned long long limit) {
+    for (unsigned long long it = 0; it < limit; it++) {
+        if (mbar_try_wait_cluster(bar, parity)) return true;
+        if ((it & 1023) == 1023 && *(volatile int*)err) return false;
+    }
+    atomicCAS(err, 0, code);
+    return false;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const __nv_bfloat16* __restrict__ A_tiled,
+                                                                        const __grid_constant__ CUtensorMap tmB,
+                                                                        int k_tiles, GmSched sched,
+                                                                        int* __restrict__ S, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + GP_STAGES * GP_STAGE_BYTES);
+    u32* tmem_slot = (u32*)(bars + GP_NBAR);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const u32 rank = cluster_rank();  // 0: the even CTA (the MMA issuer's), 1: the odd one
+    const int pair_id = (int)(blockIdx.x >> 1);
+    const long long u0 = gm_unit_begin(sched, pair_id);
+    const int chunks = (int)(gm_unit_begin(sched, pair_id + 1) - u0);
+    auto unit_tile = [&](int lu) { return (u0 + lu) / sched.chunks; };
+    // this CTA's 128-row key tile of the unit's 256-row tile, its witness half, its first K tile
+    auto unit_m128 = [&](int lu) { return (int)(unit_tile(lu) % sched.tiles_m) * 2 + (int)rank; };
+    auto unit_n0 = [&](int lu) { return (int)(unit_tile(lu) / sched.tiles_m) * GM_BN + (int)rank * GP_BN_HALF; };
+    auto unit_k0 = [&](int lu) { return (int)((u0 + lu) % sched.chunks) * GM_CHUNK_TILES; };
+
+    auto full = [&](int s) { return smem_u32(bars + s); };
+    auto empty = [&](int s) { return smem_u32(bars + GP_STAGES + s); };
+    auto pfull = [&](int s) { return smem_u32(bars + 2 * GP_STAGES + s); };  // even CTA: the odd CTA's stage is in
+    auto acc_full = [&](int a) { return smem_u32(bars + 3 * GP_STAGES + a); };
+    auto acc_empty = [&](int a) { return smem_u32(bars + 3 * GP_STAGES + 2 + a); };  // even CTA: both drained
+    const u32 mma_done = smem_u32(bars + 3 * GP_STAGES + 4);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < GP_STAGES; s++) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+            mbar_init(pfull(s), 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(acc_full(a), 1);
+            mbar_init(acc_empty(a), 2 * GM_EPI_WARPS);  // one arrival per epilogue warp of each CTA
+        }
+        mbar_init(mma_done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    cluster_sync_all();  // both CTAs resident, every barrier initialised before any remote arrival
+    if (warp == 1) {  // TMEM, allocated by one warp of each CTA together: two 256-column accumulators
+        __syncwarp();
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    cluster_sync_all();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const u32 tmem = *(volatile u32*)tmem_slot;
+    u32 tmem_peer;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(tmem_peer) : "r"(peer_addr(smem_u32(tmem_slot), rank ^ 1u)));
+    // the MMAs address both CTAs' TMEM through one address: a pair that got different ones does no work
+    const bool bad = tmem != tmem_peer;
+    if (bad && threadIdx.x == 0) atomicCAS(err, 0, 7);
+    const int my_tiles = (bad || sched.starve) ? 0 : chunks * GM_CHUNK_TILES;
+    const int my_chunks = bad ? 0 : chunks;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const u64 pol_key = l2_evict_first();  // the key expansion is read once (as in ajtai_gemm_kernel)
+            int issued = 0;
+            for (int kt = 0; kt < my_tiles; kt++) {
+                const int s = kt % GP_STAGES;
+                const u32 ph = (kt / GP_STAGES) & 1;
+                if (!mbar_wait(empty(s), ph ^ 1, err, 1, sched.spin_limit)) break;
+                mbar_expect_tx(full(s), GP_STAGE_BYTES);
+                uint8_t* sa = smem + s * GP_STAGE_BYTES;
+                const int lu = kt / GM_CHUNK_TILES, x = (unit_k0(lu) + kt % GM_CHUNK_TILES) * GM_BK;
+                bulk_load_hint(smem_u32(sa), A_tiled + ((size_t)unit_m128(lu) * k_tiles + x / GM_BK) * (GM_A_BYTES / 2),
+                               GM_A_BYTES, full(s), pol_key);
+                tma_load_2d(smem_u32(sa + GM_A_BYTES), &tmB, x, unit_n0(lu), full(s));
+                issued = kt + 1;
+            }
+            // the loads still in flight land, then the issuer's last commits for this CTA's stages
+            // arrive here, before the CTA may leave
+            const int first = issued - GP_STAGES < 0 ? 0 : issued - GP_STAGES;
+            for (int kt = first; kt < issued; kt++)
+                mbar_wait(full(kt % GP_STAGES), (kt / GP_STAGES) & 1, err, 5, sched.spin_limit);
+            for (int kt = first; kt < issued; kt++)
+                mbar_wait(empty(kt % GP_STAGES), (kt / GP_STAGES) & 1, err, 9, sched.spin_limit);
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 1) {
+            // relay: each loaded stage of this CTA becomes one arrival on the even CTA's pair-full
+            for (int kt = 0; kt < my_tiles; kt++) {
+                const int s = kt % GP_STAGES;
+                if (!mbar_wait(full(s), (kt / GP_STAGES) & 1, err, 8, sched.spin_limit)) break;
+                mbar_arrive_remote(peer_addr(pfull(s), 0));
+            }
+        } else if (lane == 0 && rank == 0) {
+            bool ok = true;
+            int used = 0;  // accumulators handed out, for the final wait on their drains
+            for (int c = 0; c < my_chunks && ok; c++) {
+                const int a = c & 1;
+                const u32 use = (u32)(c >> 1);
+                if (!mbar_wait_cluster(acc_empty(a), (use & 1) ^ 1, err, 2, sched.spin_limit)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const u32 d_tmem = tmem + (u32)(a * GM_BN);
+                for (int t = 0; t < GM_CHUNK_TILES; t++) {
+                    const int kt = c * GM_CHUNK_TILES + t;
+                    const int s = kt % GP_STAGES;
+                    const u32 ph = (kt / GP_STAGES) & 1;
+                    if (!mbar_wait(full(s), ph, err, 3, sched.spin_limit) ||
+                        !mbar_wait(pfull(s), ph, err, 10, sched.spin_limit)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const u32 sa = smem_u32(smem + s * GP_STAGE_BYTES);
+                    const u64 adesc = umma_desc_sw128(sa), bdesc = umma_desc_sw128(sa + GM_A_BYTES);
+#pragma unroll
+                    for (int k = 0; k < GM_BK / 16; k++) {
+                        const u32 acc = (t > 0 || k > 0) ? 1u : 0u;
+                        const u64 ad = adesc + (u64)((k * 32) >> 4), bd = bdesc + (u64)((k * 32) >> 4);
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                            "l"(ad), "l"(bd), "r"(GP_IDESC), "r"(acc));
+                    }
+                    // the stage is free again in both CTAs once these MMAs have read it
+                    asm volatile(
+                        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+                        "[%0], %1;" ::"r"(empty(s)),
+                        "h"((unsigned short)3));
+                }
+                if (!ok) break;
+                asm volatile(
+                    "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+                    "[%0], %1;" ::"r"(acc_full(a)),
+                    "h"((unsigned short)3));
+                used = c + 1;
+            }
+            asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done));
+            mbar_wait(mma_done, 0, err, 6, sched.spin_limit);
+            // the odd CTA's epilogue arrives here after each drain: wait for the last ones
+            for (int c = used - 2 < 0 ? 0 : used - 2; c < used; c++)
+                mbar_wait_cluster(acc_empty(c & 1), (u32)(c >> 1) & 1, err, 11, sched.spin_limit);
+        }
+    } else {
+        // epilogue: int32 totals of one TMEM row (lane) x 64 columns in registers
+        const int quarter = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const int row = quarter * 32 + lane;
+        constexpr int COLS = 64;
+        int acc[COLS];
+#pragma unroll
+        for (int q = 0; q < COLS; q++) acc[q] = 0;
+        for (int c = 0; c < my_chunks; c++) {
+            const int a = c & 1;
+            const u32 use = (u32)(c >> 1);
+            if (!mbar_wait(acc_full(a), use & 1, err, 4, sched.spin_limit)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+            for (int cb = 0; cb < COLS; cb += 16) {
+                u32 v[16];
+                const u32 taddr = tmem + ((u32)(quarter * 32) << 16) + (u32)(a * GM_BN + half * COLS + cb);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int e = 0; e < 16; e++) acc[cb + e] += __float2int_rn(__uint_as_float(v[e]));
+            }
+            // every lane's TMEM reads have completed (wait::ld): one arrival for the warp, on the
+            // even CTA's barrier
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) {
+                if (rank == 0)
+                    mbar_arrive(acc_empty(a));
+                else
+                    mbar_arrive_remote(peer_addr(acc_empty(a), 0));
+            }
+            // the tile's last unit of this pair: its sums go to this pair's slot of the CTA's half
+            const long long t = unit_tile(c);
+            if (c + 1 == chunks || unit_tile(c + 1) != t) {
+                const int k = pair_id - gm_cta_of(sched, t * sched.chunks);
+                int* dst = S + ((((size_t)t * 2 + rank) * sched.slots + k) * GM_BM + row) * GM_BN + half * COLS;
+#pragma unroll
+                for (int q = 0; q < COLS; q += 4) {
+                    *reinterpret_cast<int4*>(dst + q) = make_int4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
+                    acc[q] = acc[q + 1] = acc[q + 2] = acc[q + 3] = 0;
+                }
+            }
+        }
+    }
+    // neither CTA leaves (or frees TMEM) while the other may still use its shared memory or TMEM
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    cluster_sync_all();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 1) {
+        __syncwarp();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1063,35 +1358,77 @@ static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
 }
 
 // Form of the calling thread's batched commitments (gb_ajtai_set_batch_form): 0 by batch size,
-// 1 the witness-circulant GEMM, 2 the key-Toeplitz GEMM.  Results never depend on it.
+// 1 the witness-circulant GEMM, 2 the key-Toeplitz GEMM, 3 the key-Toeplitz GEMM on CTA pairs.
+// Results never depend on it.
 static thread_local int t_batch_form = 0;
 // Largest batch that the automatic choice gives the witness-circulant GEMM.  Its work grows with
 // the batch (one N = 64 MMA per witness and K step), while the key-Toeplitz GEMM streams the
-// 1.07 GB key expansion whatever the batch.
+// 1.07 GB key expansion whatever the batch; larger batches take its CTA-pair form.
 constexpr int AJ_WC_MAX_AUTO = 192;
+
+// Launch shape of the pair GEMM: a cluster of 2 CTAs, GP_SMEM bytes each.
+static cudaLaunchConfig_t pair_config(int clusters, cudaStream_t s, cudaLaunchAttribute* attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(2 * clusters));
+    cfg.blockDim = dim3(GM_THREADS);
+    cfg.dynamicSmemBytes = GP_SMEM;
+    cfg.stream = s;
+    attr->id = cudaLaunchAttributeClusterDimension;
+    attr->val.clusterDim.x = 2;
+    attr->val.clusterDim.y = 1;
+    attr->val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+// CTA pairs that the device runs at once (0 when clusters of two cannot run the pair GEMM).
+static int pair_clusters() {
+    if (cudaFuncSetAttribute(ajtai_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GP_SMEM) !=
+        cudaSuccess)
+        return 0;
+    cudaLaunchAttribute attr;
+    cudaLaunchConfig_t cfg = pair_config(1, stream(), &attr);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, ajtai_gemm_pair_kernel, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
 
 static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     if (B < 1) return GB_EINVAL;
-    const int form = t_batch_form ? t_batch_form : (B <= AJ_WC_MAX_AUTO ? 1 : 2);
+    int form = t_batch_form ? t_batch_form : (B <= AJ_WC_MAX_AUTO ? 1 : 3);
     if (form == 1) return commit_batch_wc(k, d_z, B, d_out);
     if (int rc = key_expand(k)) return rc;
     cudaStream_t s = stream();
     const int Bp = (int)round_up((size_t)B, GM_BN);
     const size_t Mrows = (size_t)8 * k->rows * AJ_D;
-    // persistent schedule: one CTA per SM (or per unit, when there are fewer), equal unit ranges
+    // form 3: CTA pairs, 256-row tiles; the device must run clusters of two at this size (the
+    // automatic choice falls back to the one-CTA form when it cannot)
+    const int clusters = form == 3 ? pair_clusters() : 0;
+    if (form == 3 && clusters < 1 && t_batch_form == 0) form = 2;
+    if (form == 3 && clusters < 1) {
+        set_error_msg("ajtai pair GEMM: the device runs no cluster of two CTAs of this size");
+        return GB_ECUDA;
+    }
+    const int pair = form == 3 ? 1 : 0;
+    // persistent schedule: one CTA (pair) per SM (pair), or per unit when there are fewer, equal unit ranges
     GmSched sched;
-    sched.tiles_m = (int)(Mrows / GM_BM);
+    sched.pair = pair;
+    sched.tiles_m = (int)(Mrows / (GM_BM << pair));
     sched.chunks = (int)(k->Kp / ((size_t)GM_BK * GM_CHUNK_TILES));
     const long long tiles = (long long)sched.tiles_m * (Bp / GM_BN);
     sched.units = tiles * sched.chunks;
-    sched.ctas = (int)std::min<long long>(num_sms(), sched.units);
+    sched.ctas = (int)std::min<long long>(pair ? clusters : num_sms(), sched.units);
     sched.slots = 1;
     sched.starve = t_starve;
     sched.spin_limit = t_starve ? GM_SPIN_LIMIT_TEST : GM_SPIN_LIMIT;
     for (long long t = 0; t < tiles; t++)
         sched.slots = std::max(sched.slots, gm_cta_of(sched, (t + 1) * sched.chunks - 1) -
                                                 gm_cta_of(sched, t * sched.chunks) + 1);
-    const size_t s_ints = (size_t)tiles * sched.slots * GM_BM * GM_BN;
+    const size_t s_ints = ((size_t)tiles << pair) * sched.slots * GM_BM * GM_BN;
     __nv_bfloat16* zc = nullptr;
     int* S = nullptr;
     int* err = nullptr;
@@ -1105,11 +1442,21 @@ static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
         ajtai_zprep_scalar_kernel<<<grid_for((size_t)Bp * k->Kp, 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
     int rc = check_launch("ajtai_zprep_kernel");
     CUtensorMap mapB;
-    if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp, GM_BN);
-    if (!rc) {
+    if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp, pair ? GP_BN_HALF : GM_BN);
+    const int k_tiles = (int)(k->Kp / GM_BK);
+    if (!rc && pair) {
+        cudaLaunchAttribute attr;
+        cudaLaunchConfig_t cfg = pair_config(sched.ctas, s, &attr);
+        const cudaError_t e =
+            cudaLaunchKernelEx(&cfg, ajtai_gemm_pair_kernel, (const __nv_bfloat16*)k->d_T, mapB, k_tiles, sched, S, err);
+        rc = check_launch("ajtai_gemm_pair_kernel");
+        if (!rc && e != cudaSuccess) {
+            set_error("ajtai_gemm_pair_kernel", e);
+            rc = GB_ECUDA;
+        }
+    } else if (!rc) {
         // set on every call: idempotent, per device, and free of shared state between threads
         cudaFuncSetAttribute(ajtai_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GM_SMEM);
-        int k_tiles = (int)(k->Kp / GM_BK);
         ajtai_gemm_kernel<<<sched.ctas, GM_THREADS, GM_SMEM, s>>>(k->d_T, mapB, k_tiles, sched, S, err);
         rc = check_launch("ajtai_gemm_kernel");
     }
@@ -1124,7 +1471,8 @@ static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     cudaFreeAsync(S, s);
     cudaFreeAsync(err, s);
     if (!rc && h_err) {
-        set_error_msg("ajtai_gemm_kernel: pipeline wait timed out (code " + std::to_string(h_err) + ")");
+        set_error_msg(std::string(pair ? "ajtai_gemm_pair_kernel" : "ajtai_gemm_kernel") +
+                      ": pipeline wait timed out (code " + std::to_string(h_err) + ")");
         rc = GB_ECUDA;
     }
     return rc;
@@ -1511,8 +1859,8 @@ int gb_ajtai_commit_u8_batched(void* handle, const uint8_t* d_z, int num_witness
 }
 
 int gb_ajtai_set_batch_form(int form) {
-    if (form < 0 || form > 2) {
-        set_error_msg("gb_ajtai_set_batch_form: form must be 0 (by batch size), 1 or 2");
+    if (form < 0 || form > 3) {
+        set_error_msg("gb_ajtai_set_batch_form: form must be 0 (by batch size), 1, 2 or 3");
         return GB_EINVAL;
     }
     const int old = t_batch_form;
