@@ -226,20 +226,22 @@ __host__ __device__ inline int gm_cta_of(const GmSched& g, long long u) {  // th
 }
 
 // c[b][i][r] = sum_p 256^p S[(p, i, r)][b] + 128 rowsum[i][r]  mod q, canonical; S[(p, i, r)][b]
-// is the sum of the slots of its tile.  A block takes 32 witnesses x 32 output coefficients
-// through shared memory, so that it reads the slots along b and writes out along (i, r).
-constexpr int AJ_CB = 32;
+// is the sum of the slots of its tile.  A block takes 32 witnesses x 8 output coefficients, one
+// output per thread with all of its slot loads in flight together (the work is ~20 MB of loads,
+// so latency, not bandwidth, sets its time), and writes them out along (i, r) through shared
+// memory.
+constexpr int AJ_CB = 32, AJ_CR = 8;
 __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restrict__ S, GmSched sched, int rows,
                                                             int B, const u64* __restrict__ RS,
                                                             u64* __restrict__ out) {
-    __shared__ u64 tile[AJ_CB][AJ_CB + 1];
+    __shared__ u64 tile[AJ_CR][AJ_CB + 1];
     __shared__ const int* s_base[8];  // per digit plane: the block's first output row in slot 0 of its tile
     __shared__ int s_slots[8];        // and how many slots that tile has
     const int IR = rows * AJ_D;
-    const int b0 = blockIdx.x * AJ_CB, ir0 = blockIdx.y * AJ_CB;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of 32
+    const int b0 = blockIdx.x * AJ_CB, ir0 = blockIdx.y * AJ_CR;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // witness b0 + tx, output ir0 + ty
     if (threadIdx.x < 8) {
-        // rows p IR + ir0 .. +31 lie in one 128-row tile (IR is a multiple of 64, ir0 of 32); with
+        // rows p IR + ir0 .. +7 lie in one 128-row tile (IR is a multiple of 64, ir0 of 8); with
         // pairs, 128-row tile mt is half mt % 2 of the schedule's tile mt / 2, and the halves of
         // one tile keep their slots one after the other
         const int p = threadIdx.x, m = p * IR + ir0, nt = b0 / GM_BN_C;
@@ -249,46 +251,43 @@ __global__ void __launch_bounds__(256) ajtai_combine_kernel(const int* __restric
         s_base[p] = S + (((size_t)t * w + mt % w) * sched.slots * GM_BM_C + m % GM_BM_C) * GM_BN_C + b0 % GM_BN_C;
     }
     __syncthreads();
-    // up to 4 slots per tile (any full 256-witness batch of 16 rows): every load of a plane's
-    // slots unrolled, so that all of a thread's loads are in flight together
-    bool few = true;
-#pragma unroll
-    for (int p = 0; p < 8; p++) few = few && s_slots[p] <= 4;
     const size_t slot = (size_t)GM_BM_C * GM_BN_C;
-    for (int j = ty; j < AJ_CB; j += 8) {
-        const int ir = ir0 + j, b = b0 + tx;
-        u64 val = 0;
-        if (ir < IR && b < B) {
-            long long part[8];  // |each slot| < 2^31
-            if (few) {
+    const int ir = ir0 + ty, b = b0 + tx;
+    u64 val = 0;
+    if (ir < IR && b < B) {
+        long long part[8];  // |each slot| < 2^31
+        // up to 4 slots per tile (any full 256-witness batch of 16 rows): every load unrolled
+        bool few = true;
 #pragma unroll
-                for (int p = 0; p < 8; p++) {
-                    const int* sp = s_base[p] + (size_t)j * GM_BN_C + tx;  // row ir0 + j, witness b0 + tx
-                    const int ns = s_slots[p];
-                    const long long v0 = __ldg(sp), v1 = ns > 1 ? __ldg(sp + slot) : 0;
-                    const long long v2 = ns > 2 ? __ldg(sp + 2 * slot) : 0, v3 = ns > 3 ? __ldg(sp + 3 * slot) : 0;
-                    part[p] = v0 + v1 + v2 + v3;
-                }
-            } else {
-                for (int p = 0; p < 8; p++) {
-                    const int* sp = s_base[p] + (size_t)j * GM_BN_C + tx;
-                    long long sum = 0;
-                    for (int k = 0; k < s_slots[p]; k++) sum += __ldg(sp + (size_t)k * slot);
-                    part[p] = sum;
-                }
+        for (int p = 0; p < 8; p++) few = few && s_slots[p] <= 4;
+        if (few) {
+#pragma unroll
+            for (int p = 0; p < 8; p++) {
+                const int* sp = s_base[p] + (size_t)ty * GM_BN_C + tx;  // row ir0 + ty, witness b0 + tx
+                const int ns = s_slots[p];
+                const long long v0 = __ldg(sp), v1 = ns > 1 ? __ldg(sp + slot) : 0;
+                const long long v2 = ns > 2 ? __ldg(sp + 2 * slot) : 0, v3 = ns > 3 ? __ldg(sp + 3 * slot) : 0;
+                part[p] = v0 + v1 + v2 + v3;
             }
-            __int128 acc = 0;
-#pragma unroll
-            for (int p = 7; p >= 0; p--) acc = acc * 256 + (__int128)part[p];
-            const u64 rs128 = agl_mul(__ldg(RS + ir), 128);
-            val = agl_canon(agl_add(agl_from_i128(acc), agl_canon(rs128)));
+        } else {
+            for (int p = 0; p < 8; p++) {
+                const int* sp = s_base[p] + (size_t)ty * GM_BN_C + tx;
+                long long sum = 0;
+                for (int k = 0; k < s_slots[p]; k++) sum += __ldg(sp + (size_t)k * slot);
+                part[p] = sum;
+            }
         }
-        tile[j][tx] = val;
+        __int128 acc = 0;
+#pragma unroll
+        for (int p = 7; p >= 0; p--) acc = acc * 256 + (__int128)part[p];
+        const u64 rs128 = agl_mul(__ldg(RS + ir), 128);
+        val = agl_canon(agl_add(agl_from_i128(acc), agl_canon(rs128)));
     }
+    tile[ty][tx] = val;
     __syncthreads();
-    for (int j = ty; j < AJ_CB; j += 8) {
-        const int b = b0 + j, ir = ir0 + tx;
-        if (b < B && ir < IR) out[(size_t)b * IR + ir] = tile[tx][j];
+    {
+        const int bo = b0 + (threadIdx.x >> 3), io = ir0 + (threadIdx.x & 7);  // 8 outputs of one witness
+        if (bo < B && io < IR) out[(size_t)bo * IR + io] = tile[threadIdx.x & 7][threadIdx.x >> 3];
     }
 }
 
@@ -1461,7 +1460,7 @@ static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
         rc = check_launch("ajtai_gemm_kernel");
     }
     if (!rc) {
-        dim3 cg((unsigned)((B + AJ_CB - 1) / AJ_CB), (unsigned)((k->rows * AJ_D + AJ_CB - 1) / AJ_CB));
+        dim3 cg((unsigned)((B + AJ_CB - 1) / AJ_CB), (unsigned)((k->rows * AJ_D + AJ_CR - 1) / AJ_CR));
         ajtai_combine_kernel<<<cg, 256, 0, s>>>(S, sched, k->rows, B, k->d_RS, d_out);
         rc = check_launch("ajtai_combine_kernel");
     }
