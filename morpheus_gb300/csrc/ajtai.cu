@@ -152,16 +152,44 @@ __global__ void __launch_bounds__(64) ajtai_planes_kernel(const u64* __restrict_
 }
 
 // rowsum(T)[i][r] mod q = sum_j (2 prefix_r(M_ij) - total(M_ij)), one thread per (i, r)
-__global__ void ajtai_rowsum_kernel(const u64* __restrict__ M, int rows, u64 N, u64* __restrict__ RS) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= rows * AJ_D) return;
-    int i = t / AJ_D, r = t % AJ_D;
-    u64 acc = 0;
-    for (u64 j = 0; j < N; j++) {
-        const u64* m = M + ((size_t)i * N + j) * AJ_D;
-        for (int k = 0; k < AJ_D; k++) acc = k <= r ? agl_add(acc, m[k]) : agl_sub(acc, m[k]);
+// Canonical residue mod q of a signed 128-bit value x with |x| < 2^88 (the GEMMs' digit-plane
+// combinations: 8 planes of int32 sums, sum_p 256^p S_p; the key's column sums over at most 2^24
+// ring columns).  Adding q 2^25 makes it positive and
+// below 2^90; then 2^64 == 2^32 + 31 (mod q) folds the high word in twice.
+__device__ __forceinline__ u64 agl_from_i128(__int128 x) {
+    const unsigned __int128 a = (unsigned __int128)(x + ((__int128)AGL_Q << 25));
+    const u64 lo = (u64)a, hi = (u64)(a >> 64);  // hi < 2^26
+    constexpr u64 C = (1ull << 32) + 31;         // 2^64 mod q
+    const unsigned __int128 r = (unsigned __int128)lo + (unsigned __int128)hi * C;  // < 2^64 + 2^59
+    const u64 r_lo = (u64)r, r_hi = (u64)(r >> 64);  // r_hi <= 1, and r_lo < 2^59 when it is 1
+    const u64 v = r_lo + r_hi * C;
+    return v >= AGL_Q ? v - AGL_Q : v;
+}
+
+// RS[i][r] = sum_j sum_k s(k, r) M[i][j][k], s = +1 for k <= r, -1 above: the row sums of the
+// negacyclic expansion, used for the witnesses' -128 offset.  It factors through the column sums
+// C[i][k] = sum_j M[i][j][k]: RS[i][r] = sum_{k <= r} C[i][k] - sum_{k > r} C[i][k].  One block per
+// ring row: thread (slice, k) sums column k over a quarter of the ring columns exactly in 128 bits
+// (coalesced along k), the quarters meet in shared memory, then thread r forms its signed sum.
+__global__ void __launch_bounds__(256) ajtai_rowsum_kernel(const u64* __restrict__ M, u64 N, u64* __restrict__ RS) {
+    __shared__ unsigned __int128 part[4][AJ_D];
+    __shared__ u64 col[AJ_D];
+    const int i = blockIdx.x, k = threadIdx.x & 63, slice = threadIdx.x >> 6;
+    unsigned __int128 acc = 0;  // < 2^24 ring columns x 2^64
+    for (u64 j = slice; j < N; j += 4) acc += M[((size_t)i * N + j) * AJ_D + k];
+    part[slice][k] = acc;
+    __syncthreads();
+    if (threadIdx.x < AJ_D) {
+        const unsigned __int128 t = part[0][k] + part[1][k] + part[2][k] + part[3][k];
+        col[k] = agl_canon(agl_from_i128((__int128)t));
     }
-    RS[t] = agl_canon(acc);
+    __syncthreads();
+    if (threadIdx.x < AJ_D) {
+        const int r = threadIdx.x;
+        u64 v = 0;
+        for (int c = 0; c < AJ_D; c++) v = c <= r ? agl_add(v, col[c]) : agl_sub(v, col[c]);
+        RS[(size_t)i * AJ_D + r] = agl_canon(v);
+    }
 }
 
 // z'[b][k] = z[b][k] - 128 (bf16); padded witnesses / columns are 0.  Eight coefficients per
@@ -191,19 +219,6 @@ __global__ void ajtai_zprep_scalar_kernel(const uint8_t* __restrict__ z, int B, 
     size_t b = t / Kp, k = t % Kp;
     int v = (b < (size_t)B && k < K) ? (int)z[b * K + k] - 128 : 0;
     zc[t] = __int2bfloat16_rn(v);
-}
-
-// Canonical residue mod q of a signed 128-bit value x with |x| < 2^88 (the GEMMs' digit-plane
-// combinations: 8 planes of int32 sums, sum_p 256^p S_p).  Adding q 2^25 makes it positive and
-// below 2^90; then 2^64 == 2^32 + 31 (mod q) folds the high word in twice.
-__device__ __forceinline__ u64 agl_from_i128(__int128 x) {
-    const unsigned __int128 a = (unsigned __int128)(x + ((__int128)AGL_Q << 25));
-    const u64 lo = (u64)a, hi = (u64)(a >> 64);  // hi < 2^26
-    constexpr u64 C = (1ull << 32) + 31;         // 2^64 mod q
-    const unsigned __int128 r = (unsigned __int128)lo + (unsigned __int128)hi * C;  // < 2^64 + 2^59
-    const u64 r_lo = (u64)r, r_hi = (u64)(r >> 64);  // r_hi <= 1, and r_lo < 2^59 when it is 1
-    const u64 v = r_lo + r_hi * C;
-    return v >= AGL_Q ? v - AGL_Q : v;
 }
 
 constexpr int GM_BM_C = 128, GM_BN_C = 256;  // the GEMM's M and N tiles (GM_BM, GM_BN below)
@@ -1240,7 +1255,7 @@ static int key_create(const u32* h_seed, int row_lo, int rows, u64 N, AjtaiKey* 
         ajtai_planes_kernel<<<g, 64, 0, s>>>(k->d_M, N, k->Kp / GM_BK, k->d_A);
         GB_LAUNCH_CHECK("ajtai_planes_kernel");
     }
-    ajtai_rowsum_kernel<<<grid_for((size_t)rows * AJ_D, 64), 64, 0, s>>>(k->d_M, rows, N, k->d_RS);
+    ajtai_rowsum_kernel<<<rows, 256, 0, s>>>(k->d_M, N, k->d_RS);
     GB_LAUNCH_CHECK("ajtai_rowsum_kernel");
     cudaFreeAsync(d_key, s);
     GB_CUDA_TRY(cudaStreamSynchronize(s));
