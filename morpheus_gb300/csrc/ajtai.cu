@@ -30,6 +30,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -1398,18 +1399,29 @@ static cudaLaunchConfig_t pair_config(int clusters, cudaStream_t s, cudaLaunchAt
     return cfg;
 }
 
-// CTA pairs that the device runs at once (0 when clusters of two cannot run the pair GEMM).
+// CTA pairs that the device runs at once (0 when clusters of two cannot run the pair GEMM).  The
+// shared-memory attribute is set on every call (idempotent, per device); the occupancy answer
+// depends only on the device and is kept per device (a race only recomputes the same value).
 static int pair_clusters() {
     if (cudaFuncSetAttribute(ajtai_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GP_SMEM) !=
         cudaSuccess)
         return 0;
+    constexpr int MAX_DEVICES = 64;
+    static std::atomic<int> known[MAX_DEVICES];  // 0: not yet asked, else clusters + 1
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (dev >= 0 && dev < MAX_DEVICES) {
+        const int k = known[dev].load(std::memory_order_relaxed);
+        if (k > 0) return k - 1;
+    }
     cudaLaunchAttribute attr;
     cudaLaunchConfig_t cfg = pair_config(1, stream(), &attr);
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, ajtai_gemm_pair_kernel, &cfg) != cudaSuccess) {
         cudaGetLastError();
-        return 0;
+        return 0;  // not kept: a later call asks again
     }
+    if (dev >= 0 && dev < MAX_DEVICES) known[dev].store(n + 1, std::memory_order_relaxed);
     return n;
 }
 
