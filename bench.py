@@ -324,7 +324,8 @@ def run_side_workload(args):
         unit, metric, work = "commitments/s", "ajtai witness commitments/s", float(Bw)
         cfg = {"workload": f"ajtai commit, {Bw} witnesses x 2^16 coefficients in [0,256), rows 0..15, "
                            "q = 2^64-2^32-31", "form": ["by batch size", "witness-circulant", "key-Toeplitz",
-                                                                "key-Toeplitz on CTA pairs"][args.ajtai_form],
+                                                                "key-Toeplitz on CTA pairs",
+                                                                "Hankel key windows on CTA pairs"][args.ajtai_form],
                "l2": "flushed between timed steps"}
     for _ in range(args.warmup):
         step()
@@ -357,9 +358,12 @@ def run_side_workload(args):
         # stream: the key's 8 digit planes (bf16) once, plus the witness digits (bf16)
         peak, src = measured_peaks()
         circulant = args.ajtai_form == 1 or (args.ajtai_form == 0 and Bw <= 172)
-        pair = args.ajtai_form == 3 or (args.ajtai_form == 0 and Bw > 172)
+        hankel = args.ajtai_form == 4 or (args.ajtai_form == 0 and Bw > 172)
+        pair = args.ajtai_form == 3
         if circulant:  # the key's digit planes once (16 MB) plus the witness bytes
             op_bytes = 8 * rows * n_ring * 64 * 2 + Bw * n_ring * 64
+        elif hankel:  # the key's Hankel windows once (3840 B per 128 rows and ring column) plus the witness digits
+            op_bytes = 4 * rows * n_ring * 3840 + Bw * n_ring * 64 * 2
         else:  # the key's Toeplitz expansion once (1.07 GB) plus the witness digits
             op_bytes = 8 * rows * 64 * n_ring * 64 * 2 + Bw * n_ring * 64 * 2
         try:
@@ -369,7 +373,8 @@ def run_side_workload(args):
             tpeak = 1900.0
         line["roofline"] = {"bound": "hbm",
                             "kernel": ("ajtai_gemm_wc_kernel" if circulant else
-                                       "ajtai_gemm_pair_kernel" if pair else "ajtai_gemm_kernel") +
+                                       "ajtai_gemm_pair_kernel<true> (Hankel windows)" if hankel else
+                                       "ajtai_gemm_pair_kernel<false>" if pair else "ajtai_gemm_kernel") +
                                       " (whole batch timed)",
                             "achieved": op_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                             "frac": op_bytes / (ms * 1e-3) / 1e9 / peak, "peak_source": src,
@@ -411,13 +416,16 @@ def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):  # ev_time flushes L2 before
     times = [timed(step) for _ in range(10)]
     ms = statistics.median(times)
     got = out.to_numpy()
-    # the same batch in the one-CTA key-Toeplitz form (the automatic choice takes CTA pairs)
-    old = L.gb_ajtai_set_batch_form(2)
-    for _ in range(2):
-        step()
-    ms_one_cta = statistics.median(timed(step) for _ in range(10))
-    assert np.array_equal(out.to_numpy(), got)
-    L.gb_ajtai_set_batch_form(old)
+    # the same batch through the key's Toeplitz expansion (1.07 GB), on one CTA per SM and on CTA
+    # pairs; the automatic choice reads the Hankel windows (252 MB) on CTA pairs
+    other = {}
+    for name, form in (("one_cta_toeplitz", 2), ("pair_toeplitz", 3)):
+        old = L.gb_ajtai_set_batch_form(form)
+        for _ in range(2):
+            step()
+        other[name] = statistics.median(timed(step) for _ in range(10))
+        assert np.array_equal(out.to_numpy(), got)
+        L.gb_ajtai_set_batch_form(old)
     # one witness: the automatic form (witness-circulant) against the key-Toeplitz form
     one = {}
     for name, form in (("auto", 0), ("toeplitz", 2)):
@@ -442,7 +450,8 @@ def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):  # ev_time flushes L2 before
     alg_bytes = Bw * n_ring * 64 + rows * n_ring * 64 * 8 + Bw * rows * 64 * 8  # Z (u8) + M + out
     tf = flop / (ms * 1e-3) / 1e12
     return {"ms_per_batch": ms, "value": Bw / (ms * 1e-3), "unit": "commitments/s",
-            "form": "key-Toeplitz GEMM on CTA pairs (ajtai_gemm_pair_kernel)", "ms_one_cta_form": ms_one_cta,
+            "form": "CTA-pair GEMM on the key's Hankel windows (ajtai_gemm_pair_kernel<true>)",
+            "ms_other_forms": other,
             "roofline": {"bound": "tensor", "achieved": tf, "peak": tpeak, "unit": "TFLOP/s", "frac": tf / tpeak,
                          "peak_source": "measured (bf16 burst)" if peaks else "fallback",
                          "hbm_algorithmic_GB_s": alg_bytes / (ms * 1e-3) / 1e9, "hbm_peak": hpeak,
@@ -753,9 +762,9 @@ def main():
     ap.add_argument("--workers", type=int, default=8, help="served workload: prover service workers")
     ap.add_argument("--hbm-budget-gb", type=int, default=96, help="served workload: admission budget")
     ap.add_argument("--witnesses", type=int, default=256, help="ajtai workload: witnesses per batch (1..256)")
-    ap.add_argument("--ajtai-form", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--ajtai-form", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="ajtai workload: 0 by batch size, 1 witness-circulant GEMM, 2 key-Toeplitz GEMM, "
-                         "3 key-Toeplitz GEMM on CTA pairs")
+                         "3 key-Toeplitz GEMM on CTA pairs, 4 the pair GEMM on the key's Hankel windows")
     ap.add_argument("--workload", default="basefold", choices=["basefold", "sumcheck", "fold", "batch_open", "peval", "ajtai", "batched", "served"],
                     help="basefold (headline): commit+open proofs; sumcheck: 2 x 2^20 product sumcheck; "
                          "fold: one fused fold round over 2 x 2^24 Ext2; "

@@ -154,9 +154,11 @@ int aext2_eq_dp_all_batched_ffi(const uint64_t *d_r_all, uint64_t *d_buf_a_all, 
 /* Matrix rows [row_lo, row_lo + rows) over n_ring ring columns of the ChaCha8 key h_seed, with
  * the device-resident operands of the tensor-core commitments: the 8 bf16 digit planes
  * (ceil(rows / 16) * 128 * roundup(64 n_ring, 1024) * 2 bytes, 16 MB for 16 rows x 1024 columns),
- * built here, and their negacyclic expansion (8 * rows * 64 * roundup(64 n_ring, 1024) * 2 bytes,
- * 1.07 GB), built by the first gb_ajtai_commit_u8_batched call that takes the key-Toeplitz form
- * (that call then synchronises for it; concurrent callers wait for the one build).  Synchronising. */
+ * built here; their Hankel windows (4 * rows * roundup(n_ring, 16) * 3840 bytes, 252 MB), built
+ * by the first gb_ajtai_commit_u8_batched call that takes the Hankel form; and their negacyclic
+ * expansion (8 * rows * 64 * roundup(64 n_ring, 1024) * 2 bytes, 1.07 GB), built only by a call
+ * that takes a key-Toeplitz form (such a first call synchronises for the build; concurrent callers
+ * wait for the one build).  Synchronising. */
 int gb_ajtai_key_create(const uint32_t *h_seed, int row_lo, int rows, uint64_t n_ring, void **handle);
 int gb_ajtai_key_destroy(void *handle);
 /* The key's first row, row count and ring columns (any output pointer may be NULL). */
@@ -169,9 +171,11 @@ int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses,
  * 0 chooses by batch size (the default), 1 the witness-circulant tensor-core GEMM (work
  * proportional to the batch; the automatic choice up to 172 witnesses), 2 the key-Toeplitz
  * tensor-core GEMM (streams the key's 1.07 GB expansion once per batch of up to 256 witnesses),
- * 3 the key-Toeplitz GEMM on CTA pairs (clusters of two CTAs, M = 256 tcgen05 MMAs; the
- * automatic choice above 172 witnesses, or form 2 where the device cannot run the pairs).
- * Results never depend on it.  Returns the previous form, or -2 for a form outside 0..3. */
+ * 3 the key-Toeplitz GEMM on CTA pairs (clusters of two CTAs, M = 256 tcgen05 MMAs), 4 the
+ * same CTA-pair GEMM reading the key's Hankel windows instead of its expansion (252 MB for 16 rows
+ * x 1024 ring columns, built on first use; the automatic choice above 172 witnesses, or form 2
+ * where the device cannot run the pairs).  Results never depend on it.  Returns the previous
+ * form, or -2 for a form outside 0..4. */
 int gb_ajtai_set_batch_form(int form);
 /* Test switch of the calling thread for the GEMM's bounded waits: with on != 0 the following
  * gb_ajtai_commit_u8_batched calls launch the tensor-core GEMM with its operand loads left out and

@@ -33,8 +33,8 @@ def commit_wide(seed, z_wide, col_offset=0, chunk=None):
 
 class batch_form:
     """Context manager: the calling thread's form of AjtaiKey.commit_u8_batched (0 by batch size,
-    1 witness-circulant GEMM, 2 key-Toeplitz GEMM, 3 key-Toeplitz GEMM on CTA pairs;
-    gb_ajtai_set_batch_form).  Results never depend on it."""
+    1 witness-circulant GEMM, 2 key-Toeplitz GEMM, 3 key-Toeplitz GEMM on CTA pairs, 4 the pair
+    GEMM on the key's Hankel windows; gb_ajtai_set_batch_form).  Results never depend on it."""
 
     def __init__(self, form):
         self.form = form
@@ -49,9 +49,10 @@ class batch_form:
 
 
 class AjtaiKey:
-    """Rows [row_lo, row_lo + rows) of the matrix over n_ring columns, with both GEMM operands
-    built once: the digit planes (16 MB for 16 rows x 1024 columns) and their Toeplitz expansion
-    (1.07 GB)."""
+    """Rows [row_lo, row_lo + rows) of the matrix over n_ring columns, with the GEMM operands each
+    built once: the digit planes (16 MB for 16 rows x 1024 columns) at creation, their Hankel
+    windows (252 MB) and their Toeplitz expansion (1.07 GB) by the first batch whose form reads
+    them."""
 
     def __init__(self, seed, row_lo, rows, n_ring):
         self.rows, self.n_ring = rows, n_ring

@@ -125,6 +125,47 @@ __global__ void __launch_bounds__(64) ajtai_expand_kernel(const u64* __restrict_
     }
 }
 
+// The key's Hankel windows: with K reversed inside each ring column (kappa = 63 - l) the 64 x 64
+// negacyclic block of (digit plane p, ring row i, ring column j) is
+//   H[r][kappa] = G[r + kappa],   G[t] = d_p(M[i][j][t - 63]) (t >= 63), -d_p(M[i][j][t + 1]) (t < 63),
+// so its 8 x 8 core matrix (row group a, column group b) depends only on q = a + b: row rho of
+// core matrix q is G[8 q + rho .. 8 q + rho + 7].  Block (p, i) is half beta = (p rows + i) % 2 of
+// the 128-row key tile m = (p rows + i) / 2, and the tile's two halves interleave by core
+// matrix: core matrix q of half beta sits at byte (2 q + beta) 128 of the tile's 3840-byte window
+// for ring column j, window (m, j) at (m KT + j) 3840.  A no-swizzle K-major descriptor with a
+// 256-byte step along K and a 128-byte step per 8 rows then reads the tile's 128 rows x 64 columns
+// in place, row group 2 a' + beta being group a' of half beta.  Padding columns stay zero.  One
+// block per (j, i): thread k takes the digits of M[i][j][k], then thread (q, rho) writes row rho of
+// core matrix q for every plane.
+constexpr int GW_A_BYTES = 15 * 2 * 128;  // a 128-row tile's window for one ring column
+__global__ void __launch_bounds__(128) ajtai_window_kernel(const u64* __restrict__ M, int rows, u64 N, size_t KT,
+                                                           uint8_t* __restrict__ W) {
+    __shared__ short dig[AJ_D][8];  // the top digit can be +128: not a signed char
+    const u64 j = blockIdx.x;
+    const int i = blockIdx.y;
+    if (threadIdx.x < AJ_D) {
+        int d[8];
+        centred_digits(M[((size_t)i * N + j) * AJ_D + threadIdx.x], d);
+#pragma unroll
+        for (int p = 0; p < 8; p++) dig[threadIdx.x][p] = (short)d[p];
+    }
+    __syncthreads();
+    const int q = threadIdx.x >> 3, rho = threadIdx.x & 7;
+    if (q >= 15) return;  // 120 rows of 16 bytes per plane
+#pragma unroll 1
+    for (int p = 0; p < 8; p++) {
+        const int blk = p * rows + i;
+        uint8_t* dst = W + ((size_t)(blk >> 1) * KT + j) * GW_A_BYTES + (2 * q + (blk & 1)) * 128 + rho * 16;
+        __align__(16) __nv_bfloat16 w[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const int t = 8 * q + rho + c;  // 0 .. 126
+            w[c] = __int2bfloat16_rn(t >= 63 ? (int)dig[t - 63][p] : -(int)dig[t + 1][p]);
+        }
+        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(w);
+    }
+}
+
 // Key operand of the witness-circulant GEMM: A[m][(j, kappa)] = d_p(M[i][j][63 - kappa]) as bf16,
 // m = 16 p + (i mod 16) in the 128-row tile i / 16, stored tile by tile like ajtai_expand_kernel's
 // output (tile (i / 16, j) 16 KB contiguous at ((i / 16) KT + j) 16 KB, 128-byte swizzled).  Rows
@@ -193,32 +234,39 @@ __global__ void __launch_bounds__(256) ajtai_rowsum_kernel(const u64* __restrict
     }
 }
 
-// z'[b][k] = z[b][k] - 128 (bf16); padded witnesses / columns are 0.  Eight coefficients per
-// thread: one 8-byte load (K and Kp are multiples of 64; the host checks z's alignment) and one
-// 16-byte store.
+// z'[b][k] = z[b][k] - 128 (bf16); padded witnesses / columns are 0.  With REV the K index is
+// reversed inside each ring column, z'[b][64 j + kappa] = z[b][64 j + 63 - kappa] - 128 (the
+// operand of the Hankel key form).  Eight coefficients per thread: one 8-byte load (K and Kp are
+// multiples of 64; the host checks z's alignment) and one 16-byte store.
+template <bool REV>
 __global__ void ajtai_zprep_kernel(const uint8_t* __restrict__ z, int B, size_t K, int Bp, size_t Kp,
                                    __nv_bfloat16* __restrict__ zc) {
     const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const size_t per_row = Kp / 8;
     if (t >= (size_t)Bp * per_row) return;
     const size_t b = t / per_row, k = (t % per_row) * 8;
+    // REV: outputs kappa = k % 64 .. +7 of ring column k / 64 read bytes 56 - kappa .. 63 - kappa
+    const size_t src = REV ? (k & ~(size_t)63) + 56 - (k & 63) : k;
     uint2 raw = make_uint2(0x80808080u, 0x80808080u);  // 128 - 128 = 0 for padding
-    if (b < (size_t)B && k < K) raw = __ldg(reinterpret_cast<const uint2*>(z + b * K + k));
+    if (b < (size_t)B && src < K) raw = __ldg(reinterpret_cast<const uint2*>(z + b * K + src));
     __align__(16) __nv_bfloat16 w[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) {
-        const u32 word = e < 4 ? raw.x : raw.y;
-        w[e] = __int2bfloat16_rn((int)((word >> (8 * (e & 3))) & 0xFF) - 128);
+        const int byte = REV ? 7 - e : e;
+        const u32 word = byte < 4 ? raw.x : raw.y;
+        w[e] = __int2bfloat16_rn((int)((word >> (8 * (byte & 3))) & 0xFF) - 128);
     }
     *reinterpret_cast<uint4*>(zc + b * Kp + k) = *reinterpret_cast<const uint4*>(w);
 }
 // the same, one coefficient per thread, for witness arrays that are not 8-byte aligned
+template <bool REV>
 __global__ void ajtai_zprep_scalar_kernel(const uint8_t* __restrict__ z, int B, size_t K, int Bp, size_t Kp,
                                           __nv_bfloat16* __restrict__ zc) {
     size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (t >= (size_t)Bp * Kp) return;
     size_t b = t / Kp, k = t % Kp;
-    int v = (b < (size_t)B && k < K) ? (int)z[b * K + k] - 128 : 0;
+    const size_t src = REV ? (k & ~(size_t)63) + 63 - (k & 63) : k;
+    int v = (b < (size_t)B && src < K) ? (int)z[b * K + src] - 128 : 0;
     zc[t] = __int2bfloat16_rn(v);
 }
 
@@ -399,6 +447,16 @@ __device__ __forceinline__ u64 umma_desc_sw128(u32 saddr) {
     d |= (u64)(1024 >> 4) << 32;         // stride-dimension offset
     d |= (u64)1 << 46;                   // descriptor version for tcgen05
     d |= (u64)2 << 61;                   // 128-byte swizzle
+    return d;
+}
+
+// shared-memory matrix descriptor of a Hankel window (ajtai_window_kernel): K-major, no swizzle,
+// core matrices 256 bytes apart along K and 128 bytes apart per 8 rows
+__device__ __forceinline__ u64 umma_desc_hankel(u32 saddr) {
+    u64 d = (u64)((saddr & 0x3FFFF) >> 4);
+    d |= (u64)(256 >> 4) << 16;  // leading-dimension (K) offset
+    d |= (u64)(128 >> 4) << 32;  // stride-dimension (8-row group) offset
+    d |= (u64)1 << 46;           // descriptor version for tcgen05; layout 0 = no swizzle
     return d;
 }
 
@@ -594,13 +652,23 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
 // start and one at the end (none returns early), both CTAs allocate and free TMEM together, and
 // each CTA waits for the arrivals the other still owes it before the last barrier.
 // ---------------------------------------------------------------------------
-constexpr int GP_STAGES = 6;
-constexpr int GP_BN_HALF = GM_BN / 2;                    // witnesses of one CTA
-constexpr int GP_B_BYTES = GP_BN_HALF * GM_BK * 2;       // 16 KB
-constexpr int GP_STAGE_BYTES = GM_A_BYTES + GP_B_BYTES;  // 32 KB
-constexpr int GP_NBAR = 3 * GP_STAGES + 5;               // full, empty, pair-full, accumulators x 4, mma_done
-constexpr int GP_SMEM = GP_STAGES * GP_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-static_assert(GP_NBAR * 8 + 8 <= 256, "barrier area");
+constexpr int GP_BN_HALF = GM_BN / 2;               // witnesses of one CTA
+constexpr int GP_B_BYTES = GP_BN_HALF * GM_BK * 2;  // 16 KB
+// Stage shape per key layout.  HANKEL = false: the Toeplitz expansion's 16 KB swizzled tile, then
+// the witness half.  HANKEL = true: the tile's 3840-byte window (ajtai_window_kernel) in a 4 KB
+// slot, then the witness half at a 1024-byte boundary (its 128-byte swizzle needs one).
+template <bool HANKEL>
+struct GpShape {
+    static constexpr int STAGES = HANKEL ? 10 : 6;
+    static constexpr int A_BYTES = HANKEL ? GW_A_BYTES : GM_A_BYTES;
+    static constexpr int B_OFF = HANKEL ? 4096 : GM_A_BYTES;
+    static constexpr int STAGE_BYTES = B_OFF + GP_B_BYTES;
+    static constexpr int TX_BYTES = A_BYTES + GP_B_BYTES;  // what one stage's copies deliver
+    static constexpr int NBAR = 3 * STAGES + 5;            // full, empty, pair-full, accumulators x 4, mma_done
+    static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 512 /*barriers*/;
+    static_assert(NBAR * 8 + 8 <= 512, "barrier area");
+    static_assert(A_BYTES <= B_OFF && B_OFF % 1024 == 0 && STAGE_BYTES % 1024 == 0, "stage layout");
+};
 // instruction descriptor: D f32, A/B bf16, both K-major, M = 256 (the pair), N = 256
 constexpr u32 GP_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(GM_BN >> 3) << 17) | ((u32)(256 >> 4) << 24);
 
@@ -643,14 +711,17 @@ __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const __nv_bfloat16* __restrict__ A_tiled,
+template <bool HANKEL>
+__global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const uint8_t* __restrict__ A_tiles,
                                                                         const __grid_constant__ CUtensorMap tmB,
                                                                         int k_tiles, GmSched sched,
                                                                         int* __restrict__ S, int* __restrict__ err) {
+    using SH = GpShape<HANKEL>;
+    constexpr int GP_STAGES = SH::STAGES;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = (uint64_t*)(smem + GP_STAGES * GP_STAGE_BYTES);
-    u32* tmem_slot = (u32*)(bars + GP_NBAR);
+    uint64_t* bars = (uint64_t*)(smem + GP_STAGES * SH::STAGE_BYTES);
+    u32* tmem_slot = (u32*)(bars + SH::NBAR);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const u32 rank = cluster_rank();  // 0: the even CTA (the MMA issuer's), 1: the odd one
     const int pair_id = (int)(blockIdx.x >> 1);
@@ -708,12 +779,13 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const __
                 const int s = kt % GP_STAGES;
                 const u32 ph = (kt / GP_STAGES) & 1;
                 if (!mbar_wait(empty(s), ph ^ 1, err, 1, sched.spin_limit)) break;
-                mbar_expect_tx(full(s), GP_STAGE_BYTES);
-                uint8_t* sa = smem + s * GP_STAGE_BYTES;
+                mbar_expect_tx(full(s), SH::TX_BYTES);
+                uint8_t* sa = smem + s * SH::STAGE_BYTES;
                 const int lu = kt / GM_CHUNK_TILES, x = (unit_k0(lu) + kt % GM_CHUNK_TILES) * GM_BK;
-                bulk_load_hint(smem_u32(sa), A_tiled + ((size_t)unit_m128(lu) * k_tiles + x / GM_BK) * (GM_A_BYTES / 2),
-                               GM_A_BYTES, full(s), pol_key);
-                tma_load_2d(smem_u32(sa + GM_A_BYTES), &tmB, x, unit_n0(lu), full(s));
+                // the key tile (or window) of (m128, x / 64) is A_BYTES contiguous, in its smem layout
+                bulk_load_hint(smem_u32(sa), A_tiles + ((size_t)unit_m128(lu) * k_tiles + x / GM_BK) * SH::A_BYTES,
+                               SH::A_BYTES, full(s), pol_key);
+                tma_load_2d(smem_u32(sa + SH::B_OFF), &tmB, x, unit_n0(lu), full(s));
                 issued = kt + 1;
             }
             // the loads still in flight land, then the issuer's last commits for this CTA's stages
@@ -751,12 +823,16 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const __
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const u32 sa = smem_u32(smem + s * GP_STAGE_BYTES);
-                    const u64 adesc = umma_desc_sw128(sa), bdesc = umma_desc_sw128(sa + GM_A_BYTES);
+                    const u32 sa = smem_u32(smem + s * SH::STAGE_BYTES);
+                    const u64 adesc = HANKEL ? umma_desc_hankel(sa) : umma_desc_sw128(sa);
+                    const u64 bdesc = umma_desc_sw128(sa + SH::B_OFF);
 #pragma unroll
                     for (int k = 0; k < GM_BK / 16; k++) {
                         const u32 acc = (t > 0 || k > 0) ? 1u : 0u;
-                        const u64 ad = adesc + (u64)((k * 32) >> 4), bd = bdesc + (u64)((k * 32) >> 4);
+                        // K step k: 16 columns = 32 bytes inside the swizzled rows, or two core
+                        // matrices (2 x 256 bytes) along K in the window
+                        const u64 ad = adesc + (u64)((HANKEL ? k * 512 : k * 32) >> 4);
+                        const u64 bd = bdesc + (u64)((k * 32) >> 4);
                         asm volatile(
                             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                             "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
@@ -824,7 +900,9 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const __
             const long long t = unit_tile(c);
             if (c + 1 == chunks || unit_tile(c + 1) != t) {
                 const int k = pair_id - gm_cta_of(sched, t * sched.chunks);
-                int* dst = S + ((((size_t)t * 2 + rank) * sched.slots + k) * GM_BM + row) * GM_BN + half * COLS;
+                // the window's row group 2 a' + beta is group a' of the tile's 64-row half beta
+                const int srow = HANKEL ? ((row >> 3) & 1) * 64 + (row >> 4) * 8 + (row & 7) : row;
+                int* dst = S + ((((size_t)t * 2 + rank) * sched.slots + k) * GM_BM + srow) * GM_BN + half * COLS;
 #pragma unroll
                 for (int q = 0; q < COLS; q += 4) {
                     *reinterpret_cast<int4*>(dst + q) = make_int4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
@@ -1223,10 +1301,15 @@ struct AjtaiKey {
     __nv_bfloat16* d_T = nullptr;    // 8 * rows * 64 x Kp, tile by tile (ajtai_expand_kernel); built
                                      // by the first batch that takes the key-Toeplitz form
     __nv_bfloat16* d_A = nullptr;    // ceil(rows / 16) * 128 x Kp, tile by tile (ajtai_planes_kernel)
+    uint8_t* d_W = nullptr;          // the Hankel windows, 3840 B per (128-row tile, ring column)
+                                     // (ajtai_window_kernel); built by the first batch that needs them
     u64* d_RS = nullptr;             // [rows][64]
     std::once_flag t_once;           // the expansion's one build (any thread may commit)
     int t_rc = GB_OK;                // its outcome
     std::string t_err;
+    std::once_flag w_once;           // the windows' one build
+    int w_rc = GB_OK;
+    std::string w_err;
 };
 
 static size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
@@ -1290,13 +1373,42 @@ static int key_expand(AjtaiKey* k) {
     return k->t_rc;
 }
 
+// The Hankel form's operand: the key's windows, 252 MB for 16 rows x 1024 ring columns (a quarter
+// of the expansion).  Built once, like the expansion, by the first batch that needs it.
+static int key_window(AjtaiKey* k) {
+    std::call_once(k->w_once, [k] {
+        cudaStream_t s = stream();
+        const size_t KT = k->Kp / GM_BK;
+        const size_t bytes = (size_t)4 * k->rows * KT * GW_A_BYTES;  // 8 rows x 64 / 128 tiles per ring row
+        int rc = GB_OK;
+        cudaError_t e = cudaMalloc(&k->d_W, bytes);
+        if (e == cudaSuccess && k->Kp > k->K) e = cudaMemsetAsync(k->d_W, 0, bytes, s);  // the padding columns
+        if (e == cudaSuccess) {
+            dim3 g((unsigned)k->N, (unsigned)k->rows);
+            ajtai_window_kernel<<<g, 128, 0, s>>>(k->d_M, k->rows, k->N, KT, k->d_W);
+            rc = check_launch("ajtai_window_kernel");
+            if (!rc) e = cudaStreamSynchronize(s);
+        }
+        if (e != cudaSuccess) {
+            set_error("ajtai key windows", e);
+            rc = GB_ECUDA;
+        }
+        k->w_rc = rc;
+        if (rc) k->w_err = gb_last_error();
+    });
+    if (k->w_rc) set_error_msg(k->w_err);
+    return k->w_rc;
+}
+
 static void key_free(AjtaiKey* k) {
     if (k->d_M) cudaFree(k->d_M);
+    if (k->d_W) cudaFree(k->d_W);
     if (k->d_T) cudaFree(k->d_T);
     if (k->d_A) cudaFree(k->d_A);
     if (k->d_RS) cudaFree(k->d_RS);
     k->d_M = nullptr;
     k->d_T = nullptr;
+    k->d_W = nullptr;
     k->d_A = nullptr;
     k->d_RS = nullptr;
 }
@@ -1373,7 +1485,8 @@ static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
 }
 
 // Form of the calling thread's batched commitments (gb_ajtai_set_batch_form): 0 by batch size,
-// 1 the witness-circulant GEMM, 2 the key-Toeplitz GEMM, 3 the key-Toeplitz GEMM on CTA pairs.
+// 1 the witness-circulant GEMM, 2 the key-Toeplitz GEMM, 3 the key-Toeplitz GEMM on CTA pairs,
+// 4 the same pair GEMM reading the key's Hankel windows (a quarter of the expansion's bytes).
 // Results never depend on it.
 static thread_local int t_batch_form = 0;
 // Largest batch that the automatic choice gives the witness-circulant GEMM.  Its work grows with
@@ -1383,12 +1496,13 @@ static thread_local int t_batch_form = 0;
 // 0.263 against 0.258 ms at 176).
 constexpr int AJ_WC_MAX_AUTO = 172;
 
-// Launch shape of the pair GEMM: a cluster of 2 CTAs, GP_SMEM bytes each.
+// Launch shape of the pair GEMM: a cluster of 2 CTAs, GpShape<HANKEL>::SMEM bytes each.
+template <bool HANKEL>
 static cudaLaunchConfig_t pair_config(int clusters, cudaStream_t s, cudaLaunchAttribute* attr) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(2 * clusters));
     cfg.blockDim = dim3(GM_THREADS);
-    cfg.dynamicSmemBytes = GP_SMEM;
+    cfg.dynamicSmemBytes = GpShape<HANKEL>::SMEM;
     cfg.stream = s;
     attr->id = cudaLaunchAttributeClusterDimension;
     attr->val.clusterDim.x = 2;
@@ -1402,9 +1516,10 @@ static cudaLaunchConfig_t pair_config(int clusters, cudaStream_t s, cudaLaunchAt
 // CTA pairs that the device runs at once (0 when clusters of two cannot run the pair GEMM).  The
 // shared-memory attribute is set on every call (idempotent, per device); the occupancy answer
 // depends only on the device and is kept per device (a race only recomputes the same value).
+template <bool HANKEL>
 static int pair_clusters() {
-    if (cudaFuncSetAttribute(ajtai_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GP_SMEM) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(ajtai_gemm_pair_kernel<HANKEL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             GpShape<HANKEL>::SMEM) != cudaSuccess)
         return 0;
     constexpr int MAX_DEVICES = 64;
     static std::atomic<int> known[MAX_DEVICES];  // 0: not yet asked, else clusters + 1
@@ -1415,9 +1530,9 @@ static int pair_clusters() {
         if (k > 0) return k - 1;
     }
     cudaLaunchAttribute attr;
-    cudaLaunchConfig_t cfg = pair_config(1, stream(), &attr);
+    cudaLaunchConfig_t cfg = pair_config<HANKEL>(1, stream(), &attr);
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, ajtai_gemm_pair_kernel, &cfg) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveClusters(&n, ajtai_gemm_pair_kernel<HANKEL>, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;  // not kept: a later call asks again
     }
@@ -1427,21 +1542,22 @@ static int pair_clusters() {
 
 static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     if (B < 1) return GB_EINVAL;
-    int form = t_batch_form ? t_batch_form : (B <= AJ_WC_MAX_AUTO ? 1 : 3);
+    int form = t_batch_form ? t_batch_form : (B <= AJ_WC_MAX_AUTO ? 1 : 4);
     if (form == 1) return commit_batch_wc(k, d_z, B, d_out);
-    if (int rc = key_expand(k)) return rc;
-    cudaStream_t s = stream();
-    const int Bp = (int)round_up((size_t)B, GM_BN);
-    const size_t Mrows = (size_t)8 * k->rows * AJ_D;
-    // form 3: CTA pairs, 256-row tiles; the device must run clusters of two at this size (the
-    // automatic choice falls back to the one-CTA form when it cannot)
-    const int clusters = form == 3 ? pair_clusters() : 0;
-    if (form == 3 && clusters < 1 && t_batch_form == 0) form = 2;
-    if (form == 3 && clusters < 1) {
+    // forms 3 and 4: CTA pairs, 256-row tiles; the device must run clusters of two at this size
+    // (the automatic choice falls back to the one-CTA form when it cannot)
+    const int clusters = form == 3 ? pair_clusters<false>() : form == 4 ? pair_clusters<true>() : 0;
+    if (form >= 3 && clusters < 1 && t_batch_form == 0) form = 2;
+    if (form >= 3 && clusters < 1) {
         set_error_msg("ajtai pair GEMM: the device runs no cluster of two CTAs of this size");
         return GB_ECUDA;
     }
-    const int pair = form == 3 ? 1 : 0;
+    const bool hankel = form == 4;
+    if (int rc = hankel ? key_window(k) : key_expand(k)) return rc;
+    cudaStream_t s = stream();
+    const int Bp = (int)round_up((size_t)B, GM_BN);
+    const size_t Mrows = (size_t)8 * k->rows * AJ_D;
+    const int pair = form >= 3 ? 1 : 0;
     // persistent schedule: one CTA (pair) per SM (pair), or per unit when there are fewer, equal unit ranges
     GmSched sched;
     sched.pair = pair;
@@ -1464,19 +1580,35 @@ static int commit_batch(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
     GB_CUDA_TRY(cudaMallocAsync(&S, s_ints * 4, s));
     GB_CUDA_TRY(cudaMallocAsync(&err, 4, s));
     GB_CUDA_TRY(cudaMemsetAsync(err, 0, 4, s));
-    if (((uintptr_t)d_z & 7) == 0)
-        ajtai_zprep_kernel<<<grid_for((size_t)Bp * (k->Kp / 8), 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
-    else
-        ajtai_zprep_scalar_kernel<<<grid_for((size_t)Bp * k->Kp, 256), 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+    // the Hankel form reads the witnesses with K reversed inside each ring column
+    const unsigned g8 = grid_for((size_t)Bp * (k->Kp / 8), 256), g1 = grid_for((size_t)Bp * k->Kp, 256);
+    if (((uintptr_t)d_z & 7) == 0) {
+        if (hankel)
+            ajtai_zprep_kernel<true><<<g8, 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+        else
+            ajtai_zprep_kernel<false><<<g8, 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+    } else {
+        if (hankel)
+            ajtai_zprep_scalar_kernel<true><<<g1, 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+        else
+            ajtai_zprep_scalar_kernel<false><<<g1, 256, 0, s>>>(d_z, B, k->K, Bp, k->Kp, zc);
+    }
     int rc = check_launch("ajtai_zprep_kernel");
     CUtensorMap mapB;
     if (!rc) rc = make_map(&mapB, zc, k->Kp, (u64)Bp, pair ? GP_BN_HALF : GM_BN);
     const int k_tiles = (int)(k->Kp / GM_BK);
     if (!rc && pair) {
         cudaLaunchAttribute attr;
-        cudaLaunchConfig_t cfg = pair_config(sched.ctas, s, &attr);
-        const cudaError_t e =
-            cudaLaunchKernelEx(&cfg, ajtai_gemm_pair_kernel, (const __nv_bfloat16*)k->d_T, mapB, k_tiles, sched, S, err);
+        cudaError_t e;
+        if (hankel) {
+            cudaLaunchConfig_t cfg = pair_config<true>(sched.ctas, s, &attr);
+            e = cudaLaunchKernelEx(&cfg, ajtai_gemm_pair_kernel<true>, (const uint8_t*)k->d_W, mapB, k_tiles, sched, S,
+                                   err);
+        } else {
+            cudaLaunchConfig_t cfg = pair_config<false>(sched.ctas, s, &attr);
+            e = cudaLaunchKernelEx(&cfg, ajtai_gemm_pair_kernel<false>, (const uint8_t*)k->d_T, mapB, k_tiles, sched, S,
+                                   err);
+        }
         rc = check_launch("ajtai_gemm_pair_kernel");
         if (!rc && e != cudaSuccess) {
             set_error("ajtai_gemm_pair_kernel", e);
@@ -1887,8 +2019,8 @@ int gb_ajtai_commit_u8_batched(void* handle, const uint8_t* d_z, int num_witness
 }
 
 int gb_ajtai_set_batch_form(int form) {
-    if (form < 0 || form > 3) {
-        set_error_msg("gb_ajtai_set_batch_form: form must be 0 (by batch size), 1, 2 or 3");
+    if (form < 0 || form > 4) {
+        set_error_msg("gb_ajtai_set_batch_form: form must be 0 (by batch size), 1, 2, 3 or 4");
         return GB_EINVAL;
     }
     const int old = t_batch_form;

@@ -8,7 +8,7 @@ Q = O.Q_AGL
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=[1, 2, 3], ids=["circulant", "toeplitz", "toeplitz-pair"])
+@pytest.fixture(params=[1, 2, 3, 4], ids=["circulant", "toeplitz", "toeplitz-pair", "hankel-pair"])
 def form(request, gpu_lib):
     """Runs the test once with each tensor-core form of the batched commitment."""
     from morpheus_gb300.ajtai import batch_form
@@ -242,16 +242,16 @@ def test_gemm_bounded_waits_time_out_and_the_context_recovers(gpu_lib, form):
 
 @pytest.mark.parametrize("B", [1, 4, 5, 6, 172, 173, 300])
 def test_batch_forms_agree(gpu_lib, B):
-    """The three tensor-core forms and the automatic choice (witness-circulant up to 172 witnesses,
-    CTA pairs above) give the same commitments, on either side of the threshold and over several
-    witness tiles."""
+    """The four tensor-core forms and the automatic choice (witness-circulant up to 172 witnesses,
+    the Hankel-window pair GEMM above) give the same commitments, on either side of the threshold
+    and over several witness tiles."""
     from morpheus_gb300.ajtai import AjtaiKey, batch_form
     key = np.array([2, 7, 1, 8, 2, 8, 1, 8], np.uint32)
     n_ring = 48
     z8 = np.random.default_rng(B).integers(0, 256, size=(B, n_ring * 64), dtype=np.uint8)
     k = AjtaiKey(key, 1, 16, n_ring)
     outs = []
-    for f in (0, 1, 2, 3):
+    for f in (0, 1, 2, 3, 4):
         with batch_form(f):
             outs.append(k.commit_u8_batched(z8))
     assert all(np.array_equal(outs[0], o) for o in outs[1:])
@@ -262,7 +262,7 @@ def test_batch_forms_agree(gpu_lib, B):
 def test_batch_form_rejects_out_of_range(gpu_lib):
     from morpheus_gb300 import _native as N
     L = N.lib()
-    assert L.gb_ajtai_set_batch_form(4) == -2 and L.gb_ajtai_set_batch_form(-1) == -2
+    assert L.gb_ajtai_set_batch_form(5) == -2 and L.gb_ajtai_set_batch_form(-1) == -2
     assert L.gb_ajtai_set_batch_form(0) == 0
 
 
