@@ -654,20 +654,24 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_kernel(const __nv_bf
 // ---------------------------------------------------------------------------
 constexpr int GP_BN_HALF = GM_BN / 2;               // witnesses of one CTA
 constexpr int GP_B_BYTES = GP_BN_HALF * GM_BK * 2;  // 16 KB
-// Stage shape per key layout.  HANKEL = false: the Toeplitz expansion's 16 KB swizzled tile, then
-// the witness half.  HANKEL = true: the tile's 3840-byte window (ajtai_window_kernel) in a 4 KB
-// slot, then the witness half at a 1024-byte boundary (its 128-byte swizzle needs one).
+// Stage shape per key layout.  HANKEL = false: one ring column (K = 64) per stage, the Toeplitz
+// expansion's 16 KB swizzled tile, then the witness half.  HANKEL = true: two ring columns per
+// stage (half the waits and commits per MMA), their two 3840-byte windows (ajtai_window_kernel,
+// adjacent in memory: one copy) in an 8 KB slot, then the two witness halves, each at a
+// 1024-byte boundary (their 128-byte swizzle needs one).
 template <bool HANKEL>
 struct GpShape {
-    static constexpr int STAGES = HANKEL ? 10 : 6;
-    static constexpr int A_BYTES = HANKEL ? GW_A_BYTES : GM_A_BYTES;
-    static constexpr int B_OFF = HANKEL ? 4096 : GM_A_BYTES;
-    static constexpr int STAGE_BYTES = B_OFF + GP_B_BYTES;
-    static constexpr int TX_BYTES = A_BYTES + GP_B_BYTES;  // what one stage's copies deliver
-    static constexpr int NBAR = 3 * STAGES + 5;            // full, empty, pair-full, accumulators x 4, mma_done
+    static constexpr int COLS = HANKEL ? 2 : 1;  // ring columns (64-deep K tiles) per stage
+    static constexpr int STAGES = HANKEL ? 5 : 6;
+    static constexpr int A_BYTES = HANKEL ? GW_A_BYTES : GM_A_BYTES;  // one column's key operand
+    static constexpr int B_OFF = HANKEL ? 8192 : GM_A_BYTES;
+    static constexpr int STAGE_BYTES = B_OFF + COLS * GP_B_BYTES;
+    static constexpr int TX_BYTES = COLS * (A_BYTES + GP_B_BYTES);  // what one stage's copies deliver
+    static constexpr int NBAR = 3 * STAGES + 5;  // full, empty, pair-full, accumulators x 4, mma_done
     static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 512 /*barriers*/;
     static_assert(NBAR * 8 + 8 <= 512, "barrier area");
-    static_assert(A_BYTES <= B_OFF && B_OFF % 1024 == 0 && STAGE_BYTES % 1024 == 0, "stage layout");
+    static_assert(COLS * A_BYTES <= B_OFF && B_OFF % 1024 == 0 && STAGE_BYTES % 1024 == 0, "stage layout");
+    static_assert(GM_CHUNK_TILES % COLS == 0, "whole stages per 1024-deep chunk");
 };
 // instruction descriptor: D f32, A/B bf16, both K-major, M = 256 (the pair), N = 256
 constexpr u32 GP_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(GM_BN >> 3) << 17) | ((u32)(256 >> 4) << 24);
@@ -718,6 +722,7 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const ui
                                                                         int* __restrict__ S, int* __restrict__ err) {
     using SH = GpShape<HANKEL>;
     constexpr int GP_STAGES = SH::STAGES;
+    constexpr int SPC = GM_CHUNK_TILES / SH::COLS;  // stages per 1024-deep chunk
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + GP_STAGES * SH::STAGE_BYTES);
@@ -768,7 +773,7 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const ui
     // the MMAs address both CTAs' TMEM through one address: a pair that got different ones does no work
     const bool bad = tmem != tmem_peer;
     if (bad && threadIdx.x == 0) atomicCAS(err, 0, 7);
-    const int my_tiles = (bad || sched.starve) ? 0 : chunks * GM_CHUNK_TILES;
+    const int my_tiles = (bad || sched.starve) ? 0 : chunks * SPC;  // this CTA's stages
     const int my_chunks = bad ? 0 : chunks;
 
     if (warp == 0) {
@@ -781,11 +786,14 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const ui
                 if (!mbar_wait(empty(s), ph ^ 1, err, 1, sched.spin_limit)) break;
                 mbar_expect_tx(full(s), SH::TX_BYTES);
                 uint8_t* sa = smem + s * SH::STAGE_BYTES;
-                const int lu = kt / GM_CHUNK_TILES, x = (unit_k0(lu) + kt % GM_CHUNK_TILES) * GM_BK;
-                // the key tile (or window) of (m128, x / 64) is A_BYTES contiguous, in its smem layout
+                const int lu = kt / SPC, x = (unit_k0(lu) + (kt % SPC) * SH::COLS) * GM_BK;
+                // the key tiles (or windows) of (m128, x / 64 ..) are COLS x A_BYTES contiguous,
+                // in their smem layout
                 bulk_load_hint(smem_u32(sa), A_tiles + ((size_t)unit_m128(lu) * k_tiles + x / GM_BK) * SH::A_BYTES,
-                               SH::A_BYTES, full(s), pol_key);
-                tma_load_2d(smem_u32(sa + SH::B_OFF), &tmB, x, unit_n0(lu), full(s));
+                               SH::COLS * SH::A_BYTES, full(s), pol_key);
+#pragma unroll
+                for (int col = 0; col < SH::COLS; col++)
+                    tma_load_2d(smem_u32(sa + SH::B_OFF + col * GP_B_BYTES), &tmB, x + col * GM_BK, unit_n0(lu), full(s));
                 issued = kt + 1;
             }
             // the loads still in flight land, then the issuer's last commits for this CTA's stages
@@ -813,8 +821,8 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const ui
                 if (!mbar_wait_cluster(acc_empty(a), (use & 1) ^ 1, err, 2, sched.spin_limit)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const u32 d_tmem = tmem + (u32)(a * GM_BN);
-                for (int t = 0; t < GM_CHUNK_TILES; t++) {
-                    const int kt = c * GM_CHUNK_TILES + t;
+                for (int t = 0; t < SPC; t++) {
+                    const int kt = c * SPC + t;
                     const int s = kt % GP_STAGES;
                     const u32 ph = (kt / GP_STAGES) & 1;
                     if (!mbar_wait(full(s), ph, err, 3, sched.spin_limit) ||
@@ -824,19 +832,23 @@ __global__ void __launch_bounds__(GM_THREADS, 1) ajtai_gemm_pair_kernel(const ui
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const u32 sa = smem_u32(smem + s * SH::STAGE_BYTES);
-                    const u64 adesc = HANKEL ? umma_desc_hankel(sa) : umma_desc_sw128(sa);
-                    const u64 bdesc = umma_desc_sw128(sa + SH::B_OFF);
 #pragma unroll
-                    for (int k = 0; k < GM_BK / 16; k++) {
-                        const u32 acc = (t > 0 || k > 0) ? 1u : 0u;
-                        // K step k: 16 columns = 32 bytes inside the swizzled rows, or two core
-                        // matrices (2 x 256 bytes) along K in the window
-                        const u64 ad = adesc + (u64)((HANKEL ? k * 512 : k * 32) >> 4);
-                        const u64 bd = bdesc + (u64)((k * 32) >> 4);
-                        asm volatile(
-                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                            "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-                            "l"(ad), "l"(bd), "r"(GP_IDESC), "r"(acc));
+                    for (int col = 0; col < SH::COLS; col++) {
+                        const u32 a_col = sa + col * SH::A_BYTES;
+                        const u64 adesc = HANKEL ? umma_desc_hankel(a_col) : umma_desc_sw128(a_col);
+                        const u64 bdesc = umma_desc_sw128(sa + SH::B_OFF + col * GP_B_BYTES);
+#pragma unroll
+                        for (int k = 0; k < GM_BK / 16; k++) {
+                            const u32 acc = (t > 0 || col > 0 || k > 0) ? 1u : 0u;
+                            // K step k: 16 columns = 32 bytes inside the swizzled rows, or two core
+                            // matrices (2 x 256 bytes) along K in the window
+                            const u64 ad = adesc + (u64)((HANKEL ? k * 512 : k * 32) >> 4);
+                            const u64 bd = bdesc + (u64)((k * 32) >> 4);
+                            asm volatile(
+                                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                                "l"(ad), "l"(bd), "r"(GP_IDESC), "r"(acc));
+                        }
                     }
                     // the stage is free again in both CTAs once these MMAs have read it
                     asm volatile(
