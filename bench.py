@@ -357,8 +357,8 @@ def run_side_workload(args):
         # whole batch (digit prep, GEMM, combine) against the HBM bound of the GEMM's operand
         # stream: the key's 8 digit planes (bf16) once, plus the witness digits (bf16)
         peak, src = measured_peaks()
-        circulant = args.ajtai_form == 1 or (args.ajtai_form == 0 and Bw <= 172)
-        hankel = args.ajtai_form == 4 or (args.ajtai_form == 0 and Bw > 172)
+        circulant = args.ajtai_form == 1 or (args.ajtai_form == 0 and Bw <= 104)
+        hankel = args.ajtai_form == 4 or (args.ajtai_form == 0 and Bw > 104)
         pair = args.ajtai_form == 3
         if circulant:  # the key's digit planes once (16 MB) plus the witness bytes
             op_bytes = 8 * rows * n_ring * 64 * 2 + Bw * n_ring * 64
@@ -459,7 +459,7 @@ def ajtai_c3_summary(L, Nn, DeviceBuffer, ev_time):  # ev_time flushes L2 before
             "single_witness": {"ms_witness_circulant": one["auto"], "ms_key_toeplitz": one["toeplitz"],
                                "identical": True, "note": "one 2^16-coefficient witness, as in a served job; "
                                                          "the automatic choice takes the witness-circulant "
-                                                         "form up to 172 witnesses"},
+                                                         "form up to 104 witnesses"},
             "cpu_baseline": cpu_ajtai_sample(key, z_host[:64], rows, got.reshape(Bw, rows, 64)[:64]),
             "step_ms_all": [round(t, 4) for t in times],
             "workload": "256 witnesses x 2^16 coefficients in [0, 256), rows 0..15 of the ChaCha8 matrix, "

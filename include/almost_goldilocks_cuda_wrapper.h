@@ -169,11 +169,11 @@ int gb_ajtai_key_info(void *handle, int *row_lo, int *rows, uint64_t *n_ring);
 int gb_ajtai_commit_u8_batched(void *key, const uint8_t *d_z, int num_witnesses, uint64_t *d_out);
 /* Form of the calling thread's gb_ajtai_commit_u8_batched calls (no reference counterpart):
  * 0 chooses by batch size (the default), 1 the witness-circulant tensor-core GEMM (work
- * proportional to the batch; the automatic choice up to 172 witnesses), 2 the key-Toeplitz
+ * proportional to the batch; the automatic choice up to 104 witnesses), 2 the key-Toeplitz
  * tensor-core GEMM (streams the key's 1.07 GB expansion once per batch of up to 256 witnesses),
  * 3 the key-Toeplitz GEMM on CTA pairs (clusters of two CTAs, M = 256 tcgen05 MMAs), 4 the
  * same CTA-pair GEMM reading the key's Hankel windows instead of its expansion (252 MB for 16 rows
- * x 1024 ring columns, built on first use; the automatic choice above 172 witnesses, or form 2
+ * x 1024 ring columns, built on first use; the automatic choice above 104 witnesses, or form 2
  * where the device cannot run the pairs).  Results never depend on it.  Returns the previous
  * form, or -2 for a form outside 0..4. */
 int gb_ajtai_set_batch_form(int form);

@@ -1502,11 +1502,11 @@ static int commit_batch_wc(AjtaiKey* k, const uint8_t* d_z, int B, u64* d_out) {
 // Results never depend on it.
 static thread_local int t_batch_form = 0;
 // Largest batch that the automatic choice gives the witness-circulant GEMM.  Its work grows with
-// the batch (one N = 64 MMA per witness and K step), while the key-Toeplitz GEMM streams the
-// 1.07 GB key expansion whatever the batch; larger batches take its CTA-pair form.  The two
-// measured level near 172 witnesses (16 rows x 1024 ring columns: 0.239 against 0.256 ms at 160,
-// 0.263 against 0.258 ms at 176).
-constexpr int AJ_WC_MAX_AUTO = 172;
+// the batch (one N = 64 MMA per witness and K step), while the pair GEMM streams the key's
+// operand (its Hankel windows) whatever the batch; larger batches take the CTA-pair GEMM on
+// the windows.  The two measured level near 105 witnesses (16 rows x 1024 ring columns: 0.169
+// against 0.179 ms at 96, 0.185 against 0.180 ms at 112).
+constexpr int AJ_WC_MAX_AUTO = 104;
 
 // Launch shape of the pair GEMM: a cluster of 2 CTAs, GpShape<HANKEL>::SMEM bytes each.
 template <bool HANKEL>
